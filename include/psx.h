@@ -1,0 +1,147 @@
+/*
+ * psx.h — C ABI of the GB300-native Physecs simulation hot path.
+ *
+ * This is the drop-in boundary for physecs::Scene::simulate(timeStep)
+ * (Physecs src/Physecs.cpp:112-561).  Plain pointers and sizes only: no C++,
+ * no torch, no CUDA types.  The library keeps every scene's state resident in
+ * device memory; callers move body state in and out explicitly, the way the
+ * reference reads and writes its EnTT components in place.
+ *
+ * Conventions
+ *   - Every entry point returns psx_status; psx_last_error_string() describes
+ *     the most recent failure on the calling thread.
+ *   - float3 arrays are tightly packed x,y,z; quaternions are x,y,z,w (the
+ *     storage order of glm::quat in TransformComponent, src/Transform.h:6-10);
+ *     3x3 matrices are column-major (glm::mat3).
+ *   - A scene handle is single-threaded: the caller serialises calls on it.
+ */
+#ifndef PSX_H
+#define PSX_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define PSX_API __attribute__((visibility("default")))
+#else
+#define PSX_API
+#endif
+
+typedef enum psx_status {
+    PSX_OK = 0,
+    PSX_ERR_INVALID_ARG = 1,
+    PSX_ERR_OUT_OF_MEMORY = 2,
+    PSX_ERR_CAPACITY = 3,     /* a fixed-capacity device buffer overflowed */
+    PSX_ERR_TIMEOUT = 4,      /* a bounded device wait gave up */
+    PSX_ERR_CUDA = 5,
+    PSX_ERR_NOT_READY = 6
+} psx_status;
+
+/* physecs::GeometryType, include/Physecs/Colliders.h:9 */
+enum {
+    PSX_SPHERE = 0,
+    PSX_CAPSULE = 1,
+    PSX_BOX = 2,
+    PSX_CONVEX_MESH = 3,
+    PSX_TRIANGLE_MESH = 4
+};
+
+/* body flags */
+enum {
+    PSX_BODY_DYNAMIC = 1,   /* entity carries a RigidBodyDynamicComponent */
+    PSX_BODY_KINEMATIC = 2  /* RigidBodyDynamicComponent::isKinematic */
+};
+
+/* joint kinds: the Joint subclasses in include/Physecs/Joints/*.h */
+enum {
+    PSX_JOINT_FIXED = 0,
+    PSX_JOINT_REVOLUTE = 1,
+    PSX_JOINT_SPHERICAL = 2,
+    PSX_JOINT_PRISMATIC = 3,
+    PSX_JOINT_UNIVERSAL = 4,
+    PSX_JOINT_GEAR = 5,
+    PSX_JOINT_SERVO = 6
+};
+
+/*
+ * Joint parameter block (8 floats per joint), by kind:
+ *   REVOLUTE  [driveEnabled, driveVelocity, driveMaxTorque]        (RevoluteJoint.h:11-15)
+ *   PRISMATIC [upperLimit, lowerLimit, driveEnabled, targetPosition,
+ *              driveStiffness, driveDamping]                         (PrismaticJoint.h:9-18)
+ *   GEAR      [gearRatio]                                            (GearJoint.h:10-17)
+ *   SERVO     [targetAngle, driveStiffness, driveDamping]            (ServoJoint.h:10-14)
+ *   others    unused
+ */
+#define PSX_JOINT_PARAMS 8
+
+/*
+ * A scene as the reference's registry holds it: entities in creation order,
+ * each with a TransformComponent, a RigidBodyCollisionComponent (colliders
+ * [collider_start[i], collider_start[i+1])) and optionally a
+ * RigidBodyDynamicComponent (include/Physecs/Components.h:6-17).
+ */
+typedef struct psx_scene_desc {
+    int32_t n_bodies;
+    const uint32_t* entity;        /* [n] entt::entity value; orders pairs (src/Physecs.cpp:158) */
+    const uint32_t* flags;         /* [n] PSX_BODY_* */
+    const float* pos;              /* [n*3] TransformComponent::position */
+    const float* quat;             /* [n*4] TransformComponent::orientation (x,y,z,w) */
+    const float* vel;              /* [n*3] RigidBodyDynamicComponent::velocity */
+    const float* ang_vel;          /* [n*3] RigidBodyDynamicComponent::angularVelocity */
+    const float* inv_mass;         /* [n]   RigidBodyDynamicComponent::invMass */
+    const float* com;              /* [n*3] RigidBodyDynamicComponent::com (body frame) */
+    const float* inv_inertia;      /* [n*9] RigidBodyDynamicComponent::invInertiaTensor, column-major */
+    const int32_t* collider_start; /* [n+1] */
+
+    int32_t n_colliders;
+    const float* col_pos;          /* [m*3] Collider::position */
+    const float* col_quat;         /* [m*4] Collider::orientation (x,y,z,w) */
+    const int32_t* col_type;       /* [m]   PSX_SPHERE.. */
+    const float* col_params;       /* [m*4] sphere {r}; capsule {halfHeight, r}; box {hx,hy,hz};
+                                             convex {sx,sy,sz}; triangle mesh {} */
+    const int32_t* col_mesh;       /* [m]   convex / triangle mesh index, else -1 */
+    const float* col_material;     /* [m*3] Material {friction, restitution, damping} */
+    const uint8_t* col_is_trigger; /* [m] */
+    const uint8_t* col_enable_sim; /* [m] */
+    const int32_t* col_data;       /* [m] */
+
+    /* ConvexMesh (include/Physecs/ConvexMesh.h:29-34): vertices and polygon faces */
+    int32_t n_convex;
+    const int32_t* convex_vert_start;   /* [n_convex+1] into convex_verts (unpadded) */
+    const float* convex_verts;          /* [*3] */
+    const int32_t* convex_face_start;   /* [n_convex+1] into the face arrays */
+    const int32_t* face_index_start;    /* [n_faces+1] into face_indices */
+    const int32_t* face_indices;        /* vertex indices local to the mesh */
+    const float* face_normal;           /* [n_faces*3] */
+    const float* face_centroid;         /* [n_faces*3] */
+
+    /* TriangleMesh (include/Physecs/TriangleMesh.h:24-41): vertices and index triples */
+    int32_t n_trimesh;
+    const int32_t* tri_vert_start;      /* [n_trimesh+1] into tri_verts */
+    const float* tri_verts;             /* [*3] */
+    const int32_t* tri_index_start;     /* [n_trimesh+1] into tri_indices (multiple of 3) */
+    const uint32_t* tri_indices;
+
+    /* joints in creation order (Scene::createJoint, include/Physecs/Physecs.h:209-214) */
+    int32_t n_joints;
+    const int32_t* joint_type;     /* [j] PSX_JOINT_* */
+    const int32_t* joint_body0;    /* [j] body index */
+    const int32_t* joint_body1;    /* [j] body index */
+    const float* joint_frames;     /* [j*14] anchor0 pos(3) quat(4), anchor1 pos(3) quat(4) */
+    const float* joint_params;     /* [j*PSX_JOINT_PARAMS] */
+
+    /* Scene knobs (include/Physecs/Physecs.h:156-159) */
+    int32_t num_substeps;
+    int32_t num_iterations;
+    float gravity;
+} psx_scene_desc;
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PSX_H */

@@ -1,0 +1,323 @@
+/*
+ * ref_capi.cpp — a C entry layer over the UNMODIFIED Physecs reference, used
+ * only to generate and check golden fixtures (test infrastructure).  It is
+ * compiled together with the reference's own sources by oracle/ref/build_ref.py
+ * and never linked into the physecs_gb300 product.
+ *
+ * It builds an entt::registry from a psx_scene_desc exactly the way a Physecs
+ * user does (demo/Demo.cpp:29-43: Transform, then RigidBodyCollisionComponent,
+ * then RigidBodyDynamicComponent), drives physecs::Scene::simulate, and reads
+ * back the scene's internal buffers: the broadphase pair list
+ * (src/Physecs.cpp:134-172), the contact constraints (src/Physecs.cpp:274-314)
+ * and the per-collider bounds (src/Physecs.cpp:79-90).
+ */
+#include "Physecs.h"
+#include "Components.h"
+#include "Transform.h"
+#include "Collision.h"
+#include "ContactManifold.h"
+#include "ContactConstraints.h"
+#include "BoundsUtil.h"
+#include "FixedJoint.h"
+#include "RevoluteJoint.h"
+#include "SphericalJoint.h"
+#include "PrismaticJoint.h"
+#include "UniversalJoint.h"
+#include "GearJoint.h"
+#include "ServoJoint.h"
+#include "psx.h"
+
+#include <memory>
+#include <vector>
+
+/* src/ConvexMesh.cpp defines ConvexMeshVertices<N>'s constructor as a template
+ * without instantiating it; GCC needs an explicit instantiation to construct a
+ * ConvexMesh from outside that translation unit. */
+#include "ConvexMesh.cpp"
+template physecs::ConvexMeshVertices<4>::ConvexMeshVertices(const std::vector<glm::vec3>&&);
+#include <cstring>
+#include <cstdio>
+
+namespace {
+
+struct RefWorld {
+    entt::registry registry;
+    std::unique_ptr<physecs::Scene> scene;
+    std::vector<entt::entity> entities;
+    std::vector<std::unique_ptr<physecs::ConvexMesh>> convex;
+    std::vector<std::unique_ptr<physecs::TriangleMesh>> trimesh;
+};
+
+glm::vec3 v3(const float* p) { return glm::vec3(p[0], p[1], p[2]); }
+glm::quat q4(const float* p) { return glm::quat(p[3], p[0], p[1], p[2]); }
+
+physecs::Collider make_collider(RefWorld& w, const psx_scene_desc* d, int c) {
+    physecs::Collider col{};
+    col.position = v3(d->col_pos + 3 * c);
+    col.orientation = q4(d->col_quat + 4 * c);
+    const float* p = d->col_params + 4 * c;
+    switch (d->col_type[c]) {
+        case PSX_SPHERE: col.geometry.type = physecs::SPHERE; col.geometry.sphere = {p[0]}; break;
+        case PSX_CAPSULE: col.geometry.type = physecs::CAPSULE; col.geometry.capsule = {p[0], p[1]}; break;
+        case PSX_BOX: col.geometry.type = physecs::BOX; col.geometry.box = {glm::vec3(p[0], p[1], p[2])}; break;
+        case PSX_CONVEX_MESH:
+            col.geometry.type = physecs::CONVEX_MESH;
+            col.geometry.convex.mesh = w.convex[d->col_mesh[c]].get();
+            col.geometry.convex.scale = glm::vec3(p[0], p[1], p[2]);
+            break;
+        case PSX_TRIANGLE_MESH:
+            col.geometry.type = physecs::TRIANGLE_MESH;
+            col.geometry.triangleMesh.mesh = w.trimesh[d->col_mesh[c]].get();
+            break;
+    }
+    const float* m = d->col_material + 3 * c;
+    col.material = {m[0], m[1], m[2]};
+    col.isTrigger = d->col_is_trigger ? d->col_is_trigger[c] != 0 : false;
+    col.enableSimulation = d->col_enable_sim ? d->col_enable_sim[c] != 0 : true;
+    col.data = d->col_data ? d->col_data[c] : 0;
+    return col;
+}
+
+}  // namespace
+
+extern "C" {
+
+void* ref_scene_create(const psx_scene_desc* d, int num_threads) {
+    auto* w = new RefWorld();
+    for (int m = 0; m < d->n_convex; ++m) {
+        std::vector<glm::vec3> verts;
+        for (int v = d->convex_vert_start[m]; v < d->convex_vert_start[m + 1]; ++v) verts.push_back(v3(d->convex_verts + 3 * v));
+        std::vector<physecs::ConvexMeshFace> faces;
+        for (int f = d->convex_face_start[m]; f < d->convex_face_start[m + 1]; ++f) {
+            physecs::ConvexMeshFace face;
+            for (int k = d->face_index_start[f]; k < d->face_index_start[f + 1]; ++k) face.indices.push_back(d->face_indices[k]);
+            face.normal = v3(d->face_normal + 3 * f);
+            face.centroid = v3(d->face_centroid + 3 * f);
+            faces.push_back(face);
+        }
+        w->convex.emplace_back(new physecs::ConvexMesh(std::move(verts), std::move(faces)));
+    }
+    for (int m = 0; m < d->n_trimesh; ++m) {
+        std::vector<glm::vec3> verts;
+        for (int v = d->tri_vert_start[m]; v < d->tri_vert_start[m + 1]; ++v) verts.push_back(v3(d->tri_verts + 3 * v));
+        std::vector<unsigned int> idx(d->tri_indices + d->tri_index_start[m], d->tri_indices + d->tri_index_start[m + 1]);
+        w->trimesh.emplace_back(new physecs::TriangleMesh(verts, idx));
+    }
+    w->scene.reset(new physecs::Scene(w->registry, num_threads));
+    w->scene->setNumSubSteps(d->num_substeps);
+    w->scene->setNumIterations(d->num_iterations);
+    w->scene->setGravity(d->gravity);
+    for (int b = 0; b < d->n_bodies; ++b) {
+        entt::entity e = w->registry.create();
+        if ((uint32_t)e != d->entity[b]) {
+            std::fprintf(stderr, "ref_scene_create: entity %u != desc %u\n", (uint32_t)e, d->entity[b]);
+        }
+        w->entities.push_back(e);
+        w->registry.emplace<TransformComponent>(e, v3(d->pos + 3 * b), q4(d->quat + 4 * b), glm::vec3(1));
+        std::vector<physecs::Collider> cols;
+        for (int c = d->collider_start[b]; c < d->collider_start[b + 1]; ++c) cols.push_back(make_collider(*w, d, c));
+        w->registry.emplace<physecs::RigidBodyCollisionComponent>(e, cols);
+        if (d->flags[b] & PSX_BODY_DYNAMIC) {
+            glm::mat3 invI;
+            for (int k = 0; k < 9; ++k) invI[k / 3][k % 3] = d->inv_inertia[9 * b + k];
+            w->registry.emplace<physecs::RigidBodyDynamicComponent>(
+                e, (d->flags[b] & PSX_BODY_KINEMATIC) != 0, v3(d->vel + 3 * b), v3(d->ang_vel + 3 * b),
+                d->inv_mass[b], v3(d->com + 3 * b), invI);
+        }
+    }
+    for (int j = 0; j < d->n_joints; ++j) {
+        entt::entity e0 = w->entities[d->joint_body0[j]];
+        entt::entity e1 = w->entities[d->joint_body1[j]];
+        const float* f = d->joint_frames + 14 * j;
+        const float* p = d->joint_params + PSX_JOINT_PARAMS * j;
+        glm::vec3 p0 = v3(f), p1 = v3(f + 7);
+        glm::quat o0 = q4(f + 3), o1 = q4(f + 10);
+        switch (d->joint_type[j]) {
+            case PSX_JOINT_FIXED: w->scene->createJoint<physecs::FixedJoint>(e0, p0, o0, e1, p1, o1); break;
+            case PSX_JOINT_REVOLUTE: {
+                auto* jt = w->scene->createJoint<physecs::RevoluteJoint>(e0, p0, o0, e1, p1, o1);
+                jt->setDriveEnabled(p[0] != 0.f);
+                jt->setDriveVelocity(p[1]);
+                jt->setDriveMaxTorque(p[2]);
+                break;
+            }
+            case PSX_JOINT_SPHERICAL: w->scene->createJoint<physecs::SphericalJoint>(e0, p0, o0, e1, p1, o1); break;
+            case PSX_JOINT_PRISMATIC: {
+                auto* jt = w->scene->createJoint<physecs::PrismaticJoint>(e0, p0, o0, e1, p1, o1);
+                jt->setUpperLimit(p[0]);
+                jt->setLowerLimit(p[1]);
+                jt->setDriveEnabled(p[2] != 0.f);
+                jt->setTargetPosition(p[3]);
+                jt->setDriveStiffness(p[4]);
+                jt->setDriveDamping(p[5]);
+                break;
+            }
+            case PSX_JOINT_UNIVERSAL: w->scene->createJoint<physecs::UniversalJoint>(e0, p0, o0, e1, p1, o1); break;
+            case PSX_JOINT_GEAR: {
+                auto* jt = w->scene->createJoint<physecs::GearJoint>(e0, p0, o0, e1, p1, o1);
+                jt->setGearRatio(p[0]);
+                break;
+            }
+            case PSX_JOINT_SERVO: {
+                auto* jt = w->scene->createJoint<physecs::ServoJoint>(e0, p0, o0, e1, p1, o1);
+                jt->setTargetAngle(p[0]);
+                jt->setDriveStiffness(p[1]);
+                jt->setDriveDamping(p[2]);
+                break;
+            }
+        }
+    }
+    return w;
+}
+
+void ref_scene_destroy(void* h) {
+    auto* w = static_cast<RefWorld*>(h);
+    w->scene.reset();
+    delete w;
+}
+
+void ref_scene_step(void* h, float dt) { static_cast<RefWorld*>(h)->scene->simulate(dt); }
+
+void ref_scene_set_knobs(void* h, int substeps, int iterations, float gravity) {
+    auto* w = static_cast<RefWorld*>(h);
+    w->scene->setNumSubSteps(substeps);
+    w->scene->setNumIterations(iterations);
+    w->scene->setGravity(gravity);
+}
+
+/* Body state in desc order. */
+void ref_scene_read(void* h, float* pos, float* quat, float* vel, float* ang_vel) {
+    auto* w = static_cast<RefWorld*>(h);
+    for (size_t b = 0; b < w->entities.size(); ++b) {
+        auto& t = w->registry.get<TransformComponent>(w->entities[b]);
+        pos[3 * b + 0] = t.position.x; pos[3 * b + 1] = t.position.y; pos[3 * b + 2] = t.position.z;
+        quat[4 * b + 0] = t.orientation.x; quat[4 * b + 1] = t.orientation.y;
+        quat[4 * b + 2] = t.orientation.z; quat[4 * b + 3] = t.orientation.w;
+        auto* dyn = w->registry.try_get<physecs::RigidBodyDynamicComponent>(w->entities[b]);
+        glm::vec3 v(0), a(0);
+        if (dyn) { v = dyn->velocity; a = dyn->angularVelocity; }
+        vel[3 * b + 0] = v.x; vel[3 * b + 1] = v.y; vel[3 * b + 2] = v.z;
+        ang_vel[3 * b + 0] = a.x; ang_vel[3 * b + 1] = a.y; ang_vel[3 * b + 2] = a.z;
+    }
+}
+
+/* Overwrite body state (a user patching components between frames). */
+void ref_scene_write(void* h, const float* pos, const float* quat, const float* vel, const float* ang_vel) {
+    auto* w = static_cast<RefWorld*>(h);
+    for (size_t b = 0; b < w->entities.size(); ++b) {
+        auto& t = w->registry.get<TransformComponent>(w->entities[b]);
+        t.position = v3(pos + 3 * b);
+        t.orientation = q4(quat + 4 * b);
+        auto* dyn = w->registry.try_get<physecs::RigidBodyDynamicComponent>(w->entities[b]);
+        if (dyn) { dyn->velocity = v3(vel + 3 * b); dyn->angularVelocity = v3(ang_vel + 3 * b); }
+    }
+}
+
+/* Broadphase pairs of the last simulate(): {entity0, collider0, entity1, collider1}. */
+int ref_scene_pairs(void* h, int32_t* out, int cap) {
+    auto* w = static_cast<RefWorld*>(h);
+    int n = (int)w->scene->potentialContacts.size();
+    for (int i = 0; i < n && i < cap; ++i) {
+        auto& p = w->scene->potentialContacts[i];
+        out[4 * i + 0] = (int32_t)(uint32_t)p.entity0;
+        out[4 * i + 1] = p.colliderIndex0;
+        out[4 * i + 2] = (int32_t)(uint32_t)p.entity1;
+        out[4 * i + 3] = p.colliderIndex1;
+    }
+    return n;
+}
+
+/* Broadphase entry bounds in broadphase order: ids {entity, collider}, bounds {min, max}. */
+int ref_scene_bounds(void* h, int32_t* ids, float* bounds, int cap) {
+    auto* w = static_cast<RefWorld*>(h);
+    int n = (int)w->scene->broadPhaseEntries.size();
+    for (int i = 0; i < n && i < cap; ++i) {
+        auto& e = w->scene->broadPhaseEntries[i];
+        ids[2 * i + 0] = (int32_t)(uint32_t)e.entity;
+        ids[2 * i + 1] = e.colliderIndex;
+        bounds[6 * i + 0] = e.bounds.min.x; bounds[6 * i + 1] = e.bounds.min.y; bounds[6 * i + 2] = e.bounds.min.z;
+        bounds[6 * i + 3] = e.bounds.max.x; bounds[6 * i + 4] = e.bounds.max.y; bounds[6 * i + 5] = e.bounds.max.z;
+    }
+    return n;
+}
+
+/*
+ * Contact constraints of the last simulate(), in solve order.
+ * ids: {b0, b1, numPoints, isSoft}; f: 8 + 4*12 floats per manifold:
+ *   n(3) friction frequency damping pad pad | per point r0(3) r1(3) targetVelocity c lambdaN lambdaT pad pad
+ */
+int ref_scene_contacts(void* h, int32_t* ids, float* f, int cap) {
+    auto* w = static_cast<RefWorld*>(h);
+    int n = (int)w->scene->contactConstraints.size();
+    for (int i = 0; i < n && i < cap; ++i) {
+        auto& c = w->scene->contactConstraints[i];
+        ids[4 * i + 0] = c.b0; ids[4 * i + 1] = c.b1; ids[4 * i + 2] = c.numPoints; ids[4 * i + 3] = c.isSoft;
+        float* o = f + 56 * i;
+        std::memset(o, 0, 56 * sizeof(float));
+        o[0] = c.n.x; o[1] = c.n.y; o[2] = c.n.z; o[3] = c.friction; o[4] = c.frequency; o[5] = c.dampingRatio;
+        for (int k = 0; k < c.numPoints; ++k) {
+            auto& p = c.contactPointConstraints[k];
+            float* q = o + 8 + 12 * k;
+            q[0] = p.r0.x; q[1] = p.r0.y; q[2] = p.r0.z; q[3] = p.r1.x; q[4] = p.r1.y; q[5] = p.r1.z;
+            q[6] = p.targetVelocity; q[7] = p.c; q[8] = p.totalLambdaN; q[9] = p.totalLambdaT;
+        }
+    }
+    return n;
+}
+
+/*
+ * Narrowphase of the reference, physecs::collision (src/Collision.cpp:895),
+ * run on explicit collider pairs at the scene's current poses exactly as
+ * simulate() does (src/Physecs.cpp:188-213).  pairs: {body0, col0, body1, col1}
+ * as desc indices (collider index local to the body).  Per manifold out:
+ * ids {pair, triangleIndex, numPoints, 0}; f: normal(3) pad, then 4 x {p0(3), p1(3)}.
+ */
+int ref_scene_collide(void* h, int n_pairs, const int32_t* pairs, int32_t* ids, float* f, int cap) {
+    auto* w = static_cast<RefWorld*>(h);
+    int n = 0;
+    std::vector<physecs::ContactManifold> buf;
+    for (int i = 0; i < n_pairs; ++i) {
+        entt::entity e0 = w->entities[pairs[4 * i + 0]], e1 = w->entities[pairs[4 * i + 2]];
+        auto& col0 = w->registry.get<physecs::RigidBodyCollisionComponent>(e0).colliders[pairs[4 * i + 1]];
+        auto& col1 = w->registry.get<physecs::RigidBodyCollisionComponent>(e1).colliders[pairs[4 * i + 3]];
+        auto& t0 = w->registry.get<TransformComponent>(e0);
+        auto& t1 = w->registry.get<TransformComponent>(e1);
+        auto pos0 = t0.position + t0.orientation * col0.position;
+        auto or0 = t0.orientation * col0.orientation;
+        auto pos1 = t1.position + t1.orientation * col1.position;
+        auto or1 = t1.orientation * col1.orientation;
+        buf.clear();
+        if (!physecs::collision(pos0, or0, col0.geometry, pos1, or1, col1.geometry, buf)) continue;
+        for (auto& m : buf) {
+            if (!m.numPoints) continue;
+            if (n < cap) {
+                ids[4 * n + 0] = i; ids[4 * n + 1] = m.triangleIndex; ids[4 * n + 2] = m.numPoints; ids[4 * n + 3] = 0;
+                float* o = f + 28 * n;
+                std::memset(o, 0, 28 * sizeof(float));
+                o[0] = m.normal.x; o[1] = m.normal.y; o[2] = m.normal.z;
+                for (int k = 0; k < m.numPoints; ++k) {
+                    float* q = o + 4 + 6 * k;
+                    q[0] = m.points[k].position0.x; q[1] = m.points[k].position0.y; q[2] = m.points[k].position0.z;
+                    q[3] = m.points[k].position1.x; q[4] = m.points[k].position1.y; q[5] = m.points[k].position1.z;
+                }
+            }
+            ++n;
+        }
+    }
+    return n;
+}
+
+/* Joint colour chosen by Scene::addJoint (src/Physecs.cpp:690-710), in creation order. */
+int ref_scene_joint_colors(void* h, int32_t* out, int cap) {
+    auto* w = static_cast<RefWorld*>(h);
+    int n = 0;
+    for (int c = 0; c <= physecs::Scene::JointGraph::maxColors; ++c) {
+        for (auto* j : w->scene->jointGraph.colors[c].joints) {
+            if (n < cap) { out[2 * n] = c; out[2 * n + 1] = (int32_t)(uint32_t)j->getEntity1(); }
+            ++n;
+        }
+    }
+    return n;
+}
+
+}  // extern "C"
