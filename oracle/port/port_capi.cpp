@@ -1,0 +1,142 @@
+/*
+ * port_capi.cpp — C entry points of the CPU oracle (liborc.so).
+ * ORACLE (test infrastructure only): called by tests/, smoke() and bench.py's
+ * CPU-baseline leg through ctypes; never by the physecs_gb300 product.
+ * The entry points and output layouts mirror oracle/ref/ref_capi.cpp so the
+ * restatement can be checked against the reference call for call.
+ */
+#include "world.h"
+#include <cstring>
+
+using namespace orc;
+
+extern "C" {
+
+void* orc_scene_create(const psx_scene_desc* d) {
+    World* w = new World();
+    w->init(d);
+    return w;
+}
+
+void orc_scene_destroy(void* h) { delete static_cast<World*>(h); }
+
+void orc_scene_step(void* h, float dt) { static_cast<World*>(h)->step(dt); }
+
+void orc_scene_set_knobs(void* h, int substeps, int iterations, float gravity) {
+    World* w = static_cast<World*>(h);
+    w->substeps = substeps; w->iterations = iterations; w->g = gravity;
+}
+
+void orc_scene_read(void* h, float* pos, float* quat, float* vel, float* ang) {
+    World* w = static_cast<World*>(h);
+    for (size_t b = 0; b < w->bodies.size(); ++b) {
+        const Body& B = w->bodies[b];
+        std::memcpy(pos + 3 * b, &B.pos, 12);
+        std::memcpy(quat + 4 * b, &B.q, 16);
+        V3 v = B.hasDyn ? B.vel : V3{0, 0, 0}, a = B.hasDyn ? B.ang : V3{0, 0, 0};
+        std::memcpy(vel + 3 * b, &v, 12);
+        std::memcpy(ang + 3 * b, &a, 12);
+    }
+}
+
+void orc_scene_write(void* h, const float* pos, const float* quat, const float* vel, const float* ang) {
+    World* w = static_cast<World*>(h);
+    for (size_t b = 0; b < w->bodies.size(); ++b) {
+        Body& B = w->bodies[b];
+        std::memcpy(&B.pos, pos + 3 * b, 12);
+        std::memcpy(&B.q, quat + 4 * b, 16);
+        if (B.hasDyn) { std::memcpy(&B.vel, vel + 3 * b, 12); std::memcpy(&B.ang, ang + 3 * b, 12); }
+    }
+}
+
+int orc_scene_pairs(void* h, int32_t* out, int cap) {
+    World* w = static_cast<World*>(h);
+    int n = (int)w->pairs.size() / 4;
+    for (int i = 0; i < n && i < cap; ++i) {
+        out[4 * i + 0] = (int32_t)w->bodies[w->pairs[4 * i]].entity;
+        out[4 * i + 1] = w->pairs[4 * i + 1];
+        out[4 * i + 2] = (int32_t)w->bodies[w->pairs[4 * i + 2]].entity;
+        out[4 * i + 3] = w->pairs[4 * i + 3];
+    }
+    return n;
+}
+
+int orc_scene_bounds(void* h, int32_t* ids, float* bounds, int cap) {
+    World* w = static_cast<World*>(h);
+    int n = (int)w->bp.size();
+    for (int i = 0; i < n && i < cap; ++i) {
+        const BPEntry& e = w->bp[i];
+        ids[2 * i] = (int32_t)e.entity; ids[2 * i + 1] = e.col;
+        std::memcpy(bounds + 6 * i, &e.b.min, 12);
+        std::memcpy(bounds + 6 * i + 3, &e.b.max, 12);
+    }
+    return n;
+}
+
+/* same layout as ref_scene_contacts; ids[3] also carries the source pair index in bits 8.. */
+int orc_scene_contacts(void* h, int32_t* ids, float* f, int cap) {
+    World* w = static_cast<World*>(h);
+    int n = (int)w->contacts.size();
+    for (int i = 0; i < n && i < cap; ++i) {
+        const Contact& c = w->contacts[i];
+        ids[4 * i] = c.b0; ids[4 * i + 1] = c.b1; ids[4 * i + 2] = c.np; ids[4 * i + 3] = c.soft ? 1 : 0;
+        float* o = f + 56 * i;
+        std::memset(o, 0, 56 * sizeof(float));
+        o[0] = c.n.x; o[1] = c.n.y; o[2] = c.n.z; o[3] = c.friction; o[4] = c.frequency; o[5] = c.damping;
+        for (int k = 0; k < c.np; ++k) {
+            const CPoint& p = c.p[k];
+            float* q = o + 8 + 12 * k;
+            q[0] = p.r0.x; q[1] = p.r0.y; q[2] = p.r0.z; q[3] = p.r1.x; q[4] = p.r1.y; q[5] = p.r1.z;
+            q[6] = p.targetVelocity; q[7] = p.c; q[8] = p.lamN; q[9] = p.lamT;
+        }
+    }
+    return n;
+}
+
+int orc_scene_collide(void* h, int n_pairs, const int32_t* pairs, int32_t* ids, float* f, int cap) {
+    World* w = static_cast<World*>(h);
+    int n = 0;
+    std::vector<Manifold> buf;
+    for (int i = 0; i < n_pairs; ++i) {
+        int b0 = pairs[4 * i], b1 = pairs[4 * i + 2];
+        int c0 = w->bodies[b0].firstCol + pairs[4 * i + 1], c1 = w->bodies[b1].firstCol + pairs[4 * i + 3];
+        buf.clear();
+        if (!collision(w->colPos(c0), w->colQ(c0), w->colliders[c0].g, w->colPos(c1), w->colQ(c1), w->colliders[c1].g, buf)) continue;
+        for (const Manifold& m : buf) {
+            if (!m.numPoints) continue;
+            if (n < cap) {
+                ids[4 * n] = i; ids[4 * n + 1] = m.triangleIndex; ids[4 * n + 2] = m.numPoints; ids[4 * n + 3] = 0;
+                float* o = f + 28 * n;
+                std::memset(o, 0, 28 * sizeof(float));
+                o[0] = m.normal.x; o[1] = m.normal.y; o[2] = m.normal.z;
+                for (int k = 0; k < m.numPoints; ++k) {
+                    std::memcpy(o + 4 + 6 * k, &m.points[k].p0, 12);
+                    std::memcpy(o + 7 + 6 * k, &m.points[k].p1, 12);
+                }
+            }
+            ++n;
+        }
+    }
+    return n;
+}
+
+int orc_scene_joint_colors(void* h, int32_t* out, int cap) {
+    World* w = static_cast<World*>(h);
+    int n = 0;
+    for (int c = 0; c <= 8; ++c)
+        for (int j : w->colors[c]) {
+            if (n < cap) { out[2 * n] = c; out[2 * n + 1] = (int32_t)w->bodies[w->joints[j].body1].entity; }
+            ++n;
+        }
+    return n;
+}
+
+/* Broadphase bounds of one collider (desc collider index) at the current pose, without margin. */
+void orc_collider_bounds(void* h, int collider, float* out6) {
+    World* w = static_cast<World*>(h);
+    Bounds b = getBounds(w->colPos(collider), w->colQ(collider), w->colliders[collider].g);
+    std::memcpy(out6, &b.min, 12);
+    std::memcpy(out6 + 3, &b.max, 12);
+}
+
+}  // extern "C"

@@ -1,0 +1,127 @@
+/*
+ * world.h — the CPU oracle's restatement of physecs::Scene::simulate.
+ * ORACLE (test infrastructure only; see omath.h).
+ */
+#pragma once
+#include <map>
+#include <memory>
+#include <tuple>
+#include <vector>
+#include "geom.h"
+#include "psx.h"
+
+namespace orc {
+
+struct Body {
+    uint32_t entity;
+    bool hasDyn = false, kinematic = false;
+    V3 pos; Q4 q;
+    V3 vel{0, 0, 0}, ang{0, 0, 0};
+    float invMass = 0;
+    V3 com{0, 0, 0};
+    M3 invI{};
+    int firstCol = 0, nCol = 0;
+    int dyn = -1;               // position in dynamic storage (src/Physecs.cpp:271)
+    bool simulated() const { return hasDyn && !kinematic; }
+};
+
+struct Collider {
+    int body;
+    V3 pos; Q4 q;
+    Geometry g;
+    float friction, restitution, damping;
+    bool trigger, enable;
+    int data;
+};
+
+struct BPEntry { uint32_t entity; int body; int col; Bounds b; bool enable, dynamic; };
+
+struct CPoint {  // ContactPointConstraints, src/ContactConstraints.h:11-29
+    V3 r0, r1, r0xn{}, r1xn{}, t{}, r0xt{}, r1xt{};
+    float targetVelocity, c = 0, lamN = 0, lamT = 0;
+    V3 r0xnt{}, r1xnt{}, r0xtt{}, r1xtt{};
+    float invEffN = 0, invEffT = 0;
+};
+
+struct Contact {  // ContactConstraints, src/ContactConstraints.h:31-48
+    int body0, body1;  // desc body indices (TransformComponent)
+    int b0, b1;        // dynamic indices or -1
+    V3 n;
+    float friction;
+    bool soft;
+    float frequency, damping;
+    int np;
+    CPoint p[4];
+    // provenance for ordering / parity
+    int pair = -1, manifold = 0, tri = -1;
+};
+
+enum RowFlags { RF_NONE = 0, RF_SOFT = 1, RF_ANGULAR = 2, RF_LIMITED = 4 };
+
+struct Row {  // Constraint1D / one lane of Constraint1DW (include/Physecs/Constraint1D*.h)
+    int flags;
+    int b0, b1;
+    V3 linear{0, 0, 0}, angular0{0, 0, 0}, angular1{0, 0, 0};
+    float targetVelocity = 0, c = 0, min = -FLT_MAX, max = FLT_MAX, frequency = 0, damping = 0;
+    V3 linear0t{0, 0, 0}, linear1t{0, 0, 0}, angular0t{0, 0, 0}, angular1t{0, 0, 0};
+    float invEffMass = 0, totalLambda = 0;
+};
+
+struct Joint {
+    int type;
+    int body0, body1;
+    V3 a0p, a1p; Q4 a0q, a1q;
+    float params[PSX_JOINT_PARAMS];
+    int color = -1;
+    // persistent per-joint data (PrismaticJoint.h:9-18, GearJoint.h:10-17)
+    bool makeUpper = false, makeLower = false;
+    float persistent0 = 0, persistent1 = 0, virtual0 = 0, virtual1 = 0;
+    bool gearInit = false;
+    // per-frame rows, creation order
+    std::vector<Row> rows;
+    V3 r0, r1;
+};
+
+struct Velocity { V3 v, w; };
+struct Pseudo { V3 v, w; int count; };
+struct Mass { float invMass; M3 invI; };
+
+using CacheKey = std::tuple<uint32_t, int, uint32_t, int, int>;
+struct CacheVal { int np; V3 r0[4]; float tv[4]; };
+
+struct World {
+    std::vector<Body> bodies;
+    std::vector<Collider> colliders;
+    std::vector<std::unique_ptr<ConvexMesh>> convex;
+    std::vector<std::unique_ptr<TriangleMesh>> tri;
+    std::vector<BPEntry> bp;
+    std::vector<Joint> joints;
+    std::vector<std::vector<int>> colors{9};   // joints per colour (src/Physecs.cpp:690-710)
+    std::vector<unsigned char> colorBits;      // per body
+    std::map<std::pair<uint32_t, uint32_t>, int> nonColliding;
+    std::vector<int> dynBodies;                // dyn index -> body
+    int substeps = 8, iterations = 2;
+    float g = 9.81f;
+
+    std::vector<int> pairs;                    // last frame: {body0, col0, body1, col1} (desc indices / local collider)
+    std::vector<Contact> contacts;
+    std::map<CacheKey, CacheVal> cache, cacheTemp;
+    std::vector<Velocity> vt;
+    std::vector<Pseudo> pv;
+    std::vector<Mass> mt;
+
+    // optional explicit contact solve order: indices into `contacts` as built by the narrowphase
+    std::vector<int> contactOrder;
+    bool useOrder = false;
+
+    void init(const psx_scene_desc* d);
+    void step(float dt);
+    void broadphase();
+    void narrowphase();
+    void buildJointRows();
+    void updateBounds(int body, bool margin);
+    V3 colPos(int c) const;
+    Q4 colQ(int c) const;
+};
+
+}  // namespace orc

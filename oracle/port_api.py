@@ -1,0 +1,132 @@
+"""ctypes access to the CPU oracle (oracle/_build/liborc.so).
+
+ORACLE (test infrastructure only): imported by tests/, __graft_entry__.smoke()
+and bench.py's CPU-baseline leg, never by the physecs_gb300 product.  The
+interface mirrors oracle/ref/ref_api.RefScene so restatement and reference
+can be compared call for call.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liborc.so")
+_lib = None
+
+
+def build():
+    from oracle.build_oracle import build as _b
+    return _b()
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        _lib = C.CDLL(LIB)
+        p = "orc_scene_"
+        getattr(_lib, p + "create").restype = C.c_void_p
+        getattr(_lib, p + "create").argtypes = [C.c_void_p]
+        getattr(_lib, p + "destroy").argtypes = [C.c_void_p]
+        getattr(_lib, p + "step").argtypes = [C.c_void_p, C.c_float]
+        getattr(_lib, p + "set_knobs").argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float]
+        for fn in ("read", "write"):
+            getattr(_lib, p + fn).argtypes = [C.c_void_p] + [C.c_void_p] * 4
+        getattr(_lib, p + "pairs").argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+        getattr(_lib, p + "bounds").argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        getattr(_lib, p + "contacts").argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        getattr(_lib, p + "collide").argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        getattr(_lib, p + "joint_colors").argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+        _lib.orc_collider_bounds.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class OracleScene:
+    """The CPU restatement of physecs::Scene::simulate over a SceneData."""
+
+    h = None
+
+    def __init__(self, scene):
+        from physecs_gb300.desc import make_desc
+        self.scene = scene
+        self._desc = make_desc(scene)
+        self.h = lib().orc_scene_create(C.byref(self._desc))
+        self.n = len(scene.arrays["pos"])
+
+    def close(self):
+        if self.h:
+            lib().orc_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def step(self, dt=None, frames=1):
+        dt = self.scene.dt if dt is None else dt
+        for _ in range(frames):
+            lib().orc_scene_step(self.h, dt)
+
+    def set_knobs(self, substeps, iterations, gravity):
+        lib().orc_scene_set_knobs(self.h, substeps, iterations, gravity)
+
+    def state(self):
+        n = self.n
+        pos, quat = np.zeros((n, 3), np.float32), np.zeros((n, 4), np.float32)
+        vel, ang = np.zeros((n, 3), np.float32), np.zeros((n, 3), np.float32)
+        lib().orc_scene_read(self.h, _p(pos), _p(quat), _p(vel), _p(ang))
+        return dict(pos=pos, quat=quat, vel=vel, ang_vel=ang)
+
+    def write_state(self, st):
+        arrs = [np.ascontiguousarray(st[k], np.float32) for k in ("pos", "quat", "vel", "ang_vel")]
+        lib().orc_scene_write(self.h, *[_p(a) for a in arrs])
+
+    def pairs(self):
+        cap = 1 << 16
+        while True:
+            out = np.zeros((cap, 4), np.int32)
+            n = lib().orc_scene_pairs(self.h, _p(out), cap)
+            if n <= cap:
+                return out[:n]
+            cap = n
+
+    def bounds(self):
+        cap = self.scene.arrays["col_type"].size
+        ids = np.zeros((cap, 2), np.int32)
+        b = np.zeros((cap, 6), np.float32)
+        n = lib().orc_scene_bounds(self.h, _p(ids), _p(b), cap)
+        return ids[:n], b[:n]
+
+    def contacts(self):
+        cap = 1 << 16
+        while True:
+            ids = np.zeros((cap, 4), np.int32)
+            f = np.zeros((cap, 56), np.float32)
+            n = lib().orc_scene_contacts(self.h, _p(ids), _p(f), cap)
+            if n <= cap:
+                return ids[:n], f[:n]
+            cap = n
+
+    def collide(self, pairs):
+        pairs = np.ascontiguousarray(pairs, np.int32).reshape(-1, 4)
+        cap = max(16, 8 * len(pairs))
+        while True:
+            ids = np.zeros((cap, 4), np.int32)
+            f = np.zeros((cap, 28), np.float32)
+            n = lib().orc_scene_collide(self.h, len(pairs), _p(pairs), _p(ids), _p(f), cap)
+            if n <= cap:
+                return ids[:n], f[:n]
+            cap = n
+
+    def joint_colors(self):
+        cap = max(1, len(self.scene.arrays["joint_type"]))
+        out = np.zeros((cap, 2), np.int32)
+        n = lib().orc_scene_joint_colors(self.h, _p(out), cap)
+        return out[:n]
