@@ -140,6 +140,67 @@ typedef struct psx_scene_desc {
     float gravity;
 } psx_scene_desc;
 
+
+/* ------------------------------------------------------------------------
+ * Worlds: one or many independent scenes stepped together.
+ *
+ * A world of one scene is the drop-in for physecs::Scene; a world of many
+ * scenes is the batched form (every kernel carries per-scene segment offsets).
+ * Bodies are addressed scene-major: all bodies of scene 0 in desc order, then
+ * scene 1, and so on.
+ * ---------------------------------------------------------------------- */
+typedef struct psx_world psx_world;
+
+typedef struct psx_world_opts {
+    int32_t pairs_per_collider;      /* broadphase pair capacity per collider (0: default 8) */
+    int32_t manifolds_per_collider;  /* contact manifold capacity per collider (0: default 4) */
+    int32_t block_scene_max_dyn;     /* scenes up to this many dynamic bodies run one per CTA (0: default 8192) */
+    int32_t use_graph;               /* capture the frame in a CUDA graph after the first step */
+} psx_world_opts;
+
+/* Scene::Scene(registry, numThreads) plus the registry's contents
+ * (src/Physecs.cpp:92-98, onRigidBodyCreate :25-37, addJoint :690-710). */
+PSX_API psx_status psx_world_create(const psx_scene_desc* scenes, int32_t n_scenes, const psx_world_opts* opts,
+                                    psx_world** out);
+/* Scene::~Scene (src/Physecs.cpp:815-821) for every scene of the world. */
+PSX_API psx_status psx_world_destroy(psx_world* w);
+/* Scene::simulate(timeStep) (src/Physecs.cpp:112-561), `frames` times, every scene.
+ * Asynchronous: returns once the work is queued on the world's stream. */
+PSX_API psx_status psx_world_step(psx_world* w, float dt, int32_t frames);
+/* Waits for queued work and reports a device-side error (capacity, timeout). */
+PSX_API psx_status psx_world_synchronize(psx_world* w);
+/* Scene::setNumSubSteps / setNumIterations / setGravity (src/Physecs.cpp:100-110) for one scene (-1: all). */
+PSX_API psx_status psx_world_set_knobs(psx_world* w, int32_t scene, int32_t substeps, int32_t iterations, float gravity);
+/* Copy every body's TransformComponent and velocities out of / into device memory
+ * (pos n*3, quat n*4 x,y,z,w, vel n*3, ang_vel n*3; host pointers, any may be NULL). */
+PSX_API psx_status psx_world_read_bodies(psx_world* w, float* pos, float* quat, float* vel, float* ang_vel);
+PSX_API psx_status psx_world_write_bodies(psx_world* w, const float* pos, const float* quat, const float* vel,
+                                          const float* ang_vel);
+/* One end-to-end simulate through host buffers: upload the given state, step one
+ * frame, download the new state into the same buffers, and wait. */
+PSX_API psx_status psx_world_simulate_host(psx_world* w, float dt, float* pos, float* quat, float* vel, float* ang_vel);
+/* counts[8] = {bodies, colliders, dynamic bodies, joints, scenes, pairs, manifolds, error bits} */
+PSX_API psx_status psx_world_counts(psx_world* w, int32_t* counts);
+/* Inspection of the last frame (synchronises):
+ *   pairs: {scene, entity0, collider0, entity1, collider1} per broadphase pair
+ *   contacts: ids {scene, b0, b1, np | soft << 8, entity0, collider0, entity1, collider1} per
+ *             manifold, b = scene-local dynamic index or -1; f = 56 floats per manifold
+ *             (normal, friction, frequency, damping, pad, pad, then per point r0, r1,
+ *             targetVelocity, c, lambdaN, lambdaT, pad, pad), in solve order (colour by
+ *             colour); meta = {colour, triangleIndex} per manifold
+ *   bounds: {min xyz, max xyz} per collider, desc order */
+PSX_API int32_t psx_world_get_pairs(psx_world* w, int32_t* out, int32_t cap);
+PSX_API int32_t psx_world_get_contacts(psx_world* w, int32_t* ids, float* f, int32_t* meta, int32_t cap);
+PSX_API int32_t psx_world_get_bounds(psx_world* w, float* bounds, int32_t cap);
+/* Human-readable description of the calling thread's last error. */
+PSX_API const char* psx_last_error_string(void);
+
+/* ---- single-scene spelling of the same entry points (physecs::Scene) ---- */
+typedef psx_world psx_scene;
+PSX_API psx_status psx_scene_create(const psx_scene_desc* desc, psx_scene** out);
+PSX_API psx_status psx_scene_destroy(psx_scene* s);
+PSX_API psx_status psx_scene_simulate(psx_scene* s, float dt);
+
 #ifdef __cplusplus
 }
 #endif

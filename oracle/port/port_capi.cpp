@@ -131,6 +131,34 @@ int orc_scene_joint_colors(void* h, int32_t* out, int cap) {
     return n;
 }
 
+/* Solve the next step's contacts in the given order: keys {entity0, collider0, entity1,
+ * collider1, triangleIndex} per manifold.  Returns nothing; the count of manifolds that
+ * did not match is reported by orc_scene_order_error after the step. */
+void orc_scene_set_contact_order(void* h, int n, const int32_t* keys) {
+    World* w = static_cast<World*>(h);
+    w->orderKeys.clear();
+    for (int i = 0; i < n; ++i)
+        w->orderKeys.emplace_back((uint32_t)keys[5 * i], keys[5 * i + 1], (uint32_t)keys[5 * i + 2], keys[5 * i + 3], keys[5 * i + 4]);
+    w->useOrder = true;
+}
+
+int orc_scene_order_error(void* h) { return static_cast<World*>(h)->orderError; }
+
+/* Manifold keys {entity0, collider0, entity1, collider1, triangleIndex} of the last
+ * step's contacts, in the same order as orc_scene_contacts. */
+int orc_scene_contact_keys(void* h, int32_t* keys, int cap) {
+    World* w = static_cast<World*>(h);
+    int n = (int)w->contacts.size();
+    for (int i = 0; i < n && i < cap; ++i) {
+        const Contact& c = w->contacts[i];
+        const int* pr = &w->pairs[4 * c.pair];
+        keys[5 * i] = (int32_t)w->bodies[pr[0]].entity; keys[5 * i + 1] = pr[1];
+        keys[5 * i + 2] = (int32_t)w->bodies[pr[2]].entity; keys[5 * i + 3] = pr[3];
+        keys[5 * i + 4] = c.tri;
+    }
+    return n;
+}
+
 /* Broadphase bounds of one collider (desc collider index) at the current pose, without margin. */
 void orc_collider_bounds(void* h, int collider, float* out6) {
     World* w = static_cast<World*>(h);

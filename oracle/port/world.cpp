@@ -596,8 +596,26 @@ void World::step(float dt) {
     narrowphase();
     buildJointRows();
     std::vector<int> order;
-    if (useOrder && contactOrder.size() == contacts.size()) order = contactOrder;
-    else { order.resize(contacts.size()); for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i; }
+    orderError = 0;
+    if (useOrder) {
+        std::map<CacheKey, int> byKey;
+        for (size_t i = 0; i < contacts.size(); ++i) {
+            const Contact& c = contacts[i];
+            const int* pr = &pairs[4 * c.pair];
+            byKey[CacheKey{bodies[pr[0]].entity, pr[1], bodies[pr[2]].entity, pr[3], c.tri}] = (int)i;
+        }
+        for (const CacheKey& k : orderKeys) {
+            auto it = byKey.find(k);
+            if (it == byKey.end()) { ++orderError; continue; }
+            order.push_back(it->second);
+            byKey.erase(it);
+        }
+        orderError += (int)byKey.size();
+        useOrder = false;
+    } else {
+        order.resize(contacts.size());
+        for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+    }
     size_t nd = dynBodies.size();
     vt.resize(nd); pv.resize(nd); mt.resize(nd);
     float h = dt / substeps;

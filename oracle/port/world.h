@@ -110,9 +110,11 @@ struct World {
     std::vector<Pseudo> pv;
     std::vector<Mass> mt;
 
-    // optional explicit contact solve order: indices into `contacts` as built by the narrowphase
-    std::vector<int> contactOrder;
+    // optional explicit contact solve order for the next step, as manifold keys
+    // {entity0, collider0, entity1, collider1, triangleIndex}; unmatched keys set orderError
+    std::vector<CacheKey> orderKeys;
     bool useOrder = false;
+    int orderError = 0;
 
     void init(const psx_scene_desc* d);
     void step(float dt);

@@ -42,6 +42,9 @@ def lib():
         getattr(_lib, p + "collide").argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         getattr(_lib, p + "joint_colors").argtypes = [C.c_void_p, C.c_void_p, C.c_int]
         _lib.orc_collider_bounds.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        _lib.orc_scene_set_contact_order.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        _lib.orc_scene_order_error.argtypes = [C.c_void_p]
+        _lib.orc_scene_contact_keys.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
     return _lib
 
 
@@ -130,3 +133,21 @@ class OracleScene:
         out = np.zeros((cap, 2), np.int32)
         n = lib().orc_scene_joint_colors(self.h, _p(out), cap)
         return out[:n]
+
+    def set_contact_order(self, keys):
+        """Solve the next step's contacts in this order (rows {e0, c0, e1, c1, tri})."""
+        k = np.ascontiguousarray(keys, np.int32).reshape(-1, 5)
+        self._order_keys = k
+        lib().orc_scene_set_contact_order(self.h, len(k), _p(k))
+
+    def order_error(self):
+        return lib().orc_scene_order_error(self.h)
+
+    def contact_keys(self):
+        cap = 1 << 16
+        while True:
+            out = np.zeros((cap, 5), np.int32)
+            n = lib().orc_scene_contact_keys(self.h, _p(out), cap)
+            if n <= cap:
+                return out[:n]
+            cap = n

@@ -1,0 +1,162 @@
+"""Python face of the GB300 simulation hot path: ctypes over libpsx.so (include/psx.h).
+
+``World`` mirrors physecs::Scene (Physecs include/Physecs/Physecs.h:199-229) for one
+or many scenes: ``step(dt)`` is ``simulate(dt)``, ``set_knobs`` is
+setNumSubSteps / setNumIterations / setGravity, and body state moves between host
+arrays and device memory explicitly, the way the reference reads and writes its
+EnTT components.  There is no CPU fallback: if the CUDA library is missing or no
+GPU is present, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .desc import PsxSceneDesc, make_desc
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libpsx.so")
+
+PSX_STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OUT_OF_MEMORY", 3: "CAPACITY", 4: "TIMEOUT", 5: "CUDA", 6: "NOT_READY"}
+EXPORTS = ["psx_world_create", "psx_world_destroy", "psx_world_step", "psx_world_synchronize", "psx_world_set_knobs",
+           "psx_world_read_bodies", "psx_world_write_bodies", "psx_world_simulate_host", "psx_world_counts",
+           "psx_world_get_pairs", "psx_world_get_contacts", "psx_world_get_bounds", "psx_last_error_string",
+           "psx_scene_create", "psx_scene_destroy", "psx_scene_simulate"]
+
+_lib = None
+
+
+class PsxError(RuntimeError):
+    pass
+
+
+class PsxWorldOpts(C.Structure):
+    _fields_ = [("pairs_per_collider", C.c_int32), ("manifolds_per_collider", C.c_int32),
+                ("block_scene_max_dyn", C.c_int32), ("use_graph", C.c_int32)]
+
+
+def load():
+    """Load libpsx.so (building it first when this checkout has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        from . import _build
+        _build.build()
+    lib = C.CDLL(LIB_PATH)
+    vp = C.c_void_p
+    lib.psx_world_create.argtypes = [C.POINTER(PsxSceneDesc), C.c_int32, C.POINTER(PsxWorldOpts), C.POINTER(vp)]
+    lib.psx_world_destroy.argtypes = [vp]
+    lib.psx_world_step.argtypes = [vp, C.c_float, C.c_int32]
+    lib.psx_world_synchronize.argtypes = [vp]
+    lib.psx_world_set_knobs.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_float]
+    lib.psx_world_read_bodies.argtypes = [vp, vp, vp, vp, vp]
+    lib.psx_world_write_bodies.argtypes = [vp, vp, vp, vp, vp]
+    lib.psx_world_simulate_host.argtypes = [vp, C.c_float, vp, vp, vp, vp]
+    lib.psx_world_counts.argtypes = [vp, vp]
+    lib.psx_world_get_pairs.argtypes = [vp, vp, C.c_int32]
+    lib.psx_world_get_pairs.restype = C.c_int32
+    lib.psx_world_get_contacts.argtypes = [vp, vp, vp, vp, C.c_int32]
+    lib.psx_world_get_contacts.restype = C.c_int32
+    lib.psx_world_get_bounds.argtypes = [vp, vp, C.c_int32]
+    lib.psx_world_get_bounds.restype = C.c_int32
+    lib.psx_last_error_string.restype = C.c_char_p
+    _lib = lib
+    return lib
+
+
+def _check(status):
+    if status != 0:
+        msg = load().psx_last_error_string().decode(errors="replace")
+        raise PsxError("psx %s: %s" % (PSX_STATUS.get(status, status), msg))
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class World:
+    """One or many scenes resident on the GPU, stepped together."""
+
+    h = None
+
+    def __init__(self, scenes, pairs_per_collider=0, manifolds_per_collider=0, block_scene_max_dyn=0, use_graph=False):
+        lib = load()
+        if not isinstance(scenes, (list, tuple)):
+            scenes = [scenes]
+        self.scenes = list(scenes)
+        arr = (PsxSceneDesc * len(scenes))()
+        for i, s in enumerate(scenes):
+            arr[i] = make_desc(s)
+        self._descs = arr
+        opts = PsxWorldOpts(pairs_per_collider, manifolds_per_collider, block_scene_max_dyn, 1 if use_graph else 0)
+        h = C.c_void_p()
+        _check(lib.psx_world_create(arr, len(scenes), C.byref(opts), C.byref(h)))
+        self.h = h
+        self.n_bodies = sum(len(s.arrays["pos"]) for s in scenes)
+        self.body_start = np.cumsum([0] + [len(s.arrays["pos"]) for s in scenes])
+
+    def close(self):
+        if self.h:
+            load().psx_world_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, dt=None, frames=1):
+        dt = self.scenes[0].dt if dt is None else dt
+        _check(load().psx_world_step(self.h, C.c_float(dt), frames))
+
+    def synchronize(self):
+        _check(load().psx_world_synchronize(self.h))
+
+    def set_knobs(self, substeps, iterations, gravity, scene=-1):
+        _check(load().psx_world_set_knobs(self.h, scene, substeps, iterations, C.c_float(gravity)))
+
+    def read_bodies(self):
+        n = self.n_bodies
+        st = dict(pos=np.zeros((n, 3), np.float32), quat=np.zeros((n, 4), np.float32),
+                  vel=np.zeros((n, 3), np.float32), ang_vel=np.zeros((n, 3), np.float32))
+        _check(load().psx_world_read_bodies(self.h, _p(st["pos"]), _p(st["quat"]), _p(st["vel"]), _p(st["ang_vel"])))
+        return st
+
+    def write_bodies(self, st):
+        a = [np.ascontiguousarray(st[k], np.float32) for k in ("pos", "quat", "vel", "ang_vel")]
+        _check(load().psx_world_write_bodies(self.h, *[_p(x) for x in a]))
+
+    def simulate_host(self, dt, st):
+        """End-to-end simulate through host buffers (upload, one frame, download) in place."""
+        _check(load().psx_world_simulate_host(self.h, C.c_float(dt), _p(st["pos"]), _p(st["quat"]), _p(st["vel"]),
+                                              _p(st["ang_vel"])))
+
+    def counts(self):
+        c = np.zeros(8, np.int32)
+        _check(load().psx_world_counts(self.h, _p(c)))
+        keys = ["bodies", "colliders", "dynamic", "joints", "scenes", "pairs", "manifolds", "error"]
+        return dict(zip(keys, (int(v) for v in c)))
+
+    def pairs(self):
+        n = self.counts()["pairs"]
+        out = np.zeros((max(n, 1), 5), np.int32)
+        m = load().psx_world_get_pairs(self.h, _p(out), len(out))
+        return out[:m]
+
+    def contacts(self):
+        n = self.counts()["manifolds"]
+        ids = np.zeros((max(n, 1), 8), np.int32)
+        f = np.zeros((max(n, 1), 56), np.float32)
+        meta = np.zeros((max(n, 1), 2), np.int32)
+        m = load().psx_world_get_contacts(self.h, _p(ids), _p(f), _p(meta), len(ids))
+        return ids[:m], f[:m], meta[:m]
+
+    def bounds(self):
+        n = self.counts()["colliders"]
+        b = np.zeros((n, 6), np.float32)
+        load().psx_world_get_bounds(self.h, _p(b), n)
+        return b

@@ -1,0 +1,278 @@
+// broadphase.cu — collider bounds and the LBVH broadphase.
+//
+// Replaces the reference's sweep-and-prune (Physecs src/Physecs.cpp:119-173).  The
+// pair SET is identical: a pair is reported iff both colliders have
+// enableSimulation, they belong to different entities, at least one is dynamic, and
+// their bounds overlap inclusively on all three axes — exactly the SAP conditions.
+// Steps per frame: per-scene centroid bounds -> 30-bit (or scene-prefixed) Morton
+// keys -> radix sort -> Karras (2012) radix tree per scene segment -> bottom-up
+// refit -> per-leaf traversal (count, scan, emit) writing canonical pairs
+// (entity0 < entity1, src/Physecs.cpp:156-170).
+#include "frame.cuh"
+#include "narrow_convex.cuh"
+
+namespace psx {
+
+// ---------------------------------------------------------------- bounds
+
+// getBounds (src/BoundsUtil.cpp:23-85) at the collider's world pose (src/Physecs.cpp:79-90).
+// margin_mode 0: every collider, no margin (onRigidBodyCreate, src/Physecs.cpp:25-37);
+// margin_mode 1: colliders of simulated dynamic bodies, +0.01 m (src/Physecs.cpp:555-559).
+__global__ void k_aabb(World w, int margin_mode) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= w.n_colliders) return;
+    int4 ci = w.col_info[c];
+    int4 bi = w.info[ci.x];
+    bool simulated = (bi.y & BODY_DYN) && !(bi.y & BODY_KIN);
+    if (margin_mode == 1 && !simulated) return;
+    if (ci.y == G_TRIMESH && margin_mode == 1) return;
+    Q4 bq = ld4(w.quat[ci.x]);
+    V3 bp = ld3(w.pos[ci.x]);
+    V3 pos = bp + qrot(bq, ld3(w.col_pos[c]));
+    Q4 ori = qmul(bq, ld4(w.col_quat[c]));
+    float4 pr = w.col_params[c];
+    GeomD g{ci.y, {pr.x, pr.y, pr.z}, ci.z};
+    Bounds b;
+    if (ci.y == G_TRIMESH) {
+        TriMeshDev tm = w.trimesh[ci.z];
+        V3 mn = v3s(FLT_MAX), mx = v3s(-FLT_MAX);
+        for (int i = 0; i < tm.vert_count; ++i) {
+            V3 t = pos + qrot(ori, ld3(w.tri_verts[tm.vert_start + i]));
+            mn = vmin(mn, t); mx = vmax(mx, t);
+        }
+        b = {mn, mx};
+    } else {
+        b = getBounds(w, pos, ori, g);
+    }
+    if (margin_mode == 1) { b.max += v3s(0.01f); b.min -= v3s(0.01f); }
+    w.aabb_min[c] = st4(b.min);
+    w.aabb_max[c] = st4(b.max);
+}
+
+void launch_aabb(const World& w, int margin_mode, cudaStream_t s) {
+    if (w.n_colliders == 0) return;
+    k_aabb<<<(w.n_colliders + 255) / 256, 256, 0, s>>>(w, margin_mode);
+}
+
+// ---------------------------------------------------------------- Morton keys
+
+__global__ void k_scene_bounds(World w, FrameBuf f) {
+    int s = blockIdx.x;
+    int cs = w.scene_col[s], ce = w.scene_col[s + 1];
+    float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (int c = cs + threadIdx.x; c < ce; c += blockDim.x) {
+        float4 a = w.aabb_min[c], b = w.aabb_max[c];
+        float m[3] = {(a.x + b.x) * 0.5f, (a.y + b.y) * 0.5f, (a.z + b.z) * 0.5f};
+        for (int k = 0; k < 3; ++k) { lo[k] = fminf(lo[k], m[k]); hi[k] = fmaxf(hi[k], m[k]); }
+    }
+    __shared__ float sh[6][32];
+    for (int k = 0; k < 3; ++k) {
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
+            hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
+        }
+    }
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) for (int k = 0; k < 3; ++k) { sh[k][wid] = lo[k]; sh[3 + k][wid] = hi[k]; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int q = 1; q < (int)(blockDim.x >> 5); ++q)
+            for (int k = 0; k < 3; ++k) { sh[k][0] = fminf(sh[k][0], sh[k][q]); sh[3 + k][0] = fmaxf(sh[3 + k][0], sh[3 + k][q]); }
+        f.scene_lo[s] = make_float4(sh[0][0], sh[1][0], sh[2][0], 0.f);
+        f.scene_hi[s] = make_float4(sh[3][0], sh[4][0], sh[5][0], 0.f);
+    }
+}
+
+__device__ __forceinline__ uint32_t expand_bits(uint32_t v, int bits) {
+    // spread the low `bits` bits of v three positions apart
+    uint32_t r = 0;
+    for (int i = 0; i < bits; ++i) r |= ((v >> i) & 1u) << (3 * i);
+    return r;
+}
+
+__global__ void k_morton(World w, FrameBuf f, int mbits) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= w.n_colliders) return;
+    int s = w.info[w.col_info[c].x].w;
+    float4 lo = f.scene_lo[s], hi = f.scene_hi[s];
+    float4 a = w.aabb_min[c], b = w.aabb_max[c];
+    int per = mbits / 3;
+    float scale = (float)(1u << per);
+    float m[3] = {(a.x + b.x) * 0.5f, (a.y + b.y) * 0.5f, (a.z + b.z) * 0.5f};
+    float l[3] = {lo.x, lo.y, lo.z}, h[3] = {hi.x, hi.y, hi.z};
+    uint32_t code = 0;
+    for (int k = 0; k < 3; ++k) {
+        float ext = h[k] - l[k];
+        float u = ext > 0.f ? (m[k] - l[k]) / ext : 0.f;
+        u = fminf(fmaxf(u, 0.f), 1.f);
+        uint32_t q = (uint32_t)fminf(u * scale, scale - 1.f);
+        code |= expand_bits(q, per) << (2 - k);
+    }
+    f.keys[c] = ((uint32_t)s << mbits) | code;
+    f.order[c] = c;
+}
+
+// ---------------------------------------------------------------- Karras radix tree
+
+__device__ __forceinline__ int kdelta(const uint32_t* keys, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    uint32_t a = keys[i], b = keys[j];
+    if (a == b) return 32 + __clz((uint32_t)(i ^ j));
+    return __clz(a ^ b);
+}
+
+__device__ __forceinline__ int scene_of_position(const World& w, int p) {
+    int lo = 0, hi = w.n_scenes;  // largest s with scene_col[s] <= p
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (w.scene_col[mid] <= p) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// one thread per sorted leaf position p; position p builds internal node (p - cs) of its scene
+__global__ void k_karras(World w, FrameBuf f) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= w.n_colliders) return;
+    int s = scene_of_position(w, p);
+    int cs = w.scene_col[s], ce = w.scene_col[s + 1];
+    int n = ce - cs;
+    int i = p - cs;
+    if (n < 2 || i >= n - 1) return;
+    const uint32_t* keys = f.keys + cs;
+    int ibase = cs - s;
+    int d = (kdelta(keys, n, i, i + 1) - kdelta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+    int dmin = kdelta(keys, n, i, i - d);
+    int lmax = 2;
+    while (kdelta(keys, n, i, i + lmax * d) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (kdelta(keys, n, i, i + (l + t) * d) > dmin) l += t;
+    int j = i + l * d;
+    int dnode = kdelta(keys, n, i, j);
+    int sp = 0, t = l;
+    do {
+        t = (t + 1) >> 1;
+        if (kdelta(keys, n, i, i + (sp + t) * d) > dnode) sp += t;
+    } while (t > 1);
+    int gamma = i + sp * d + min(d, 0);
+    int lo = min(i, j), hi = max(i, j);
+    int node = ibase + i;
+    int left = (lo == gamma) ? ~(cs + gamma) : ibase + gamma;
+    int right = (hi == gamma + 1) ? ~(cs + gamma + 1) : ibase + gamma + 1;
+    f.bvh.left[node] = left;
+    f.bvh.right[node] = right;
+    f.bvh.first[node] = cs + lo;
+    f.bvh.last[node] = cs + hi;
+    f.bvh.visits[node] = 0;
+    if (left >= 0) f.bvh.parent[left] = node; else f.bvh.leaf_parent[~left] = node;
+    if (right >= 0) f.bvh.parent[right] = node; else f.bvh.leaf_parent[~right] = node;
+    if (i == 0) f.bvh.parent[node] = -1;
+}
+
+__global__ void k_refit(World w, FrameBuf f) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= w.n_colliders) return;
+    int s = scene_of_position(w, p);
+    int n = w.scene_col[s + 1] - w.scene_col[s];
+    if (n < 2) return;
+    int node = f.bvh.leaf_parent[p];
+    while (node >= 0) {
+        __threadfence();
+        if (atomicAdd(&f.bvh.visits[node], 1) == 0) return;
+        __threadfence();
+        int L = f.bvh.left[node], R = f.bvh.right[node];
+        float4 lmin, lmax, rmin, rmax;
+        if (L < 0) { int c = f.order[~L]; lmin = w.aabb_min[c]; lmax = w.aabb_max[c]; }
+        else { lmin = __ldcg(&f.bvh.bmin[L]); lmax = __ldcg(&f.bvh.bmax[L]); }
+        if (R < 0) { int c = f.order[~R]; rmin = w.aabb_min[c]; rmax = w.aabb_max[c]; }
+        else { rmin = __ldcg(&f.bvh.bmin[R]); rmax = __ldcg(&f.bvh.bmax[R]); }
+        f.bvh.bmin[node] = make_float4(fminf(lmin.x, rmin.x), fminf(lmin.y, rmin.y), fminf(lmin.z, rmin.z), 0.f);
+        f.bvh.bmax[node] = make_float4(fmaxf(lmax.x, rmax.x), fmaxf(lmax.y, rmax.y), fmaxf(lmax.z, rmax.z), 0.f);
+        node = f.bvh.parent[node];
+    }
+}
+
+// ---------------------------------------------------------------- traversal
+
+__device__ __forceinline__ bool overlap_incl(float4 amin, float4 amax, float4 bmin, float4 bmax) {
+    if (amax.x < bmin.x || amin.x > bmax.x) return false;
+    if (amax.y < bmin.y || amin.y > bmax.y) return false;
+    if (amax.z < bmin.z || amin.z > bmax.z) return false;
+    return true;
+}
+
+// SAP filters of src/Physecs.cpp:138-147
+__device__ __forceinline__ bool pair_ok(const World& w, int ca, int cb) {
+    int4 a = w.col_info[ca], b = w.col_info[cb];
+    if (!(a.w & COL_ENABLE) || !(b.w & COL_ENABLE)) return false;
+    if (a.x == b.x) return false;
+    if (!((a.w & COL_DYNAMIC) || (b.w & COL_DYNAMIC))) return false;
+    return true;
+}
+
+template <bool EMIT>
+__global__ void k_traverse(World w, FrameBuf f) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= w.n_colliders) return;
+    int ca = f.order[p];
+    int s = w.info[w.col_info[ca].x].w;
+    int cs = w.scene_col[s], n = w.scene_col[s + 1] - cs;
+    int count = 0;
+    int out = EMIT ? f.leaf_off[p] : 0;
+    if (n >= 2 && (w.col_info[ca].w & COL_ENABLE)) {
+        float4 qmin = w.aabb_min[ca], qmax = w.aabb_max[ca];
+        int stack[64];
+        int sp = 0;
+        stack[sp++] = cs - s;  // root of this scene's tree
+        while (sp) {
+            int node = stack[--sp];
+            int ch[2] = {f.bvh.left[node], f.bvh.right[node]};
+            for (int k = 0; k < 2; ++k) {
+                int c = ch[k];
+                if (c < 0) {
+                    int q = ~c;
+                    if (q <= p) continue;
+                    int cb = f.order[q];
+                    if (!overlap_incl(qmin, qmax, w.aabb_min[cb], w.aabb_max[cb])) continue;
+                    if (!pair_ok(w, ca, cb)) continue;
+                    if (EMIT) {
+                        int slot = out + count;
+                        if (slot < f.pair_cap) {
+                            uint32_t ea = (uint32_t)w.info[w.col_info[ca].x].x, eb = (uint32_t)w.info[w.col_info[cb].x].x;
+                            f.pairs[slot] = ea < eb ? make_int2(ca, cb) : make_int2(cb, ca);
+                        }
+                    }
+                    ++count;
+                } else {
+                    if (f.bvh.last[c] <= p) continue;
+                    if (!overlap_incl(qmin, qmax, f.bvh.bmin[c], f.bvh.bmax[c])) continue;
+                    if (sp < 64) stack[sp++] = c;
+                    else atomicOr(w.err, ERR_STACK_CAPACITY);
+                }
+            }
+        }
+    }
+    if (!EMIT) f.leaf_cnt[p] = count;
+}
+
+__global__ void k_pairs_check(FrameBuf f, int* err) {
+    if (*f.n_pairs > f.pair_cap) { atomicOr(err, ERR_PAIR_CAPACITY); *f.n_pairs = f.pair_cap; }
+}
+
+void launch_broadphase(const World& w, FrameBuf& f, int mbits, int total_bits, cudaStream_t s) {
+    int n = w.n_colliders;
+    if (n == 0) return;
+    int nb = (n + 255) / 256;
+    k_scene_bounds<<<w.n_scenes, 256, 0, s>>>(w, f);
+    k_morton<<<nb, 256, 0, s>>>(w, f, mbits);
+    radix_sort_pairs(f.keys, f.order, f.keys_tmp, f.order_tmp, n, total_bits, f.radix_hist, s);
+    k_karras<<<nb, 256, 0, s>>>(w, f);
+    k_refit<<<nb, 256, 0, s>>>(w, f);
+    k_traverse<false><<<nb, 256, 0, s>>>(w, f);
+    scan_exclusive(f.leaf_cnt, f.leaf_off, n, f.n_pairs, f.scan_scratch, s);
+    k_traverse<true><<<nb, 256, 0, s>>>(w, f);
+    k_pairs_check<<<1, 1, 0, s>>>(f, w.err);
+}
+
+}  // namespace psx

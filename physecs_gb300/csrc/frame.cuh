@@ -1,0 +1,79 @@
+// frame.cuh — per-frame device buffers and the kernel entry points of one frame.
+#pragma once
+#include "types.cuh"
+#include "prims.cuh"
+
+namespace psx {
+
+struct BVHNodes {
+    int* left;        // child index: >= 0 internal node (global), < 0 leaf ~(sorted position)
+    int* right;
+    int* parent;      // parent of internal nodes (global internal index), -1 for roots
+    int* leaf_parent; // parent of each sorted leaf
+    int* first;       // sorted-leaf range covered by each internal node
+    int* last;
+    float4* bmin;
+    float4* bmax;
+    int* visits;
+};
+
+struct FrameBuf {
+    // broadphase
+    float4* scene_lo;     // [S] centroid bounds for Morton quantisation
+    float4* scene_hi;
+    uint32_t* keys;       // [n_colliders]
+    int* order;           // sorted leaf -> collider
+    uint32_t* keys_tmp;
+    int* order_tmp;
+    int* radix_hist;
+    BVHNodes bvh;
+    int* leaf_cnt;        // [n_colliders] pairs found per sorted leaf
+    int* leaf_off;
+    int* scan_scratch;
+    int pair_cap;
+    int2* pairs;          // collider indices, entity(a) < entity(b)
+    int* n_pairs;         // device scalar
+    // narrowphase
+    int* pair_cat;        // 0 analytic, 1 convex mesh, 2 triangle mesh
+    int* cat_flag;        // scratch 0/1 per pair
+    int* cat_pos[3];
+    int* cat_count;       // [3]
+    int* cat_list;        // [3 * pair_cap]
+    Manifold* man_pair;   // one slot per pair (analytic / convex categories)
+    int tri_cap;          // triangle-mesh pair slots
+    Manifold* man_tri;    // kTriManifolds slots per triangle-mesh pair slot
+    int* pair_tslot;      // triangle-mesh slot of a pair
+    int* pair_nman;
+    int* pair_moff;
+    int man_cap;
+    int* n_man;
+    Contact* contacts;    // one per manifold, in pair order
+    int* man_scene_cnt;   // [S]
+    int* scene_man;       // [S+1]
+    // colouring
+    int* claim;           // [n_dyn]
+    int* color_of;        // [man_cap]
+    int* corder;          // [man_cap] manifolds sorted by (scene, colour, index)
+    int* scene_ncolor;    // [S]
+    int* color_start;     // [S * (kMaxColors+1)]
+    int* claim_pos;       // [S * (kMaxColors+1)] scatter counters
+    // restitution cache: open addressing, two tables; cache_parity selects the current one
+    int cache_cap;        // power of two
+    CacheEntry* cache_a;
+    CacheEntry* cache_b;
+    int* cache_parity;
+    // grid barrier: count, generation, flag
+    unsigned int* bar;
+};
+
+// kernel launch helpers (definitions in the .cu files)
+void launch_aabb(const World& w, int margin_mode, cudaStream_t s);
+void launch_broadphase(const World& w, FrameBuf& f, int mbits, int total_bits, cudaStream_t s);
+void launch_narrowphase(const World& w, FrameBuf& f, cudaStream_t s);
+void launch_contacts(const World& w, FrameBuf& f, cudaStream_t s);
+void launch_solver(const World& w, FrameBuf& f, const int* block_scenes, int n_block_scenes, const int* grid_scenes,
+                   int n_grid_scenes, int grid_blocks, cudaStream_t s);
+int solver_grid_blocks();
+void launch_joint_layout(const World& w, cudaStream_t s);
+
+}  // namespace psx

@@ -1,0 +1,804 @@
+// solver.cu — contact rows, graph colouring, joint rows and the TGS substep loop.
+//
+// Restates Physecs src/Physecs.cpp:209-531 with src/ContactConstraints.cpp,
+// src/Constraint1D.cpp (scalar rows, joint colour 8) and src/Constraint1DW.cpp
+// (4-lane rows, joint colours 0-7).  The reference solves every contact serially;
+// here contacts are graph-coloured so that each colour is body-disjoint and its
+// contacts can be solved in parallel with a result identical to any serial order
+// of that colour.  Joints keep the reference's own colouring (colours 0-7 are
+// entity-disjoint); the overflow colour is split into sub-colours on the host.
+//
+// One persistent kernel runs a whole frame of a scene: colouring, then every
+// substep's row update, velocity integration, preSolve, iterations, position
+// integration, relaxation and write-back.  Small scenes run one per CTA with
+// __syncthreads between phases; large scenes run on the whole grid with a
+// bounded grid barrier.
+#include "frame.cuh"
+
+namespace psx {
+
+constexpr float kPi = 3.14159265358979323846f;
+
+// ---------------------------------------------------------------- restitution cache
+
+__device__ __forceinline__ unsigned long long cache_key(int ca, int cb, int tri) {
+    return ((unsigned long long)(uint32_t)ca << 41) | ((unsigned long long)(uint32_t)cb << 18) | (unsigned long long)(uint32_t)(tri + 1);
+}
+__device__ __forceinline__ uint32_t cache_hash(unsigned long long k) {
+    k ^= k >> 33; k *= 0xff51afd7ed558ccdull; k ^= k >> 33; k *= 0xc4ceb9fe1a85ec53ull; k ^= k >> 33;
+    return (uint32_t)k;
+}
+constexpr unsigned long long kEmpty = ~0ull;
+
+__global__ void k_cache_clear(FrameBuf f) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= f.cache_cap) return;
+    CacheEntry* cur = f.cache_parity[0] ? f.cache_b : f.cache_a;
+    cur[i].key = kEmpty;
+}
+
+__global__ void k_cache_flip(FrameBuf f) { f.cache_parity[0] ^= 1; }
+
+// ---------------------------------------------------------------- contact rows (src/Physecs.cpp:215-314)
+
+__global__ void k_build_contacts(World w, FrameBuf f) {
+    int np = *f.n_pairs;
+    CacheEntry* cur = f.cache_parity[0] ? f.cache_b : f.cache_a;
+    const CacheEntry* prev = f.cache_parity[0] ? f.cache_a : f.cache_b;
+    unsigned mask = (unsigned)f.cache_cap - 1u;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+        int cnt = f.pair_nman[p];
+        if (!cnt) continue;
+        int off = f.pair_moff[p];
+        int2 pr = f.pairs[p];
+        int4 cA = w.col_info[pr.x], cB = w.col_info[pr.y];
+        int bodyA = cA.x, bodyB = cB.x;
+        int4 iA = w.info[bodyA], iB = w.info[bodyB];
+        bool simA = (iA.y & BODY_DYN) && !(iA.y & BODY_KIN), simB = (iB.y & BODY_DYN) && !(iB.y & BODY_KIN);
+        Q4 qA = ld4(w.quat[bodyA]), qB = ld4(w.quat[bodyB]);
+        V3 com0 = {0, 0, 0}, v0 = {0, 0, 0}, w0 = {0, 0, 0}, com1 = {0, 0, 0}, v1 = {0, 0, 0}, w1 = {0, 0, 0};
+        if (simA) { com0 = ld3(w.pos[bodyA]) + qrot(qA, ld3(w.com[iA.z])); v0 = ld3(w.vel[iA.z]); w0 = ld3(w.ang[iA.z]); }
+        if (simB) { com1 = ld3(w.pos[bodyB]) + qrot(qB, ld3(w.com[iB.z])); v1 = ld3(w.vel[iB.z]); w1 = ld3(w.ang[iB.z]); }
+        float4 mA = w.col_mat[pr.x], mB = w.col_mat[pr.y];
+        float friction = (mA.x + mB.x) * 0.5f;
+        bool soft;
+        float freq = 0, damp = 0, rest = 0;
+        if (mA.z || mB.z) {
+            soft = true;
+            if (mA.z && mB.z) { freq = fminG(mA.y, mB.y); damp = fminG(mA.z, mB.z); }
+            else if (mA.z) { freq = mA.y; damp = mA.z; }
+            else { freq = mB.y; damp = mB.z; }
+        } else {
+            soft = false;
+            rest = (mA.y + mB.y) * 0.5f;
+        }
+        Q4 iqA = qinverse(qA), iqB = qinverse(qB);
+        bool tri = f.pair_cat[p] == 2;
+        for (int k = 0; k < cnt; ++k) {
+            int idx = off + k;
+            if (idx >= f.man_cap) { atomicOr(w.err, ERR_MANIFOLD_CAPACITY); break; }
+            const Manifold& m = tri ? f.man_tri[f.pair_tslot[p] * kTriManifolds + k] : f.man_pair[p];
+            Contact c;
+            c.b0 = simA ? iA.z : -1;
+            c.b1 = simB ? iB.z : -1;
+            c.body0 = bodyA; c.body1 = bodyB;
+            V3 n = ld3(m.n);
+            c.n = st4(n, friction);
+            c.frequency = freq; c.damping = damp;
+            c.np = m.np; c.soft = soft ? 1 : 0;
+            c.color = -1; c.scene = iA.w; c.pair = p; c.tri = m.tri;
+            unsigned long long key = cache_key(pr.x, pr.y, m.tri);
+            // previous frame's entry, if any
+            const CacheEntry* pe = nullptr;
+            for (unsigned h = cache_hash(key) & mask, probe = 0; probe < (unsigned)f.cache_cap; ++probe, h = (h + 1) & mask) {
+                unsigned long long kk = prev[h].key;
+                if (kk == key) { pe = &prev[h]; break; }
+                if (kk == kEmpty) break;
+            }
+            CacheEntry ne;
+            ne.key = key; ne.np = m.np;
+            for (int q = 0; q < m.np; ++q) {
+                V3 r0 = ld3(m.p0[q]) - com0;
+                V3 r1 = ld3(m.p1[q]) - com1;
+                V3 rel = v1 + cross(w1, r1) - v0 - cross(w0, r0);
+                float relN = dot(rel, n);
+                r0 = qrot(iqA, r0);
+                r1 = qrot(iqB, r1);
+                float tv = 0;
+                bool found = false;
+                if (pe) {
+                    for (int i = 0; i < pe->np; ++i) {
+                        float4 e = pe->r0tv[i];
+                        if ((double)distance(r0, ld3(e)) < 0.1) { found = true; tv = e.w; break; }
+                    }
+                }
+                if (!found) tv = -rest * relN;
+                ne.r0tv[q] = st4(r0, tv);
+                ContactPt& cp = c.p[q];
+                cp.r0 = st4(r0, tv);
+                cp.r1 = st4(r1, 0.f);
+            }
+            // insert into this frame's table
+            bool placed = false;
+            for (unsigned h = cache_hash(key) & mask, probe = 0; probe < (unsigned)f.cache_cap; ++probe, h = (h + 1) & mask) {
+                unsigned long long old = atomicCAS(&cur[h].key, kEmpty, key);
+                if (old == kEmpty || old == key) {
+                    cur[h].np = ne.np;
+                    for (int q = 0; q < ne.np; ++q) cur[h].r0tv[q] = ne.r0tv[q];
+                    placed = true;
+                    break;
+                }
+            }
+            if (!placed) atomicOr(w.err, ERR_CACHE_CAPACITY);
+            f.contacts[idx] = c;
+            atomicAdd(&f.man_scene_cnt[iA.w], 1);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- joints
+
+// getSolverDesc of each joint type (src/Joints/*.cpp): row flags in creation order,
+// evaluated at frame start; the prismatic limit row exists only while violated.
+__global__ void k_joint_layout(World w) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= w.n_joints) return;
+    JointDev J = w.joints[j];
+    int f[kMaxRowsPerJoint];
+    int n = 0;
+    auto add = [&](int fl, int cnt) { for (int i = 0; i < cnt; ++i) f[n++] = fl; };
+    enum { RN = 0, RS = 1, RA = 2, RL = 4 };
+    switch (J.type) {
+        case 0: add(RN, 3); add(RA, 3); break;                                        // fixed
+        case 1: add(RN, 3); add(RA, 2); if (J.params[0] != 0.f) add(RA | RL, 1); break;  // revolute
+        case 2: add(RN, 3); break;                                                    // spherical
+        case 3: {                                                                     // prismatic
+            V3 p0 = ld3(w.pos[J.body0]) + qrot(ld4(w.quat[J.body0]), ld3(J.a0p));
+            V3 p1 = ld3(w.pos[J.body1]) + qrot(ld4(w.quat[J.body1]), ld3(J.a1p));
+            V3 d = p1 - p0;
+            V3 u00 = qrot(qmul(ld4(w.quat[J.body0]), ld4(J.a0q)), {1, 0, 0});
+            float dx = dot(d, u00);
+            add(RN, 2); add(RA, 3);
+            if (dx > J.params[0]) { J.makeUpper = 1; J.makeLower = 0; add(RL, 1); }
+            else if (dx < J.params[1]) { J.makeUpper = 0; J.makeLower = 1; add(RL, 1); }
+            else { J.makeUpper = 0; J.makeLower = 0; }
+            if (J.params[2] != 0.f) add(RS, 1);
+            break;
+        }
+        case 4: add(RN, 3); add(RA, 1); break;                                        // universal
+        case 5: add(RA, 1); break;                                                    // gear
+        default: add(RN, 3); add(RA, 2); add(RA | RS, 1); break;                      // servo
+    }
+    J.nrows = n;
+    for (int i = 0; i < kMaxRowsPerJoint; ++i) J.rowflags[i] = i < n ? f[i] : -1;
+    w.joints[j].makeUpper = J.makeUpper;
+    w.joints[j].makeLower = J.makeLower;
+    w.joints[j].nrows = n;
+    for (int i = 0; i < kMaxRowsPerJoint; ++i) w.joints[j].rowflags[i] = J.rowflags[i];
+    for (int i = 0; i < n; ++i) {
+        Row r;
+        r.linear = make_float4(0, 0, 0, 0);
+        r.angular0 = make_float4(0, 0, 0, 0);
+        r.angular1 = make_float4(0, 0, 0, -FLT_MAX);
+        r.linear0t = make_float4(0, 0, 0, FLT_MAX);
+        r.linear1t = make_float4(0, 0, 0, 0);
+        r.angular0t = make_float4(0, 0, 0, 0);
+        r.angular1t = make_float4(0, 0, 0, 0);
+        r.totalLambda = 0;
+        r.flags = f[i]; r.b0 = J.b0; r.b1 = J.b1;
+        w.rows[j * kMaxRowsPerJoint + i] = r;
+    }
+}
+
+void launch_joint_layout(const World& w, cudaStream_t s) {
+    if (w.n_joints) k_joint_layout<<<(w.n_joints + 127) / 128, 128, 0, s>>>(w);
+}
+
+__device__ __forceinline__ float angleDiffD(float a0, float a1) {  // GearJoint.cpp:5-8
+    const float pi = kPi, two_pi = 6.28318530717958647692f;
+    float diff = fmodf(a1 - a0 + pi, two_pi) - pi;
+    return diff < -pi ? diff + two_pi : diff;
+}
+
+// makeConstraints of each joint type (src/Joints/*.cpp, src/JointsUtil.h:8-28), rows in creation order
+__device__ void make_joint_rows(const World& w, int j) {
+    JointDev& J = w.joints[j];
+    Q4 q0 = ld4(w.quat[J.body0]), q1 = ld4(w.quat[J.body1]);
+    M3 u0 = mat3_cast(qmul(q0, ld4(J.a0q))), u1 = mat3_cast(qmul(q1, ld4(J.a1q)));
+    V3 r0 = qrot(q0, ld3(J.r0)), r1 = qrot(q1, ld3(J.r1));
+    V3 p0 = ld3(w.pos[J.body0]) + qrot(q0, ld3(J.a0p)), p1 = ld3(w.pos[J.body1]) + qrot(q1, ld3(J.a1p));
+    Row* R = w.rows + j * kMaxRowsPerJoint;
+    int k = 0;
+    auto lin = [&](V3 l, V3 a0, V3 a1, float c) {
+        R[k].linear = st4(l, R[k].linear.w); R[k].angular0 = st4(a0, c); R[k].angular1 = st4(a1, R[k].angular1.w); ++k;
+    };
+    auto ang = [&](V3 a, float c) {
+        R[k].angular0 = st4(a, c); R[k].angular1 = st4(a, R[k].angular1.w); ++k;
+    };
+    auto p2p = [&]() {
+        V3 d = p1 - p0;
+        lin({1, 0, 0}, {0, r0.z, -r0.y}, {0, r1.z, -r1.y}, d.x);
+        lin({0, 1, 0}, {-r0.z, 0, r0.x}, {-r1.z, 0, r1.x}, d.y);
+        lin({0, 0, 1}, {r0.y, -r0.x, 0}, {r1.y, -r1.x, 0}, d.z);
+    };
+    switch (J.type) {
+        case 0:
+            p2p();
+            ang(cross(u1.c[1], u0.c[0]), dot(u0.c[0], u1.c[1]));
+            ang(cross(u1.c[2], u0.c[0]), dot(u0.c[0], u1.c[2]));
+            ang(cross(u1.c[2], u0.c[1]), dot(u0.c[1], u1.c[2]));
+            break;
+        case 2: p2p(); break;
+        case 4:
+            p2p();
+            ang(cross(u1.c[2], u0.c[2]), dot(u0.c[2], u1.c[2]));
+            break;
+        case 1:
+            p2p();
+            ang(cross(u1.c[1], u0.c[0]), dot(u0.c[0], u1.c[1]));
+            ang(cross(u1.c[2], u0.c[0]), dot(u0.c[0], u1.c[2]));
+            if (J.params[0] != 0.f) {
+                R[k].angular0 = st4(u0.c[0], R[k].angular0.w);
+                R[k].angular1 = st4(u0.c[0], -J.params[2]);
+                R[k].linear.w = J.params[1];
+                R[k].linear0t.w = J.params[2];
+                ++k;
+            }
+            break;
+        case 6: {
+            p2p();
+            ang(cross(u1.c[1], u0.c[0]), dot(u0.c[0], u1.c[1]));
+            ang(cross(u1.c[2], u0.c[0]), dot(u0.c[0], u1.c[2]));
+            float a = acosf(clampG(dot(u0.c[2], u1.c[2]), -1.f, 1.f));
+            if (dot(u0.c[0], cross(u0.c[2], u1.c[2])) < 0.f) a = -a;
+            R[k].angular0 = st4(u0.c[0], a - J.params[0]);
+            R[k].angular1 = st4(u0.c[0], R[k].angular1.w);
+            R[k].linear1t.w = J.params[1];
+            R[k].angular0t.w = J.params[2];
+            ++k;
+            break;
+        }
+        case 3: {
+            V3 d = p1 - p0;
+            lin(u0.c[1], cross(r0, u0.c[1]), cross(r1, u0.c[1]), dot(d, u0.c[1]));
+            lin(u0.c[2], cross(r0, u0.c[2]), cross(r1, u0.c[2]), dot(d, u0.c[2]));
+            ang(cross(u1.c[1], u0.c[0]), dot(u0.c[0], u1.c[1]));
+            ang(cross(u1.c[2], u0.c[0]), dot(u0.c[0], u1.c[2]));
+            ang(cross(u1.c[2], u0.c[1]), dot(u0.c[1], u1.c[2]));
+            float dx = dot(d, u0.c[0]);
+            V3 r0xx = cross(r0, u0.c[0]), r1xx = cross(r1, u0.c[0]);
+            if (J.makeUpper) {
+                R[k].angular1.w = 0.f;  // min = 0
+                lin(u0.c[0], r0xx, r1xx, dx - J.params[0]);
+            } else if (J.makeLower) {
+                R[k].linear0t.w = 0.f;  // max = 0
+                lin(u0.c[0], r0xx, r1xx, dx - J.params[1]);
+            }
+            if (J.params[2] != 0.f) {
+                R[k].linear1t.w = J.params[4];
+                R[k].angular0t.w = J.params[5];
+                lin(u0.c[0], r0xx, r1xx, dx - J.params[3]);
+            }
+            break;
+        }
+        default: {  // gear (GearJoint.cpp:10-50)
+            float a0, a1;
+            {
+                V3 p1p = p1 + dot(p0 - p1, u0.c[0]) * u0.c[0];
+                V3 dir = normalize(p0 - p1p);
+                V3 n = cross(u0.c[0], dir);
+                M3 t = mm(transpose(m3cols(u0.c[0], -n, dir)), u0);
+                a0 = atan2f(at(t.c[1], 2), at(t.c[2], 2));
+            }
+            {
+                V3 p0p = p0 + dot(p1 - p0, u1.c[0]) * u1.c[0];
+                V3 dir = normalize(p0p - p1);
+                V3 n = cross(u1.c[0], dir);
+                M3 t = mm(transpose(u1), m3cols(u1.c[0], -n, dir));
+                a1 = atan2f(at(t.c[1], 2), at(t.c[2], 2));
+            }
+            if (!J.gearInit) { J.persistent0 = a0; J.persistent1 = a1; J.gearInit = 1; }
+            J.virtual0 += angleDiffD(a0, J.persistent0);
+            J.virtual1 += angleDiffD(a1, J.persistent1);
+            J.persistent0 = a0; J.persistent1 = a1;
+            float ratio = J.params[0];
+            R[k].angular0 = st4(u0.c[0] * ratio, J.virtual0 * ratio - J.virtual1);
+            R[k].angular1 = st4(-u1.c[0], R[k].angular1.w);
+            ++k;
+            break;
+        }
+    }
+}
+
+// Constraint1D(W)::preSolve for one row (Constraint1D.cpp:5-52 / Constraint1DW.cpp:5-115)
+__device__ void row_presolve(const World& w, Row& r, bool simd) {
+    int fl = r.flags;
+    bool angf = fl & 2, soft = fl & 1, lim = fl & 4;
+    float im0 = 0, im1 = 0;
+    M3 I0 = m3zero(), I1 = m3zero();
+    if (r.b0 >= 0) { im0 = w.com[r.b0].w; I0 = m3cols(ld3(w.mt[3 * r.b0]), ld3(w.mt[3 * r.b0 + 1]), ld3(w.mt[3 * r.b0 + 2])); }
+    if (r.b1 >= 0) { im1 = w.com[r.b1].w; I1 = m3cols(ld3(w.mt[3 * r.b1]), ld3(w.mt[3 * r.b1 + 1]), ld3(w.mt[3 * r.b1 + 2])); }
+    V3 a0 = ld3(r.angular0), a1 = ld3(r.angular1), l = ld3(r.linear);
+    V3 a0t = mv(I0, a0), a1t = mv(I1, a1);
+    float inv = dot(a0, a0t) + dot(a1, a1t);
+    V3 l0t = ld3(r.linear0t), l1t = ld3(r.linear1t);
+    if (!angf) {
+        inv += dot(l, l) * (im0 + im1);
+        l0t = im0 * l;
+        l1t = im1 * l;
+    }
+    r.angular0t = st4(a0t, r.angular0t.w);
+    r.angular1t = st4(a1t, inv);
+    r.linear0t = st4(l0t, r.linear0t.w);
+    r.linear1t = st4(l1t, r.linear1t.w);
+    if (soft) return;
+    float c = r.angular0.w, mn = r.angular1.w, mx = r.linear0t.w;
+    float lambda;
+    if (!simd) {
+        if (!c || !inv) return;
+        lambda = c / inv;
+        if (lim) lambda = clampG(lambda, mn, mx);
+    } else {
+        if (!(inv != 0.f && c != 0.f)) return;
+        lambda = c / inv;
+        if (lim) { lambda = lambda > mn ? lambda : mn; lambda = lambda < mx ? lambda : mx; }
+    }
+    if (r.b0 >= 0) {
+        float4 pv = w.pv_v[r.b0], pw = w.pv_w[r.b0];
+        V3 v = ld3(pv), wv = ld3(pw);
+        if (!angf) v += lambda * l0t;
+        wv += lambda * a0t;
+        w.pv_v[r.b0] = st4(v, pv.w + 1.f);
+        w.pv_w[r.b0] = st4(wv, 0.f);
+    }
+    if (r.b1 >= 0) {
+        float4 pv = w.pv_v[r.b1], pw = w.pv_w[r.b1];
+        V3 v = ld3(pv), wv = ld3(pw);
+        if (!angf) v -= lambda * l1t;
+        wv -= lambda * a1t;
+        w.pv_v[r.b1] = st4(v, pv.w + 1.f);
+        w.pv_w[r.b1] = st4(wv, 0.f);
+    }
+}
+
+// Constraint1D(W)::solve for one row (Constraint1D.cpp:54-127 / Constraint1DW.cpp:117-233)
+__device__ void row_solve(const World& w, Row& r, float h, bool warm, bool simd) {
+    int fl = r.flags;
+    bool angf = fl & 2, soft = fl & 1, lim = fl & 4;
+    float inv = r.angular1t.w;
+    if (!simd && !inv) return;
+    V3 v0 = {0, 0, 0}, w0 = {0, 0, 0}, v1 = {0, 0, 0}, w1 = {0, 0, 0};
+    if (r.b0 >= 0) { if (!angf) v0 = ld3(w.vt_v[r.b0]); w0 = ld3(w.vt_w[r.b0]); }
+    if (r.b1 >= 0) { if (!angf) v1 = ld3(w.vt_v[r.b1]); w1 = ld3(w.vt_w[r.b1]); }
+    V3 l0t = ld3(r.linear0t), l1t = ld3(r.linear1t), a0t = ld3(r.angular0t), a1t = ld3(r.angular1t);
+    float c = r.angular0.w;
+    if (!soft && warm) {
+        bool apply = simd ? (fabsf(c) < (float)1e-4 && fabsf(r.totalLambda) < 10000.f)
+                          : !((double)fabsf(c) > 1e-4 || fabsf(r.totalLambda) > 10000.f);
+        if (apply) {
+            float lw = r.totalLambda * 0.5f;
+            r.totalLambda = lw;
+            if (!angf) { v0 += lw * l0t; v1 -= lw * l1t; }
+            w0 += lw * a0t;
+            w1 -= lw * a1t;
+        }
+    }
+    if (simd && !inv) return;
+    V3 a0 = ld3(r.angular0), a1 = ld3(r.angular1), l = ld3(r.linear);
+    float rv = dot(a1, w1) - dot(a0, w0);
+    if (!angf) rv += dot(l, v1) - dot(l, v0);
+    float tvel = r.linear.w, mn = r.angular1.w, mx = r.linear0t.w, freq = r.linear1t.w, damp = r.angular0t.w;
+    float lambda;
+    if (simd) {
+        float eff = 1.f / inv;
+        if (soft) {
+            float af = (2.f * kPi) * freq;
+            float stiffness = af * af * eff;
+            float damping = 2.f * af * damp * eff;
+            float gamma = 1.f / (damping + h * stiffness);
+            float beta = h * stiffness * gamma;
+            lambda = (rv + beta * c / h) / (inv + gamma / h);
+        } else {
+            float bias = (float)(0.2 / (double)h);
+            lambda = (rv - tvel + bias * c) * eff;
+        }
+    } else {
+        if (soft) {
+            float af = 2.f * kPi * freq;
+            float stiffness = af * af / inv;
+            float damping = 2.f * af * damp / inv;
+            float gamma = 1.f / (damping + h * stiffness);
+            float beta = h * stiffness / (damping + h * stiffness);
+            lambda = (rv + beta * c / h) / (inv + gamma / h);
+        } else {
+            lambda = (rv - tvel + 0.2f * c / h) / inv;
+        }
+    }
+    if (lim) {
+        float prev = r.totalLambda;
+        r.totalLambda += lambda;
+        if (simd) {
+            float lo = mn * h, hi = mx * h;
+            r.totalLambda = r.totalLambda > lo ? r.totalLambda : lo;
+            r.totalLambda = r.totalLambda < hi ? r.totalLambda : hi;
+        } else {
+            r.totalLambda = clampG(r.totalLambda, mn, mx);
+        }
+        lambda = r.totalLambda - prev;
+    } else {
+        r.totalLambda += lambda;
+    }
+    if (!simd) {
+        // the scalar row applies only this iteration's impulse (Constraint1D.cpp:158-168)
+        if (r.b0 >= 0) {
+            if (!angf) w.vt_v[r.b0] = st4(ld3(w.vt_v[r.b0]) + lambda * l0t);
+            w.vt_w[r.b0] = st4(ld3(w.vt_w[r.b0]) + lambda * a0t);
+        }
+        if (r.b1 >= 0) {
+            if (!angf) w.vt_v[r.b1] = st4(ld3(w.vt_v[r.b1]) - lambda * l1t);
+            w.vt_w[r.b1] = st4(ld3(w.vt_w[r.b1]) - lambda * a1t);
+        }
+        return;
+    }
+    if (!angf) { v0 += lambda * l0t; v1 -= lambda * l1t; }
+    w0 += lambda * a0t;
+    w1 -= lambda * a1t;
+    if (r.b0 >= 0) { if (!angf) w.vt_v[r.b0] = st4(v0); w.vt_w[r.b0] = st4(w0); }
+    if (r.b1 >= 0) { if (!angf) w.vt_v[r.b1] = st4(v1); w.vt_w[r.b1] = st4(w1); }
+}
+
+__constant__ int c_flag_order[6] = {0, 2, 1, 4, 3, 6};
+
+__device__ void joint_presolve(const World& w, int j) {
+    JointDev& J = w.joints[j];
+    Row* R = w.rows + j * kMaxRowsPerJoint;
+    for (int fi = 0; fi < 6; ++fi)
+        for (int k = 0; k < J.nrows; ++k)
+            if (J.rowflags[k] == c_flag_order[fi]) row_presolve(w, R[k], J.simd != 0);
+}
+
+__device__ void joint_solve(const World& w, int j, float h, bool warm) {
+    JointDev& J = w.joints[j];
+    Row* R = w.rows + j * kMaxRowsPerJoint;
+    for (int fi = 0; fi < 6; ++fi)
+        for (int k = 0; k < J.nrows; ++k)
+            if (J.rowflags[k] == c_flag_order[fi]) row_solve(w, R[k], h, warm, J.simd != 0);
+}
+
+// ---------------------------------------------------------------- contacts (ContactConstraints.cpp)
+
+__device__ __forceinline__ M3 world_invI(const World& w, int d) {
+    return m3cols(ld3(w.mt[3 * d]), ld3(w.mt[3 * d + 1]), ld3(w.mt[3 * d + 2]));
+}
+
+// update contact rows (src/Physecs.cpp:366-427)
+__device__ void contact_update(const World& w, Contact& c) {
+    int4 i0 = w.info[c.body0], i1 = w.info[c.body1];
+    Q4 q0 = ld4(w.quat[c.body0]), q1 = ld4(w.quat[c.body1]);
+    V3 com0 = {0, 0, 0}, v0 = {0, 0, 0}, w0 = {0, 0, 0}, com1 = {0, 0, 0}, v1 = {0, 0, 0}, w1 = {0, 0, 0};
+    if (c.b0 >= 0) { com0 = ld3(w.pos[c.body0]) + qrot(q0, ld3(w.com[i0.z])); v0 = ld3(w.vel[i0.z]); w0 = ld3(w.ang[i0.z]); }
+    if (c.b1 >= 0) { com1 = ld3(w.pos[c.body1]) + qrot(q1, ld3(w.com[i1.z])); v1 = ld3(w.vel[i1.z]); w1 = ld3(w.ang[i1.z]); }
+    V3 n = ld3(c.n);
+    for (int k = 0; k < c.np; ++k) {
+        ContactPt& p = c.p[k];
+        V3 r0 = qrot(q0, ld3(p.r0)), r1 = qrot(q1, ld3(p.r1));
+        V3 cp0 = com0 + r0, cp1 = com1 + r1;
+        float cn = dot(cp1 - cp0, n);
+        V3 r0xn = cross(r0, n), r1xn = cross(r1, n);
+        V3 rel = v1 + cross(w1, r1) - v0 - cross(w0, r0);
+        float relN = dot(rel, n);
+        V3 t = rel - relN * n;
+        float tl = length(t);
+        if (tl) t = t / tl;
+        p.r1.w = cn;
+        p.r0xn = st4(r0xn, 0.f);      // lambdaN = 0
+        p.r1xn = st4(r1xn, 0.f);      // lambdaT = 0
+        p.t = st4(t, p.t.w);
+        p.r0xt = st4(cross(r0, t), p.r0xt.w);
+        p.r1xt = st4(cross(r1, t), 0.f);
+    }
+}
+
+__device__ void contact_presolve(const World& w, Contact& c) {
+    float im0 = 0, im1 = 0;
+    M3 I0 = m3zero(), I1 = m3zero();
+    if (c.b0 >= 0) { im0 = w.com[c.b0].w; I0 = world_invI(w, c.b0); }
+    if (c.b1 >= 0) { im1 = w.com[c.b1].w; I1 = world_invI(w, c.b1); }
+    V3 n = ld3(c.n);
+    for (int k = 0; k < c.np; ++k) {
+        ContactPt& p = c.p[k];
+        V3 r0xn = ld3(p.r0xn), r1xn = ld3(p.r1xn), r0xt = ld3(p.r0xt), r1xt = ld3(p.r1xt), t = ld3(p.t);
+        V3 r0xnt = mv(I0, r0xn), r1xnt = mv(I1, r1xn), r0xtt = mv(I0, r0xt), r1xtt = mv(I1, r1xt);
+        p.r0xnt = st4(r0xnt); p.r1xnt = st4(r1xnt); p.r0xtt = st4(r0xtt); p.r1xtt = st4(r1xtt);
+        p.t.w = dot(n, n) * (im0 + im1) + dot(r0xn, r0xnt) + dot(r1xn, r1xnt);
+        p.r0xt.w = dot(t, t) * (im0 + im1) + dot(r0xt, r0xtt) + dot(r1xt, r1xtt);
+    }
+}
+
+__device__ void contact_solve(const World& w, Contact& c, bool useBias, float h) {
+    V3 n = ld3(c.n);
+    float friction = c.n.w;
+    float im0 = c.b0 >= 0 ? w.com[c.b0].w : 0.f, im1 = c.b1 >= 0 ? w.com[c.b1].w : 0.f;
+    for (int i = 0; i < c.np; ++i) {
+        ContactPt& p = c.p[i];
+        float invN = p.t.w;
+        if (!invN) continue;
+        V3 v0 = {0, 0, 0}, w0 = {0, 0, 0}, v1 = {0, 0, 0}, w1 = {0, 0, 0};
+        if (c.b0 >= 0) { v0 = ld3(w.vt_v[c.b0]); w0 = ld3(w.vt_w[c.b0]); }
+        if (c.b1 >= 0) { v1 = ld3(w.vt_v[c.b1]); w1 = ld3(w.vt_w[c.b1]); }
+        V3 r0xn = ld3(p.r0xn), r1xn = ld3(p.r1xn);
+        float rv = dot(-n, v0) + dot(-r0xn, w0) + dot(n, v1) + dot(r1xn, w1);
+        float eff = 1.f / invN;
+        float lambda;
+        float cc = p.r1.w;
+        if (c.soft) {
+            float af = 2.f * kPi * c.frequency;
+            float stiffness = af * af * eff;
+            float damping = 2.f * af * c.damping * eff;
+            float gamma = 1.f / (damping + h * stiffness);
+            float beta = h * stiffness / (damping + h * stiffness);
+            lambda = (rv + beta * cc / h) / (invN + gamma / h);
+        } else {
+            lambda = (rv - p.r0.w + (useBias ? 0.1f * cc / h : 0.f)) * eff;
+        }
+        float prev = p.r0xn.w;
+        float tot = prev + lambda;
+        tot = fminG(tot, 0.f);
+        p.r0xn.w = tot;
+        lambda = tot - prev;
+        if (c.b0 >= 0) {
+            w.vt_v[c.b0] = st4(v0 + lambda * im0 * n);
+            w.vt_w[c.b0] = st4(w0 + lambda * ld3(p.r0xnt));
+        }
+        if (c.b1 >= 0) {
+            w.vt_v[c.b1] = st4(v1 - lambda * im1 * n);
+            w.vt_w[c.b1] = st4(w1 - lambda * ld3(p.r1xnt));
+        }
+    }
+    // friction reads the component velocities (ContactConstraints.cpp:93-101)
+    for (int i = 0; i < c.np; ++i) {
+        ContactPt& p = c.p[i];
+        float invT = p.r0xt.w;
+        if (!invT) continue;
+        V3 v0 = {0, 0, 0}, w0 = {0, 0, 0}, v1 = {0, 0, 0}, w1 = {0, 0, 0};
+        if (c.b0 >= 0) { v0 = ld3(w.vel[c.b0]); w0 = ld3(w.ang[c.b0]); }
+        if (c.b1 >= 0) { v1 = ld3(w.vel[c.b1]); w1 = ld3(w.ang[c.b1]); }
+        V3 t = ld3(p.t), r0xt = ld3(p.r0xt), r1xt = ld3(p.r1xt);
+        float rv = dot(-t, v0) + dot(-r0xt, w0) + dot(t, v1) + dot(r1xt, w1);
+        float lambda = rv / invT;
+        float limit = friction * p.r0xn.w;
+        float prev = p.r1xn.w;
+        float tot = prev + lambda;
+        tot = clampG(tot, limit, -limit);
+        p.r1xn.w = tot;
+        lambda = tot - prev;
+        if (c.b0 >= 0) {
+            w.vt_v[c.b0] = st4(ld3(w.vt_v[c.b0]) + lambda * im0 * t);
+            w.vt_w[c.b0] = st4(ld3(w.vt_w[c.b0]) + lambda * ld3(p.r0xtt));
+        }
+        if (c.b1 >= 0) {
+            w.vt_v[c.b1] = st4(ld3(w.vt_v[c.b1]) - lambda * im1 * t);
+            w.vt_w[c.b1] = st4(ld3(w.vt_w[c.b1]) - lambda * ld3(p.r1xtt));
+        }
+    }
+}
+
+// ---------------------------------------------------------------- bodies
+
+// integrate velocities (src/Physecs.cpp:441-469)
+__device__ void integrate_velocity(const World& w, int d, float h, float g) {
+    int b = w.dyn_body[d];
+    if (w.info[b].y & BODY_KIN) return;
+    M3 rot = mat3_cast(ld4(w.quat[b]));
+    M3 invRot = transpose(rot);
+    V3 vel = ld3(w.vel[d]) + h * V3{0, -g, 0};
+    V3 ang = ld3(w.ang[d]);
+    V3 wl = mv(invRot, ang);
+    M3 invIl = m3cols(ld3(w.invI[3 * d]), ld3(w.invI[3 * d + 1]), ld3(w.invI[3 * d + 2]));
+    M3 I = inverse(invIl);
+    V3 f = h * cross(wl, mv(I, wl));
+    M3 J = madd(I, mscale(h, msub(mm(matrixCross3(wl), I), matrixCross3(mv(I, wl)))));
+    wl = wl - solve33(J, f);
+    ang = mv(rot, wl);
+    w.vel[d] = st4(vel);
+    w.ang[d] = st4(ang);
+    w.vt_v[d] = st4(vel);
+    w.vt_w[d] = st4(ang);
+    w.pv_v[d] = make_float4(0, 0, 0, 0);
+    w.pv_w[d] = make_float4(0, 0, 0, 0);
+    M3 wi = mm(mm(rot, invIl), invRot);
+    w.mt[3 * d] = st4(wi.c[0]);
+    w.mt[3 * d + 1] = st4(wi.c[1]);
+    w.mt[3 * d + 2] = st4(wi.c[2]);
+}
+
+// integrate positions (src/Physecs.cpp:492-512)
+__device__ void integrate_position(const World& w, int d, float h) {
+    int b = w.dyn_body[d];
+    if (w.info[b].y & BODY_KIN) return;
+    float4 pv = w.pv_v[d];
+    float s = pv.w != 0.f ? 1.f / pv.w : 1.f;
+    V3 pos = ld3(w.pos[b]);
+    Q4 q = ld4(w.quat[b]);
+    V3 com = ld3(w.com[d]);
+    pos += h * ld3(w.vt_v[d]) + s * ld3(pv);
+    V3 prevCom = qrot(q, com);
+    V3 wv = 0.5f * (h * ld3(w.vt_w[d]) + s * ld3(w.pv_w[d]));
+    q = qadd(q, qmul(Q4{wv.x, wv.y, wv.z, 0.f}, q));
+    q = qnormalize(q);
+    pos += prevCom - qrot(q, com);
+    w.pos[b] = st4(pos);
+    w.quat[b] = st4(q);
+}
+
+// ---------------------------------------------------------------- frame kernel
+
+struct BlockSync {
+    __device__ __forceinline__ void sync() const { __syncthreads(); }
+    __device__ __forceinline__ int tid() const { return threadIdx.x; }
+    __device__ __forceinline__ int nth() const { return blockDim.x; }
+    __device__ __forceinline__ bool any(bool v) const { return __syncthreads_or(v) != 0; }
+};
+struct GridSync {
+    GridBarrier bar;
+    int* flag;
+    __device__ __forceinline__ void sync() const { bar.sync(); }
+    __device__ __forceinline__ int tid() const { return blockIdx.x * blockDim.x + threadIdx.x; }
+    __device__ __forceinline__ int nth() const { return gridDim.x * blockDim.x; }
+    __device__ __forceinline__ bool any(bool v) const {
+        if (threadIdx.x == 0 && blockIdx.x == 0) atomicExch(flag, 0);
+        bar.sync();
+        if (__syncthreads_or(v) && threadIdx.x == 0) atomicOr(flag, 1);
+        bar.sync();
+        bool r = *(volatile int*)flag != 0;
+        bar.sync();
+        return r;
+    }
+};
+
+template <class S>
+__device__ void solve_scene(const World& w, FrameBuf& f, int s, const S& sy) {
+    const int tid = sy.tid(), nth = sy.nth();
+    int ds = w.scene_dyn[s], de = w.scene_dyn[s + 1];
+    int ms = f.scene_man[s], me = f.scene_man[s + 1];
+    float4 kn = w.knobs[s];
+    int substeps = (int)kn.x, iterations = (int)kn.y;
+    float g = kn.z, dt = kn.w;
+    int* colstart = f.color_start + s * (kMaxColors + 1);
+    // ---- graph colouring of the contacts: rounds of body claims, lowest index wins
+    for (int d = ds + tid; d < de; d += nth) f.claim[d] = 0x7fffffff;
+    for (int m = ms + tid; m < me; m += nth) f.color_of[m] = -1;
+    sy.sync();
+    int ncol = 0;
+    for (;;) {
+        for (int m = ms + tid; m < me; m += nth) {
+            if (f.color_of[m] >= 0) continue;
+            const Contact& c = f.contacts[m];
+            if (c.b0 >= 0) atomicMin(&f.claim[c.b0], m);
+            if (c.b1 >= 0) atomicMin(&f.claim[c.b1], m);
+        }
+        sy.sync();
+        bool left = false;
+        for (int m = ms + tid; m < me; m += nth) {
+            if (f.color_of[m] >= 0) continue;
+            const Contact& c = f.contacts[m];
+            bool ok = (c.b0 < 0 || f.claim[c.b0] == m) && (c.b1 < 0 || f.claim[c.b1] == m);
+            if (ok && ncol < kMaxColors) f.color_of[m] = ncol;
+            else left = true;
+        }
+        bool any = sy.any(left);
+        for (int d = ds + tid; d < de; d += nth) f.claim[d] = 0x7fffffff;
+        ++ncol;
+        sy.sync();
+        if (!any) break;
+        if (ncol >= kMaxColors) { if (tid == 0) atomicOr(w.err, ERR_COLOR_CAPACITY); break; }
+    }
+    // counting sort of the scene's contacts by colour
+    for (int k = tid; k <= kMaxColors; k += nth) colstart[k] = 0;
+    sy.sync();
+    for (int m = ms + tid; m < me; m += nth) { int cl = f.color_of[m]; if (cl >= 0) atomicAdd(&colstart[cl + 1], 1); }
+    sy.sync();
+    if (tid == 0) {
+        for (int k = 0; k < kMaxColors; ++k) colstart[k + 1] += colstart[k];
+        f.scene_ncolor[s] = ncol;
+    }
+    sy.sync();
+    for (int m = ms + tid; m < me; m += nth) {
+        int cl = f.color_of[m];
+        if (cl < 0) continue;
+        // position within the colour: count of lower-index contacts of the same colour is not needed,
+        // contacts of one colour touch disjoint bodies and may be solved in any order
+        int pos = atomicAdd(&f.claim_pos[s * (kMaxColors + 1) + cl], 1);
+        f.corder[ms + colstart[cl] + pos] = m;
+    }
+    sy.sync();
+    int js0 = w.scene_jsteps[s], js1 = w.scene_jsteps[s + 1];
+    int jb = w.scene_joint[s], je = w.scene_joint[s + 1];
+    float h = dt / substeps;
+    for (int sub = 0; sub < substeps; ++sub) {
+        for (int m = ms + tid; m < me; m += nth) contact_update(w, f.contacts[m]);
+        for (int j = jb + tid; j < je; j += nth) make_joint_rows(w, j);
+        sy.sync();
+        for (int d = ds + tid; d < de; d += nth) integrate_velocity(w, d, h, g);
+        sy.sync();
+        for (int m = ms + tid; m < me; m += nth) contact_presolve(w, f.contacts[m]);
+        for (int st = js0; st < js1; ++st) {
+            for (int k = w.jstep_start[st] + tid; k < w.jstep_start[st + 1]; k += nth) joint_presolve(w, w.jsched[k]);
+            sy.sync();
+        }
+        sy.sync();
+        for (int it = 0; it < iterations; ++it) {
+            for (int cl = 0; cl < ncol; ++cl) {
+                for (int k = colstart[cl] + tid; k < colstart[cl + 1]; k += nth) contact_solve(w, f.contacts[f.corder[ms + k]], true, h);
+                sy.sync();
+            }
+            for (int st = js0; st < js1; ++st) {
+                for (int k = w.jstep_start[st] + tid; k < w.jstep_start[st + 1]; k += nth) joint_solve(w, w.jsched[k], h, it == 0);
+                sy.sync();
+            }
+        }
+        for (int d = ds + tid; d < de; d += nth) integrate_position(w, d, h);
+        sy.sync();
+        for (int cl = 0; cl < ncol; ++cl) {
+            for (int k = colstart[cl] + tid; k < colstart[cl + 1]; k += nth) {
+                Contact& c = f.contacts[f.corder[ms + k]];
+                if (!c.soft) contact_solve(w, c, false, 0.f);
+            }
+            sy.sync();
+        }
+        for (int d = ds + tid; d < de; d += nth) {
+            int b = w.dyn_body[d];
+            if (w.info[b].y & BODY_KIN) continue;
+            w.vel[d] = w.vt_v[d];
+            w.ang[d] = w.vt_w[d];
+        }
+        sy.sync();
+    }
+}
+
+__global__ void __launch_bounds__(256) k_solve_block(World w, FrameBuf f, const int* scenes) {
+    BlockSync sy;
+    solve_scene(w, f, scenes[blockIdx.x], sy);
+}
+
+__global__ void __launch_bounds__(256) k_solve_grid(World w, FrameBuf f, const int* scenes, int n) {
+    GridSync sy{GridBarrier{f.bar, f.bar + 1, w.err}, (int*)(f.bar + 2)};
+    for (int i = 0; i < n; ++i) {
+        solve_scene(w, f, scenes[i], sy);
+        sy.sync();
+    }
+}
+
+__global__ void k_zero_ints(int* p, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = 0;
+}
+
+void launch_contacts(const World& w, FrameBuf& f, cudaStream_t s) {
+    k_cache_clear<<<(f.cache_cap + 255) / 256, 256, 0, s>>>(f);
+    k_zero_ints<<<(w.n_scenes + 256) / 256, 256, 0, s>>>(f.man_scene_cnt, w.n_scenes + 1);
+    k_build_contacts<<<1216, 128, 0, s>>>(w, f);
+    scan_exclusive(f.man_scene_cnt, f.scene_man, w.n_scenes + 1, nullptr, f.scan_scratch, s);
+}
+
+int solver_grid_blocks() {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_solve_grid, 256, 0);
+    if (per < 1) per = 1;
+    return sms * per;
+}
+
+void launch_solver(const World& w, FrameBuf& f, const int* block_scenes, int n_block_scenes, const int* grid_scenes,
+                   int n_grid_scenes, int grid_blocks, cudaStream_t s) {
+    k_zero_ints<<<(w.n_scenes * (kMaxColors + 1) + 255) / 256, 256, 0, s>>>(f.claim_pos, w.n_scenes * (kMaxColors + 1));
+    if (n_block_scenes) k_solve_block<<<n_block_scenes, 256, 0, s>>>(w, f, block_scenes);
+    if (n_grid_scenes) {
+        void* args[] = {(void*)&w, (void*)&f, (void*)&grid_scenes, (void*)&n_grid_scenes};
+        cudaLaunchCooperativeKernel((void*)k_solve_grid, grid_blocks, 256, args, 0, s);
+    }
+    k_cache_flip<<<1, 1, 0, s>>>(f);
+}
+
+}  // namespace psx

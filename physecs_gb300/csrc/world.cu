@@ -1,0 +1,800 @@
+// world.cu — host runtime and C ABI of the GB300 simulation hot path.
+//
+// Owns every device buffer of a world (one or many scenes), packs scene
+// descriptors into the device layout of types.cuh, reproduces the host-side
+// work the reference does when a scene is populated (triangle-mesh BVH build,
+// src/TriangleMesh.cpp:7-164; joint colouring, src/Physecs.cpp:690-710), and
+// queues one frame as a fixed sequence of kernels on the world's stream.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+#include "frame.cuh"
+#include "../../include/psx.h"
+
+using namespace psx;
+
+namespace {
+
+thread_local std::string g_err;
+
+psx_status fail(psx_status s, const std::string& msg) {
+    g_err = msg;
+    return s;
+}
+
+#define PSX_CUDA(call)                                                                     \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess) return fail(PSX_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+// ---------------------------------------------------------------- triangle-mesh BVH (host)
+// Binned SAH with six buckets, exactly as src/TriangleMesh.cpp:7-164, so that triangle
+// indices (which the BVH build permutes) match the reference's.
+
+struct HTri { uint32_t idx[3]; Bounds b; V3 normal, centroid; };
+struct HNode { Bounds b; int triCount; int index; };
+
+Bounds bunion(const Bounds& a, const Bounds& b) {
+    return {{fminG(a.min.x, b.min.x), fminG(a.min.y, b.min.y), fminG(a.min.z, b.min.z)},
+            {fmaxG(a.max.x, b.max.x), fmaxG(a.max.y, b.max.y), fmaxG(a.max.z, b.max.z)}};
+}
+float barea(const Bounds& b) {
+    V3 d = b.max - b.min;
+    return 2 * (d.x * d.y + d.y * d.z + d.z * d.x);
+}
+Bounds empty_bounds() { return {v3s(FLT_MAX), v3s(-FLT_MAX)}; }
+
+struct MeshBVH {
+    std::vector<HTri> tris;
+    std::vector<HNode> nodes;
+    static constexpr int kB = 6;
+    void node_bounds(int id) {
+        Bounds b = empty_bounds();
+        for (int i = 0; i < nodes[id].triCount; ++i) b = bunion(b, tris[nodes[id].index + i].b);
+        nodes[id].b = b;
+    }
+    bool fill(int id, int axis, Bounds* bb, int* bc) {
+        const HNode& n = nodes[id];
+        for (int i = 0; i < kB; ++i) { bb[i] = empty_bounds(); bc[i] = 0; }
+        float s = at(n.b.min, axis), e = at(n.b.max, axis), len = e - s;
+        if (!len) return false;
+        for (int i = 0; i < n.triCount; ++i) {
+            const HTri& t = tris[n.index + i];
+            int bi = std::min(kB - 1, (int)((at(t.centroid, axis) - s) / len * kB));
+            bb[bi] = bunion(bb[bi], t.b);
+            bc[bi]++;
+        }
+        return true;
+    }
+    void subdivide(int id) {
+        float best = FLT_MAX;
+        int axis = 0, split = 0, cl = 0, cr = 0;
+        Bounds L{}, R{};
+        for (int a = 0; a < 3; ++a) {
+            Bounds bb[kB];
+            int bc[kB];
+            if (!fill(id, a, bb, bc)) continue;
+            for (int sp = 1; sp < kB; ++sp) {
+                Bounds l = empty_bounds(), r = empty_bounds();
+                int nl = 0, nr = 0;
+                for (int i = 0; i < kB; ++i) {
+                    if (i < sp) { l = bunion(l, bb[i]); nl += bc[i]; }
+                    else { r = bunion(r, bb[i]); nr += bc[i]; }
+                }
+                if (!nl || !nr) continue;
+                float cost = nl * barea(l) + nr * barea(r);
+                if (cost < best) { best = cost; axis = a; split = sp; L = l; R = r; cl = nl; cr = nr; }
+            }
+        }
+        if (!(cl && cr)) return;
+        HNode n = nodes[id];
+        float s = at(n.b.min, axis), e = at(n.b.max, axis), len = e - s;
+        int i = n.index, j = i + n.triCount - 1;
+        while (i <= j) {
+            int bi = (int)((at(tris[i].centroid, axis) - s) / len * kB);
+            if (bi < split) ++i;
+            else std::swap(tris[i], tris[j--]);
+        }
+        nodes.push_back({L, cl, n.index});
+        nodes.push_back({R, cr, i});
+        nodes[id].triCount = 0;
+        nodes[id].index = (int)nodes.size() - 2;
+        int left = nodes[id].index;
+        subdivide(left);
+        subdivide(left + 1);
+    }
+    void build(const float* verts, const uint32_t* idx, int nidx) {
+        for (int k = 0; k + 2 < nidx; k += 3) {
+            HTri t;
+            t.idx[0] = idx[k]; t.idx[1] = idx[k + 1]; t.idx[2] = idx[k + 2];
+            V3 a = {verts[3 * t.idx[0]], verts[3 * t.idx[0] + 1], verts[3 * t.idx[0] + 2]};
+            V3 b = {verts[3 * t.idx[1]], verts[3 * t.idx[1] + 1], verts[3 * t.idx[1] + 2]};
+            V3 c = {verts[3 * t.idx[2]], verts[3 * t.idx[2] + 1], verts[3 * t.idx[2] + 2]};
+            t.b = {vmin(vmin(a, b), c), vmax(vmax(a, b), c)};
+            t.normal = normalize(cross(b - a, c - a));
+            t.centroid = (a + b + c) / 3.f;
+            tris.push_back(t);
+        }
+        nodes.reserve(2 * tris.size() + 1);
+        nodes.push_back({Bounds{}, (int)tris.size(), 0});
+        node_bounds(0);
+        subdivide(0);
+    }
+};
+
+float4 f4(float x, float y, float z, float w = 0.f) { return make_float4(x, y, z, w); }
+int ilog2ceil(int v) { int b = 0; while ((1 << b) < v) ++b; return b; }
+
+template <class T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+};
+
+}  // namespace
+
+struct psx_world {
+    World w{};
+    FrameBuf f{};
+    cudaStream_t stream = nullptr;
+    std::vector<void*> allocs;
+    int n_scenes = 0;
+    int mbits = 30, total_bits = 30;
+    std::vector<int> h_scene_body, h_scene_col, h_scene_dyn;
+    std::vector<uint32_t> h_entity;        // per body
+    std::vector<int> h_body_dyn;           // per body: global dyn index or -1
+    std::vector<int> h_col_local;          // per collider: index within its body
+    std::vector<int> block_scenes_h, grid_scenes_h;
+    int* block_scenes = nullptr;
+    int* grid_scenes = nullptr;
+    int grid_blocks = 0;
+    std::vector<float4> h_knobs;
+    bool use_graph = false;
+    cudaGraphExec_t graph = nullptr;
+    float graph_dt = -1.f;
+    bool knobs_dirty = true;
+    // pinned staging for body transfers
+    float4* pin = nullptr;
+    size_t pin_n = 0;
+
+    template <class T>
+    psx_status alloc(T*& p, size_t n) {
+        if (n == 0) n = 1;
+        void* q = nullptr;
+        cudaError_t e = cudaMalloc(&q, n * sizeof(T));
+        if (e != cudaSuccess) return fail(PSX_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        allocs.push_back(q);
+        p = (T*)q;
+        return PSX_OK;
+    }
+    template <class T>
+    psx_status upload(T*& p, const std::vector<T>& v) {
+        psx_status s = alloc(p, v.size());
+        if (s != PSX_OK) return s;
+        if (!v.empty()) PSX_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+        return PSX_OK;
+    }
+    ~psx_world() {
+        if (graph) cudaGraphExecDestroy(graph);
+        for (void* p : allocs) cudaFree(p);
+        if (pin) cudaFreeHost(pin);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+#define PSX_TRY(expr)                       \
+    do {                                    \
+        psx_status s_ = (expr);             \
+        if (s_ != PSX_OK) return s_;        \
+    } while (0)
+
+static psx_status validate(const psx_scene_desc& d) {
+    if (d.n_bodies <= 0) return fail(PSX_ERR_INVALID_ARG, "scene without bodies");
+    if (!d.entity || !d.flags || !d.pos || !d.quat || !d.collider_start) return fail(PSX_ERR_INVALID_ARG, "missing body arrays");
+    if (d.collider_start[0] != 0 || d.collider_start[d.n_bodies] != d.n_colliders) return fail(PSX_ERR_INVALID_ARG, "collider_start");
+    if (d.n_colliders <= 0) return fail(PSX_ERR_INVALID_ARG, "scene without colliders");
+    for (int c = 0; c < d.n_colliders; ++c) {
+        int t = d.col_type[c];
+        if (t < 0 || t > 4) return fail(PSX_ERR_INVALID_ARG, "collider type");
+        if (t == PSX_CONVEX_MESH && (d.col_mesh[c] < 0 || d.col_mesh[c] >= d.n_convex)) return fail(PSX_ERR_INVALID_ARG, "convex mesh index");
+        if (t == PSX_TRIANGLE_MESH && (d.col_mesh[c] < 0 || d.col_mesh[c] >= d.n_trimesh)) return fail(PSX_ERR_INVALID_ARG, "triangle mesh index");
+    }
+    for (int j = 0; j < d.n_joints; ++j) {
+        if (d.joint_type[j] < 0 || d.joint_type[j] > 6) return fail(PSX_ERR_INVALID_ARG, "joint type");
+        if (d.joint_body0[j] < 0 || d.joint_body0[j] >= d.n_bodies || d.joint_body1[j] < 0 || d.joint_body1[j] >= d.n_bodies)
+            return fail(PSX_ERR_INVALID_ARG, "joint body index");
+    }
+    if (d.num_substeps <= 0 || d.num_iterations < 0) return fail(PSX_ERR_INVALID_ARG, "knobs");
+    return PSX_OK;
+}
+
+static psx_status build_world(psx_world* W, const psx_scene_desc* scenes, int S, const psx_world_opts& o) {
+    W->n_scenes = S;
+    std::vector<int> scene_body{0}, scene_col{0}, scene_dyn{0}, scene_joint{0};
+    std::vector<float4> pos, quat, vel, ang, com, invI, col_pos, col_quat, col_params, col_mat;
+    std::vector<int4> info, col_info;
+    std::vector<int> dyn_body;
+    std::vector<ConvexMeshDev> convex;
+    std::vector<float4> convex_verts, face_normal, face_centroid;
+    std::vector<int> face_idx_start{0}, face_idx;
+    std::vector<TriMeshDev> trimesh;
+    std::vector<float4> tri_verts;
+    std::vector<TriDev> tris;
+    std::vector<TriNodeDev> tri_nodes;
+    std::vector<JointDev> joints;
+    std::vector<int2> nc;
+    std::vector<int> jsched, jstep_start{0}, scene_jsteps{0};
+    for (int s = 0; s < S; ++s) {
+        const psx_scene_desc& d = scenes[s];
+        PSX_TRY(validate(d));
+        int bbase = (int)pos.size(), cbase = (int)col_info.size(), dbase = (int)dyn_body.size();
+        int mbase = (int)convex.size(), tbase = (int)trimesh.size(), jbase = (int)joints.size();
+        // convex meshes: vertex buffer padded to a multiple of four with the last vertex (src/ConvexMesh.cpp:3-11)
+        for (int m = 0; m < d.n_convex; ++m) {
+            ConvexMeshDev cm;
+            cm.vert_start = (int)convex_verts.size();
+            int v0 = d.convex_vert_start[m], v1 = d.convex_vert_start[m + 1];
+            cm.vert_count = v1 - v0;
+            cm.vert_count_padded = (cm.vert_count + 3) / 4 * 4;
+            for (int v = v0; v < v1; ++v) convex_verts.push_back(f4(d.convex_verts[3 * v], d.convex_verts[3 * v + 1], d.convex_verts[3 * v + 2]));
+            for (int v = cm.vert_count; v < cm.vert_count_padded; ++v) convex_verts.push_back(convex_verts.back());
+            cm.face_start = (int)face_normal.size();
+            for (int fi = d.convex_face_start[m]; fi < d.convex_face_start[m + 1]; ++fi) {
+                for (int k = d.face_index_start[fi]; k < d.face_index_start[fi + 1]; ++k) face_idx.push_back(d.face_indices[k]);
+                face_idx_start.push_back((int)face_idx.size());
+                face_normal.push_back(f4(d.face_normal[3 * fi], d.face_normal[3 * fi + 1], d.face_normal[3 * fi + 2]));
+                face_centroid.push_back(f4(d.face_centroid[3 * fi], d.face_centroid[3 * fi + 1], d.face_centroid[3 * fi + 2]));
+            }
+            cm.face_count = (int)face_normal.size() - cm.face_start;
+            convex.push_back(cm);
+        }
+        for (int m = 0; m < d.n_trimesh; ++m) {
+            int v0 = d.tri_vert_start[m], v1 = d.tri_vert_start[m + 1];
+            int i0 = d.tri_index_start[m], i1 = d.tri_index_start[m + 1];
+            MeshBVH bvh;
+            bvh.build(d.tri_verts + 3 * v0, d.tri_indices + i0, i1 - i0);
+            TriMeshDev tm;
+            tm.vert_start = (int)tri_verts.size();
+            tm.vert_count = v1 - v0;
+            tm.tri_start = (int)tris.size();
+            tm.tri_count = (int)bvh.tris.size();
+            tm.node_start = (int)tri_nodes.size();
+            for (int v = v0; v < v1; ++v) tri_verts.push_back(f4(d.tri_verts[3 * v], d.tri_verts[3 * v + 1], d.tri_verts[3 * v + 2]));
+            for (const HTri& t : bvh.tris) {
+                TriDev td;
+                td.idx = make_int4((int)t.idx[0], (int)t.idx[1], (int)t.idx[2], 0);
+                td.bmin = st4(t.b.min); td.bmax = st4(t.b.max);
+                td.normal = st4(t.normal); td.centroid = st4(t.centroid);
+                tris.push_back(td);
+            }
+            for (const HNode& n : bvh.nodes) {
+                TriNodeDev nd;
+                nd.bmin = f4(n.b.min.x, n.b.min.y, n.b.min.z, bits_as_float(n.triCount));
+                nd.bmax = f4(n.b.max.x, n.b.max.y, n.b.max.z, bits_as_float(n.index));
+                tri_nodes.push_back(nd);
+            }
+            trimesh.push_back(tm);
+        }
+        for (int b = 0; b < d.n_bodies; ++b) {
+            uint32_t fl = d.flags[b];
+            bool dyn = fl & PSX_BODY_DYNAMIC;
+            bool sim = dyn && !(fl & PSX_BODY_KINEMATIC);
+            int di = -1;
+            pos.push_back(f4(d.pos[3 * b], d.pos[3 * b + 1], d.pos[3 * b + 2]));
+            quat.push_back(f4(d.quat[4 * b], d.quat[4 * b + 1], d.quat[4 * b + 2], d.quat[4 * b + 3]));
+            if (dyn) {
+                di = (int)dyn_body.size();
+                dyn_body.push_back(bbase + b);
+                vel.push_back(f4(d.vel[3 * b], d.vel[3 * b + 1], d.vel[3 * b + 2]));
+                ang.push_back(f4(d.ang_vel[3 * b], d.ang_vel[3 * b + 1], d.ang_vel[3 * b + 2]));
+                com.push_back(f4(d.com[3 * b], d.com[3 * b + 1], d.com[3 * b + 2], d.inv_mass[b]));
+                for (int k = 0; k < 3; ++k) invI.push_back(f4(d.inv_inertia[9 * b + 3 * k], d.inv_inertia[9 * b + 3 * k + 1], d.inv_inertia[9 * b + 3 * k + 2]));
+            }
+            info.push_back(make_int4((int)d.entity[b], (int)fl, di, s));
+            W->h_entity.push_back(d.entity[b]);
+            W->h_body_dyn.push_back(di);
+            for (int c = d.collider_start[b]; c < d.collider_start[b + 1]; ++c) {
+                int t = d.col_type[c];
+                int mesh = t == PSX_CONVEX_MESH ? mbase + d.col_mesh[c] : (t == PSX_TRIANGLE_MESH ? tbase + d.col_mesh[c] : -1);
+                int flags = 0;
+                if (!d.col_enable_sim || d.col_enable_sim[c]) flags |= COL_ENABLE;
+                if (d.col_is_trigger && d.col_is_trigger[c]) flags |= COL_TRIGGER;
+                if (sim) flags |= COL_DYNAMIC;
+                col_info.push_back(make_int4(bbase + b, t, mesh, flags));
+                col_pos.push_back(f4(d.col_pos[3 * c], d.col_pos[3 * c + 1], d.col_pos[3 * c + 2]));
+                col_quat.push_back(f4(d.col_quat[4 * c], d.col_quat[4 * c + 1], d.col_quat[4 * c + 2], d.col_quat[4 * c + 3]));
+                col_params.push_back(f4(d.col_params[4 * c], d.col_params[4 * c + 1], d.col_params[4 * c + 2], d.col_params[4 * c + 3]));
+                col_mat.push_back(f4(d.col_material[3 * c], d.col_material[3 * c + 1], d.col_material[3 * c + 2],
+                                     bits_as_float(d.col_data ? d.col_data[c] : 0)));
+                W->h_col_local.push_back(c - d.collider_start[b]);
+            }
+        }
+        // joints: the reference's greedy per-entity colour bitsets (src/Physecs.cpp:690-710);
+        // colours 0-7 are entity-disjoint, colour 8 collects the overflow
+        std::vector<unsigned char> bits(d.n_bodies, 0);
+        std::vector<std::vector<int>> colors(9);
+        for (int j = 0; j < d.n_joints; ++j) {
+            int b0 = d.joint_body0[j], b1 = d.joint_body1[j];
+            unsigned u = bits[b0] | bits[b1];
+            int c = __builtin_ctz(~u);
+            bits[b0] |= (unsigned char)(1u << c);
+            bits[b1] |= (unsigned char)(1u << c);
+            colors[c].push_back(j);
+            int lo = std::min(bbase + b0, bbase + b1), hi = std::max(bbase + b0, bbase + b1);
+            nc.push_back(make_int2(lo, hi));
+            JointDev J{};
+            J.type = d.joint_type[j];
+            J.body0 = bbase + b0; J.body1 = bbase + b1;
+            J.color = c; J.simd = c < 8 ? 1 : 0;
+            bool s0 = (d.flags[b0] & PSX_BODY_DYNAMIC) && !(d.flags[b0] & PSX_BODY_KINEMATIC);
+            bool s1 = (d.flags[b1] & PSX_BODY_DYNAMIC) && !(d.flags[b1] & PSX_BODY_KINEMATIC);
+            J.b0 = s0 ? W->h_body_dyn[bbase + b0] : -1;
+            J.b1 = s1 ? W->h_body_dyn[bbase + b1] : -1;
+            const float* fr = d.joint_frames + 14 * j;
+            J.a0p = f4(fr[0], fr[1], fr[2]); J.a0q = f4(fr[3], fr[4], fr[5], fr[6]);
+            J.a1p = f4(fr[7], fr[8], fr[9]); J.a1q = f4(fr[10], fr[11], fr[12], fr[13]);
+            V3 a0 = {fr[0], fr[1], fr[2]}, a1 = {fr[7], fr[8], fr[9]};
+            V3 r0 = s0 ? a0 - V3{d.com[3 * b0], d.com[3 * b0 + 1], d.com[3 * b0 + 2]} : a0;
+            V3 r1 = s1 ? a1 - V3{d.com[3 * b1], d.com[3 * b1 + 1], d.com[3 * b1 + 2]} : a1;
+            J.r0 = st4(r0); J.r1 = st4(r1);
+            for (int k = 0; k < 8; ++k) J.params[k] = d.joint_params ? d.joint_params[PSX_JOINT_PARAMS * j + k] : 0.f;
+            joints.push_back(J);
+        }
+        // solve schedule: one step per reference colour 0-7; the overflow colour is split into
+        // steps by creation order so that joints sharing a dynamic body stay ordered
+        for (int c = 0; c < 8; ++c) {
+            if (colors[c].empty()) continue;
+            for (int j : colors[c]) jsched.push_back(jbase + j);
+            jstep_start.push_back((int)jsched.size());
+        }
+        if (!colors[8].empty()) {
+            std::map<int, int> level_of_body;
+            std::vector<std::vector<int>> levels;
+            for (int j : colors[8]) {
+                int lv = 0;
+                for (int b : {d.joint_body0[j], d.joint_body1[j]}) {
+                    bool sim = (d.flags[b] & PSX_BODY_DYNAMIC) && !(d.flags[b] & PSX_BODY_KINEMATIC);
+                    if (!sim) continue;
+                    auto it = level_of_body.find(b);
+                    if (it != level_of_body.end()) lv = std::max(lv, it->second + 1);
+                }
+                for (int b : {d.joint_body0[j], d.joint_body1[j]}) level_of_body[b] = lv;
+                if ((int)levels.size() <= lv) levels.resize(lv + 1);
+                levels[lv].push_back(j);
+            }
+            for (auto& L : levels) {
+                for (int j : L) jsched.push_back(jbase + j);
+                jstep_start.push_back((int)jsched.size());
+            }
+        }
+        scene_jsteps.push_back((int)jstep_start.size() - 1);
+        scene_body.push_back((int)pos.size());
+        scene_col.push_back((int)col_info.size());
+        scene_dyn.push_back((int)dyn_body.size());
+        scene_joint.push_back((int)joints.size());
+        W->h_knobs.push_back(f4((float)d.num_substeps, (float)d.num_iterations, d.gravity, 1.f / 60.f));
+        int nd = scene_dyn[s + 1] - scene_dyn[s];
+        if (nd <= o.block_scene_max_dyn) W->block_scenes_h.push_back(s);
+        else W->grid_scenes_h.push_back(s);
+    }
+    std::sort(nc.begin(), nc.end(), [](int2 a, int2 b) { return a.x < b.x || (a.x == b.x && a.y < b.y); });
+    nc.erase(std::unique(nc.begin(), nc.end(), [](int2 a, int2 b) { return a.x == b.x && a.y == b.y; }), nc.end());
+    W->h_scene_body = scene_body;
+    W->h_scene_col = scene_col;
+    W->h_scene_dyn = scene_dyn;
+    World& w = W->w;
+    w.n_scenes = S;
+    w.n_bodies = (int)pos.size();
+    w.n_colliders = (int)col_info.size();
+    w.n_dyn = (int)dyn_body.size();
+    w.n_joints = (int)joints.size();
+    if (w.n_colliders >= (1 << 23)) return fail(PSX_ERR_CAPACITY, "more than 2^23 colliders in one world");
+    for (const TriMeshDev& tm : trimesh) if (tm.tri_count >= (1 << 18) - 1) return fail(PSX_ERR_CAPACITY, "triangle mesh above 262142 triangles");
+    PSX_TRY(W->upload(w.scene_body, scene_body));
+    PSX_TRY(W->upload(w.scene_col, scene_col));
+    PSX_TRY(W->upload(w.scene_dyn, scene_dyn));
+    PSX_TRY(W->upload(w.scene_joint, scene_joint));
+    PSX_TRY(W->upload(w.knobs, W->h_knobs));
+    PSX_TRY(W->upload(w.pos, pos));
+    PSX_TRY(W->upload(w.quat, quat));
+    PSX_TRY(W->upload(w.info, info));
+    PSX_TRY(W->upload(w.dyn_body, dyn_body));
+    PSX_TRY(W->upload(w.vel, vel));
+    PSX_TRY(W->upload(w.ang, ang));
+    PSX_TRY(W->upload(w.com, com));
+    PSX_TRY(W->upload(w.invI, invI));
+    PSX_TRY(W->alloc(w.vt_v, w.n_dyn));
+    PSX_TRY(W->alloc(w.vt_w, w.n_dyn));
+    PSX_TRY(W->alloc(w.pv_v, w.n_dyn));
+    PSX_TRY(W->alloc(w.pv_w, w.n_dyn));
+    PSX_TRY(W->alloc(w.mt, 3 * (size_t)w.n_dyn));
+    PSX_TRY(W->upload(w.col_info, col_info));
+    PSX_TRY(W->upload(w.col_pos, col_pos));
+    PSX_TRY(W->upload(w.col_quat, col_quat));
+    PSX_TRY(W->upload(w.col_params, col_params));
+    PSX_TRY(W->upload(w.col_mat, col_mat));
+    PSX_TRY(W->alloc(w.aabb_min, w.n_colliders));
+    PSX_TRY(W->alloc(w.aabb_max, w.n_colliders));
+    PSX_TRY(W->upload(w.convex, convex));
+    PSX_TRY(W->upload(w.convex_verts, convex_verts));
+    PSX_TRY(W->upload(w.face_idx_start, face_idx_start));
+    PSX_TRY(W->upload(w.face_idx, face_idx));
+    PSX_TRY(W->upload(w.face_normal, face_normal));
+    PSX_TRY(W->upload(w.face_centroid, face_centroid));
+    PSX_TRY(W->upload(w.trimesh, trimesh));
+    PSX_TRY(W->upload(w.tri_verts, tri_verts));
+    PSX_TRY(W->upload(w.tris, tris));
+    PSX_TRY(W->upload(w.tri_nodes, tri_nodes));
+    PSX_TRY(W->upload(w.joints, joints));
+    PSX_TRY(W->alloc(w.rows, (size_t)kMaxRowsPerJoint * std::max(1, w.n_joints)));
+    PSX_TRY(W->upload(w.jsched, jsched));
+    PSX_TRY(W->upload(w.jstep_start, jstep_start));
+    PSX_TRY(W->upload(w.scene_jsteps, scene_jsteps));
+    w.scene_jsched = nullptr;
+    w.jsched_step = nullptr;
+    w.jstep_simd = nullptr;
+    PSX_TRY(W->upload(w.nc_pairs, nc));
+    w.n_nc = (int)nc.size();
+    PSX_TRY(W->alloc(w.err, 1));
+    PSX_CUDA(cudaMemset(w.err, 0, sizeof(int)));
+
+    // ---- frame buffers
+    FrameBuf& f = W->f;
+    int n = w.n_colliders;
+    int ppc = o.pairs_per_collider > 0 ? o.pairs_per_collider : 8;
+    int mpc = o.manifolds_per_collider > 0 ? o.manifolds_per_collider : 4;
+    f.pair_cap = std::max(1024, ppc * n);
+    f.man_cap = std::max(1024, mpc * n);
+    int tri_pairs = 0;
+    for (int s = 0; s < S; ++s) if (scenes[s].n_trimesh) tri_pairs += scenes[s].n_bodies;
+    f.tri_cap = std::max(64, 2 * tri_pairs);
+    f.cache_cap = 1 << ilog2ceil(2 * f.man_cap);
+    PSX_TRY(W->alloc(f.scene_lo, S));
+    PSX_TRY(W->alloc(f.scene_hi, S));
+    PSX_TRY(W->alloc(f.keys, n));
+    PSX_TRY(W->alloc(f.order, n));
+    PSX_TRY(W->alloc(f.keys_tmp, n));
+    PSX_TRY(W->alloc(f.order_tmp, n));
+    PSX_TRY(W->alloc(f.radix_hist, radix_hist_ints(n)));
+    BVHNodes& v = f.bvh;
+    PSX_TRY(W->alloc(v.left, n)); PSX_TRY(W->alloc(v.right, n)); PSX_TRY(W->alloc(v.parent, n));
+    PSX_TRY(W->alloc(v.leaf_parent, n)); PSX_TRY(W->alloc(v.first, n)); PSX_TRY(W->alloc(v.last, n));
+    PSX_TRY(W->alloc(v.bmin, n)); PSX_TRY(W->alloc(v.bmax, n)); PSX_TRY(W->alloc(v.visits, n));
+    PSX_TRY(W->alloc(f.leaf_cnt, n));
+    PSX_TRY(W->alloc(f.leaf_off, n));
+    size_t scr = std::max(scan_scratch_ints(std::max(f.pair_cap, n)), scan_scratch_ints(S + 1));
+    PSX_TRY(W->alloc(f.scan_scratch, scr));
+    PSX_TRY(W->alloc(f.pairs, f.pair_cap));
+    PSX_TRY(W->alloc(f.n_pairs, 1));
+    PSX_TRY(W->alloc(f.pair_cat, f.pair_cap));
+    PSX_TRY(W->alloc(f.cat_flag, f.pair_cap));
+    for (int c = 0; c < 3; ++c) PSX_TRY(W->alloc(f.cat_pos[c], f.pair_cap));
+    PSX_TRY(W->alloc(f.cat_count, 3));
+    PSX_TRY(W->alloc(f.cat_list, 3 * (size_t)f.pair_cap));
+    PSX_TRY(W->alloc(f.man_pair, f.pair_cap));
+    PSX_TRY(W->alloc(f.man_tri, (size_t)f.tri_cap * kTriManifolds));
+    PSX_TRY(W->alloc(f.pair_tslot, f.pair_cap));
+    PSX_TRY(W->alloc(f.pair_nman, f.pair_cap));
+    PSX_TRY(W->alloc(f.pair_moff, f.pair_cap));
+    PSX_TRY(W->alloc(f.n_man, 1));
+    PSX_TRY(W->alloc(f.contacts, f.man_cap));
+    PSX_TRY(W->alloc(f.man_scene_cnt, S + 1));
+    PSX_TRY(W->alloc(f.scene_man, S + 1));
+    PSX_TRY(W->alloc(f.claim, std::max(1, w.n_dyn)));
+    PSX_TRY(W->alloc(f.color_of, f.man_cap));
+    PSX_TRY(W->alloc(f.corder, f.man_cap));
+    PSX_TRY(W->alloc(f.scene_ncolor, S));
+    PSX_TRY(W->alloc(f.color_start, (size_t)S * (kMaxColors + 1)));
+    PSX_TRY(W->alloc(f.claim_pos, (size_t)S * (kMaxColors + 1)));
+    PSX_TRY(W->alloc(f.cache_a, f.cache_cap));
+    PSX_TRY(W->alloc(f.cache_b, f.cache_cap));
+    PSX_TRY(W->alloc(f.cache_parity, 1));
+    PSX_TRY(W->alloc(f.bar, 4));
+    PSX_CUDA(cudaMemset(f.bar, 0, 4 * sizeof(unsigned)));
+    PSX_CUDA(cudaMemset(f.cache_parity, 0, sizeof(int)));
+    PSX_CUDA(cudaMemset(f.cache_a, 0xff, sizeof(CacheEntry) * (size_t)f.cache_cap));
+    PSX_CUDA(cudaMemset(f.cache_b, 0xff, sizeof(CacheEntry) * (size_t)f.cache_cap));
+    PSX_CUDA(cudaMemset(f.n_pairs, 0, sizeof(int)));
+    PSX_CUDA(cudaMemset(f.n_man, 0, sizeof(int)));
+    PSX_CUDA(cudaMemset(f.scene_man, 0, sizeof(int) * (S + 1)));
+    PSX_TRY(W->upload(W->block_scenes, W->block_scenes_h));
+    PSX_TRY(W->upload(W->grid_scenes, W->grid_scenes_h));
+    W->grid_blocks = W->grid_scenes_h.empty() ? 0 : solver_grid_blocks();
+    int sbits = ilog2ceil(S);
+    if (S <= 1) { W->mbits = 30; W->total_bits = 30; }
+    else {
+        int mb = std::min(30, (32 - sbits) / 3 * 3);
+        W->mbits = mb;
+        W->total_bits = mb + sbits;
+    }
+    // creation bounds: no margin (src/Physecs.cpp:32)
+    launch_aabb(w, 0, W->stream);
+    PSX_CUDA(cudaGetLastError());
+    PSX_CUDA(cudaStreamSynchronize(W->stream));
+    return PSX_OK;
+}
+
+static void queue_frame(psx_world* W) {
+    launch_broadphase(W->w, W->f, W->mbits, W->total_bits, W->stream);
+    launch_narrowphase(W->w, W->f, W->stream);
+    launch_contacts(W->w, W->f, W->stream);
+    launch_joint_layout(W->w, W->stream);
+    launch_solver(W->w, W->f, W->block_scenes, (int)W->block_scenes_h.size(), W->grid_scenes, (int)W->grid_scenes_h.size(),
+                  W->grid_blocks, W->stream);
+    launch_aabb(W->w, 1, W->stream);
+}
+
+static psx_status check_err(psx_world* W) {
+    int e = 0;
+    PSX_CUDA(cudaMemcpy(&e, W->w.err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (!e) return PSX_OK;
+    char buf[160];
+    std::snprintf(buf, sizeof buf, "device error bits 0x%x", e);
+    if (e & ERR_BARRIER_TIMEOUT) return fail(PSX_ERR_TIMEOUT, buf);
+    return fail(PSX_ERR_CAPACITY, buf);
+}
+
+static psx_status ensure_pinned(psx_world* W, size_t n4) {
+    if (W->pin_n >= n4) return PSX_OK;
+    if (W->pin) cudaFreeHost(W->pin);
+    W->pin = nullptr;
+    W->pin_n = 0;
+    PSX_CUDA(cudaMallocHost(&W->pin, n4 * sizeof(float4)));
+    W->pin_n = n4;
+    return PSX_OK;
+}
+
+extern "C" {
+
+PSX_API const char* psx_last_error_string(void) { return g_err.c_str(); }
+
+PSX_API psx_status psx_world_create(const psx_scene_desc* scenes, int32_t n_scenes, const psx_world_opts* opts, psx_world** out) {
+    if (!scenes || n_scenes <= 0 || !out) return fail(PSX_ERR_INVALID_ARG, "psx_world_create: bad arguments");
+    psx_world_opts o{};
+    if (opts) o = *opts;
+    if (o.block_scene_max_dyn <= 0) o.block_scene_max_dyn = 8192;
+    int dev_count = 0;
+    if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0) return fail(PSX_ERR_CUDA, "no CUDA device");
+    psx_world* W = new psx_world();
+    W->use_graph = o.use_graph != 0;
+    cudaError_t e = cudaStreamCreateWithFlags(&W->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { delete W; return fail(PSX_ERR_CUDA, cudaGetErrorString(e)); }
+    psx_status s = build_world(W, scenes, n_scenes, o);
+    if (s != PSX_OK) { delete W; return s; }
+    *out = W;
+    return PSX_OK;
+}
+
+PSX_API psx_status psx_world_destroy(psx_world* w) {
+    if (!w) return fail(PSX_ERR_INVALID_ARG, "null world");
+    cudaStreamSynchronize(w->stream);
+    delete w;
+    return PSX_OK;
+}
+
+PSX_API psx_status psx_world_set_knobs(psx_world* W, int32_t scene, int32_t substeps, int32_t iterations, float gravity) {
+    if (!W || substeps <= 0 || iterations < 0 || scene >= W->n_scenes) return fail(PSX_ERR_INVALID_ARG, "set_knobs");
+    for (int s = 0; s < W->n_scenes; ++s) {
+        if (scene >= 0 && s != scene) continue;
+        W->h_knobs[s].x = (float)substeps; W->h_knobs[s].y = (float)iterations; W->h_knobs[s].z = gravity;
+    }
+    W->knobs_dirty = true;
+    return PSX_OK;
+}
+
+PSX_API psx_status psx_world_step(psx_world* W, float dt, int32_t frames) {
+    if (!W || frames < 0) return fail(PSX_ERR_INVALID_ARG, "psx_world_step");
+    if (W->knobs_dirty || W->h_knobs.empty() || W->h_knobs[0].w != dt) {
+        for (auto& k : W->h_knobs) k.w = dt;
+        PSX_CUDA(cudaMemcpyAsync(W->w.knobs, W->h_knobs.data(), sizeof(float4) * W->h_knobs.size(), cudaMemcpyHostToDevice, W->stream));
+        W->knobs_dirty = false;
+    }
+    for (int i = 0; i < frames; ++i) {
+        if (W->use_graph) {
+            if (!W->graph) {
+                cudaGraph_t g;
+                PSX_CUDA(cudaStreamBeginCapture(W->stream, cudaStreamCaptureModeThreadLocal));
+                queue_frame(W);
+                PSX_CUDA(cudaStreamEndCapture(W->stream, &g));
+                PSX_CUDA(cudaGraphInstantiate(&W->graph, g, 0));
+                cudaGraphDestroy(g);
+            }
+            PSX_CUDA(cudaGraphLaunch(W->graph, W->stream));
+        } else {
+            queue_frame(W);
+        }
+    }
+    PSX_CUDA(cudaGetLastError());
+    return PSX_OK;
+}
+
+PSX_API psx_status psx_world_synchronize(psx_world* W) {
+    if (!W) return fail(PSX_ERR_INVALID_ARG, "null world");
+    PSX_CUDA(cudaStreamSynchronize(W->stream));
+    return check_err(W);
+}
+
+static psx_status read_bodies(psx_world* W, float* pos, float* quat, float* vel, float* ang, bool sync_after) {
+    const World& w = W->w;
+    size_t nb = w.n_bodies, nd = w.n_dyn;
+    PSX_TRY(ensure_pinned(W, 2 * nb + 2 * nd));
+    float4* hp = W->pin;
+    float4* hq = hp + nb;
+    float4* hv = hq + nb;
+    float4* ha = hv + nd;
+    PSX_CUDA(cudaMemcpyAsync(hp, w.pos, nb * sizeof(float4), cudaMemcpyDeviceToHost, W->stream));
+    PSX_CUDA(cudaMemcpyAsync(hq, w.quat, nb * sizeof(float4), cudaMemcpyDeviceToHost, W->stream));
+    if (nd) {
+        PSX_CUDA(cudaMemcpyAsync(hv, w.vel, nd * sizeof(float4), cudaMemcpyDeviceToHost, W->stream));
+        PSX_CUDA(cudaMemcpyAsync(ha, w.ang, nd * sizeof(float4), cudaMemcpyDeviceToHost, W->stream));
+    }
+    PSX_CUDA(cudaStreamSynchronize(W->stream));
+    (void)sync_after;
+    for (size_t b = 0; b < nb; ++b) {
+        if (pos) { pos[3 * b] = hp[b].x; pos[3 * b + 1] = hp[b].y; pos[3 * b + 2] = hp[b].z; }
+        if (quat) { quat[4 * b] = hq[b].x; quat[4 * b + 1] = hq[b].y; quat[4 * b + 2] = hq[b].z; quat[4 * b + 3] = hq[b].w; }
+        int d = W->h_body_dyn[b];
+        float4 v = d >= 0 ? hv[d] : make_float4(0, 0, 0, 0), a = d >= 0 ? ha[d] : make_float4(0, 0, 0, 0);
+        if (vel) { vel[3 * b] = v.x; vel[3 * b + 1] = v.y; vel[3 * b + 2] = v.z; }
+        if (ang) { ang[3 * b] = a.x; ang[3 * b + 1] = a.y; ang[3 * b + 2] = a.z; }
+    }
+    return PSX_OK;
+}
+
+PSX_API psx_status psx_world_read_bodies(psx_world* W, float* pos, float* quat, float* vel, float* ang_vel) {
+    if (!W) return fail(PSX_ERR_INVALID_ARG, "null world");
+    return read_bodies(W, pos, quat, vel, ang_vel, true);
+}
+
+PSX_API psx_status psx_world_write_bodies(psx_world* W, const float* pos, const float* quat, const float* vel, const float* ang) {
+    if (!W) return fail(PSX_ERR_INVALID_ARG, "null world");
+    const World& w = W->w;
+    size_t nb = w.n_bodies, nd = w.n_dyn;
+    PSX_TRY(ensure_pinned(W, 2 * nb + 2 * nd));
+    PSX_CUDA(cudaStreamSynchronize(W->stream));
+    float4* hp = W->pin;
+    float4* hq = hp + nb;
+    float4* hv = hq + nb;
+    float4* ha = hv + nd;
+    for (size_t b = 0; b < nb; ++b) {
+        if (pos) hp[b] = make_float4(pos[3 * b], pos[3 * b + 1], pos[3 * b + 2], 0.f);
+        if (quat) hq[b] = make_float4(quat[4 * b], quat[4 * b + 1], quat[4 * b + 2], quat[4 * b + 3]);
+        int d = W->h_body_dyn[b];
+        if (d >= 0) {
+            if (vel) hv[d] = make_float4(vel[3 * b], vel[3 * b + 1], vel[3 * b + 2], 0.f);
+            if (ang) ha[d] = make_float4(ang[3 * b], ang[3 * b + 1], ang[3 * b + 2], 0.f);
+        }
+    }
+    if (pos) PSX_CUDA(cudaMemcpyAsync(w.pos, hp, nb * sizeof(float4), cudaMemcpyHostToDevice, W->stream));
+    if (quat) PSX_CUDA(cudaMemcpyAsync(w.quat, hq, nb * sizeof(float4), cudaMemcpyHostToDevice, W->stream));
+    if (nd && vel) PSX_CUDA(cudaMemcpyAsync(w.vel, hv, nd * sizeof(float4), cudaMemcpyHostToDevice, W->stream));
+    if (nd && ang) PSX_CUDA(cudaMemcpyAsync(w.ang, ha, nd * sizeof(float4), cudaMemcpyHostToDevice, W->stream));
+    PSX_CUDA(cudaStreamSynchronize(W->stream));
+    return PSX_OK;
+}
+
+PSX_API psx_status psx_world_simulate_host(psx_world* W, float dt, float* pos, float* quat, float* vel, float* ang) {
+    PSX_TRY(psx_world_write_bodies(W, pos, quat, vel, ang));
+    PSX_TRY(psx_world_step(W, dt, 1));
+    PSX_TRY(read_bodies(W, pos, quat, vel, ang, true));
+    return check_err(W);
+}
+
+PSX_API psx_status psx_world_counts(psx_world* W, int32_t* counts) {
+    if (!W || !counts) return fail(PSX_ERR_INVALID_ARG, "counts");
+    PSX_CUDA(cudaStreamSynchronize(W->stream));
+    int np = 0, nm = 0, e = 0;
+    PSX_CUDA(cudaMemcpy(&np, W->f.n_pairs, sizeof(int), cudaMemcpyDeviceToHost));
+    PSX_CUDA(cudaMemcpy(&nm, W->f.n_man, sizeof(int), cudaMemcpyDeviceToHost));
+    PSX_CUDA(cudaMemcpy(&e, W->w.err, sizeof(int), cudaMemcpyDeviceToHost));
+    counts[0] = W->w.n_bodies; counts[1] = W->w.n_colliders; counts[2] = W->w.n_dyn; counts[3] = W->w.n_joints;
+    counts[4] = W->n_scenes; counts[5] = np; counts[6] = std::min(nm, W->f.man_cap); counts[7] = e;
+    return PSX_OK;
+}
+
+PSX_API int32_t psx_world_get_pairs(psx_world* W, int32_t* out, int32_t cap) {
+    if (!W) return -1;
+    cudaStreamSynchronize(W->stream);
+    int np = 0;
+    cudaMemcpy(&np, W->f.n_pairs, sizeof(int), cudaMemcpyDeviceToHost);
+    std::vector<int2> pr(np);
+    if (np) cudaMemcpy(pr.data(), W->f.pairs, np * sizeof(int2), cudaMemcpyDeviceToHost);
+    std::vector<int4> ci(W->w.n_colliders);
+    cudaMemcpy(ci.data(), W->w.col_info, ci.size() * sizeof(int4), cudaMemcpyDeviceToHost);
+    for (int i = 0; i < np && i < cap; ++i) {
+        int a = pr[i].x, b = pr[i].y;
+        int ba = ci[a].x, bb = ci[b].x;
+        int s = (int)(std::upper_bound(W->h_scene_body.begin(), W->h_scene_body.end(), ba) - W->h_scene_body.begin()) - 1;
+        out[5 * i + 0] = s;
+        out[5 * i + 1] = (int32_t)W->h_entity[ba];
+        out[5 * i + 2] = W->h_col_local[a];
+        out[5 * i + 3] = (int32_t)W->h_entity[bb];
+        out[5 * i + 4] = W->h_col_local[b];
+    }
+    return np;
+}
+
+PSX_API int32_t psx_world_get_contacts(psx_world* W, int32_t* ids, float* f, int32_t* meta, int32_t cap) {
+    if (!W) return -1;
+    cudaStreamSynchronize(W->stream);
+    int S = W->n_scenes;
+    std::vector<int> scene_man(S + 1), cstart((size_t)S * (kMaxColors + 1)), ncol(S);
+    cudaMemcpy(scene_man.data(), W->f.scene_man, (S + 1) * sizeof(int), cudaMemcpyDeviceToHost);
+    int nm = scene_man[S];
+    std::vector<Contact> cs(nm);
+    std::vector<int> corder(nm), color_of(nm);
+    if (nm) {
+        cudaMemcpy(cs.data(), W->f.contacts, nm * sizeof(Contact), cudaMemcpyDeviceToHost);
+        cudaMemcpy(corder.data(), W->f.corder, nm * sizeof(int), cudaMemcpyDeviceToHost);
+        cudaMemcpy(color_of.data(), W->f.color_of, nm * sizeof(int), cudaMemcpyDeviceToHost);
+    }
+    std::vector<int2> pr;
+    int np = 0;
+    cudaMemcpy(&np, W->f.n_pairs, sizeof(int), cudaMemcpyDeviceToHost);
+    pr.resize(np);
+    if (np) cudaMemcpy(pr.data(), W->f.pairs, np * sizeof(int2), cudaMemcpyDeviceToHost);
+    std::vector<int4> ci(W->w.n_colliders);
+    cudaMemcpy(ci.data(), W->w.col_info, ci.size() * sizeof(int4), cudaMemcpyDeviceToHost);
+    int out = 0;
+    for (int s = 0; s < S; ++s) {
+        // solve order: colour by colour, contacts of one colour by index
+        std::vector<int> idx;
+        for (int m = scene_man[s]; m < scene_man[s + 1]; ++m) idx.push_back(m);
+        std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return color_of[a] < color_of[b]; });
+        for (int m : idx) {
+            if (out < cap) {
+                const Contact& c = cs[m];
+                int d0 = W->h_scene_dyn[s];
+                int2 p = pr[c.pair];
+                ids[8 * out + 0] = s;
+                ids[8 * out + 1] = c.b0 >= 0 ? c.b0 - d0 : -1;
+                ids[8 * out + 2] = c.b1 >= 0 ? c.b1 - d0 : -1;
+                ids[8 * out + 3] = c.np | (c.soft << 8);
+                ids[8 * out + 4] = (int32_t)W->h_entity[ci[p.x].x];
+                ids[8 * out + 5] = W->h_col_local[p.x];
+                ids[8 * out + 6] = (int32_t)W->h_entity[ci[p.y].x];
+                ids[8 * out + 7] = W->h_col_local[p.y];
+                float* o = f + 56 * out;
+                std::memset(o, 0, 56 * sizeof(float));
+                o[0] = c.n.x; o[1] = c.n.y; o[2] = c.n.z; o[3] = c.n.w; o[4] = c.frequency; o[5] = c.damping;
+                for (int k = 0; k < c.np; ++k) {
+                    const ContactPt& p = c.p[k];
+                    float* q = o + 8 + 12 * k;
+                    q[0] = p.r0.x; q[1] = p.r0.y; q[2] = p.r0.z; q[3] = p.r1.x; q[4] = p.r1.y; q[5] = p.r1.z;
+                    q[6] = p.r0.w; q[7] = p.r1.w; q[8] = p.r0xn.w; q[9] = p.r1xn.w;
+                }
+                if (meta) { meta[2 * out] = color_of[m]; meta[2 * out + 1] = c.tri; }
+            }
+            ++out;
+        }
+    }
+    return out;
+}
+
+PSX_API int32_t psx_world_get_bounds(psx_world* W, float* bounds, int32_t cap) {
+    if (!W) return -1;
+    cudaStreamSynchronize(W->stream);
+    int n = W->w.n_colliders;
+    std::vector<float4> a(n), b(n);
+    cudaMemcpy(a.data(), W->w.aabb_min, n * sizeof(float4), cudaMemcpyDeviceToHost);
+    cudaMemcpy(b.data(), W->w.aabb_max, n * sizeof(float4), cudaMemcpyDeviceToHost);
+    for (int i = 0; i < n && i < cap; ++i) {
+        bounds[6 * i] = a[i].x; bounds[6 * i + 1] = a[i].y; bounds[6 * i + 2] = a[i].z;
+        bounds[6 * i + 3] = b[i].x; bounds[6 * i + 4] = b[i].y; bounds[6 * i + 5] = b[i].z;
+    }
+    return n;
+}
+
+PSX_API psx_status psx_scene_create(const psx_scene_desc* desc, psx_scene** out) { return psx_world_create(desc, 1, nullptr, out); }
+PSX_API psx_status psx_scene_destroy(psx_scene* s) { return psx_world_destroy(s); }
+PSX_API psx_status psx_scene_simulate(psx_scene* s, float dt) {
+    PSX_TRY(psx_world_step(s, dt, 1));
+    return psx_world_synchronize(s);
+}
+
+}  // extern "C"

@@ -1,0 +1,26 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+@pytest.fixture(scope="session")
+def oracle_lib():
+    from oracle import port_api
+    port_api.build()
+    return port_api
+
+
+@pytest.fixture(scope="session")
+def gpu_lib():
+    from physecs_gb300 import api
+    lib = api.load()
+    return api

@@ -1,0 +1,138 @@
+"""GPU parity: the CUDA path against the CPU oracle on the same seeded scenes.
+
+Tolerances (from the hot path's parity contract):
+  * collider bounds and broadphase pair sets: bit-exact;
+  * manifold normals, points and target velocities from identical poses: 1e-5;
+  * a frame from identical state, with the oracle fed the GPU's colour-sorted
+    contact order: 1e-5 relative.
+The library is built with -fmad=false, so in practice these match bit for bit.
+"""
+import numpy as np
+import pytest
+
+from physecs_gb300 import scenes
+from tests.parity import compare_contacts, gpu_keys, pair_set, rel_state_diff
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+
+
+def _mini_mixed(seed=7, n=60):
+    return scenes.batch_scene(seed, n_bodies=n)
+
+
+def _scenes():
+    return {
+        "pyramid": scenes.pyramid(rows=8),
+        "mixed": _mini_mixed(),
+        "chain": scenes.batch_scene(11, n_bodies=40, chain_prob=1.0),
+        "heightfield": scenes.large_mixed(n_bodies=300, cells=32),
+        "joints": scenes.joint_chains(n_chains=12, links=6),
+    }
+
+
+@pytest.fixture(scope="module")
+def all_scenes():
+    return _scenes()
+
+
+def _oracle(s):
+    from oracle.port_api import OracleScene
+    return OracleScene(s)
+
+
+def _gpu(s, **kw):
+    from physecs_gb300.api import World
+    return World([s], **kw)
+
+
+@pytest.mark.parametrize("name", ["pyramid", "mixed", "chain", "heightfield", "joints"])
+def test_creation_bounds_bit_exact(all_scenes, name, gpu_lib, oracle_lib):
+    s = all_scenes[name]
+    g = _gpu(s)
+    o = _oracle(s)
+    gb = g.bounds()
+    ids, ob = o.bounds()
+    # oracle bounds are listed per collider in creation order before the first step
+    starts = s.arrays["collider_start"]
+    order = np.array([starts[e] + c for e, c in ids])
+    assert np.array_equal(gb[order].view(np.uint32), ob.view(np.uint32))
+
+
+@pytest.mark.parametrize("name", ["pyramid", "mixed", "chain", "heightfield", "joints"])
+def test_first_frame_pairs_and_manifolds(all_scenes, name, gpu_lib, oracle_lib):
+    s = all_scenes[name]
+    g = _gpu(s)
+    o = _oracle(s)
+    g.step(); g.synchronize()
+    o.step()
+    gp = g.pairs()[:, 1:]
+    op = o.pairs()
+    assert pair_set(gp) == pair_set(op)
+    ids, gf, meta = g.contacts()
+    _, of = o.contacts()
+    worst = compare_contacts(gpu_keys(ids, meta), gf, o.contact_keys(), of)
+    assert worst <= TOL, worst
+    assert g.counts()["error"] == 0
+
+
+@pytest.mark.parametrize("name,frames", [("pyramid", 40), ("mixed", 30), ("chain", 30), ("heightfield", 10), ("joints", 30)])
+def test_frames_in_lockstep_with_oracle_fed_gpu_order(all_scenes, name, frames, gpu_lib, oracle_lib):
+    """Each frame: step the GPU, hand its colour-sorted contact order to the oracle, step the
+    oracle, compare full body state.  Any divergence shows up within a frame."""
+    s = all_scenes[name]
+    g = _gpu(s)
+    o = _oracle(s)
+    for f in range(frames):
+        g.step(); g.synchronize()
+        ids, gf, meta = g.contacts()
+        o.set_contact_order(gpu_keys(ids, meta))
+        o.step()
+        assert o.order_error() == 0, "frame %d: GPU manifolds not found in the oracle" % f
+        d = rel_state_diff(g.read_bodies(), o.state())
+        assert d <= TOL, "frame %d: relative state difference %g" % (f, d)
+    assert g.counts()["error"] == 0
+
+
+def test_batched_world_matches_scene_by_scene(gpu_lib, oracle_lib):
+    """Eight uneven scenes in one world: every scene equals its own oracle run."""
+    ss = [scenes.batch_scene(i, n_bodies=n) for i, n in enumerate([16, 40, 90, 23, 150, 64, 31, 200])]
+    ss[3] = scenes.batch_scene(3, n_bodies=23, chain_prob=1.0)
+    g = _gpu(ss)
+    os_ = [_oracle(s) for s in ss]
+    start = g.body_start
+    for f in range(15):
+        g.step(); g.synchronize()
+        ids, gf, meta = g.contacts()
+        st = g.read_bodies()
+        for i, o in enumerate(os_):
+            sel = ids[:, 0] == i
+            o.set_contact_order(gpu_keys(ids[sel], meta[sel]))
+            o.step()
+            assert o.order_error() == 0
+            d = rel_state_diff({k: v[start[i]:start[i + 1]] for k, v in st.items()}, o.state())
+            assert d <= TOL, "scene %d frame %d: %g" % (i, f, d)
+
+
+def test_one_substep_from_identical_state(gpu_lib, oracle_lib):
+    """One substep (substeps = 1) from an identical mid-simulation state."""
+    s = scenes.pyramid(rows=10)
+    o = _oracle(s)
+    o.step(frames=25)
+    st = o.state()
+    s2 = scenes.pyramid(rows=10)
+    s2.num_substeps = 1
+    g = _gpu(s2)
+    g.write_bodies(st)
+    o.set_knobs(1, s.num_iterations, s.gravity)
+    # same pose history matters only through the broadphase margins, which start fresh on both sides
+    from oracle.port_api import OracleScene
+    o2 = OracleScene(s2)
+    o2.write_state(st)
+    g.step(); g.synchronize()
+    ids, gf, meta = g.contacts()
+    o2.set_contact_order(gpu_keys(ids, meta))
+    o2.step()
+    assert o2.order_error() == 0
+    assert rel_state_diff(g.read_bodies(), o2.state()) <= TOL
