@@ -1,0 +1,384 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 simulation hot path (physecs::Scene::simulate).
+
+Metric: body-substeps/s = simulated bodies x substeps x frames / wall seconds.
+Default workload: the batched form, 4096 independent scenes in one world, each
+with N log-uniform in [16, 2048] bodies (box / sphere / capsule / convex hull mix,
+uniform random orientations, dropped on a per-scene ground box, 10% of scenes
+with an 8-link revolute chain), dt = 1/60 s, 4 substeps, 8 iterations, FP32.
+Scenes are seeded synthetic data (Physecs publishes no dataset).
+
+One step = one frame of every scene.  The timed region is bracketed by a
+barrier and device synchronisation and timed with CUDA events on the world's
+own stream; the working set (bodies, contacts, rows: GBs) exceeds the 129 MB L2,
+so no flush is needed between steps.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+Under torchrun each rank simulates its own 4096 scenes (weak scaling, no
+data-path collective); rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "body-substeps/s"
+DT = 1.0 / 60.0
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+class Dist:
+    """Barrier and max-reduction over ranks (torch.distributed when launched with several ranks)."""
+
+    def __init__(self, world, local):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch
+            import torch.distributed as td
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(local)
+            td.init_process_group(backend=backend)
+            self.td, self.torch, self.backend = td, torch, backend
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, v):
+        if self.world == 1:
+            return v
+        t = self.torch.tensor([v], dtype=self.torch.float64,
+                              device="cuda" if self.backend == "nccl" else "cpu")
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v):
+        if self.world == 1:
+            return v
+        t = self.torch.tensor([v], dtype=self.torch.float64,
+                              device="cuda" if self.backend == "nccl" else "cpu")
+        self.td.all_reduce(t, op=self.td.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def build_workload(name, rank, n_scenes):
+    from physecs_gb300 import scenes
+    if name == "batched":
+        pool = scenes._hull_pool(scenes.SplitMix64(scenes.scene_seed(4, 1 << 19)), count=8)
+        ss = [scenes.batch_scene(rank * n_scenes + i, pool=pool) for i in range(n_scenes)]
+        cfg = {"workload": "batched: %d independent scenes per GPU, N log-uniform in [16,2048] bodies, "
+                           "box/sphere/capsule/hull 40/30/20/10 on a ground box, 10%% with an 8-link revolute chain, "
+                           "dt=1/60 s, 4 substeps, 8 iterations" % n_scenes, "scenes": n_scenes}
+    elif name == "large":
+        ss = [scenes.large_mixed()]
+        cfg = {"workload": "large single scene: 65536 mixed bodies over a 256x256-cell heightfield, dt=1/60, 4x8",
+               "scenes": 1}
+    elif name == "chains":
+        ss = [scenes.joint_chains()]
+        cfg = {"workload": "2048 capsule chains x 32 links, mixed joints, dt=1/60, 8 substeps x 4 iterations", "scenes": 1}
+    else:
+        ss = [scenes.pyramid()]
+        cfg = {"workload": "20-row box pyramid (210 cubes) on a ground box, dt=1/60, 4x8", "scenes": 1}
+    return ss, cfg
+
+
+def simulated_bodies(ss):
+    return sum(s.n_dynamic for s in ss)
+
+
+# ---------------------------------------------------------------- CPU side
+
+def _cpu_worker(args):
+    """Oracle (CPU restatement) on a subset of scenes: returns (seconds, body-substeps)."""
+    kind, specs, frames, warm = args
+    sys.path.insert(0, ROOT)
+    from physecs_gb300 import scenes
+    if kind == "reference":
+        from oracle.ref.ref_api import RefScene as Sim
+    else:
+        from oracle.port_api import OracleScene as Sim
+    pool = scenes._hull_pool(scenes.SplitMix64(scenes.scene_seed(4, 1 << 19)), count=8)
+    sims, work = [], 0
+    for idx in specs:
+        s = scenes.batch_scene(idx, pool=pool)
+        sims.append(Sim(s))
+        work += s.n_dynamic * s.num_substeps
+    for sim in sims:
+        sim.step(DT, warm)
+    t = time.perf_counter()
+    for sim in sims:
+        sim.step(DT, frames)
+    return time.perf_counter() - t, work * frames
+
+
+def cpu_throughput(kind, scene_ids, frames, warm, procs):
+    """body-substeps/s of the CPU implementation over `scene_ids`, using `procs` processes."""
+    import multiprocessing as mp
+    chunks = [scene_ids[i::procs] for i in range(procs)]
+    chunks = [c for c in chunks if c]
+    if len(chunks) == 1:
+        t, work = _cpu_worker((kind, chunks[0], frames, warm))
+        return work / t, t, 1
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(len(chunks)) as pool:
+        res = pool.map(_cpu_worker, [(kind, c, frames, warm) for c in chunks])
+    wall = max(r[0] for r in res)
+    work = sum(r[1] for r in res)
+    return work / wall, wall, len(chunks)
+
+
+def cpu_kind():
+    try:
+        from oracle.ref import ref_api
+        if ref_api.available():
+            return "reference"
+    except Exception:
+        pass
+    return "port"
+
+
+# ---------------------------------------------------------------- main
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--workload", default="batched", choices=["batched", "large", "chains", "pyramid"])
+    ap.add_argument("--scenes", type=int, default=4096)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--plain-scenes", type=int, default=64)
+    ap.add_argument("--cpu-scenes", type=int, default=256)
+    ap.add_argument("--cpu-frames", type=int, default=20)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_info()
+    assert args.warmup >= 3, "at least three warm-up steps"
+
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    dist = Dist(world, local)
+    from physecs_gb300.api import World
+    ss, cfg = build_workload(args.workload, rank, args.scenes)
+    n_sim = simulated_bodies(ss)
+    substeps = ss[0].num_substeps
+    w = World(ss, device=local if world > 1 else 0)
+    for _ in range(args.warmup):
+        w.step(DT)
+    w.synchronize()
+    counts = w.counts()
+    dist.barrier()
+    with ClockSampler(local) as clk:
+        total_ms, stage_ms, kernels = w.step_timed(DT, args.steps)
+    dist.barrier()
+    t_max = dist.max(total_ms)
+    work = n_sim * substeps * args.steps
+    value = dist.sum(work) / (t_max / 1000.0)
+    counts = w.counts()
+    if counts["error"]:
+        raise RuntimeError("device error bits %d" % counts["error"])
+
+    # roofline of the dominant kernel: the solver (one launch per frame covers every substep)
+    pts, rows = counts["points"], counts["rows"]
+    alg_bytes = substeps * (156.0 * n_sim + 52.0 * pts + 76.0 * rows)
+    solver_s = stage_ms[3] / 1000.0 / args.steps
+    achieved = alg_bytes / solver_s / 1e9
+    peak, peak_src = measured_peaks()
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "solver_traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as f:
+            tj = json.load(f)
+        if tj.get("workload") == args.workload and tj.get("bytes_per_body_frame"):
+            traffic = float(tj["bytes_per_body_frame"]) * n_sim
+
+    # end to end through the public API with host buffers: upload, one frame, download
+    st = w.read_bodies()
+    nb, nd = w.n_bodies, counts["dynamic"]
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        w.simulate_host(DT, st)
+    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+    e2e_s = dist.max(e2e_s)
+    e2e_value = dist.sum(n_sim * substeps) / e2e_s
+    h2d = 16 * (2 * nb + 2 * nd)
+
+    # the plain path: the same scenes, one world per scene, stepped one scene at a time
+    plain = None
+    if args.workload == "batched" and args.plain_scenes > 0 and rank == 0:
+        sub = ss[:args.plain_scenes]
+        ws = [World([s]) for s in sub]
+        for x in ws:
+            x.step(DT, 3)
+        for x in ws:
+            x.synchronize()
+        t0 = time.perf_counter()
+        frames = 3
+        for x in ws:
+            for _ in range(frames):
+                x.step(DT)
+            x.synchronize()
+        pt = time.perf_counter() - t0
+        plain = simulated_bodies(sub) * substeps * frames / pt
+        for x in ws:
+            x.close()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu and args.workload == "batched":
+        try:
+            kind = "port"
+            ids = list(range(args.cpu_scenes))
+            v, wall, procs = cpu_throughput(kind, ids, args.cpu_frames, 2, 1)
+            cpu = {"value": v, "unit": METRIC, "cores": procs, "kind": kind,
+                   "sample": "%d of the batched scenes x %d frames on %d thread (%.1f s)" % (len(ids), args.cpu_frames, procs, wall)}
+        except Exception as e:  # the baseline is reported, never required
+            cpu = {"value": None, "unit": METRIC, "cores": 0, "kind": "port", "sample": "failed: %s" % e}
+
+    clocks = clk.summary()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 in GJK/EPA)",
+            "data": "synthetic (seeded SplitMix64 scenes)",
+            "config": dict(cfg, parallelism="scene shards" if world > 1 else "single GPU",
+                           l2="working set larger than L2 (no flush)", simulated_bodies=n_sim,
+                           contact_points=pts, joint_rows=rows, pairs=counts["pairs"], manifolds=counts["manifolds"]),
+            "stage_ms_per_step": {k: v / args.steps for k, v in zip(
+                ["broadphase", "narrowphase", "contact_joint_rows", "solver", "bounds"], stage_ms)},
+            "roofline": {"kernel": "k_solve_block (solver, all substeps of a frame)", "bound": "hbm",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_source": peak_src, "traffic": traffic,
+                         "algorithmic_bytes": alg_bytes},
+            "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d},
+            "plain_gpu_scene_by_scene": None if plain is None else {"value": plain, "unit": METRIC,
+                                                                    "scenes": min(args.plain_scenes, len(ss))},
+            "batched_vs_plain": None if plain is None else value / plain,
+            "gpu_launches": kernels,
+            "clocks": clocks,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    w.close()
+    dist.close()
+
+
+def run_reference(args, rank, world):
+    """The reference's own CPU implementation on the host cores, same metric and workload."""
+    if rank != 0:
+        return 0
+    kind = cpu_kind()
+    procs = max(1, os.cpu_count() or 1)
+    ids = list(range(min(args.scenes, 16 * procs)))
+    vals = []
+    for _ in range(max(1, args.steps // 10)):
+        v, wall, used = cpu_throughput(kind, ids, 2, 1, procs)
+        vals.append(v)
+    value = statistics.median(vals)
+    cfg = build_workload.__doc__
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "impl": "reference",
+        "data": "synthetic (seeded SplitMix64 scenes)",
+        "config": {"workload": "batched scenes (same generator), sample of %d scenes x 2 frames per step" % len(ids)},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": used, "kind": kind,
+                         "sample": "%d scenes x 2 frames, one process per host core" % len(ids)},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    del cfg
+    print(json.dumps(line))
+    return 0
+
+
+if __name__ == "__main__":
+    main()

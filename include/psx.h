@@ -156,6 +156,7 @@ typedef struct psx_world_opts {
     int32_t manifolds_per_collider;  /* contact manifold capacity per collider (0: default 4) */
     int32_t block_scene_max_dyn;     /* scenes up to this many dynamic bodies run one per CTA (0: default 8192) */
     int32_t use_graph;               /* capture the frame in a CUDA graph after the first step */
+    int32_t device;                  /* CUDA device ordinal the world lives on */
 } psx_world_opts;
 
 /* Scene::Scene(registry, numThreads) plus the registry's contents
@@ -167,6 +168,11 @@ PSX_API psx_status psx_world_destroy(psx_world* w);
 /* Scene::simulate(timeStep) (src/Physecs.cpp:112-561), `frames` times, every scene.
  * Asynchronous: returns once the work is queued on the world's stream. */
 PSX_API psx_status psx_world_step(psx_world* w, float dt, int32_t frames);
+/* Like psx_world_step, timed on the world's stream with CUDA events: total_ms for all
+ * frames, stage_ms[5] = {broadphase, narrowphase, contact + joint rows, solver,
+ * end-of-frame bounds} summed over the frames, kernels = kernels queued.  Waits. */
+PSX_API psx_status psx_world_step_timed(psx_world* w, float dt, int32_t frames, float* total_ms, float* stage_ms,
+                                        int64_t* kernels);
 /* Waits for queued work and reports a device-side error (capacity, timeout). */
 PSX_API psx_status psx_world_synchronize(psx_world* w);
 /* Scene::setNumSubSteps / setNumIterations / setGravity (src/Physecs.cpp:100-110) for one scene (-1: all). */
@@ -179,7 +185,9 @@ PSX_API psx_status psx_world_write_bodies(psx_world* w, const float* pos, const 
 /* One end-to-end simulate through host buffers: upload the given state, step one
  * frame, download the new state into the same buffers, and wait. */
 PSX_API psx_status psx_world_simulate_host(psx_world* w, float dt, float* pos, float* quat, float* vel, float* ang_vel);
-/* counts[8] = {bodies, colliders, dynamic bodies, joints, scenes, pairs, manifolds, error bits} */
+/* counts[12] = {bodies, colliders, dynamic bodies, joints, scenes, pairs, manifolds, error bits,
+ *              contact points, joint rows, simulated bodies, kernels queued since creation}
+ * (per-frame values describe the last frame) */
 PSX_API psx_status psx_world_counts(psx_world* w, int32_t* counts);
 /* Inspection of the last frame (synchronises):
  *   pairs: {scene, entity0, collider0, entity1, collider1} per broadphase pair

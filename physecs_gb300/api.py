@@ -20,7 +20,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libpsx.so")
 
 PSX_STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OUT_OF_MEMORY", 3: "CAPACITY", 4: "TIMEOUT", 5: "CUDA", 6: "NOT_READY"}
-EXPORTS = ["psx_world_create", "psx_world_destroy", "psx_world_step", "psx_world_synchronize", "psx_world_set_knobs",
+EXPORTS = ["psx_world_create", "psx_world_destroy", "psx_world_step", "psx_world_step_timed", "psx_world_synchronize", "psx_world_set_knobs",
            "psx_world_read_bodies", "psx_world_write_bodies", "psx_world_simulate_host", "psx_world_counts",
            "psx_world_get_pairs", "psx_world_get_contacts", "psx_world_get_bounds", "psx_last_error_string",
            "psx_scene_create", "psx_scene_destroy", "psx_scene_simulate"]
@@ -34,7 +34,7 @@ class PsxError(RuntimeError):
 
 class PsxWorldOpts(C.Structure):
     _fields_ = [("pairs_per_collider", C.c_int32), ("manifolds_per_collider", C.c_int32),
-                ("block_scene_max_dyn", C.c_int32), ("use_graph", C.c_int32)]
+                ("block_scene_max_dyn", C.c_int32), ("use_graph", C.c_int32), ("device", C.c_int32)]
 
 
 def load():
@@ -56,6 +56,7 @@ def load():
     lib.psx_world_write_bodies.argtypes = [vp, vp, vp, vp, vp]
     lib.psx_world_simulate_host.argtypes = [vp, C.c_float, vp, vp, vp, vp]
     lib.psx_world_counts.argtypes = [vp, vp]
+    lib.psx_world_step_timed.argtypes = [vp, C.c_float, C.c_int32, vp, vp, vp]
     lib.psx_world_get_pairs.argtypes = [vp, vp, C.c_int32]
     lib.psx_world_get_pairs.restype = C.c_int32
     lib.psx_world_get_contacts.argtypes = [vp, vp, vp, vp, C.c_int32]
@@ -82,7 +83,8 @@ class World:
 
     h = None
 
-    def __init__(self, scenes, pairs_per_collider=0, manifolds_per_collider=0, block_scene_max_dyn=0, use_graph=False):
+    def __init__(self, scenes, pairs_per_collider=0, manifolds_per_collider=0, block_scene_max_dyn=0, use_graph=False,
+                 device=0):
         lib = load()
         if not isinstance(scenes, (list, tuple)):
             scenes = [scenes]
@@ -91,7 +93,8 @@ class World:
         for i, s in enumerate(scenes):
             arr[i] = make_desc(s)
         self._descs = arr
-        opts = PsxWorldOpts(pairs_per_collider, manifolds_per_collider, block_scene_max_dyn, 1 if use_graph else 0)
+        opts = PsxWorldOpts(pairs_per_collider, manifolds_per_collider, block_scene_max_dyn, 1 if use_graph else 0,
+                            device)
         h = C.c_void_p()
         _check(lib.psx_world_create(arr, len(scenes), C.byref(opts), C.byref(h)))
         self.h = h
@@ -112,6 +115,16 @@ class World:
     def step(self, dt=None, frames=1):
         dt = self.scenes[0].dt if dt is None else dt
         _check(load().psx_world_step(self.h, C.c_float(dt), frames))
+
+    def step_timed(self, dt=None, frames=1):
+        """Step `frames` frames timed with CUDA events on the world's stream.
+        Returns (total_ms, stage_ms[5], kernels queued)."""
+        dt = self.scenes[0].dt if dt is None else dt
+        tot = np.zeros(1, np.float32)
+        st = np.zeros(5, np.float32)
+        k = np.zeros(1, np.int64)
+        _check(load().psx_world_step_timed(self.h, C.c_float(dt), frames, _p(tot), _p(st), _p(k)))
+        return float(tot[0]), st.astype(np.float64), int(k[0])
 
     def synchronize(self):
         _check(load().psx_world_synchronize(self.h))
@@ -136,9 +149,10 @@ class World:
                                               _p(st["ang_vel"])))
 
     def counts(self):
-        c = np.zeros(8, np.int32)
+        c = np.zeros(12, np.int32)
         _check(load().psx_world_counts(self.h, _p(c)))
-        keys = ["bodies", "colliders", "dynamic", "joints", "scenes", "pairs", "manifolds", "error"]
+        keys = ["bodies", "colliders", "dynamic", "joints", "scenes", "pairs", "manifolds", "error", "points", "rows",
+                "simulated", "kernels"]
         return dict(zip(keys, (int(v) for v in c)))
 
     def pairs(self):

@@ -49,9 +49,10 @@ __global__ void k_aabb(World w, int margin_mode) {
     w.aabb_max[c] = st4(b.max);
 }
 
-void launch_aabb(const World& w, int margin_mode, cudaStream_t s) {
-    if (w.n_colliders == 0) return;
+int launch_aabb(const World& w, int margin_mode, cudaStream_t s) {
+    if (w.n_colliders == 0) return 0;
     k_aabb<<<(w.n_colliders + 255) / 256, 256, 0, s>>>(w, margin_mode);
+    return 1;
 }
 
 // ---------------------------------------------------------------- Morton keys
@@ -260,19 +261,20 @@ __global__ void k_pairs_check(FrameBuf f, int* err) {
     if (*f.n_pairs > f.pair_cap) { atomicOr(err, ERR_PAIR_CAPACITY); *f.n_pairs = f.pair_cap; }
 }
 
-void launch_broadphase(const World& w, FrameBuf& f, int mbits, int total_bits, cudaStream_t s) {
+int launch_broadphase(const World& w, FrameBuf& f, int mbits, int total_bits, cudaStream_t s) {
     int n = w.n_colliders;
-    if (n == 0) return;
+    if (n == 0) return 0;
     int nb = (n + 255) / 256;
     k_scene_bounds<<<w.n_scenes, 256, 0, s>>>(w, f);
     k_morton<<<nb, 256, 0, s>>>(w, f, mbits);
-    radix_sort_pairs(f.keys, f.order, f.keys_tmp, f.order_tmp, n, total_bits, f.radix_hist, s);
+    int k = 2 + radix_sort_pairs(f.keys, f.order, f.keys_tmp, f.order_tmp, n, total_bits, f.radix_hist, s);
     k_karras<<<nb, 256, 0, s>>>(w, f);
     k_refit<<<nb, 256, 0, s>>>(w, f);
     k_traverse<false><<<nb, 256, 0, s>>>(w, f);
     scan_exclusive(f.leaf_cnt, f.leaf_off, n, f.n_pairs, f.scan_scratch, s);
     k_traverse<true><<<nb, 256, 0, s>>>(w, f);
     k_pairs_check<<<1, 1, 0, s>>>(f, w.err);
+    return k + 4 + 3 + 1;
 }
 
 }  // namespace psx

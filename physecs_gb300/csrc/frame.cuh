@@ -64,16 +64,20 @@ struct FrameBuf {
     int* cache_parity;
     // grid barrier: count, generation, flag
     unsigned int* bar;
+    // per-frame totals: contact points, joint rows (for throughput accounting)
+    int* n_points;
+    int* n_rows;
 };
 
-// kernel launch helpers (definitions in the .cu files)
-void launch_aabb(const World& w, int margin_mode, cudaStream_t s);
-void launch_broadphase(const World& w, FrameBuf& f, int mbits, int total_bits, cudaStream_t s);
-void launch_narrowphase(const World& w, FrameBuf& f, cudaStream_t s);
-void launch_contacts(const World& w, FrameBuf& f, cudaStream_t s);
-void launch_solver(const World& w, FrameBuf& f, const int* block_scenes, int n_block_scenes, const int* grid_scenes,
-                   int n_grid_scenes, int grid_blocks, cudaStream_t s);
+// kernel launch helpers (definitions in the .cu files); each returns the number of
+// kernels it queued
+int launch_aabb(const World& w, int margin_mode, cudaStream_t s);
+int launch_broadphase(const World& w, FrameBuf& f, int mbits, int total_bits, cudaStream_t s);
+int launch_narrowphase(const World& w, FrameBuf& f, cudaStream_t s);
+int launch_contacts(const World& w, FrameBuf& f, cudaStream_t s);
+int launch_solver(const World& w, FrameBuf& f, const int* block_scenes, int n_block_scenes, const int* grid_scenes,
+                  int n_grid_scenes, int grid_blocks, cudaStream_t s);
 int solver_grid_blocks();
-void launch_joint_layout(const World& w, cudaStream_t s);
+int launch_joint_layout(const World& w, FrameBuf& f, cudaStream_t s);
 
 }  // namespace psx

@@ -171,8 +171,8 @@ size_t radix_hist_ints(int n) {
     return 2 * h + scan_scratch_ints((int)h) + 1;
 }
 
-void radix_sort_pairs(uint32_t* keys, int* vals, uint32_t* tmpk, int* tmpv, int n, int bits, int* hist, cudaStream_t s) {
-    if (n <= 0) return;
+int radix_sort_pairs(uint32_t* keys, int* vals, uint32_t* tmpk, int* tmpv, int n, int bits, int* hist, cudaStream_t s) {
+    if (n <= 0) return 0;
     int ntiles = (n + kTile - 1) / kTile;
     int h = 256 * ntiles;
     int* offs = hist + h;
@@ -192,6 +192,7 @@ void radix_sort_pairs(uint32_t* keys, int* vals, uint32_t* tmpk, int* tmpv, int 
         cudaMemcpyAsync(keys, ka, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s);
         cudaMemcpyAsync(vals, va, sizeof(int) * n, cudaMemcpyDeviceToDevice, s);
     }
+    return passes * 5;
 }
 
 }  // namespace psx

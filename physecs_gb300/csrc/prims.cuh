@@ -15,8 +15,9 @@ void scan_exclusive_dev(const int* in, int* out, const int* n_dev, int n_max, in
 
 // Stable LSD radix sort of (key, value) pairs over bits [0, bits).  The result ends
 // up in (keys, vals); tmp buffers hold n elements each; hist needs radix_hist_ints(n).
+// Returns the number of kernels queued.
 size_t radix_hist_ints(int n);
-void radix_sort_pairs(uint32_t* keys, int* vals, uint32_t* tmpk, int* tmpv, int n, int bits, int* hist, cudaStream_t s);
+int radix_sort_pairs(uint32_t* keys, int* vals, uint32_t* tmpk, int* tmpv, int n, int bits, int* hist, cudaStream_t s);
 
 // Grid-wide barrier for cooperative launches.  Every block calls it; the wait is
 // bounded: after ~0.5 s without progress the barrier records ERR_BARRIER_TIMEOUT in

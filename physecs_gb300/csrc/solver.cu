@@ -132,6 +132,7 @@ __global__ void k_build_contacts(World w, FrameBuf f) {
             if (!placed) atomicOr(w.err, ERR_CACHE_CAPACITY);
             f.contacts[idx] = c;
             atomicAdd(&f.man_scene_cnt[iA.w], 1);
+            atomicAdd(f.n_points, m.np);
         }
     }
 }
@@ -140,7 +141,7 @@ __global__ void k_build_contacts(World w, FrameBuf f) {
 
 // getSolverDesc of each joint type (src/Joints/*.cpp): row flags in creation order,
 // evaluated at frame start; the prismatic limit row exists only while violated.
-__global__ void k_joint_layout(World w) {
+__global__ void k_joint_layout(World w, int* n_rows) {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= w.n_joints) return;
     JointDev J = w.joints[j];
@@ -170,6 +171,7 @@ __global__ void k_joint_layout(World w) {
         default: add(RN, 3); add(RA, 2); add(RA | RS, 1); break;                      // servo
     }
     J.nrows = n;
+    atomicAdd(n_rows, n);
     for (int i = 0; i < kMaxRowsPerJoint; ++i) J.rowflags[i] = i < n ? f[i] : -1;
     w.joints[j].makeUpper = J.makeUpper;
     w.joints[j].makeLower = J.makeLower;
@@ -190,8 +192,11 @@ __global__ void k_joint_layout(World w) {
     }
 }
 
-void launch_joint_layout(const World& w, cudaStream_t s) {
-    if (w.n_joints) k_joint_layout<<<(w.n_joints + 127) / 128, 128, 0, s>>>(w);
+int launch_joint_layout(const World& w, FrameBuf& f, cudaStream_t s) {
+    cudaMemsetAsync(f.n_rows, 0, sizeof(int), s);
+    if (!w.n_joints) return 0;
+    k_joint_layout<<<(w.n_joints + 127) / 128, 128, 0, s>>>(w, f.n_rows);
+    return 1;
 }
 
 __device__ __forceinline__ float angleDiffD(float a0, float a1) {  // GearJoint.cpp:5-8
@@ -774,11 +779,13 @@ __global__ void k_zero_ints(int* p, int n) {
     if (i < n) p[i] = 0;
 }
 
-void launch_contacts(const World& w, FrameBuf& f, cudaStream_t s) {
+int launch_contacts(const World& w, FrameBuf& f, cudaStream_t s) {
     k_cache_clear<<<(f.cache_cap + 255) / 256, 256, 0, s>>>(f);
     k_zero_ints<<<(w.n_scenes + 256) / 256, 256, 0, s>>>(f.man_scene_cnt, w.n_scenes + 1);
+    k_zero_ints<<<1, 32, 0, s>>>(f.n_points, 1);
     k_build_contacts<<<1216, 128, 0, s>>>(w, f);
     scan_exclusive(f.man_scene_cnt, f.scene_man, w.n_scenes + 1, nullptr, f.scan_scratch, s);
+    return 4 + 3;
 }
 
 int solver_grid_blocks() {
@@ -790,15 +797,20 @@ int solver_grid_blocks() {
     return sms * per;
 }
 
-void launch_solver(const World& w, FrameBuf& f, const int* block_scenes, int n_block_scenes, const int* grid_scenes,
-                   int n_grid_scenes, int grid_blocks, cudaStream_t s) {
+int launch_solver(const World& w, FrameBuf& f, const int* block_scenes, int n_block_scenes, const int* grid_scenes,
+                  int n_grid_scenes, int grid_blocks, cudaStream_t s) {
     k_zero_ints<<<(w.n_scenes * (kMaxColors + 1) + 255) / 256, 256, 0, s>>>(f.claim_pos, w.n_scenes * (kMaxColors + 1));
-    if (n_block_scenes) k_solve_block<<<n_block_scenes, 256, 0, s>>>(w, f, block_scenes);
+    int k = 2;
+    if (n_block_scenes) { k_solve_block<<<n_block_scenes, 256, 0, s>>>(w, f, block_scenes); ++k; }
     if (n_grid_scenes) {
-        void* args[] = {(void*)&w, (void*)&f, (void*)&grid_scenes, (void*)&n_grid_scenes};
+        World wc = w;
+        FrameBuf fc = f;
+        void* args[] = {(void*)&wc, (void*)&fc, (void*)&grid_scenes, (void*)&n_grid_scenes};
         cudaLaunchCooperativeKernel((void*)k_solve_grid, grid_blocks, 256, args, 0, s);
+        ++k;
     }
     k_cache_flip<<<1, 1, 0, s>>>(f);
+    return k;
 }
 
 }  // namespace psx

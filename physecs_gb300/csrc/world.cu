@@ -161,6 +161,10 @@ struct psx_world {
     // pinned staging for body transfers
     float4* pin = nullptr;
     size_t pin_n = 0;
+    int device = 0;
+    long long launches = 0;          // kernels queued since creation
+    int n_simulated = 0;             // dynamic, non-kinematic bodies
+    std::vector<cudaEvent_t> events; // stage events of timed steps
 
     template <class T>
     psx_status alloc(T*& p, size_t n) {
@@ -180,6 +184,7 @@ struct psx_world {
         return PSX_OK;
     }
     ~psx_world() {
+        for (cudaEvent_t e : events) cudaEventDestroy(e);
         if (graph) cudaGraphExecDestroy(graph);
         for (void* p : allocs) cudaFree(p);
         if (pin) cudaFreeHost(pin);
@@ -285,6 +290,7 @@ static psx_status build_world(psx_world* W, const psx_scene_desc* scenes, int S,
             bool dyn = fl & PSX_BODY_DYNAMIC;
             bool sim = dyn && !(fl & PSX_BODY_KINEMATIC);
             int di = -1;
+            if (sim) ++W->n_simulated;
             pos.push_back(f4(d.pos[3 * b], d.pos[3 * b + 1], d.pos[3 * b + 2]));
             quat.push_back(f4(d.quat[4 * b], d.quat[4 * b + 1], d.quat[4 * b + 2], d.quat[4 * b + 3]));
             if (dyn) {
@@ -495,6 +501,10 @@ static psx_status build_world(psx_world* W, const psx_scene_desc* scenes, int S,
     PSX_TRY(W->alloc(f.cache_b, f.cache_cap));
     PSX_TRY(W->alloc(f.cache_parity, 1));
     PSX_TRY(W->alloc(f.bar, 4));
+    PSX_TRY(W->alloc(f.n_points, 1));
+    PSX_TRY(W->alloc(f.n_rows, 1));
+    PSX_CUDA(cudaMemset(f.n_points, 0, sizeof(int)));
+    PSX_CUDA(cudaMemset(f.n_rows, 0, sizeof(int)));
     PSX_CUDA(cudaMemset(f.bar, 0, 4 * sizeof(unsigned)));
     PSX_CUDA(cudaMemset(f.cache_parity, 0, sizeof(int)));
     PSX_CUDA(cudaMemset(f.cache_a, 0xff, sizeof(CacheEntry) * (size_t)f.cache_cap));
@@ -519,14 +529,27 @@ static psx_status build_world(psx_world* W, const psx_scene_desc* scenes, int S,
     return PSX_OK;
 }
 
-static void queue_frame(psx_world* W) {
-    launch_broadphase(W->w, W->f, W->mbits, W->total_bits, W->stream);
-    launch_narrowphase(W->w, W->f, W->stream);
-    launch_contacts(W->w, W->f, W->stream);
-    launch_joint_layout(W->w, W->stream);
-    launch_solver(W->w, W->f, W->block_scenes, (int)W->block_scenes_h.size(), W->grid_scenes, (int)W->grid_scenes_h.size(),
-                  W->grid_blocks, W->stream);
-    launch_aabb(W->w, 1, W->stream);
+// One frame = Scene::simulate for every scene: broadphase, narrowphase, contact rows,
+// joint layout, the solver kernel (colouring + all substeps), end-of-frame bounds.
+// ev (optional) receives 6 events delimiting the 5 stages.  Returns kernels queued.
+static int queue_frame(psx_world* W, cudaEvent_t* ev = nullptr) {
+    int k = 0;
+    cudaStream_t s = W->stream;
+    if (ev) cudaEventRecord(ev[0], s);
+    k += launch_broadphase(W->w, W->f, W->mbits, W->total_bits, s);
+    if (ev) cudaEventRecord(ev[1], s);
+    k += launch_narrowphase(W->w, W->f, s);
+    if (ev) cudaEventRecord(ev[2], s);
+    k += launch_contacts(W->w, W->f, s);
+    k += launch_joint_layout(W->w, W->f, s);
+    if (ev) cudaEventRecord(ev[3], s);
+    k += launch_solver(W->w, W->f, W->block_scenes, (int)W->block_scenes_h.size(), W->grid_scenes,
+                       (int)W->grid_scenes_h.size(), W->grid_blocks, s);
+    if (ev) cudaEventRecord(ev[4], s);
+    k += launch_aabb(W->w, 1, s);
+    if (ev) cudaEventRecord(ev[5], s);
+    W->launches += k;
+    return k;
 }
 
 static psx_status check_err(psx_world* W) {
@@ -560,7 +583,10 @@ PSX_API psx_status psx_world_create(const psx_scene_desc* scenes, int32_t n_scen
     if (o.block_scene_max_dyn <= 0) o.block_scene_max_dyn = 8192;
     int dev_count = 0;
     if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0) return fail(PSX_ERR_CUDA, "no CUDA device");
+    if (o.device < 0 || o.device >= dev_count) return fail(PSX_ERR_INVALID_ARG, "device ordinal");
+    if (cudaSetDevice(o.device) != cudaSuccess) return fail(PSX_ERR_CUDA, "cudaSetDevice");
     psx_world* W = new psx_world();
+    W->device = o.device;
     W->use_graph = o.use_graph != 0;
     cudaError_t e = cudaStreamCreateWithFlags(&W->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { delete W; return fail(PSX_ERR_CUDA, cudaGetErrorString(e)); }
@@ -571,6 +597,7 @@ PSX_API psx_status psx_world_create(const psx_scene_desc* scenes, int32_t n_scen
 }
 
 PSX_API psx_status psx_world_destroy(psx_world* w) {
+    if (w) cudaSetDevice(w->device);
     if (!w) return fail(PSX_ERR_INVALID_ARG, "null world");
     cudaStreamSynchronize(w->stream);
     delete w;
@@ -578,6 +605,7 @@ PSX_API psx_status psx_world_destroy(psx_world* w) {
 }
 
 PSX_API psx_status psx_world_set_knobs(psx_world* W, int32_t scene, int32_t substeps, int32_t iterations, float gravity) {
+    if (W) cudaSetDevice(W->device);
     if (!W || substeps <= 0 || iterations < 0 || scene >= W->n_scenes) return fail(PSX_ERR_INVALID_ARG, "set_knobs");
     for (int s = 0; s < W->n_scenes; ++s) {
         if (scene >= 0 && s != scene) continue;
@@ -588,6 +616,7 @@ PSX_API psx_status psx_world_set_knobs(psx_world* W, int32_t scene, int32_t subs
 }
 
 PSX_API psx_status psx_world_step(psx_world* W, float dt, int32_t frames) {
+    if (W) cudaSetDevice(W->device);
     if (!W || frames < 0) return fail(PSX_ERR_INVALID_ARG, "psx_world_step");
     if (W->knobs_dirty || W->h_knobs.empty() || W->h_knobs[0].w != dt) {
         for (auto& k : W->h_knobs) k.w = dt;
@@ -613,7 +642,42 @@ PSX_API psx_status psx_world_step(psx_world* W, float dt, int32_t frames) {
     return PSX_OK;
 }
 
+PSX_API psx_status psx_world_step_timed(psx_world* W, float dt, int32_t frames, float* total_ms, float* stage_ms,
+                                        int64_t* kernels) {
+    if (!W || frames <= 0) return fail(PSX_ERR_INVALID_ARG, "psx_world_step_timed");
+    if (W->knobs_dirty || W->h_knobs.empty() || W->h_knobs[0].w != dt) {
+        for (auto& k : W->h_knobs) k.w = dt;
+        PSX_CUDA(cudaMemcpyAsync(W->w.knobs, W->h_knobs.data(), sizeof(float4) * W->h_knobs.size(), cudaMemcpyHostToDevice, W->stream));
+        W->knobs_dirty = false;
+    }
+    size_t need = 6 * (size_t)frames;
+    while (W->events.size() < need) {
+        cudaEvent_t e;
+        PSX_CUDA(cudaEventCreate(&e));
+        W->events.push_back(e);
+    }
+    long long k0 = W->launches;
+    for (int i = 0; i < frames; ++i) queue_frame(W, &W->events[6 * (size_t)i]);
+    PSX_CUDA(cudaGetLastError());
+    PSX_CUDA(cudaEventSynchronize(W->events[6 * (size_t)frames - 1]));
+    float st[5] = {0, 0, 0, 0, 0};
+    for (int i = 0; i < frames; ++i) {
+        for (int s = 0; s < 5; ++s) {
+            float ms = 0;
+            PSX_CUDA(cudaEventElapsedTime(&ms, W->events[6 * i + s], W->events[6 * i + s + 1]));
+            st[s] += ms;
+        }
+    }
+    float tot = 0;
+    PSX_CUDA(cudaEventElapsedTime(&tot, W->events[0], W->events[6 * (size_t)frames - 1]));
+    if (total_ms) *total_ms = tot;
+    if (stage_ms) for (int s = 0; s < 5; ++s) stage_ms[s] = st[s];
+    if (kernels) *kernels = W->launches - k0;
+    return check_err(W);
+}
+
 PSX_API psx_status psx_world_synchronize(psx_world* W) {
+    if (W) cudaSetDevice(W->device);
     if (!W) return fail(PSX_ERR_INVALID_ARG, "null world");
     PSX_CUDA(cudaStreamSynchronize(W->stream));
     return check_err(W);
@@ -647,11 +711,13 @@ static psx_status read_bodies(psx_world* W, float* pos, float* quat, float* vel,
 }
 
 PSX_API psx_status psx_world_read_bodies(psx_world* W, float* pos, float* quat, float* vel, float* ang_vel) {
+    if (W) cudaSetDevice(W->device);
     if (!W) return fail(PSX_ERR_INVALID_ARG, "null world");
     return read_bodies(W, pos, quat, vel, ang_vel, true);
 }
 
 PSX_API psx_status psx_world_write_bodies(psx_world* W, const float* pos, const float* quat, const float* vel, const float* ang) {
+    if (W) cudaSetDevice(W->device);
     if (!W) return fail(PSX_ERR_INVALID_ARG, "null world");
     const World& w = W->w;
     size_t nb = w.n_bodies, nd = w.n_dyn;
@@ -679,6 +745,7 @@ PSX_API psx_status psx_world_write_bodies(psx_world* W, const float* pos, const 
 }
 
 PSX_API psx_status psx_world_simulate_host(psx_world* W, float dt, float* pos, float* quat, float* vel, float* ang) {
+    if (W) cudaSetDevice(W->device);
     PSX_TRY(psx_world_write_bodies(W, pos, quat, vel, ang));
     PSX_TRY(psx_world_step(W, dt, 1));
     PSX_TRY(read_bodies(W, pos, quat, vel, ang, true));
@@ -686,18 +753,25 @@ PSX_API psx_status psx_world_simulate_host(psx_world* W, float dt, float* pos, f
 }
 
 PSX_API psx_status psx_world_counts(psx_world* W, int32_t* counts) {
+    if (W) cudaSetDevice(W->device);
     if (!W || !counts) return fail(PSX_ERR_INVALID_ARG, "counts");
     PSX_CUDA(cudaStreamSynchronize(W->stream));
-    int np = 0, nm = 0, e = 0;
+    int np = 0, nm = 0, e = 0, pts = 0, rows = 0;
     PSX_CUDA(cudaMemcpy(&np, W->f.n_pairs, sizeof(int), cudaMemcpyDeviceToHost));
     PSX_CUDA(cudaMemcpy(&nm, W->f.n_man, sizeof(int), cudaMemcpyDeviceToHost));
     PSX_CUDA(cudaMemcpy(&e, W->w.err, sizeof(int), cudaMemcpyDeviceToHost));
+    PSX_CUDA(cudaMemcpy(&pts, W->f.n_points, sizeof(int), cudaMemcpyDeviceToHost));
+    PSX_CUDA(cudaMemcpy(&rows, W->f.n_rows, sizeof(int), cudaMemcpyDeviceToHost));
     counts[0] = W->w.n_bodies; counts[1] = W->w.n_colliders; counts[2] = W->w.n_dyn; counts[3] = W->w.n_joints;
     counts[4] = W->n_scenes; counts[5] = np; counts[6] = std::min(nm, W->f.man_cap); counts[7] = e;
+    counts[8] = pts; counts[9] = rows;
+    counts[10] = W->n_simulated;
+    counts[11] = (int32_t)std::min<long long>(W->launches, 0x7fffffff);
     return PSX_OK;
 }
 
 PSX_API int32_t psx_world_get_pairs(psx_world* W, int32_t* out, int32_t cap) {
+    if (W) cudaSetDevice(W->device);
     if (!W) return -1;
     cudaStreamSynchronize(W->stream);
     int np = 0;
@@ -720,6 +794,7 @@ PSX_API int32_t psx_world_get_pairs(psx_world* W, int32_t* out, int32_t cap) {
 }
 
 PSX_API int32_t psx_world_get_contacts(psx_world* W, int32_t* ids, float* f, int32_t* meta, int32_t cap) {
+    if (W) cudaSetDevice(W->device);
     if (!W) return -1;
     cudaStreamSynchronize(W->stream);
     int S = W->n_scenes;
@@ -777,6 +852,7 @@ PSX_API int32_t psx_world_get_contacts(psx_world* W, int32_t* ids, float* f, int
 }
 
 PSX_API int32_t psx_world_get_bounds(psx_world* W, float* bounds, int32_t cap) {
+    if (W) cudaSetDevice(W->device);
     if (!W) return -1;
     cudaStreamSynchronize(W->stream);
     int n = W->w.n_colliders;
@@ -793,6 +869,7 @@ PSX_API int32_t psx_world_get_bounds(psx_world* W, float* bounds, int32_t cap) {
 PSX_API psx_status psx_scene_create(const psx_scene_desc* desc, psx_scene** out) { return psx_world_create(desc, 1, nullptr, out); }
 PSX_API psx_status psx_scene_destroy(psx_scene* s) { return psx_world_destroy(s); }
 PSX_API psx_status psx_scene_simulate(psx_scene* s, float dt) {
+    if (s) cudaSetDevice(s->device);
     PSX_TRY(psx_world_step(s, dt, 1));
     return psx_world_synchronize(s);
 }

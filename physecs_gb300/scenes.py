@@ -396,49 +396,76 @@ def _hull_pool(rng: SplitMix64, count=32, points=16):
     return pool
 
 
+_HULL_UNIT = {}
+
+
+def _hull_unit_props(mesh):
+    """Unit-scale mass, COM and inverse inertia (column-major) of a pool hull; cached."""
+    key = id(mesh)
+    if key not in _HULL_UNIT:
+        verts, faces = mesh
+        m, com, I = mass_convex(verts, faces, (1.0, 1.0, 1.0))
+        _HULL_UNIT[key] = (m, com, np.linalg.inv(I).T.ravel())
+    return _HULL_UNIT[key]
+
+
 def _mixed_bodies(s: SceneData, rng: SplitMix64, centers: np.ndarray, hull_base: int, hull_pool,
                   mix=(0.4, 0.3, 0.2, 0.1), material=(0.5, 0.0, 0.0)):
-    """Append len(centers) dynamic bodies with the config-2 shape mix and size distributions."""
+    """Append len(centers) dynamic bodies with the config-2 shape mix and size distributions.
+
+    Mass properties follow src/MassUtil.cpp for one collider at the body origin; a hull
+    scaled uniformly by s has mass m1*s^3, COM com1*s and inertia I1*s^5."""
     n = len(centers)
     u = rng.uniform(n)
     c = np.cumsum(mix)
     kind = np.where(u < c[0], BOX, np.where(u < c[1], SPHERE, np.where(u < c[2], CAPSULE, CONVEX_MESH)))
     q = rng.quaternions(n)
     a, b, cc = rng.uniform(n), rng.uniform(n), rng.uniform(n)
-    hp = rng.next_u64(n) % np.uint64(len(hull_pool))
+    hp = (rng.next_u64(n) % np.uint64(len(hull_pool))).astype(np.int64)
     params = np.zeros((n, 4))
     mesh = np.full(n, -1, np.int32)
     inv_mass = np.zeros(n)
     com = np.zeros((n, 3))
     invI = np.zeros((n, 9))
-    hull_cache = {}
-    for i in range(n):
-        k = kind[i]
-        if k == BOX:
-            he = (0.25 + 0.75 * a[i], 0.25 + 0.75 * b[i], 0.25 + 0.75 * cc[i])
-            params[i, :3] = he
-            m, cm, I = mass_box(he)
-        elif k == SPHERE:
-            r = 0.25 + 0.5 * a[i]
-            params[i, 0] = r
-            m, cm, I = mass_sphere(r)
-        elif k == CAPSULE:
-            r, hh = 0.2 + 0.3 * a[i], 0.25 + 0.75 * b[i]
-            params[i, 0], params[i, 1] = hh, r
-            m, cm, I = mass_capsule(hh, r)
-        else:
-            sc = 0.5 + a[i]
-            params[i, :3] = sc
-            h = int(hp[i])
-            mesh[i] = hull_base + h
-            key = (h, round(sc * 1e6))
-            if key not in hull_cache:
-                verts, faces = hull_pool[h]
-                hull_cache[key] = mass_convex(verts, faces, (sc, sc, sc))
-            m, cm, I = hull_cache[key]
-        inv_mass[i] = 1.0 / m
-        com[i] = cm
-        invI[i] = _inv3(I)
+    def diag_inv(sel, dx, dy, dz):
+        invI[sel, 0], invI[sel, 4], invI[sel, 8] = 1.0 / dx, 1.0 / dy, 1.0 / dz
+    sel = kind == BOX
+    if sel.any():
+        hx, hy, hz = 0.25 + 0.75 * a[sel], 0.25 + 0.75 * b[sel], 0.25 + 0.75 * cc[sel]
+        params[sel, 0], params[sel, 1], params[sel, 2] = hx, hy, hz
+        m = DENSITY * 8.0 * hx * hy * hz
+        k = m / 12.0
+        inv_mass[sel] = 1.0 / m
+        diag_inv(sel, k * (hy * hy + hz * hz), k * (hx * hx + hz * hz), k * (hx * hx + hy * hy))
+    sel = kind == SPHERE
+    if sel.any():
+        r = 0.25 + 0.5 * a[sel]
+        params[sel, 0] = r
+        m = DENSITY * 4.0 * math.pi * r ** 3 / 3.0
+        i = 2.0 * m * r * r / 5.0
+        inv_mass[sel] = 1.0 / m
+        diag_inv(sel, i, i, i)
+    sel = kind == CAPSULE
+    if sel.any():
+        r, hh = 0.2 + 0.3 * a[sel], 0.25 + 0.75 * b[sel]
+        params[sel, 0], params[sel, 1] = hh, r
+        vc = 2 * r * r * math.pi * hh
+        vs = 4 * r ** 3 * math.pi / 3.0
+        m = DENSITY * (vc + vs)
+        mc, ms = vc * m / (vc + vs), vs * m / (vc + vs)
+        ixx = mc * (hh * hh / 3.0 + r * r / 4.0) + ms * (hh * hh + 3.0 * hh * r / 4.0 + 2 * r * r / 5.0)
+        iyy = mc * r * r / 2.0 + ms * 2 * r * r / 5.0
+        inv_mass[sel] = 1.0 / m
+        diag_inv(sel, ixx, iyy, ixx)
+    for i in np.nonzero(kind == CONVEX_MESH)[0]:
+        sc = 0.5 + a[i]
+        params[i, :3] = sc
+        h = int(hp[i])
+        mesh[i] = hull_base + h
+        m1, com1, inv1 = _hull_unit_props(hull_pool[h])
+        inv_mass[i] = 1.0 / (m1 * sc ** 3)
+        com[i] = com1 * sc
+        invI[i] = inv1 / sc ** 5
     return s.add_bodies(pos=centers, quat=q, flags=BODY_DYNAMIC, inv_mass=inv_mass, com=com,
                         inv_inertia=invI, col_type=kind.astype(np.int32), col_params=params, col_mesh=mesh,
                         material=material)

@@ -44,7 +44,7 @@ def _oracle(s):
 
 def _gpu(s, **kw):
     from physecs_gb300.api import World
-    return World([s], **kw)
+    return World(s if isinstance(s, list) else [s], **kw)
 
 
 @pytest.mark.parametrize("name", ["pyramid", "mixed", "chain", "heightfield", "joints"])
