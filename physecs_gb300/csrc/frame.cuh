@@ -51,7 +51,7 @@ struct FrameBuf {
     int* man_scene_cnt;   // [S]
     int* scene_man;       // [S+1]
     // colouring
-    int* claim;           // [n_dyn]
+    unsigned long long* claim;  // [n_dyn] (hashed priority << 32 | contact index)
     int* color_of;        // [man_cap]
     int* corder;          // [man_cap] manifolds sorted by (scene, colour, index)
     int* scene_ncolor;    // [S]

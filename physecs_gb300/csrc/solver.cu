@@ -670,8 +670,11 @@ __device__ void solve_scene(const World& w, FrameBuf& f, int s, const S& sy) {
     int substeps = (int)kn.x, iterations = (int)kn.y;
     float g = kn.z, dt = kn.w;
     int* colstart = f.color_start + s * (kMaxColors + 1);
-    // ---- graph colouring of the contacts: rounds of body claims, lowest index wins
-    for (int d = ds + tid; d < de; d += nth) f.claim[d] = 0x7fffffff;
+    // ---- graph colouring of the contacts: rounds in which every uncoloured contact claims
+    // its dynamic bodies with a hashed priority; a contact that holds all its bodies takes
+    // the round's colour.  Hashed (not index) priorities keep the round count logarithmic.
+    const unsigned long long kFree = ~0ull;
+    for (int d = ds + tid; d < de; d += nth) f.claim[d] = kFree;
     for (int m = ms + tid; m < me; m += nth) f.color_of[m] = -1;
     sy.sync();
     int ncol = 0;
@@ -679,20 +682,21 @@ __device__ void solve_scene(const World& w, FrameBuf& f, int s, const S& sy) {
         for (int m = ms + tid; m < me; m += nth) {
             if (f.color_of[m] >= 0) continue;
             const Contact& c = f.contacts[m];
-            if (c.b0 >= 0) atomicMin(&f.claim[c.b0], m);
-            if (c.b1 >= 0) atomicMin(&f.claim[c.b1], m);
+            unsigned long long pri = ((unsigned long long)cache_hash((unsigned long long)m * 0x9E3779B97F4A7C15ull + ncol) << 32) | (unsigned)m;
+            if (c.b0 >= 0) atomicMin(&f.claim[c.b0], pri);
+            if (c.b1 >= 0) atomicMin(&f.claim[c.b1], pri);
         }
         sy.sync();
         bool left = false;
         for (int m = ms + tid; m < me; m += nth) {
             if (f.color_of[m] >= 0) continue;
             const Contact& c = f.contacts[m];
-            bool ok = (c.b0 < 0 || f.claim[c.b0] == m) && (c.b1 < 0 || f.claim[c.b1] == m);
+            bool ok = (c.b0 < 0 || (unsigned)f.claim[c.b0] == (unsigned)m) && (c.b1 < 0 || (unsigned)f.claim[c.b1] == (unsigned)m);
             if (ok && ncol < kMaxColors) f.color_of[m] = ncol;
             else left = true;
         }
         bool any = sy.any(left);
-        for (int d = ds + tid; d < de; d += nth) f.claim[d] = 0x7fffffff;
+        for (int d = ds + tid; d < de; d += nth) f.claim[d] = kFree;
         ++ncol;
         sy.sync();
         if (!any) break;

@@ -31,7 +31,7 @@ constexpr int kMaxPoly = 64;       // polygon vertices after clipping (reference
 constexpr int kTriManifolds = 16;  // manifolds one body may produce against one triangle mesh
 constexpr int kTriCandidates = 64; // candidate triangles per body-mesh pair
 constexpr int kMaxRowsPerJoint = 8;
-constexpr int kMaxColors = 64;     // contact colours per scene
+constexpr int kMaxColors = 128;    // contact colours per scene
 
 struct ConvexMeshDev {   // one ConvexMesh
     int vert_start, vert_count_padded, vert_count;
