@@ -1,0 +1,136 @@
+#!/usr/bin/env python3
+"""Generate golden fixtures from the UNMODIFIED Physecs reference (oracle/_ref).
+
+Physecs ships no tests and no golden vectors, so every fixture here is produced
+by running the reference itself (built from its own sources by
+oracle/ref/build_ref.py) on seeded scenes from physecs_gb300.scenes:
+
+  frames_<name>.npz    creation bounds, first-frame pair set and contact rows,
+                       and body state after selected frames, for whole scenes
+  narrow_pairs.npz     manifolds of physecs::collision for every shape pair at
+                       seeded touching poses (known-answer tests)
+
+Run in a checkout with the reference present:  python tests/golden/make_golden.py
+"""
+import hashlib
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from physecs_gb300 import scenes  # noqa: E402
+
+
+def scene_hash(s):
+    h = hashlib.sha256()
+    for k in sorted(s.arrays):
+        h.update(k.encode())
+        h.update(np.ascontiguousarray(s.arrays[k]).tobytes())
+    return h.hexdigest()
+
+
+def golden_scenes():
+    """name -> (scene, frames at which state is recorded)."""
+    return {
+        "pyramid": (scenes.pyramid(), [1, 2, 5, 10, 30, 60]),
+        "mixed_a": (scenes.batch_scene(101, n_bodies=60), [1, 5, 20]),
+        "mixed_b": (scenes.batch_scene(202, n_bodies=120), [1, 5, 20]),
+        "chain": (scenes.batch_scene(303, n_bodies=30, chain_prob=1.0), [1, 5, 20]),
+        "joints": (scenes.joint_chains(n_chains=12, links=6), [1, 5, 20, 40]),
+        "heightfield": (scenes.large_mixed(n_bodies=300, cells=32), [1, 3, 6]),
+    }
+
+
+def pair_poses(rng, n):
+    """Seeded poses that put two unit-ish shapes within touching distance."""
+    p0 = np.zeros((n, 3))
+    d = rng.normal(3 * n).reshape(n, 3)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    p1 = d * rng.uniform(n, 0.3, 1.6)[:, None]
+    return p0, rng.quaternions(n), p1, rng.quaternions(n)
+
+
+def narrow_kat():
+    from oracle.ref.ref_api import RefScene
+    rng = scenes.SplitMix64(0x5EED0000 + 99)
+    hull = scenes.convex_hull(np.asarray(scenes._hull_pool(scenes.SplitMix64(7), count=1)[0][0]))
+    box_hull = scenes.box_hull((0.5, 0.4, 0.3))
+    shapes = {
+        "sphere": (scenes.SPHERE, [0.5], None),
+        "capsule": (scenes.CAPSULE, [0.4, 0.3], None),
+        "box": (scenes.BOX, [0.5, 0.4, 0.3], None),
+        "hull": (scenes.CONVEX_MESH, [0.8, 0.8, 0.8], hull),
+        "boxhull": (scenes.CONVEX_MESH, [1.0, 1.0, 1.0], box_hull),
+    }
+    out = {}
+    n = 40
+    for a, (ta, pa, ma) in shapes.items():
+        for b, (tb, pb, mb) in shapes.items():
+            p0, q0, p1, q1 = pair_poses(rng, n)
+            rows_ids, rows_f = [], []
+            for i in range(n):
+                s = scenes.pair_scene(ta, pa, (p0[i], q0[i]), tb, pb, (p1[i], q1[i]), mesh0=ma, mesh1=mb)
+                r = RefScene(s)
+                ids, f = r.collide([[0, 0, 1, 0]])
+                for k in range(len(ids)):
+                    rows_ids.append([i] + list(ids[k][1:3]))
+                    rows_f.append(f[k])
+            key = "%s__%s" % (a, b)
+            out[key + "__poses"] = np.concatenate([p0, q0, p1, q1], axis=1).astype(np.float32)
+            out[key + "__ids"] = np.asarray(rows_ids, np.int32).reshape(-1, 3)
+            out[key + "__f"] = np.asarray(rows_f, np.float32).reshape(-1, 28)
+    # shapes against a small triangle mesh (a 6x6 heightfield patch)
+    tri = scenes.heightfield(scenes.SplitMix64(5), cells=6, amplitude=0.3, lattice=3)
+    for a, (ta, pa, ma) in shapes.items():
+        p0 = np.stack([rng.uniform(n, -2, 2), 0.2 + rng.uniform(n, 0, 0.6), rng.uniform(n, -2, 2)], axis=1)
+        q0 = rng.quaternions(n)
+        rows_ids, rows_f = [], []
+        for i in range(n):
+            s = scenes.pair_scene(ta, pa, (p0[i], q0[i]), scenes.TRIANGLE_MESH, [], ([0, 0, 0], scenes.IDENTITY_Q),
+                                  mesh0=ma, mesh1=(tri[0], tri[1]), dynamic=(True, False))
+            r = RefScene(s)
+            ids, f = r.collide([[0, 0, 1, 0]])
+            for k in range(len(ids)):
+                rows_ids.append([i] + list(ids[k][1:3]))
+                rows_f.append(f[k])
+        key = "%s__trimesh" % a
+        out[key + "__poses"] = np.concatenate([p0, q0, np.zeros((n, 3)), np.tile([0, 0, 0, 1.0], (n, 1))], axis=1).astype(np.float32)
+        out[key + "__ids"] = np.asarray(rows_ids, np.int32).reshape(-1, 3)
+        out[key + "__f"] = np.asarray(rows_f, np.float32).reshape(-1, 28)
+    return out
+
+
+def main():
+    from oracle.ref import build_ref, ref_api
+    if not ref_api.available():
+        build_ref.build()
+    from oracle.ref.ref_api import RefScene
+    for name, (s, frames) in golden_scenes().items():
+        r = RefScene(s)
+        ids, b = r.bounds()
+        rec = {"scene_sha256": np.array(scene_hash(s)), "bounds_ids": ids, "bounds": b}
+        f = 0
+        for target in frames:
+            while f < target:
+                r.step()
+                f += 1
+                if f == 1:
+                    rec["pairs_f1"] = r.pairs()
+                    cid, cf = r.contacts()
+                    rec["contacts_f1_ids"], rec["contacts_f1"] = cid, cf
+            st = r.state()
+            for k, v in st.items():
+                rec["state_f%d_%s" % (f, k)] = v
+        rec["frames"] = np.array(frames, np.int32)
+        np.savez_compressed(os.path.join(HERE, "frames_%s.npz" % name), **rec)
+        print(name, "ok")
+    np.savez_compressed(os.path.join(HERE, "narrow_pairs.npz"), **narrow_kat())
+    print("narrow_pairs ok")
+
+
+if __name__ == "__main__":
+    main()

@@ -136,3 +136,45 @@ def test_one_substep_from_identical_state(gpu_lib, oracle_lib):
     o2.step()
     assert o2.order_error() == 0
     assert rel_state_diff(g.read_bodies(), o2.state()) <= TOL
+
+
+def _kat_scene_list(case):
+    """The known-answer pair scenes of tests/golden/narrow_pairs.npz for one shape pair."""
+    from tests.test_oracle_golden import SHAPES, _load, _meshes
+    poses = _load("narrow_pairs.npz")[case + "__poses"]
+    a, b = case.split("__")
+    meshes = _meshes()
+    ta, pa = SHAPES[a]
+    out = []
+    for p in poses:
+        if b == "trimesh":
+            out.append(scenes.pair_scene(ta, pa, (p[0:3], p[3:7]), scenes.TRIANGLE_MESH, [], ([0, 0, 0], scenes.IDENTITY_Q),
+                                         mesh0=meshes.get(a), mesh1=meshes["trimesh"], dynamic=(True, False)))
+        else:
+            tb, pb = SHAPES[b]
+            out.append(scenes.pair_scene(ta, pa, (p[0:3], p[3:7]), tb, pb, (p[7:10], p[10:14]),
+                                         mesh0=meshes.get(a), mesh1=meshes.get(b)))
+    return out
+
+
+def test_narrowphase_every_shape_pair(gpu_lib, oracle_lib):
+    """Every shape pair at the seeded touching poses of the known-answer fixtures, as one
+    batched world per shape pair: GPU manifolds equal the oracle's (which equal the
+    reference's, checked on the CPU)."""
+    from tests.test_oracle_golden import _kat_cases
+    for case in _kat_cases():
+        ss = _kat_scene_list(case)
+        g = _gpu(ss)
+        g.step(); g.synchronize()
+        ids, gf, meta = g.contacts()
+        total = 0
+        for i, s in enumerate(ss):
+            o = _oracle(s)
+            o.step()
+            sel = ids[:, 0] == i
+            _, of = o.contacts()
+            worst = compare_contacts(gpu_keys(ids[sel], meta[sel]), gf[sel], o.contact_keys(), of)
+            assert worst <= TOL, (case, i, worst)
+            total += int(sel.sum())
+        assert total > 0, case
+        assert g.counts()["error"] == 0, case
