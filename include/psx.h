@@ -182,6 +182,20 @@ PSX_API psx_status psx_world_set_knobs(psx_world* w, int32_t scene, int32_t subs
 PSX_API psx_status psx_world_read_bodies(psx_world* w, float* pos, float* quat, float* vel, float* ang_vel);
 PSX_API psx_status psx_world_write_bodies(psx_world* w, const float* pos, const float* quat, const float* vel,
                                           const float* ang_vel);
+/* The same read as psx_world_read_bodies, for callers that must not allocate while
+ * they run: a frame loop with a hard deadline (cudaMalloc / cudaMallocHost can stall
+ * the device for milliseconds) or a process whose device memory is already handed
+ * out to its own pool.  psx_world_read_bodies grows a pinned staging buffer on first
+ * use; this call instead packs the state on the device into one fixed array that
+ * the library holds for the whole process (3.4 MB per device) and copies from there
+ * into the caller's arrays.  On success it calls no allocator, host or device.
+ *   - Limit: worlds of at most 65536 bodies; larger worlds get PSX_ERR_CAPACITY.
+ *   - The first call on a device looks up that array's device address; make this
+ *     first call before any stream capture begins.
+ *   - Every call in the process shares the array.  Calls whose GPU work overlaps
+ *     (different streams or host threads at once) race on it; serialise them.
+ * It has no counterpart in the reference, where Scene state is host memory. */
+PSX_API psx_status psx_world_read_bodies_noalloc(psx_world* w, float* pos, float* quat, float* vel, float* ang_vel);
 /* One end-to-end simulate through host buffers: upload the given state, step one
  * frame, download the new state into the same buffers, and wait. */
 PSX_API psx_status psx_world_simulate_host(psx_world* w, float dt, float* pos, float* quat, float* vel, float* ang_vel);

@@ -23,7 +23,7 @@ PSX_STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OUT_OF_MEMORY", 3: "CAPACITY", 4: "
 EXPORTS = ["psx_world_create", "psx_world_destroy", "psx_world_step", "psx_world_step_timed", "psx_world_synchronize", "psx_world_set_knobs",
            "psx_world_read_bodies", "psx_world_write_bodies", "psx_world_simulate_host", "psx_world_counts",
            "psx_world_get_pairs", "psx_world_get_contacts", "psx_world_get_bounds", "psx_last_error_string",
-           "psx_scene_create", "psx_scene_destroy", "psx_scene_simulate"]
+           "psx_scene_create", "psx_scene_destroy", "psx_scene_simulate", "psx_world_read_bodies_noalloc"]
 
 _lib = None
 
@@ -54,6 +54,7 @@ def load():
     lib.psx_world_set_knobs.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_float]
     lib.psx_world_read_bodies.argtypes = [vp, vp, vp, vp, vp]
     lib.psx_world_write_bodies.argtypes = [vp, vp, vp, vp, vp]
+    lib.psx_world_read_bodies_noalloc.argtypes = [vp, vp, vp, vp, vp]
     lib.psx_world_simulate_host.argtypes = [vp, C.c_float, vp, vp, vp, vp]
     lib.psx_world_counts.argtypes = [vp, vp]
     lib.psx_world_step_timed.argtypes = [vp, C.c_float, C.c_int32, vp, vp, vp]

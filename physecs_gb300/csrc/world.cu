@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 #include "frame.cuh"
@@ -872,6 +873,95 @@ PSX_API psx_status psx_scene_simulate(psx_scene* s, float dt) {
     if (s) cudaSetDevice(s->device);
     PSX_TRY(psx_world_step(s, dt, 1));
     return psx_world_synchronize(s);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- allocation-free body read
+// psx_world_read_bodies stages through a pinned host buffer that it allocates with
+// cudaMallocHost on first use.  Some callers cannot allocate at all while they run:
+// a render or control loop with a per-frame deadline (cudaMalloc / cudaMallocHost can
+// stall the whole device for milliseconds), or a process whose device memory is
+// reserved up front by its own pool allocator.  psx_world_read_bodies_noalloc serves
+// them: a pack kernel writes the caller's layout into one fixed, file-scope device
+// array, and plain copies move it into the caller's host arrays.
+
+namespace {
+
+constexpr int kNoAllocMaxBodies = 65536;    // bodies one call can read
+constexpr int kNoAllocFloatsPerBody = 13;   // pos 3, quat 4, vel 3, ang_vel 3
+constexpr int kNoAllocMaxDevices = 64;
+
+// 3.4 MB shared by every call in the process on a given device.  It keeps the
+// last call's contents; the pack kernel rewrites every float a call copies out
+// (zero velocities for static bodies included), so nothing stale is returned.
+// Calls that overlap on the GPU (two streams, two host threads) race on it.
+static __device__ __align__(256) float g_noalloc_scratch[kNoAllocMaxBodies * kNoAllocFloatsPerBody];
+
+std::mutex g_noalloc_mu;
+float* g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device, looked up once per device.
+psx_status noalloc_scratch(int device, float** out) {
+    if (device < 0 || device >= kNoAllocMaxDevices) return fail(PSX_ERR_INVALID_ARG, "device index out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[device]) {
+        float* p = nullptr;
+        PSX_CUDA(cudaGetSymbolAddress((void**)&p, g_noalloc_scratch));
+        g_noalloc_addr[device] = p;
+    }
+    *out = g_noalloc_addr[device];
+    return PSX_OK;
+}
+
+// One thread per body; writes pos[3n] | quat[4n] | vel[3n] | ang_vel[3n] into out.
+__global__ void k_pack_bodies(const float4* __restrict__ pos, const float4* __restrict__ quat,
+                              const int4* __restrict__ info, const float4* __restrict__ vel,
+                              const float4* __restrict__ ang, int n, float* __restrict__ out) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= n) return;
+    float* P = out;
+    float* Q = out + 3 * (size_t)n;
+    float* V = out + 7 * (size_t)n;
+    float* A = out + 10 * (size_t)n;
+    float4 p = pos[b], q = quat[b];
+    int d = info[b].z;
+    float4 v = d >= 0 ? vel[d] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 a = d >= 0 ? ang[d] : make_float4(0.f, 0.f, 0.f, 0.f);
+    P[3 * b] = p.x; P[3 * b + 1] = p.y; P[3 * b + 2] = p.z;
+    Q[4 * b] = q.x; Q[4 * b + 1] = q.y; Q[4 * b + 2] = q.z; Q[4 * b + 3] = q.w;
+    V[3 * b] = v.x; V[3 * b + 1] = v.y; V[3 * b + 2] = v.z;
+    A[3 * b] = a.x; A[3 * b + 1] = a.y; A[3 * b + 2] = a.z;
+}
+
+}  // namespace
+
+extern "C" {
+
+PSX_API psx_status psx_world_read_bodies_noalloc(psx_world* W, float* pos, float* quat, float* vel, float* ang_vel) {
+    if (!W) return fail(PSX_ERR_INVALID_ARG, "null world");
+    PSX_CUDA(cudaSetDevice(W->device));
+    const int n = W->w.n_bodies;
+    if (n > kNoAllocMaxBodies) {
+        char buf[160];
+        std::snprintf(buf, sizeof buf, "psx_world_read_bodies_noalloc: world has %d bodies, the limit is %d", n,
+                      kNoAllocMaxBodies);
+        return fail(PSX_ERR_CAPACITY, buf);
+    }
+    if (n == 0) return PSX_OK;
+    float* scratch = nullptr;
+    PSX_TRY(noalloc_scratch(W->device, &scratch));
+    const World& w = W->w;
+    k_pack_bodies<<<(n + 255) / 256, 256, 0, W->stream>>>(w.pos, w.quat, w.info, w.vel, w.ang, n, scratch);
+    PSX_CUDA(cudaGetLastError());
+    W->launches += 1;
+    const size_t fb = sizeof(float);
+    if (pos) PSX_CUDA(cudaMemcpyAsync(pos, scratch, 3 * (size_t)n * fb, cudaMemcpyDeviceToHost, W->stream));
+    if (quat) PSX_CUDA(cudaMemcpyAsync(quat, scratch + 3 * (size_t)n, 4 * (size_t)n * fb, cudaMemcpyDeviceToHost, W->stream));
+    if (vel) PSX_CUDA(cudaMemcpyAsync(vel, scratch + 7 * (size_t)n, 3 * (size_t)n * fb, cudaMemcpyDeviceToHost, W->stream));
+    if (ang_vel) PSX_CUDA(cudaMemcpyAsync(ang_vel, scratch + 10 * (size_t)n, 3 * (size_t)n * fb, cudaMemcpyDeviceToHost, W->stream));
+    PSX_CUDA(cudaStreamSynchronize(W->stream));
+    return PSX_OK;
 }
 
 }  // extern "C"
