@@ -120,9 +120,13 @@ __device__ inline float sqrDistPointToLine(V3 p, V3 a, V3 b) {
 }
 __device__ inline float distPointToPlane(V3 p, V3 o, V3 n) { return fabsf(dot(p - o, n)); }
 __device__ inline bool isZeroF(V3 v) { return (double)length2(v) < 1e-6; }
-__device__ inline bool checkDirection(const Support& s0, const Support& s1, D3 dir, GjkVertex& v) {
+// The GJK routines are generic over the Minkowski-difference support `mk(dir)`, so
+// that the thread-per-pair path (mink of two Supports) and the warp-per-pair path
+// (lane-parallel support search) share one statement of the algorithm.
+template <class MK>
+__device__ inline bool checkDirection(MK& mk, D3 dir, GjkVertex& v) {
     dir = normalize(dir);
-    v = mink(s0, s1, f3(dir));
+    v = mk(f3(dir));
     return dot(v.pos, dir) >= 0;
 }
 __device__ inline bool checkFace(D3 v0, D3 v1, D3 v2, D3 opp, D3& n) {
@@ -137,50 +141,63 @@ __device__ inline bool containsOrigin(GjkSimplex& s, D3& dir, int& fi) {
     if (checkFace(s.v[3].pos, s.v[1].pos, s.v[2].pos, s.v[--fi].pos, dir)) return false;
     return true;
 }
-__device__ inline void completeFromLine(const Support& s0, const Support& s1, GjkSimplex& s) {
+template <class MK>
+__device__ inline void completeFromLine(MK& mk, GjkSimplex& s) {
     D3 dir = cross(s.v[0].pos - s.v[1].pos, D3{0, 1, 0});
     if (isZeroF(f3(dir))) dir = cross(s.v[0].pos - s.v[1].pos, D3{0, 0, 1});
-    s.v[2] = mink(s0, s1, f3(normalize(dir)));
-    if (sqrDistPointToLine(f3(s.v[2].pos), f3(s.v[0].pos), f3(s.v[1].pos)) < 0.00001f) s.v[2] = mink(s0, s1, f3(-dir));
+    s.v[2] = mk(f3(normalize(dir)));
+    if (sqrDistPointToLine(f3(s.v[2].pos), f3(s.v[0].pos), f3(s.v[1].pos)) < 0.00001f) s.v[2] = mk(f3(-dir));
     dir = normalize(cross(s.v[1].pos - s.v[0].pos, s.v[2].pos - s.v[0].pos));
-    s.v[3] = mink(s0, s1, f3(dir));
-    if (distPointToPlane(f3(s.v[3].pos), f3(s.v[0].pos), f3(dir)) < 0.0001f) s.v[3] = mink(s0, s1, f3(-dir));
+    s.v[3] = mk(f3(dir));
+    if (distPointToPlane(f3(s.v[3].pos), f3(s.v[0].pos), f3(dir)) < 0.0001f) s.v[3] = mk(f3(-dir));
 }
 
 // GJK.h:226-292
-__device__ inline bool gjk(const Support& s0, const Support& s1, V3 startDir, GjkSimplex& s) {
+template <class MK>
+__device__ inline bool gjkT(MK& mk, V3 startDir, GjkSimplex& s) {
     D3 dir = d3(normalize(startDir));
-    s.v[0] = mink(s0, s1, f3(dir));
+    s.v[0] = mk(f3(dir));
     if (isZeroF(f3(s.v[0].pos))) {
         dir = -dir;
-        s.v[1] = mink(s0, s1, f3(dir));
-        completeFromLine(s0, s1, s);
+        s.v[1] = mk(f3(dir));
+        completeFromLine(mk, s);
         return true;
     }
     dir = -s.v[0].pos;
-    if (!checkDirection(s0, s1, dir, s.v[1])) return false;
+    if (!checkDirection(mk, dir, s.v[1])) return false;
     dir = cross(cross(s.v[0].pos - s.v[1].pos, -s.v[1].pos), s.v[0].pos - s.v[1].pos);
-    if (isZeroF(f3(dir))) { completeFromLine(s0, s1, s); return true; }
-    if (!checkDirection(s0, s1, dir, s.v[2])) return false;
+    if (isZeroF(f3(dir))) { completeFromLine(mk, s); return true; }
+    if (!checkDirection(mk, dir, s.v[2])) return false;
     dir = cross(s.v[1].pos - s.v[0].pos, s.v[2].pos - s.v[0].pos);
     double sg = signD(dot(-s.v[0].pos, dir));
     if (!sg) {
         dir = normalize(dir);
-        s.v[3] = mink(s0, s1, f3(dir));
-        if (distPointToPlane(f3(s.v[3].pos), f3(s.v[0].pos), f3(dir)) < 0.0001f) s.v[3] = mink(s0, s1, f3(-dir));
+        s.v[3] = mk(f3(dir));
+        if (distPointToPlane(f3(s.v[3].pos), f3(s.v[0].pos), f3(dir)) < 0.0001f) s.v[3] = mk(f3(-dir));
         return true;
     }
     dir = sg * dir;
-    if (!checkDirection(s0, s1, dir, s.v[3])) return false;
+    if (!checkDirection(mk, dir, s.v[3])) return false;
     int fi;
     for (int i = 0; i < 100; ++i) {
         if (containsOrigin(s, dir, fi)) return true;
-        if (!checkDirection(s0, s1, dir, s.v[fi])) return false;
+        if (!checkDirection(mk, dir, s.v[fi])) return false;
         GjkVertex t = s.v[fi];
         s.v[fi] = s.v[3];
         s.v[3] = t;
     }
     return false;
+}
+
+struct PairMink {
+    const Support& s0;
+    const Support& s1;
+    __device__ GjkVertex operator()(V3 dir) const { return mink(s0, s1, dir); }
+};
+
+__device__ inline bool gjk(const Support& s0, const Support& s1, V3 startDir, GjkSimplex& s) {
+    PairMink mk{s0, s1};
+    return gjkT(mk, startDir, s);
 }
 
 // EPA.h:10-186 with fixed capacities (104 vertices = 4 + 100 iterations)
@@ -769,35 +786,36 @@ __device__ inline bool collideAnalytic(V3 pos0, Q4 or0, const GeomD& g0, V3 pos1
     }
 }
 
-// convex-mesh pairs of physecs::collision (Collision.cpp:414-426, 488-499, 787-807, 873-887)
-__device__ inline bool collideConvexOrdered(const World& w, V3 pos0, Q4 or0, const GeomD& g0, V3 pos1, Q4 or1, const GeomD& g1,
-                                            ManifoldL& r, Polytope& poly, int* err) {
-    // g1 is always the convex mesh here
-    Support b = convexSupport(w, pos1, or1, g1.mesh, gv(g1));
-    Support a;
-    M3 basis0 = mat3_cast(or0);
+// convex-mesh pairs of physecs::collision (Collision.cpp:414-426, 488-499, 787-807, 873-887),
+// in three parts: the two supports, GJK + EPA, and the contact generation that
+// follows EPA.  g1 is always the convex mesh here.
+__device__ inline void convexOrderedSupports(const World& w, V3 pos0, Q4 or0, const GeomD& g0, V3 pos1, Q4 or1,
+                                             const GeomD& g1, Support& a, Support& b) {
+    b = convexSupport(w, pos1, or1, g1.mesh, gv(g1));
     switch (g0.type) {
         case G_SPHERE: a.kind = 0; a.pos = pos0; a.radius = g0.p[0]; break;
         case G_CAPSULE: a.kind = 1; a.pos = pos0; a.axis = qrot(or0, {0, 1, 0}); a.halfHeight = g0.p[0]; a.radius = g0.p[1]; break;
-        case G_BOX: a.kind = 2; a.pos = pos0; a.basis = basis0; a.he = gv(g0); break;
+        case G_BOX: a.kind = 2; a.pos = pos0; a.basis = mat3_cast(or0); a.he = gv(g0); break;
         default: a = convexSupport(w, pos0, or0, g0.mesh, gv(g0)); break;
     }
-    GjkSimplex s;
-    if (!gjk(a, b, pos1 - pos0, s)) return false;
-    r.normal = epa(a, b, s, r.points[0].p0, r.points[0].p1, poly, err);
+}
+
+// r.normal and r.points[0] hold the EPA normal and closest points on entry.
+__device__ inline void convexOrderedContacts(const World& w, V3 pos0, Q4 or0, const GeomD& g0, V3 pos1, Q4 or1,
+                                             const GeomD& g1, ManifoldL& r, int* err) {
     switch (g0.type) {
         case G_SPHERE: r.numPoints = 1; break;
         case G_CAPSULE: {
-            M3 c2w = b.basis;
+            M3 c2w = mat3_cast(or1);
             M3 w2c = inverse(c2w);
             V3 p = mv(w2c, pos0 - pos1);
-            V3 al = mv(w2c, a.axis);
+            V3 al = mv(w2c, qrot(or0, {0, 1, 0}));
             capsuleConvexContacts(w, p + al * g0.p[0], p - al * g0.p[0], g0.p[1], pos1, c2w, g1.mesh, gv(g1), r);
             if (!r.numPoints) r.numPoints = 1;
             break;
         }
         case G_BOX:
-            boxConvexContacts(w, pos0, basis0, gv(g0), pos1, or1, g1.mesh, gv(g1), r.normal, r.points, r.numPoints, err);
+            boxConvexContacts(w, pos0, mat3_cast(or0), gv(g0), pos1, or1, g1.mesh, gv(g1), r.normal, r.points, r.numPoints, err);
             if (!r.numPoints) r.numPoints = 1;
             break;
         default:
@@ -805,6 +823,17 @@ __device__ inline bool collideConvexOrdered(const World& w, V3 pos0, Q4 or0, con
             if (!r.numPoints) r.numPoints = 1;
             break;
     }
+}
+
+__device__ inline bool collideConvexOrdered(const World& w, V3 pos0, Q4 or0, const GeomD& g0, V3 pos1, Q4 or1, const GeomD& g1,
+                                            ManifoldL& r, Polytope& poly, int* err) {
+    Support a, b;
+    convexOrderedSupports(w, pos0, or0, g0, pos1, or1, g1, a, b);
+    GjkSimplex s;
+    if (!gjk(a, b, pos1 - pos0, s)) return false;
+    r.normal = epa(a, b, s, r.points[0].p0, r.points[0].p1, poly, err);
+    r.numPoints = 0;
+    convexOrderedContacts(w, pos0, or0, g0, pos1, or1, g1, r, err);
     return true;
 }
 

@@ -9,6 +9,7 @@
 // pose = body pose composed with the collider's local pose.
 #include "frame.cuh"
 #include "narrow_tri.cuh"
+#include "narrow_warp.cuh"
 
 namespace psx {
 
@@ -96,22 +97,75 @@ __global__ void __launch_bounds__(128) k_narrow_analytic(World w, FrameBuf f) {
     }
 }
 
-// convex-mesh pairs: GJK + EPA + clipping
-__global__ void __launch_bounds__(64) k_narrow_convex(World w, FrameBuf f) {
-    int n = f.cat_count[1];
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        int p = f.cat_list[f.pair_cap + t];
-        int2 pr = f.pairs[p];
+// convex-mesh pairs, part 1: GJK + EPA with one warp per pair.  The EPA normal and
+// closest points (or "no contact") are staged in the pair's manifold slot.
+constexpr int kConvexWarps = 4;
+constexpr int kConvexBlocksPerSM = 5;
+
+__device__ __forceinline__ bool convex_pair_ordered(const World& w, int2 pr, V3& pos0, Q4& or0, GeomD& g0, V3& pos1,
+                                                    Q4& or1, GeomD& g1) {
+    collider_pose(w, pr.x, pos0, or0, g0);
+    collider_pose(w, pr.y, pos1, or1, g1);
+    // physecs::collision calls the (other, convex mesh) routine and flips the result
+    // when only the first collider is the convex mesh (Collision.cpp:910-1016)
+    bool swap = g1.type != G_CONVEX;
+    if (swap) {
+        V3 tp = pos0; pos0 = pos1; pos1 = tp;
+        Q4 tq = or0; or0 = or1; or1 = tq;
+        GeomD tg = g0; g0 = g1; g1 = tg;
+    }
+    return swap;
+}
+
+__global__ void __launch_bounds__(32 * kConvexWarps, kConvexBlocksPerSM) k_convex_gjk_epa(World w, FrameBuf f) {
+    __shared__ WarpPoly polys[kConvexWarps];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    WarpPoly& P = polys[wid];
+    const int n = f.cat_count[1];
+    for (int t = blockIdx.x * kConvexWarps + wid; t < n; t += gridDim.x * kConvexWarps) {
+        const int p = f.cat_list[f.pair_cap + t];
         V3 pos0, pos1;
         Q4 or0, or1;
         GeomD g0, g1;
-        collider_pose(w, pr.x, pos0, or0, g0);
-        collider_pose(w, pr.y, pos1, or1, g1);
-        ManifoldL m;
-        Polytope poly;
-        bool hit = collideConvex(w, pos0, or0, g0, pos1, or1, g1, m, poly, w.err);
-        int cnt = (hit && m.numPoints) ? 1 : 0;
-        if (cnt) store_manifold(f.man_pair[p], m, p);
+        convex_pair_ordered(w, f.pairs[p], pos0, or0, g0, pos1, or1, g1);
+        Support a, b;
+        convexOrderedSupports(w, pos0, or0, g0, pos1, or1, g1, a, b);
+        WarpMink mk{a, b, lane};
+        GjkSimplex s;
+        bool hit = gjkT(mk, pos1 - pos0, s);
+        V3 nrm = {0, 0, 0}, c0 = {0, 0, 0}, c1 = {0, 0, 0};
+        if (hit) nrm = warp_epa(mk, s, c0, c1, P, lane, w.err);
+        if (lane == 0) {
+            Manifold& m = f.man_pair[p];
+            m.np = hit ? 1 : -1;
+            m.n = st4(nrm);
+            m.p0[0] = st4(c0);
+            m.p1[0] = st4(c1);
+        }
+    }
+}
+
+// convex-mesh pairs, part 2: contact generation after EPA (face selection and
+// clipping, Collision.cpp:352-887), one thread per pair.
+__global__ void __launch_bounds__(128) k_convex_contacts(World w, FrameBuf f) {
+    const int n = f.cat_count[1];
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int p = f.cat_list[f.pair_cap + t];
+        Manifold& m = f.man_pair[p];
+        if (m.np < 0) { f.pair_nman[p] = 0; continue; }
+        V3 pos0, pos1;
+        Q4 or0, or1;
+        GeomD g0, g1;
+        bool swap = convex_pair_ordered(w, f.pairs[p], pos0, or0, g0, pos1, or1, g1);
+        ManifoldL r;
+        r.numPoints = 0;
+        r.triangleIndex = -1;
+        r.normal = ld3(m.n);
+        r.points[0] = {ld3(m.p0[0]), ld3(m.p1[0])};
+        convexOrderedContacts(w, pos0, or0, g0, pos1, or1, g1, r, w.err);
+        if (swap) flipM(r);
+        int cnt = r.numPoints ? 1 : 0;
+        if (cnt) store_manifold(m, r, p);
         f.pair_nman[p] = cnt;
     }
 }
@@ -157,10 +211,17 @@ int launch_narrowphase(const World& w, FrameBuf& f, cudaStream_t s) {
         k_cat_scatter<<<nb, 256, 0, s>>>(f, c);
     }
     k_narrow_analytic<<<1216, 128, 0, s>>>(w, f);
-    k_narrow_convex<<<1216, 64, 0, s>>>(w, f);
+    static bool carveout_set = false;
+    if (!carveout_set) {
+        // five blocks of four polytopes (about 39 KB each) per SM
+        cudaFuncSetAttribute(k_convex_gjk_epa, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        carveout_set = true;
+    }
+    k_convex_gjk_epa<<<152 * kConvexBlocksPerSM, 32 * kConvexWarps, 0, s>>>(w, f);
+    k_convex_contacts<<<1216, 128, 0, s>>>(w, f);
     k_narrow_tri<<<1216, 64, 0, s>>>(w, f);
     scan_exclusive_dev(f.pair_nman, f.pair_moff, f.n_pairs, f.pair_cap, f.n_man, f.scan_scratch, s);
-    return 1 + 3 * 5 + 3 + 3;
+    return 1 + 3 * 5 + 4 + 3;
 }
 
 }  // namespace psx
