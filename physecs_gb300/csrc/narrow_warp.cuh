@@ -17,9 +17,10 @@
 // (faces from last to first, edges removed by swapping in the last edge), which
 // fixes the order of the faces and so every later tie-break.
 //
-// Every vertex of the polytope is the float difference of two float support
-// points, so it is held in shared memory as floats (exactly); face normals are
-// doubles.  The whole polytope of one pair takes about 10 KB of shared memory.
+// Every support point of the polytope is a float (held as float in shared
+// memory, exactly); the Minkowski vertices and face normals are held as doubles
+// so that the face loops convert nothing.  The whole polytope of one pair takes
+// about 11 KB of shared memory.
 #pragma once
 #include <math_constants.h>
 #include "narrow_convex.cuh"
@@ -30,7 +31,7 @@ constexpr int kFaceSlots = (kEpaFaces + 31) / 32;   // faces per lane
 
 struct WarpPoly {
     double nx[kEpaFaces], ny[kEpaFaces], nz[kEpaFaces];
-    float px[kEpaVerts], py[kEpaVerts], pz[kEpaVerts];      // Minkowski vertex
+    double px[kEpaVerts], py[kEpaVerts], pz[kEpaVerts];     // Minkowski vertex
     float ax[kEpaVerts], ay[kEpaVerts], az[kEpaVerts];      // support point on shape 0
     float bx[kEpaVerts], by[kEpaVerts], bz[kEpaVerts];      // support point on shape 1
     unsigned char i0[kEpaFaces], i1[kEpaFaces], i2[kEpaFaces];
@@ -39,10 +40,10 @@ struct WarpPoly {
     int nf, nv, ne;
 };
 
-__device__ __forceinline__ D3 wp_pos(const WarpPoly& P, int i) { return {(double)P.px[i], (double)P.py[i], (double)P.pz[i]}; }
+__device__ __forceinline__ D3 wp_pos(const WarpPoly& P, int i) { return {P.px[i], P.py[i], P.pz[i]}; }
 __device__ __forceinline__ D3 wp_n(const WarpPoly& P, int f) { return {P.nx[f], P.ny[f], P.nz[f]}; }
 __device__ __forceinline__ void wp_set_vertex(WarpPoly& P, int i, const GjkVertex& v) {
-    P.px[i] = (float)v.pos.x; P.py[i] = (float)v.pos.y; P.pz[i] = (float)v.pos.z;
+    P.px[i] = v.pos.x; P.py[i] = v.pos.y; P.pz[i] = v.pos.z;
     P.ax[i] = (float)v.sp0.x; P.ay[i] = (float)v.sp0.y; P.az[i] = (float)v.sp0.z;
     P.bx[i] = (float)v.sp1.x; P.by[i] = (float)v.sp1.y; P.bz[i] = (float)v.sp1.z;
 }
@@ -84,15 +85,19 @@ __device__ __forceinline__ V3 warp_support(const Support& s, V3 dir, int lane) {
     return support(s, dir);
 }
 
+// Not inlined: GJK and EPA call it from a dozen places, and one copy of the
+// support code keeps the kernel within the instruction cache.
+__device__ __noinline__ GjkVertex warp_mink(const Support& s0, const Support& s1, V3 dir, int lane) {
+    V3 a = warp_support(s0, dir, lane);
+    V3 b = warp_support(s1, -dir, lane);
+    return {d3(a - b), d3(a), d3(b)};
+}
+
 struct WarpMink {
     const Support& s0;
     const Support& s1;
     int lane;
-    __device__ GjkVertex operator()(V3 dir) const {
-        V3 a = warp_support(s0, dir, lane);
-        V3 b = warp_support(s1, -dir, lane);
-        return {d3(a - b), d3(a), d3(b)};
-    }
+    __device__ GjkVertex operator()(V3 dir) const { return warp_mink(s0, s1, dir, lane); }
 };
 
 __device__ __forceinline__ double warp_min_d(double v) {
