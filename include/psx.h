@@ -217,6 +217,46 @@ PSX_API int32_t psx_world_get_bounds(psx_world* w, float* bounds, int32_t cap);
 /* Human-readable description of the calling thread's last error. */
 PSX_API const char* psx_last_error_string(void);
 
+/* ------------------------------------------------------------------------
+ * Serving: continuous batching of independent scene requests.  No counterpart
+ * in the reference (one Scene per registry there); each request is a scene as
+ * psx_world_create takes it plus a frame count, and its results equal those of
+ * a world holding that scene alone.
+ *
+ * The server holds slots in size classes (class_bodies ascending, bodies per
+ * slot including the request's static ones).  Requests carry no joints and no
+ * triangle meshes; their convex meshes must equal meshes of mesh_pool (a scene
+ * desc of which only the convex-mesh arrays are read).  Single-threaded: the
+ * caller serialises calls on one server.
+ * ---------------------------------------------------------------------- */
+typedef struct psx_server psx_server;
+
+typedef struct psx_server_opts {
+    int32_t n_classes;
+    const int32_t* class_bodies;      /* [n_classes] body capacity of a slot, ascending */
+    const int32_t* class_slots;       /* [n_classes] slots of that class */
+    const psx_scene_desc* mesh_pool;  /* convex meshes requests may use, or NULL */
+    int32_t pairs_per_collider;       /* as psx_world_opts (0: default) */
+    int32_t manifolds_per_collider;
+    int32_t device;
+} psx_server_opts;
+
+PSX_API psx_status psx_server_create(const psx_server_opts* opts, psx_server** out);
+PSX_API psx_status psx_server_destroy(psx_server* s);
+/* Place a request in the smallest free slot that holds it; it runs from the next
+ * tick for `frames` frames of dt seconds.  PSX_ERR_CAPACITY: no free slot fits. */
+PSX_API psx_status psx_server_admit(psx_server* s, const psx_scene_desc* request, int32_t frames, float dt,
+                                    int32_t* slot);
+/* One frame of every running request, in one batched frame; waits for it.  The
+ * slots whose request ran its last frame are written to done[0..min(n,cap)). */
+PSX_API psx_status psx_server_tick(psx_server* s, int32_t* done, int32_t cap, int32_t* n_done);
+/* Body state of a running or finished request (arrays as psx_world_read_bodies). */
+PSX_API psx_status psx_server_read(psx_server* s, int32_t slot, float* pos, float* quat, float* vel, float* ang_vel);
+/* Free a slot (a running request is dropped). */
+PSX_API psx_status psx_server_release(psx_server* s, int32_t slot);
+/* out[6] = {running, finished, free slots, bodies running, body-frames so far, slots} */
+PSX_API psx_status psx_server_stats(psx_server* s, int64_t* out);
+
 /* ---- single-scene spelling of the same entry points (physecs::Scene) ---- */
 typedef psx_world psx_scene;
 PSX_API psx_status psx_scene_create(const psx_scene_desc* desc, psx_scene** out);

@@ -128,7 +128,7 @@ def build(jobs=8, verbose=False):
         cmd = ["g++"] + flags + inc + ["-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
-            raise RuntimeError("compile failed: %s\n%s" % (" ".join(cmd), r.stderr[-4000:]))
+            raise RuntimeError("compile failed: %s: %s" % (os.path.basename(src), " | ".join(r.stderr.strip().splitlines()[-12:])))
         return obj
 
     with ThreadPoolExecutor(jobs) as ex:

@@ -23,7 +23,9 @@ PSX_STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OUT_OF_MEMORY", 3: "CAPACITY", 4: "
 EXPORTS = ["psx_world_create", "psx_world_destroy", "psx_world_step", "psx_world_step_timed", "psx_world_synchronize", "psx_world_set_knobs",
            "psx_world_read_bodies", "psx_world_write_bodies", "psx_world_simulate_host", "psx_world_counts",
            "psx_world_get_pairs", "psx_world_get_contacts", "psx_world_get_bounds", "psx_last_error_string",
-           "psx_scene_create", "psx_scene_destroy", "psx_scene_simulate", "psx_world_read_bodies_noalloc"]
+           "psx_scene_create", "psx_scene_destroy", "psx_scene_simulate", "psx_world_read_bodies_noalloc",
+           "psx_server_create", "psx_server_destroy", "psx_server_admit", "psx_server_tick", "psx_server_read",
+           "psx_server_release", "psx_server_stats"]
 
 _lib = None
 
@@ -35,6 +37,12 @@ class PsxError(RuntimeError):
 class PsxWorldOpts(C.Structure):
     _fields_ = [("pairs_per_collider", C.c_int32), ("manifolds_per_collider", C.c_int32),
                 ("block_scene_max_dyn", C.c_int32), ("use_graph", C.c_int32), ("device", C.c_int32)]
+
+
+class PsxServerOpts(C.Structure):
+    _fields_ = [("n_classes", C.c_int32), ("class_bodies", C.c_void_p), ("class_slots", C.c_void_p),
+                ("mesh_pool", C.c_void_p), ("pairs_per_collider", C.c_int32), ("manifolds_per_collider", C.c_int32),
+                ("device", C.c_int32)]
 
 
 def load():
@@ -65,6 +73,13 @@ def load():
     lib.psx_world_get_bounds.argtypes = [vp, vp, C.c_int32]
     lib.psx_world_get_bounds.restype = C.c_int32
     lib.psx_last_error_string.restype = C.c_char_p
+    lib.psx_server_create.argtypes = [C.POINTER(PsxServerOpts), C.POINTER(vp)]
+    lib.psx_server_destroy.argtypes = [vp]
+    lib.psx_server_admit.argtypes = [vp, C.POINTER(PsxSceneDesc), C.c_int32, C.c_float, vp]
+    lib.psx_server_tick.argtypes = [vp, vp, C.c_int32, vp]
+    lib.psx_server_read.argtypes = [vp, C.c_int32, vp, vp, vp, vp]
+    lib.psx_server_release.argtypes = [vp, C.c_int32]
+    lib.psx_server_stats.argtypes = [vp, vp]
     _lib = lib
     return lib
 
@@ -175,3 +190,74 @@ class World:
         b = np.zeros((n, 6), np.float32)
         load().psx_world_get_bounds(self.h, _p(b), n)
         return b
+
+
+class Server:
+    """Continuous batching of scene requests (psx_server_*): admit, tick, read, release.
+
+    classes: [(bodies per slot, slots)] in ascending size; mesh_pool: a scene whose
+    convex meshes the requests may use."""
+
+    h = None
+
+    def __init__(self, classes, mesh_pool=None, device=0, pairs_per_collider=0, manifolds_per_collider=0):
+        lib = load()
+        self._cb = np.ascontiguousarray([c[0] for c in classes], np.int32)
+        self._cs = np.ascontiguousarray([c[1] for c in classes], np.int32)
+        self._pool_scene = mesh_pool
+        self._pool = make_desc(mesh_pool) if mesh_pool is not None else None
+        opts = PsxServerOpts(len(classes), self._cb.ctypes.data, self._cs.ctypes.data,
+                             C.cast(C.pointer(self._pool), C.c_void_p) if self._pool is not None else None,
+                             pairs_per_collider, manifolds_per_collider, device)
+        h = C.c_void_p()
+        _check(lib.psx_server_create(C.byref(opts), C.byref(h)))
+        self.h = h
+        self.n_bodies = {}
+
+    def close(self):
+        if self.h:
+            load().psx_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def admit(self, scene, frames, dt=None):
+        """Returns the slot, or None when no free slot fits (PSX_ERR_CAPACITY)."""
+        dt = scene.dt if dt is None else dt
+        d = make_desc(scene)
+        slot = C.c_int32(-1)
+        st = load().psx_server_admit(self.h, C.byref(d), frames, C.c_float(dt), C.byref(slot))
+        if st == 3:
+            return None
+        _check(st)
+        self.n_bodies[slot.value] = len(scene.arrays["pos"])
+        return slot.value
+
+    def tick(self):
+        """One frame of every running request; returns the slots that finished."""
+        done = np.zeros(max(1, len(self.n_bodies) + 64), np.int32)
+        n = C.c_int32(0)
+        _check(load().psx_server_tick(self.h, _p(done), len(done), C.byref(n)))
+        if n.value > len(done):
+            raise PsxError("tick: more finished slots than the result buffer holds")
+        return done[:n.value].tolist()
+
+    def read(self, slot):
+        n = self.n_bodies[slot]
+        st = dict(pos=np.zeros((n, 3), np.float32), quat=np.zeros((n, 4), np.float32),
+                  vel=np.zeros((n, 3), np.float32), ang_vel=np.zeros((n, 3), np.float32))
+        _check(load().psx_server_read(self.h, slot, _p(st["pos"]), _p(st["quat"]), _p(st["vel"]), _p(st["ang_vel"])))
+        return st
+
+    def release(self, slot):
+        _check(load().psx_server_release(self.h, slot))
+        self.n_bodies.pop(slot, None)
+
+    def stats(self):
+        out = np.zeros(6, np.int64)
+        _check(load().psx_server_stats(self.h, _p(out)))
+        return dict(zip(["running", "finished", "free", "bodies", "body_frames", "slots"], (int(v) for v in out)))

@@ -4,10 +4,11 @@
 // pair SET is identical: a pair is reported iff both colliders have
 // enableSimulation, they belong to different entities, at least one is dynamic, and
 // their bounds overlap inclusively on all three axes — exactly the SAP conditions.
-// Steps per frame: per-scene centroid bounds -> 30-bit (or scene-prefixed) Morton
-// keys -> radix sort -> Karras (2012) radix tree per scene segment -> bottom-up
+// Steps per frame: per-scene centroid bounds -> 30-bit Morton keys -> radix sort
+// by (scene, Morton) -> Karras (2012) radix tree per scene segment -> bottom-up
 // refit -> per-leaf traversal (count, scan, emit) writing canonical pairs
-// (entity0 < entity1, src/Physecs.cpp:156-170).
+// (entity0 < entity1, src/Physecs.cpp:156-170), each leaf's pairs ordered by
+// partner collider.
 #include "frame.cuh"
 #include "narrow_convex.cuh"
 
@@ -18,9 +19,9 @@ namespace psx {
 // getBounds (src/BoundsUtil.cpp:23-85) at the collider's world pose (src/Physecs.cpp:79-90).
 // margin_mode 0: every collider, no margin (onRigidBodyCreate, src/Physecs.cpp:25-37);
 // margin_mode 1: colliders of simulated dynamic bodies, +0.01 m (src/Physecs.cpp:555-559).
-__global__ void k_aabb(World w, int margin_mode) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= w.n_colliders) return;
+__global__ void k_aabb(World w, int c0, int c1, int margin_mode) {
+    int c = c0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= c1) return;
     int4 ci = w.col_info[c];
     int4 bi = w.info[ci.x];
     bool simulated = (bi.y & BODY_DYN) && !(bi.y & BODY_KIN);
@@ -50,8 +51,12 @@ __global__ void k_aabb(World w, int margin_mode) {
 }
 
 int launch_aabb(const World& w, int margin_mode, cudaStream_t s) {
-    if (w.n_colliders == 0) return 0;
-    k_aabb<<<(w.n_colliders + 255) / 256, 256, 0, s>>>(w, margin_mode);
+    return launch_aabb_range(w, 0, w.n_colliders, margin_mode, s);
+}
+
+int launch_aabb_range(const World& w, int c0, int c1, int margin_mode, cudaStream_t s) {
+    if (c1 <= c0) return 0;
+    k_aabb<<<(c1 - c0 + 255) / 256, 256, 0, s>>>(w, c0, c1, margin_mode);
     return 1;
 }
 
@@ -62,6 +67,7 @@ __global__ void k_scene_bounds(World w, FrameBuf f) {
     int cs = w.scene_col[s], ce = w.scene_col[s + 1];
     float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
     for (int c = cs + threadIdx.x; c < ce; c += blockDim.x) {
+        if (!(w.col_info[c].w & COL_ENABLE)) continue;   // disabled colliders never pair
         float4 a = w.aabb_min[c], b = w.aabb_max[c];
         float m[3] = {(a.x + b.x) * 0.5f, (a.y + b.y) * 0.5f, (a.z + b.z) * 0.5f};
         for (int k = 0; k < 3; ++k) { lo[k] = fminf(lo[k], m[k]); hi[k] = fmaxf(hi[k], m[k]); }
@@ -91,26 +97,48 @@ __device__ __forceinline__ uint32_t expand_bits(uint32_t v, int bits) {
     return r;
 }
 
-__global__ void k_morton(World w, FrameBuf f, int mbits) {
+// 30-bit Morton code of the collider's bounds centre within its scene's bounds; bit 30
+// marks disabled colliders so that they sort after every collider that can pair.  The
+// code depends only on the collider's own scene, never on how many scenes share the
+// world, so a scene gets the same tree order alone or in any batch.
+__global__ void k_morton(World w, FrameBuf f) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= w.n_colliders) return;
-    int s = w.info[w.col_info[c].x].w;
-    float4 lo = f.scene_lo[s], hi = f.scene_hi[s];
-    float4 a = w.aabb_min[c], b = w.aabb_max[c];
-    int per = mbits / 3;
-    float scale = (float)(1u << per);
-    float m[3] = {(a.x + b.x) * 0.5f, (a.y + b.y) * 0.5f, (a.z + b.z) * 0.5f};
-    float l[3] = {lo.x, lo.y, lo.z}, h[3] = {hi.x, hi.y, hi.z};
-    uint32_t code = 0;
-    for (int k = 0; k < 3; ++k) {
-        float ext = h[k] - l[k];
-        float u = ext > 0.f ? (m[k] - l[k]) / ext : 0.f;
-        u = fminf(fmaxf(u, 0.f), 1.f);
-        uint32_t q = (uint32_t)fminf(u * scale, scale - 1.f);
-        code |= expand_bits(q, per) << (2 - k);
+    int4 ci = w.col_info[c];
+    uint32_t code = 1u << 30;
+    if (ci.w & COL_ENABLE) {
+        int s = w.info[ci.x].w;
+        float4 lo = f.scene_lo[s], hi = f.scene_hi[s];
+        float4 a = w.aabb_min[c], b = w.aabb_max[c];
+        const float scale = 1024.f;
+        float m[3] = {(a.x + b.x) * 0.5f, (a.y + b.y) * 0.5f, (a.z + b.z) * 0.5f};
+        float l[3] = {lo.x, lo.y, lo.z}, h[3] = {hi.x, hi.y, hi.z};
+        code = 0;
+        for (int k = 0; k < 3; ++k) {
+            float ext = h[k] - l[k];
+            float u = ext > 0.f ? (m[k] - l[k]) / ext : 0.f;
+            u = fminf(fmaxf(u, 0.f), 1.f);
+            uint32_t q = (uint32_t)fminf(u * scale, scale - 1.f);
+            code |= expand_bits(q, 10) << (2 - k);
+        }
     }
-    f.keys[c] = ((uint32_t)s << mbits) | code;
+    f.mkey[c] = code;
+    f.keys[c] = code;
     f.order[c] = c;
+}
+
+// after the Morton sort: scene index of each sorted leaf, for the stable scene pass
+__global__ void k_scene_keys(World w, FrameBuf f) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= w.n_colliders) return;
+    f.keys[p] = (uint32_t)w.info[w.col_info[f.order[p]].x].w;
+}
+
+// after the scene pass: the Morton code of each sorted leaf again, for the tree build
+__global__ void k_gather_keys(World w, FrameBuf f) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= w.n_colliders) return;
+    f.keys[p] = f.mkey[f.order[p]];
 }
 
 // ---------------------------------------------------------------- Karras radix tree
@@ -221,7 +249,8 @@ __global__ void k_traverse(World w, FrameBuf f) {
     int cs = w.scene_col[s], n = w.scene_col[s + 1] - cs;
     int count = 0;
     int out = EMIT ? f.leaf_off[p] : 0;
-    if (n >= 2 && (w.col_info[ca].w & COL_ENABLE)) {
+    bool active = !w.scene_active || w.scene_active[s];
+    if (n >= 2 && active && (w.col_info[ca].w & COL_ENABLE)) {
         float4 qmin = w.aabb_min[ca], qmax = w.aabb_max[ca];
         int stack[64];
         int sp = 0;
@@ -254,20 +283,45 @@ __global__ void k_traverse(World w, FrameBuf f) {
             }
         }
     }
-    if (!EMIT) f.leaf_cnt[p] = count;
+    if (!EMIT) {
+        f.leaf_cnt[p] = count;
+    } else {
+        // the traversal order depends on the tree's shape; order the leaf's pairs by the
+        // partner collider instead, so the pair list depends only on the scene itself
+        int n_out = min(count, f.pair_cap - out);
+        for (int i = 1; i < n_out; ++i) {
+            int2 v = f.pairs[out + i];
+            int kv = v.x == ca ? v.y : v.x;
+            int j = i - 1;
+            for (; j >= 0; --j) {
+                int2 u = f.pairs[out + j];
+                int ku = u.x == ca ? u.y : u.x;
+                if (ku <= kv) break;
+                f.pairs[out + j + 1] = u;
+            }
+            f.pairs[out + j + 1] = v;
+        }
+    }
 }
 
 __global__ void k_pairs_check(FrameBuf f, int* err) {
     if (*f.n_pairs > f.pair_cap) { atomicOr(err, ERR_PAIR_CAPACITY); *f.n_pairs = f.pair_cap; }
 }
 
-int launch_broadphase(const World& w, FrameBuf& f, int mbits, int total_bits, cudaStream_t s) {
+int launch_broadphase(const World& w, FrameBuf& f, int scene_bits, cudaStream_t s) {
     int n = w.n_colliders;
     if (n == 0) return 0;
     int nb = (n + 255) / 256;
     k_scene_bounds<<<w.n_scenes, 256, 0, s>>>(w, f);
-    k_morton<<<nb, 256, 0, s>>>(w, f, mbits);
-    int k = 2 + radix_sort_pairs(f.keys, f.order, f.keys_tmp, f.order_tmp, n, total_bits, f.radix_hist, s);
+    k_morton<<<nb, 256, 0, s>>>(w, f);
+    // (scene, Morton) order as two stable LSD sorts: Morton first, then scene
+    int k = 2 + radix_sort_pairs(f.keys, f.order, f.keys_tmp, f.order_tmp, n, 31, f.radix_hist, s);
+    if (scene_bits > 0) {
+        k_scene_keys<<<nb, 256, 0, s>>>(w, f);
+        k += 1 + radix_sort_pairs(f.keys, f.order, f.keys_tmp, f.order_tmp, n, scene_bits, f.radix_hist, s);
+    }
+    k_gather_keys<<<nb, 256, 0, s>>>(w, f);
+    ++k;
     k_karras<<<nb, 256, 0, s>>>(w, f);
     k_refit<<<nb, 256, 0, s>>>(w, f);
     k_traverse<false><<<nb, 256, 0, s>>>(w, f);

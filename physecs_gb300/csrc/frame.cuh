@@ -21,7 +21,8 @@ struct FrameBuf {
     // broadphase
     float4* scene_lo;     // [S] centroid bounds for Morton quantisation
     float4* scene_hi;
-    uint32_t* keys;       // [n_colliders]
+    uint32_t* keys;       // [n_colliders] sort keys, then the sorted leaves' Morton codes
+    uint32_t* mkey;       // [n_colliders] Morton code per collider
     int* order;           // sorted leaf -> collider
     uint32_t* keys_tmp;
     int* order_tmp;
@@ -72,7 +73,8 @@ struct FrameBuf {
 // kernel launch helpers (definitions in the .cu files); each returns the number of
 // kernels it queued
 int launch_aabb(const World& w, int margin_mode, cudaStream_t s);
-int launch_broadphase(const World& w, FrameBuf& f, int mbits, int total_bits, cudaStream_t s);
+int launch_aabb_range(const World& w, int c0, int c1, int margin_mode, cudaStream_t s);
+int launch_broadphase(const World& w, FrameBuf& f, int scene_bits, cudaStream_t s);
 int launch_narrowphase(const World& w, FrameBuf& f, cudaStream_t s);
 int launch_contacts(const World& w, FrameBuf& f, cudaStream_t s);
 int launch_solver(const World& w, FrameBuf& f, const int* block_scenes, int n_block_scenes, const int* grid_scenes,

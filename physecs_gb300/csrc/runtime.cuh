@@ -1,0 +1,98 @@
+// runtime.cuh — host-side state of a world and the runtime helpers shared by the
+// C-ABI entry points (world.cu) and the serving loop (server.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <string>
+#include <vector>
+#include "frame.cuh"
+#include "../../include/psx.h"
+
+namespace psx {
+namespace rt {
+// records msg for psx_last_error_string() on the calling thread and returns s
+psx_status fail(psx_status s, const std::string& msg);
+inline float4 f4(float x, float y, float z, float w = 0.f) { return make_float4(x, y, z, w); }
+inline int ilog2ceil(int v) { int b = 0; while ((1 << b) < v) ++b; return b; }
+}  // namespace rt
+}  // namespace psx
+
+#define PSX_CUDA(call)                                                                     \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess) return psx::rt::fail(PSX_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+#define PSX_TRY(expr)                       \
+    do {                                    \
+        psx_status s_ = (expr);             \
+        if (s_ != PSX_OK) return s_;        \
+    } while (0)
+
+struct psx_world {
+    psx::World w{};
+    psx::FrameBuf f{};
+    cudaStream_t stream = nullptr;
+    std::vector<void*> allocs;
+    int n_scenes = 0;
+    int scene_bits = 0;     // bits of the scene index in the broadphase sort
+    std::vector<int> h_scene_body, h_scene_col, h_scene_dyn;
+    std::vector<uint32_t> h_entity;        // per body
+    std::vector<int> h_body_dyn;           // per body: global dyn index or -1
+    std::vector<int> h_col_local;          // per collider: index within its body
+    std::vector<int> block_scenes_h, grid_scenes_h;
+    int* block_scenes = nullptr;
+    int* grid_scenes = nullptr;
+    int grid_blocks = 0;
+    std::vector<float4> h_knobs;
+    bool use_graph = false;
+    cudaGraphExec_t graph = nullptr;
+    float graph_dt = -1.f;
+    bool knobs_dirty = true;
+    // pinned staging for body transfers
+    float4* pin = nullptr;
+    size_t pin_n = 0;
+    int device = 0;
+    long long launches = 0;          // kernels queued since creation
+    int n_simulated = 0;             // dynamic, non-kinematic bodies
+    std::vector<cudaEvent_t> events; // stage events of timed steps
+
+    template <class T>
+    psx_status alloc(T*& p, size_t n) {
+        if (n == 0) n = 1;
+        void* q = nullptr;
+        cudaError_t e = cudaMalloc(&q, n * sizeof(T));
+        if (e != cudaSuccess) return psx::rt::fail(PSX_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        allocs.push_back(q);
+        p = (T*)q;
+        return PSX_OK;
+    }
+    template <class T>
+    psx_status upload(T*& p, const std::vector<T>& v) {
+        psx_status s = alloc(p, v.size());
+        if (s != PSX_OK) return s;
+        if (!v.empty()) PSX_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+        return PSX_OK;
+    }
+    ~psx_world() {
+        for (cudaEvent_t e : events) cudaEventDestroy(e);
+        if (graph) cudaGraphExecDestroy(graph);
+        for (void* p : allocs) cudaFree(p);
+        if (pin) cudaFreeHost(pin);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+
+namespace psx {
+namespace rt {
+psx_status validate(const psx_scene_desc& d);
+// packs scenes into W's device buffers and computes the creation bounds
+psx_status build_world(psx_world* W, const psx_scene_desc* scenes, int S, const psx_world_opts& o);
+// queues one frame on W's stream; ev (optional) receives 6 stage events; returns kernels queued
+int queue_frame(psx_world* W, cudaEvent_t* ev = nullptr);
+// reads the device error word; maps its bits to a status
+psx_status check_err(psx_world* W);
+// pinned host staging of at least n4 float4
+psx_status ensure_pinned(psx_world* W, size_t n4);
+}  // namespace rt
+}  // namespace psx

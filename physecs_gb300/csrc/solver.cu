@@ -90,7 +90,8 @@ __global__ void k_build_contacts(World w, FrameBuf f) {
             unsigned long long key = cache_key(pr.x, pr.y, m.tri);
             // previous frame's entry, if any
             const CacheEntry* pe = nullptr;
-            for (unsigned h = cache_hash(key) & mask, probe = 0; probe < (unsigned)f.cache_cap; ++probe, h = (h + 1) & mask) {
+            const bool fresh = w.scene_fresh && w.scene_fresh[iA.w];
+            for (unsigned h = cache_hash(key) & mask, probe = 0; !fresh && probe < (unsigned)f.cache_cap; ++probe, h = (h + 1) & mask) {
                 unsigned long long kk = prev[h].key;
                 if (kk == key) { pe = &prev[h]; break; }
                 if (kk == kEmpty) break;
@@ -663,6 +664,7 @@ struct GridSync {
 
 template <class S>
 __device__ void solve_scene(const World& w, FrameBuf& f, int s, const S& sy) {
+    if (w.scene_active && !w.scene_active[s]) return;
     const int tid = sy.tid(), nth = sy.nth();
     int ds = w.scene_dyn[s], de = w.scene_dyn[s + 1];
     int ms = f.scene_man[s], me = f.scene_man[s + 1];
@@ -673,6 +675,8 @@ __device__ void solve_scene(const World& w, FrameBuf& f, int s, const S& sy) {
     // ---- graph colouring of the contacts: rounds in which every uncoloured contact claims
     // its dynamic bodies with a hashed priority; a contact that holds all its bodies takes
     // the round's colour.  Hashed (not index) priorities keep the round count logarithmic.
+    // Priorities use the contact's index within its scene, so a scene is coloured the
+    // same way whatever other scenes share the world.
     const unsigned long long kFree = ~0ull;
     for (int d = ds + tid; d < de; d += nth) f.claim[d] = kFree;
     for (int m = ms + tid; m < me; m += nth) f.color_of[m] = -1;
@@ -682,7 +686,8 @@ __device__ void solve_scene(const World& w, FrameBuf& f, int s, const S& sy) {
         for (int m = ms + tid; m < me; m += nth) {
             if (f.color_of[m] >= 0) continue;
             const Contact& c = f.contacts[m];
-            unsigned long long pri = ((unsigned long long)cache_hash((unsigned long long)m * 0x9E3779B97F4A7C15ull + ncol) << 32) | (unsigned)m;
+            const unsigned ml = (unsigned)(m - ms);
+            unsigned long long pri = ((unsigned long long)cache_hash((unsigned long long)ml * 0x9E3779B97F4A7C15ull + ncol) << 32) | ml;
             if (c.b0 >= 0) atomicMin(&f.claim[c.b0], pri);
             if (c.b1 >= 0) atomicMin(&f.claim[c.b1], pri);
         }
@@ -691,7 +696,8 @@ __device__ void solve_scene(const World& w, FrameBuf& f, int s, const S& sy) {
         for (int m = ms + tid; m < me; m += nth) {
             if (f.color_of[m] >= 0) continue;
             const Contact& c = f.contacts[m];
-            bool ok = (c.b0 < 0 || (unsigned)f.claim[c.b0] == (unsigned)m) && (c.b1 < 0 || (unsigned)f.claim[c.b1] == (unsigned)m);
+            const unsigned ml = (unsigned)(m - ms);
+            bool ok = (c.b0 < 0 || (unsigned)f.claim[c.b0] == ml) && (c.b1 < 0 || (unsigned)f.claim[c.b1] == ml);
             if (ok && ncol < kMaxColors) f.color_of[m] = ncol;
             else left = true;
         }

@@ -160,6 +160,9 @@ struct World {
     // jointed body pairs, sorted (lo, hi): such pairs never collide (src/Physecs.cpp:209, 694)
     int2* nc_pairs;
     int n_nc;
+    // serving: per-scene flags, null for a plain world (every scene runs, cache on)
+    int* scene_active;     // [S] 0: the scene is skipped by the traversal and the solver
+    int* scene_fresh;      // [S] 1: first frame of a newly placed scene, no cached contacts
     // errors
     int* err;
 };

@@ -13,12 +13,12 @@
 #include <mutex>
 #include <string>
 #include <vector>
-#include "frame.cuh"
-#include "../../include/psx.h"
+#include "runtime.cuh"
 
 using namespace psx;
 
-namespace {
+namespace psx {
+namespace rt {
 
 thread_local std::string g_err;
 
@@ -27,11 +27,12 @@ psx_status fail(psx_status s, const std::string& msg) {
     return s;
 }
 
-#define PSX_CUDA(call)                                                                     \
-    do {                                                                                   \
-        cudaError_t e_ = (call);                                                           \
-        if (e_ != cudaSuccess) return fail(PSX_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
-    } while (0)
+}  // namespace rt
+}  // namespace psx
+
+using namespace psx::rt;
+
+namespace {
 
 // ---------------------------------------------------------------- triangle-mesh BVH (host)
 // Binned SAH with six buckets, exactly as src/TriangleMesh.cpp:7-164, so that triangle
@@ -128,8 +129,6 @@ struct MeshBVH {
     }
 };
 
-float4 f4(float x, float y, float z, float w = 0.f) { return make_float4(x, y, z, w); }
-int ilog2ceil(int v) { int b = 0; while ((1 << b) < v) ++b; return b; }
 
 template <class T>
 struct DBuf {
@@ -139,67 +138,9 @@ struct DBuf {
 
 }  // namespace
 
-struct psx_world {
-    World w{};
-    FrameBuf f{};
-    cudaStream_t stream = nullptr;
-    std::vector<void*> allocs;
-    int n_scenes = 0;
-    int mbits = 30, total_bits = 30;
-    std::vector<int> h_scene_body, h_scene_col, h_scene_dyn;
-    std::vector<uint32_t> h_entity;        // per body
-    std::vector<int> h_body_dyn;           // per body: global dyn index or -1
-    std::vector<int> h_col_local;          // per collider: index within its body
-    std::vector<int> block_scenes_h, grid_scenes_h;
-    int* block_scenes = nullptr;
-    int* grid_scenes = nullptr;
-    int grid_blocks = 0;
-    std::vector<float4> h_knobs;
-    bool use_graph = false;
-    cudaGraphExec_t graph = nullptr;
-    float graph_dt = -1.f;
-    bool knobs_dirty = true;
-    // pinned staging for body transfers
-    float4* pin = nullptr;
-    size_t pin_n = 0;
-    int device = 0;
-    long long launches = 0;          // kernels queued since creation
-    int n_simulated = 0;             // dynamic, non-kinematic bodies
-    std::vector<cudaEvent_t> events; // stage events of timed steps
 
-    template <class T>
-    psx_status alloc(T*& p, size_t n) {
-        if (n == 0) n = 1;
-        void* q = nullptr;
-        cudaError_t e = cudaMalloc(&q, n * sizeof(T));
-        if (e != cudaSuccess) return fail(PSX_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e));
-        allocs.push_back(q);
-        p = (T*)q;
-        return PSX_OK;
-    }
-    template <class T>
-    psx_status upload(T*& p, const std::vector<T>& v) {
-        psx_status s = alloc(p, v.size());
-        if (s != PSX_OK) return s;
-        if (!v.empty()) PSX_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
-        return PSX_OK;
-    }
-    ~psx_world() {
-        for (cudaEvent_t e : events) cudaEventDestroy(e);
-        if (graph) cudaGraphExecDestroy(graph);
-        for (void* p : allocs) cudaFree(p);
-        if (pin) cudaFreeHost(pin);
-        if (stream) cudaStreamDestroy(stream);
-    }
-};
 
-#define PSX_TRY(expr)                       \
-    do {                                    \
-        psx_status s_ = (expr);             \
-        if (s_ != PSX_OK) return s_;        \
-    } while (0)
-
-static psx_status validate(const psx_scene_desc& d) {
+psx_status psx::rt::validate(const psx_scene_desc& d) {
     if (d.n_bodies <= 0) return fail(PSX_ERR_INVALID_ARG, "scene without bodies");
     if (!d.entity || !d.flags || !d.pos || !d.quat || !d.collider_start) return fail(PSX_ERR_INVALID_ARG, "missing body arrays");
     if (d.collider_start[0] != 0 || d.collider_start[d.n_bodies] != d.n_colliders) return fail(PSX_ERR_INVALID_ARG, "collider_start");
@@ -219,7 +160,7 @@ static psx_status validate(const psx_scene_desc& d) {
     return PSX_OK;
 }
 
-static psx_status build_world(psx_world* W, const psx_scene_desc* scenes, int S, const psx_world_opts& o) {
+psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int S, const psx_world_opts& o) {
     W->n_scenes = S;
     std::vector<int> scene_body{0}, scene_col{0}, scene_dyn{0}, scene_joint{0};
     std::vector<float4> pos, quat, vel, ang, com, invI, col_pos, col_quat, col_params, col_mat;
@@ -464,6 +405,7 @@ static psx_status build_world(psx_world* W, const psx_scene_desc* scenes, int S,
     PSX_TRY(W->alloc(f.scene_lo, S));
     PSX_TRY(W->alloc(f.scene_hi, S));
     PSX_TRY(W->alloc(f.keys, n));
+    PSX_TRY(W->alloc(f.mkey, n));
     PSX_TRY(W->alloc(f.order, n));
     PSX_TRY(W->alloc(f.keys_tmp, n));
     PSX_TRY(W->alloc(f.order_tmp, n));
@@ -516,13 +458,7 @@ static psx_status build_world(psx_world* W, const psx_scene_desc* scenes, int S,
     PSX_TRY(W->upload(W->block_scenes, W->block_scenes_h));
     PSX_TRY(W->upload(W->grid_scenes, W->grid_scenes_h));
     W->grid_blocks = W->grid_scenes_h.empty() ? 0 : solver_grid_blocks();
-    int sbits = ilog2ceil(S);
-    if (S <= 1) { W->mbits = 30; W->total_bits = 30; }
-    else {
-        int mb = std::min(30, (32 - sbits) / 3 * 3);
-        W->mbits = mb;
-        W->total_bits = mb + sbits;
-    }
+    W->scene_bits = S <= 1 ? 0 : ilog2ceil(S);
     // creation bounds: no margin (src/Physecs.cpp:32)
     launch_aabb(w, 0, W->stream);
     PSX_CUDA(cudaGetLastError());
@@ -533,11 +469,11 @@ static psx_status build_world(psx_world* W, const psx_scene_desc* scenes, int S,
 // One frame = Scene::simulate for every scene: broadphase, narrowphase, contact rows,
 // joint layout, the solver kernel (colouring + all substeps), end-of-frame bounds.
 // ev (optional) receives 6 events delimiting the 5 stages.  Returns kernels queued.
-static int queue_frame(psx_world* W, cudaEvent_t* ev = nullptr) {
+int psx::rt::queue_frame(psx_world* W, cudaEvent_t* ev) {
     int k = 0;
     cudaStream_t s = W->stream;
     if (ev) cudaEventRecord(ev[0], s);
-    k += launch_broadphase(W->w, W->f, W->mbits, W->total_bits, s);
+    k += launch_broadphase(W->w, W->f, W->scene_bits, s);
     if (ev) cudaEventRecord(ev[1], s);
     k += launch_narrowphase(W->w, W->f, s);
     if (ev) cudaEventRecord(ev[2], s);
@@ -553,7 +489,7 @@ static int queue_frame(psx_world* W, cudaEvent_t* ev = nullptr) {
     return k;
 }
 
-static psx_status check_err(psx_world* W) {
+psx_status psx::rt::check_err(psx_world* W) {
     int e = 0;
     PSX_CUDA(cudaMemcpy(&e, W->w.err, sizeof(int), cudaMemcpyDeviceToHost));
     if (!e) return PSX_OK;
@@ -563,7 +499,7 @@ static psx_status check_err(psx_world* W) {
     return fail(PSX_ERR_CAPACITY, buf);
 }
 
-static psx_status ensure_pinned(psx_world* W, size_t n4) {
+psx_status psx::rt::ensure_pinned(psx_world* W, size_t n4) {
     if (W->pin_n >= n4) return PSX_OK;
     if (W->pin) cudaFreeHost(W->pin);
     W->pin = nullptr;
