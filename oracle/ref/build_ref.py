@@ -87,7 +87,8 @@ def prepare_tree():
            lambda s: s.replace("    class Scene {\n", "    class Scene { public:\n", 1))
 
 
-def build(jobs=8, verbose=False):
+def build(jobs=8, verbose=False, portable=None):
+    """portable: emulate SSE on GCC vector extensions (default: on hosts other than x86)."""
     if os.path.isdir(REFERENCE):
         prepare_tree()
     elif not os.path.isdir(TREE):
@@ -114,7 +115,17 @@ def build(jobs=8, verbose=False):
              "-DENTT_PACKED_PAGE=131072",
              "-w", "-include", os.path.join(shim_dir, "ref_shim.h")]
     import platform
-    if platform.machine() in ("x86_64", "AMD64", "i686"):
+    if portable is None:
+        portable = platform.machine() not in ("x86_64", "AMD64", "i686")
+    out_dir = OUT
+    if portable:
+        inc = ["-I" + os.path.join(HERE, "arm_include")] + inc
+        flags += ["-DPSX_SSE_PORTABLE"]
+        if platform.machine() in ("x86_64", "AMD64", "i686"):
+            out_dir = os.path.join(OUT, "portable")   # validation build of the emulation on x86
+            objdir = os.path.join(out_dir, "obj")
+            os.makedirs(objdir, exist_ok=True)
+    else:
         flags += ["-msse4.2"]
     srcs = []
     for root, _, files in os.walk(os.path.join(TREE, "src")):
@@ -133,7 +144,7 @@ def build(jobs=8, verbose=False):
 
     with ThreadPoolExecutor(jobs) as ex:
         objs = list(ex.map(compile_one, srcs))
-    lib = os.path.join(OUT, "libphysecs_ref.so")
+    lib = os.path.join(out_dir, "libphysecs_ref.so")
     r = subprocess.run(["g++", "-shared", "-o", lib] + objs + ["-lpthread"], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stderr[-4000:])

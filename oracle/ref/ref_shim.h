@@ -14,7 +14,7 @@
  */
 #pragma once
 
-#if defined(__x86_64__) || defined(__i386__)
+#if (defined(__x86_64__) || defined(__i386__)) && !defined(PSX_SSE_PORTABLE)
 #include <immintrin.h>
 #else
 #include "psx_sse_portable.h"
@@ -32,7 +32,7 @@ static inline unsigned char _BitScanForward(unsigned long* index, unsigned long 
     return 1;
 }
 
-#if defined(__x86_64__) || defined(__i386__)
+#if (defined(__x86_64__) || defined(__i386__)) && !defined(PSX_SSE_PORTABLE)
 #ifndef _mm_and_epi32
 #define _mm_and_epi32(a, b) _mm_and_si128((a), (b))
 #endif
