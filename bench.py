@@ -232,6 +232,110 @@ def cpu_kind():
     return "port"
 
 
+
+# ---------------------------------------------------------------- serving
+
+SERVE_CLASSES = [(17, 96), (33, 96), (65, 96), (129, 96), (257, 96), (513, 96), (1025, 64), (2049, 48), (4097, 32),
+                 (8193, 24)]
+
+
+def serving_requests(count, rank=0):
+    """Seeded serving requests (N log-uniform in [8, 8192] bodies, K uniform in [1, 120] frames)."""
+    from physecs_gb300 import scenes
+    pool = scenes._hull_pool(scenes.SplitMix64(scenes.scene_seed(5, 1 << 19)), count=8)
+    reqs = [scenes.serving_request(rank * count + i, pool=pool) for i in range(count)]
+    ps = scenes.SceneData("pool")
+    ps.convex.extend(pool)
+    import numpy as np
+    ps.add_bodies(pos=[[0, 0, 0]], quat=[scenes.IDENTITY_Q], flags=0, inv_mass=0.0, com=np.zeros(3),
+                  inv_inertia=np.zeros(9), col_type=scenes.SPHERE, col_params=[0.5, 0, 0, 0], col_mesh=-1)
+    return reqs, ps.finalize()
+
+
+def _serve(srv, reqs, arrivals, t_end, max_backlog=None):
+    """Drive the server: admit arrived requests at each tick, tick, retire.  arrivals[i]
+    is request i's arrival (seconds from start) or None for a permanent backlog.
+    Returns (frame latencies s, request latencies s, body-substeps run, wall s)."""
+    import collections
+    t0 = time.perf_counter()
+    queue = collections.deque()
+    nxt = 0
+    live = {}          # slot -> [request index, arrival, last frame ready]
+    frame_lat, req_lat = [], []
+    work = 0
+    while True:
+        now = time.perf_counter() - t0
+        if now >= t_end:
+            break
+        if arrivals is None:
+            while len(queue) < (max_backlog or 64):
+                queue.append((nxt % len(reqs), now)); nxt += 1
+        else:
+            while nxt < len(arrivals) and arrivals[nxt] <= now:
+                queue.append((nxt % len(reqs), arrivals[nxt])); nxt += 1
+        # first come, first served among the requests a free slot fits
+        waiting = collections.deque()
+        while queue:
+            i, ta = queue.popleft()
+            s, k = reqs[i]
+            slot = srv.admit(s, k)
+            if slot is None:
+                waiting.append((i, ta))
+                continue
+            live[slot] = [i, ta, ta, s.n_dynamic * s.num_substeps]
+        queue = waiting
+        if not live:
+            time.sleep(0.0005)
+            continue
+        done = set(srv.tick())
+        t_ready = time.perf_counter() - t0
+        for slot, rec in list(live.items()):
+            frame_lat.append(t_ready - rec[2])
+            rec[2] = t_ready
+            work += rec[3]
+            if slot in done:
+                req_lat.append(t_ready - rec[1])
+                srv.read(slot)
+                srv.release(slot)
+                del live[slot]
+    return frame_lat, req_lat, work, time.perf_counter() - t0
+
+
+def run_serving(args, rank, world, local):
+    import numpy as np
+    from physecs_gb300.api import Server
+    reqs, pool_scene = serving_requests(384, rank)
+    srv = Server(SERVE_CLASSES, mesh_pool=pool_scene, device=local if world > 1 else 0)
+    # saturated throughput: a permanent backlog keeps every fitting slot busy
+    _serve(srv, reqs, None, 3.0)
+    _, _, work_sat, wall_sat = _serve(srv, reqs, None, max(5.0, args.serve_seconds / 3))
+    sat = work_sat / wall_sat
+    for slot in list(srv.n_bodies):
+        srv.release(slot)
+    mean_work = float(np.mean([s.n_dynamic * s.num_substeps * k for s, k in reqs]))
+    lam = args.serve_load * sat / mean_work          # requests per second
+    rng = np.random.default_rng(5 + rank)
+    arrivals = np.cumsum(rng.exponential(1.0 / lam, size=int(lam * args.serve_seconds * 1.5) + 16))
+    fl, rl, work, wall = _serve(srv, reqs, list(arrivals), args.serve_seconds)
+    fl, rl = np.asarray(fl) * 1e3, np.asarray(rl) * 1e3
+    line = {
+        "metric": "serving frame latency p99", "value": float(np.percentile(fl, 99)), "unit": "ms", "n_gpus": world,
+        "steps": len(fl), "warmup": 1, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (f64 in GJK/EPA)", "data": "synthetic (seeded SplitMix64 requests)",
+        "config": {"workload": "serving: Poisson request stream at %.0f%% of saturated throughput, N log-uniform in "
+                               "[8,8192] bodies, K uniform in [1,120] frames, dt=1/60, 4x8" % (100 * args.serve_load),
+                   "slot_classes": SERVE_CLASSES, "seconds": args.serve_seconds},
+        "p50_ms": float(np.percentile(fl, 50)), "p99_ms": float(np.percentile(fl, 99)),
+        "request_p50_ms": float(np.percentile(rl, 50)) if len(rl) else None,
+        "request_p99_ms": float(np.percentile(rl, 99)) if len(rl) else None,
+        "lambda_req_per_s": lam, "saturated_body_substeps_per_s": sat,
+        "served_body_substeps_per_s": work / wall, "requests_finished": int(len(rl)),
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    srv.close()
+    return 0
+
 # ---------------------------------------------------------------- main
 
 def main():
@@ -240,7 +344,9 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--workload", default="batched", choices=["batched", "large", "chains", "pyramid"])
+    ap.add_argument("--workload", default="batched", choices=["batched", "large", "chains", "pyramid", "serving"])
+    ap.add_argument("--serve-seconds", type=float, default=20.0)
+    ap.add_argument("--serve-load", type=float, default=0.7)
     ap.add_argument("--scenes", type=int, default=4096)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--plain-scenes", type=int, default=64)
@@ -253,6 +359,8 @@ def main():
 
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.workload == "serving":
+        return run_serving(args, rank, world, local)
 
     dist = Dist(world, local)
     from physecs_gb300.api import World

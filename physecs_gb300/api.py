@@ -213,6 +213,9 @@ class Server:
         _check(lib.psx_server_create(C.byref(opts), C.byref(h)))
         self.h = h
         self.n_bodies = {}
+        self._caps = [int(c[0]) for c in classes]
+        self._free = [int(c[1]) for c in classes]
+        self._cls = {}
 
     def close(self):
         if self.h:
@@ -228,12 +231,18 @@ class Server:
     def admit(self, scene, frames, dt=None):
         """Returns the slot, or None when no free slot fits (PSX_ERR_CAPACITY)."""
         dt = scene.dt if dt is None else dt
+        need = max(len(scene.arrays["pos"]), len(scene.arrays["col_type"]) - 1)
+        cls = next((c for c, cap in enumerate(self._caps) if cap >= need and self._free[c] > 0), None)
+        if cls is None:
+            return None          # the library would answer PSX_ERR_CAPACITY; skip the call
         d = make_desc(scene)
         slot = C.c_int32(-1)
         st = load().psx_server_admit(self.h, C.byref(d), frames, C.c_float(dt), C.byref(slot))
         if st == 3:
             return None
         _check(st)
+        self._free[cls] -= 1
+        self._cls[slot.value] = cls
         self.n_bodies[slot.value] = len(scene.arrays["pos"])
         return slot.value
 
@@ -256,6 +265,9 @@ class Server:
     def release(self, slot):
         _check(load().psx_server_release(self.h, slot))
         self.n_bodies.pop(slot, None)
+        cls = self._cls.pop(slot, None)
+        if cls is not None:
+            self._free[cls] += 1
 
     def stats(self):
         out = np.zeros(6, np.int64)

@@ -97,15 +97,19 @@ __device__ __forceinline__ uint32_t expand_bits(uint32_t v, int bits) {
     return r;
 }
 
-// 30-bit Morton code of the collider's bounds centre within its scene's bounds; bit 30
-// marks disabled colliders so that they sort after every collider that can pair.  The
-// code depends only on the collider's own scene, never on how many scenes share the
-// world, so a scene gets the same tree order alone or in any batch.
+// 30-bit Morton code of the collider's bounds centre within its scene's bounds.  Bit 30
+// marks a collider as large (its bounds' longest side at least a quarter of the longest
+// side of the scene's centre bounds: ground boxes, terrain), bit 31 a disabled one, so that within a scene the
+// ordinary colliders sort first, then the large ones, then those that never pair.  Every
+// leaf looks for partners after itself, so a large collider is found from the small
+// ones' leaves instead of walking the whole tree itself.  The code depends only on the
+// collider's own scene, never on how many scenes share the world, so a scene gets the
+// same order alone or in any batch.
 __global__ void k_morton(World w, FrameBuf f) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= w.n_colliders) return;
     int4 ci = w.col_info[c];
-    uint32_t code = 1u << 30;
+    uint32_t code = 1u << 31;
     if (ci.w & COL_ENABLE) {
         int s = w.info[ci.x].w;
         float4 lo = f.scene_lo[s], hi = f.scene_hi[s];
@@ -121,6 +125,9 @@ __global__ void k_morton(World w, FrameBuf f) {
             uint32_t q = (uint32_t)fminf(u * scale, scale - 1.f);
             code |= expand_bits(q, 10) << (2 - k);
         }
+        float spread = fmaxf(fmaxf(h[0] - l[0], h[1] - l[1]), h[2] - l[2]);
+        float size = fmaxf(fmaxf(b.x - a.x, b.y - a.y), b.z - a.z);
+        if (spread > 0.f && size >= 0.25f * spread) code |= 1u << 30;
     }
     f.mkey[c] = code;
     f.keys[c] = code;
@@ -224,11 +231,13 @@ __global__ void k_refit(World w, FrameBuf f) {
 
 // ---------------------------------------------------------------- traversal
 
+// Inclusive overlap on all three axes (physecs::intersects, src/BoundsUtil.cpp:87-92),
+// written as a conjunction so that bounds holding a NaN overlap nothing: for finite
+// bounds the result is the reference's; a body whose state has become NaN is left
+// without pairs instead of pairing with every collider of its scene.
 __device__ __forceinline__ bool overlap_incl(float4 amin, float4 amax, float4 bmin, float4 bmax) {
-    if (amax.x < bmin.x || amin.x > bmax.x) return false;
-    if (amax.y < bmin.y || amin.y > bmax.y) return false;
-    if (amax.z < bmin.z || amin.z > bmax.z) return false;
-    return true;
+    return amax.x >= bmin.x && amin.x <= bmax.x && amax.y >= bmin.y && amin.y <= bmax.y && amax.z >= bmin.z &&
+           amin.z <= bmax.z;
 }
 
 // SAP filters of src/Physecs.cpp:138-147
@@ -240,6 +249,9 @@ __device__ __forceinline__ bool pair_ok(const World& w, int ca, int cb) {
     return true;
 }
 
+// One thread per sorted leaf p finds its partners q > p by a left-first depth-first walk
+// of its scene's tree, so partners come out in increasing sorted position: an order that
+// depends only on the scene (its Morton codes), never on the tree's shape or the batch.
 template <bool EMIT>
 __global__ void k_traverse(World w, FrameBuf f) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -256,52 +268,34 @@ __global__ void k_traverse(World w, FrameBuf f) {
         int sp = 0;
         stack[sp++] = cs - s;  // root of this scene's tree
         while (sp) {
-            int node = stack[--sp];
-            int ch[2] = {f.bvh.left[node], f.bvh.right[node]};
-            for (int k = 0; k < 2; ++k) {
-                int c = ch[k];
-                if (c < 0) {
-                    int q = ~c;
-                    if (q <= p) continue;
-                    int cb = f.order[q];
-                    if (!overlap_incl(qmin, qmax, w.aabb_min[cb], w.aabb_max[cb])) continue;
-                    if (!pair_ok(w, ca, cb)) continue;
-                    if (EMIT) {
-                        int slot = out + count;
-                        if (slot < f.pair_cap) {
-                            uint32_t ea = (uint32_t)w.info[w.col_info[ca].x].x, eb = (uint32_t)w.info[w.col_info[cb].x].x;
-                            f.pairs[slot] = ea < eb ? make_int2(ca, cb) : make_int2(cb, ca);
-                        }
+            int c = stack[--sp];
+            if (c < 0) {
+                int q = ~c;
+                if (q <= p) continue;
+                int cb = f.order[q];
+                if (!overlap_incl(qmin, qmax, w.aabb_min[cb], w.aabb_max[cb])) continue;
+                if (!pair_ok(w, ca, cb)) continue;
+                if (EMIT) {
+                    int slot = out + count;
+                    if (slot < f.pair_cap) {
+                        uint32_t ea = (uint32_t)w.info[w.col_info[ca].x].x, eb = (uint32_t)w.info[w.col_info[cb].x].x;
+                        f.pairs[slot] = ea < eb ? make_int2(ca, cb) : make_int2(cb, ca);
                     }
-                    ++count;
+                }
+                ++count;
+            } else {
+                if (f.bvh.last[c] <= p) continue;
+                if (!overlap_incl(qmin, qmax, f.bvh.bmin[c], f.bvh.bmax[c])) continue;
+                if (sp + 2 <= 64) {
+                    stack[sp++] = f.bvh.right[c];
+                    stack[sp++] = f.bvh.left[c];
                 } else {
-                    if (f.bvh.last[c] <= p) continue;
-                    if (!overlap_incl(qmin, qmax, f.bvh.bmin[c], f.bvh.bmax[c])) continue;
-                    if (sp < 64) stack[sp++] = c;
-                    else atomicOr(w.err, ERR_STACK_CAPACITY);
+                    atomicOr(w.err, ERR_STACK_CAPACITY);
                 }
             }
         }
     }
-    if (!EMIT) {
-        f.leaf_cnt[p] = count;
-    } else {
-        // the traversal order depends on the tree's shape; order the leaf's pairs by the
-        // partner collider instead, so the pair list depends only on the scene itself
-        int n_out = min(count, f.pair_cap - out);
-        for (int i = 1; i < n_out; ++i) {
-            int2 v = f.pairs[out + i];
-            int kv = v.x == ca ? v.y : v.x;
-            int j = i - 1;
-            for (; j >= 0; --j) {
-                int2 u = f.pairs[out + j];
-                int ku = u.x == ca ? u.y : u.x;
-                if (ku <= kv) break;
-                f.pairs[out + j + 1] = u;
-            }
-            f.pairs[out + j + 1] = v;
-        }
-    }
+    if (!EMIT) f.leaf_cnt[p] = count;
 }
 
 __global__ void k_pairs_check(FrameBuf f, int* err) {
@@ -315,7 +309,7 @@ int launch_broadphase(const World& w, FrameBuf& f, int scene_bits, cudaStream_t 
     k_scene_bounds<<<w.n_scenes, 256, 0, s>>>(w, f);
     k_morton<<<nb, 256, 0, s>>>(w, f);
     // (scene, Morton) order as two stable LSD sorts: Morton first, then scene
-    int k = 2 + radix_sort_pairs(f.keys, f.order, f.keys_tmp, f.order_tmp, n, 31, f.radix_hist, s);
+    int k = 2 + radix_sort_pairs(f.keys, f.order, f.keys_tmp, f.order_tmp, n, 32, f.radix_hist, s);
     if (scene_bits > 0) {
         k_scene_keys<<<nb, 256, 0, s>>>(w, f);
         k += 1 + radix_sort_pairs(f.keys, f.order, f.keys_tmp, f.order_tmp, n, scene_bits, f.radix_hist, s);

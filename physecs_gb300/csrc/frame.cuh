@@ -58,6 +58,11 @@ struct FrameBuf {
     int* scene_ncolor;    // [S]
     int* color_start;     // [S * (kMaxColors+1)]
     int* claim_pos;       // [S * (kMaxColors+1)] scatter counters
+    // per-substep contact records of scenes whose records do not fit in shared memory
+    int* pt_off;          // [man_cap] first point of each contact, colour order
+    int2* cbody;          // [man_cap] colouring: scene-local dynamic bodies of each contact
+    SHdr* s_hdr;          // [man_cap]
+    SPt* s_pts;           // [4 * man_cap]
     // restitution cache: open addressing, two tables; cache_parity selects the current one
     int cache_cap;        // power of two
     CacheEntry* cache_a;
@@ -77,8 +82,17 @@ int launch_aabb_range(const World& w, int c0, int c1, int margin_mode, cudaStrea
 int launch_broadphase(const World& w, FrameBuf& f, int scene_bits, cudaStream_t s);
 int launch_narrowphase(const World& w, FrameBuf& f, cudaStream_t s);
 int launch_contacts(const World& w, FrameBuf& f, cudaStream_t s);
-int launch_solver(const World& w, FrameBuf& f, const int* block_scenes, int n_block_scenes, const int* grid_scenes,
-                  int n_grid_scenes, int grid_blocks, cudaStream_t s);
+// scenes of one frame's solver launch: small block scenes (one 256-thread block each),
+// large block scenes (one 512-thread block each, on the aux stream), grid scenes
+// (the whole grid, one after another)
+struct SolverLaunch {
+    const int* small; int n_small; int smem_small;
+    const int* large; int n_large; int smem_large;
+    const int* grid; int n_grid; int grid_blocks;
+    cudaStream_t aux;
+    cudaEvent_t fork, join;
+};
+int launch_solver(const World& w, FrameBuf& f, const SolverLaunch& L, cudaStream_t s);
 int solver_grid_blocks();
 int launch_joint_layout(const World& w, FrameBuf& f, cudaStream_t s);
 

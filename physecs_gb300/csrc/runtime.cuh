@@ -43,6 +43,12 @@ struct psx_world {
     int* block_scenes = nullptr;
     int* grid_scenes = nullptr;
     int grid_blocks = 0;
+    int solver_smem = 0;             // dynamic shared memory per solver block (bytes)
+    int solver_smem_large = 0;       // the same for the 512-thread blocks of large scenes
+    std::vector<int> large_scenes_h; // block scenes above 1024 dynamic bodies
+    int* large_scenes = nullptr;
+    cudaStream_t aux_stream = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::vector<float4> h_knobs;
     bool use_graph = false;
     cudaGraphExec_t graph = nullptr;
@@ -78,6 +84,9 @@ struct psx_world {
         if (graph) cudaGraphExecDestroy(graph);
         for (void* p : allocs) cudaFree(p);
         if (pin) cudaFreeHost(pin);
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
+        if (aux_stream) cudaStreamDestroy(aux_stream);
         if (stream) cudaStreamDestroy(stream);
     }
 };

@@ -367,15 +367,40 @@ __device__ void row_presolve(const World& w, Row& r, bool simd) {
     }
 }
 
+// Body velocities the iterations work on: six float arrays in shared memory for a scene
+// that fits (s != null, body d at index d - off), else the world's vt arrays.
+struct VelRef {
+    float* s;
+    float4* v;
+    float4* w;
+    int off, n;
+    __device__ __forceinline__ V3 lv(int d) const {
+        if (s) { int i = d - off; return {s[i], s[n + i], s[2 * n + i]}; }
+        return ld3(v[d]);
+    }
+    __device__ __forceinline__ V3 lw(int d) const {
+        if (s) { int i = d - off; return {s[3 * n + i], s[4 * n + i], s[5 * n + i]}; }
+        return ld3(w[d]);
+    }
+    __device__ __forceinline__ void sv(int d, V3 x) const {
+        if (s) { int i = d - off; s[i] = x.x; s[n + i] = x.y; s[2 * n + i] = x.z; }
+        else v[d] = st4(x);
+    }
+    __device__ __forceinline__ void sw(int d, V3 x) const {
+        if (s) { int i = d - off; s[3 * n + i] = x.x; s[4 * n + i] = x.y; s[5 * n + i] = x.z; }
+        else w[d] = st4(x);
+    }
+};
+
 // Constraint1D(W)::solve for one row (Constraint1D.cpp:54-127 / Constraint1DW.cpp:117-233)
-__device__ void row_solve(const World& w, Row& r, float h, bool warm, bool simd) {
+__device__ void row_solve(const World& w, Row& r, float h, bool warm, bool simd, const VelRef& vr) {
     int fl = r.flags;
     bool angf = fl & 2, soft = fl & 1, lim = fl & 4;
     float inv = r.angular1t.w;
     if (!simd && !inv) return;
     V3 v0 = {0, 0, 0}, w0 = {0, 0, 0}, v1 = {0, 0, 0}, w1 = {0, 0, 0};
-    if (r.b0 >= 0) { if (!angf) v0 = ld3(w.vt_v[r.b0]); w0 = ld3(w.vt_w[r.b0]); }
-    if (r.b1 >= 0) { if (!angf) v1 = ld3(w.vt_v[r.b1]); w1 = ld3(w.vt_w[r.b1]); }
+    if (r.b0 >= 0) { if (!angf) v0 = vr.lv(r.b0); w0 = vr.lw(r.b0); }
+    if (r.b1 >= 0) { if (!angf) v1 = vr.lv(r.b1); w1 = vr.lw(r.b1); }
     V3 l0t = ld3(r.linear0t), l1t = ld3(r.linear1t), a0t = ld3(r.angular0t), a1t = ld3(r.angular1t);
     float c = r.angular0.w;
     if (!soft && warm) {
@@ -437,20 +462,20 @@ __device__ void row_solve(const World& w, Row& r, float h, bool warm, bool simd)
     if (!simd) {
         // the scalar row applies only this iteration's impulse (Constraint1D.cpp:158-168)
         if (r.b0 >= 0) {
-            if (!angf) w.vt_v[r.b0] = st4(ld3(w.vt_v[r.b0]) + lambda * l0t);
-            w.vt_w[r.b0] = st4(ld3(w.vt_w[r.b0]) + lambda * a0t);
+            if (!angf) vr.sv(r.b0, vr.lv(r.b0) + lambda * l0t);
+            vr.sw(r.b0, vr.lw(r.b0) + lambda * a0t);
         }
         if (r.b1 >= 0) {
-            if (!angf) w.vt_v[r.b1] = st4(ld3(w.vt_v[r.b1]) - lambda * l1t);
-            w.vt_w[r.b1] = st4(ld3(w.vt_w[r.b1]) - lambda * a1t);
+            if (!angf) vr.sv(r.b1, vr.lv(r.b1) - lambda * l1t);
+            vr.sw(r.b1, vr.lw(r.b1) - lambda * a1t);
         }
         return;
     }
     if (!angf) { v0 += lambda * l0t; v1 -= lambda * l1t; }
     w0 += lambda * a0t;
     w1 -= lambda * a1t;
-    if (r.b0 >= 0) { if (!angf) w.vt_v[r.b0] = st4(v0); w.vt_w[r.b0] = st4(w0); }
-    if (r.b1 >= 0) { if (!angf) w.vt_v[r.b1] = st4(v1); w.vt_w[r.b1] = st4(w1); }
+    if (r.b0 >= 0) { if (!angf) vr.sv(r.b0, v0); vr.sw(r.b0, w0); }
+    if (r.b1 >= 0) { if (!angf) vr.sv(r.b1, v1); vr.sw(r.b1, w1); }
 }
 
 __constant__ int c_flag_order[6] = {0, 2, 1, 4, 3, 6};
@@ -463,12 +488,12 @@ __device__ void joint_presolve(const World& w, int j) {
             if (J.rowflags[k] == c_flag_order[fi]) row_presolve(w, R[k], J.simd != 0);
 }
 
-__device__ void joint_solve(const World& w, int j, float h, bool warm) {
+__device__ void joint_solve(const World& w, int j, float h, bool warm, const VelRef& vr) {
     JointDev& J = w.joints[j];
     Row* R = w.rows + j * kMaxRowsPerJoint;
     for (int fi = 0; fi < 6; ++fi)
         for (int k = 0; k < J.nrows; ++k)
-            if (J.rowflags[k] == c_flag_order[fi]) row_solve(w, R[k], h, warm, J.simd != 0);
+            if (J.rowflags[k] == c_flag_order[fi]) row_solve(w, R[k], h, warm, J.simd != 0, vr);
 }
 
 // ---------------------------------------------------------------- contacts (ContactConstraints.cpp)
@@ -477,114 +502,137 @@ __device__ __forceinline__ M3 world_invI(const World& w, int d) {
     return m3cols(ld3(w.mt[3 * d]), ld3(w.mt[3 * d + 1]), ld3(w.mt[3 * d + 2]));
 }
 
+
 // update contact rows (src/Physecs.cpp:366-427)
-__device__ void contact_update(const World& w, Contact& c) {
+__device__ void contact_update(const World& w, Contact& c, SHdr& H, SPt* P) {
     int4 i0 = w.info[c.body0], i1 = w.info[c.body1];
     Q4 q0 = ld4(w.quat[c.body0]), q1 = ld4(w.quat[c.body1]);
     V3 com0 = {0, 0, 0}, v0 = {0, 0, 0}, w0 = {0, 0, 0}, com1 = {0, 0, 0}, v1 = {0, 0, 0}, w1 = {0, 0, 0};
     if (c.b0 >= 0) { com0 = ld3(w.pos[c.body0]) + qrot(q0, ld3(w.com[i0.z])); v0 = ld3(w.vel[i0.z]); w0 = ld3(w.ang[i0.z]); }
     if (c.b1 >= 0) { com1 = ld3(w.pos[c.body1]) + qrot(q1, ld3(w.com[i1.z])); v1 = ld3(w.vel[i1.z]); w1 = ld3(w.ang[i1.z]); }
     V3 n = ld3(c.n);
+    H.n = c.n;
+    H.m = make_float4(c.b0 >= 0 ? w.com[c.b0].w : 0.f, c.b1 >= 0 ? w.com[c.b1].w : 0.f, c.frequency, c.damping);
+    H.i.x = c.b0;
+    H.i.y = c.b1;
+    H.i.z = c.np | (c.soft << 8);
     for (int k = 0; k < c.np; ++k) {
         ContactPt& p = c.p[k];
         V3 r0 = qrot(q0, ld3(p.r0)), r1 = qrot(q1, ld3(p.r1));
         V3 cp0 = com0 + r0, cp1 = com1 + r1;
         float cn = dot(cp1 - cp0, n);
-        V3 r0xn = cross(r0, n), r1xn = cross(r1, n);
         V3 rel = v1 + cross(w1, r1) - v0 - cross(w0, r0);
         float relN = dot(rel, n);
         V3 t = rel - relN * n;
         float tl = length(t);
         if (tl) t = t / tl;
         p.r1.w = cn;
-        p.r0xn = st4(r0xn, 0.f);      // lambdaN = 0
-        p.r1xn = st4(r1xn, 0.f);      // lambdaT = 0
-        p.t = st4(t, p.t.w);
-        p.r0xt = st4(cross(r0, t), p.r0xt.w);
-        p.r1xt = st4(cross(r1, t), 0.f);
+        SPt& q = P[k];
+        q.a = st4(cross(r0, n), 0.f);
+        q.b = st4(cross(r1, n), p.r0.w);
+        q.c.w = cn;
+        q.e = st4(t, 0.f);
+        q.f = st4(cross(r0, t), 0.f);
+        q.g = st4(cross(r1, t), 0.f);
     }
 }
 
-__device__ void contact_presolve(const World& w, Contact& c) {
-    float im0 = 0, im1 = 0;
+// ContactConstraints::preSolve (src/ContactConstraints.cpp:4-31) and the per-substep
+// constants of solve (:33-101)
+__device__ void contact_presolve(const World& w, SHdr& H, SPt* P, float h) {
+    const int b0 = H.i.x, b1 = H.i.y, np = H.i.z & 0xff;
+    const bool soft = (H.i.z >> 8) != 0;
+    const float im0 = H.m.x, im1 = H.m.y;
     M3 I0 = m3zero(), I1 = m3zero();
-    if (c.b0 >= 0) { im0 = w.com[c.b0].w; I0 = world_invI(w, c.b0); }
-    if (c.b1 >= 0) { im1 = w.com[c.b1].w; I1 = world_invI(w, c.b1); }
-    V3 n = ld3(c.n);
-    for (int k = 0; k < c.np; ++k) {
-        ContactPt& p = c.p[k];
-        V3 r0xn = ld3(p.r0xn), r1xn = ld3(p.r1xn), r0xt = ld3(p.r0xt), r1xt = ld3(p.r1xt), t = ld3(p.t);
+    V3 v0 = {0, 0, 0}, w0 = {0, 0, 0}, v1 = {0, 0, 0}, w1 = {0, 0, 0};
+    if (b0 >= 0) { I0 = world_invI(w, b0); v0 = ld3(w.vel[b0]); w0 = ld3(w.ang[b0]); }
+    if (b1 >= 0) { I1 = world_invI(w, b1); v1 = ld3(w.vel[b1]); w1 = ld3(w.ang[b1]); }
+    V3 n = ld3(H.n);
+    for (int k = 0; k < np; ++k) {
+        SPt& p = P[k];
+        V3 r0xn = ld3(p.a), r1xn = ld3(p.b), r0xt = ld3(p.f), r1xt = ld3(p.g), t = ld3(p.e);
         V3 r0xnt = mv(I0, r0xn), r1xnt = mv(I1, r1xn), r0xtt = mv(I0, r0xt), r1xtt = mv(I1, r1xt);
-        p.r0xnt = st4(r0xnt); p.r1xnt = st4(r1xnt); p.r0xtt = st4(r0xtt); p.r1xtt = st4(r1xtt);
-        p.t.w = dot(n, n) * (im0 + im1) + dot(r0xn, r0xnt) + dot(r1xn, r1xnt);
-        p.r0xt.w = dot(t, t) * (im0 + im1) + dot(r0xt, r0xtt) + dot(r1xt, r1xtt);
+        float invN = dot(n, n) * (im0 + im1) + dot(r0xn, r0xnt) + dot(r1xn, r1xnt);
+        float invT = dot(t, t) * (im0 + im1) + dot(r0xt, r0xtt) + dot(r1xt, r1xtt);
+        float cc = p.c.w;
+        float t1 = 0.f, t2 = 0.f, lamT = 0.f;
+        if (invN) {
+            float eff = 1.f / invN;
+            if (soft) {
+                float af = 2.f * kPi * H.m.z;
+                float stiffness = af * af * eff;
+                float damping = 2.f * af * H.m.w * eff;
+                float gamma = 1.f / (damping + h * stiffness);
+                float beta = h * stiffness / (damping + h * stiffness);
+                t1 = beta * cc / h;
+                t2 = invN + gamma / h;
+            } else {
+                t1 = 0.1f * cc / h;
+                t2 = eff;
+            }
+        }
+        if (invT) {
+            float rv = dot(-t, v0) + dot(-r0xt, w0) + dot(t, v1) + dot(r1xt, w1);
+            lamT = rv / invT;
+        }
+        int live = (invN ? 1 : 0) | (invT ? 2 : 0);
+        p.c = st4(r0xnt, t1);
+        p.d = st4(r1xnt, t2);
+        p.f = st4(r0xtt, lamT);
+        p.g = st4(r1xtt, __int_as_float(live));
     }
 }
 
-__device__ void contact_solve(const World& w, Contact& c, bool useBias, float h) {
-    V3 n = ld3(c.n);
-    float friction = c.n.w;
-    float im0 = c.b0 >= 0 ? w.com[c.b0].w : 0.f, im1 = c.b1 >= 0 ? w.com[c.b1].w : 0.f;
-    for (int i = 0; i < c.np; ++i) {
-        ContactPt& p = c.p[i];
-        float invN = p.t.w;
-        if (!invN) continue;
+// ContactConstraints::solve (src/ContactConstraints.cpp:33-124)
+__device__ void contact_solve(const SHdr& H, SPt* P, bool useBias, const VelRef& vr) {
+    const V3 n = ld3(H.n);
+    const float friction = H.n.w;
+    const float im0 = H.m.x, im1 = H.m.y;
+    const int b0 = H.i.x, b1 = H.i.y, np = H.i.z & 0xff;
+    const bool soft = (H.i.z >> 8) != 0;
+    for (int i = 0; i < np; ++i) {
+        SPt& p = P[i];
+        if (!(__float_as_int(p.g.w) & 1)) continue;
         V3 v0 = {0, 0, 0}, w0 = {0, 0, 0}, v1 = {0, 0, 0}, w1 = {0, 0, 0};
-        if (c.b0 >= 0) { v0 = ld3(w.vt_v[c.b0]); w0 = ld3(w.vt_w[c.b0]); }
-        if (c.b1 >= 0) { v1 = ld3(w.vt_v[c.b1]); w1 = ld3(w.vt_w[c.b1]); }
-        V3 r0xn = ld3(p.r0xn), r1xn = ld3(p.r1xn);
+        if (b0 >= 0) { v0 = vr.lv(b0); w0 = vr.lw(b0); }
+        if (b1 >= 0) { v1 = vr.lv(b1); w1 = vr.lw(b1); }
+        V3 r0xn = ld3(p.a), r1xn = ld3(p.b);
         float rv = dot(-n, v0) + dot(-r0xn, w0) + dot(n, v1) + dot(r1xn, w1);
-        float eff = 1.f / invN;
         float lambda;
-        float cc = p.r1.w;
-        if (c.soft) {
-            float af = 2.f * kPi * c.frequency;
-            float stiffness = af * af * eff;
-            float damping = 2.f * af * c.damping * eff;
-            float gamma = 1.f / (damping + h * stiffness);
-            float beta = h * stiffness / (damping + h * stiffness);
-            lambda = (rv + beta * cc / h) / (invN + gamma / h);
-        } else {
-            lambda = (rv - p.r0.w + (useBias ? 0.1f * cc / h : 0.f)) * eff;
-        }
-        float prev = p.r0xn.w;
+        if (soft) lambda = (rv + p.c.w) / p.d.w;
+        else lambda = (rv - p.b.w + (useBias ? p.c.w : 0.f)) * p.d.w;
+        float prev = p.a.w;
         float tot = prev + lambda;
         tot = fminG(tot, 0.f);
-        p.r0xn.w = tot;
+        p.a.w = tot;
         lambda = tot - prev;
-        if (c.b0 >= 0) {
-            w.vt_v[c.b0] = st4(v0 + lambda * im0 * n);
-            w.vt_w[c.b0] = st4(w0 + lambda * ld3(p.r0xnt));
+        if (b0 >= 0) {
+            vr.sv(b0, v0 + lambda * im0 * n);
+            vr.sw(b0, w0 + lambda * ld3(p.c));
         }
-        if (c.b1 >= 0) {
-            w.vt_v[c.b1] = st4(v1 - lambda * im1 * n);
-            w.vt_w[c.b1] = st4(w1 - lambda * ld3(p.r1xnt));
+        if (b1 >= 0) {
+            vr.sv(b1, v1 - lambda * im1 * n);
+            vr.sw(b1, w1 - lambda * ld3(p.d));
         }
     }
-    // friction reads the component velocities (ContactConstraints.cpp:93-101)
-    for (int i = 0; i < c.np; ++i) {
-        ContactPt& p = c.p[i];
-        float invT = p.r0xt.w;
-        if (!invT) continue;
-        V3 v0 = {0, 0, 0}, w0 = {0, 0, 0}, v1 = {0, 0, 0}, w1 = {0, 0, 0};
-        if (c.b0 >= 0) { v0 = ld3(w.vel[c.b0]); w0 = ld3(w.ang[c.b0]); }
-        if (c.b1 >= 0) { v1 = ld3(w.vel[c.b1]); w1 = ld3(w.ang[c.b1]); }
-        V3 t = ld3(p.t), r0xt = ld3(p.r0xt), r1xt = ld3(p.r1xt);
-        float rv = dot(-t, v0) + dot(-r0xt, w0) + dot(t, v1) + dot(r1xt, w1);
-        float lambda = rv / invT;
-        float limit = friction * p.r0xn.w;
-        float prev = p.r1xn.w;
+    for (int i = 0; i < np; ++i) {
+        SPt& p = P[i];
+        if (!(__float_as_int(p.g.w) & 2)) continue;
+        V3 t = ld3(p.e);
+        float lambda = p.f.w;
+        float limit = friction * p.a.w;
+        float prev = p.e.w;
         float tot = prev + lambda;
         tot = clampG(tot, limit, -limit);
-        p.r1xn.w = tot;
+        p.e.w = tot;
         lambda = tot - prev;
-        if (c.b0 >= 0) {
-            w.vt_v[c.b0] = st4(ld3(w.vt_v[c.b0]) + lambda * im0 * t);
-            w.vt_w[c.b0] = st4(ld3(w.vt_w[c.b0]) + lambda * ld3(p.r0xtt));
+        if (b0 >= 0) {
+            vr.sv(b0, vr.lv(b0) + lambda * im0 * t);
+            vr.sw(b0, vr.lw(b0) + lambda * ld3(p.f));
         }
-        if (c.b1 >= 0) {
-            w.vt_v[c.b1] = st4(ld3(w.vt_v[c.b1]) - lambda * im1 * t);
-            w.vt_w[c.b1] = st4(ld3(w.vt_w[c.b1]) - lambda * ld3(p.r1xtt));
+        if (b1 >= 0) {
+            vr.sv(b1, vr.lv(b1) - lambda * im1 * t);
+            vr.sw(b1, vr.lw(b1) - lambda * ld3(p.g));
         }
     }
 }
@@ -592,7 +640,7 @@ __device__ void contact_solve(const World& w, Contact& c, bool useBias, float h)
 // ---------------------------------------------------------------- bodies
 
 // integrate velocities (src/Physecs.cpp:441-469)
-__device__ void integrate_velocity(const World& w, int d, float h, float g) {
+__device__ void integrate_velocity(const World& w, int d, float h, float g, const VelRef& vr) {
     int b = w.dyn_body[d];
     if (w.info[b].y & BODY_KIN) return;
     M3 rot = mat3_cast(ld4(w.quat[b]));
@@ -608,8 +656,8 @@ __device__ void integrate_velocity(const World& w, int d, float h, float g) {
     ang = mv(rot, wl);
     w.vel[d] = st4(vel);
     w.ang[d] = st4(ang);
-    w.vt_v[d] = st4(vel);
-    w.vt_w[d] = st4(ang);
+    vr.sv(d, vel);
+    vr.sw(d, ang);
     w.pv_v[d] = make_float4(0, 0, 0, 0);
     w.pv_w[d] = make_float4(0, 0, 0, 0);
     M3 wi = mm(mm(rot, invIl), invRot);
@@ -619,7 +667,7 @@ __device__ void integrate_velocity(const World& w, int d, float h, float g) {
 }
 
 // integrate positions (src/Physecs.cpp:492-512)
-__device__ void integrate_position(const World& w, int d, float h) {
+__device__ void integrate_position(const World& w, int d, float h, const VelRef& vr) {
     int b = w.dyn_body[d];
     if (w.info[b].y & BODY_KIN) return;
     float4 pv = w.pv_v[d];
@@ -627,9 +675,9 @@ __device__ void integrate_position(const World& w, int d, float h) {
     V3 pos = ld3(w.pos[b]);
     Q4 q = ld4(w.quat[b]);
     V3 com = ld3(w.com[d]);
-    pos += h * ld3(w.vt_v[d]) + s * ld3(pv);
+    pos += h * vr.lv(d) + s * ld3(pv);
     V3 prevCom = qrot(q, com);
-    V3 wv = 0.5f * (h * ld3(w.vt_w[d]) + s * ld3(w.pv_w[d]));
+    V3 wv = 0.5f * (h * vr.lw(d) + s * ld3(w.pv_w[d]));
     q = qadd(q, qmul(Q4{wv.x, wv.y, wv.z, 0.f}, q));
     q = qnormalize(q);
     pos += prevCom - qrot(q, com);
@@ -644,6 +692,32 @@ struct BlockSync {
     __device__ __forceinline__ int tid() const { return threadIdx.x; }
     __device__ __forceinline__ int nth() const { return blockDim.x; }
     __device__ __forceinline__ bool any(bool v) const { return __syncthreads_or(v) != 0; }
+    // bit 0: a == true somewhere, bit 1: b == true somewhere
+    __device__ __forceinline__ int any2(bool a, bool b) const {
+        return (__syncthreads_or(a) ? 1 : 0) | (__syncthreads_or(b) ? 2 : 0);
+    }
+    // first point of each contact (colour order) packed without gaps; returns the point count
+    __device__ int point_offsets(FrameBuf& f, int ms, int nc) const {
+        __shared__ int part[1025];
+        const int t = threadIdx.x, T = blockDim.x;
+        const int chunk = (nc + T - 1) / T;
+        const int k0 = min(nc, t * chunk), k1 = min(nc, k0 + chunk);
+        int sum = 0;
+        for (int k = k0; k < k1; ++k) sum += f.contacts[f.corder[ms + k]].np;
+        part[t] = sum;
+        __syncthreads();
+        if (t == 0) {
+            int acc = 0;
+            for (int i = 0; i < T; ++i) { int v = part[i]; part[i] = acc; acc += v; }
+            part[T] = acc;
+        }
+        __syncthreads();
+        int acc = part[t];
+        for (int k = k0; k < k1; ++k) { f.pt_off[ms + k] = acc; acc += f.contacts[f.corder[ms + k]].np; }
+        const int total = part[T];
+        __syncthreads();
+        return total;
+    }
 };
 struct GridSync {
     GridBarrier bar;
@@ -660,10 +734,87 @@ struct GridSync {
         bar.sync();
         return r;
     }
+    __device__ __forceinline__ int any2(bool a, bool b) const { return (any(a) ? 1 : 0) | (any(b) ? 2 : 0); }
+    // four point slots per contact (no cross-block scan in grid mode)
+    __device__ int point_offsets(FrameBuf& f, int ms, int nc) const {
+        for (int k = tid(); k < nc; k += nth()) f.pt_off[ms + k] = 4 * k;
+        bar.sync();
+        return 4 * nc;
+    }
 };
 
+// Colouring of one scene's contacts (see solve_scene); claim[d - ds], cb[k], col[k] are
+// indexed by scene-local dynamic body and contact.  Returns the number of colours.  When
+// kMaxColors - 1 colours leave contacts over (a body touching more than that many others),
+// the rest form a last colour that is solved by one thread in contact order.
 template <class S>
-__device__ void solve_scene(const World& w, FrameBuf& f, int s, const S& sy) {
+__device__ int colour_contacts(const World& w, FrameBuf& f, int ms, int nc, int ds, int nd, const S& sy,
+                               unsigned long long* claim, int2* cb, int* col) {
+    const int tid = sy.tid(), nth = sy.nth();
+    const unsigned long long kFree = ~0ull;
+    for (int d = tid; d < nd; d += nth) claim[d] = kFree;
+    for (int k = tid; k < nc; k += nth) {
+        const Contact& c = f.contacts[ms + k];
+        cb[k] = make_int2(c.b0 >= 0 ? c.b0 - ds : -1, c.b1 >= 0 ? c.b1 - ds : -1);
+        col[k] = -1;
+    }
+    sy.sync();
+    int ncol = 0;
+    for (;;) {
+        bool any_left = false;
+        for (int round = 0;; ++round) {
+            for (int k = tid; k < nc; k += nth) {
+                if (col[k] >= 0) continue;
+                const int2 b = cb[k];
+                bool free0 = b.x < 0 || (unsigned)(claim[b.x] >> 48) != (unsigned)ncol;
+                bool free1 = b.y < 0 || (unsigned)(claim[b.y] >> 48) != (unsigned)ncol;
+                if (!(free0 && free1)) continue;
+                unsigned long long pri = 0xffff000000000000ull |
+                    ((unsigned long long)(cache_hash((unsigned long long)k * 0x9E3779B97F4A7C15ull + 131u * ncol + round) & 0xffffu) << 32) |
+                    (unsigned)k;
+                if (b.x >= 0) atomicMin(&claim[b.x], pri);
+                if (b.y >= 0) atomicMin(&claim[b.y], pri);
+            }
+            sy.sync();
+            bool joined = false, left = false;
+            for (int k = tid; k < nc; k += nth) {
+                if (col[k] >= 0) continue;
+                const int2 b = cb[k];
+                unsigned long long k0 = b.x >= 0 ? claim[b.x] : 0, k1 = b.y >= 0 ? claim[b.y] : 0;
+                bool own0 = b.x < 0 || ((k0 >> 48) == 0xffffull && (unsigned)k0 == (unsigned)k);
+                bool own1 = b.y < 0 || ((k1 >> 48) == 0xffffull && (unsigned)k1 == (unsigned)k);
+                if (own0 && own1) { col[k] = ncol; joined = true; }
+                else left = true;
+            }
+            sy.sync();
+            // bodies of the colour's members are held by the colour; other claims reset
+            for (int k = tid; k < nc; k += nth) {
+                if (col[k] != ncol) continue;
+                const int2 b = cb[k];
+                if (b.x >= 0) claim[b.x] = (unsigned long long)ncol << 48;
+                if (b.y >= 0) claim[b.y] = (unsigned long long)ncol << 48;
+            }
+            sy.sync();
+            for (int d = tid; d < nd; d += nth)
+                if ((claim[d] >> 48) == 0xffffull) claim[d] = kFree;
+            int flags = sy.any2(joined, left);
+            if (!(flags & 1) || !(flags & 2)) { any_left = (flags & 2) != 0; break; }
+        }
+        ++ncol;
+        for (int d = tid; d < nd; d += nth) claim[d] = kFree;   // the next colour starts free
+        sy.sync();
+        if (!any_left) break;
+        if (ncol == kMaxColors - 1) {
+            for (int k = tid; k < nc; k += nth) if (col[k] < 0) col[k] = ncol;
+            sy.sync();
+            return -kMaxColors;   // negative: the last colour is serial
+        }
+    }
+    return ncol;
+}
+
+template <class S>
+__device__ void solve_scene(const World& w, FrameBuf& f, int s, const S& sy, float4* smem, int smem_f4) {
     if (w.scene_active && !w.scene_active[s]) return;
     const int tid = sy.tid(), nth = sy.nth();
     int ds = w.scene_dyn[s], de = w.scene_dyn[s + 1];
@@ -672,71 +823,67 @@ __device__ void solve_scene(const World& w, FrameBuf& f, int s, const S& sy) {
     int substeps = (int)kn.x, iterations = (int)kn.y;
     float g = kn.z, dt = kn.w;
     int* colstart = f.color_start + s * (kMaxColors + 1);
-    // ---- graph colouring of the contacts: rounds in which every uncoloured contact claims
-    // its dynamic bodies with a hashed priority; a contact that holds all its bodies takes
-    // the round's colour.  Hashed (not index) priorities keep the round count logarithmic.
-    // Priorities use the contact's index within its scene, so a scene is coloured the
-    // same way whatever other scenes share the world.
-    const unsigned long long kFree = ~0ull;
-    for (int d = ds + tid; d < de; d += nth) f.claim[d] = kFree;
-    for (int m = ms + tid; m < me; m += nth) f.color_of[m] = -1;
-    sy.sync();
-    int ncol = 0;
-    for (;;) {
-        for (int m = ms + tid; m < me; m += nth) {
-            if (f.color_of[m] >= 0) continue;
-            const Contact& c = f.contacts[m];
-            const unsigned ml = (unsigned)(m - ms);
-            unsigned long long pri = ((unsigned long long)cache_hash((unsigned long long)ml * 0x9E3779B97F4A7C15ull + ncol) << 32) | ml;
-            if (c.b0 >= 0) atomicMin(&f.claim[c.b0], pri);
-            if (c.b1 >= 0) atomicMin(&f.claim[c.b1], pri);
-        }
-        sy.sync();
-        bool left = false;
-        for (int m = ms + tid; m < me; m += nth) {
-            if (f.color_of[m] >= 0) continue;
-            const Contact& c = f.contacts[m];
-            const unsigned ml = (unsigned)(m - ms);
-            bool ok = (c.b0 < 0 || (unsigned)f.claim[c.b0] == ml) && (c.b1 < 0 || (unsigned)f.claim[c.b1] == ml);
-            if (ok && ncol < kMaxColors) f.color_of[m] = ncol;
-            else left = true;
-        }
-        bool any = sy.any(left);
-        for (int d = ds + tid; d < de; d += nth) f.claim[d] = kFree;
-        ++ncol;
-        sy.sync();
-        if (!any) break;
-        if (ncol >= kMaxColors) { if (tid == 0) atomicOr(w.err, ERR_COLOR_CAPACITY); break; }
-    }
+    // ---- graph colouring of the contacts.  Each colour is a maximal set of contacts with
+    // no dynamic body in common, grown in rounds: every uncoloured contact whose bodies
+    // the colour does not hold yet claims them with a hashed priority, and the contacts
+    // that hold all their bodies join the colour.  Priorities use the contact's index
+    // within its scene, so a scene is coloured the same way whatever other scenes
+    // share the world.  The working arrays (bodies of each contact, colour of each
+    // contact, one claim word per dynamic body) live in shared memory when they fit.
+    const int nd = de - ds, nc = me - ms;
+    const bool col_smem = 8 * (size_t)nd + 12 * (size_t)nc <= 16 * (size_t)smem_f4;
+    unsigned long long* claim = col_smem ? (unsigned long long*)smem : f.claim + ds;
+    int2* cb = col_smem ? (int2*)(claim + nd) : f.cbody + ms;
+    int* col = col_smem ? (int*)(cb + nc) : f.color_of + ms;
+    int ncol = colour_contacts(w, f, ms, nc, ds, nd, sy, claim, cb, col);
+    const bool serial_last = ncol < 0;
+    if (serial_last) ncol = -ncol;
     // counting sort of the scene's contacts by colour
     for (int k = tid; k <= kMaxColors; k += nth) colstart[k] = 0;
     sy.sync();
-    for (int m = ms + tid; m < me; m += nth) { int cl = f.color_of[m]; if (cl >= 0) atomicAdd(&colstart[cl + 1], 1); }
+    for (int k = tid; k < nc; k += nth) { int cl = col[k]; if (cl >= 0) atomicAdd(&colstart[cl + 1], 1); }
     sy.sync();
     if (tid == 0) {
         for (int k = 0; k < kMaxColors; ++k) colstart[k + 1] += colstart[k];
         f.scene_ncolor[s] = ncol;
     }
     sy.sync();
-    for (int m = ms + tid; m < me; m += nth) {
-        int cl = f.color_of[m];
-        if (cl < 0) continue;
-        // position within the colour: count of lower-index contacts of the same colour is not needed,
+    for (int k = tid; k < nc; k += nth) {
+        int cl = col[k];
+        if (col_smem) f.color_of[ms + k] = cl;   // kept for inspection
+        if (cl < 0 || (serial_last && cl == ncol - 1)) continue;
         // contacts of one colour touch disjoint bodies and may be solved in any order
         int pos = atomicAdd(&f.claim_pos[s * (kMaxColors + 1) + cl], 1);
-        f.corder[ms + colstart[cl] + pos] = m;
+        f.corder[ms + colstart[cl] + pos] = ms + k;
     }
+    if (serial_last && tid == 0) {
+        // the serial colour keeps contact order
+        int pos = 0;
+        for (int k = 0; k < nc; ++k) if (col[k] == ncol - 1) f.corder[ms + colstart[ncol - 1] + pos++] = ms + k;
+    }
+    sy.sync();
+    // ---- where the substep data lives: velocities and contact records in shared memory
+    // when they fit, velocities alone when only they fit, else the world's buffers
+    const int ncl = colstart[kMaxColors];   // coloured contacts (all, unless the colour cap was hit)
+    int npts = sy.point_offsets(f, ms, ncl);   // first point of each contact -> f.pt_off[ms + k]
+    const int vel_f4 = (6 * nd + 3) / 4;
+    const bool vel_smem = vel_f4 <= smem_f4;
+    const bool rec_smem = vel_smem && vel_f4 + kHdrF4 * ncl + kPtF4 * npts <= smem_f4;
+    VelRef vr = vel_smem ? VelRef{(float*)smem, nullptr, nullptr, ds, nd} : VelRef{nullptr, w.vt_v, w.vt_w, 0, 0};
+    SHdr* H = rec_smem ? (SHdr*)(smem + vel_f4) : f.s_hdr + ms;
+    SPt* P = rec_smem ? (SPt*)(smem + vel_f4 + kHdrF4 * ncl) : f.s_pts + 4 * (size_t)ms;
+    for (int k = tid; k < ncl; k += nth) H[k].i.w = f.pt_off[ms + k];
     sy.sync();
     int js0 = w.scene_jsteps[s], js1 = w.scene_jsteps[s + 1];
     int jb = w.scene_joint[s], je = w.scene_joint[s + 1];
     float h = dt / substeps;
     for (int sub = 0; sub < substeps; ++sub) {
-        for (int m = ms + tid; m < me; m += nth) contact_update(w, f.contacts[m]);
+        for (int k = tid; k < ncl; k += nth) contact_update(w, f.contacts[f.corder[ms + k]], H[k], P + H[k].i.w);
         for (int j = jb + tid; j < je; j += nth) make_joint_rows(w, j);
         sy.sync();
-        for (int d = ds + tid; d < de; d += nth) integrate_velocity(w, d, h, g);
+        for (int d = ds + tid; d < de; d += nth) integrate_velocity(w, d, h, g, vr);
         sy.sync();
-        for (int m = ms + tid; m < me; m += nth) contact_presolve(w, f.contacts[m]);
+        for (int k = tid; k < ncl; k += nth) contact_presolve(w, H[k], P + H[k].i.w, h);
         for (int st = js0; st < js1; ++st) {
             for (int k = w.jstep_start[st] + tid; k < w.jstep_start[st + 1]; k += nth) joint_presolve(w, w.jsched[k]);
             sy.sync();
@@ -744,42 +891,60 @@ __device__ void solve_scene(const World& w, FrameBuf& f, int s, const S& sy) {
         sy.sync();
         for (int it = 0; it < iterations; ++it) {
             for (int cl = 0; cl < ncol; ++cl) {
-                for (int k = colstart[cl] + tid; k < colstart[cl + 1]; k += nth) contact_solve(w, f.contacts[f.corder[ms + k]], true, h);
+                if (serial_last && cl == ncol - 1) {
+                    if (tid == 0)
+                        for (int k = colstart[cl]; k < colstart[cl + 1]; ++k) contact_solve(H[k], P + H[k].i.w, true, vr);
+                } else {
+                    for (int k = colstart[cl] + tid; k < colstart[cl + 1]; k += nth) contact_solve(H[k], P + H[k].i.w, true, vr);
+                }
                 sy.sync();
             }
             for (int st = js0; st < js1; ++st) {
-                for (int k = w.jstep_start[st] + tid; k < w.jstep_start[st + 1]; k += nth) joint_solve(w, w.jsched[k], h, it == 0);
+                for (int k = w.jstep_start[st] + tid; k < w.jstep_start[st + 1]; k += nth) joint_solve(w, w.jsched[k], h, it == 0, vr);
                 sy.sync();
             }
         }
-        for (int d = ds + tid; d < de; d += nth) integrate_position(w, d, h);
+        for (int d = ds + tid; d < de; d += nth) integrate_position(w, d, h, vr);
         sy.sync();
         for (int cl = 0; cl < ncol; ++cl) {
-            for (int k = colstart[cl] + tid; k < colstart[cl + 1]; k += nth) {
-                Contact& c = f.contacts[f.corder[ms + k]];
-                if (!c.soft) contact_solve(w, c, false, 0.f);
+            if (serial_last && cl == ncol - 1) {
+                if (tid == 0)
+                    for (int k = colstart[cl]; k < colstart[cl + 1]; ++k)
+                        if (!(H[k].i.z >> 8)) contact_solve(H[k], P + H[k].i.w, false, vr);
+            } else {
+                for (int k = colstart[cl] + tid; k < colstart[cl + 1]; k += nth)
+                    if (!(H[k].i.z >> 8)) contact_solve(H[k], P + H[k].i.w, false, vr);
             }
             sy.sync();
         }
         for (int d = ds + tid; d < de; d += nth) {
             int b = w.dyn_body[d];
             if (w.info[b].y & BODY_KIN) continue;
-            w.vel[d] = w.vt_v[d];
-            w.ang[d] = w.vt_w[d];
+            w.vel[d] = st4(vr.lv(d));
+            w.ang[d] = st4(vr.lw(d));
         }
         sy.sync();
     }
+    // accumulated impulses back into the frame's contacts (inspection only)
+    for (int k = tid; k < ncl; k += nth) {
+        Contact& c = f.contacts[f.corder[ms + k]];
+        const SPt* q = P + H[k].i.w;
+        for (int i = 0; i < c.np; ++i) { c.p[i].r0xn.w = q[i].a.w; c.p[i].r1xn.w = q[i].e.w; }
+    }
 }
 
-__global__ void __launch_bounds__(256) k_solve_block(World w, FrameBuf f, const int* scenes) {
+// one scene per block; NT = 256 for scenes up to 1024 dynamic bodies, 512 above
+template <int NT>
+__global__ void __launch_bounds__(NT) k_solve_block(World w, FrameBuf f, const int* scenes, int smem_f4) {
+    extern __shared__ float4 smem[];
     BlockSync sy;
-    solve_scene(w, f, scenes[blockIdx.x], sy);
+    solve_scene(w, f, scenes[blockIdx.x], sy, smem, smem_f4);
 }
 
 __global__ void __launch_bounds__(256) k_solve_grid(World w, FrameBuf f, const int* scenes, int n) {
     GridSync sy{GridBarrier{f.bar, f.bar + 1, w.err}, (int*)(f.bar + 2)};
     for (int i = 0; i < n; ++i) {
-        solve_scene(w, f, scenes[i], sy);
+        solve_scene(w, f, scenes[i], sy, nullptr, 0);
         sy.sync();
     }
 }
@@ -807,16 +972,40 @@ int solver_grid_blocks() {
     return sms * per;
 }
 
-int launch_solver(const World& w, FrameBuf& f, const int* block_scenes, int n_block_scenes, const int* grid_scenes,
-                  int n_grid_scenes, int grid_blocks, cudaStream_t s) {
+template <int NT>
+static void set_smem(int bytes) {
+    static int done = -1;
+    if (done != bytes) {
+        cudaFuncSetAttribute(k_solve_block<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        done = bytes;
+    }
+}
+
+int launch_solver(const World& w, FrameBuf& f, const SolverLaunch& L, cudaStream_t s) {
     k_zero_ints<<<(w.n_scenes * (kMaxColors + 1) + 255) / 256, 256, 0, s>>>(f.claim_pos, w.n_scenes * (kMaxColors + 1));
     int k = 2;
-    if (n_block_scenes) { k_solve_block<<<n_block_scenes, 256, 0, s>>>(w, f, block_scenes); ++k; }
-    if (n_grid_scenes) {
+    // large scenes on a second stream, concurrently with the small ones
+    if (L.n_large) {
+        set_smem<512>(L.smem_large);
+        cudaEventRecord(L.fork, s);
+        cudaStreamWaitEvent(L.aux, L.fork, 0);
+        k_solve_block<512><<<L.n_large, 512, L.smem_large, L.aux>>>(w, f, L.large, L.smem_large / 16);
+        cudaEventRecord(L.join, L.aux);
+        ++k;
+    }
+    if (L.n_small) {
+        set_smem<256>(L.smem_small);
+        k_solve_block<256><<<L.n_small, 256, L.smem_small, s>>>(w, f, L.small, L.smem_small / 16);
+        ++k;
+    }
+    if (L.n_large) cudaStreamWaitEvent(s, L.join, 0);
+    if (L.n_grid) {
         World wc = w;
         FrameBuf fc = f;
-        void* args[] = {(void*)&wc, (void*)&fc, (void*)&grid_scenes, (void*)&n_grid_scenes};
-        cudaLaunchCooperativeKernel((void*)k_solve_grid, grid_blocks, 256, args, 0, s);
+        const int* gs = L.grid;
+        int ng = L.n_grid;
+        void* args[] = {(void*)&wc, (void*)&fc, (void*)&gs, (void*)&ng};
+        cudaLaunchCooperativeKernel((void*)k_solve_grid, L.grid_blocks, 256, args, 0, s);
         ++k;
     }
     k_cache_flip<<<1, 1, 0, s>>>(f);

@@ -101,6 +101,28 @@ struct JointDev {
     int rowflags[kMaxRowsPerJoint];
 };
 
+// Per-substep solver record of one contact (ContactConstraints, src/ContactConstraints.h:31-48),
+// written in colour order:
+//   n = {normal, friction}   m = {invMass0, invMass1, frequency, damping}
+//   i = {dynamic body 0 or -1, dynamic body 1 or -1, numPoints | soft << 8, first point}
+struct SHdr {
+    float4 n, m;
+    int4 i;
+};
+// One ContactPointConstraints as the iterations read it:
+//   a = {r0 x n, lambdaN}          b = {r1 x n, targetVelocity}
+//   c = {I0 (r0 x n), bias term}   d = {I1 (r1 x n), effective-mass term}
+//   e = {t, lambdaT}               f = {I0 (r0 x t), friction impulse}
+//   g = {I1 (r1 x t), live rows: 1 normal (invEffMassN != 0), 2 friction (invEffMassT != 0)}
+// Between the row update and preSolve, f/g.xyz hold r0 x t / r1 x t and c.w the separation.
+// Friction reads the component velocities, which stay fixed through a substep's
+// iterations (ContactConstraints.cpp:93-101), so its unclamped impulse is formed once
+// per substep in preSolve with the same operations.
+struct SPt {
+    float4 a, b, c, d, e, f, g;
+};
+constexpr int kHdrF4 = 3, kPtF4 = 7;
+
 struct CacheEntry {      // restitution cache (include/Physecs/Physecs.h:127-135)
     unsigned long long key;
     int np, pad;

@@ -327,8 +327,9 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
         scene_joint.push_back((int)joints.size());
         W->h_knobs.push_back(f4((float)d.num_substeps, (float)d.num_iterations, d.gravity, 1.f / 60.f));
         int nd = scene_dyn[s + 1] - scene_dyn[s];
-        if (nd <= o.block_scene_max_dyn) W->block_scenes_h.push_back(s);
-        else W->grid_scenes_h.push_back(s);
+        if (nd > o.block_scene_max_dyn) W->grid_scenes_h.push_back(s);
+        else if (nd > 1024) W->large_scenes_h.push_back(s);
+        else W->block_scenes_h.push_back(s);
     }
     std::sort(nc.begin(), nc.end(), [](int2 a, int2 b) { return a.x < b.x || (a.x == b.x && a.y < b.y); });
     nc.erase(std::unique(nc.begin(), nc.end(), [](int2 a, int2 b) { return a.x == b.x && a.y == b.y; }), nc.end());
@@ -440,6 +441,10 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
     PSX_TRY(W->alloc(f.scene_ncolor, S));
     PSX_TRY(W->alloc(f.color_start, (size_t)S * (kMaxColors + 1)));
     PSX_TRY(W->alloc(f.claim_pos, (size_t)S * (kMaxColors + 1)));
+    PSX_TRY(W->alloc(f.pt_off, f.man_cap));
+    PSX_TRY(W->alloc(f.cbody, f.man_cap));
+    PSX_TRY(W->alloc(f.s_hdr, f.man_cap));
+    PSX_TRY(W->alloc(f.s_pts, 4 * (size_t)f.man_cap));
     PSX_TRY(W->alloc(f.cache_a, f.cache_cap));
     PSX_TRY(W->alloc(f.cache_b, f.cache_cap));
     PSX_TRY(W->alloc(f.cache_parity, 1));
@@ -456,8 +461,20 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
     PSX_CUDA(cudaMemset(f.n_man, 0, sizeof(int)));
     PSX_CUDA(cudaMemset(f.scene_man, 0, sizeof(int) * (S + 1)));
     PSX_TRY(W->upload(W->block_scenes, W->block_scenes_h));
+    PSX_TRY(W->upload(W->large_scenes, W->large_scenes_h));
     PSX_TRY(W->upload(W->grid_scenes, W->grid_scenes_h));
     W->grid_blocks = W->grid_scenes_h.empty() ? 0 : solver_grid_blocks();
+    // shared memory per solver block: the most a block may have when there are at most as
+    // many block scenes as SMs, else a size that keeps three blocks resident per SM
+    {
+        int dev = 0, sms = 0, optin = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        int want = (int)W->block_scenes_h.size() <= sms ? optin - 5120 : 64 * 1024;
+        W->solver_smem = std::max(0, std::min(want, optin - 5120)) / 16 * 16;
+        W->solver_smem_large = std::max(0, optin - 5120) / 16 * 16;
+    }
     W->scene_bits = S <= 1 ? 0 : ilog2ceil(S);
     // creation bounds: no margin (src/Physecs.cpp:32)
     launch_aabb(w, 0, W->stream);
@@ -480,8 +497,11 @@ int psx::rt::queue_frame(psx_world* W, cudaEvent_t* ev) {
     k += launch_contacts(W->w, W->f, s);
     k += launch_joint_layout(W->w, W->f, s);
     if (ev) cudaEventRecord(ev[3], s);
-    k += launch_solver(W->w, W->f, W->block_scenes, (int)W->block_scenes_h.size(), W->grid_scenes,
-                       (int)W->grid_scenes_h.size(), W->grid_blocks, s);
+    SolverLaunch L{W->block_scenes, (int)W->block_scenes_h.size(), W->solver_smem,
+                   W->large_scenes, (int)W->large_scenes_h.size(), W->solver_smem_large,
+                   W->grid_scenes, (int)W->grid_scenes_h.size(), W->grid_blocks,
+                   W->aux_stream, W->ev_fork, W->ev_join};
+    k += launch_solver(W->w, W->f, L, s);
     if (ev) cudaEventRecord(ev[4], s);
     k += launch_aabb(W->w, 1, s);
     if (ev) cudaEventRecord(ev[5], s);
@@ -526,6 +546,9 @@ PSX_API psx_status psx_world_create(const psx_scene_desc* scenes, int32_t n_scen
     W->device = o.device;
     W->use_graph = o.use_graph != 0;
     cudaError_t e = cudaStreamCreateWithFlags(&W->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&W->aux_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&W->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&W->ev_join, cudaEventDisableTiming);
     if (e != cudaSuccess) { delete W; return fail(PSX_ERR_CUDA, cudaGetErrorString(e)); }
     psx_status s = build_world(W, scenes, n_scenes, o);
     if (s != PSX_OK) { delete W; return s; }

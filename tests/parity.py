@@ -26,19 +26,35 @@ def compare_contacts(gk, gf, ok, of, atol=1e-5):
     worst = 0.0
     cols = list(range(0, 4)) + [8 + 12 * k + j for k in range(4) for j in range(7)]
     for k in g:
-        d = np.abs(g[k][cols].astype(np.float64) - o[k][cols].astype(np.float64))
-        worst = max(worst, float(d.max()))
+        x, y = g[k][cols].astype(np.float64), o[k][cols].astype(np.float64)
+        if not np.array_equal(np.isnan(x), np.isnan(y)):
+            return float("inf")
+        ok = ~np.isnan(x)
+        if ok.any():
+            worst = max(worst, float(np.abs(x[ok] - y[ok]).max()))
     return worst
 
 
 def state_diff(a, b, sl=slice(None)):
-    return max(float(np.abs(a[k][sl].astype(np.float64) - b[k][sl].astype(np.float64)).max()) for k in ("pos", "quat", "vel", "ang_vel"))
+    out = 0.0
+    for k in ("pos", "quat", "vel", "ang_vel"):
+        d = np.abs(a[k][sl].astype(np.float64) - b[k][sl].astype(np.float64))
+        if np.isnan(d).any():
+            return float("inf")
+        out = max(out, float(d.max()))
+    return out
 
 
 def rel_state_diff(a, b, sl=slice(None)):
-    """max |a-b| / max(1, |b|) over all state components."""
+    """max |a-b| / max(1, |b|) over all state components.  A NaN counts as equal only
+    to a NaN in the same place; any other NaN makes the difference infinite."""
     worst = 0.0
     for k in ("pos", "quat", "vel", "ang_vel"):
         x, y = a[k][sl].astype(np.float64), b[k][sl].astype(np.float64)
-        worst = max(worst, float((np.abs(x - y) / np.maximum(1.0, np.abs(y))).max()))
+        nx, ny = np.isnan(x), np.isnan(y)
+        if not np.array_equal(nx, ny):
+            return float("inf")
+        ok = ~nx
+        if ok.any():
+            worst = max(worst, float((np.abs(x[ok] - y[ok]) / np.maximum(1.0, np.abs(y[ok]))).max()))
     return worst

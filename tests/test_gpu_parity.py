@@ -198,3 +198,40 @@ def test_scene_results_independent_of_batch(gpu_lib):
     for r in runs[1:]:
         for k in r:
             assert np.array_equal(r[k].view(np.uint32), runs[0][k].view(np.uint32)), k
+
+
+def _plate_with_spheres(n_side=15):
+    """A dynamic 16 x 16 m plate on the ground carrying n_side^2 spheres: the plate
+    touches more bodies than the colour limit, so its contacts overflow into the
+    serially solved last colour."""
+    s = scenes.SceneData("plate")
+    scenes._ground_box(s, (30.0, 0.5, 30.0))
+    he = (8.0, 0.25, 8.0)
+    m, com, I = scenes.mass_box(he)
+    s.add_bodies(pos=[[0.0, 0.25, 0.0]], quat=[scenes.IDENTITY_Q], flags=scenes.BODY_DYNAMIC, inv_mass=1.0 / m,
+                 com=com, inv_inertia=np.linalg.inv(I).T.ravel(), col_type=scenes.BOX, col_params=[*he, 0.0])
+    r = 0.4
+    ms, comS, IS = scenes.mass_sphere(r)
+    g = (np.arange(n_side) - (n_side - 1) / 2.0) * 1.0
+    xs, zs = np.meshgrid(g, g)
+    pos = np.stack([xs.ravel(), np.full(xs.size, 0.5 + r - 0.005), zs.ravel()], axis=1)
+    s.add_bodies(pos=pos, quat=np.tile(scenes.IDENTITY_Q, (len(pos), 1)), flags=scenes.BODY_DYNAMIC, inv_mass=1.0 / ms,
+                 com=comS, inv_inertia=np.linalg.inv(IS).T.ravel(), col_type=scenes.SPHERE, col_params=[r, 0, 0, 0])
+    return s.finalize()
+
+
+def test_contacts_beyond_the_colour_limit(gpu_lib, oracle_lib):
+    """A body with more contacts than colours: the overflow colour is solved serially in
+    contact order, and the frame still equals the oracle fed the GPU's order."""
+    s = _plate_with_spheres()
+    g = _gpu(s)
+    o = _oracle(s)
+    for f in range(4):
+        g.step(); g.synchronize()
+        ids, gf, meta = g.contacts()
+        assert int(meta[:, 0].max()) + 1 == 128 or f > 0
+        o.set_contact_order(gpu_keys(ids, meta))
+        o.step()
+        assert o.order_error() == 0
+        assert rel_state_diff(g.read_bodies(), o.state()) <= TOL
+    assert g.counts()["error"] == 0

@@ -89,10 +89,23 @@ def test_admission_limits(gpu_lib):
     from physecs_gb300.api import Server
     pool, pool_scene = _pool()
     small, big = _requests(pool, [31, 32], [30, 300])
+    import ctypes as C
+    from physecs_gb300.api import load
+    from physecs_gb300.desc import make_desc
     srv = Server([(64, 1)], mesh_pool=pool_scene)
-    assert srv.admit(big, 3) is None          # larger than the largest class
+    lib = load()
+
+    def admit_c(scene):
+        slot = C.c_int32(-1)
+        d = make_desc(scene)
+        return lib.psx_server_admit(srv.h, C.byref(d), 3, C.c_float(1 / 60), C.byref(slot))
+
+    assert admit_c(big) == 3                  # larger than the largest class: PSX_ERR_CAPACITY
+    assert b"largest slot class" in lib.psx_last_error_string()
+    assert srv.admit(big, 3) is None
     s0 = srv.admit(small, 3)
     assert s0 is not None
-    assert srv.admit(small, 3) is None        # no free slot
+    assert admit_c(small) == 3                # no free slot
+    assert srv.admit(small, 3) is None
     st = srv.stats()
     assert st["running"] == 1 and st["free"] == 0 and st["slots"] == 1
