@@ -237,13 +237,15 @@ def cpu_kind():
 
 SERVE_CLASSES = [(17, 96), (33, 96), (65, 96), (129, 96), (257, 96), (513, 96), (1025, 64), (2049, 48), (4097, 32),
                  (8193, 24)]
+# requests of at most 1000 bodies (the latency target's class)
+SERVE_CLASSES_SMALL = [(17, 48), (33, 48), (65, 48), (129, 48), (257, 32), (513, 24), (1025, 16)]
 
 
-def serving_requests(count, rank=0):
-    """Seeded serving requests (N log-uniform in [8, 8192] bodies, K uniform in [1, 120] frames)."""
+def serving_requests(count, rank=0, n_max=8192):
+    """Seeded serving requests (N log-uniform in [8, n_max] bodies, K uniform in [1, 120] frames)."""
     from physecs_gb300 import scenes
     pool = scenes._hull_pool(scenes.SplitMix64(scenes.scene_seed(5, 1 << 19)), count=8)
-    reqs = [scenes.serving_request(rank * count + i, pool=pool) for i in range(count)]
+    reqs = [scenes.serving_request(rank * count + i, pool=pool, n_max=n_max) for i in range(count)]
     ps = scenes.SceneData("pool")
     ps.convex.extend(pool)
     import numpy as np
@@ -298,20 +300,24 @@ def _serve(srv, reqs, arrivals, t_end, max_backlog=None):
                 srv.read(slot)
                 srv.release(slot)
                 del live[slot]
-    return frame_lat, req_lat, work, time.perf_counter() - t0
+    wall = time.perf_counter() - t0
+    for slot in live:          # requests still running when the window closes are dropped
+        srv.release(slot)
+    return frame_lat, req_lat, work, wall
 
 
 def run_serving(args, rank, world, local):
     import numpy as np
     from physecs_gb300.api import Server
-    reqs, pool_scene = serving_requests(384, rank)
-    srv = Server(SERVE_CLASSES, mesh_pool=pool_scene, device=local if world > 1 else 0)
+    small = args.serve_max_bodies <= 1000
+    classes = SERVE_CLASSES_SMALL if small else SERVE_CLASSES
+    reqs, pool_scene = serving_requests(384, rank, n_max=args.serve_max_bodies)
+    srv = Server(classes, mesh_pool=pool_scene, device=local if world > 1 else 0)
     # saturated throughput: a permanent backlog keeps every fitting slot busy
-    _serve(srv, reqs, None, 3.0)
-    _, _, work_sat, wall_sat = _serve(srv, reqs, None, max(5.0, args.serve_seconds / 3))
+    backlog = 2 * sum(c[1] for c in classes)   # enough waiting requests to keep every class busy
+    _serve(srv, reqs, None, 3.0, backlog)
+    _, _, work_sat, wall_sat = _serve(srv, reqs, None, max(5.0, args.serve_seconds / 3), backlog)
     sat = work_sat / wall_sat
-    for slot in list(srv.n_bodies):
-        srv.release(slot)
     mean_work = float(np.mean([s.n_dynamic * s.num_substeps * k for s, k in reqs]))
     lam = args.serve_load * sat / mean_work          # requests per second
     rng = np.random.default_rng(5 + rank)
@@ -319,12 +325,14 @@ def run_serving(args, rank, world, local):
     fl, rl, work, wall = _serve(srv, reqs, list(arrivals), args.serve_seconds)
     fl, rl = np.asarray(fl) * 1e3, np.asarray(rl) * 1e3
     line = {
-        "metric": "serving frame latency p99", "value": float(np.percentile(fl, 99)), "unit": "ms", "n_gpus": world,
+        "metric": "serving frame latency p99" + (" (N <= %d bodies)" % args.serve_max_bodies if small else ""),
+        "value": float(np.percentile(fl, 99)), "unit": "ms", "n_gpus": world,
         "steps": len(fl), "warmup": 1, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 (f64 in GJK/EPA)", "data": "synthetic (seeded SplitMix64 requests)",
         "config": {"workload": "serving: Poisson request stream at %.0f%% of saturated throughput, N log-uniform in "
-                               "[8,8192] bodies, K uniform in [1,120] frames, dt=1/60, 4x8" % (100 * args.serve_load),
-                   "slot_classes": SERVE_CLASSES, "seconds": args.serve_seconds},
+                               "[8,%d] bodies, K uniform in [1,120] frames, dt=1/60, 4x8" % (100 * args.serve_load,
+                                                                                             args.serve_max_bodies),
+                   "slot_classes": classes, "seconds": args.serve_seconds},
         "p50_ms": float(np.percentile(fl, 50)), "p99_ms": float(np.percentile(fl, 99)),
         "request_p50_ms": float(np.percentile(rl, 50)) if len(rl) else None,
         "request_p99_ms": float(np.percentile(rl, 99)) if len(rl) else None,
@@ -347,6 +355,7 @@ def main():
     ap.add_argument("--workload", default="batched", choices=["batched", "large", "chains", "pyramid", "serving"])
     ap.add_argument("--serve-seconds", type=float, default=20.0)
     ap.add_argument("--serve-load", type=float, default=0.7)
+    ap.add_argument("--serve-max-bodies", type=int, default=8192)
     ap.add_argument("--scenes", type=int, default=4096)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--plain-scenes", type=int, default=64)

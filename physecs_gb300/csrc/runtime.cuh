@@ -44,6 +44,8 @@ struct psx_world {
     int* grid_scenes = nullptr;
     int grid_blocks = 0;
     int solver_smem = 0;             // dynamic shared memory per solver block (bytes)
+    long long frames_run = 0;        // frames queued since creation
+    int frame_kernels = 0;           // kernels in one frame
     int solver_smem_large = 0;       // the same for the 512-thread blocks of large scenes
     std::vector<int> large_scenes_h; // block scenes above 1024 dynamic bodies
     int* large_scenes = nullptr;
@@ -99,6 +101,8 @@ psx_status validate(const psx_scene_desc& d);
 psx_status build_world(psx_world* W, const psx_scene_desc* scenes, int S, const psx_world_opts& o);
 // queues one frame on W's stream; ev (optional) receives 6 stage events; returns kernels queued
 int queue_frame(psx_world* W, cudaEvent_t* ev = nullptr);
+// one frame on W's stream, through W's CUDA graph when it uses one
+psx_status run_frame(psx_world* W);
 // reads the device error word; maps its bits to a status
 psx_status check_err(psx_world* W);
 // pinned host staging of at least n4 float4

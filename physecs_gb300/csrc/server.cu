@@ -160,6 +160,7 @@ PSX_API psx_status psx_server_create(const psx_server_opts* o, psx_server** out)
     wo.pairs_per_collider = o->pairs_per_collider;
     wo.manifolds_per_collider = o->manifolds_per_collider;
     wo.block_scene_max_dyn = 1 << 30;
+    wo.use_graph = 1;   // a tick is the same fixed kernel sequence every time
     wo.device = o->device;
     psx_world* W = nullptr;
     psx_status st = psx_world_create(descs.data(), n_slots, &wo, &W);
@@ -305,7 +306,7 @@ PSX_API psx_status psx_server_tick(psx_server* S, int32_t* done, int32_t cap, in
                                  W->stream));
         S->active_dirty = false;
     }
-    queue_frame(W);
+    PSX_TRY(run_frame(W));
     PSX_CUDA(cudaMemsetAsync(S->d_fresh, 0, sizeof(int) * S->h_active.size(), W->stream));
     PSX_CUDA(cudaGetLastError());
     PSX_CUDA(cudaStreamSynchronize(W->stream));

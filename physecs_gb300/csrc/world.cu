@@ -509,6 +509,29 @@ int psx::rt::queue_frame(psx_world* W, cudaEvent_t* ev) {
     return k;
 }
 
+// One frame, launched from a CUDA graph once the world uses one: the first frame runs
+// uncaptured (it sets the kernels' one-time attributes), the second is captured, and
+// every later frame replays the graph.
+psx_status psx::rt::run_frame(psx_world* W) {
+    if (!W->use_graph || W->frames_run == 0) {
+        W->frame_kernels = queue_frame(W);
+    } else {
+        if (!W->graph) {
+            cudaGraph_t g;
+            PSX_CUDA(cudaStreamBeginCapture(W->stream, cudaStreamCaptureModeThreadLocal));
+            int k = queue_frame(W);
+            W->launches -= k;   // counted when the graph runs
+            PSX_CUDA(cudaStreamEndCapture(W->stream, &g));
+            PSX_CUDA(cudaGraphInstantiate(&W->graph, g, 0));
+            cudaGraphDestroy(g);
+        }
+        PSX_CUDA(cudaGraphLaunch(W->graph, W->stream));
+        W->launches += W->frame_kernels;
+    }
+    ++W->frames_run;
+    return PSX_OK;
+}
+
 psx_status psx::rt::check_err(psx_world* W) {
     int e = 0;
     PSX_CUDA(cudaMemcpy(&e, W->w.err, sizeof(int), cudaMemcpyDeviceToHost));
@@ -584,19 +607,7 @@ PSX_API psx_status psx_world_step(psx_world* W, float dt, int32_t frames) {
         W->knobs_dirty = false;
     }
     for (int i = 0; i < frames; ++i) {
-        if (W->use_graph) {
-            if (!W->graph) {
-                cudaGraph_t g;
-                PSX_CUDA(cudaStreamBeginCapture(W->stream, cudaStreamCaptureModeThreadLocal));
-                queue_frame(W);
-                PSX_CUDA(cudaStreamEndCapture(W->stream, &g));
-                PSX_CUDA(cudaGraphInstantiate(&W->graph, g, 0));
-                cudaGraphDestroy(g);
-            }
-            PSX_CUDA(cudaGraphLaunch(W->graph, W->stream));
-        } else {
-            queue_frame(W);
-        }
+        PSX_TRY(run_frame(W));
     }
     PSX_CUDA(cudaGetLastError());
     return PSX_OK;

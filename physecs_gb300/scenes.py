@@ -571,10 +571,10 @@ def batch_scenes(count=4096, config=4, chain_prob=0.1):
     return [batch_scene(i, config=config, chain_prob=chain_prob, pool=pool) for i in range(count)]
 
 
-def serving_request(index, pool=None):
-    """Config 5 request: N log-uniform in [8, 8192] bodies, K uniform in [1, 120] frames."""
+def serving_request(index, pool=None, n_max=8192):
+    """Config 5 request: N log-uniform in [8, n_max] bodies, K uniform in [1, 120] frames."""
     rng = SplitMix64(scene_seed(5, index))
-    n = int(round(math.exp(rng.uniform(1, math.log(8), math.log(8192))[0])))
+    n = int(round(math.exp(rng.uniform(1, math.log(8), math.log(n_max))[0])))
     k = int(1 + (rng.next_u64(1)[0] % np.uint64(120)))
     s = batch_scene(index, n_bodies=n, config=5, chain_prob=0.0, pool=pool)
     return s, k

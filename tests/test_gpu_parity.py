@@ -235,3 +235,18 @@ def test_contacts_beyond_the_colour_limit(gpu_lib, oracle_lib):
         assert o.order_error() == 0
         assert rel_state_diff(g.read_bodies(), o.state()) <= TOL
     assert g.counts()["error"] == 0
+
+
+def test_graph_launched_frames_equal_eager_frames(gpu_lib):
+    """use_graph: the first frame runs eagerly, the second is captured, later ones replay
+    the graph; the states equal those of eager frames bit for bit."""
+    ss = [scenes.batch_scene(70 + i, n_bodies=n) for i, n in enumerate([30, 1200, 90])]
+    a = _gpu(ss)
+    b = _gpu(ss, use_graph=True)
+    for f in range(6):
+        a.step(); b.step()
+        a.synchronize(); b.synchronize()
+        sa, sb = a.read_bodies(), b.read_bodies()
+        for k in sa:
+            assert np.array_equal(sa[k].view(np.uint32), sb[k].view(np.uint32)), (f, k)
+    assert b.counts()["kernels"] > 0
