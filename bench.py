@@ -254,56 +254,87 @@ def serving_requests(count, rank=0, n_max=8192):
     return reqs, ps.finalize()
 
 
-def _serve(srv, reqs, arrivals, t_end, max_backlog=None):
-    """Drive the server: admit arrived requests at each tick, tick, retire.  arrivals[i]
-    is request i's arrival (seconds from start) or None for a permanent backlog.
-    Returns (frame latencies s, request latencies s, body-substeps run, wall s)."""
+def _serve(srv, reqs, arrivals, t_end, max_backlog=None, descs=None):
+    """Drive the server: while a tick runs on the GPU, admit the requests that have
+    arrived and read and release the finished ones; then wait for the tick and start
+    the next.  arrivals[i] is request i's arrival (seconds from start) or None for a
+    permanent backlog.  Returns (frame latencies s, request latencies s, body-substeps
+    run, wall s).  A frame's latency runs from the moment it could start (the
+    request's admission for its first frame, the previous frame's result for the
+    others) to its result being ready."""
     import collections
+    import numpy as np
+    n_slots = srv.stats()["slots"]
+    last = np.zeros(n_slots)              # admission time, then the previous frame's ready time
+    arrival = np.zeros(n_slots)
+    wps = np.zeros(n_slots)               # body-substeps per frame of the slot's request
+    on = np.zeros(n_slots, bool)
+    first = np.zeros(n_slots, np.int64)   # first tick that simulates the slot's request
     t0 = time.perf_counter()
     queue = collections.deque()
     nxt = 0
-    live = {}          # slot -> [request index, arrival, last frame ready]
     frame_lat, req_lat = [], []
-    work = 0
+    work = 0.0
+    ticks = 0
+    in_flight = False
+    finished = []
     while True:
         now = time.perf_counter() - t0
         if now >= t_end:
             break
+        # ---- host work, beside the tick in flight
+        for slot in finished:
+            srv.read(slot)
+            srv.release(slot)
+        finished = []
         if arrivals is None:
             while len(queue) < (max_backlog or 64):
                 queue.append((nxt % len(reqs), now)); nxt += 1
         else:
             while nxt < len(arrivals) and arrivals[nxt] <= now:
                 queue.append((nxt % len(reqs), arrivals[nxt])); nxt += 1
-        # first come, first served among the requests a free slot fits
-        waiting = collections.deque()
+        waiting = collections.deque()      # first come, first served among the requests a free slot fits
         while queue:
             i, ta = queue.popleft()
             s, k = reqs[i]
-            slot = srv.admit(s, k)
+            slot = srv.admit(s, k, desc=descs[i] if descs else None)
             if slot is None:
                 waiting.append((i, ta))
                 continue
-            live[slot] = [i, ta, ta, s.n_dynamic * s.num_substeps]
+            on[slot] = True
+            arrival[slot] = ta
+            last[slot] = time.perf_counter() - t0
+            wps[slot] = s.n_dynamic * s.num_substeps
+            first[slot] = ticks + 1
         queue = waiting
-        if not live:
+        # ---- finish the tick in flight, start the next
+        if in_flight:
+            done = srv.tick_end()
+            t_ready = time.perf_counter() - t0
+            ran = on & (first <= ticks)
+            frame_lat.append(t_ready - last[ran])
+            last[ran] = t_ready
+            work += float(wps[ran].sum())
+            for slot in done:
+                req_lat.append(t_ready - arrival[slot])
+                on[slot] = False
+                finished.append(slot)
+            in_flight = False
+        if on.any():
+            srv.tick_begin()
+            ticks += 1
+            in_flight = True
+        else:
             time.sleep(0.0005)
-            continue
-        done = set(srv.tick())
-        t_ready = time.perf_counter() - t0
-        for slot, rec in list(live.items()):
-            frame_lat.append(t_ready - rec[2])
-            rec[2] = t_ready
-            work += rec[3]
-            if slot in done:
-                req_lat.append(t_ready - rec[1])
-                srv.read(slot)
-                srv.release(slot)
-                del live[slot]
+    if in_flight:
+        srv.tick_end()
     wall = time.perf_counter() - t0
-    for slot in live:          # requests still running when the window closes are dropped
+    for slot in finished:
         srv.release(slot)
-    return frame_lat, req_lat, work, wall
+    for slot in np.nonzero(on)[0]:        # requests still running when the window closes are dropped
+        srv.release(int(slot))
+    fl = np.concatenate(frame_lat) if frame_lat else np.zeros(0)
+    return fl, req_lat, work, wall
 
 
 def run_serving(args, rank, world, local):
@@ -312,17 +343,19 @@ def run_serving(args, rank, world, local):
     small = args.serve_max_bodies <= 1000
     classes = SERVE_CLASSES_SMALL if small else SERVE_CLASSES
     reqs, pool_scene = serving_requests(384, rank, n_max=args.serve_max_bodies)
+    from physecs_gb300.desc import make_desc
+    descs = [make_desc(s) for s, _ in reqs]          # the clients' packed requests
     srv = Server(classes, mesh_pool=pool_scene, device=local if world > 1 else 0)
     # saturated throughput: a permanent backlog keeps every fitting slot busy
     backlog = 2 * sum(c[1] for c in classes)   # enough waiting requests to keep every class busy
-    _serve(srv, reqs, None, 3.0, backlog)
-    _, _, work_sat, wall_sat = _serve(srv, reqs, None, max(5.0, args.serve_seconds / 3), backlog)
+    _serve(srv, reqs, None, 3.0, backlog, descs)
+    _, _, work_sat, wall_sat = _serve(srv, reqs, None, max(5.0, args.serve_seconds / 3), backlog, descs)
     sat = work_sat / wall_sat
     mean_work = float(np.mean([s.n_dynamic * s.num_substeps * k for s, k in reqs]))
     lam = args.serve_load * sat / mean_work          # requests per second
     rng = np.random.default_rng(5 + rank)
     arrivals = np.cumsum(rng.exponential(1.0 / lam, size=int(lam * args.serve_seconds * 1.5) + 16))
-    fl, rl, work, wall = _serve(srv, reqs, list(arrivals), args.serve_seconds)
+    fl, rl, work, wall = _serve(srv, reqs, list(arrivals), args.serve_seconds, None, descs)
     fl, rl = np.asarray(fl) * 1e3, np.asarray(rl) * 1e3
     line = {
         "metric": "serving frame latency p99" + (" (N <= %d bodies)" % args.serve_max_bodies if small else ""),

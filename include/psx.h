@@ -239,23 +239,35 @@ typedef struct psx_server_opts {
     int32_t pairs_per_collider;       /* as psx_world_opts (0: default) */
     int32_t manifolds_per_collider;
     int32_t device;
+    int32_t eager;                    /* 1: launch every tick's kernels one by one instead of replaying a CUDA graph */
 } psx_server_opts;
 
 PSX_API psx_status psx_server_create(const psx_server_opts* opts, psx_server** out);
 PSX_API psx_status psx_server_destroy(psx_server* s);
 /* Place a request in the smallest free slot that holds it; it runs from the next
- * tick for `frames` frames of dt seconds.  PSX_ERR_CAPACITY: no free slot fits. */
+ * tick for `frames` frames of dt seconds.  PSX_ERR_CAPACITY: no free slot fits.
+ * Admission packs the request into pinned host memory only; its arrays reach the
+ * device when the next tick begins, so a request may be admitted while a tick runs. */
 PSX_API psx_status psx_server_admit(psx_server* s, const psx_scene_desc* request, int32_t frames, float dt,
                                     int32_t* slot);
-/* One frame of every running request, in one batched frame; waits for it.  The
- * slots whose request ran its last frame are written to done[0..min(n,cap)). */
+/* One frame of every running request, in one batched frame: tick_begin uploads the
+ * requests admitted since the last tick and launches the frame without waiting;
+ * tick_end waits for it and writes the slots whose request ran its last frame to
+ * done[0..min(n,cap)).  Between the two the caller may admit, read finished slots and
+ * release slots.  psx_server_tick = tick_begin + tick_end. */
+PSX_API psx_status psx_server_tick_begin(psx_server* s);
+PSX_API psx_status psx_server_tick_end(psx_server* s, int32_t* done, int32_t cap, int32_t* n_done);
 PSX_API psx_status psx_server_tick(psx_server* s, int32_t* done, int32_t cap, int32_t* n_done);
-/* Body state of a running or finished request (arrays as psx_world_read_bodies). */
+/* Body state of a running or finished request (arrays as psx_world_read_bodies).  A
+ * finished request is read beside a tick in flight; a running one after it. */
 PSX_API psx_status psx_server_read(psx_server* s, int32_t slot, float* pos, float* quat, float* vel, float* ang_vel);
 /* Free a slot (a running request is dropped). */
 PSX_API psx_status psx_server_release(psx_server* s, int32_t slot);
 /* out[6] = {running, finished, free slots, bodies running, body-frames so far, slots} */
 PSX_API psx_status psx_server_stats(psx_server* s, int64_t* out);
+/* The world that holds the slots (slot i is scene i), for the inspection entry points
+ * (psx_world_counts, psx_world_get_pairs, psx_world_get_contacts).  Owned by the server. */
+PSX_API psx_world* psx_server_world(psx_server* s);
 
 /* ---- single-scene spelling of the same entry points (physecs::Scene) ---- */
 typedef psx_world psx_scene;

@@ -25,7 +25,7 @@ EXPORTS = ["psx_world_create", "psx_world_destroy", "psx_world_step", "psx_world
            "psx_world_get_pairs", "psx_world_get_contacts", "psx_world_get_bounds", "psx_last_error_string",
            "psx_scene_create", "psx_scene_destroy", "psx_scene_simulate", "psx_world_read_bodies_noalloc",
            "psx_server_create", "psx_server_destroy", "psx_server_admit", "psx_server_tick", "psx_server_read",
-           "psx_server_release", "psx_server_stats"]
+           "psx_server_release", "psx_server_stats", "psx_server_tick_begin", "psx_server_tick_end", "psx_server_world"]
 
 _lib = None
 
@@ -42,7 +42,7 @@ class PsxWorldOpts(C.Structure):
 class PsxServerOpts(C.Structure):
     _fields_ = [("n_classes", C.c_int32), ("class_bodies", C.c_void_p), ("class_slots", C.c_void_p),
                 ("mesh_pool", C.c_void_p), ("pairs_per_collider", C.c_int32), ("manifolds_per_collider", C.c_int32),
-                ("device", C.c_int32)]
+                ("device", C.c_int32), ("eager", C.c_int32)]
 
 
 def load():
@@ -77,6 +77,10 @@ def load():
     lib.psx_server_destroy.argtypes = [vp]
     lib.psx_server_admit.argtypes = [vp, C.POINTER(PsxSceneDesc), C.c_int32, C.c_float, vp]
     lib.psx_server_tick.argtypes = [vp, vp, C.c_int32, vp]
+    lib.psx_server_tick_begin.argtypes = [vp]
+    lib.psx_server_world.argtypes = [vp]
+    lib.psx_server_world.restype = vp
+    lib.psx_server_tick_end.argtypes = [vp, vp, C.c_int32, vp]
     lib.psx_server_read.argtypes = [vp, C.c_int32, vp, vp, vp, vp]
     lib.psx_server_release.argtypes = [vp, C.c_int32]
     lib.psx_server_stats.argtypes = [vp, vp]
@@ -200,7 +204,7 @@ class Server:
 
     h = None
 
-    def __init__(self, classes, mesh_pool=None, device=0, pairs_per_collider=0, manifolds_per_collider=0):
+    def __init__(self, classes, mesh_pool=None, device=0, pairs_per_collider=0, manifolds_per_collider=0, eager=False):
         lib = load()
         self._cb = np.ascontiguousarray([c[0] for c in classes], np.int32)
         self._cs = np.ascontiguousarray([c[1] for c in classes], np.int32)
@@ -208,7 +212,7 @@ class Server:
         self._pool = make_desc(mesh_pool) if mesh_pool is not None else None
         opts = PsxServerOpts(len(classes), self._cb.ctypes.data, self._cs.ctypes.data,
                              C.cast(C.pointer(self._pool), C.c_void_p) if self._pool is not None else None,
-                             pairs_per_collider, manifolds_per_collider, device)
+                             pairs_per_collider, manifolds_per_collider, device, 1 if eager else 0)
         h = C.c_void_p()
         _check(lib.psx_server_create(C.byref(opts), C.byref(h)))
         self.h = h
@@ -228,14 +232,15 @@ class Server:
         except Exception:
             pass
 
-    def admit(self, scene, frames, dt=None):
-        """Returns the slot, or None when no free slot fits (PSX_ERR_CAPACITY)."""
+    def admit(self, scene, frames, dt=None, desc=None):
+        """Returns the slot, or None when no free slot fits (PSX_ERR_CAPACITY).  desc: the
+        scene's psx_scene_desc when the caller has built it already."""
         dt = scene.dt if dt is None else dt
         need = max(len(scene.arrays["pos"]), len(scene.arrays["col_type"]) - 1)
         cls = next((c for c, cap in enumerate(self._caps) if cap >= need and self._free[c] > 0), None)
         if cls is None:
             return None          # the library would answer PSX_ERR_CAPACITY; skip the call
-        d = make_desc(scene)
+        d = make_desc(scene) if desc is None else desc
         slot = C.c_int32(-1)
         st = load().psx_server_admit(self.h, C.byref(d), frames, C.c_float(dt), C.byref(slot))
         if st == 3:
@@ -248,9 +253,18 @@ class Server:
 
     def tick(self):
         """One frame of every running request; returns the slots that finished."""
+        self.tick_begin()
+        return self.tick_end()
+
+    def tick_begin(self):
+        """Upload the requests admitted since the last tick and launch a frame (no wait)."""
+        _check(load().psx_server_tick_begin(self.h))
+
+    def tick_end(self):
+        """Wait for the frame in flight; returns the slots that finished."""
         done = np.zeros(max(1, len(self.n_bodies) + 64), np.int32)
         n = C.c_int32(0)
-        _check(load().psx_server_tick(self.h, _p(done), len(done), C.byref(n)))
+        _check(load().psx_server_tick_end(self.h, _p(done), len(done), C.byref(n)))
         if n.value > len(done):
             raise PsxError("tick: more finished slots than the result buffer holds")
         return done[:n.value].tolist()

@@ -206,6 +206,18 @@ __global__ void k_karras(World w, FrameBuf f) {
     if (i == 0) f.bvh.parent[node] = -1;
 }
 
+// a disabled collider never pairs: it contributes empty bounds to its tree nodes, so a
+// subtree holding only disabled colliders is pruned at its root
+__device__ __forceinline__ void leaf_bounds(const World& w, int c, float4& mn, float4& mx) {
+    if (w.col_info[c].w & COL_ENABLE) {
+        mn = w.aabb_min[c];
+        mx = w.aabb_max[c];
+    } else {
+        mn = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.f);
+        mx = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.f);
+    }
+}
+
 __global__ void k_refit(World w, FrameBuf f) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= w.n_colliders) return;
@@ -219,9 +231,9 @@ __global__ void k_refit(World w, FrameBuf f) {
         __threadfence();
         int L = f.bvh.left[node], R = f.bvh.right[node];
         float4 lmin, lmax, rmin, rmax;
-        if (L < 0) { int c = f.order[~L]; lmin = w.aabb_min[c]; lmax = w.aabb_max[c]; }
+        if (L < 0) leaf_bounds(w, f.order[~L], lmin, lmax);
         else { lmin = __ldcg(&f.bvh.bmin[L]); lmax = __ldcg(&f.bvh.bmax[L]); }
-        if (R < 0) { int c = f.order[~R]; rmin = w.aabb_min[c]; rmax = w.aabb_max[c]; }
+        if (R < 0) leaf_bounds(w, f.order[~R], rmin, rmax);
         else { rmin = __ldcg(&f.bvh.bmin[R]); rmax = __ldcg(&f.bvh.bmax[R]); }
         f.bvh.bmin[node] = make_float4(fminf(lmin.x, rmin.x), fminf(lmin.y, rmin.y), fminf(lmin.z, rmin.z), 0.f);
         f.bvh.bmax[node] = make_float4(fmaxf(lmax.x, rmax.x), fmaxf(lmax.y, rmax.y), fmaxf(lmax.z, rmax.z), 0.f);

@@ -36,8 +36,6 @@ struct FrameBuf {
     int* n_pairs;         // device scalar
     // narrowphase
     int* pair_cat;        // 0 analytic, 1 convex mesh, 2 triangle mesh
-    int* cat_flag;        // scratch 0/1 per pair
-    int* cat_pos[3];
     int* cat_count;       // [3]
     int* cat_list;        // [3 * pair_cap]
     Manifold* man_pair;   // one slot per pair (analytic / convex categories)

@@ -33,49 +33,50 @@ __device__ __forceinline__ void store_manifold(Manifold& out, const ManifoldL& m
 }
 
 // pair category and trigger / joint filters (src/Physecs.cpp:200-209)
+// Pair category and the trigger / jointed-pair filters (src/Physecs.cpp:200-209), appended
+// to the category lists with one atomic per warp and category.  A list's order decides
+// only which thread handles which pair: every pair writes its own manifold slots.
 __global__ void k_classify(World w, FrameBuf f) {
     const int2* noncolliding = w.nc_pairs;
-    int n_nc = w.n_nc;
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    int np = *f.n_pairs;
-    if (p >= f.pair_cap) return;
-    int cat = 3;  // 3 = skipped
-    if (p < np) {
-        int2 pr = f.pairs[p];
-        int4 a = w.col_info[pr.x], b = w.col_info[pr.y];
-        bool trigger = (a.w & COL_TRIGGER) || (b.w & COL_TRIGGER);
-        bool jointed = false;
-        if (n_nc) {
-            // sorted (body_lo, body_hi) list of jointed body pairs
-            int lo = min(a.x, b.x), hi = max(a.x, b.x);
-            int L = 0, R = n_nc;
-            while (L < R) {
-                int m = (L + R) >> 1;
-                int2 v = noncolliding[m];
-                if (v.x < lo || (v.x == lo && v.y < hi)) L = m + 1; else R = m;
+    const int n_nc = w.n_nc;
+    const int np = *f.n_pairs;
+    const int lane = threadIdx.x & 31;
+    for (int base = blockIdx.x * blockDim.x; base < np; base += gridDim.x * blockDim.x) {
+        const int p = base + threadIdx.x;
+        int cat = 3;  // 3 = skipped
+        if (p < np) {
+            int2 pr = f.pairs[p];
+            int4 a = w.col_info[pr.x], b = w.col_info[pr.y];
+            bool trigger = (a.w & COL_TRIGGER) || (b.w & COL_TRIGGER);
+            bool jointed = false;
+            if (n_nc) {
+                // sorted (body_lo, body_hi) list of jointed body pairs
+                int lo = min(a.x, b.x), hi = max(a.x, b.x);
+                int L = 0, R = n_nc;
+                while (L < R) {
+                    int m = (L + R) >> 1;
+                    int2 v = noncolliding[m];
+                    if (v.x < lo || (v.x == lo && v.y < hi)) L = m + 1; else R = m;
+                }
+                jointed = L < n_nc && noncolliding[L].x == lo && noncolliding[L].y == hi;
             }
-            jointed = L < n_nc && noncolliding[L].x == lo && noncolliding[L].y == hi;
+            if (!trigger && !jointed) {
+                if (a.y == G_TRIMESH || b.y == G_TRIMESH) cat = 2;
+                else if (a.y == G_CONVEX || b.y == G_CONVEX) cat = 1;
+                else cat = 0;
+            }
+            f.pair_cat[p] = cat;
+            f.pair_nman[p] = 0;
         }
-        if (!trigger && !jointed) {
-            if (a.y == G_TRIMESH || b.y == G_TRIMESH) cat = 2;
-            else if (a.y == G_CONVEX || b.y == G_CONVEX) cat = 1;
-            else cat = 0;
+        for (int c = 0; c < 3; ++c) {
+            unsigned m = __ballot_sync(0xffffffffu, cat == c);
+            if (!m) continue;
+            int first = 0;
+            if (lane == __ffs(m) - 1) first = atomicAdd(&f.cat_count[c], __popc(m));
+            first = __shfl_sync(0xffffffffu, first, __ffs(m) - 1);
+            if (cat == c) f.cat_list[c * f.pair_cap + first + __popc(m & ((1u << lane) - 1u))] = p;
         }
     }
-    f.pair_cat[p] = cat;
-    f.pair_nman[p] = 0;
-}
-
-__global__ void k_cat_flags(FrameBuf f, int cat) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= f.pair_cap) return;
-    f.cat_flag[p] = (p < *f.n_pairs && f.pair_cat[p] == cat) ? 1 : 0;
-}
-
-__global__ void k_cat_scatter(FrameBuf f, int cat) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= f.pair_cap || p >= *f.n_pairs) return;
-    if (f.pair_cat[p] == cat) f.cat_list[cat * f.pair_cap + f.cat_pos[cat][p]] = p;
 }
 
 // analytic pairs: sphere / capsule / box
@@ -203,13 +204,8 @@ __global__ void __launch_bounds__(64) k_narrow_tri(World w, FrameBuf f) {
 }
 
 int launch_narrowphase(const World& w, FrameBuf& f, cudaStream_t s) {
-    int nb = (f.pair_cap + 255) / 256;
-    k_classify<<<nb, 256, 0, s>>>(w, f);
-    for (int c = 0; c < 3; ++c) {
-        k_cat_flags<<<nb, 256, 0, s>>>(f, c);
-        scan_exclusive(f.cat_flag, f.cat_pos[c], f.pair_cap, f.cat_count + c, f.scan_scratch, s);
-        k_cat_scatter<<<nb, 256, 0, s>>>(f, c);
-    }
+    cudaMemsetAsync(f.cat_count, 0, 3 * sizeof(int), s);
+    k_classify<<<1216, 256, 0, s>>>(w, f);
     k_narrow_analytic<<<1216, 128, 0, s>>>(w, f);
     static bool carveout_set = false;
     if (!carveout_set) {
@@ -221,7 +217,7 @@ int launch_narrowphase(const World& w, FrameBuf& f, cudaStream_t s) {
     k_convex_contacts<<<1216, 128, 0, s>>>(w, f);
     k_narrow_tri<<<1216, 64, 0, s>>>(w, f);
     scan_exclusive_dev(f.pair_nman, f.pair_moff, f.n_pairs, f.pair_cap, f.n_man, f.scan_scratch, s);
-    return 1 + 3 * 5 + 4 + 3;
+    return 2 + 4 + 3;
 }
 
 }  // namespace psx

@@ -25,6 +25,7 @@ using namespace psx::rt;
 namespace {
 
 struct Slot {
+    long long first_tick = 0;                     // the first tick that simulates the request
     int cls = 0, scene = 0;
     int body0 = 0, col0 = 0, dyn0 = 0, cap = 0;   // world ranges: cap + 1 bodies, colliders and dynamic entries
     int state = 0;                                // 0 free, 1 running, 2 finished
@@ -90,6 +91,23 @@ struct TemplateScene {
 
 }  // namespace
 
+// Host staging of admitted requests: their arrays are packed into pinned memory at
+// admission and copied to the device at the start of the next tick.  Two stages
+// alternate so that packing never waits for the copies of the tick in flight.
+struct Upload {
+    void* dst;
+    size_t src;   // offset in the stage
+    size_t bytes;
+};
+struct Stage {
+    char* pin = nullptr;
+    size_t cap = 0, used = 0;
+    std::vector<Upload> ups;
+    std::vector<int2> aabb;          // collider ranges that need creation bounds
+    cudaEvent_t copied = nullptr;    // recorded after the stage's copies
+    bool pending = false;            // copies issued, completion not yet observed
+};
+
 struct psx_server {
     psx_world* W = nullptr;
     std::vector<Slot> slots;
@@ -101,11 +119,33 @@ struct psx_server {
     std::vector<int> h_active;
     bool active_dirty = true;
     long long body_frames = 0;                  // simulated-body frames run so far
-    // admission staging
+    // admission packing (host) and staging (pinned)
     std::vector<float4> pos, quat, vel, ang, com, invI, cpos, cquat, cpar, cmat;
     std::vector<int4> info, cinfo;
     std::vector<int> dynb;
+    Stage stage[2];
+    int cur = 0;
+    // tick state
+    long long ticks_begun = 0;
+    bool in_flight = false;
+    cudaEvent_t tick_done = nullptr;
+    int* pin_active = nullptr;       // pinned mirror of h_active for the flag copy
+    int* pin_err = nullptr;          // device error word of the last tick
+    // reads of finished requests run on their own stream, beside the next tick
+    cudaStream_t read_stream = nullptr;
+    float4* read_pin = nullptr;
+    size_t read_cap = 0;
     ~psx_server() {
+        if (W) cudaStreamSynchronize(W->stream);
+        if (read_stream) { cudaStreamSynchronize(read_stream); cudaStreamDestroy(read_stream); }
+        for (Stage& st : stage) {
+            if (st.pin) cudaFreeHost(st.pin);
+            if (st.copied) cudaEventDestroy(st.copied);
+        }
+        if (tick_done) cudaEventDestroy(tick_done);
+        if (pin_active) cudaFreeHost(pin_active);
+        if (pin_err) cudaFreeHost(pin_err);
+        if (read_pin) cudaFreeHost(read_pin);
         if (d_active) cudaFree(d_active);
         if (d_fresh) cudaFree(d_fresh);
         delete W;
@@ -160,7 +200,7 @@ PSX_API psx_status psx_server_create(const psx_server_opts* o, psx_server** out)
     wo.pairs_per_collider = o->pairs_per_collider;
     wo.manifolds_per_collider = o->manifolds_per_collider;
     wo.block_scene_max_dyn = 1 << 30;
-    wo.use_graph = 1;   // a tick is the same fixed kernel sequence every time
+    wo.use_graph = o->eager ? 0 : 1;   // a tick is the same fixed kernel sequence every time
     wo.device = o->device;
     psx_world* W = nullptr;
     psx_status st = psx_world_create(descs.data(), n_slots, &wo, &W);
@@ -176,6 +216,16 @@ PSX_API psx_status psx_server_create(const psx_server_opts* o, psx_server** out)
     S->h_active.assign(n_slots, 0);
     W->w.scene_active = S->d_active;
     W->w.scene_fresh = S->d_fresh;
+    if (cudaMallocHost(&S->pin_active, sizeof(int) * n_slots) != cudaSuccess ||
+        cudaMallocHost(&S->pin_err, sizeof(int)) != cudaSuccess ||
+        cudaEventCreateWithFlags(&S->tick_done, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&S->stage[0].copied, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&S->stage[1].copied, cudaEventDisableTiming) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&S->read_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete S;
+        return fail(PSX_ERR_OUT_OF_MEMORY, "server host staging");
+    }
+    *S->pin_err = 0;
     PSX_CUDA(cudaDeviceSynchronize());
     *out = S;
     return PSX_OK;
@@ -184,7 +234,6 @@ PSX_API psx_status psx_server_create(const psx_server_opts* o, psx_server** out)
 PSX_API psx_status psx_server_destroy(psx_server* S) {
     if (!S) return fail(PSX_ERR_INVALID_ARG, "null server");
     cudaSetDevice(S->W->device);
-    cudaStreamSynchronize(S->W->stream);
     delete S;
     return PSX_OK;
 }
@@ -262,31 +311,48 @@ PSX_API psx_status psx_server_admit(psx_server* S, const psx_scene_desc* d, int3
     S->info[cap] = make_int4(-1, PSX_BODY_DYNAMIC | PSX_BODY_KINEMATIC, sl.dyn0 + nd, sl.scene);
     S->dynb[nd] = inert;   // the inert body's own dynamic entry (and every unused one) points at it
     World& w = S->W->w;
-    cudaStream_t st = S->W->stream;
-    auto up = [&](auto* dst, const auto& v, int off) {
-        return cudaMemcpyAsync(dst + off, v.data(), v.size() * sizeof(v[0]), cudaMemcpyHostToDevice, st);
+    // stage the slot's arrays; they reach the device at the start of the next tick
+    Stage& stg = S->stage[S->cur];
+    if (stg.pending) {
+        PSX_CUDA(cudaEventSynchronize(stg.copied));
+        stg.pending = false;
+        stg.used = 0;
+    }
+    const size_t stage_need = stg.used + (size_t)nb * (16 * sizeof(float4)) + 4 * sizeof(float4);
+    if (stage_need > stg.cap) {
+        size_t new_cap = std::max(stage_need, 2 * stg.cap);
+        char* np = nullptr;
+        PSX_CUDA(cudaMallocHost(&np, new_cap));
+        if (stg.used) std::memcpy(np, stg.pin, stg.used);
+        if (stg.pin) cudaFreeHost(stg.pin);
+        stg.pin = np;
+        stg.cap = new_cap;
+    }
+    auto up = [&](auto* dst, const auto* src, size_t count, int off) {
+        size_t bytes = count * sizeof(src[0]);
+        std::memcpy(stg.pin + stg.used, src, bytes);
+        stg.ups.push_back(Upload{(void*)(dst + off), stg.used, bytes});
+        stg.used += (bytes + 15) / 16 * 16;
     };
-    PSX_CUDA(up(w.pos, S->pos, sl.body0));
-    PSX_CUDA(up(w.quat, S->quat, sl.body0));
-    PSX_CUDA(up(w.info, S->info, sl.body0));
-    PSX_CUDA(up(w.dyn_body, S->dynb, sl.dyn0));
-    PSX_CUDA(up(w.vel, S->vel, sl.dyn0));
-    PSX_CUDA(up(w.ang, S->ang, sl.dyn0));
-    PSX_CUDA(up(w.com, S->com, sl.dyn0));
-    PSX_CUDA(up(w.invI, S->invI, 3 * sl.dyn0));
-    PSX_CUDA(up(w.col_info, S->cinfo, sl.col0));
-    PSX_CUDA(up(w.col_pos, S->cpos, sl.col0));
-    PSX_CUDA(up(w.col_quat, S->cquat, sl.col0));
-    PSX_CUDA(up(w.col_params, S->cpar, sl.col0));
-    PSX_CUDA(up(w.col_mat, S->cmat, sl.col0));
+    up(w.pos, S->pos.data(), S->pos.size(), sl.body0);
+    up(w.quat, S->quat.data(), S->quat.size(), sl.body0);
+    up(w.info, S->info.data(), S->info.size(), sl.body0);
+    up(w.dyn_body, S->dynb.data(), S->dynb.size(), sl.dyn0);
+    up(w.vel, S->vel.data(), S->vel.size(), sl.dyn0);
+    up(w.ang, S->ang.data(), S->ang.size(), sl.dyn0);
+    up(w.com, S->com.data(), S->com.size(), sl.dyn0);
+    up(w.invI, S->invI.data(), S->invI.size(), 3 * sl.dyn0);
+    up(w.col_info, S->cinfo.data(), S->cinfo.size(), sl.col0);
+    up(w.col_pos, S->cpos.data(), S->cpos.size(), sl.col0);
+    up(w.col_quat, S->cquat.data(), S->cquat.size(), sl.col0);
+    up(w.col_params, S->cpar.data(), S->cpar.size(), sl.col0);
+    up(w.col_mat, S->cmat.data(), S->cmat.size(), sl.col0);
     S->W->h_knobs[sl.scene] = f4((float)d->num_substeps, (float)d->num_iterations, d->gravity, dt);
-    PSX_CUDA(cudaMemcpyAsync(w.knobs + sl.scene, &S->W->h_knobs[sl.scene], sizeof(float4), cudaMemcpyHostToDevice, st));
-    static const int one = 1;
-    PSX_CUDA(cudaMemcpyAsync(S->d_fresh + sl.scene, &one, sizeof(int), cudaMemcpyHostToDevice, st));
-    // creation bounds carry no margin (src/Physecs.cpp:25-37)
-    launch_aabb_range(w, sl.col0, sl.col0 + nb, 0, st);
-    PSX_CUDA(cudaGetLastError());
-    PSX_CUDA(cudaStreamSynchronize(st));   // the staging vectors are reused by the next admission
+    up(w.knobs, &S->W->h_knobs[sl.scene], 1, sl.scene);
+    const int one = 1;   // first frame: no cached contacts from the slot's previous request
+    up(S->d_fresh, &one, 1, sl.scene);
+    stg.aabb.push_back(make_int2(sl.col0, sl.col0 + nb));
+    sl.first_tick = S->ticks_begun + 1;
     sl.state = 1;
     sl.frames_left = frames;
     sl.n_bodies = d->n_bodies;
@@ -297,24 +363,54 @@ PSX_API psx_status psx_server_admit(psx_server* S, const psx_scene_desc* d, int3
     return PSX_OK;
 }
 
-PSX_API psx_status psx_server_tick(psx_server* S, int32_t* done, int32_t cap, int32_t* n_done) {
+PSX_API psx_status psx_server_tick_begin(psx_server* S) {
     if (!S) return fail(PSX_ERR_INVALID_ARG, "null server");
+    if (S->in_flight) return fail(PSX_ERR_INVALID_ARG, "psx_server_tick_begin: a tick is in flight");
     psx_world* W = S->W;
     PSX_CUDA(cudaSetDevice(W->device));
+    cudaStream_t st = W->stream;
+    Stage& stg = S->stage[S->cur];
+    if (!stg.ups.empty()) {
+        for (const Upload& u : stg.ups)
+            PSX_CUDA(cudaMemcpyAsync(u.dst, stg.pin + u.src, u.bytes, cudaMemcpyHostToDevice, st));
+        // creation bounds carry no margin (src/Physecs.cpp:25-37)
+        for (int2 r : stg.aabb) launch_aabb_range(W->w, r.x, r.y, 0, st);
+        PSX_CUDA(cudaEventRecord(stg.copied, st));
+        stg.pending = true;   // the pinned bytes stay untouched until the copies are seen complete
+        stg.ups.clear();
+        stg.aabb.clear();
+        S->cur ^= 1;
+    }
     if (S->active_dirty) {
-        PSX_CUDA(cudaMemcpyAsync(S->d_active, S->h_active.data(), sizeof(int) * S->h_active.size(), cudaMemcpyHostToDevice,
-                                 W->stream));
+        std::memcpy(S->pin_active, S->h_active.data(), sizeof(int) * S->h_active.size());
+        PSX_CUDA(cudaMemcpyAsync(S->d_active, S->pin_active, sizeof(int) * S->h_active.size(), cudaMemcpyHostToDevice, st));
         S->active_dirty = false;
     }
+    ++S->ticks_begun;
     PSX_TRY(run_frame(W));
-    PSX_CUDA(cudaMemsetAsync(S->d_fresh, 0, sizeof(int) * S->h_active.size(), W->stream));
+    PSX_CUDA(cudaMemsetAsync(S->d_fresh, 0, sizeof(int) * S->h_active.size(), st));
+    PSX_CUDA(cudaMemcpyAsync(S->pin_err, W->w.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    PSX_CUDA(cudaEventRecord(S->tick_done, st));
     PSX_CUDA(cudaGetLastError());
-    PSX_CUDA(cudaStreamSynchronize(W->stream));
-    PSX_TRY(check_err(W));
+    S->in_flight = true;
+    return PSX_OK;
+}
+
+PSX_API psx_status psx_server_tick_end(psx_server* S, int32_t* done, int32_t cap, int32_t* n_done) {
+    if (!S) return fail(PSX_ERR_INVALID_ARG, "null server");
+    if (!S->in_flight) return fail(PSX_ERR_INVALID_ARG, "psx_server_tick_end: no tick in flight");
+    PSX_CUDA(cudaSetDevice(S->W->device));
+    PSX_CUDA(cudaEventSynchronize(S->tick_done));
+    S->in_flight = false;
+    if (int e = *S->pin_err) {
+        char buf[160];
+        std::snprintf(buf, sizeof buf, "device error bits 0x%x", e);
+        return fail((e & ERR_BARRIER_TIMEOUT) ? PSX_ERR_TIMEOUT : PSX_ERR_CAPACITY, buf);
+    }
     int nd = 0;
     for (size_t i = 0; i < S->slots.size(); ++i) {
         Slot& sl = S->slots[i];
-        if (sl.state != 1) continue;
+        if (sl.state != 1 || sl.first_tick > S->ticks_begun) continue;
         S->body_frames += sl.n_bodies;
         if (--sl.frames_left == 0) {
             sl.state = 2;
@@ -328,21 +424,37 @@ PSX_API psx_status psx_server_tick(psx_server* S, int32_t* done, int32_t cap, in
     return PSX_OK;
 }
 
+PSX_API psx_status psx_server_tick(psx_server* S, int32_t* done, int32_t cap, int32_t* n_done) {
+    PSX_TRY(psx_server_tick_begin(S));
+    return psx_server_tick_end(S, done, cap, n_done);
+}
+
 PSX_API psx_status psx_server_read(psx_server* S, int32_t slot, float* pos, float* quat, float* vel, float* ang_vel) {
     if (!S || slot < 0 || slot >= (int)S->slots.size()) return fail(PSX_ERR_INVALID_ARG, "psx_server_read: slot");
     Slot& sl = S->slots[slot];
     if (sl.state == 0) return fail(PSX_ERR_INVALID_ARG, "psx_server_read: slot is free");
     psx_world* W = S->W;
     PSX_CUDA(cudaSetDevice(W->device));
+    // a finished request is not simulated any more and can be read beside a tick in
+    // flight; a running one is read after that tick
+    if (sl.state == 1 && S->in_flight) PSX_CUDA(cudaEventSynchronize(S->tick_done));
     int nb = sl.n_bodies, nd = sl.cap + 1;
-    PSX_TRY(ensure_pinned(W, 2 * (size_t)nb + 2 * (size_t)nd));
-    float4 *hp = W->pin, *hq = hp + nb, *hv = hq + nb, *ha = hv + nd;
+    size_t n4 = 2 * (size_t)nb + 2 * (size_t)nd;
+    if (S->read_cap < n4) {
+        if (S->read_pin) cudaFreeHost(S->read_pin);
+        S->read_pin = nullptr;
+        S->read_cap = 0;
+        PSX_CUDA(cudaMallocHost(&S->read_pin, n4 * sizeof(float4)));
+        S->read_cap = n4;
+    }
+    float4 *hp = S->read_pin, *hq = hp + nb, *hv = hq + nb, *ha = hv + nd;
     const World& w = W->w;
-    PSX_CUDA(cudaMemcpyAsync(hp, w.pos + sl.body0, nb * sizeof(float4), cudaMemcpyDeviceToHost, W->stream));
-    PSX_CUDA(cudaMemcpyAsync(hq, w.quat + sl.body0, nb * sizeof(float4), cudaMemcpyDeviceToHost, W->stream));
-    PSX_CUDA(cudaMemcpyAsync(hv, w.vel + sl.dyn0, nd * sizeof(float4), cudaMemcpyDeviceToHost, W->stream));
-    PSX_CUDA(cudaMemcpyAsync(ha, w.ang + sl.dyn0, nd * sizeof(float4), cudaMemcpyDeviceToHost, W->stream));
-    PSX_CUDA(cudaStreamSynchronize(W->stream));
+    cudaStream_t rs = S->read_stream;
+    PSX_CUDA(cudaMemcpyAsync(hp, w.pos + sl.body0, nb * sizeof(float4), cudaMemcpyDeviceToHost, rs));
+    PSX_CUDA(cudaMemcpyAsync(hq, w.quat + sl.body0, nb * sizeof(float4), cudaMemcpyDeviceToHost, rs));
+    PSX_CUDA(cudaMemcpyAsync(hv, w.vel + sl.dyn0, nd * sizeof(float4), cudaMemcpyDeviceToHost, rs));
+    PSX_CUDA(cudaMemcpyAsync(ha, w.ang + sl.dyn0, nd * sizeof(float4), cudaMemcpyDeviceToHost, rs));
+    PSX_CUDA(cudaStreamSynchronize(rs));
     for (int b = 0; b < nb; ++b) {
         if (pos) { pos[3 * b] = hp[b].x; pos[3 * b + 1] = hp[b].y; pos[3 * b + 2] = hp[b].z; }
         if (quat) { quat[4 * b] = hq[b].x; quat[4 * b + 1] = hq[b].y; quat[4 * b + 2] = hq[b].z; quat[4 * b + 3] = hq[b].w; }
@@ -363,6 +475,8 @@ PSX_API psx_status psx_server_release(psx_server* S, int32_t slot) {
     S->free_slots[sl.cls].push_back(slot);
     return PSX_OK;
 }
+
+PSX_API psx_world* psx_server_world(psx_server* S) { return S ? S->W : nullptr; }
 
 PSX_API psx_status psx_server_stats(psx_server* S, int64_t* out) {
     if (!S || !out) return fail(PSX_ERR_INVALID_ARG, "psx_server_stats");

@@ -583,19 +583,22 @@ __device__ void contact_presolve(const World& w, SHdr& H, SPt* P, float h) {
     }
 }
 
-// ContactConstraints::solve (src/ContactConstraints.cpp:33-124)
+// ContactConstraints::solve (src/ContactConstraints.cpp:33-124).  No other thread touches
+// the contact's bodies within its colour, so their velocities stay in registers from the
+// first point to the last; every value equals a reload after each point.
 __device__ void contact_solve(const SHdr& H, SPt* P, bool useBias, const VelRef& vr) {
     const V3 n = ld3(H.n);
     const float friction = H.n.w;
     const float im0 = H.m.x, im1 = H.m.y;
     const int b0 = H.i.x, b1 = H.i.y, np = H.i.z & 0xff;
     const bool soft = (H.i.z >> 8) != 0;
+    V3 v0 = {0, 0, 0}, w0 = {0, 0, 0}, v1 = {0, 0, 0}, w1 = {0, 0, 0};
+    if (b0 >= 0) { v0 = vr.lv(b0); w0 = vr.lw(b0); }
+    if (b1 >= 0) { v1 = vr.lv(b1); w1 = vr.lw(b1); }
+    bool touched = false;
     for (int i = 0; i < np; ++i) {
         SPt& p = P[i];
         if (!(__float_as_int(p.g.w) & 1)) continue;
-        V3 v0 = {0, 0, 0}, w0 = {0, 0, 0}, v1 = {0, 0, 0}, w1 = {0, 0, 0};
-        if (b0 >= 0) { v0 = vr.lv(b0); w0 = vr.lw(b0); }
-        if (b1 >= 0) { v1 = vr.lv(b1); w1 = vr.lw(b1); }
         V3 r0xn = ld3(p.a), r1xn = ld3(p.b);
         float rv = dot(-n, v0) + dot(-r0xn, w0) + dot(n, v1) + dot(r1xn, w1);
         float lambda;
@@ -607,13 +610,14 @@ __device__ void contact_solve(const SHdr& H, SPt* P, bool useBias, const VelRef&
         p.a.w = tot;
         lambda = tot - prev;
         if (b0 >= 0) {
-            vr.sv(b0, v0 + lambda * im0 * n);
-            vr.sw(b0, w0 + lambda * ld3(p.c));
+            v0 = v0 + lambda * im0 * n;
+            w0 = w0 + lambda * ld3(p.c);
         }
         if (b1 >= 0) {
-            vr.sv(b1, v1 - lambda * im1 * n);
-            vr.sw(b1, w1 - lambda * ld3(p.d));
+            v1 = v1 - lambda * im1 * n;
+            w1 = w1 - lambda * ld3(p.d);
         }
+        touched = true;
     }
     for (int i = 0; i < np; ++i) {
         SPt& p = P[i];
@@ -627,13 +631,18 @@ __device__ void contact_solve(const SHdr& H, SPt* P, bool useBias, const VelRef&
         p.e.w = tot;
         lambda = tot - prev;
         if (b0 >= 0) {
-            vr.sv(b0, vr.lv(b0) + lambda * im0 * t);
-            vr.sw(b0, vr.lw(b0) + lambda * ld3(p.f));
+            v0 = v0 + lambda * im0 * t;
+            w0 = w0 + lambda * ld3(p.f);
         }
         if (b1 >= 0) {
-            vr.sv(b1, vr.lv(b1) - lambda * im1 * t);
-            vr.sw(b1, vr.lw(b1) - lambda * ld3(p.g));
+            v1 = v1 - lambda * im1 * t;
+            w1 = w1 - lambda * ld3(p.g);
         }
+        touched = true;
+    }
+    if (touched) {
+        if (b0 >= 0) { vr.sv(b0, v0); vr.sw(b0, w0); }
+        if (b1 >= 0) { vr.sv(b1, v1); vr.sw(b1, w1); }
     }
 }
 
@@ -935,13 +944,13 @@ __device__ void solve_scene(const World& w, FrameBuf& f, int s, const S& sy, flo
 
 // one scene per block; NT = 256 for scenes up to 1024 dynamic bodies, 512 above
 template <int NT>
-__global__ void __launch_bounds__(NT) k_solve_block(World w, FrameBuf f, const int* scenes, int smem_f4) {
+__global__ void __launch_bounds__(NT, 512 / NT) k_solve_block(World w, FrameBuf f, const int* scenes, int smem_f4) {
     extern __shared__ float4 smem[];
     BlockSync sy;
     solve_scene(w, f, scenes[blockIdx.x], sy, smem, smem_f4);
 }
 
-__global__ void __launch_bounds__(256) k_solve_grid(World w, FrameBuf f, const int* scenes, int n) {
+__global__ void __launch_bounds__(256, 2) k_solve_grid(World w, FrameBuf f, const int* scenes, int n) {
     GridSync sy{GridBarrier{f.bar, f.bar + 1, w.err}, (int*)(f.bar + 2)};
     for (int i = 0; i < n; ++i) {
         solve_scene(w, f, scenes[i], sy, nullptr, 0);

@@ -422,8 +422,6 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
     PSX_TRY(W->alloc(f.pairs, f.pair_cap));
     PSX_TRY(W->alloc(f.n_pairs, 1));
     PSX_TRY(W->alloc(f.pair_cat, f.pair_cap));
-    PSX_TRY(W->alloc(f.cat_flag, f.pair_cap));
-    for (int c = 0; c < 3; ++c) PSX_TRY(W->alloc(f.cat_pos[c], f.pair_cap));
     PSX_TRY(W->alloc(f.cat_count, 3));
     PSX_TRY(W->alloc(f.cat_list, 3 * (size_t)f.pair_cap));
     PSX_TRY(W->alloc(f.man_pair, f.pair_cap));
@@ -465,13 +463,14 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
     PSX_TRY(W->upload(W->grid_scenes, W->grid_scenes_h));
     W->grid_blocks = W->grid_scenes_h.empty() ? 0 : solver_grid_blocks();
     // shared memory per solver block: the most a block may have when there are at most as
-    // many block scenes as SMs, else a size that keeps three blocks resident per SM
+    // many block scenes as SMs, else a size that keeps two blocks resident per SM (the
+    // register budget of the 256-thread solver allows two)
     {
         int dev = 0, sms = 0, optin = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        int want = (int)W->block_scenes_h.size() <= sms ? optin - 5120 : 64 * 1024;
+        int want = (int)W->block_scenes_h.size() <= sms ? optin - 5120 : 100 * 1024;   // two blocks per SM
         W->solver_smem = std::max(0, std::min(want, optin - 5120)) / 16 * 16;
         W->solver_smem_large = std::max(0, optin - 5120) / 16 * 16;
     }

@@ -109,3 +109,38 @@ def test_admission_limits(gpu_lib):
     assert srv.admit(small, 3) is None
     st = srv.stats()
     assert st["running"] == 1 and st["free"] == 0 and st["slots"] == 1
+
+
+def test_pipelined_ticks_admit_while_a_frame_runs(gpu_lib):
+    """Admissions, reads and releases between tick_begin and tick_end: requests admitted
+    while a frame is in flight start with the next frame, and every result still equals
+    the scene simulated alone."""
+    from physecs_gb300.api import Server
+    pool, pool_scene = _pool()
+    reqs = _requests(pool, [41, 42, 43, 44], [35, 150, 300, 12])
+    frames = [6, 9, 4, 11]
+    srv = Server(CLASSES, mesh_pool=pool_scene)
+    live, results, pending = {}, {}, list(range(len(reqs)))
+    slot = srv.admit(reqs[0], frames[0])
+    live[slot] = 0
+    pending.pop(0)
+    srv.tick_begin()
+    finished = []
+    for t in range(40):
+        for sl in finished:                  # the finished requests are read beside the frame in flight
+            results[live.pop(sl)] = srv.read(sl)
+            srv.release(sl)
+        finished = []
+        if pending and t % 2 == 0:           # admitted while a frame runs
+            i = pending.pop(0)
+            live[srv.admit(reqs[i], frames[i])] = i
+        finished = srv.tick_end()
+        if not live and not pending:
+            break
+        srv.tick_begin()
+    for sl in finished:
+        results[live.pop(sl)] = srv.read(sl)
+        srv.release(sl)
+    assert not live
+    for i, r in enumerate(reqs):
+        _same(results[i], _alone(r, frames[i]))
