@@ -104,13 +104,16 @@ __device__ inline V3 support(const Support& s, V3 dir) {
     }
 }
 
-struct GjkVertex { D3 pos, sp0, sp1; };
+// The simplex / polytope vertex (GJK.h): the f64 Minkowski point and the two f32 support
+// points it came from (the reference widens them to f64 when it stores them; they are
+// widened here where they are used, with identical values).
+struct GjkVertex { D3 pos; V3 sp0, sp1; };
 struct GjkSimplex { GjkVertex v[4]; };
 
 __device__ inline GjkVertex mink(const Support& s0, const Support& s1, V3 dir) {
     V3 a = support(s0, dir);
     V3 b = support(s1, -dir);
-    return {d3(a - b), d3(a), d3(b)};
+    return {d3(a - b), a, b};
 }
 __device__ inline float sqrDistPointToLine(V3 p, V3 a, V3 b) {
     V3 r = p - a, d = b - a;
@@ -180,7 +183,7 @@ __device__ inline bool gjkT(MK& mk, V3 startDir, GjkSimplex& s) {
     if (!checkDirection(mk, dir, s.v[3])) return false;
     int fi;
     for (int i = 0; i < 100; ++i) {
-        if (containsOrigin(s, dir, fi)) return true;
+        if (mk.containsOrigin(s, dir, fi)) return true;
         if (!checkDirection(mk, dir, s.v[fi])) return false;
         GjkVertex t = s.v[fi];
         s.v[fi] = s.v[3];
@@ -193,6 +196,7 @@ struct PairMink {
     const Support& s0;
     const Support& s1;
     __device__ GjkVertex operator()(V3 dir) const { return mink(s0, s1, dir); }
+    __device__ bool containsOrigin(GjkSimplex& s, D3& dir, int& fi) const { return psx::containsOrigin(s, dir, fi); }
 };
 
 __device__ inline bool gjk(const Support& s0, const Support& s1, V3 startDir, GjkSimplex& s) {
@@ -294,8 +298,8 @@ __device__ inline V3 epa(const Support& s0, const Support& s1, GjkSimplex& s, V3
         if (d00) { vv = d20 / d00; u = 1.0f - vv; }
         else { vv = 0; u = 1.0; }
     }
-    cp0 = f3(u * a.sp0 + vv * b.sp0 + ww * c.sp0);
-    cp1 = f3(u * a.sp1 + vv * b.sp1 + ww * c.sp1);
+    cp0 = f3(u * d3(a.sp0) + vv * d3(b.sp0) + ww * d3(c.sp0));
+    cp1 = f3(u * d3(a.sp1) + vv * d3(b.sp1) + ww * d3(c.sp1));
     return f3(normal);
 }
 

@@ -18,9 +18,9 @@
 // fixes the order of the faces and so every later tie-break.
 //
 // Every support point of the polytope is a float (held as float in shared
-// memory, exactly); the Minkowski vertices and face normals are held as doubles
-// so that the face loops convert nothing.  The whole polytope of one pair takes
-// about 11 KB of shared memory.
+// memory, exactly); the Minkowski vertices, face normals and face distances are
+// held as doubles so that the face loops convert and recompute nothing.  The whole
+// polytope of one pair takes about 12.5 KB of shared memory.
 #pragma once
 #include <math_constants.h>
 #include "narrow_convex.cuh"
@@ -31,6 +31,7 @@ constexpr int kFaceSlots = (kEpaFaces + 31) / 32;   // faces per lane
 
 struct WarpPoly {
     double nx[kEpaFaces], ny[kEpaFaces], nz[kEpaFaces];
+    double fd[kEpaFaces];                                   // face distance dot(v[i0], n), fixed at creation
     double px[kEpaVerts], py[kEpaVerts], pz[kEpaVerts];     // Minkowski vertex
     float ax[kEpaVerts], ay[kEpaVerts], az[kEpaVerts];      // support point on shape 0
     float bx[kEpaVerts], by[kEpaVerts], bz[kEpaVerts];      // support point on shape 1
@@ -44,8 +45,8 @@ __device__ __forceinline__ D3 wp_pos(const WarpPoly& P, int i) { return {P.px[i]
 __device__ __forceinline__ D3 wp_n(const WarpPoly& P, int f) { return {P.nx[f], P.ny[f], P.nz[f]}; }
 __device__ __forceinline__ void wp_set_vertex(WarpPoly& P, int i, const GjkVertex& v) {
     P.px[i] = v.pos.x; P.py[i] = v.pos.y; P.pz[i] = v.pos.z;
-    P.ax[i] = (float)v.sp0.x; P.ay[i] = (float)v.sp0.y; P.az[i] = (float)v.sp0.z;
-    P.bx[i] = (float)v.sp1.x; P.by[i] = (float)v.sp1.y; P.bz[i] = (float)v.sp1.z;
+    P.ax[i] = v.sp0.x; P.ay[i] = v.sp0.y; P.az[i] = v.sp0.z;
+    P.bx[i] = v.sp1.x; P.by[i] = v.sp1.y; P.bz[i] = v.sp1.z;
 }
 // EPA.h face construction: normal = normalize(cross(v0 - v1, v2 - v1)), left as is when degenerate
 __device__ __forceinline__ void wp_set_face(WarpPoly& P, int slot, int i0, int i1, int i2) {
@@ -53,6 +54,7 @@ __device__ __forceinline__ void wp_set_face(WarpPoly& P, int slot, int i0, int i
     double len = length(n);
     if (len) n = n / len;
     P.nx[slot] = n.x; P.ny[slot] = n.y; P.nz[slot] = n.z;
+    P.fd[slot] = dot(wp_pos(P, i0), n);
     P.i0[slot] = (unsigned char)i0; P.i1[slot] = (unsigned char)i1; P.i2[slot] = (unsigned char)i2;
 }
 
@@ -90,7 +92,23 @@ __device__ __forceinline__ V3 warp_support(const Support& s, V3 dir, int lane) {
 __device__ __noinline__ GjkVertex warp_mink(const Support& s0, const Support& s1, V3 dir, int lane) {
     V3 a = warp_support(s0, dir, lane);
     V3 b = warp_support(s1, -dir, lane);
-    return {d3(a - b), d3(a), d3(b)};
+    return {d3(a - b), a, b};
+}
+
+// GJK.h containsOrigin with its three face tests on lanes 0-2 at once; the first face
+// (in the reference's order) whose test holds gives the new direction, as in the
+// sequential version.
+__device__ inline bool warp_contains_origin(GjkSimplex& s, D3& dir, int& fi, int lane) {
+    const int j = lane < 3 ? lane : 0;
+    const int b = j == 0 ? 0 : (j == 1 ? 2 : 1), c = j == 0 ? 1 : (j == 1 ? 0 : 2), o = 2 - j;
+    D3 n;
+    bool hit = checkFace(s.v[3].pos, s.v[b].pos, s.v[c].pos, s.v[o].pos, n);
+    unsigned m = __ballot_sync(0xffffffffu, hit && lane < 3);
+    if (!m) { fi = 0; return true; }
+    int w = __ffs(m) - 1;
+    dir = {__shfl_sync(0xffffffffu, n.x, w), __shfl_sync(0xffffffffu, n.y, w), __shfl_sync(0xffffffffu, n.z, w)};
+    fi = 2 - w;
+    return false;
 }
 
 struct WarpMink {
@@ -98,6 +116,7 @@ struct WarpMink {
     const Support& s1;
     int lane;
     __device__ GjkVertex operator()(V3 dir) const { return warp_mink(s0, s1, dir, lane); }
+    __device__ bool containsOrigin(GjkSimplex& s, D3& dir, int& fi) const { return warp_contains_origin(s, dir, fi, lane); }
 };
 
 __device__ __forceinline__ double warp_min_d(double v) {
@@ -142,7 +161,7 @@ __device__ inline V3 warp_epa(const WarpMink& mk, const GjkSimplex& s, V3& cp0, 
             int k = lane + 32 * j;
             dk[j] = CUDART_NAN;
             if (k < nf) {
-                dk[j] = dot(wp_pos(P, P.i0[k]), wp_n(P, k));
+                dk[j] = P.fd[k];
                 if (dk[j] < dmin) dmin = dk[j];
             }
         }
@@ -169,7 +188,7 @@ __device__ inline V3 warp_epa(const WarpMink& mk, const GjkSimplex& s, V3& cp0, 
             last = __reduce_max_sync(0xffffffffu, last);
             fi = last >= 0 ? last : first;
             normal = wp_n(P, fi);
-            minDist = (float)dot(wp_pos(P, P.i0[fi]), normal);
+            minDist = (float)P.fd[fi];
         }
         GjkVertex v = mk(f3(normal));
         if (dot(v.pos, normal) - minDist < (double)0.00001f) break;
@@ -207,7 +226,7 @@ __device__ inline V3 warp_epa(const WarpMink& mk, const GjkSimplex& s, V3& cp0, 
                 }
                 // remove face k: the last face moves into its slot
                 int l = n - 1;
-                P.nx[k] = P.nx[l]; P.ny[k] = P.ny[l]; P.nz[k] = P.nz[l];
+                P.nx[k] = P.nx[l]; P.ny[k] = P.ny[l]; P.nz[k] = P.nz[l]; P.fd[k] = P.fd[l];
                 P.i0[k] = P.i0[l]; P.i1[k] = P.i1[l]; P.i2[k] = P.i2[l];
                 --n;
             }
@@ -237,7 +256,7 @@ __device__ inline V3 warp_epa(const WarpMink& mk, const GjkSimplex& s, V3& cp0, 
     const int f0 = P.i0[fi], f1 = P.i1[fi], f2 = P.i2[fi];
     D3 fn = wp_n(P, fi);
     D3 pa = wp_pos(P, f0), pb = wp_pos(P, f1), pc = wp_pos(P, f2);
-    D3 proj = fn + dot(pa, fn);
+    D3 proj = fn + P.fd[fi];
     V3 v0 = f3(pb - pa), v1 = f3(pc - pa), v2 = f3(proj - pa);
     double d00 = dot(v0, v0), d01 = dot(v0, v1), d11 = dot(v1, v1), d20 = dot(v2, v0), d21 = dot(v2, v1);
     double denom = d00 * d11 - d01 * d01;
@@ -251,7 +270,7 @@ __device__ inline V3 warp_epa(const WarpMink& mk, const GjkSimplex& s, V3& cp0, 
         if (d00) { vv = d20 / d00; u = 1.0f - vv; }
         else { vv = 0; u = 1.0; }
     }
-    D3 a0 = {(double)P.ax[f0], (double)P.ay[f0], (double)P.az[f0]};
+    D3 a0 = {(double)P.ax[f0], (double)P.ay[f0], (double)P.az[f0]};   // f32 support points widened here
     D3 a1 = {(double)P.ax[f1], (double)P.ay[f1], (double)P.az[f1]};
     D3 a2 = {(double)P.ax[f2], (double)P.ay[f2], (double)P.az[f2]};
     D3 b0 = {(double)P.bx[f0], (double)P.by[f0], (double)P.bz[f0]};

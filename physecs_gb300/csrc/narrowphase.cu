@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(128) k_narrow_analytic(World w, FrameBuf f) {
 
 // convex-mesh pairs, part 1: GJK + EPA with one warp per pair.  The EPA normal and
 // closest points (or "no contact") are staged in the pair's manifold slot.
-constexpr int kConvexWarps = 4;
+constexpr int kConvexWarps = 3;
 constexpr int kConvexBlocksPerSM = 5;
 
 __device__ __forceinline__ bool convex_pair_ordered(const World& w, int2 pr, V3& pos0, Q4& or0, GeomD& g0, V3& pos1,
@@ -209,7 +209,7 @@ int launch_narrowphase(const World& w, FrameBuf& f, cudaStream_t s) {
     k_narrow_analytic<<<1216, 128, 0, s>>>(w, f);
     static bool carveout_set = false;
     if (!carveout_set) {
-        // five blocks of four polytopes (about 39 KB each) per SM
+        // five blocks of three polytopes (about 38 KB each) per SM
         cudaFuncSetAttribute(k_convex_gjk_epa, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         carveout_set = true;
     }
