@@ -239,6 +239,9 @@ SERVE_CLASSES = [(17, 96), (33, 96), (65, 96), (129, 96), (257, 96), (513, 96), 
                  (8193, 24)]
 # requests of at most 1000 bodies (the latency target's class)
 SERVE_CLASSES_SMALL = [(17, 48), (33, 48), (65, 48), (129, 48), (257, 32), (513, 24), (1025, 16)]
+# the same requests with the slot budget sized for a frame latency target: fewer slots,
+# so that a full server's tick stays near 2 ms
+SERVE_CLASSES_SLO = [(17, 16), (33, 16), (65, 16), (129, 12), (257, 8), (513, 6), (1025, 4)]
 
 
 def serving_requests(count, rank=0, n_max=8192):
@@ -341,7 +344,7 @@ def run_serving(args, rank, world, local):
     import numpy as np
     from physecs_gb300.api import Server
     small = args.serve_max_bodies <= 1000
-    classes = SERVE_CLASSES_SMALL if small else SERVE_CLASSES
+    classes = (SERVE_CLASSES_SLO if args.serve_slo else SERVE_CLASSES_SMALL) if small else SERVE_CLASSES
     reqs, pool_scene = serving_requests(384, rank, n_max=args.serve_max_bodies)
     from physecs_gb300.desc import make_desc
     descs = [make_desc(s) for s, _ in reqs]          # the clients' packed requests
@@ -389,6 +392,7 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=20.0)
     ap.add_argument("--serve-load", type=float, default=0.7)
     ap.add_argument("--serve-max-bodies", type=int, default=8192)
+    ap.add_argument("--serve-slo", action="store_true", help="slot budget sized for the 2 ms frame target")
     ap.add_argument("--scenes", type=int, default=4096)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--plain-scenes", type=int, default=64)

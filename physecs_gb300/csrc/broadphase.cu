@@ -314,20 +314,64 @@ __global__ void k_pairs_check(FrameBuf f, int* err) {
     if (*f.n_pairs > f.pair_cap) { atomicOr(err, ERR_PAIR_CAPACITY); *f.n_pairs = f.pair_cap; }
 }
 
-int launch_broadphase(const World& w, FrameBuf& f, int scene_bits, cudaStream_t s) {
+// One block per scene sorts the scene's (Morton code, collider) pairs in shared memory
+// with a bitonic network over 64-bit keys (code << 32 | collider), which orders equal
+// codes by collider exactly like the stable radix sort.  A scene that is not running
+// gets a constant code instead: its tree is never walked, only built and refitted.
+__global__ void __launch_bounds__(256) k_scene_sort(World w, FrameBuf f, int pmax) {
+    extern __shared__ unsigned long long sk[];
+    const int s = blockIdx.x;
+    const int cs = w.scene_col[s], n = w.scene_col[s + 1] - cs;
+    if (n <= 0) return;
+    if (w.scene_active && !w.scene_active[s]) {
+        for (int i = threadIdx.x; i < n; i += blockDim.x) { f.order[cs + i] = cs + i; f.keys[cs + i] = 0u; }
+        return;
+    }
+    int P = 1;
+    while (P < n) P <<= 1;
+    if (P > pmax) return;   // the launch sizes pmax for the largest scene
+    for (int i = threadIdx.x; i < P; i += blockDim.x)
+        sk[i] = i < n ? ((unsigned long long)f.mkey[cs + i] << 32) | (unsigned)(cs + i) : ~0ull;
+    __syncthreads();
+    for (int size = 2; size <= P; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int t = threadIdx.x; t < P / 2; t += blockDim.x) {
+                int i = 2 * t - (t & (stride - 1));   // first of the pair
+                int j = i + stride;
+                bool up = (i & size) == 0;
+                unsigned long long a = sk[i], b = sk[j];
+                if ((a > b) == up) { sk[i] = b; sk[j] = a; }
+            }
+            __syncthreads();
+        }
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        unsigned long long v = sk[i];
+        f.order[cs + i] = (int)(unsigned)v;
+        f.keys[cs + i] = (uint32_t)(v >> 32);
+    }
+}
+
+int launch_broadphase(const World& w, FrameBuf& f, int scene_bits, int scene_sort_pmax, cudaStream_t s) {
     int n = w.n_colliders;
     if (n == 0) return 0;
     int nb = (n + 255) / 256;
     k_scene_bounds<<<w.n_scenes, 256, 0, s>>>(w, f);
     k_morton<<<nb, 256, 0, s>>>(w, f);
-    // (scene, Morton) order as two stable LSD sorts: Morton first, then scene
-    int k = 2 + radix_sort_pairs(f.keys, f.order, f.keys_tmp, f.order_tmp, n, 32, f.radix_hist, s);
-    if (scene_bits > 0) {
-        k_scene_keys<<<nb, 256, 0, s>>>(w, f);
-        k += 1 + radix_sort_pairs(f.keys, f.order, f.keys_tmp, f.order_tmp, n, scene_bits, f.radix_hist, s);
+    int k = 2;
+    if (scene_sort_pmax > 0) {
+        k_scene_sort<<<w.n_scenes, 256, scene_sort_pmax * sizeof(unsigned long long), s>>>(w, f, scene_sort_pmax);
+        ++k;
+    } else {
+        // (scene, Morton) order as two stable LSD sorts: Morton first, then scene
+        k += radix_sort_pairs(f.keys, f.order, f.keys_tmp, f.order_tmp, n, 32, f.radix_hist, s);
+        if (scene_bits > 0) {
+            k_scene_keys<<<nb, 256, 0, s>>>(w, f);
+            k += 1 + radix_sort_pairs(f.keys, f.order, f.keys_tmp, f.order_tmp, n, scene_bits, f.radix_hist, s);
+        }
+        k_gather_keys<<<nb, 256, 0, s>>>(w, f);
+        ++k;
     }
-    k_gather_keys<<<nb, 256, 0, s>>>(w, f);
-    ++k;
     k_karras<<<nb, 256, 0, s>>>(w, f);
     k_refit<<<nb, 256, 0, s>>>(w, f);
     k_traverse<false><<<nb, 256, 0, s>>>(w, f);

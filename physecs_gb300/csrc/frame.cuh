@@ -77,7 +77,9 @@ struct FrameBuf {
 // kernels it queued
 int launch_aabb(const World& w, int margin_mode, cudaStream_t s);
 int launch_aabb_range(const World& w, int c0, int c1, int margin_mode, cudaStream_t s);
-int launch_broadphase(const World& w, FrameBuf& f, int scene_bits, cudaStream_t s);
+// scene_sort_pmax > 0: every scene has at most that many colliders (a power of two) and
+// is sorted by its own block in shared memory; 0: one radix sort over the whole world
+int launch_broadphase(const World& w, FrameBuf& f, int scene_bits, int scene_sort_pmax, cudaStream_t s);
 int launch_narrowphase(const World& w, FrameBuf& f, cudaStream_t s);
 int launch_contacts(const World& w, FrameBuf& f, cudaStream_t s);
 // scenes of one frame's solver launch: small block scenes (one 256-thread block each),

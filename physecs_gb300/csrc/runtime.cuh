@@ -35,6 +35,7 @@ struct psx_world {
     std::vector<void*> allocs;
     int n_scenes = 0;
     int scene_bits = 0;     // bits of the scene index in the broadphase sort
+    int scene_sort_pmax = 0; // > 0: per-scene sort in shared memory, scenes padded to this size
     std::vector<int> h_scene_body, h_scene_col, h_scene_dyn;
     std::vector<uint32_t> h_entity;        // per body
     std::vector<int> h_body_dyn;           // per body: global dyn index or -1

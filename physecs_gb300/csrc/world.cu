@@ -475,6 +475,14 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
         W->solver_smem_large = std::max(0, optin - 5120) / 16 * 16;
     }
     W->scene_bits = S <= 1 ? 0 : ilog2ceil(S);
+    {
+        // scenes of at most 4096 colliders are sorted block by block in shared memory
+        int maxc = 0;
+        for (int s = 0; s < S; ++s) maxc = std::max(maxc, scene_col[s + 1] - scene_col[s]);
+        int P = 1;
+        while (P < maxc) P <<= 1;
+        W->scene_sort_pmax = (S > 1 && P <= 4096) ? P : 0;   // at most 32 KB of shared memory
+    }
     // creation bounds: no margin (src/Physecs.cpp:32)
     launch_aabb(w, 0, W->stream);
     PSX_CUDA(cudaGetLastError());
@@ -489,7 +497,7 @@ int psx::rt::queue_frame(psx_world* W, cudaEvent_t* ev) {
     int k = 0;
     cudaStream_t s = W->stream;
     if (ev) cudaEventRecord(ev[0], s);
-    k += launch_broadphase(W->w, W->f, W->scene_bits, s);
+    k += launch_broadphase(W->w, W->f, W->scene_bits, W->scene_sort_pmax, s);
     if (ev) cudaEventRecord(ev[1], s);
     k += launch_narrowphase(W->w, W->f, s);
     if (ev) cudaEventRecord(ev[2], s);
