@@ -262,9 +262,10 @@ def _serve(srv, reqs, arrivals, t_end, max_backlog=None, descs=None):
     arrived and read and release the finished ones; then wait for the tick and start
     the next.  arrivals[i] is request i's arrival (seconds from start) or None for a
     permanent backlog.  Returns (frame latencies s, request latencies s, body-substeps
-    run, wall s).  A frame's latency runs from the moment it could start (the
-    request's admission for its first frame, the previous frame's result for the
-    others) to its result being ready."""
+    run, wall s).  A frame's latency runs from the moment it could start (for the first
+    frame, the start of the tick in which the request joins the batch; for the others,
+    the previous frame's result) to its result being ready.  Waiting for a slot counts
+    in the request latency (arrival to final result)."""
     import collections
     import numpy as np
     n_slots = srv.stats()["slots"]
@@ -281,6 +282,7 @@ def _serve(srv, reqs, arrivals, t_end, max_backlog=None, descs=None):
     ticks = 0
     in_flight = False
     finished = []
+    joining = []
     while True:
         now = time.perf_counter() - t0
         if now >= t_end:
@@ -306,9 +308,9 @@ def _serve(srv, reqs, arrivals, t_end, max_backlog=None, descs=None):
                 continue
             on[slot] = True
             arrival[slot] = ta
-            last[slot] = time.perf_counter() - t0
             wps[slot] = s.n_dynamic * s.num_substeps
             first[slot] = ticks + 1
+            joining.append(slot)
         queue = waiting
         # ---- finish the tick in flight, start the next
         if in_flight:
@@ -325,6 +327,9 @@ def _serve(srv, reqs, arrivals, t_end, max_backlog=None, descs=None):
             in_flight = False
         if on.any():
             srv.tick_begin()
+            # a request is admitted when it joins the running batch: the start of its first tick
+            last[joining] = time.perf_counter() - t0
+            joining = []
             ticks += 1
             in_flight = True
         else:
