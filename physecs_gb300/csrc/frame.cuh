@@ -59,6 +59,7 @@ struct FrameBuf {
     // per-substep contact records of scenes whose records do not fit in shared memory
     int* pt_off;          // [man_cap] first point of each contact, colour order
     int2* cbody;          // [man_cap] colouring: scene-local dynamic bodies of each contact
+    uint4* cmask;         // [n_dyn] colouring: colours each dynamic body carries (128 bits)
     SHdr* s_hdr;          // [man_cap]
     SPt* s_pts;           // [4 * man_cap]
     // restitution cache: open addressing, two tables; cache_parity selects the current one

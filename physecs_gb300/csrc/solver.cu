@@ -705,6 +705,17 @@ struct BlockSync {
     __device__ __forceinline__ int any2(bool a, bool b) const {
         return (__syncthreads_or(a) ? 1 : 0) | (__syncthreads_or(b) ? 2 : 0);
     }
+    // block-wide maximum of v (v >= -1)
+    __device__ int max_int(int v) const {
+        __shared__ int mx;
+        if (threadIdx.x == 0) mx = -1;
+        __syncthreads();
+        atomicMax(&mx, v);
+        __syncthreads();
+        int r = mx;
+        __syncthreads();
+        return r;
+    }
     // first point of each contact (colour order) packed without gaps; returns the point count
     __device__ int point_offsets(FrameBuf& f, int ms, int nc) const {
         __shared__ int part[1025];
@@ -744,6 +755,17 @@ struct GridSync {
         return r;
     }
     __device__ __forceinline__ int any2(bool a, bool b) const { return (any(a) ? 1 : 0) | (any(b) ? 2 : 0); }
+    // grid-wide maximum of v (v >= -1), through the barrier's spare word
+    __device__ int max_int(int v) const {
+        int* slot = flag + 1;
+        if (threadIdx.x == 0 && blockIdx.x == 0) atomicExch(slot, -1);
+        bar.sync();
+        atomicMax(slot, v);
+        bar.sync();
+        int r = *(volatile int*)slot;
+        bar.sync();
+        return r;
+    }
     // four point slots per contact (no cross-block scan in grid mode)
     __device__ int point_offsets(FrameBuf& f, int ms, int nc) const {
         for (int k = tid(); k < nc; k += nth()) f.pt_off[ms + k] = 4 * k;
@@ -752,16 +774,22 @@ struct GridSync {
     }
 };
 
-// Colouring of one scene's contacts (see solve_scene); claim[d - ds], cb[k], col[k] are
-// indexed by scene-local dynamic body and contact.  Returns the number of colours.  When
-// kMaxColors - 1 colours leave contacts over (a body touching more than that many others),
-// the rest form a last colour that is solved by one thread in contact order.
+// Colouring of one scene's contacts (see solve_scene): first fit, in rounds.  Every
+// uncoloured contact proposes the lowest colour that neither of its dynamic bodies
+// carries yet (a 128-bit mask per body); each body accepts the lowest proposal, ties
+// going to a hashed priority of the contact's index within the scene; a contact
+// accepted by both bodies takes its colour.  At most one contact per body is coloured
+// per round, so no two contacts of a colour share a dynamic body, and the result does
+// not depend on thread timing.  mask[d - ds], claim[d - ds], cb[k], col[k] are indexed
+// by scene-local dynamic body and contact.  Contacts that find no colour below
+// kMaxColors - 1 form a last colour that one thread solves in contact order; the
+// return value is then negative.
 template <class S>
 __device__ int colour_contacts(const World& w, FrameBuf& f, int ms, int nc, int ds, int nd, const S& sy,
-                               unsigned long long* claim, int2* cb, int* col) {
+                               unsigned long long* claim, uint4* mask, int2* cb, int* col) {
     const int tid = sy.tid(), nth = sy.nth();
     const unsigned long long kFree = ~0ull;
-    for (int d = tid; d < nd; d += nth) claim[d] = kFree;
+    for (int d = tid; d < nd; d += nth) { claim[d] = kFree; mask[d] = make_uint4(0, 0, 0, 0); }
     for (int k = tid; k < nc; k += nth) {
         const Contact& c = f.contacts[ms + k];
         cb[k] = make_int2(c.b0 >= 0 ? c.b0 - ds : -1, c.b1 >= 0 ? c.b1 - ds : -1);
@@ -769,55 +797,63 @@ __device__ int colour_contacts(const World& w, FrameBuf& f, int ms, int nc, int 
     }
     sy.sync();
     int ncol = 0;
-    for (;;) {
-        bool any_left = false;
-        for (int round = 0;; ++round) {
-            for (int k = tid; k < nc; k += nth) {
-                if (col[k] >= 0) continue;
-                const int2 b = cb[k];
-                bool free0 = b.x < 0 || (unsigned)(claim[b.x] >> 48) != (unsigned)ncol;
-                bool free1 = b.y < 0 || (unsigned)(claim[b.y] >> 48) != (unsigned)ncol;
-                if (!(free0 && free1)) continue;
-                unsigned long long pri = 0xffff000000000000ull |
-                    ((unsigned long long)(cache_hash((unsigned long long)k * 0x9E3779B97F4A7C15ull + 131u * ncol + round) & 0xffffu) << 32) |
-                    (unsigned)k;
-                if (b.x >= 0) atomicMin(&claim[b.x], pri);
-                if (b.y >= 0) atomicMin(&claim[b.y], pri);
-            }
-            sy.sync();
-            bool joined = false, left = false;
-            for (int k = tid; k < nc; k += nth) {
-                if (col[k] >= 0) continue;
-                const int2 b = cb[k];
-                unsigned long long k0 = b.x >= 0 ? claim[b.x] : 0, k1 = b.y >= 0 ? claim[b.y] : 0;
-                bool own0 = b.x < 0 || ((k0 >> 48) == 0xffffull && (unsigned)k0 == (unsigned)k);
-                bool own1 = b.y < 0 || ((k1 >> 48) == 0xffffull && (unsigned)k1 == (unsigned)k);
-                if (own0 && own1) { col[k] = ncol; joined = true; }
-                else left = true;
-            }
-            sy.sync();
-            // bodies of the colour's members are held by the colour; other claims reset
-            for (int k = tid; k < nc; k += nth) {
-                if (col[k] != ncol) continue;
-                const int2 b = cb[k];
-                if (b.x >= 0) claim[b.x] = (unsigned long long)ncol << 48;
-                if (b.y >= 0) claim[b.y] = (unsigned long long)ncol << 48;
-            }
-            sy.sync();
-            for (int d = tid; d < nd; d += nth)
-                if ((claim[d] >> 48) == 0xffffull) claim[d] = kFree;
-            int flags = sy.any2(joined, left);
-            if (!(flags & 1) || !(flags & 2)) { any_left = (flags & 2) != 0; break; }
+    bool overflow = false;
+    for (int round = 0;; ++round) {
+        bool left = false, committed = false;
+        for (int k = tid; k < nc; k += nth) {
+            if (col[k] >= 0) continue;
+            const int2 b = cb[k];
+            uint4 m0 = b.x >= 0 ? mask[b.x] : make_uint4(0, 0, 0, 0);
+            uint4 m1 = b.y >= 0 ? mask[b.y] : make_uint4(0, 0, 0, 0);
+            unsigned u[4] = {m0.x | m1.x, m0.y | m1.y, m0.z | m1.z, m0.w | m1.w};
+            int c = kMaxColors - 1;
+            for (int q = 0; q < 4; ++q)
+                if (~u[q]) { c = 32 * q + __ffs(~u[q]) - 1; break; }
+            if (c >= kMaxColors - 1) continue;   // no colour left: the serial colour takes it
+            unsigned long long v = ((unsigned long long)c << 40) |
+                                   ((unsigned long long)(cache_hash((unsigned long long)k * 0x9E3779B97F4A7C15ull + round) & 0xffffu) << 24) |
+                                   (unsigned)k;
+            if (b.x >= 0) atomicMin(&claim[b.x], v);
+            if (b.y >= 0) atomicMin(&claim[b.y], v);
         }
-        ++ncol;
-        for (int d = tid; d < nd; d += nth) claim[d] = kFree;   // the next colour starts free
         sy.sync();
-        if (!any_left) break;
-        if (ncol == kMaxColors - 1) {
-            for (int k = tid; k < nc; k += nth) if (col[k] < 0) col[k] = ncol;
-            sy.sync();
-            return -kMaxColors;   // negative: the last colour is serial
+        for (int k = tid; k < nc; k += nth) {
+            if (col[k] >= 0) continue;
+            const int2 b = cb[k];
+            unsigned long long v0 = b.x >= 0 ? claim[b.x] : kFree, v1 = b.y >= 0 ? claim[b.y] : kFree;
+            bool mine0 = b.x < 0 || (v0 != kFree && (unsigned)(v0 & 0xffffffu) == (unsigned)k);
+            bool mine1 = b.y < 0 || (v1 != kFree && (unsigned)(v1 & 0xffffffu) == (unsigned)k);
+            if (b.x < 0 && b.y < 0) { col[k] = 0; committed = true; continue; }
+            if (mine0 && mine1) {
+                int c = (int)((b.x >= 0 ? v0 : v1) >> 40);
+                col[k] = c;
+                committed = true;
+                // each body accepted only this contact this round: plain updates suffice
+                unsigned bit = 1u << (c & 31);
+                int q = c >> 5;
+                if (b.x >= 0) { unsigned* mm = (unsigned*)&mask[b.x]; mm[q] |= bit; }
+                if (b.y >= 0) { unsigned* mm = (unsigned*)&mask[b.y]; mm[q] |= bit; }
+            } else {
+                left = true;
+            }
         }
+        sy.sync();
+        for (int d = tid; d < nd; d += nth) claim[d] = kFree;
+        // the lowest proposal of a round always wins both its bodies, so a round without a
+        // new colour means every open contact is out of colours
+        int flags = sy.any2(left, committed);
+        if (!(flags & 1)) break;
+        if (!(flags & 2)) { overflow = true; break; }
+    }
+    // colours used; contacts left without one form a last colour, solved serially
+    int top = -1;
+    for (int k = tid; k < nc; k += nth) if (col[k] >= 0) top = max(top, col[k]);
+    top = sy.max_int(top);
+    ncol = top + 1;
+    if (overflow) {
+        for (int k = tid; k < nc; k += nth) if (col[k] < 0) col[k] = ncol;
+        sy.sync();
+        return -(ncol + 1);   // negative: the last colour is serial
     }
     return ncol;
 }
@@ -840,11 +876,12 @@ __device__ void solve_scene(const World& w, FrameBuf& f, int s, const S& sy, flo
     // share the world.  The working arrays (bodies of each contact, colour of each
     // contact, one claim word per dynamic body) live in shared memory when they fit.
     const int nd = de - ds, nc = me - ms;
-    const bool col_smem = 8 * (size_t)nd + 12 * (size_t)nc <= 16 * (size_t)smem_f4;
-    unsigned long long* claim = col_smem ? (unsigned long long*)smem : f.claim + ds;
+    const bool col_smem = 24 * (size_t)nd + 12 * (size_t)nc <= 16 * (size_t)smem_f4;
+    uint4* cmask = col_smem ? (uint4*)smem : f.cmask + ds;
+    unsigned long long* claim = col_smem ? (unsigned long long*)(cmask + nd) : f.claim + ds;
     int2* cb = col_smem ? (int2*)(claim + nd) : f.cbody + ms;
     int* col = col_smem ? (int*)(cb + nc) : f.color_of + ms;
-    int ncol = colour_contacts(w, f, ms, nc, ds, nd, sy, claim, cb, col);
+    int ncol = colour_contacts(w, f, ms, nc, ds, nd, sy, claim, cmask, cb, col);
     const bool serial_last = ncol < 0;
     if (serial_last) ncol = -ncol;
     // counting sort of the scene's contacts by colour

@@ -441,6 +441,7 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
     PSX_TRY(W->alloc(f.claim_pos, (size_t)S * (kMaxColors + 1)));
     PSX_TRY(W->alloc(f.pt_off, f.man_cap));
     PSX_TRY(W->alloc(f.cbody, f.man_cap));
+    PSX_TRY(W->alloc(f.cmask, std::max(1, w.n_dyn)));
     PSX_TRY(W->alloc(f.s_hdr, f.man_cap));
     PSX_TRY(W->alloc(f.s_pts, 4 * (size_t)f.man_cap));
     PSX_TRY(W->alloc(f.cache_a, f.cache_cap));
