@@ -81,7 +81,12 @@ int launch_aabb_range(const World& w, int c0, int c1, int margin_mode, cudaStrea
 // scene_sort_pmax > 0: every scene has at most that many colliders (a power of two) and
 // is sorted by its own block in shared memory; 0: one radix sort over the whole world
 int launch_broadphase(const World& w, FrameBuf& f, int scene_bits, int scene_sort_pmax, cudaStream_t s);
-int launch_narrowphase(const World& w, FrameBuf& f, cudaStream_t s);
+// a second stream with a fork / join event pair, for kernels that may overlap
+struct StreamPair {
+    cudaStream_t aux;
+    cudaEvent_t fork, join;
+};
+int launch_narrowphase(const World& w, FrameBuf& f, const StreamPair& sp, cudaStream_t s);
 int launch_contacts(const World& w, FrameBuf& f, cudaStream_t s);
 // scenes of one frame's solver launch: small block scenes (one 256-thread block each),
 // large block scenes (one 512-thread block each, on the aux stream), grid scenes

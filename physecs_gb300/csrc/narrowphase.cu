@@ -203,19 +203,25 @@ __global__ void __launch_bounds__(64) k_narrow_tri(World w, FrameBuf f) {
     }
 }
 
-int launch_narrowphase(const World& w, FrameBuf& f, cudaStream_t s) {
+// The convex kernels (bound by the FP64 pipe) run on the aux stream beside the analytic
+// and triangle-mesh kernels (FP32, latency-bound); the categories write disjoint slots.
+int launch_narrowphase(const World& w, FrameBuf& f, const StreamPair& sp, cudaStream_t s) {
     cudaMemsetAsync(f.cat_count, 0, 3 * sizeof(int), s);
     k_classify<<<1216, 256, 0, s>>>(w, f);
-    k_narrow_analytic<<<1216, 128, 0, s>>>(w, f);
     static bool carveout_set = false;
     if (!carveout_set) {
         // five blocks of three polytopes (about 38 KB each) per SM
         cudaFuncSetAttribute(k_convex_gjk_epa, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         carveout_set = true;
     }
-    k_convex_gjk_epa<<<152 * kConvexBlocksPerSM, 32 * kConvexWarps, 0, s>>>(w, f);
-    k_convex_contacts<<<1216, 128, 0, s>>>(w, f);
+    cudaEventRecord(sp.fork, s);
+    cudaStreamWaitEvent(sp.aux, sp.fork, 0);
+    k_convex_gjk_epa<<<152 * kConvexBlocksPerSM, 32 * kConvexWarps, 0, sp.aux>>>(w, f);
+    k_convex_contacts<<<1216, 128, 0, sp.aux>>>(w, f);
+    cudaEventRecord(sp.join, sp.aux);
+    k_narrow_analytic<<<1216, 128, 0, s>>>(w, f);
     k_narrow_tri<<<1216, 64, 0, s>>>(w, f);
+    cudaStreamWaitEvent(s, sp.join, 0);
     scan_exclusive_dev(f.pair_nman, f.pair_moff, f.n_pairs, f.pair_cap, f.n_man, f.scan_scratch, s);
     return 2 + 4 + 3;
 }

@@ -51,7 +51,8 @@ struct psx_world {
     std::vector<int> large_scenes_h; // block scenes above 1024 dynamic bodies
     int* large_scenes = nullptr;
     cudaStream_t aux_stream = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;     // solver: large scenes on the aux stream
+    cudaEvent_t ev_fork2 = nullptr, ev_join2 = nullptr;   // narrowphase: convex pairs on the aux stream
     std::vector<float4> h_knobs;
     bool use_graph = false;
     cudaGraphExec_t graph = nullptr;
@@ -88,6 +89,8 @@ struct psx_world {
         for (void* p : allocs) cudaFree(p);
         if (pin) cudaFreeHost(pin);
         if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_fork2) cudaEventDestroy(ev_fork2);
+        if (ev_join2) cudaEventDestroy(ev_join2);
         if (ev_join) cudaEventDestroy(ev_join);
         if (aux_stream) cudaStreamDestroy(aux_stream);
         if (stream) cudaStreamDestroy(stream);

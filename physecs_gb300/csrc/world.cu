@@ -500,7 +500,7 @@ int psx::rt::queue_frame(psx_world* W, cudaEvent_t* ev) {
     if (ev) cudaEventRecord(ev[0], s);
     k += launch_broadphase(W->w, W->f, W->scene_bits, W->scene_sort_pmax, s);
     if (ev) cudaEventRecord(ev[1], s);
-    k += launch_narrowphase(W->w, W->f, s);
+    k += launch_narrowphase(W->w, W->f, StreamPair{W->aux_stream, W->ev_fork2, W->ev_join2}, s);
     if (ev) cudaEventRecord(ev[2], s);
     k += launch_contacts(W->w, W->f, s);
     k += launch_joint_layout(W->w, W->f, s);
@@ -580,6 +580,8 @@ PSX_API psx_status psx_world_create(const psx_scene_desc* scenes, int32_t n_scen
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&W->aux_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&W->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&W->ev_join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&W->ev_fork2, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&W->ev_join2, cudaEventDisableTiming);
     if (e != cudaSuccess) { delete W; return fail(PSX_ERR_CUDA, cudaGetErrorString(e)); }
     psx_status s = build_world(W, scenes, n_scenes, o);
     if (s != PSX_OK) { delete W; return s; }
