@@ -250,3 +250,39 @@ def test_graph_launched_frames_equal_eager_frames(gpu_lib):
         for k in sa:
             assert np.array_equal(sa[k].view(np.uint32), sb[k].view(np.uint32)), (f, k)
     assert b.counts()["kernels"] > 0
+
+
+def test_kinematic_trigger_disabled_and_empty_scenes(gpu_lib, oracle_lib):
+    """A ragged batch with kinematic bodies, trigger and disabled colliders, a scene without
+    dynamic bodies and a scene without contacts: every scene equals its own oracle run."""
+    from tests.scene_variants import apart_scene, flagged_scene, static_only_scene
+    ss = [flagged_scene(), static_only_scene(), apart_scene(), scenes.pyramid(rows=3), flagged_scene(32, 40)]
+    g = _gpu(ss)
+    os_ = [_oracle(s) for s in ss]
+    start = g.body_start
+    for f in range(20):
+        g.step(); g.synchronize()
+        ids, gf, meta = g.contacts()
+        st = g.read_bodies()
+        gp = g.pairs()
+        for i, o in enumerate(os_):
+            sel = ids[:, 0] == i
+            o.set_contact_order(gpu_keys(ids[sel], meta[sel]))
+            o.step()
+            assert o.order_error() == 0
+            if f == 0:
+                assert pair_set(gp[gp[:, 0] == i][:, 1:]) == pair_set(o.pairs())
+            d = rel_state_diff({k: v[start[i]:start[i + 1]] for k, v in st.items()}, o.state())
+            assert d <= TOL, "scene %d frame %d: %g" % (i, f, d)
+    assert g.counts()["error"] == 0
+
+
+def test_capacity_overflow_is_reported(gpu_lib):
+    """A pair capacity far below the scene's pair count: the frame reports
+    PSX_ERR_CAPACITY through the device error word instead of dropping pairs silently."""
+    from physecs_gb300.api import PsxError
+    s = scenes.pyramid(rows=40)   # 820 cubes: about 2500 pairs once the margins apply
+    g = _gpu(s, pairs_per_collider=1, manifolds_per_collider=1)   # capacity max(1024, colliders)
+    g.step(frames=3)
+    with pytest.raises(PsxError, match="CAPACITY"):
+        g.synchronize()

@@ -130,6 +130,22 @@ def _ref_available():
 
 
 @pytest.mark.skipif(not _ref_available(), reason="oracle/_ref (the reference built from its sources) is not built here")
+def test_oracle_matches_live_reference_on_flagged_scenes(oracle_lib):
+    """Kinematic bodies, triggers, disabled colliders, no dynamic bodies, no contacts."""
+    from oracle.ref.ref_api import RefScene
+    from tests.scene_variants import apart_scene, flagged_scene, static_only_scene
+    for s in (flagged_scene(), static_only_scene(), apart_scene(), flagged_scene(32, 40)):
+        o, r = oracle_lib.OracleScene(s), RefScene(s)
+        for f in range(30):
+            o.step()
+            r.step()
+            a, b = o.state(), r.state()
+            for k in a:
+                np.testing.assert_array_equal(a[k], b[k], err_msg="frame %d %s" % (f, k))
+        np.testing.assert_array_equal(o.pairs(), r.pairs())
+
+
+@pytest.mark.skipif(not _ref_available(), reason="oracle/_ref (the reference built from its sources) is not built here")
 @pytest.mark.parametrize("seed,n,chain", [(11, 300, 0.0), (12, 200, 1.0), (13, 1500, 0.3)])
 def test_oracle_matches_live_reference(oracle_lib, seed, n, chain):
     """Where the reference library is built, run both side by side for 40 frames."""
