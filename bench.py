@@ -404,6 +404,7 @@ def main():
     ap.add_argument("--cpu-scenes", type=int, default=256)
     ap.add_argument("--cpu-frames", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default kernel launch shapes")
     args = ap.parse_args()
     rank, world, local = dist_info()
     assert args.warmup >= 3, "at least three warm-up steps"
@@ -418,7 +419,16 @@ def main():
     ss, cfg = build_workload(args.workload, rank, args.scenes)
     n_sim = simulated_bodies(ss)
     substeps = ss[0].num_substeps
-    w = World(ss, device=local if world > 1 else 0)
+    dev = local if world > 1 else 0
+    w = World(ss, device=dev)
+    if not args.no_tune and len(ss) > 1:
+        # warm-up includes the autotuner: it picks launch shapes on a throwaway world's
+        # frames, and the measured world is created afresh with them
+        launch = w.tune(frames=2)
+        w.close()
+        w = World(ss, device=dev, launch=launch)
+        cfg = dict(cfg)
+        cfg["launch"] = launch
     for _ in range(args.warmup):
         w.step(DT)
     w.synchronize()

@@ -151,12 +151,24 @@ typedef struct psx_scene_desc {
  * ---------------------------------------------------------------------- */
 typedef struct psx_world psx_world;
 
+/* Launch shapes of the kernels whose best shape depends on the workload.  None of them
+ * changes a result; 0 in a field keeps the default.  psx_world_tune picks them. */
+typedef struct psx_launch_config {
+    int32_t convex_warps;            /* GJK/EPA: warps (pairs) per block, 1-3 (default 3) */
+    int32_t convex_blocks_per_sm;    /* GJK/EPA: blocks per SM in the grid (default 5) */
+    int32_t analytic_threads;        /* sphere/capsule/box pairs: threads per block, <= 256 (default 128) */
+    int32_t analytic_blocks_per_sm;  /* (default 8) */
+    int32_t contacts_threads;        /* convex contact generation: threads per block, <= 256 (default 128) */
+    int32_t solver_smem_kb;          /* shared memory per 256-thread solver block in KB (default: by scene count) */
+} psx_launch_config;
+
 typedef struct psx_world_opts {
     int32_t pairs_per_collider;      /* broadphase pair capacity per collider (0: default 8) */
     int32_t manifolds_per_collider;  /* contact manifold capacity per collider (0: default 4) */
     int32_t block_scene_max_dyn;     /* scenes up to this many dynamic bodies run one per CTA (0: default 8192) */
     int32_t use_graph;               /* capture the frame in a CUDA graph after the first step */
     int32_t device;                  /* CUDA device ordinal the world lives on */
+    const psx_launch_config* launch; /* kernel launch shapes, or NULL for the defaults */
 } psx_world_opts;
 
 /* Scene::Scene(registry, numThreads) plus the registry's contents
@@ -199,6 +211,11 @@ PSX_API psx_status psx_world_read_bodies_noalloc(psx_world* w, float* pos, float
 /* One end-to-end simulate through host buffers: upload the given state, step one
  * frame, download the new state into the same buffers, and wait. */
 PSX_API psx_status psx_world_simulate_host(psx_world* w, float dt, float* pos, float* quat, float* vel, float* ang_vel);
+/* Autotuner: runs `frames` frames (they advance the world) for each candidate launch
+ * shape of each tunable kernel, one kernel at a time, timing its stage with CUDA events;
+ * keeps the fastest and writes the chosen configuration to *best.  Results do not
+ * depend on the launch shapes; throughput does. */
+PSX_API psx_status psx_world_tune(psx_world* w, int32_t frames, psx_launch_config* best);
 /* counts[12] = {bodies, colliders, dynamic bodies, joints, scenes, pairs, manifolds, error bits,
  *              contact points, joint rows, simulated bodies, kernels queued since creation}
  * (per-frame values describe the last frame) */

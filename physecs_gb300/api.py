@@ -25,7 +25,8 @@ EXPORTS = ["psx_world_create", "psx_world_destroy", "psx_world_step", "psx_world
            "psx_world_get_pairs", "psx_world_get_contacts", "psx_world_get_bounds", "psx_last_error_string",
            "psx_scene_create", "psx_scene_destroy", "psx_scene_simulate", "psx_world_read_bodies_noalloc",
            "psx_server_create", "psx_server_destroy", "psx_server_admit", "psx_server_tick", "psx_server_read",
-           "psx_server_release", "psx_server_stats", "psx_server_tick_begin", "psx_server_tick_end", "psx_server_world"]
+           "psx_server_release", "psx_server_stats", "psx_server_tick_begin", "psx_server_tick_end", "psx_server_world",
+           "psx_world_tune"]
 
 _lib = None
 
@@ -34,9 +35,18 @@ class PsxError(RuntimeError):
     pass
 
 
+LAUNCH_FIELDS = ["convex_warps", "convex_blocks_per_sm", "analytic_threads", "analytic_blocks_per_sm",
+                 "contacts_threads", "solver_smem_kb"]
+
+
+class PsxLaunchConfig(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in LAUNCH_FIELDS]
+
+
 class PsxWorldOpts(C.Structure):
     _fields_ = [("pairs_per_collider", C.c_int32), ("manifolds_per_collider", C.c_int32),
-                ("block_scene_max_dyn", C.c_int32), ("use_graph", C.c_int32), ("device", C.c_int32)]
+                ("block_scene_max_dyn", C.c_int32), ("use_graph", C.c_int32), ("device", C.c_int32),
+                ("launch", C.c_void_p)]
 
 
 class PsxServerOpts(C.Structure):
@@ -78,6 +88,7 @@ def load():
     lib.psx_server_admit.argtypes = [vp, C.POINTER(PsxSceneDesc), C.c_int32, C.c_float, vp]
     lib.psx_server_tick.argtypes = [vp, vp, C.c_int32, vp]
     lib.psx_server_tick_begin.argtypes = [vp]
+    lib.psx_world_tune.argtypes = [vp, C.c_int32, vp]
     lib.psx_server_world.argtypes = [vp]
     lib.psx_server_world.restype = vp
     lib.psx_server_tick_end.argtypes = [vp, vp, C.c_int32, vp]
@@ -104,7 +115,8 @@ class World:
     h = None
 
     def __init__(self, scenes, pairs_per_collider=0, manifolds_per_collider=0, block_scene_max_dyn=0, use_graph=False,
-                 device=0):
+                 device=0, launch=None):
+        """launch: dict of psx_launch_config fields (missing or 0: default shapes)."""
         lib = load()
         if not isinstance(scenes, (list, tuple)):
             scenes = [scenes]
@@ -113,8 +125,11 @@ class World:
         for i, s in enumerate(scenes):
             arr[i] = make_desc(s)
         self._descs = arr
+        self._launch = None
+        if launch:
+            self._launch = PsxLaunchConfig(*[int(launch.get(n, 0)) for n in LAUNCH_FIELDS])
         opts = PsxWorldOpts(pairs_per_collider, manifolds_per_collider, block_scene_max_dyn, 1 if use_graph else 0,
-                            device)
+                            device, C.cast(C.pointer(self._launch), C.c_void_p) if self._launch is not None else None)
         h = C.c_void_p()
         _check(lib.psx_world_create(arr, len(scenes), C.byref(opts), C.byref(h)))
         self.h = h
@@ -148,6 +163,13 @@ class World:
 
     def synchronize(self):
         _check(load().psx_world_synchronize(self.h))
+
+    def tune(self, frames=2):
+        """psx_world_tune: pick the kernels' launch shapes on this world's frames (they
+        advance the world).  Returns the chosen configuration as a dict."""
+        c = PsxLaunchConfig()
+        _check(load().psx_world_tune(self.h, frames, C.byref(c)))
+        return {n: int(getattr(c, n)) for n in LAUNCH_FIELDS}
 
     def set_knobs(self, substeps, iterations, gravity, scene=-1):
         _check(load().psx_world_set_knobs(self.h, scene, substeps, iterations, C.c_float(gravity)))

@@ -86,7 +86,12 @@ struct StreamPair {
     cudaStream_t aux;
     cudaEvent_t fork, join;
 };
-int launch_narrowphase(const World& w, FrameBuf& f, const StreamPair& sp, cudaStream_t s);
+struct NarrowShape {
+    int convex_warps, convex_blocks_per_sm;
+    int analytic_threads, analytic_blocks_per_sm;
+    int contacts_threads;
+};
+int launch_narrowphase(const World& w, FrameBuf& f, const StreamPair& sp, const NarrowShape& ns, cudaStream_t s);
 int launch_contacts(const World& w, FrameBuf& f, cudaStream_t s);
 // scenes of one frame's solver launch: small block scenes (one 256-thread block each),
 // large block scenes (one 512-thread block each, on the aux stream), grid scenes

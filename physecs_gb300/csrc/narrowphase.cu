@@ -80,7 +80,7 @@ __global__ void k_classify(World w, FrameBuf f) {
 }
 
 // analytic pairs: sphere / capsule / box
-__global__ void __launch_bounds__(128) k_narrow_analytic(World w, FrameBuf f) {
+__global__ void __launch_bounds__(256) k_narrow_analytic(World w, FrameBuf f) {
     int n = f.cat_count[0];
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         int p = f.cat_list[t];
@@ -100,8 +100,6 @@ __global__ void __launch_bounds__(128) k_narrow_analytic(World w, FrameBuf f) {
 
 // convex-mesh pairs, part 1: GJK + EPA with one warp per pair.  The EPA normal and
 // closest points (or "no contact") are staged in the pair's manifold slot.
-constexpr int kConvexWarps = 3;
-constexpr int kConvexBlocksPerSM = 5;
 
 __device__ __forceinline__ bool convex_pair_ordered(const World& w, int2 pr, V3& pos0, Q4& or0, GeomD& g0, V3& pos1,
                                                     Q4& or1, GeomD& g1) {
@@ -118,12 +116,15 @@ __device__ __forceinline__ bool convex_pair_ordered(const World& w, int2 pr, V3&
     return swap;
 }
 
-__global__ void __launch_bounds__(32 * kConvexWarps, kConvexBlocksPerSM) k_convex_gjk_epa(World w, FrameBuf f) {
-    __shared__ WarpPoly polys[kConvexWarps];
+// WARPS pairs per block, one polytope (about 12.8 KB) each; at most 15 warps per SM share
+// the register file at 128 registers a thread
+template <int WARPS>
+__global__ void __launch_bounds__(32 * WARPS, 15 / WARPS) k_convex_gjk_epa(World w, FrameBuf f) {
+    __shared__ WarpPoly polys[WARPS];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     WarpPoly& P = polys[wid];
     const int n = f.cat_count[1];
-    for (int t = blockIdx.x * kConvexWarps + wid; t < n; t += gridDim.x * kConvexWarps) {
+    for (int t = blockIdx.x * WARPS + wid; t < n; t += gridDim.x * WARPS) {
         const int p = f.cat_list[f.pair_cap + t];
         V3 pos0, pos1;
         Q4 or0, or1;
@@ -148,7 +149,7 @@ __global__ void __launch_bounds__(32 * kConvexWarps, kConvexBlocksPerSM) k_conve
 
 // convex-mesh pairs, part 2: contact generation after EPA (face selection and
 // clipping, Collision.cpp:352-887), one thread per pair.
-__global__ void __launch_bounds__(128) k_convex_contacts(World w, FrameBuf f) {
+__global__ void __launch_bounds__(256) k_convex_contacts(World w, FrameBuf f) {
     const int n = f.cat_count[1];
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         const int p = f.cat_list[f.pair_cap + t];
@@ -203,23 +204,29 @@ __global__ void __launch_bounds__(64) k_narrow_tri(World w, FrameBuf f) {
     }
 }
 
-// The convex kernels (bound by the FP64 pipe) run on the aux stream beside the analytic
-// and triangle-mesh kernels (FP32, latency-bound); the categories write disjoint slots.
-int launch_narrowphase(const World& w, FrameBuf& f, const StreamPair& sp, cudaStream_t s) {
-    cudaMemsetAsync(f.cat_count, 0, 3 * sizeof(int), s);
-    k_classify<<<1216, 256, 0, s>>>(w, f);
+template <int WARPS>
+static void launch_convex(const World& w, FrameBuf& f, int blocks_per_sm, cudaStream_t s) {
     static bool carveout_set = false;
     if (!carveout_set) {
-        // five blocks of three polytopes (about 38 KB each) per SM
-        cudaFuncSetAttribute(k_convex_gjk_epa, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        cudaFuncSetAttribute(k_convex_gjk_epa<WARPS>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         carveout_set = true;
     }
+    k_convex_gjk_epa<WARPS><<<152 * blocks_per_sm, 32 * WARPS, 0, s>>>(w, f);
+}
+
+// The convex kernels (bound by the FP64 pipe) run on the aux stream beside the analytic
+// and triangle-mesh kernels (FP32, latency-bound); the categories write disjoint slots.
+int launch_narrowphase(const World& w, FrameBuf& f, const StreamPair& sp, const NarrowShape& ns, cudaStream_t s) {
+    cudaMemsetAsync(f.cat_count, 0, 3 * sizeof(int), s);
+    k_classify<<<1216, 256, 0, s>>>(w, f);
     cudaEventRecord(sp.fork, s);
     cudaStreamWaitEvent(sp.aux, sp.fork, 0);
-    k_convex_gjk_epa<<<152 * kConvexBlocksPerSM, 32 * kConvexWarps, 0, sp.aux>>>(w, f);
-    k_convex_contacts<<<1216, 128, 0, sp.aux>>>(w, f);
+    if (ns.convex_warps == 1) launch_convex<1>(w, f, ns.convex_blocks_per_sm, sp.aux);
+    else if (ns.convex_warps == 2) launch_convex<2>(w, f, ns.convex_blocks_per_sm, sp.aux);
+    else launch_convex<3>(w, f, ns.convex_blocks_per_sm, sp.aux);
+    k_convex_contacts<<<1216 * 128 / ns.contacts_threads, ns.contacts_threads, 0, sp.aux>>>(w, f);
     cudaEventRecord(sp.join, sp.aux);
-    k_narrow_analytic<<<1216, 128, 0, s>>>(w, f);
+    k_narrow_analytic<<<152 * ns.analytic_blocks_per_sm, ns.analytic_threads, 0, s>>>(w, f);
     k_narrow_tri<<<1216, 64, 0, s>>>(w, f);
     cudaStreamWaitEvent(s, sp.join, 0);
     scan_exclusive_dev(f.pair_nman, f.pair_moff, f.n_pairs, f.pair_cap, f.n_man, f.scan_scratch, s);

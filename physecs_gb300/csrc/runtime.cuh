@@ -45,6 +45,7 @@ struct psx_world {
     int* grid_scenes = nullptr;
     int grid_blocks = 0;
     int solver_smem = 0;             // dynamic shared memory per solver block (bytes)
+    psx::NarrowShape narrow{3, 5, 128, 8, 128};   // launch shapes of the narrowphase kernels
     long long frames_run = 0;        // frames queued since creation
     int frame_kernels = 0;           // kernels in one frame
     int solver_smem_large = 0;       // the same for the 512-thread blocks of large scenes
@@ -107,6 +108,9 @@ psx_status build_world(psx_world* W, const psx_scene_desc* scenes, int S, const 
 int queue_frame(psx_world* W, cudaEvent_t* ev = nullptr);
 // one frame on W's stream, through W's CUDA graph when it uses one
 psx_status run_frame(psx_world* W);
+// launch shapes: apply (0 fields keep the current value) and read back
+psx_status apply_launch(psx_world* W, const psx_launch_config& c);
+psx_launch_config current_launch(const psx_world* W);
 // reads the device error word; maps its bits to a status
 psx_status check_err(psx_world* W);
 // pinned host staging of at least n4 float4

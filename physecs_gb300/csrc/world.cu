@@ -482,7 +482,7 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
         for (int s = 0; s < S; ++s) maxc = std::max(maxc, scene_col[s + 1] - scene_col[s]);
         int P = 1;
         while (P < maxc) P <<= 1;
-        W->scene_sort_pmax = (S > 1 && P <= 4096) ? P : 0;   // at most 32 KB of shared memory
+        W->scene_sort_pmax = P <= 4096 ? P : 0;   // at most 32 KB of shared memory
     }
     // creation bounds: no margin (src/Physecs.cpp:32)
     launch_aabb(w, 0, W->stream);
@@ -500,7 +500,7 @@ int psx::rt::queue_frame(psx_world* W, cudaEvent_t* ev) {
     if (ev) cudaEventRecord(ev[0], s);
     k += launch_broadphase(W->w, W->f, W->scene_bits, W->scene_sort_pmax, s);
     if (ev) cudaEventRecord(ev[1], s);
-    k += launch_narrowphase(W->w, W->f, StreamPair{W->aux_stream, W->ev_fork2, W->ev_join2}, s);
+    k += launch_narrowphase(W->w, W->f, StreamPair{W->aux_stream, W->ev_fork2, W->ev_join2}, W->narrow, s);
     if (ev) cudaEventRecord(ev[2], s);
     k += launch_contacts(W->w, W->f, s);
     k += launch_joint_layout(W->w, W->f, s);
@@ -538,6 +538,44 @@ psx_status psx::rt::run_frame(psx_world* W) {
     }
     ++W->frames_run;
     return PSX_OK;
+}
+
+// Validate and apply launch shapes (0 keeps the current value).
+psx_status psx::rt::apply_launch(psx_world* W, const psx_launch_config& c) {
+    NarrowShape n = W->narrow;
+    if (c.convex_warps) n.convex_warps = c.convex_warps;
+    if (c.convex_blocks_per_sm) n.convex_blocks_per_sm = c.convex_blocks_per_sm;
+    if (c.analytic_threads) n.analytic_threads = c.analytic_threads;
+    if (c.analytic_blocks_per_sm) n.analytic_blocks_per_sm = c.analytic_blocks_per_sm;
+    if (c.contacts_threads) n.contacts_threads = c.contacts_threads;
+    auto threads_ok = [](int t) { return t == 32 || t == 64 || t == 128 || t == 256; };
+    if (n.convex_warps < 1 || n.convex_warps > 3 || n.convex_blocks_per_sm < 1 || n.convex_blocks_per_sm > 32 ||
+        !threads_ok(n.analytic_threads) || n.analytic_blocks_per_sm < 1 || n.analytic_blocks_per_sm > 64 ||
+        !threads_ok(n.contacts_threads))
+        return fail(PSX_ERR_INVALID_ARG, "launch config out of range");
+    int smem = W->solver_smem;
+    if (c.solver_smem_kb) {
+        int dev = 0, optin = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        smem = c.solver_smem_kb * 1024;
+        if (smem < 16 * 1024 || smem > optin - 5120) return fail(PSX_ERR_INVALID_ARG, "solver shared memory out of range");
+    }
+    W->narrow = n;
+    W->solver_smem = smem;
+    if (W->graph) { cudaGraphExecDestroy(W->graph); W->graph = nullptr; }   // recaptured with the new shapes
+    return PSX_OK;
+}
+
+psx_launch_config psx::rt::current_launch(const psx_world* W) {
+    psx_launch_config c{};
+    c.convex_warps = W->narrow.convex_warps;
+    c.convex_blocks_per_sm = W->narrow.convex_blocks_per_sm;
+    c.analytic_threads = W->narrow.analytic_threads;
+    c.analytic_blocks_per_sm = W->narrow.analytic_blocks_per_sm;
+    c.contacts_threads = W->narrow.contacts_threads;
+    c.solver_smem_kb = W->solver_smem / 1024;
+    return c;
 }
 
 psx_status psx::rt::check_err(psx_world* W) {
@@ -585,6 +623,10 @@ PSX_API psx_status psx_world_create(const psx_scene_desc* scenes, int32_t n_scen
     if (e != cudaSuccess) { delete W; return fail(PSX_ERR_CUDA, cudaGetErrorString(e)); }
     psx_status s = build_world(W, scenes, n_scenes, o);
     if (s != PSX_OK) { delete W; return s; }
+    if (o.launch) {
+        s = apply_launch(W, *o.launch);
+        if (s != PSX_OK) { delete W; return s; }
+    }
     *out = W;
     return PSX_OK;
 }
@@ -655,6 +697,94 @@ PSX_API psx_status psx_world_step_timed(psx_world* W, float dt, int32_t frames, 
     if (stage_ms) for (int s = 0; s < 5; ++s) stage_ms[s] = st[s];
     if (kernels) *kernels = W->launches - k0;
     return check_err(W);
+}
+
+// Mean time of one stage (0 broadphase, 1 narrowphase, 2 contact rows, 3 solver) over
+// `frames` frames, after one untimed frame with the same shapes.
+static psx_status time_stage(psx_world* W, int frames, int stage, float* ms) {
+    queue_frame(W);
+    size_t need = 6 * (size_t)frames;
+    while (W->events.size() < need) {
+        cudaEvent_t e;
+        PSX_CUDA(cudaEventCreate(&e));
+        W->events.push_back(e);
+    }
+    for (int i = 0; i < frames; ++i) queue_frame(W, &W->events[6 * (size_t)i]);
+    PSX_CUDA(cudaStreamSynchronize(W->stream));
+    PSX_TRY(check_err(W));
+    float sum = 0;
+    for (int i = 0; i < frames; ++i) {
+        float t = 0;
+        PSX_CUDA(cudaEventElapsedTime(&t, W->events[6 * (size_t)i + stage], W->events[6 * (size_t)i + stage + 1]));
+        sum += t;
+    }
+    *ms = sum / frames;
+    return PSX_OK;
+}
+
+PSX_API psx_status psx_world_tune(psx_world* W, int32_t frames, psx_launch_config* best) {
+    if (!W || frames < 1) return fail(PSX_ERR_INVALID_ARG, "psx_world_tune");
+    PSX_CUDA(cudaSetDevice(W->device));
+    if (W->h_knobs.empty()) return fail(PSX_ERR_INVALID_ARG, "empty world");
+    psx_launch_config cur = current_launch(W);
+    struct Knob { int stage; std::vector<psx_launch_config> cands; };
+    std::vector<Knob> knobs;
+    {   // GJK/EPA: warps per block x blocks per SM (at most 15 warps per SM)
+        Knob k{1, {}};
+        for (int wv : {1, 2, 3})
+            for (int b : {3, 5, 7, 10, 15}) {
+                if (wv * b > 15) continue;
+                psx_launch_config c{};
+                c.convex_warps = wv;
+                c.convex_blocks_per_sm = b;
+                k.cands.push_back(c);
+            }
+        knobs.push_back(k);
+    }
+    {   // analytic pairs
+        Knob k{1, {}};
+        for (int t : {64, 128, 256})
+            for (int b : {4, 8, 16}) {
+                psx_launch_config c{};
+                c.analytic_threads = t;
+                c.analytic_blocks_per_sm = b;
+                k.cands.push_back(c);
+            }
+        knobs.push_back(k);
+    }
+    {   // convex contact generation
+        Knob k{1, {}};
+        for (int t : {64, 128, 256}) {
+            psx_launch_config c{};
+            c.contacts_threads = t;
+            k.cands.push_back(c);
+        }
+        knobs.push_back(k);
+    }
+    if (W->block_scenes_h.size() > 152) {   // many small scenes: shared memory per solver block
+        Knob k{3, {}};
+        for (int kb : {48, 64, 100}) {
+            psx_launch_config c{};
+            c.solver_smem_kb = kb;
+            k.cands.push_back(c);
+        }
+        knobs.push_back(k);
+    }
+    for (const Knob& k : knobs) {
+        float best_ms = 1e30f;
+        psx_launch_config pick = cur;
+        for (const psx_launch_config& c : k.cands) {
+            PSX_TRY(apply_launch(W, cur));
+            PSX_TRY(apply_launch(W, c));
+            float ms = 0;
+            PSX_TRY(time_stage(W, frames, k.stage, &ms));
+            if (ms < best_ms) { best_ms = ms; pick = current_launch(W); }
+        }
+        cur = pick;
+        PSX_TRY(apply_launch(W, cur));
+    }
+    if (best) *best = cur;
+    return PSX_OK;
 }
 
 PSX_API psx_status psx_world_synchronize(psx_world* W) {

@@ -286,3 +286,19 @@ def test_capacity_overflow_is_reported(gpu_lib):
     g.step(frames=3)
     with pytest.raises(PsxError, match="CAPACITY"):
         g.synchronize()
+
+
+def test_launch_shapes_do_not_change_results(gpu_lib):
+    """Any launch configuration the tuner may pick gives the same frames bit for bit."""
+    ss = [scenes.batch_scene(80 + i, n_bodies=n) for i, n in enumerate([60, 1300, 200, 25])]
+    a = _gpu(ss)
+    b = _gpu(ss, launch=dict(convex_warps=1, convex_blocks_per_sm=12, analytic_threads=64, analytic_blocks_per_sm=4,
+                             contacts_threads=256, solver_smem_kb=48))
+    for f in range(8):
+        a.step(); b.step()
+        a.synchronize(); b.synchronize()
+        sa, sb = a.read_bodies(), b.read_bodies()
+        for k in sa:
+            assert np.array_equal(sa[k].view(np.uint32), sb[k].view(np.uint32)), (f, k)
+    cfg = b.tune(frames=1)
+    assert set(cfg) >= {"convex_warps", "analytic_threads", "solver_smem_kb"}
