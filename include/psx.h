@@ -160,6 +160,9 @@ typedef struct psx_launch_config {
     int32_t analytic_blocks_per_sm;  /* (default 8) */
     int32_t contacts_threads;        /* convex contact generation: threads per block, <= 256 (default 128) */
     int32_t solver_smem_kb;          /* shared memory per 256-thread solver block in KB (default: by scene count) */
+    int32_t large_scene_solver;      /* scenes above the block limit: 1 one thread-block cluster each (those whose
+                                      * velocities fit the cluster's shared memory), 2 the whole grid, one scene
+                                      * after another (default: clusters when two or more scenes fit them) */
 } psx_launch_config;
 
 typedef struct psx_world_opts {
@@ -216,6 +219,8 @@ PSX_API psx_status psx_world_simulate_host(psx_world* w, float dt, float* pos, f
  * keeps the fastest and writes the chosen configuration to *best.  Results do not
  * depend on the launch shapes; throughput does. */
 PSX_API psx_status psx_world_tune(psx_world* w, int32_t frames, psx_launch_config* best);
+/* The launch shapes in effect (after defaults, tuning or opts.launch). */
+PSX_API psx_status psx_world_launch_config(psx_world* w, psx_launch_config* out);
 /* counts[12] = {bodies, colliders, dynamic bodies, joints, scenes, pairs, manifolds, error bits,
  *              contact points, joint rows, simulated bodies, kernels queued since creation}
  * (per-frame values describe the last frame) */

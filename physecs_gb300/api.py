@@ -26,7 +26,7 @@ EXPORTS = ["psx_world_create", "psx_world_destroy", "psx_world_step", "psx_world
            "psx_scene_create", "psx_scene_destroy", "psx_scene_simulate", "psx_world_read_bodies_noalloc",
            "psx_server_create", "psx_server_destroy", "psx_server_admit", "psx_server_tick", "psx_server_read",
            "psx_server_release", "psx_server_stats", "psx_server_tick_begin", "psx_server_tick_end", "psx_server_world",
-           "psx_world_tune"]
+           "psx_world_tune", "psx_world_launch_config"]
 
 _lib = None
 
@@ -36,7 +36,7 @@ class PsxError(RuntimeError):
 
 
 LAUNCH_FIELDS = ["convex_warps", "convex_blocks_per_sm", "analytic_threads", "analytic_blocks_per_sm",
-                 "contacts_threads", "solver_smem_kb"]
+                 "contacts_threads", "solver_smem_kb", "large_scene_solver"]
 
 
 class PsxLaunchConfig(C.Structure):
@@ -169,6 +169,12 @@ class World:
         advance the world).  Returns the chosen configuration as a dict."""
         c = PsxLaunchConfig()
         _check(load().psx_world_tune(self.h, frames, C.byref(c)))
+        return {n: int(getattr(c, n)) for n in LAUNCH_FIELDS}
+
+    def launch_config(self):
+        """psx_world_launch_config: the launch shapes in effect, as a dict."""
+        c = PsxLaunchConfig()
+        _check(load().psx_world_launch_config(self.h, C.byref(c)))
         return {n: int(getattr(c, n)) for n in LAUNCH_FIELDS}
 
     def set_knobs(self, substeps, iterations, gravity, scene=-1):

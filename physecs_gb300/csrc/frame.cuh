@@ -96,9 +96,11 @@ int launch_contacts(const World& w, FrameBuf& f, cudaStream_t s);
 // scenes of one frame's solver launch: small block scenes (one 256-thread block each),
 // large block scenes (one 512-thread block each, on the aux stream), grid scenes
 // (the whole grid, one after another)
+constexpr int kClusterBlocks = 8;   // blocks of the cluster that solves one large scene
 struct SolverLaunch {
     const int* small; int n_small; int smem_small;
     const int* large; int n_large; int smem_large;
+    const int* cluster; int n_cluster;     // large scenes solved by one cluster each
     const int* grid; int n_grid; int grid_blocks;
     cudaStream_t aux;
     cudaEvent_t fork, join;

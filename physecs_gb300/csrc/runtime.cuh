@@ -51,6 +51,10 @@ struct psx_world {
     int solver_smem_large = 0;       // the same for the 512-thread blocks of large scenes
     std::vector<int> large_scenes_h; // block scenes above 1024 dynamic bodies
     int* large_scenes = nullptr;
+    std::vector<int> big_scenes_h;     // scenes above the block limit
+    std::vector<int> cluster_scenes_h; // ... solved by a thread-block cluster each
+    int* cluster_scenes = nullptr;     // (grid_scenes: the rest; both sized for every big scene)
+    int large_mode = 0;                // 1: clusters where they fit, 2: the whole grid
     cudaStream_t aux_stream = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;     // solver: large scenes on the aux stream
     cudaEvent_t ev_fork2 = nullptr, ev_join2 = nullptr;   // narrowphase: convex pairs on the aux stream
@@ -111,6 +115,9 @@ psx_status run_frame(psx_world* W);
 // launch shapes: apply (0 fields keep the current value) and read back
 psx_status apply_launch(psx_world* W, const psx_launch_config& c);
 psx_launch_config current_launch(const psx_world* W);
+// splits the scenes above the block limit between clusters and the grid (mode as
+// psx_launch_config::large_scene_solver, 0: by the default rule)
+psx_status partition_big(psx_world* W, int mode);
 // reads the device error word; maps its bits to a status
 psx_status check_err(psx_world* W);
 // pinned host staging of at least n4 float4

@@ -13,6 +13,7 @@
 // integration, relaxation and write-back.  Small scenes run one per CTA with
 // __syncthreads between phases; large scenes run on the whole grid with a
 // bounded grid barrier.
+#include <cooperative_groups.h>
 #include "frame.cuh"
 
 namespace psx {
@@ -367,27 +368,37 @@ __device__ void row_presolve(const World& w, Row& r, bool simd) {
     }
 }
 
-// Body velocities the iterations work on: six float arrays in shared memory for a scene
-// that fits (s != null, body d at index d - off), else the world's vt arrays.
+// Body velocities the iterations work on, as six float arrays of n entries:
+//   - in this block's shared memory (s != null, body d at index d - off);
+//   - spread over the blocks of a thread-block cluster (rs != null: body d at block
+//     (d - off) mod 2^lg, index (d - off) >> lg, through distributed shared memory);
+//   - else the world's vt arrays.
 struct VelRef {
     float* s;
+    float* const* rs;
     float4* v;
     float4* w;
-    int off, n;
+    int off, n, lg;
+    __device__ __forceinline__ float* base(int d, int& j) const {
+        int i = d - off;
+        if (rs) { j = i >> lg; return rs[i & ((1 << lg) - 1)]; }
+        j = i;
+        return s;
+    }
     __device__ __forceinline__ V3 lv(int d) const {
-        if (s) { int i = d - off; return {s[i], s[n + i], s[2 * n + i]}; }
+        if (s || rs) { int j; const float* b = base(d, j); return {b[j], b[n + j], b[2 * n + j]}; }
         return ld3(v[d]);
     }
     __device__ __forceinline__ V3 lw(int d) const {
-        if (s) { int i = d - off; return {s[3 * n + i], s[4 * n + i], s[5 * n + i]}; }
+        if (s || rs) { int j; const float* b = base(d, j); return {b[3 * n + j], b[4 * n + j], b[5 * n + j]}; }
         return ld3(w[d]);
     }
     __device__ __forceinline__ void sv(int d, V3 x) const {
-        if (s) { int i = d - off; s[i] = x.x; s[n + i] = x.y; s[2 * n + i] = x.z; }
+        if (s || rs) { int j; float* b = base(d, j); b[j] = x.x; b[n + j] = x.y; b[2 * n + j] = x.z; }
         else v[d] = st4(x);
     }
     __device__ __forceinline__ void sw(int d, V3 x) const {
-        if (s) { int i = d - off; s[3 * n + i] = x.x; s[4 * n + i] = x.y; s[5 * n + i] = x.z; }
+        if (s || rs) { int j; float* b = base(d, j); b[3 * n + j] = x.x; b[4 * n + j] = x.y; b[5 * n + j] = x.z; }
         else w[d] = st4(x);
     }
 };
@@ -697,6 +708,7 @@ __device__ void integrate_position(const World& w, int d, float h, const VelRef&
 // ---------------------------------------------------------------- frame kernel
 
 struct BlockSync {
+    static constexpr bool kCluster = false;
     __device__ __forceinline__ void sync() const { __syncthreads(); }
     __device__ __forceinline__ int tid() const { return threadIdx.x; }
     __device__ __forceinline__ int nth() const { return blockDim.x; }
@@ -740,6 +752,7 @@ struct BlockSync {
     }
 };
 struct GridSync {
+    static constexpr bool kCluster = false;
     GridBarrier bar;
     int* flag;
     __device__ __forceinline__ void sync() const { bar.sync(); }
@@ -770,6 +783,50 @@ struct GridSync {
     __device__ int point_offsets(FrameBuf& f, int ms, int nc) const {
         for (int k = tid(); k < nc; k += nth()) f.pt_off[ms + k] = 4 * k;
         bar.sync();
+        return 4 * nc;
+    }
+};
+
+// A thread-block cluster working on one scene: the hardware cluster barrier orders
+// shared, distributed-shared and global memory for all its threads; reductions go
+// through a small array in block 0's shared memory.
+struct ClusterSync {
+    static constexpr bool kCluster = true;
+    int rank, R, lg;
+    float* const* bases;   // every block's dynamic shared memory, mapped
+    int* red;              // R ints in block 0's shared memory, mapped
+    __device__ __forceinline__ void sync() const { cooperative_groups::this_cluster().sync(); }
+    __device__ __forceinline__ int tid() const { return rank * blockDim.x + threadIdx.x; }
+    __device__ __forceinline__ int nth() const { return R * blockDim.x; }
+    // cluster-wide bitwise OR of v's two low bits (__syncthreads_or only reports "nonzero")
+    __device__ int reduce_or(int v) const {
+        int b = (__syncthreads_or(v & 1) ? 1 : 0) | (__syncthreads_or(v & 2) ? 2 : 0);
+        if (threadIdx.x == 0) red[rank] = b;
+        sync();
+        int r = 0;
+        for (int i = 0; i < R; ++i) r |= red[i];
+        sync();
+        return r;
+    }
+    __device__ __forceinline__ bool any(bool v) const { return reduce_or(v ? 1 : 0) != 0; }
+    __device__ __forceinline__ int any2(bool a, bool b) const { return reduce_or((a ? 1 : 0) | (b ? 2 : 0)); }
+    __device__ int max_int(int v) const {
+        __shared__ int bm;
+        if (threadIdx.x == 0) bm = -1;
+        __syncthreads();
+        atomicMax(&bm, v);
+        __syncthreads();
+        if (threadIdx.x == 0) red[rank] = bm;
+        sync();
+        int r = -1;
+        for (int i = 0; i < R; ++i) r = max(r, red[i]);
+        sync();
+        return r;
+    }
+    // four point slots per contact, as in grid mode
+    __device__ int point_offsets(FrameBuf& f, int ms, int nc) const {
+        for (int k = tid(); k < nc; k += nth()) f.pt_off[ms + k] = 4 * k;
+        sync();
         return 4 * nc;
     }
 };
@@ -876,7 +933,7 @@ __device__ void solve_scene(const World& w, FrameBuf& f, int s, const S& sy, flo
     // share the world.  The working arrays (bodies of each contact, colour of each
     // contact, one claim word per dynamic body) live in shared memory when they fit.
     const int nd = de - ds, nc = me - ms;
-    const bool col_smem = 24 * (size_t)nd + 12 * (size_t)nc <= 16 * (size_t)smem_f4;
+    const bool col_smem = !S::kCluster && 24 * (size_t)nd + 12 * (size_t)nc <= 16 * (size_t)smem_f4;
     uint4* cmask = col_smem ? (uint4*)smem : f.cmask + ds;
     unsigned long long* claim = col_smem ? (unsigned long long*)(cmask + nd) : f.claim + ds;
     int2* cb = col_smem ? (int2*)(claim + nd) : f.cbody + ms;
@@ -913,9 +970,16 @@ __device__ void solve_scene(const World& w, FrameBuf& f, int s, const S& sy, flo
     const int ncl = colstart[kMaxColors];   // coloured contacts (all, unless the colour cap was hit)
     int npts = sy.point_offsets(f, ms, ncl);   // first point of each contact -> f.pt_off[ms + k]
     const int vel_f4 = (6 * nd + 3) / 4;
-    const bool vel_smem = vel_f4 <= smem_f4;
+    const bool vel_smem = !S::kCluster && vel_f4 <= smem_f4;
     const bool rec_smem = vel_smem && vel_f4 + kHdrF4 * ncl + kPtF4 * npts <= smem_f4;
-    VelRef vr = vel_smem ? VelRef{(float*)smem, nullptr, nullptr, ds, nd} : VelRef{nullptr, w.vt_v, w.vt_w, 0, 0};
+    VelRef vr = vel_smem ? VelRef{(float*)smem, nullptr, nullptr, nullptr, ds, nd, 0}
+                         : VelRef{nullptr, nullptr, w.vt_v, w.vt_w, 0, 0, 0};
+    if constexpr (S::kCluster) {
+        // velocities spread over the cluster's blocks; records and colouring stay global
+        const int per = (nd + sy.R - 1) >> sy.lg;
+        if (6 * per <= 4 * smem_f4) vr = VelRef{nullptr, sy.bases, nullptr, nullptr, ds, per, sy.lg};
+        else vr = VelRef{nullptr, nullptr, w.vt_v, w.vt_w, 0, 0, 0};
+    }
     SHdr* H = rec_smem ? (SHdr*)(smem + vel_f4) : f.s_hdr + ms;
     SPt* P = rec_smem ? (SPt*)(smem + vel_f4 + kHdrF4 * ncl) : f.s_pts + 4 * (size_t)ms;
     for (int k = tid; k < ncl; k += nth) H[k].i.w = f.pt_off[ms + k];
@@ -995,6 +1059,24 @@ __global__ void __launch_bounds__(256, 2) k_solve_grid(World w, FrameBuf f, cons
     }
 }
 
+// one cluster of kClusterBlocks blocks per large scene, velocities in distributed shared memory
+template <int NT>
+__global__ void __launch_bounds__(NT, 1) k_solve_cluster(World w, FrameBuf f, const int* scenes, int smem_f4) {
+    extern __shared__ float4 smem[];
+    __shared__ float* bases[kClusterBlocks];
+    __shared__ int red[kClusterBlocks];
+    cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
+    const int R = (int)cl.num_blocks(), rank = (int)cl.block_rank();
+    if (threadIdx.x < R) bases[threadIdx.x] = cl.map_shared_rank((float*)smem, (int)threadIdx.x);
+    int* red0 = cl.map_shared_rank(red, 0);
+    int lg = 0;
+    while ((1 << lg) < R) ++lg;
+    cl.sync();
+    ClusterSync sy{rank, R, lg, bases, red0};
+    solve_scene(w, f, scenes[blockIdx.x / R], sy, smem, smem_f4);
+    cl.sync();   // no block leaves while the others may still read its shared memory
+}
+
 __global__ void k_zero_ints(int* p, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) p[i] = 0;
@@ -1045,6 +1127,27 @@ int launch_solver(const World& w, FrameBuf& f, const SolverLaunch& L, cudaStream
         ++k;
     }
     if (L.n_large) cudaStreamWaitEvent(s, L.join, 0);
+    if (L.n_cluster) {
+        static int cluster_smem = -1;
+        if (cluster_smem != L.smem_large) {
+            cudaFuncSetAttribute(k_solve_cluster<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, L.smem_large);
+            cluster_smem = L.smem_large;
+        }
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(kClusterBlocks * L.n_cluster);
+        cfg.blockDim = dim3(512);
+        cfg.dynamicSmemBytes = L.smem_large;
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = kClusterBlocks;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        cudaLaunchKernelEx(&cfg, k_solve_cluster<512>, w, f, L.cluster, L.smem_large / 16);
+        ++k;
+    }
     if (L.n_grid) {
         World wc = w;
         FrameBuf fc = f;

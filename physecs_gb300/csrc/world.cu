@@ -459,10 +459,6 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
     PSX_CUDA(cudaMemset(f.n_pairs, 0, sizeof(int)));
     PSX_CUDA(cudaMemset(f.n_man, 0, sizeof(int)));
     PSX_CUDA(cudaMemset(f.scene_man, 0, sizeof(int) * (S + 1)));
-    PSX_TRY(W->upload(W->block_scenes, W->block_scenes_h));
-    PSX_TRY(W->upload(W->large_scenes, W->large_scenes_h));
-    PSX_TRY(W->upload(W->grid_scenes, W->grid_scenes_h));
-    W->grid_blocks = W->grid_scenes_h.empty() ? 0 : solver_grid_blocks();
     // shared memory per solver block: the most a block may have when there are at most as
     // many block scenes as SMs, else a size that keeps two blocks resident per SM (the
     // register budget of the 256-thread solver allows two)
@@ -475,6 +471,12 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
         W->solver_smem = std::max(0, std::min(want, optin - 5120)) / 16 * 16;
         W->solver_smem_large = std::max(0, optin - 5120) / 16 * 16;
     }
+    W->big_scenes_h = W->grid_scenes_h;
+    PSX_TRY(W->upload(W->block_scenes, W->block_scenes_h));
+    PSX_TRY(W->upload(W->large_scenes, W->large_scenes_h));
+    PSX_TRY(W->alloc(W->cluster_scenes, W->big_scenes_h.size()));
+    PSX_TRY(W->alloc(W->grid_scenes, W->big_scenes_h.size()));
+    PSX_TRY(partition_big(W, 0));
     W->scene_bits = S <= 1 ? 0 : ilog2ceil(S);
     {
         // scenes of at most 4096 colliders are sorted block by block in shared memory
@@ -507,6 +509,7 @@ int psx::rt::queue_frame(psx_world* W, cudaEvent_t* ev) {
     if (ev) cudaEventRecord(ev[3], s);
     SolverLaunch L{W->block_scenes, (int)W->block_scenes_h.size(), W->solver_smem,
                    W->large_scenes, (int)W->large_scenes_h.size(), W->solver_smem_large,
+                   W->cluster_scenes, (int)W->cluster_scenes_h.size(),
                    W->grid_scenes, (int)W->grid_scenes_h.size(), W->grid_blocks,
                    W->aux_stream, W->ev_fork, W->ev_join};
     k += launch_solver(W->w, W->f, L, s);
@@ -561,9 +564,38 @@ psx_status psx::rt::apply_launch(psx_world* W, const psx_launch_config& c) {
         smem = c.solver_smem_kb * 1024;
         if (smem < 16 * 1024 || smem > optin - 5120) return fail(PSX_ERR_INVALID_ARG, "solver shared memory out of range");
     }
+    if (c.large_scene_solver < 0 || c.large_scene_solver > 2) return fail(PSX_ERR_INVALID_ARG, "large_scene_solver out of range");
+    if (c.large_scene_solver && c.large_scene_solver != W->large_mode) PSX_TRY(partition_big(W, c.large_scene_solver));
     W->narrow = n;
     W->solver_smem = smem;
     if (W->graph) { cudaGraphExecDestroy(W->graph); W->graph = nullptr; }   // recaptured with the new shapes
+    return PSX_OK;
+}
+
+// A cluster holds a scene's velocities in its blocks' shared memory, so it takes the
+// scenes whose velocities fit; several cluster scenes are solved side by side, while the
+// grid solves its scenes one after another with all SMs.
+psx_status psx::rt::partition_big(psx_world* W, int mode) {
+    auto fits = [&](int s) {
+        int nd = W->h_scene_dyn[s + 1] - W->h_scene_dyn[s];
+        int per = (nd + kClusterBlocks - 1) / kClusterBlocks;
+        return (size_t)per * 6 * sizeof(float) <= (size_t)W->solver_smem_large;
+    };
+    if (mode == 0) {
+        int n = 0;
+        for (int s : W->big_scenes_h) n += fits(s);
+        mode = n >= 2 ? 1 : 2;
+    }
+    W->cluster_scenes_h.clear();
+    W->grid_scenes_h.clear();
+    for (int s : W->big_scenes_h) (mode == 1 && fits(s) ? W->cluster_scenes_h : W->grid_scenes_h).push_back(s);
+    PSX_CUDA(cudaStreamSynchronize(W->stream));
+    if (!W->cluster_scenes_h.empty())
+        PSX_CUDA(cudaMemcpy(W->cluster_scenes, W->cluster_scenes_h.data(), W->cluster_scenes_h.size() * sizeof(int), cudaMemcpyHostToDevice));
+    if (!W->grid_scenes_h.empty())
+        PSX_CUDA(cudaMemcpy(W->grid_scenes, W->grid_scenes_h.data(), W->grid_scenes_h.size() * sizeof(int), cudaMemcpyHostToDevice));
+    W->grid_blocks = W->grid_scenes_h.empty() ? 0 : solver_grid_blocks();
+    W->large_mode = mode;
     return PSX_OK;
 }
 
@@ -575,6 +607,7 @@ psx_launch_config psx::rt::current_launch(const psx_world* W) {
     c.analytic_blocks_per_sm = W->narrow.analytic_blocks_per_sm;
     c.contacts_threads = W->narrow.contacts_threads;
     c.solver_smem_kb = W->solver_smem / 1024;
+    c.large_scene_solver = W->large_mode;
     return c;
 }
 
@@ -761,6 +794,15 @@ PSX_API psx_status psx_world_tune(psx_world* W, int32_t frames, psx_launch_confi
         }
         knobs.push_back(k);
     }
+    if (!W->big_scenes_h.empty()) {   // scenes above the block limit: clusters or the grid
+        Knob k{3, {}};
+        for (int m : {1, 2}) {
+            psx_launch_config c{};
+            c.large_scene_solver = m;
+            k.cands.push_back(c);
+        }
+        knobs.push_back(k);
+    }
     if (W->block_scenes_h.size() > 152) {   // many small scenes: shared memory per solver block
         Knob k{3, {}};
         for (int kb : {48, 64, 100}) {
@@ -784,6 +826,12 @@ PSX_API psx_status psx_world_tune(psx_world* W, int32_t frames, psx_launch_confi
         PSX_TRY(apply_launch(W, cur));
     }
     if (best) *best = cur;
+    return PSX_OK;
+}
+
+PSX_API psx_status psx_world_launch_config(psx_world* W, psx_launch_config* out) {
+    if (!W || !out) return fail(PSX_ERR_INVALID_ARG, "psx_world_launch_config");
+    *out = current_launch(W);
     return PSX_OK;
 }
 

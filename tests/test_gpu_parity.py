@@ -302,3 +302,53 @@ def test_launch_shapes_do_not_change_results(gpu_lib):
             assert np.array_equal(sa[k].view(np.uint32), sb[k].view(np.uint32)), (f, k)
     cfg = b.tune(frames=1)
     assert set(cfg) >= {"convex_warps", "analytic_threads", "solver_smem_kb"}
+
+
+@pytest.mark.parametrize("solver", [1, 2], ids=["cluster", "grid"])
+@pytest.mark.parametrize("kind", ["mixed", "chains"])
+def test_large_scene_on_a_cluster_or_the_grid(gpu_lib, oracle_lib, kind, solver):
+    """Scenes above the 8192-body block limit are solved by a thread-block cluster (velocities
+    in distributed shared memory) or by the whole grid; either way frames stay in lockstep
+    with the oracle."""
+    s = scenes.batch_scene(9, n_bodies=9000) if kind == "mixed" else scenes.joint_chains(n_chains=300, links=32)
+    assert s.n_dynamic > 8192
+    g = _gpu(s, launch={"large_scene_solver": solver})
+    assert g.launch_config()["large_scene_solver"] == solver
+    o = _oracle(s)
+    for f in range(4):
+        g.step(); g.synchronize()
+        ids, gf, meta = g.contacts()
+        o.set_contact_order(gpu_keys(ids, meta))
+        o.step()
+        assert o.order_error() == 0, f
+        d = rel_state_diff(g.read_bodies(), o.state())
+        assert d <= TOL, "frame %d: %g" % (f, d)
+    assert g.counts()["error"] == 0
+
+
+def _colouring(s, **kw):
+    g = _gpu(s, **kw)
+    g.step(); g.synchronize()
+    ids, _, meta = g.contacts()
+    key = np.concatenate([ids[:, 4:8], meta[:, 1:2]], axis=1)
+    order = np.lexsort(key.T[::-1])
+    return key[order], meta[order, 0], ids[order, 1:3]
+
+
+def test_colouring_is_the_same_on_a_cluster_the_grid_and_a_block(gpu_lib):
+    """The contact colouring depends only on the scene: a scene solved by a thread-block
+    cluster or by the whole grid gets the colours it gets from a single block, and no
+    colour holds two contacts of one dynamic body."""
+    s = scenes.large_mixed(n_bodies=9000, cells=256)
+    kc, cc, bc = _colouring(s, launch={"large_scene_solver": 1})
+    kg, cg, _ = _colouring(s, launch={"large_scene_solver": 2})
+    kb, cb, bb = _colouring(s, block_scene_max_dyn=1 << 30)
+    assert np.array_equal(kc, kb) and np.array_equal(kg, kb)
+    assert np.array_equal(cc, cb), "colour counts %s vs %s" % (np.bincount(cc[cc >= 0])[:16], np.bincount(cb[cb >= 0])[:16])
+    assert np.array_equal(cg, cb)
+    assert (cc >= 0).all() and cc.max() > 4
+    for c in range(cc.max() + 1):
+        sel = cc == c
+        bodies = bc[sel].ravel()
+        bodies = bodies[bodies >= 0]
+        assert len(np.unique(bodies)) == len(bodies), "colour %d" % c
