@@ -261,30 +261,49 @@ __device__ __forceinline__ bool pair_ok(const World& w, int ca, int cb) {
     return true;
 }
 
-// One thread per sorted leaf p finds its partners q > p by a left-first depth-first walk
-// of its scene's tree, so partners come out in increasing sorted position: an order that
-// depends only on the scene (its Morton codes), never on the tree's shape or the batch.
+// A warp takes 32 consecutive sorted leaves (Morton neighbours, so their bounds are
+// close) and walks their scene's tree together: a node is entered when it may hold a
+// partner of any lane, every lane reads the same node (one broadcast load), and the
+// walk stays warp-uniform.  Each lane tests only its own leaf p against the leaves q > p
+// the walk reaches.  The walk is left-first depth-first, so each lane's partners come
+// out in increasing sorted position: an order that depends only on the scene (its
+// Morton codes), never on the tree's shape, the warp's other lanes or the batch.  A
+// warp whose leaves belong to two scenes walks them one after the other.
 template <bool EMIT>
-__global__ void k_traverse(World w, FrameBuf f) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= w.n_colliders) return;
-    int ca = f.order[p];
-    int s = w.info[w.col_info[ca].x].w;
-    int cs = w.scene_col[s], n = w.scene_col[s + 1] - cs;
+__global__ void __launch_bounds__(256) k_traverse(World w, FrameBuf f) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    int ca = 0, s = -1, root = 0;
+    float4 qmin = make_float4(0.f, 0.f, 0.f, 0.f), qmax = qmin;
+    bool want = false;
+    if (p < w.n_colliders) {
+        ca = f.order[p];
+        s = w.info[w.col_info[ca].x].w;
+        int cs = w.scene_col[s], n = w.scene_col[s + 1] - cs;
+        bool active = !w.scene_active || w.scene_active[s];
+        want = n >= 2 && active && (w.col_info[ca].w & COL_ENABLE);
+        root = cs - s;   // root of this scene's tree
+        qmin = w.aabb_min[ca];
+        qmax = w.aabb_max[ca];
+    }
     int count = 0;
-    int out = EMIT ? f.leaf_off[p] : 0;
-    bool active = !w.scene_active || w.scene_active[s];
-    if (n >= 2 && active && (w.col_info[ca].w & COL_ENABLE)) {
-        float4 qmin = w.aabb_min[ca], qmax = w.aabb_max[ca];
-        int stack[64];
+    const int out = (EMIT && p < w.n_colliders) ? f.leaf_off[p] : 0;
+    unsigned pending = __ballot_sync(~0u, want);
+    while (pending) {
+        const int leader = __ffs(pending) - 1;
+        const int gs = __shfl_sync(~0u, s, leader);
+        const int groot = __shfl_sync(~0u, root, leader);
+        const bool mine = want && s == gs;
+        pending &= ~__ballot_sync(~0u, mine);
+        int stack[64];   // the same in every lane
         int sp = 0;
-        stack[sp++] = cs - s;  // root of this scene's tree
+        stack[sp++] = groot;
         while (sp) {
-            int c = stack[--sp];
+            const int c = stack[--sp];
             if (c < 0) {
-                int q = ~c;
-                if (q <= p) continue;
-                int cb = f.order[q];
+                const int q = ~c;
+                if (!mine || q <= p) continue;
+                const int cb = f.order[q];
                 if (!overlap_incl(qmin, qmax, w.aabb_min[cb], w.aabb_max[cb])) continue;
                 if (!pair_ok(w, ca, cb)) continue;
                 if (EMIT) {
@@ -296,18 +315,18 @@ __global__ void k_traverse(World w, FrameBuf f) {
                 }
                 ++count;
             } else {
-                if (f.bvh.last[c] <= p) continue;
-                if (!overlap_incl(qmin, qmax, f.bvh.bmin[c], f.bvh.bmax[c])) continue;
+                const bool go = mine && f.bvh.last[c] > p && overlap_incl(qmin, qmax, f.bvh.bmin[c], f.bvh.bmax[c]);
+                if (!__any_sync(~0u, go)) continue;
                 if (sp + 2 <= 64) {
                     stack[sp++] = f.bvh.right[c];
                     stack[sp++] = f.bvh.left[c];
-                } else {
+                } else if (lane == 0) {
                     atomicOr(w.err, ERR_STACK_CAPACITY);
                 }
             }
         }
     }
-    if (!EMIT) f.leaf_cnt[p] = count;
+    if (!EMIT && p < w.n_colliders) f.leaf_cnt[p] = count;
 }
 
 __global__ void k_pairs_check(FrameBuf f, int* err) {

@@ -153,11 +153,13 @@ __device__ inline V3 warp_epa(const WarpMink& mk, const GjkSimplex& s, V3& cp0, 
     int fi = 0;
     for (int it = 0; it < 100; ++it) {
         const int nf = P.nf;
+        const int nslots = (nf + 31) >> 5;   // face slots in use (warp-uniform)
         // distances of this lane's faces
         double dk[kFaceSlots];
         double dmin = CUDART_INF;
 #pragma unroll
         for (int j = 0; j < kFaceSlots; ++j) {
+            if (j >= nslots) break;
             int k = lane + 32 * j;
             dk[j] = CUDART_NAN;
             if (k < nf) {
@@ -176,12 +178,14 @@ __device__ inline V3 warp_epa(const WarpMink& mk, const GjkSimplex& s, V3& cp0, 
             int first = 0x7fffffff, last = -1;
 #pragma unroll
             for (int j = 0; j < kFaceSlots; ++j) {
+                if (j >= nslots) break;
                 int k = lane + 32 * j;
                 if (k < nf && (float)dk[j] == M && dk[j] < CUDART_INF && k < first) first = k;
             }
             first = __reduce_min_sync(0xffffffffu, first);
 #pragma unroll
             for (int j = 0; j < kFaceSlots; ++j) {
+                if (j >= nslots) break;
                 int k = lane + 32 * j;
                 if (k < nf && k > first && dk[j] < (double)M) last = k;
             }
@@ -197,6 +201,7 @@ __device__ inline V3 warp_epa(const WarpMink& mk, const GjkSimplex& s, V3& cp0, 
         // visibility of every current face
 #pragma unroll
         for (int j = 0; j < kFaceSlots; ++j) {
+            if (j >= nslots) break;
             int k = lane + 32 * j;
             bool vis = false;
             if (k < nf) vis = dot(wp_n(P, k), v.pos - wp_pos(P, P.i0[k])) > 0;
