@@ -154,8 +154,8 @@ typedef struct psx_world psx_world;
 /* Launch shapes of the kernels whose best shape depends on the workload.  None of them
  * changes a result; 0 in a field keeps the default.  psx_world_tune picks them. */
 typedef struct psx_launch_config {
-    int32_t convex_warps;            /* GJK/EPA: warps (pairs) per block, 1-3 (default 3) */
-    int32_t convex_blocks_per_sm;    /* GJK/EPA: blocks per SM in the grid (default 5) */
+    int32_t convex_warps;            /* EPA: warps (pairs) per block, 1-3 (default 3) */
+    int32_t convex_blocks_per_sm;    /* EPA: blocks per SM in the grid (default 5) */
     int32_t analytic_threads;        /* sphere/capsule/box pairs: threads per block, <= 256 (default 128) */
     int32_t analytic_blocks_per_sm;  /* (default 8) */
     int32_t contacts_threads;        /* convex contact generation: threads per block, <= 256 (default 128) */
@@ -163,6 +163,7 @@ typedef struct psx_launch_config {
     int32_t large_scene_solver;      /* scenes above the block limit: 1 one thread-block cluster each (those whose
                                       * velocities fit the cluster's shared memory), 2 the whole grid, one scene
                                       * after another (default: clusters when two or more scenes fit them) */
+    int32_t gjk_blocks_per_sm;       /* GJK (one thread per convex pair): 128-thread blocks per SM, 1-16 (default 8) */
 } psx_launch_config;
 
 typedef struct psx_world_opts {

@@ -36,8 +36,8 @@ struct FrameBuf {
     int* n_pairs;         // device scalar
     // narrowphase
     int* pair_cat;        // 0 analytic, 1 convex mesh, 2 triangle mesh
-    int* cat_count;       // [3]
-    int* cat_list;        // [3 * pair_cap]
+    int* cat_count;       // [4]: analytic, convex, triangle-mesh pairs; convex pairs that overlap
+    int* cat_list;        // [4 * pair_cap]: the pairs of each category; overlapping convex pairs
     Manifold* man_pair;   // one slot per pair (analytic / convex categories)
     int tri_cap;          // triangle-mesh pair slots
     Manifold* man_tri;    // kTriManifolds slots per triangle-mesh pair slot
@@ -87,9 +87,10 @@ struct StreamPair {
     cudaEvent_t fork, join;
 };
 struct NarrowShape {
-    int convex_warps, convex_blocks_per_sm;
+    int convex_warps, convex_blocks_per_sm;   // EPA: warps per block, blocks per SM
     int analytic_threads, analytic_blocks_per_sm;
     int contacts_threads;
+    int gjk_blocks_per_sm;                    // GJK: 128-thread blocks per SM
 };
 int launch_narrowphase(const World& w, FrameBuf& f, const StreamPair& sp, const NarrowShape& ns, cudaStream_t s);
 int launch_contacts(const World& w, FrameBuf& f, cudaStream_t s);

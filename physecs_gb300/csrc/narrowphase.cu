@@ -98,8 +98,8 @@ __global__ void __launch_bounds__(256) k_narrow_analytic(World w, FrameBuf f) {
     }
 }
 
-// convex-mesh pairs, part 1: GJK + EPA with one warp per pair.  The EPA normal and
-// closest points (or "no contact") are staged in the pair's manifold slot.
+// convex-mesh pairs, part 1: GJK, then EPA for the pairs GJK finds overlapping.  The
+// EPA normal and closest points (or "no contact") are staged in the pair's manifold slot.
 
 __device__ __forceinline__ bool convex_pair_ordered(const World& w, int2 pr, V3& pos0, Q4& or0, GeomD& g0, V3& pos1,
                                                     Q4& or1, GeomD& g1) {
@@ -116,15 +116,17 @@ __device__ __forceinline__ bool convex_pair_ordered(const World& w, int2 pr, V3&
     return swap;
 }
 
-// WARPS pairs per block, one polytope (about 12.8 KB) each; at most 15 warps per SM share
-// the register file at 128 registers a thread
-template <int WARPS>
-__global__ void __launch_bounds__(32 * WARPS, 15 / WARPS) k_convex_gjk_epa(World w, FrameBuf f) {
-    __shared__ WarpPoly polys[WARPS];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    WarpPoly& P = polys[wid];
+// GJK with one thread per pair.  Its simplex arithmetic is f64, and the FP64 pipe costs
+// the same for a warp instruction whatever the number of lanes that use it, so 32 pairs
+// per warp instruction is where GJK is cheapest; the support searches are f32.  Most
+// pairs end here without contact (their bounds overlap, their shapes do not).  For an
+// overlapping pair the final simplex is kept in the pair's manifold slot (the f32
+// support points; each Minkowski vertex is their difference widened to f64, so it is
+// rebuilt exactly) and the pair joins the list that EPA works through.
+__global__ void __launch_bounds__(128, 4) k_convex_gjk(World w, FrameBuf f) {
     const int n = f.cat_count[1];
-    for (int t = blockIdx.x * WARPS + wid; t < n; t += gridDim.x * WARPS) {
+    const int lane = threadIdx.x & 31;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         const int p = f.cat_list[f.pair_cap + t];
         V3 pos0, pos1;
         Q4 or0, or1;
@@ -132,14 +134,63 @@ __global__ void __launch_bounds__(32 * WARPS, 15 / WARPS) k_convex_gjk_epa(World
         convex_pair_ordered(w, f.pairs[p], pos0, or0, g0, pos1, or1, g1);
         Support a, b;
         convexOrderedSupports(w, pos0, or0, g0, pos1, or1, g1, a, b);
-        WarpMink mk{a, b, lane};
         GjkSimplex s;
-        bool hit = gjkT(mk, pos1 - pos0, s);
-        V3 nrm = {0, 0, 0}, c0 = {0, 0, 0}, c1 = {0, 0, 0};
-        if (hit) nrm = warp_epa(mk, s, c0, c1, P, lane, w.err);
+        const bool hit = gjk(a, b, pos1 - pos0, s);
+        Manifold& m = f.man_pair[p];
+        if (hit) {
+            m.np = 1;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                m.p0[i] = make_float4(s.v[i].sp0.x, s.v[i].sp0.y, s.v[i].sp0.z, 0.f);
+                m.p1[i] = make_float4(s.v[i].sp1.x, s.v[i].sp1.y, s.v[i].sp1.z, 0.f);
+            }
+        } else {
+            m.np = -1;
+            m.n = make_float4(0.f, 0.f, 0.f, 0.f);
+            m.p0[0] = m.n;
+            m.p1[0] = m.n;
+        }
+        const unsigned act = __activemask();
+        const unsigned hm = __ballot_sync(act, hit);
+        int first = 0;
+        if (hm) {
+            const int leader = __ffs(hm) - 1;
+            if (lane == leader) first = atomicAdd(&f.cat_count[3], __popc(hm));
+            first = __shfl_sync(act, first, leader);
+            if (hit) f.cat_list[3 * (size_t)f.pair_cap + first + __popc(hm & ((1u << lane) - 1u))] = t;
+        }
+    }
+}
+
+// EPA with one warp per overlapping pair, from the simplex GJK kept; WARPS pairs per
+// block, one polytope (about 12.8 KB) each; at most 15 warps per SM share the register
+// file at 128 registers a thread.
+template <int WARPS>
+__global__ void __launch_bounds__(32 * WARPS, 15 / WARPS) k_convex_epa(World w, FrameBuf f) {
+    __shared__ WarpPoly polys[WARPS];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    WarpPoly& P = polys[wid];
+    const int n = f.cat_count[3];
+    for (int h = blockIdx.x * WARPS + wid; h < n; h += gridDim.x * WARPS) {
+        const int t = f.cat_list[3 * (size_t)f.pair_cap + h];
+        const int p = f.cat_list[f.pair_cap + t];
+        V3 pos0, pos1;
+        Q4 or0, or1;
+        GeomD g0, g1;
+        convex_pair_ordered(w, f.pairs[p], pos0, or0, g0, pos1, or1, g1);
+        Support a, b;
+        convexOrderedSupports(w, pos0, or0, g0, pos1, or1, g1, a, b);
+        Manifold& m = f.man_pair[p];
+        GjkSimplex s;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const V3 sa = ld3(m.p0[i]), sb = ld3(m.p1[i]);
+            s.v[i] = {d3(sa - sb), sa, sb};
+        }
+        WarpMink mk{a, b, lane};
+        V3 c0, c1;
+        const V3 nrm = warp_epa(mk, s, c0, c1, P, lane, w.err);   // ends with a warp barrier
         if (lane == 0) {
-            Manifold& m = f.man_pair[p];
-            m.np = hit ? 1 : -1;
             m.n = st4(nrm);
             m.p0[0] = st4(c0);
             m.p1[0] = st4(c1);
@@ -205,32 +256,33 @@ __global__ void __launch_bounds__(64) k_narrow_tri(World w, FrameBuf f) {
 }
 
 template <int WARPS>
-static void launch_convex(const World& w, FrameBuf& f, int blocks_per_sm, cudaStream_t s) {
+static void launch_convex_epa(const World& w, FrameBuf& f, int blocks_per_sm, cudaStream_t s) {
     static bool carveout_set = false;
     if (!carveout_set) {
-        cudaFuncSetAttribute(k_convex_gjk_epa<WARPS>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        cudaFuncSetAttribute(k_convex_epa<WARPS>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         carveout_set = true;
     }
-    k_convex_gjk_epa<WARPS><<<152 * blocks_per_sm, 32 * WARPS, 0, s>>>(w, f);
+    k_convex_epa<WARPS><<<152 * blocks_per_sm, 32 * WARPS, 0, s>>>(w, f);
 }
 
 // The convex kernels (bound by the FP64 pipe) run on the aux stream beside the analytic
 // and triangle-mesh kernels (FP32, latency-bound); the categories write disjoint slots.
 int launch_narrowphase(const World& w, FrameBuf& f, const StreamPair& sp, const NarrowShape& ns, cudaStream_t s) {
-    cudaMemsetAsync(f.cat_count, 0, 3 * sizeof(int), s);
+    cudaMemsetAsync(f.cat_count, 0, 4 * sizeof(int), s);
     k_classify<<<1216, 256, 0, s>>>(w, f);
     cudaEventRecord(sp.fork, s);
     cudaStreamWaitEvent(sp.aux, sp.fork, 0);
-    if (ns.convex_warps == 1) launch_convex<1>(w, f, ns.convex_blocks_per_sm, sp.aux);
-    else if (ns.convex_warps == 2) launch_convex<2>(w, f, ns.convex_blocks_per_sm, sp.aux);
-    else launch_convex<3>(w, f, ns.convex_blocks_per_sm, sp.aux);
+    k_convex_gjk<<<152 * ns.gjk_blocks_per_sm, 128, 0, sp.aux>>>(w, f);
+    if (ns.convex_warps == 1) launch_convex_epa<1>(w, f, ns.convex_blocks_per_sm, sp.aux);
+    else if (ns.convex_warps == 2) launch_convex_epa<2>(w, f, ns.convex_blocks_per_sm, sp.aux);
+    else launch_convex_epa<3>(w, f, ns.convex_blocks_per_sm, sp.aux);
     k_convex_contacts<<<1216 * 128 / ns.contacts_threads, ns.contacts_threads, 0, sp.aux>>>(w, f);
     cudaEventRecord(sp.join, sp.aux);
     k_narrow_analytic<<<152 * ns.analytic_blocks_per_sm, ns.analytic_threads, 0, s>>>(w, f);
     k_narrow_tri<<<1216, 64, 0, s>>>(w, f);
     cudaStreamWaitEvent(s, sp.join, 0);
     scan_exclusive_dev(f.pair_nman, f.pair_moff, f.n_pairs, f.pair_cap, f.n_man, f.scan_scratch, s);
-    return 2 + 4 + 3;
+    return 2 + 5 + 3;
 }
 
 }  // namespace psx

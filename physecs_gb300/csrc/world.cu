@@ -422,8 +422,8 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
     PSX_TRY(W->alloc(f.pairs, f.pair_cap));
     PSX_TRY(W->alloc(f.n_pairs, 1));
     PSX_TRY(W->alloc(f.pair_cat, f.pair_cap));
-    PSX_TRY(W->alloc(f.cat_count, 3));
-    PSX_TRY(W->alloc(f.cat_list, 3 * (size_t)f.pair_cap));
+    PSX_TRY(W->alloc(f.cat_count, 4));
+    PSX_TRY(W->alloc(f.cat_list, 4 * (size_t)f.pair_cap));
     PSX_TRY(W->alloc(f.man_pair, f.pair_cap));
     PSX_TRY(W->alloc(f.man_tri, (size_t)f.tri_cap * kTriManifolds));
     PSX_TRY(W->alloc(f.pair_tslot, f.pair_cap));
@@ -551,10 +551,11 @@ psx_status psx::rt::apply_launch(psx_world* W, const psx_launch_config& c) {
     if (c.analytic_threads) n.analytic_threads = c.analytic_threads;
     if (c.analytic_blocks_per_sm) n.analytic_blocks_per_sm = c.analytic_blocks_per_sm;
     if (c.contacts_threads) n.contacts_threads = c.contacts_threads;
+    if (c.gjk_blocks_per_sm) n.gjk_blocks_per_sm = c.gjk_blocks_per_sm;
     auto threads_ok = [](int t) { return t == 32 || t == 64 || t == 128 || t == 256; };
     if (n.convex_warps < 1 || n.convex_warps > 3 || n.convex_blocks_per_sm < 1 || n.convex_blocks_per_sm > 32 ||
         !threads_ok(n.analytic_threads) || n.analytic_blocks_per_sm < 1 || n.analytic_blocks_per_sm > 64 ||
-        !threads_ok(n.contacts_threads))
+        !threads_ok(n.contacts_threads) || n.gjk_blocks_per_sm < 1 || n.gjk_blocks_per_sm > 16)
         return fail(PSX_ERR_INVALID_ARG, "launch config out of range");
     int smem = W->solver_smem;
     if (c.solver_smem_kb) {
@@ -606,6 +607,7 @@ psx_launch_config psx::rt::current_launch(const psx_world* W) {
     c.analytic_threads = W->narrow.analytic_threads;
     c.analytic_blocks_per_sm = W->narrow.analytic_blocks_per_sm;
     c.contacts_threads = W->narrow.contacts_threads;
+    c.gjk_blocks_per_sm = W->narrow.gjk_blocks_per_sm;
     c.solver_smem_kb = W->solver_smem / 1024;
     c.large_scene_solver = W->large_mode;
     return c;
@@ -762,7 +764,16 @@ PSX_API psx_status psx_world_tune(psx_world* W, int32_t frames, psx_launch_confi
     psx_launch_config cur = current_launch(W);
     struct Knob { int stage; std::vector<psx_launch_config> cands; };
     std::vector<Knob> knobs;
-    {   // GJK/EPA: warps per block x blocks per SM (at most 15 warps per SM)
+    {   // GJK: 128-thread blocks per SM
+        Knob k{1, {}};
+        for (int b : {4, 8, 12, 16}) {
+            psx_launch_config c{};
+            c.gjk_blocks_per_sm = b;
+            k.cands.push_back(c);
+        }
+        knobs.push_back(k);
+    }
+    {   // EPA: warps per block x blocks per SM (at most 15 warps per SM)
         Knob k{1, {}};
         for (int wv : {1, 2, 3})
             for (int b : {3, 5, 7, 10, 15}) {
