@@ -971,7 +971,22 @@ __device__ void solve_scene(const World& w, FrameBuf& f, int s, const S& sy, flo
     int npts = sy.point_offsets(f, ms, ncl);   // first point of each contact -> f.pt_off[ms + k]
     const int vel_f4 = (6 * nd + 3) / 4;
     const bool vel_smem = !S::kCluster && vel_f4 <= smem_f4;
-    const bool rec_smem = vel_smem && vel_f4 + kHdrF4 * ncl + kPtF4 * npts <= smem_f4;
+    // contact headers in shared memory when they fit beside the velocities; point records
+    // fill what is left, in colour order, up to the first contact whose points no longer
+    // fit (contacts ks.. keep theirs in the world's buffer), so a scene slightly too big
+    // for shared memory loses only its tail, not every record
+    const bool hdr_smem = vel_smem && vel_f4 + kHdrF4 * ncl <= smem_f4;
+    const int pbase_f4 = vel_f4 + (hdr_smem ? kHdrF4 * ncl : 0);
+    const int pcap = vel_smem ? max(0, (smem_f4 - pbase_f4) / kPtF4) : 0;
+    int ks = 0;
+    if (vel_smem) {
+        int fit = 0;
+        for (int k = tid; k < ncl; k += nth) {
+            const int end = k + 1 < ncl ? f.pt_off[ms + k + 1] : npts;
+            if (end <= pcap) fit = k + 1;
+        }
+        ks = sy.max_int(fit);
+    }
     VelRef vr = vel_smem ? VelRef{(float*)smem, nullptr, nullptr, nullptr, ds, nd, 0}
                          : VelRef{nullptr, nullptr, w.vt_v, w.vt_w, 0, 0, 0};
     if constexpr (S::kCluster) {
@@ -980,20 +995,22 @@ __device__ void solve_scene(const World& w, FrameBuf& f, int s, const S& sy, flo
         if (6 * per <= 4 * smem_f4) vr = VelRef{nullptr, sy.bases, nullptr, nullptr, ds, per, sy.lg};
         else vr = VelRef{nullptr, nullptr, w.vt_v, w.vt_w, 0, 0, 0};
     }
-    SHdr* H = rec_smem ? (SHdr*)(smem + vel_f4) : f.s_hdr + ms;
-    SPt* P = rec_smem ? (SPt*)(smem + vel_f4 + kHdrF4 * ncl) : f.s_pts + 4 * (size_t)ms;
+    SHdr* H = hdr_smem ? (SHdr*)(smem + vel_f4) : f.s_hdr + ms;
+    SPt* const Ps = (SPt*)(smem + pbase_f4);
+    SPt* const Pg = f.s_pts + 4 * (size_t)ms;
+    auto PK = [&](int k) -> SPt* { return (k < ks ? Ps : Pg) + H[k].i.w; };
     for (int k = tid; k < ncl; k += nth) H[k].i.w = f.pt_off[ms + k];
     sy.sync();
     int js0 = w.scene_jsteps[s], js1 = w.scene_jsteps[s + 1];
     int jb = w.scene_joint[s], je = w.scene_joint[s + 1];
     float h = dt / substeps;
     for (int sub = 0; sub < substeps; ++sub) {
-        for (int k = tid; k < ncl; k += nth) contact_update(w, f.contacts[f.corder[ms + k]], H[k], P + H[k].i.w);
+        for (int k = tid; k < ncl; k += nth) contact_update(w, f.contacts[f.corder[ms + k]], H[k], PK(k));
         for (int j = jb + tid; j < je; j += nth) make_joint_rows(w, j);
         sy.sync();
         for (int d = ds + tid; d < de; d += nth) integrate_velocity(w, d, h, g, vr);
         sy.sync();
-        for (int k = tid; k < ncl; k += nth) contact_presolve(w, H[k], P + H[k].i.w, h);
+        for (int k = tid; k < ncl; k += nth) contact_presolve(w, H[k], PK(k), h);
         for (int st = js0; st < js1; ++st) {
             for (int k = w.jstep_start[st] + tid; k < w.jstep_start[st + 1]; k += nth) joint_presolve(w, w.jsched[k]);
             sy.sync();
@@ -1003,9 +1020,9 @@ __device__ void solve_scene(const World& w, FrameBuf& f, int s, const S& sy, flo
             for (int cl = 0; cl < ncol; ++cl) {
                 if (serial_last && cl == ncol - 1) {
                     if (tid == 0)
-                        for (int k = colstart[cl]; k < colstart[cl + 1]; ++k) contact_solve(H[k], P + H[k].i.w, true, vr);
+                        for (int k = colstart[cl]; k < colstart[cl + 1]; ++k) contact_solve(H[k], PK(k), true, vr);
                 } else {
-                    for (int k = colstart[cl] + tid; k < colstart[cl + 1]; k += nth) contact_solve(H[k], P + H[k].i.w, true, vr);
+                    for (int k = colstart[cl] + tid; k < colstart[cl + 1]; k += nth) contact_solve(H[k], PK(k), true, vr);
                 }
                 sy.sync();
             }
@@ -1020,10 +1037,10 @@ __device__ void solve_scene(const World& w, FrameBuf& f, int s, const S& sy, flo
             if (serial_last && cl == ncol - 1) {
                 if (tid == 0)
                     for (int k = colstart[cl]; k < colstart[cl + 1]; ++k)
-                        if (!(H[k].i.z >> 8)) contact_solve(H[k], P + H[k].i.w, false, vr);
+                        if (!(H[k].i.z >> 8)) contact_solve(H[k], PK(k), false, vr);
             } else {
                 for (int k = colstart[cl] + tid; k < colstart[cl + 1]; k += nth)
-                    if (!(H[k].i.z >> 8)) contact_solve(H[k], P + H[k].i.w, false, vr);
+                    if (!(H[k].i.z >> 8)) contact_solve(H[k], PK(k), false, vr);
             }
             sy.sync();
         }
@@ -1038,7 +1055,7 @@ __device__ void solve_scene(const World& w, FrameBuf& f, int s, const S& sy, flo
     // accumulated impulses back into the frame's contacts (inspection only)
     for (int k = tid; k < ncl; k += nth) {
         Contact& c = f.contacts[f.corder[ms + k]];
-        const SPt* q = P + H[k].i.w;
+        const SPt* q = PK(k);
         for (int i = 0; i < c.np; ++i) { c.p[i].r0xn.w = q[i].a.w; c.p[i].r1xn.w = q[i].e.w; }
     }
 }
