@@ -154,16 +154,16 @@ typedef struct psx_world psx_world;
 /* Launch shapes of the kernels whose best shape depends on the workload.  None of them
  * changes a result; 0 in a field keeps the default.  psx_world_tune picks them. */
 typedef struct psx_launch_config {
-    int32_t convex_warps;            /* EPA: warps (pairs) per block, 1-3 (default 3) */
-    int32_t convex_blocks_per_sm;    /* EPA: blocks per SM in the grid (default 5) */
-    int32_t analytic_threads;        /* sphere/capsule/box pairs: threads per block, <= 256 (default 128) */
-    int32_t analytic_blocks_per_sm;  /* (default 8) */
-    int32_t contacts_threads;        /* convex contact generation: threads per block, <= 256 (default 128) */
+    int32_t convex_warps;            /* EPA: warps (pairs) per block, 1-3 (default 1) */
+    int32_t convex_blocks_per_sm;    /* EPA: blocks per SM in the grid (default 15) */
+    int32_t analytic_threads;        /* sphere/capsule/box pairs: threads per block, <= 256 (default 64) */
+    int32_t analytic_blocks_per_sm;  /* (default 16) */
+    int32_t contacts_threads;        /* convex contact generation: threads per block, <= 256 (default 64) */
     int32_t solver_smem_kb;          /* shared memory per 256-thread solver block in KB (default: by scene count) */
     int32_t large_scene_solver;      /* scenes above the block limit: 1 one thread-block cluster each (those whose
                                       * velocities fit the cluster's shared memory), 2 the whole grid, one scene
                                       * after another (default: clusters when two or more scenes fit them) */
-    int32_t gjk_blocks_per_sm;       /* GJK (one thread per convex pair): 128-thread blocks per SM, 1-16 (default 8) */
+    int32_t gjk_blocks_per_sm;       /* GJK (one thread per convex pair): 128-thread blocks per SM, 1-16 (default 16) */
 } psx_launch_config;
 
 typedef struct psx_world_opts {
@@ -263,6 +263,8 @@ typedef struct psx_server_opts {
     int32_t manifolds_per_collider;
     int32_t device;
     int32_t eager;                    /* 1: launch every tick's kernels one by one instead of replaying a CUDA graph */
+    int32_t profile;                  /* 1: time each tick's stages with CUDA events (ticks then run eagerly);
+                                       * psx_server_tick_stages reads them */
 } psx_server_opts;
 
 PSX_API psx_status psx_server_create(const psx_server_opts* opts, psx_server** out);
@@ -291,6 +293,10 @@ PSX_API psx_status psx_server_stats(psx_server* s, int64_t* out);
 /* The world that holds the slots (slot i is scene i), for the inspection entry points
  * (psx_world_counts, psx_world_get_pairs, psx_world_get_contacts).  Owned by the server. */
 PSX_API psx_world* psx_server_world(psx_server* s);
+/* With opts.profile set: the last finished tick's stage times in ms, out[6] = {staged
+ * admissions (uploads and creation bounds), broadphase, narrowphase, contact and joint
+ * rows, solver, end-of-frame bounds}. */
+PSX_API psx_status psx_server_tick_stages(psx_server* s, float* out);
 
 /* ---- single-scene spelling of the same entry points (physecs::Scene) ---- */
 typedef psx_world psx_scene;

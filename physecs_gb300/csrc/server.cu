@@ -129,6 +129,8 @@ struct psx_server {
     long long ticks_begun = 0;
     bool in_flight = false;
     cudaEvent_t tick_done = nullptr;
+    bool profile = false;            // stage events around each tick (ticks run eagerly)
+    cudaEvent_t prof[7] = {};        // tick start, then the frame's six stage events
     int* pin_active = nullptr;       // pinned mirror of h_active for the flag copy
     int* pin_err = nullptr;          // device error word of the last tick
     // reads of finished requests run on their own stream, beside the next tick
@@ -143,6 +145,7 @@ struct psx_server {
             if (st.copied) cudaEventDestroy(st.copied);
         }
         if (tick_done) cudaEventDestroy(tick_done);
+        for (cudaEvent_t e : prof) if (e) cudaEventDestroy(e);
         if (pin_active) cudaFreeHost(pin_active);
         if (pin_err) cudaFreeHost(pin_err);
         if (read_pin) cudaFreeHost(read_pin);
@@ -200,7 +203,7 @@ PSX_API psx_status psx_server_create(const psx_server_opts* o, psx_server** out)
     wo.pairs_per_collider = o->pairs_per_collider;
     wo.manifolds_per_collider = o->manifolds_per_collider;
     wo.block_scene_max_dyn = 1 << 30;
-    wo.use_graph = o->eager ? 0 : 1;   // a tick is the same fixed kernel sequence every time
+    wo.use_graph = (o->eager || o->profile) ? 0 : 1;   // a tick is the same fixed kernel sequence every time
     wo.device = o->device;
     psx_world* W = nullptr;
     psx_status st = psx_world_create(descs.data(), n_slots, &wo, &W);
@@ -226,6 +229,9 @@ PSX_API psx_status psx_server_create(const psx_server_opts* o, psx_server** out)
         return fail(PSX_ERR_OUT_OF_MEMORY, "server host staging");
     }
     *S->pin_err = 0;
+    S->profile = o->profile != 0;
+    for (int i = 0; S->profile && i < 7; ++i)
+        if (cudaEventCreate(&S->prof[i]) != cudaSuccess) { delete S; return fail(PSX_ERR_CUDA, "server profile events"); }
     PSX_CUDA(cudaDeviceSynchronize());
     *out = S;
     return PSX_OK;
@@ -370,6 +376,7 @@ PSX_API psx_status psx_server_tick_begin(psx_server* S) {
     PSX_CUDA(cudaSetDevice(W->device));
     cudaStream_t st = W->stream;
     Stage& stg = S->stage[S->cur];
+    if (S->profile) PSX_CUDA(cudaEventRecord(S->prof[0], st));
     if (!stg.ups.empty()) {
         for (const Upload& u : stg.ups)
             PSX_CUDA(cudaMemcpyAsync(u.dst, stg.pin + u.src, u.bytes, cudaMemcpyHostToDevice, st));
@@ -387,7 +394,12 @@ PSX_API psx_status psx_server_tick_begin(psx_server* S) {
         S->active_dirty = false;
     }
     ++S->ticks_begun;
-    PSX_TRY(run_frame(W));
+    if (S->profile) {
+        W->frame_kernels = queue_frame(W, S->prof + 1);
+        ++W->frames_run;
+    } else {
+        PSX_TRY(run_frame(W));
+    }
     PSX_CUDA(cudaMemsetAsync(S->d_fresh, 0, sizeof(int) * S->h_active.size(), st));
     PSX_CUDA(cudaMemcpyAsync(S->pin_err, W->w.err, sizeof(int), cudaMemcpyDeviceToHost, st));
     PSX_CUDA(cudaEventRecord(S->tick_done, st));
@@ -477,6 +489,15 @@ PSX_API psx_status psx_server_release(psx_server* S, int32_t slot) {
 }
 
 PSX_API psx_world* psx_server_world(psx_server* S) { return S ? S->W : nullptr; }
+
+PSX_API psx_status psx_server_tick_stages(psx_server* S, float* out) {
+    if (!S || !out) return fail(PSX_ERR_INVALID_ARG, "psx_server_tick_stages");
+    if (!S->profile) return fail(PSX_ERR_INVALID_ARG, "psx_server_tick_stages: the server was created without profile");
+    if (S->in_flight || S->ticks_begun == 0) return fail(PSX_ERR_INVALID_ARG, "psx_server_tick_stages: no finished tick");
+    PSX_CUDA(cudaSetDevice(S->W->device));
+    for (int i = 0; i < 6; ++i) PSX_CUDA(cudaEventElapsedTime(&out[i], S->prof[i], S->prof[i + 1]));
+    return PSX_OK;
+}
 
 PSX_API psx_status psx_server_stats(psx_server* S, int64_t* out) {
     if (!S || !out) return fail(PSX_ERR_INVALID_ARG, "psx_server_stats");

@@ -144,3 +144,29 @@ def test_pipelined_ticks_admit_while_a_frame_runs(gpu_lib):
     assert not live
     for i, r in enumerate(reqs):
         _same(results[i], _alone(r, frames[i]))
+
+
+def test_profiled_ticks_report_stages_and_keep_results(gpu_lib):
+    """A server made with profile=True times each tick's stages with CUDA events; its
+    results are those of the graph-replaying server."""
+    from physecs_gb300.api import Server
+    pool, ps = _pool()
+    reqs = _requests(pool, [41, 42], [200, 700])
+    frames = 5
+    out = []
+    for profile in (False, True):
+        srv = Server(CLASSES, mesh_pool=ps, profile=profile)
+        slots = [srv.admit(s, frames) for s in reqs]
+        stages = []
+        for _ in range(frames):
+            srv.tick()
+            if profile:
+                stages.append(srv.tick_stages())
+        out.append([srv.read(sl) for sl in slots])
+        srv.close()
+    for a, b in zip(*out):
+        _same(a, b)
+    st = np.array(stages)
+    assert st.shape == (frames, 6) and (st >= 0).all()
+    assert (st[:, 1:5].sum(axis=1) > 0).all()
+    assert st[0, 0] > 0   # the first tick uploads the admitted requests
