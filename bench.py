@@ -235,6 +235,7 @@ def cpu_kind():
 
 # ---------------------------------------------------------------- serving
 
+SERVE_HBM_BUDGET = 120 * 10 ** 9   # device bytes the serving slots may hold (requests stay resident)
 SERVE_CLASSES = [(17, 96), (33, 96), (65, 96), (129, 96), (257, 96), (513, 96), (1025, 64), (2049, 48), (4097, 32),
                  (8193, 24)]
 # requests of at most 1000 bodies (the latency target's class)
@@ -353,7 +354,7 @@ def run_serving(args, rank, world, local):
     reqs, pool_scene = serving_requests(384, rank, n_max=args.serve_max_bodies)
     from physecs_gb300.desc import make_desc
     descs = [make_desc(s) for s, _ in reqs]          # the clients' packed requests
-    srv = Server(classes, mesh_pool=pool_scene, device=local if world > 1 else 0)
+    srv = Server(classes, mesh_pool=pool_scene, device=local if world > 1 else 0, hbm_budget=SERVE_HBM_BUDGET)
     # saturated throughput: a permanent backlog keeps every fitting slot busy
     backlog = 2 * sum(c[1] for c in classes)   # enough waiting requests to keep every class busy
     _serve(srv, reqs, None, 3.0, backlog, descs)
@@ -373,7 +374,8 @@ def run_serving(args, rank, world, local):
         "config": {"workload": "serving: Poisson request stream at %.0f%% of saturated throughput, N log-uniform in "
                                "[8,%d] bodies, K uniform in [1,120] frames, dt=1/60, 4x8" % (100 * args.serve_load,
                                                                                              args.serve_max_bodies),
-                   "slot_classes": classes, "seconds": args.serve_seconds},
+                   "slot_classes": classes, "seconds": args.serve_seconds,
+                   "hbm_budget_gb": SERVE_HBM_BUDGET / 1e9, "device_gb": srv.device_bytes() / 1e9},
         "p50_ms": float(np.percentile(fl, 50)), "p99_ms": float(np.percentile(fl, 99)),
         "request_p50_ms": float(np.percentile(rl, 50)) if len(rl) else None,
         "request_p99_ms": float(np.percentile(rl, 99)) if len(rl) else None,

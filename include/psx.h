@@ -265,6 +265,9 @@ typedef struct psx_server_opts {
     int32_t eager;                    /* 1: launch every tick's kernels one by one instead of replaying a CUDA graph */
     int32_t profile;                  /* 1: time each tick's stages with CUDA events (ticks then run eagerly);
                                        * psx_server_tick_stages reads them */
+    int64_t hbm_budget;               /* device bytes the server may hold, 0: no cap.  Every slot keeps its
+                                       * request's state resident, so the budget caps the slots: creation
+                                       * fails with PSX_ERR_OUT_OF_MEMORY when they need more */
 } psx_server_opts;
 
 PSX_API psx_status psx_server_create(const psx_server_opts* opts, psx_server** out);
@@ -297,6 +300,8 @@ PSX_API psx_world* psx_server_world(psx_server* s);
  * admissions (uploads and creation bounds), broadphase, narrowphase, contact and joint
  * rows, solver, end-of-frame bounds}. */
 PSX_API psx_status psx_server_tick_stages(psx_server* s, float* out);
+/* Device memory the server holds (its slots' world and flags), in bytes. */
+PSX_API psx_status psx_server_device_bytes(psx_server* s, int64_t* out);
 
 /* ---- single-scene spelling of the same entry points (physecs::Scene) ---- */
 typedef psx_world psx_scene;

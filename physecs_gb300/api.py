@@ -26,7 +26,7 @@ EXPORTS = ["psx_world_create", "psx_world_destroy", "psx_world_step", "psx_world
            "psx_scene_create", "psx_scene_destroy", "psx_scene_simulate", "psx_world_read_bodies_noalloc",
            "psx_server_create", "psx_server_destroy", "psx_server_admit", "psx_server_tick", "psx_server_read",
            "psx_server_release", "psx_server_stats", "psx_server_tick_begin", "psx_server_tick_end", "psx_server_world",
-           "psx_server_tick_stages",
+           "psx_server_tick_stages", "psx_server_device_bytes",
            "psx_world_tune", "psx_world_launch_config"]
 
 _lib = None
@@ -54,7 +54,8 @@ class PsxWorldOpts(C.Structure):
 class PsxServerOpts(C.Structure):
     _fields_ = [("n_classes", C.c_int32), ("class_bodies", C.c_void_p), ("class_slots", C.c_void_p),
                 ("mesh_pool", C.c_void_p), ("pairs_per_collider", C.c_int32), ("manifolds_per_collider", C.c_int32),
-                ("device", C.c_int32), ("eager", C.c_int32), ("profile", C.c_int32)]
+                ("device", C.c_int32), ("eager", C.c_int32), ("profile", C.c_int32),
+                ("hbm_budget", C.c_int64)]
 
 
 def load():
@@ -235,7 +236,7 @@ class Server:
     h = None
 
     def __init__(self, classes, mesh_pool=None, device=0, pairs_per_collider=0, manifolds_per_collider=0, eager=False,
-                 profile=False):
+                 profile=False, hbm_budget=0):
         lib = load()
         self._cb = np.ascontiguousarray([c[0] for c in classes], np.int32)
         self._cs = np.ascontiguousarray([c[1] for c in classes], np.int32)
@@ -244,7 +245,7 @@ class Server:
         opts = PsxServerOpts(len(classes), self._cb.ctypes.data, self._cs.ctypes.data,
                              C.cast(C.pointer(self._pool), C.c_void_p) if self._pool is not None else None,
                              pairs_per_collider, manifolds_per_collider, device, 1 if eager else 0,
-                             1 if profile else 0)
+                             1 if profile else 0, int(hbm_budget))
         h = C.c_void_p()
         _check(lib.psx_server_create(C.byref(opts), C.byref(h)))
         self.h = h
@@ -314,6 +315,12 @@ class Server:
         cls = self._cls.pop(slot, None)
         if cls is not None:
             self._free[cls] += 1
+
+    def device_bytes(self):
+        """psx_server_device_bytes: device memory the server holds."""
+        out = np.zeros(1, np.int64)
+        _check(load().psx_server_device_bytes(self.h, _p(out)))
+        return int(out[0])
 
     def tick_stages(self):
         """psx_server_tick_stages (servers made with profile=True): the last finished tick's

@@ -70,6 +70,7 @@ struct psx_world {
     long long launches = 0;          // kernels queued since creation
     int n_simulated = 0;             // dynamic, non-kinematic bodies
     std::vector<cudaEvent_t> events; // stage events of timed steps
+    size_t device_bytes = 0;         // device memory held in allocs
 
     template <class T>
     psx_status alloc(T*& p, size_t n) {
@@ -78,6 +79,7 @@ struct psx_world {
         cudaError_t e = cudaMalloc(&q, n * sizeof(T));
         if (e != cudaSuccess) return psx::rt::fail(PSX_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e));
         allocs.push_back(q);
+        device_bytes += n * sizeof(T);
         p = (T*)q;
         return PSX_OK;
     }

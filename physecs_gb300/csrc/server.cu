@@ -119,6 +119,7 @@ struct psx_server {
     std::vector<int> h_active;
     bool active_dirty = true;
     long long body_frames = 0;                  // simulated-body frames run so far
+    int64_t device_bytes = 0;                   // device memory of the slots' world and the flags
     // admission packing (host) and staging (pinned)
     std::vector<float4> pos, quat, vel, ang, com, invI, cpos, cquat, cpar, cmat;
     std::vector<int4> info, cinfo;
@@ -216,6 +217,14 @@ PSX_API psx_status psx_server_create(const psx_server_opts* o, psx_server** out)
     }
     cudaMemset(S->d_active, 0, sizeof(int) * n_slots);
     cudaMemset(S->d_fresh, 0, sizeof(int) * n_slots);
+    S->device_bytes = (int64_t)W->device_bytes + 2 * (int64_t)sizeof(int) * n_slots;
+    if (o->hbm_budget > 0 && S->device_bytes > o->hbm_budget) {
+        char buf[200];
+        std::snprintf(buf, sizeof buf, "psx_server_create: the slots need %lld device bytes, above the budget of %lld",
+                      (long long)S->device_bytes, (long long)o->hbm_budget);
+        delete S;
+        return fail(PSX_ERR_OUT_OF_MEMORY, buf);
+    }
     S->h_active.assign(n_slots, 0);
     W->w.scene_active = S->d_active;
     W->w.scene_fresh = S->d_fresh;
@@ -489,6 +498,12 @@ PSX_API psx_status psx_server_release(psx_server* S, int32_t slot) {
 }
 
 PSX_API psx_world* psx_server_world(psx_server* S) { return S ? S->W : nullptr; }
+
+PSX_API psx_status psx_server_device_bytes(psx_server* S, int64_t* out) {
+    if (!S || !out) return fail(PSX_ERR_INVALID_ARG, "psx_server_device_bytes");
+    *out = S->device_bytes;
+    return PSX_OK;
+}
 
 PSX_API psx_status psx_server_tick_stages(psx_server* S, float* out) {
     if (!S || !out) return fail(PSX_ERR_INVALID_ARG, "psx_server_tick_stages");

@@ -170,3 +170,23 @@ def test_profiled_ticks_report_stages_and_keep_results(gpu_lib):
     assert st.shape == (frames, 6) and (st >= 0).all()
     assert (st[:, 1:5].sum(axis=1) > 0).all()
     assert st[0, 0] > 0   # the first tick uploads the admitted requests
+
+
+def test_hbm_budget_caps_the_slots(gpu_lib):
+    """Every slot keeps its request's state resident in device memory, so the HBM budget
+    caps the slots a server may create; the server reports what it holds."""
+    from physecs_gb300.api import PsxError, Server
+    pool, pool_scene = _pool()
+    srv = Server(CLASSES, mesh_pool=pool_scene)
+    need = srv.device_bytes()
+    srv.close()
+    assert need > 0
+    with pytest.raises(PsxError, match="OUT_OF_MEMORY"):
+        Server(CLASSES, mesh_pool=pool_scene, hbm_budget=need // 2)
+    srv = Server(CLASSES, mesh_pool=pool_scene, hbm_budget=need)
+    assert srv.device_bytes() == need
+    reqs = _requests(pool, [51], [100])
+    slot = srv.admit(reqs[0], 2)
+    srv.tick(); srv.tick()
+    _same(srv.read(slot), _alone(reqs[0], 2))
+    srv.close()
