@@ -164,6 +164,8 @@ typedef struct psx_launch_config {
                                       * velocities fit the cluster's shared memory), 2 the whole grid, one scene
                                       * after another (default: clusters when two or more scenes fit them) */
     int32_t gjk_blocks_per_sm;       /* GJK (one thread per convex pair): 128-thread blocks per SM, 1-16 (default 16) */
+    int32_t epa_lanes;               /* EPA: lanes per overlapping pair, 8, 16 or 32 (default 32); below 32 a block
+                                      * is one warp holding 32 / epa_lanes pairs */
 } psx_launch_config;
 
 typedef struct psx_world_opts {

@@ -38,7 +38,7 @@ class PsxError(RuntimeError):
 
 LAUNCH_FIELDS = ["convex_warps", "convex_blocks_per_sm", "analytic_threads", "analytic_blocks_per_sm",
                  "contacts_threads", "solver_smem_kb", "large_scene_solver",
-                 "gjk_blocks_per_sm"]
+                 "gjk_blocks_per_sm", "epa_lanes"]
 
 
 class PsxLaunchConfig(C.Structure):

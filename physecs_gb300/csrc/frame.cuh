@@ -91,6 +91,7 @@ struct NarrowShape {
     int analytic_threads, analytic_blocks_per_sm;
     int contacts_threads;
     int gjk_blocks_per_sm;                    // GJK: 128-thread blocks per SM
+    int epa_lanes;                            // EPA: lanes per pair (8, 16 or 32; below 32, one warp per block)
 };
 int launch_narrowphase(const World& w, FrameBuf& f, const StreamPair& sp, const NarrowShape& ns, cudaStream_t s);
 int launch_contacts(const World& w, FrameBuf& f, cudaStream_t s);

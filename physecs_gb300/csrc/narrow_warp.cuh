@@ -1,21 +1,26 @@
-// narrow_warp.cuh — GJK + EPA with one warp per convex pair.
+// narrow_warp.cuh — EPA with a group of G lanes per convex pair (G = 8, 16 or 32).
 //
-// The arithmetic is exactly that of gjk()/epa() in narrow_convex.cuh (GJK.h /
-// EPA.h of the reference, f32 supports and an f64 simplex and polytope); only
-// the loops over vertices and faces are spread across the 32 lanes:
-//   * support of a convex mesh: each lane scans every 32nd vertex, and a warp
+// The arithmetic is exactly that of epa() in narrow_convex.cuh (EPA.h of the
+// reference, f32 supports and an f64 polytope); only the loops over vertices and
+// faces are spread across the group's lanes:
+//   * support of a convex mesh: each lane scans every G-th vertex, and a group
 //     reduction picks the same vertex as the reference's 4-lane SIMD scan
 //     (largest dot; among equal dots the lowest vertex index modulo 4, then the
 //     lowest index);
-//   * EPA closest face: each lane measures every 32nd face; the reductions
+//   * EPA closest face: each lane measures every G-th face; the reductions
 //     below reproduce the sequential scan in which the running minimum is kept
 //     as a float (EPA.h:52-60), including which face wins among faces whose
 //     distances round to the same float;
-//   * EPA visibility of the faces from the new vertex: one ballot per 32 faces;
+//   * EPA visibility of the faces from the new vertex: one ballot per G faces;
 //   * new faces on the horizon: one lane per horizon edge.
-// The horizon edge list itself is built by lane 0 in the reference's order
-// (faces from last to first, edges removed by swapping in the last edge), which
-// fixes the order of the faces and so every later tie-break.
+// The horizon edge list itself is built by the group's first lane in the
+// reference's order (faces from last to first, edges removed by swapping in the
+// last edge), which fixes the order of the faces and so every later tie-break.
+//
+// Why groups: the FP64 pipe charges a warp instruction the same whatever the
+// number of lanes it carries, and one pair keeps only a handful of lanes busy (11
+// faces on average, fewer new faces, one lane for the horizon).  With 32 / G pairs
+// per warp, each f64 instruction serves up to 32 / G pairs.
 //
 // Every support point of the polytope is a float (held as float in shared
 // memory, exactly); the Minkowski vertices, face normals and face distances are
@@ -27,7 +32,7 @@
 
 namespace psx {
 
-constexpr int kFaceSlots = (kEpaFaces + 31) / 32;   // faces per lane
+constexpr int kFaceSlots = (kEpaFaces + 31) / 32;   // 32-bit words of the face visibility bitset
 
 struct WarpPoly {
     double nx[kEpaFaces], ny[kEpaFaces], nz[kEpaFaces];
@@ -58,12 +63,29 @@ __device__ __forceinline__ void wp_set_face(WarpPoly& P, int slot, int i0, int i
     P.i0[slot] = (unsigned char)i0; P.i1[slot] = (unsigned char)i1; P.i2[slot] = (unsigned char)i2;
 }
 
-// Support of a convex mesh with the lanes splitting its vertices.
-__device__ inline V3 warp_support_convex(const Support& s, V3 dir, int lane) {
+// Lanes of one group: gl = lane within the group, gb = the group's first lane of
+// the warp, gm = the group's lanes as a warp mask.
+template <int G>
+struct Group {
+    int gl, gb;
+    unsigned gm;
+    __device__ explicit Group(int lane)
+        : gl(lane & (G - 1)), gb(lane & ~(G - 1)), gm(G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)))) {}
+    __device__ __forceinline__ void sync() const { __syncwarp(gm); }
+    // the group's bits of a ballot, lane gb first
+    __device__ __forceinline__ unsigned ballot(bool v) const {
+        unsigned b = __ballot_sync(gm, v);
+        return G == 32 ? b : (b >> gb) & ((1u << G) - 1u);
+    }
+};
+
+// Support of a convex mesh with the group's lanes splitting its vertices.
+template <int G>
+__device__ inline V3 group_support_convex(const Support& s, V3 dir, const Group<G>& g) {
     V3 d = s.scale * multiplyTranspose(s.basis, dir);
     float best = -FLT_MAX;
     int key = 0x7fffffff;   // (index & 3) << 24 | index: smaller wins among equal dots
-    for (int i = lane; i < s.nverts; i += 32) {
+    for (int i = g.gl; i < s.nverts; i += G) {
         float4 v = __ldg(&s.verts[i]);
         float dp = (v.x * d.x + v.y * d.y) + v.z * d.z;
         // a vertex that never beats -FLT_MAX leaves its class at the class's first index
@@ -73,98 +95,71 @@ __device__ inline V3 warp_support_convex(const Support& s, V3 dir, int lane) {
         if (dp > best || (dp == best && k < key)) { best = dp; key = k; }
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        float ob = __shfl_xor_sync(0xffffffffu, best, o);
-        int ok = __shfl_xor_sync(0xffffffffu, key, o);
+    for (int o = G / 2; o > 0; o >>= 1) {
+        float ob = __shfl_xor_sync(g.gm, best, o, G);
+        int ok = __shfl_xor_sync(g.gm, key, o, G);
         if (ob > best || (ob == best && ok < key)) { best = ob; key = ok; }
     }
     int mi = key & 0xffffff;
     return s.pos + mv(s.basis, s.scale * ld3(s.verts[mi]));
 }
 
-__device__ __forceinline__ V3 warp_support(const Support& s, V3 dir, int lane) {
-    if (s.kind == 3) return warp_support_convex(s, dir, lane);
-    return support(s, dir);
-}
-
-// Not inlined: GJK and EPA call it from a dozen places, and one copy of the
-// support code keeps the kernel within the instruction cache.
-__device__ __noinline__ GjkVertex warp_mink(const Support& s0, const Support& s1, V3 dir, int lane) {
-    V3 a = warp_support(s0, dir, lane);
-    V3 b = warp_support(s1, -dir, lane);
+// Not inlined: EPA calls it from two places, and one copy of the support code keeps
+// the kernel within the instruction cache.
+template <int G>
+__device__ __noinline__ GjkVertex group_mink(const Support& s0, const Support& s1, V3 dir, const Group<G> g) {
+    V3 a = s0.kind == 3 ? group_support_convex<G>(s0, dir, g) : support(s0, dir);
+    V3 b = s1.kind == 3 ? group_support_convex<G>(s1, -dir, g) : support(s1, -dir);
     return {d3(a - b), a, b};
 }
 
-// GJK.h containsOrigin with its three face tests on lanes 0-2 at once; the first face
-// (in the reference's order) whose test holds gives the new direction, as in the
-// sequential version.
-__device__ inline bool warp_contains_origin(GjkSimplex& s, D3& dir, int& fi, int lane) {
-    const int j = lane < 3 ? lane : 0;
-    const int b = j == 0 ? 0 : (j == 1 ? 2 : 1), c = j == 0 ? 1 : (j == 1 ? 0 : 2), o = 2 - j;
-    D3 n;
-    bool hit = checkFace(s.v[3].pos, s.v[b].pos, s.v[c].pos, s.v[o].pos, n);
-    unsigned m = __ballot_sync(0xffffffffu, hit && lane < 3);
-    if (!m) { fi = 0; return true; }
-    int w = __ffs(m) - 1;
-    dir = {__shfl_sync(0xffffffffu, n.x, w), __shfl_sync(0xffffffffu, n.y, w), __shfl_sync(0xffffffffu, n.z, w)};
-    fi = 2 - w;
-    return false;
-}
-
-struct WarpMink {
-    const Support& s0;
-    const Support& s1;
-    int lane;
-    __device__ GjkVertex operator()(V3 dir) const { return warp_mink(s0, s1, dir, lane); }
-    __device__ bool containsOrigin(GjkSimplex& s, D3& dir, int& fi) const { return warp_contains_origin(s, dir, fi, lane); }
-};
-
-__device__ __forceinline__ double warp_min_d(double v) {
+template <int G>
+__device__ __forceinline__ double group_min_d(double v, const Group<G>& g) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    for (int o = G / 2; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(g.gm, v, o, G));
     return v;
 }
 
-// EPA.h:10-186 for one warp.  Every lane returns the same normal and points.
-__device__ inline V3 warp_epa(const WarpMink& mk, const GjkSimplex& s, V3& cp0, V3& cp1, WarpPoly& P, int lane, int* err) {
-    if (lane == 0) {
+// EPA.h:10-186 for one group of G lanes.  Every lane of the group returns the same
+// normal and points.
+template <int G>
+__device__ inline V3 group_epa(const Support& s0, const Support& s1, const GjkSimplex& s, V3& cp0, V3& cp1, WarpPoly& P,
+                               const Group<G>& g, int* err) {
+    const int gl = g.gl;
+    if (gl == 0) {
         for (int i = 0; i < 4; ++i) wp_set_vertex(P, i, s.v[i]);
         P.nv = 4;
     }
-    __syncwarp();
+    g.sync();
     D3 n0 = cross(s.v[0].pos - s.v[1].pos, s.v[2].pos - s.v[1].pos);
     bool flip = dot(s.v[3].pos - s.v[0].pos, n0) < 0;
-    if (lane < 4) {
+    if (gl < 4) {
         // EPA.h initial tetrahedron, wound so that every normal points outwards
         int t0, t1, t2;
-        switch (lane) {
+        switch (gl) {
             case 0: t0 = 0; t1 = flip ? 1 : 2; t2 = flip ? 2 : 1; break;
             case 1: t0 = 3; t1 = flip ? 1 : 2; t2 = 0; break;
             case 2: t0 = 3; t1 = flip ? 2 : 1; t2 = flip ? 1 : 2; break;
             default: t0 = 3; t1 = 0; t2 = flip ? 2 : 1; break;
         }
-        wp_set_face(P, lane, t0, t1, t2);
+        wp_set_face(P, gl, t0, t1, t2);
     }
-    if (lane == 0) P.nf = 4;
-    __syncwarp();
+    if (gl == 0) P.nf = 4;
+    g.sync();
 
     float minDist = 0;
     D3 normal = {0, 0, 0};
     int fi = 0;
     for (int it = 0; it < 100; ++it) {
         const int nf = P.nf;
-        const int nslots = (nf + 31) >> 5;   // face slots in use (warp-uniform)
-        // distances of this lane's faces
-        double dk[kFaceSlots];
+        const int nslots = (nf + G - 1) / G;   // face slots in use (group-uniform)
+        // smallest distance of this lane's faces
         double dmin = CUDART_INF;
-#pragma unroll
-        for (int j = 0; j < kFaceSlots; ++j) {
-            if (j >= nslots) break;
-            int k = lane + 32 * j;
-            dk[j] = CUDART_NAN;
+        for (int j = 0; j < nslots; ++j) {
+            int k = gl + G * j;
             if (k < nf) {
-                dk[j] = P.fd[k];
-                if (dk[j] < dmin) dmin = dk[j];
+                double d = P.fd[k];
+                if (d < dmin) dmin = d;
             }
         }
         // Sequential rule: a face is taken when its distance is below the running
@@ -172,44 +167,45 @@ __device__ inline V3 warp_epa(const WarpMink& mk, const GjkSimplex& s, V3& cp0, 
         // at M = float(smallest distance); the first face whose distance rounds to
         // M takes it, and after that every face with distance < M takes over.
         minDist = (float)DBL_MAX;
-        double dstar = warp_min_d(dmin);
+        double dstar = group_min_d<G>(dmin, g);
         if (dstar < CUDART_INF) {
             float M = (float)dstar;
             int first = 0x7fffffff, last = -1;
-#pragma unroll
-            for (int j = 0; j < kFaceSlots; ++j) {
-                if (j >= nslots) break;
-                int k = lane + 32 * j;
-                if (k < nf && (float)dk[j] == M && dk[j] < CUDART_INF && k < first) first = k;
+            for (int j = 0; j < nslots; ++j) {
+                int k = gl + G * j;
+                if (k < nf && k < first) {
+                    double d = P.fd[k];
+                    if ((float)d == M && d < CUDART_INF) first = k;
+                }
             }
-            first = __reduce_min_sync(0xffffffffu, first);
-#pragma unroll
-            for (int j = 0; j < kFaceSlots; ++j) {
-                if (j >= nslots) break;
-                int k = lane + 32 * j;
-                if (k < nf && k > first && dk[j] < (double)M) last = k;
+            first = __reduce_min_sync(g.gm, first);
+            for (int j = 0; j < nslots; ++j) {
+                int k = gl + G * j;
+                if (k < nf && k > first && P.fd[k] < (double)M) last = k;
             }
-            last = __reduce_max_sync(0xffffffffu, last);
+            last = __reduce_max_sync(g.gm, last);
             fi = last >= 0 ? last : first;
             normal = wp_n(P, fi);
             minDist = (float)P.fd[fi];
         }
-        GjkVertex v = mk(f3(normal));
+        GjkVertex v = group_mink<G>(s0, s1, f3(normal), g);
         if (dot(v.pos, normal) - minDist < (double)0.00001f) break;
 
         // ---- insert v (EPA.h:62-99)
-        // visibility of every current face
-#pragma unroll
-        for (int j = 0; j < kFaceSlots; ++j) {
-            if (j >= nslots) break;
-            int k = lane + 32 * j;
+        // visibility of every current face, as a bitset over the face index
+        for (int j = 0; j < nslots; ++j) {
+            int k = gl + G * j;
             bool vis = false;
             if (k < nf) vis = dot(wp_n(P, k), v.pos - wp_pos(P, P.i0[k])) > 0;
-            unsigned m = __ballot_sync(0xffffffffu, vis);
-            if (lane == 0) P.vis[j] = m;
+            unsigned m = g.ballot(vis);
+            if (gl == 0) {
+                const int bit = G * j;
+                if ((bit & 31) == 0) P.vis[bit >> 5] = m;
+                else P.vis[bit >> 5] |= m << (bit & 31);
+            }
         }
-        __syncwarp();
-        if (lane == 0) {
+        g.sync();
+        if (gl == 0) {
             int ne = 0, n = nf;
             for (int k = nf - 1; k >= 0; --k) {
                 if (!((P.vis[k >> 5] >> (k & 31)) & 1u)) continue;
@@ -245,16 +241,16 @@ __device__ inline V3 warp_epa(const WarpMink& mk, const GjkSimplex& s, V3& cp0, 
             P.ne = ne;
             P.nf = n;
         }
-        __syncwarp();
+        g.sync();
         const int ne = P.ne, nbase = P.nf, vi = P.nv - 1;
-        for (int m = lane; m < ne; m += 32) {
+        for (int m = gl; m < ne; m += G) {
             int slot = nbase + m;
             if (slot < kEpaFaces) wp_set_face(P, slot, vi, P.e0[m], P.e1[m]);
             else raise_err(err, ERR_EPA_CAPACITY);
         }
-        __syncwarp();
-        if (lane == 0) P.nf = min(nbase + ne, kEpaFaces);
-        __syncwarp();
+        g.sync();
+        if (gl == 0) P.nf = min(nbase + ne, kEpaFaces);
+        g.sync();
     }
     // closest points on the closest face (EPA.h:101-143); the projection adds the
     // face distance to every normal component, as the reference does
@@ -283,7 +279,7 @@ __device__ inline V3 warp_epa(const WarpMink& mk, const GjkSimplex& s, V3& cp0, 
     D3 b2 = {(double)P.bx[f2], (double)P.by[f2], (double)P.bz[f2]};
     cp0 = f3(u * a0 + vv * a1 + ww * a2);
     cp1 = f3(u * b0 + vv * b1 + ww * b2);
-    __syncwarp();
+    g.sync();
     return f3(normal);
 }
 

@@ -162,16 +162,18 @@ __global__ void __launch_bounds__(128, 4) k_convex_gjk(World w, FrameBuf f) {
     }
 }
 
-// EPA with one warp per overlapping pair, from the simplex GJK kept; WARPS pairs per
-// block, one polytope (about 12.8 KB) each; at most 15 warps per SM share the register
-// file at 128 registers a thread.
-template <int WARPS>
-__global__ void __launch_bounds__(32 * WARPS, 15 / WARPS) k_convex_epa(World w, FrameBuf f) {
-    __shared__ WarpPoly polys[WARPS];
+// EPA for the overlapping pairs, from the simplex GJK kept: a group of G lanes per pair
+// (32 / G pairs per warp), WARPS warps per block, one polytope (about 12.8 KB of
+// dynamic shared memory) per group.
+template <int G, int WARPS>
+__global__ void __launch_bounds__(32 * WARPS) k_convex_epa(World w, FrameBuf f) {
+    extern __shared__ __align__(16) unsigned char epa_smem[];
+    constexpr int GPW = 32 / G;   // groups per warp
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    WarpPoly& P = polys[wid];
+    const Group<G> g(lane);
+    WarpPoly& P = reinterpret_cast<WarpPoly*>(epa_smem)[wid * GPW + lane / G];
     const int n = f.cat_count[3];
-    for (int h = blockIdx.x * WARPS + wid; h < n; h += gridDim.x * WARPS) {
+    for (int h = (blockIdx.x * WARPS + wid) * GPW + lane / G; h < n; h += gridDim.x * WARPS * GPW) {
         const int t = f.cat_list[3 * (size_t)f.pair_cap + h];
         const int p = f.cat_list[f.pair_cap + t];
         V3 pos0, pos1;
@@ -187,10 +189,9 @@ __global__ void __launch_bounds__(32 * WARPS, 15 / WARPS) k_convex_epa(World w, 
             const V3 sa = ld3(m.p0[i]), sb = ld3(m.p1[i]);
             s.v[i] = {d3(sa - sb), sa, sb};
         }
-        WarpMink mk{a, b, lane};
         V3 c0, c1;
-        const V3 nrm = warp_epa(mk, s, c0, c1, P, lane, w.err);   // ends with a warp barrier
-        if (lane == 0) {
+        const V3 nrm = group_epa<G>(a, b, s, c0, c1, P, g, w.err);   // ends with a group barrier
+        if (g.gl == 0) {
             m.n = st4(nrm);
             m.p0[0] = st4(c0);
             m.p1[0] = st4(c1);
@@ -255,14 +256,16 @@ __global__ void __launch_bounds__(64) k_narrow_tri(World w, FrameBuf f) {
     }
 }
 
-template <int WARPS>
+template <int G, int WARPS>
 static void launch_convex_epa(const World& w, FrameBuf& f, int blocks_per_sm, cudaStream_t s) {
-    static bool carveout_set = false;
-    if (!carveout_set) {
-        cudaFuncSetAttribute(k_convex_epa<WARPS>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-        carveout_set = true;
+    const int smem = (int)sizeof(WarpPoly) * WARPS * (32 / G);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_convex_epa<G, WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        cudaFuncSetAttribute(k_convex_epa<G, WARPS>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        attr_set = true;
     }
-    k_convex_epa<WARPS><<<152 * blocks_per_sm, 32 * WARPS, 0, s>>>(w, f);
+    k_convex_epa<G, WARPS><<<152 * blocks_per_sm, 32 * WARPS, smem, s>>>(w, f);
 }
 
 // The convex kernels (bound by the FP64 pipe) run on the aux stream beside the analytic
@@ -273,9 +276,11 @@ int launch_narrowphase(const World& w, FrameBuf& f, const StreamPair& sp, const 
     cudaEventRecord(sp.fork, s);
     cudaStreamWaitEvent(sp.aux, sp.fork, 0);
     k_convex_gjk<<<152 * ns.gjk_blocks_per_sm, 128, 0, sp.aux>>>(w, f);
-    if (ns.convex_warps == 1) launch_convex_epa<1>(w, f, ns.convex_blocks_per_sm, sp.aux);
-    else if (ns.convex_warps == 2) launch_convex_epa<2>(w, f, ns.convex_blocks_per_sm, sp.aux);
-    else launch_convex_epa<3>(w, f, ns.convex_blocks_per_sm, sp.aux);
+    if (ns.epa_lanes == 8) launch_convex_epa<8, 1>(w, f, ns.convex_blocks_per_sm, sp.aux);
+    else if (ns.epa_lanes == 16) launch_convex_epa<16, 1>(w, f, ns.convex_blocks_per_sm, sp.aux);
+    else if (ns.convex_warps == 1) launch_convex_epa<32, 1>(w, f, ns.convex_blocks_per_sm, sp.aux);
+    else if (ns.convex_warps == 2) launch_convex_epa<32, 2>(w, f, ns.convex_blocks_per_sm, sp.aux);
+    else launch_convex_epa<32, 3>(w, f, ns.convex_blocks_per_sm, sp.aux);
     k_convex_contacts<<<1216 * 128 / ns.contacts_threads, ns.contacts_threads, 0, sp.aux>>>(w, f);
     cudaEventRecord(sp.join, sp.aux);
     k_narrow_analytic<<<152 * ns.analytic_blocks_per_sm, ns.analytic_threads, 0, s>>>(w, f);

@@ -552,10 +552,12 @@ psx_status psx::rt::apply_launch(psx_world* W, const psx_launch_config& c) {
     if (c.analytic_blocks_per_sm) n.analytic_blocks_per_sm = c.analytic_blocks_per_sm;
     if (c.contacts_threads) n.contacts_threads = c.contacts_threads;
     if (c.gjk_blocks_per_sm) n.gjk_blocks_per_sm = c.gjk_blocks_per_sm;
+    if (c.epa_lanes) n.epa_lanes = c.epa_lanes;
     auto threads_ok = [](int t) { return t == 32 || t == 64 || t == 128 || t == 256; };
     if (n.convex_warps < 1 || n.convex_warps > 3 || n.convex_blocks_per_sm < 1 || n.convex_blocks_per_sm > 32 ||
         !threads_ok(n.analytic_threads) || n.analytic_blocks_per_sm < 1 || n.analytic_blocks_per_sm > 64 ||
-        !threads_ok(n.contacts_threads) || n.gjk_blocks_per_sm < 1 || n.gjk_blocks_per_sm > 16)
+        !threads_ok(n.contacts_threads) || n.gjk_blocks_per_sm < 1 || n.gjk_blocks_per_sm > 16 ||
+        (n.epa_lanes != 8 && n.epa_lanes != 16 && n.epa_lanes != 32))
         return fail(PSX_ERR_INVALID_ARG, "launch config out of range");
     int smem = W->solver_smem;
     if (c.solver_smem_kb) {
@@ -608,6 +610,7 @@ psx_launch_config psx::rt::current_launch(const psx_world* W) {
     c.analytic_blocks_per_sm = W->narrow.analytic_blocks_per_sm;
     c.contacts_threads = W->narrow.contacts_threads;
     c.gjk_blocks_per_sm = W->narrow.gjk_blocks_per_sm;
+    c.epa_lanes = W->narrow.epa_lanes;
     c.solver_smem_kb = W->solver_smem / 1024;
     c.large_scene_solver = W->large_mode;
     return c;
@@ -773,16 +776,25 @@ PSX_API psx_status psx_world_tune(psx_world* W, int32_t frames, psx_launch_confi
         }
         knobs.push_back(k);
     }
-    {   // EPA: warps per block x blocks per SM (at most 15 warps per SM)
+    {   // EPA: lanes per pair; for 32 lanes, warps per block x blocks per SM (at most 15
+        // warps per SM); for 8 or 16 lanes, one-warp blocks (4 or 2 pairs) per SM
         Knob k{1, {}};
         for (int wv : {1, 2, 3})
             for (int b : {3, 5, 7, 10, 15}) {
                 if (wv * b > 15) continue;
                 psx_launch_config c{};
+                c.epa_lanes = 32;
                 c.convex_warps = wv;
                 c.convex_blocks_per_sm = b;
                 k.cands.push_back(c);
             }
+        for (int lanes : {8, 16}) {
+            psx_launch_config c{};
+            c.epa_lanes = lanes;
+            c.convex_warps = 1;
+            c.convex_blocks_per_sm = 64 / lanes;   // as many blocks as shared memory lets reside
+            k.cands.push_back(c);
+        }
         knobs.push_back(k);
     }
     {   // analytic pairs

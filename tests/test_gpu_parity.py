@@ -292,14 +292,22 @@ def test_launch_shapes_do_not_change_results(gpu_lib):
     """Any launch configuration the tuner may pick gives the same frames bit for bit."""
     ss = [scenes.batch_scene(80 + i, n_bodies=n) for i, n in enumerate([60, 1300, 200, 25])]
     a = _gpu(ss)
-    b = _gpu(ss, launch=dict(convex_warps=1, convex_blocks_per_sm=12, analytic_threads=64, analytic_blocks_per_sm=4,
-                             contacts_threads=256, solver_smem_kb=48))
+    others = [_gpu(ss, launch=dict(convex_warps=3, convex_blocks_per_sm=5, analytic_threads=128, analytic_blocks_per_sm=4,
+                                   contacts_threads=256, solver_smem_kb=100, gjk_blocks_per_sm=4, epa_lanes=32)),
+              _gpu(ss, launch=dict(epa_lanes=16, convex_warps=1, convex_blocks_per_sm=4)),
+              _gpu(ss, launch=dict(epa_lanes=8, convex_warps=1, convex_blocks_per_sm=2))]
+    assert [o.launch_config()["epa_lanes"] for o in others] == [32, 16, 8]
     for f in range(8):
-        a.step(); b.step()
-        a.synchronize(); b.synchronize()
-        sa, sb = a.read_bodies(), b.read_bodies()
-        for k in sa:
-            assert np.array_equal(sa[k].view(np.uint32), sb[k].view(np.uint32)), (f, k)
+        a.step()
+        a.synchronize()
+        sa = a.read_bodies()
+        for b in others:
+            b.step()
+            b.synchronize()
+            sb = b.read_bodies()
+            for k in sa:
+                assert np.array_equal(sa[k].view(np.uint32), sb[k].view(np.uint32)), (f, k, b.launch_config())
+    b = others[0]
     cfg = b.tune(frames=1)
     assert set(cfg) >= {"convex_warps", "analytic_threads", "solver_smem_kb"}
 
