@@ -36,8 +36,9 @@ struct FrameBuf {
     int* n_pairs;         // device scalar
     // narrowphase
     int* pair_cat;        // 0 analytic, 1 convex mesh, 2 triangle mesh
-    int* cat_count;       // [4]: analytic, convex, triangle-mesh pairs; convex pairs that overlap
-    int* cat_list;        // [4 * pair_cap]: the pairs of each category; overlapping convex pairs
+    int* cat_count;       // [6]: analytic pairs without a box, convex, triangle-mesh pairs, convex pairs
+                          // that overlap, analytic pairs with one box, box-box pairs
+    int* cat_list;        // [6 * pair_cap]: the pairs of each list
     Manifold* man_pair;   // one slot per pair (analytic / convex categories)
     int tri_cap;          // triangle-mesh pair slots
     Manifold* man_tri;    // kTriManifolds slots per triangle-mesh pair slot

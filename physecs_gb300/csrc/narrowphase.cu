@@ -67,23 +67,32 @@ __global__ void k_classify(World w, FrameBuf f) {
             }
             f.pair_cat[p] = cat;
             f.pair_nman[p] = 0;
+            // analytic pairs go to three lists by their boxes (none, one, two), so that a
+            // warp's pairs take the same path (box-box SAT and clipping cost the most)
+            if (cat == 0) {
+                const int boxes = (a.y == G_BOX) + (b.y == G_BOX);
+                cat = boxes == 0 ? 0 : (boxes == 1 ? 4 : 5);
+            }
         }
-        for (int c = 0; c < 3; ++c) {
+        for (int c : {0, 1, 2, 4, 5}) {
             unsigned m = __ballot_sync(0xffffffffu, cat == c);
             if (!m) continue;
             int first = 0;
             if (lane == __ffs(m) - 1) first = atomicAdd(&f.cat_count[c], __popc(m));
             first = __shfl_sync(0xffffffffu, first, __ffs(m) - 1);
-            if (cat == c) f.cat_list[c * f.pair_cap + first + __popc(m & ((1u << lane) - 1u))] = p;
+            if (cat == c) f.cat_list[c * (size_t)f.pair_cap + first + __popc(m & ((1u << lane) - 1u))] = p;
         }
     }
 }
 
-// analytic pairs: sphere / capsule / box
+// analytic pairs: sphere / capsule / box, box-box pairs first (the longest), then pairs
+// with one box, then the rest
 __global__ void __launch_bounds__(256) k_narrow_analytic(World w, FrameBuf f) {
-    int n = f.cat_count[0];
+    const int n2 = f.cat_count[5], n1 = f.cat_count[4], n0 = f.cat_count[0];
+    const int n = n2 + n1 + n0;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        int p = f.cat_list[t];
+        int p = t < n2 ? f.cat_list[5 * (size_t)f.pair_cap + t]
+                       : (t < n2 + n1 ? f.cat_list[4 * (size_t)f.pair_cap + t - n2] : f.cat_list[t - n2 - n1]);
         int2 pr = f.pairs[p];
         V3 pos0, pos1;
         Q4 or0, or1;
@@ -271,7 +280,7 @@ static void launch_convex_epa(const World& w, FrameBuf& f, int blocks_per_sm, cu
 // The convex kernels (bound by the FP64 pipe) run on the aux stream beside the analytic
 // and triangle-mesh kernels (FP32, latency-bound); the categories write disjoint slots.
 int launch_narrowphase(const World& w, FrameBuf& f, const StreamPair& sp, const NarrowShape& ns, cudaStream_t s) {
-    cudaMemsetAsync(f.cat_count, 0, 4 * sizeof(int), s);
+    cudaMemsetAsync(f.cat_count, 0, 6 * sizeof(int), s);
     k_classify<<<1216, 256, 0, s>>>(w, f);
     cudaEventRecord(sp.fork, s);
     cudaStreamWaitEvent(sp.aux, sp.fork, 0);

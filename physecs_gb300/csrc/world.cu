@@ -422,8 +422,8 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
     PSX_TRY(W->alloc(f.pairs, f.pair_cap));
     PSX_TRY(W->alloc(f.n_pairs, 1));
     PSX_TRY(W->alloc(f.pair_cat, f.pair_cap));
-    PSX_TRY(W->alloc(f.cat_count, 4));
-    PSX_TRY(W->alloc(f.cat_list, 4 * (size_t)f.pair_cap));
+    PSX_TRY(W->alloc(f.cat_count, 6));
+    PSX_TRY(W->alloc(f.cat_list, 6 * (size_t)f.pair_cap));
     PSX_TRY(W->alloc(f.man_pair, f.pair_cap));
     PSX_TRY(W->alloc(f.man_tri, (size_t)f.tri_cap * kTriManifolds));
     PSX_TRY(W->alloc(f.pair_tslot, f.pair_cap));
