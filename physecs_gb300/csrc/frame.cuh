@@ -36,9 +36,10 @@ struct FrameBuf {
     int* n_pairs;         // device scalar
     // narrowphase
     int* pair_cat;        // 0 analytic, 1 convex mesh, 2 triangle mesh
-    int* cat_count;       // [6]: analytic pairs without a box, convex, triangle-mesh pairs, convex pairs
-                          // that overlap, analytic pairs with one box, box-box pairs
-    int* cat_list;        // [6 * pair_cap]: the pairs of each list
+    int* cat_count;       // [7]: analytic pairs without a box, convex, triangle-mesh pairs, convex pairs
+                          // that overlap, analytic pairs with one box, box-box pairs, overlapping convex
+                          // pairs whose EPA polytope outgrew the small one
+    int* cat_list;        // [7 * pair_cap]: the pairs of each list
     Manifold* man_pair;   // one slot per pair (analytic / convex categories)
     int tri_cap;          // triangle-mesh pair slots
     Manifold* man_tri;    // kTriManifolds slots per triangle-mesh pair slot

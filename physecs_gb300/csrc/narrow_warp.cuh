@@ -32,29 +32,39 @@
 
 namespace psx {
 
-constexpr int kFaceSlots = (kEpaFaces + 31) / 32;   // 32-bit words of the face visibility bitset
-
-struct WarpPoly {
-    double nx[kEpaFaces], ny[kEpaFaces], nz[kEpaFaces];
-    double fd[kEpaFaces];                                   // face distance dot(v[i0], n), fixed at creation
-    double px[kEpaVerts], py[kEpaVerts], pz[kEpaVerts];     // Minkowski vertex
-    float ax[kEpaVerts], ay[kEpaVerts], az[kEpaVerts];      // support point on shape 0
-    float bx[kEpaVerts], by[kEpaVerts], bz[kEpaVerts];      // support point on shape 1
-    unsigned char i0[kEpaFaces], i1[kEpaFaces], i2[kEpaFaces];
-    unsigned char e0[kEpaEdges], e1[kEpaEdges];
-    unsigned int vis[kFaceSlots];
-    int nf, nv, ne;
+// One pair's polytope with room for VC vertices, FC faces and EC horizon edges.
+template <int VC, int FC, int EC>
+struct PolyT {
+    static constexpr int kV = VC, kF = FC, kE = EC;
+    double nx[FC], ny[FC], nz[FC];
+    double fd[FC];                                  // face distance dot(v[i0], n), fixed at creation
+    double px[VC], py[VC], pz[VC];                  // Minkowski vertex
+    float ax[VC], ay[VC], az[VC];                   // support point on shape 0
+    float bx[VC], by[VC], bz[VC];                   // support point on shape 1
+    unsigned char i0[FC], i1[FC], i2[FC];
+    unsigned char e0[EC], e1[EC];
+    unsigned int vis[(FC + 31) / 32];               // face visibility bitset
+    int nf, nv, ne, full;
 };
+// the reference's capacity (4 + 100 iterations)
+using WarpPoly = PolyT<kEpaVerts, kEpaFaces, kEpaEdges>;
+// room for 36 iterations in about a third of the space: most pairs need about five,
+// and a pair that outgrows it is solved again with WarpPoly
+using SmallPoly = PolyT<40, 76, 40>;
 
-__device__ __forceinline__ D3 wp_pos(const WarpPoly& P, int i) { return {P.px[i], P.py[i], P.pz[i]}; }
-__device__ __forceinline__ D3 wp_n(const WarpPoly& P, int f) { return {P.nx[f], P.ny[f], P.nz[f]}; }
-__device__ __forceinline__ void wp_set_vertex(WarpPoly& P, int i, const GjkVertex& v) {
+template <class PT>
+__device__ __forceinline__ D3 wp_pos(const PT& P, int i) { return {P.px[i], P.py[i], P.pz[i]}; }
+template <class PT>
+__device__ __forceinline__ D3 wp_n(const PT& P, int f) { return {P.nx[f], P.ny[f], P.nz[f]}; }
+template <class PT>
+__device__ __forceinline__ void wp_set_vertex(PT& P, int i, const GjkVertex& v) {
     P.px[i] = v.pos.x; P.py[i] = v.pos.y; P.pz[i] = v.pos.z;
     P.ax[i] = v.sp0.x; P.ay[i] = v.sp0.y; P.az[i] = v.sp0.z;
     P.bx[i] = v.sp1.x; P.by[i] = v.sp1.y; P.bz[i] = v.sp1.z;
 }
 // EPA.h face construction: normal = normalize(cross(v0 - v1, v2 - v1)), left as is when degenerate
-__device__ __forceinline__ void wp_set_face(WarpPoly& P, int slot, int i0, int i1, int i2) {
+template <class PT>
+__device__ __forceinline__ void wp_set_face(PT& P, int slot, int i0, int i1, int i2) {
     D3 n = cross(wp_pos(P, i0) - wp_pos(P, i1), wp_pos(P, i2) - wp_pos(P, i1));
     double len = length(n);
     if (len) n = n / len;
@@ -120,11 +130,14 @@ __device__ __forceinline__ double group_min_d(double v, const Group<G>& g) {
     return v;
 }
 
-// EPA.h:10-186 for one group of G lanes.  Every lane of the group returns the same
-// normal and points.
-template <int G>
-__device__ inline V3 group_epa(const Support& s0, const Support& s1, const GjkSimplex& s, V3& cp0, V3& cp1, WarpPoly& P,
-                               const Group<G>& g, int* err) {
+// EPA.h:10-186 for one group of G lanes.  Every lane of the group gets the same normal
+// and points.  Capacity: with kSpill, a polytope that would outgrow P stops the walk and
+// the call returns false (nothing is produced; the caller solves the pair again with a
+// larger polytope); without, the capacity error is raised and the walk goes on
+// truncated, as it can only with the reference's own 100-iteration room exhausted.
+template <int G, class PT, bool kSpill>
+__device__ inline bool group_epa(const Support& s0, const Support& s1, const GjkSimplex& s, V3& nrm, V3& cp0, V3& cp1,
+                                 PT& P, const Group<G>& g, int* err) {
     const int gl = g.gl;
     if (gl == 0) {
         for (int i = 0; i < 4; ++i) wp_set_vertex(P, i, s.v[i]);
@@ -207,6 +220,7 @@ __device__ inline V3 group_epa(const Support& s0, const Support& s1, const GjkSi
         g.sync();
         if (gl == 0) {
             int ne = 0, n = nf;
+            bool full = false;
             for (int k = nf - 1; k >= 0; --k) {
                 if (!((P.vis[k >> 5] >> (k & 31)) & 1u)) continue;
                 int a[3] = {P.i0[k], P.i1[k], P.i2[k]}, b[3] = {P.i1[k], P.i2[k], P.i0[k]};
@@ -222,7 +236,8 @@ __device__ inline V3 group_epa(const Support& s0, const Support& s1, const GjkSi
                 }
                 for (int j = 0; j < 3; ++j) {
                     if (found[j]) continue;
-                    if (ne < kEpaEdges) { P.e0[ne] = (unsigned char)a[j]; P.e1[ne] = (unsigned char)b[j]; ++ne; }
+                    if (ne < PT::kE) { P.e0[ne] = (unsigned char)a[j]; P.e1[ne] = (unsigned char)b[j]; ++ne; }
+                    else if (kSpill) full = true;
                     else raise_err(err, ERR_EPA_CAPACITY);
                 }
                 // remove face k: the last face moves into its slot
@@ -231,7 +246,9 @@ __device__ inline V3 group_epa(const Support& s0, const Support& s1, const GjkSi
                 P.i0[k] = P.i0[l]; P.i1[k] = P.i1[l]; P.i2[k] = P.i2[l];
                 --n;
             }
-            if (P.nv >= kEpaVerts) {
+            if (kSpill && (P.nv >= PT::kV || n + ne > PT::kF)) {
+                full = true;
+            } else if (P.nv >= PT::kV) {
                 raise_err(err, ERR_EPA_CAPACITY);
                 ne = 0;
             } else {
@@ -240,16 +257,18 @@ __device__ inline V3 group_epa(const Support& s0, const Support& s1, const GjkSi
             }
             P.ne = ne;
             P.nf = n;
+            P.full = full;
         }
         g.sync();
+        if (kSpill && P.full) return false;
         const int ne = P.ne, nbase = P.nf, vi = P.nv - 1;
         for (int m = gl; m < ne; m += G) {
             int slot = nbase + m;
-            if (slot < kEpaFaces) wp_set_face(P, slot, vi, P.e0[m], P.e1[m]);
+            if (slot < PT::kF) wp_set_face(P, slot, vi, P.e0[m], P.e1[m]);
             else raise_err(err, ERR_EPA_CAPACITY);
         }
         g.sync();
-        if (gl == 0) P.nf = min(nbase + ne, kEpaFaces);
+        if (gl == 0) P.nf = min(nbase + ne, PT::kF);
         g.sync();
     }
     // closest points on the closest face (EPA.h:101-143); the projection adds the
@@ -280,7 +299,8 @@ __device__ inline V3 group_epa(const Support& s0, const Support& s1, const GjkSi
     cp0 = f3(u * a0 + vv * a1 + ww * a2);
     cp1 = f3(u * b0 + vv * b1 + ww * b2);
     g.sync();
-    return f3(normal);
+    nrm = f3(normal);
+    return true;
 }
 
 }  // namespace psx

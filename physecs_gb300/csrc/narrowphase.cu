@@ -171,41 +171,62 @@ __global__ void __launch_bounds__(128, 4) k_convex_gjk(World w, FrameBuf f) {
     }
 }
 
-// EPA for the overlapping pairs, from the simplex GJK kept: a group of G lanes per pair
-// (32 / G pairs per warp), WARPS warps per block, one polytope (about 12.8 KB of
-// dynamic shared memory) per group.
+// EPA for one overlapping pair, from the simplex GJK kept in its manifold slot; the
+// pair's normal and closest points replace the simplex there.  false: the polytope
+// outgrew P (kSpill), nothing was written.
+template <int G, class PT, bool kSpill>
+__device__ __forceinline__ bool epa_pair(const World& w, FrameBuf& f, int t, PT& P, const Group<G>& g) {
+    const int p = f.cat_list[f.pair_cap + t];
+    V3 pos0, pos1;
+    Q4 or0, or1;
+    GeomD g0, g1;
+    convex_pair_ordered(w, f.pairs[p], pos0, or0, g0, pos1, or1, g1);
+    Support a, b;
+    convexOrderedSupports(w, pos0, or0, g0, pos1, or1, g1, a, b);
+    Manifold& m = f.man_pair[p];
+    GjkSimplex s;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const V3 sa = ld3(m.p0[i]), sb = ld3(m.p1[i]);
+        s.v[i] = {d3(sa - sb), sa, sb};
+    }
+    V3 nrm, c0, c1;
+    if (!group_epa<G, PT, kSpill>(a, b, s, nrm, c0, c1, P, g, w.err)) return false;   // ends with a group barrier
+    if (g.gl == 0) {
+        m.n = st4(nrm);
+        m.p0[0] = st4(c0);
+        m.p1[0] = st4(c1);
+    }
+    return true;
+}
+
+// EPA for the overlapping pairs: a group of G lanes per pair (32 / G pairs per warp),
+// WARPS warps per block, a SmallPoly (about 4.7 KB of dynamic shared memory) per group.
+// Pairs that outgrow it go to the overflow list for k_convex_epa_full.
 template <int G, int WARPS>
 __global__ void __launch_bounds__(32 * WARPS) k_convex_epa(World w, FrameBuf f) {
     extern __shared__ __align__(16) unsigned char epa_smem[];
     constexpr int GPW = 32 / G;   // groups per warp
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const Group<G> g(lane);
-    WarpPoly& P = reinterpret_cast<WarpPoly*>(epa_smem)[wid * GPW + lane / G];
+    SmallPoly& P = reinterpret_cast<SmallPoly*>(epa_smem)[wid * GPW + lane / G];
     const int n = f.cat_count[3];
     for (int h = (blockIdx.x * WARPS + wid) * GPW + lane / G; h < n; h += gridDim.x * WARPS * GPW) {
         const int t = f.cat_list[3 * (size_t)f.pair_cap + h];
-        const int p = f.cat_list[f.pair_cap + t];
-        V3 pos0, pos1;
-        Q4 or0, or1;
-        GeomD g0, g1;
-        convex_pair_ordered(w, f.pairs[p], pos0, or0, g0, pos1, or1, g1);
-        Support a, b;
-        convexOrderedSupports(w, pos0, or0, g0, pos1, or1, g1, a, b);
-        Manifold& m = f.man_pair[p];
-        GjkSimplex s;
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            const V3 sa = ld3(m.p0[i]), sb = ld3(m.p1[i]);
-            s.v[i] = {d3(sa - sb), sa, sb};
-        }
-        V3 c0, c1;
-        const V3 nrm = group_epa<G>(a, b, s, c0, c1, P, g, w.err);   // ends with a group barrier
-        if (g.gl == 0) {
-            m.n = st4(nrm);
-            m.p0[0] = st4(c0);
-            m.p1[0] = st4(c1);
-        }
+        if (!epa_pair<G, SmallPoly, true>(w, f, t, P, g) && g.gl == 0)
+            f.cat_list[6 * (size_t)f.pair_cap + atomicAdd(&f.cat_count[6], 1)] = t;
     }
+}
+
+// The pairs whose polytope outgrew SmallPoly, with the reference's full capacity: one
+// warp and one WarpPoly (about 12.8 KB) per block.
+__global__ void __launch_bounds__(32) k_convex_epa_full(World w, FrameBuf f) {
+    extern __shared__ __align__(16) unsigned char epa_smem[];
+    const Group<32> g(threadIdx.x);
+    WarpPoly& P = *reinterpret_cast<WarpPoly*>(epa_smem);
+    const int n = f.cat_count[6];
+    for (int h = blockIdx.x; h < n; h += gridDim.x)
+        epa_pair<32, WarpPoly, false>(w, f, f.cat_list[6 * (size_t)f.pair_cap + h], P, g);
 }
 
 // convex-mesh pairs, part 2: contact generation after EPA (face selection and
@@ -267,7 +288,7 @@ __global__ void __launch_bounds__(64) k_narrow_tri(World w, FrameBuf f) {
 
 template <int G, int WARPS>
 static void launch_convex_epa(const World& w, FrameBuf& f, int blocks_per_sm, cudaStream_t s) {
-    const int smem = (int)sizeof(WarpPoly) * WARPS * (32 / G);
+    const int smem = (int)sizeof(SmallPoly) * WARPS * (32 / G);
     static bool attr_set = false;
     if (!attr_set) {
         cudaFuncSetAttribute(k_convex_epa<G, WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -280,7 +301,7 @@ static void launch_convex_epa(const World& w, FrameBuf& f, int blocks_per_sm, cu
 // The convex kernels (bound by the FP64 pipe) run on the aux stream beside the analytic
 // and triangle-mesh kernels (FP32, latency-bound); the categories write disjoint slots.
 int launch_narrowphase(const World& w, FrameBuf& f, const StreamPair& sp, const NarrowShape& ns, cudaStream_t s) {
-    cudaMemsetAsync(f.cat_count, 0, 6 * sizeof(int), s);
+    cudaMemsetAsync(f.cat_count, 0, 7 * sizeof(int), s);
     k_classify<<<1216, 256, 0, s>>>(w, f);
     cudaEventRecord(sp.fork, s);
     cudaStreamWaitEvent(sp.aux, sp.fork, 0);
@@ -290,13 +311,21 @@ int launch_narrowphase(const World& w, FrameBuf& f, const StreamPair& sp, const 
     else if (ns.convex_warps == 1) launch_convex_epa<32, 1>(w, f, ns.convex_blocks_per_sm, sp.aux);
     else if (ns.convex_warps == 2) launch_convex_epa<32, 2>(w, f, ns.convex_blocks_per_sm, sp.aux);
     else launch_convex_epa<32, 3>(w, f, ns.convex_blocks_per_sm, sp.aux);
+    {
+        static bool attr_set = false;
+        if (!attr_set) {
+            cudaFuncSetAttribute(k_convex_epa_full, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(WarpPoly));
+            attr_set = true;
+        }
+        k_convex_epa_full<<<152 * 4, 32, sizeof(WarpPoly), sp.aux>>>(w, f);
+    }
     k_convex_contacts<<<1216 * 128 / ns.contacts_threads, ns.contacts_threads, 0, sp.aux>>>(w, f);
     cudaEventRecord(sp.join, sp.aux);
     k_narrow_analytic<<<152 * ns.analytic_blocks_per_sm, ns.analytic_threads, 0, s>>>(w, f);
     k_narrow_tri<<<1216, 64, 0, s>>>(w, f);
     cudaStreamWaitEvent(s, sp.join, 0);
     scan_exclusive_dev(f.pair_nman, f.pair_moff, f.n_pairs, f.pair_cap, f.n_man, f.scan_scratch, s);
-    return 2 + 5 + 3;
+    return 2 + 6 + 3;
 }
 
 }  // namespace psx

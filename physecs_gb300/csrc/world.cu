@@ -422,8 +422,8 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
     PSX_TRY(W->alloc(f.pairs, f.pair_cap));
     PSX_TRY(W->alloc(f.n_pairs, 1));
     PSX_TRY(W->alloc(f.pair_cat, f.pair_cap));
-    PSX_TRY(W->alloc(f.cat_count, 6));
-    PSX_TRY(W->alloc(f.cat_list, 6 * (size_t)f.pair_cap));
+    PSX_TRY(W->alloc(f.cat_count, 7));
+    PSX_TRY(W->alloc(f.cat_list, 7 * (size_t)f.pair_cap));
     PSX_TRY(W->alloc(f.man_pair, f.pair_cap));
     PSX_TRY(W->alloc(f.man_tri, (size_t)f.tri_cap * kTriManifolds));
     PSX_TRY(W->alloc(f.pair_tslot, f.pair_cap));
@@ -776,23 +776,15 @@ PSX_API psx_status psx_world_tune(psx_world* W, int32_t frames, psx_launch_confi
         }
         knobs.push_back(k);
     }
-    {   // EPA: lanes per pair; for 32 lanes, warps per block x blocks per SM (at most 15
-        // warps per SM); for 8 or 16 lanes, one-warp blocks (4 or 2 pairs) per SM
+    {   // EPA: lanes per pair, warps per block, blocks per SM (a SmallPoly per pair in shared
+        // memory; the registers allow about 28 warps per SM)
         Knob k{1, {}};
-        for (int wv : {1, 2, 3})
-            for (int b : {3, 5, 7, 10, 15}) {
-                if (wv * b > 15) continue;
-                psx_launch_config c{};
-                c.epa_lanes = 32;
-                c.convex_warps = wv;
-                c.convex_blocks_per_sm = b;
-                k.cands.push_back(c);
-            }
-        for (int lanes : {8, 16}) {
+        const int cands[][3] = {{32, 1, 15}, {32, 1, 24}, {32, 1, 32}, {32, 2, 12}, {32, 3, 8}, {16, 1, 20}, {8, 1, 12}};
+        for (const auto& c3 : cands) {
             psx_launch_config c{};
-            c.epa_lanes = lanes;
-            c.convex_warps = 1;
-            c.convex_blocks_per_sm = 64 / lanes;   // as many blocks as shared memory lets reside
+            c.epa_lanes = c3[0];
+            c.convex_warps = c3[1];
+            c.convex_blocks_per_sm = c3[2];
             k.cands.push_back(c);
         }
         knobs.push_back(k);
