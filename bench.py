@@ -235,6 +235,7 @@ def cpu_kind():
 
 # ---------------------------------------------------------------- serving
 
+SERVE_LAUNCH = None                # launch shapes of the serving world (None: the defaults)
 SERVE_HBM_BUDGET = 120 * 10 ** 9   # device bytes the serving slots may hold (requests stay resident)
 SERVE_CLASSES = [(17, 96), (33, 96), (65, 96), (129, 96), (257, 96), (513, 96), (1025, 64), (2049, 48), (4097, 32),
                  (8193, 24)]
@@ -354,7 +355,8 @@ def run_serving(args, rank, world, local):
     reqs, pool_scene = serving_requests(384, rank, n_max=args.serve_max_bodies)
     from physecs_gb300.desc import make_desc
     descs = [make_desc(s) for s, _ in reqs]          # the clients' packed requests
-    srv = Server(classes, mesh_pool=pool_scene, device=local if world > 1 else 0, hbm_budget=SERVE_HBM_BUDGET)
+    srv = Server(classes, mesh_pool=pool_scene, device=local if world > 1 else 0, hbm_budget=SERVE_HBM_BUDGET,
+                 launch=SERVE_LAUNCH)
     # saturated throughput: a permanent backlog keeps every fitting slot busy
     backlog = 2 * sum(c[1] for c in classes)   # enough waiting requests to keep every class busy
     _serve(srv, reqs, None, 3.0, backlog, descs)

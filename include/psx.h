@@ -155,7 +155,7 @@ typedef struct psx_world psx_world;
  * changes a result; 0 in a field keeps the default.  psx_world_tune picks them. */
 typedef struct psx_launch_config {
     int32_t convex_warps;            /* EPA: warps (pairs) per block, 1-3 (default 1) */
-    int32_t convex_blocks_per_sm;    /* EPA: blocks per SM in the grid (default 15) */
+    int32_t convex_blocks_per_sm;    /* EPA: blocks per SM in the grid (default 20) */
     int32_t analytic_threads;        /* sphere/capsule/box pairs: threads per block, <= 256 (default 64) */
     int32_t analytic_blocks_per_sm;  /* (default 16) */
     int32_t contacts_threads;        /* convex contact generation: threads per block, <= 256 (default 64) */
@@ -164,8 +164,13 @@ typedef struct psx_launch_config {
                                       * velocities fit the cluster's shared memory), 2 the whole grid, one scene
                                       * after another (default: clusters when two or more scenes fit them) */
     int32_t gjk_blocks_per_sm;       /* GJK (one thread per convex pair): 128-thread blocks per SM, 1-16 (default 16) */
-    int32_t epa_lanes;               /* EPA: lanes per overlapping pair, 8, 16 or 32 (default 32); below 32 a block
+    int32_t epa_lanes;               /* EPA: lanes per overlapping pair, 8, 16 or 32 (default 16); below 32 a block
                                       * is one warp holding 32 / epa_lanes pairs */
+    int32_t solver_threads_min;      /* smallest solver block: 64 (scenes up to 96 dynamic bodies on 64 threads, up to
+                                      * 384 on 128), 128 or 256 (default 64) */
+    int32_t epa_full_only;           /* 1: EPA with the full polytope only (lowest latency for the slowest pair);
+                                      * 2: a small polytope first, the full one for the pairs that outgrow it
+                                      * (highest throughput; default) */
 } psx_launch_config;
 
 typedef struct psx_world_opts {
@@ -270,6 +275,8 @@ typedef struct psx_server_opts {
     int64_t hbm_budget;               /* device bytes the server may hold, 0: no cap.  Every slot keeps its
                                        * request's state resident, so the budget caps the slots: creation
                                        * fails with PSX_ERR_OUT_OF_MEMORY when they need more */
+    const psx_launch_config* launch;  /* kernel launch shapes of the slots' world, or NULL: the world defaults
+                                       * with epa_full_only = 1 (frame latency before throughput) */
 } psx_server_opts;
 
 PSX_API psx_status psx_server_create(const psx_server_opts* opts, psx_server** out);

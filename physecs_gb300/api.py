@@ -38,7 +38,7 @@ class PsxError(RuntimeError):
 
 LAUNCH_FIELDS = ["convex_warps", "convex_blocks_per_sm", "analytic_threads", "analytic_blocks_per_sm",
                  "contacts_threads", "solver_smem_kb", "large_scene_solver",
-                 "gjk_blocks_per_sm", "epa_lanes"]
+                 "gjk_blocks_per_sm", "epa_lanes", "solver_threads_min", "epa_full_only"]
 
 
 class PsxLaunchConfig(C.Structure):
@@ -55,7 +55,7 @@ class PsxServerOpts(C.Structure):
     _fields_ = [("n_classes", C.c_int32), ("class_bodies", C.c_void_p), ("class_slots", C.c_void_p),
                 ("mesh_pool", C.c_void_p), ("pairs_per_collider", C.c_int32), ("manifolds_per_collider", C.c_int32),
                 ("device", C.c_int32), ("eager", C.c_int32), ("profile", C.c_int32),
-                ("hbm_budget", C.c_int64)]
+                ("hbm_budget", C.c_int64), ("launch", C.c_void_p)]
 
 
 def load():
@@ -236,7 +236,7 @@ class Server:
     h = None
 
     def __init__(self, classes, mesh_pool=None, device=0, pairs_per_collider=0, manifolds_per_collider=0, eager=False,
-                 profile=False, hbm_budget=0):
+                 profile=False, hbm_budget=0, launch=None):
         lib = load()
         self._cb = np.ascontiguousarray([c[0] for c in classes], np.int32)
         self._cs = np.ascontiguousarray([c[1] for c in classes], np.int32)
@@ -245,7 +245,10 @@ class Server:
         opts = PsxServerOpts(len(classes), self._cb.ctypes.data, self._cs.ctypes.data,
                              C.cast(C.pointer(self._pool), C.c_void_p) if self._pool is not None else None,
                              pairs_per_collider, manifolds_per_collider, device, 1 if eager else 0,
-                             1 if profile else 0, int(hbm_budget))
+                             1 if profile else 0, int(hbm_budget), None)
+        if launch:
+            self._launch = PsxLaunchConfig(*[int(launch.get(n, 0)) for n in LAUNCH_FIELDS])
+            opts.launch = C.cast(C.pointer(self._launch), C.c_void_p)
         h = C.c_void_p()
         _check(lib.psx_server_create(C.byref(opts), C.byref(h)))
         self.h = h

@@ -94,6 +94,7 @@ struct NarrowShape {
     int contacts_threads;
     int gjk_blocks_per_sm;                    // GJK: 128-thread blocks per SM
     int epa_lanes;                            // EPA: lanes per pair (8, 16 or 32; below 32, one warp per block)
+    int epa_full_only;                        // EPA: skip the small-polytope pass
 };
 int launch_narrowphase(const World& w, FrameBuf& f, const StreamPair& sp, const NarrowShape& ns, cudaStream_t s);
 int launch_contacts(const World& w, FrameBuf& f, cudaStream_t s);
@@ -102,7 +103,9 @@ int launch_contacts(const World& w, FrameBuf& f, cudaStream_t s);
 // (the whole grid, one after another)
 constexpr int kClusterBlocks = 8;   // blocks of the cluster that solves one large scene
 struct SolverLaunch {
-    const int* small; int n_small; int smem_small;
+    const int* tier[3]; int n_tier[3]; int smem_tier[3];   // block scenes by block size 64 / 128 / 256
+    cudaStream_t tstream[2];                               // streams of the 64- and 128-thread tiers
+    cudaEvent_t tfork, tjoin[2];
     const int* large; int n_large; int smem_large;
     const int* cluster; int n_cluster;     // large scenes solved by one cluster each
     const int* grid; int n_grid; int grid_blocks;

@@ -218,15 +218,16 @@ __global__ void __launch_bounds__(32 * WARPS) k_convex_epa(World w, FrameBuf f) 
     }
 }
 
-// The pairs whose polytope outgrew SmallPoly, with the reference's full capacity: one
-// warp and one WarpPoly (about 12.8 KB) per block.
-__global__ void __launch_bounds__(32) k_convex_epa_full(World w, FrameBuf f) {
+// EPA with the reference's full capacity, one warp and one WarpPoly (about 12.8 KB) per
+// block, over list `lst`: the pairs whose polytope outgrew SmallPoly (6), or every
+// overlapping pair (3) when the small pass is off.
+__global__ void __launch_bounds__(32) k_convex_epa_full(World w, FrameBuf f, int lst) {
     extern __shared__ __align__(16) unsigned char epa_smem[];
     const Group<32> g(threadIdx.x);
     WarpPoly& P = *reinterpret_cast<WarpPoly*>(epa_smem);
-    const int n = f.cat_count[6];
+    const int n = f.cat_count[lst];
     for (int h = blockIdx.x; h < n; h += gridDim.x)
-        epa_pair<32, WarpPoly, false>(w, f, f.cat_list[6 * (size_t)f.pair_cap + h], P, g);
+        epa_pair<32, WarpPoly, false>(w, f, f.cat_list[lst * (size_t)f.pair_cap + h], P, g);
 }
 
 // convex-mesh pairs, part 2: contact generation after EPA (face selection and
@@ -306,18 +307,22 @@ int launch_narrowphase(const World& w, FrameBuf& f, const StreamPair& sp, const 
     cudaEventRecord(sp.fork, s);
     cudaStreamWaitEvent(sp.aux, sp.fork, 0);
     k_convex_gjk<<<152 * ns.gjk_blocks_per_sm, 128, 0, sp.aux>>>(w, f);
-    if (ns.epa_lanes == 8) launch_convex_epa<8, 1>(w, f, ns.convex_blocks_per_sm, sp.aux);
-    else if (ns.epa_lanes == 16) launch_convex_epa<16, 1>(w, f, ns.convex_blocks_per_sm, sp.aux);
-    else if (ns.convex_warps == 1) launch_convex_epa<32, 1>(w, f, ns.convex_blocks_per_sm, sp.aux);
-    else if (ns.convex_warps == 2) launch_convex_epa<32, 2>(w, f, ns.convex_blocks_per_sm, sp.aux);
-    else launch_convex_epa<32, 3>(w, f, ns.convex_blocks_per_sm, sp.aux);
+    if (!ns.epa_full_only) {
+        if (ns.epa_lanes == 8) launch_convex_epa<8, 1>(w, f, ns.convex_blocks_per_sm, sp.aux);
+        else if (ns.epa_lanes == 16) launch_convex_epa<16, 1>(w, f, ns.convex_blocks_per_sm, sp.aux);
+        else if (ns.convex_warps == 1) launch_convex_epa<32, 1>(w, f, ns.convex_blocks_per_sm, sp.aux);
+        else if (ns.convex_warps == 2) launch_convex_epa<32, 2>(w, f, ns.convex_blocks_per_sm, sp.aux);
+        else launch_convex_epa<32, 3>(w, f, ns.convex_blocks_per_sm, sp.aux);
+    }
     {
         static bool attr_set = false;
         if (!attr_set) {
             cudaFuncSetAttribute(k_convex_epa_full, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(WarpPoly));
+            cudaFuncSetAttribute(k_convex_epa_full, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
             attr_set = true;
         }
-        k_convex_epa_full<<<152 * 4, 32, sizeof(WarpPoly), sp.aux>>>(w, f);
+        // the full pass alone: as many blocks as shared memory lets reside
+        k_convex_epa_full<<<ns.epa_full_only ? 152 * 16 : 152 * 4, 32, sizeof(WarpPoly), sp.aux>>>(w, f, ns.epa_full_only ? 3 : 6);
     }
     k_convex_contacts<<<1216 * 128 / ns.contacts_threads, ns.contacts_threads, 0, sp.aux>>>(w, f);
     cudaEventRecord(sp.join, sp.aux);

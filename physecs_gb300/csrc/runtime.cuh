@@ -45,7 +45,7 @@ struct psx_world {
     int* grid_scenes = nullptr;
     int grid_blocks = 0;
     int solver_smem = 0;             // dynamic shared memory per solver block (bytes)
-    psx::NarrowShape narrow{1, 15, 64, 16, 64, 16, 32};   // launch shapes of the narrowphase kernels
+    psx::NarrowShape narrow{1, 20, 64, 16, 64, 16, 16, 0};   // launch shapes of the narrowphase kernels
     long long frames_run = 0;        // frames queued since creation
     int frame_kernels = 0;           // kernels in one frame
     int solver_smem_large = 0;       // the same for the 512-thread blocks of large scenes
@@ -55,6 +55,12 @@ struct psx_world {
     std::vector<int> cluster_scenes_h; // ... solved by a thread-block cluster each
     int* cluster_scenes = nullptr;     // (grid_scenes: the rest; both sized for every big scene)
     int large_mode = 0;                // 1: clusters where they fit, 2: the whole grid
+    // block scenes by solver block size (64, 128, 256 threads), each longest first
+    std::vector<int> tier_h[3];
+    int* tier_scenes[3] = {nullptr, nullptr, nullptr};
+    int threads_min = 64;              // smallest solver block size in use
+    cudaStream_t tier_stream[2] = {nullptr, nullptr};   // the 64- and 128-thread tiers
+    cudaEvent_t ev_tfork = nullptr, ev_tjoin[2] = {nullptr, nullptr};
     cudaStream_t aux_stream = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;     // solver: large scenes on the aux stream
     cudaEvent_t ev_fork2 = nullptr, ev_join2 = nullptr;   // narrowphase: convex pairs on the aux stream
@@ -100,6 +106,9 @@ struct psx_world {
         if (ev_join2) cudaEventDestroy(ev_join2);
         if (ev_join) cudaEventDestroy(ev_join);
         if (aux_stream) cudaStreamDestroy(aux_stream);
+        for (cudaStream_t t : tier_stream) if (t) cudaStreamDestroy(t);
+        if (ev_tfork) cudaEventDestroy(ev_tfork);
+        for (cudaEvent_t e : ev_tjoin) if (e) cudaEventDestroy(e);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -120,6 +129,9 @@ psx_launch_config current_launch(const psx_world* W);
 // splits the scenes above the block limit between clusters and the grid (mode as
 // psx_launch_config::large_scene_solver, 0: by the default rule)
 psx_status partition_big(psx_world* W, int mode);
+// splits the block scenes into solver block sizes (64 / 128 / 256 threads), the
+// smallest size in use being threads_min
+psx_status partition_tiers(psx_world* W, int threads_min);
 // reads the device error word; maps its bits to a status
 psx_status check_err(psx_world* W);
 // pinned host staging of at least n4 float4

@@ -206,6 +206,12 @@ PSX_API psx_status psx_server_create(const psx_server_opts* o, psx_server** out)
     wo.block_scene_max_dyn = 1 << 30;
     wo.use_graph = (o->eager || o->profile) ? 0 : 1;   // a tick is the same fixed kernel sequence every time
     wo.device = o->device;
+    // a tick waits for its slowest pair: without shapes from the caller, EPA runs with the
+    // full polytope directly (the small-polytope pass serves throughput, and a pair that
+    // outgrows it is solved twice)
+    psx_launch_config latency{};
+    latency.epa_full_only = 1;
+    wo.launch = o->launch ? o->launch : &latency;
     psx_world* W = nullptr;
     psx_status st = psx_world_create(descs.data(), n_slots, &wo, &W);
     if (st != PSX_OK) { delete S; return st; }

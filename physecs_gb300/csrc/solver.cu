@@ -1060,7 +1060,7 @@ __device__ void solve_scene(const World& w, FrameBuf& f, int s, const S& sy, flo
     }
 }
 
-// one scene per block; NT = 256 for scenes up to 1024 dynamic bodies, 512 above
+// one scene per block; NT = 64, 128 or 256 for scenes up to 1024 dynamic bodies (by size), 512 above
 template <int NT>
 __global__ void __launch_bounds__(NT, 512 / NT) k_solve_block(World w, FrameBuf f, const int* scenes, int smem_f4) {
     extern __shared__ float4 smem[];
@@ -1138,11 +1138,29 @@ int launch_solver(const World& w, FrameBuf& f, const SolverLaunch& L, cudaStream
         cudaEventRecord(L.join, L.aux);
         ++k;
     }
-    if (L.n_small) {
-        set_smem<256>(L.smem_small);
-        k_solve_block<256><<<L.n_small, 256, L.smem_small, s>>>(w, f, L.small, L.smem_small / 16);
+    // block scenes: 64- and 128-thread tiers on their own streams beside the 256-thread one
+    if (L.n_tier[0] || L.n_tier[1]) cudaEventRecord(L.tfork, s);
+    if (L.n_tier[0]) {
+        set_smem<64>(L.smem_tier[0]);
+        cudaStreamWaitEvent(L.tstream[0], L.tfork, 0);
+        k_solve_block<64><<<L.n_tier[0], 64, L.smem_tier[0], L.tstream[0]>>>(w, f, L.tier[0], L.smem_tier[0] / 16);
+        cudaEventRecord(L.tjoin[0], L.tstream[0]);
         ++k;
     }
+    if (L.n_tier[1]) {
+        set_smem<128>(L.smem_tier[1]);
+        cudaStreamWaitEvent(L.tstream[1], L.tfork, 0);
+        k_solve_block<128><<<L.n_tier[1], 128, L.smem_tier[1], L.tstream[1]>>>(w, f, L.tier[1], L.smem_tier[1] / 16);
+        cudaEventRecord(L.tjoin[1], L.tstream[1]);
+        ++k;
+    }
+    if (L.n_tier[2]) {
+        set_smem<256>(L.smem_tier[2]);
+        k_solve_block<256><<<L.n_tier[2], 256, L.smem_tier[2], s>>>(w, f, L.tier[2], L.smem_tier[2] / 16);
+        ++k;
+    }
+    if (L.n_tier[0]) cudaStreamWaitEvent(s, L.tjoin[0], 0);
+    if (L.n_tier[1]) cudaStreamWaitEvent(s, L.tjoin[1], 0);
     if (L.n_large) cudaStreamWaitEvent(s, L.join, 0);
     if (L.n_cluster) {
         static int cluster_smem = -1;

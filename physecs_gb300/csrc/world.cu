@@ -472,8 +472,17 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
         W->solver_smem_large = std::max(0, optin - 5120) / 16 * 16;
     }
     W->big_scenes_h = W->grid_scenes_h;
+    {   // longest scenes first, so that none of them starts in the last wave
+        auto longer = [&](int a, int b) {
+            int na = scene_dyn[a + 1] - scene_dyn[a], nb = scene_dyn[b + 1] - scene_dyn[b];
+            return na > nb || (na == nb && a < b);
+        };
+        std::sort(W->large_scenes_h.begin(), W->large_scenes_h.end(), longer);
+    }
     PSX_TRY(W->upload(W->block_scenes, W->block_scenes_h));
     PSX_TRY(W->upload(W->large_scenes, W->large_scenes_h));
+    for (int t = 0; t < 3; ++t) PSX_TRY(W->alloc(W->tier_scenes[t], W->block_scenes_h.size()));
+    PSX_TRY(partition_tiers(W, 64));
     PSX_TRY(W->alloc(W->cluster_scenes, W->big_scenes_h.size()));
     PSX_TRY(W->alloc(W->grid_scenes, W->big_scenes_h.size()));
     PSX_TRY(partition_big(W, 0));
@@ -507,7 +516,11 @@ int psx::rt::queue_frame(psx_world* W, cudaEvent_t* ev) {
     k += launch_contacts(W->w, W->f, s);
     k += launch_joint_layout(W->w, W->f, s);
     if (ev) cudaEventRecord(ev[3], s);
-    SolverLaunch L{W->block_scenes, (int)W->block_scenes_h.size(), W->solver_smem,
+    auto tier_smem = [&](int nt) { return std::max(12 * 1024, W->solver_smem * nt / 256) / 16 * 16; };
+    SolverLaunch L{{W->tier_scenes[0], W->tier_scenes[1], W->tier_scenes[2]},
+                   {(int)W->tier_h[0].size(), (int)W->tier_h[1].size(), (int)W->tier_h[2].size()},
+                   {tier_smem(64), tier_smem(128), W->solver_smem},
+                   {W->tier_stream[0], W->tier_stream[1]}, W->ev_tfork, {W->ev_tjoin[0], W->ev_tjoin[1]},
                    W->large_scenes, (int)W->large_scenes_h.size(), W->solver_smem_large,
                    W->cluster_scenes, (int)W->cluster_scenes_h.size(),
                    W->grid_scenes, (int)W->grid_scenes_h.size(), W->grid_blocks,
@@ -553,6 +566,7 @@ psx_status psx::rt::apply_launch(psx_world* W, const psx_launch_config& c) {
     if (c.contacts_threads) n.contacts_threads = c.contacts_threads;
     if (c.gjk_blocks_per_sm) n.gjk_blocks_per_sm = c.gjk_blocks_per_sm;
     if (c.epa_lanes) n.epa_lanes = c.epa_lanes;
+    if (c.epa_full_only) n.epa_full_only = c.epa_full_only == 1;
     auto threads_ok = [](int t) { return t == 32 || t == 64 || t == 128 || t == 256; };
     if (n.convex_warps < 1 || n.convex_warps > 3 || n.convex_blocks_per_sm < 1 || n.convex_blocks_per_sm > 32 ||
         !threads_ok(n.analytic_threads) || n.analytic_blocks_per_sm < 1 || n.analytic_blocks_per_sm > 64 ||
@@ -569,6 +583,9 @@ psx_status psx::rt::apply_launch(psx_world* W, const psx_launch_config& c) {
     }
     if (c.large_scene_solver < 0 || c.large_scene_solver > 2) return fail(PSX_ERR_INVALID_ARG, "large_scene_solver out of range");
     if (c.large_scene_solver && c.large_scene_solver != W->large_mode) PSX_TRY(partition_big(W, c.large_scene_solver));
+    if (c.solver_threads_min && c.solver_threads_min != 64 && c.solver_threads_min != 128 && c.solver_threads_min != 256)
+        return fail(PSX_ERR_INVALID_ARG, "solver_threads_min must be 64, 128 or 256");
+    if (c.solver_threads_min && c.solver_threads_min != W->threads_min) PSX_TRY(partition_tiers(W, c.solver_threads_min));
     W->narrow = n;
     W->solver_smem = smem;
     if (W->graph) { cudaGraphExecDestroy(W->graph); W->graph = nullptr; }   // recaptured with the new shapes
@@ -602,6 +619,29 @@ psx_status psx::rt::partition_big(psx_world* W, int mode) {
     return PSX_OK;
 }
 
+// Block scenes of up to 96 dynamic bodies run on 64-thread blocks and up to 384 on
+// 128-thread blocks (when threads_min allows), the rest on 256: a colour of a small
+// scene holds few contacts, and smaller blocks let more scenes share an SM.  Each list
+// is ordered longest scene first.
+psx_status psx::rt::partition_tiers(psx_world* W, int threads_min) {
+    for (auto& t : W->tier_h) t.clear();
+    for (int s : W->block_scenes_h) {
+        int nd = W->h_scene_dyn[s + 1] - W->h_scene_dyn[s];
+        int t = (threads_min <= 64 && nd <= 96) ? 0 : ((threads_min <= 128 && nd <= 384) ? 1 : 2);
+        W->tier_h[t].push_back(s);
+    }
+    PSX_CUDA(cudaStreamSynchronize(W->stream));
+    for (int t = 0; t < 3; ++t) {
+        auto& v = W->tier_h[t];
+        std::stable_sort(v.begin(), v.end(), [&](int a, int b) {
+            return W->h_scene_dyn[a + 1] - W->h_scene_dyn[a] > W->h_scene_dyn[b + 1] - W->h_scene_dyn[b];
+        });
+        if (!v.empty()) PSX_CUDA(cudaMemcpy(W->tier_scenes[t], v.data(), v.size() * sizeof(int), cudaMemcpyHostToDevice));
+    }
+    W->threads_min = threads_min;
+    return PSX_OK;
+}
+
 psx_launch_config psx::rt::current_launch(const psx_world* W) {
     psx_launch_config c{};
     c.convex_warps = W->narrow.convex_warps;
@@ -611,8 +651,10 @@ psx_launch_config psx::rt::current_launch(const psx_world* W) {
     c.contacts_threads = W->narrow.contacts_threads;
     c.gjk_blocks_per_sm = W->narrow.gjk_blocks_per_sm;
     c.epa_lanes = W->narrow.epa_lanes;
+    c.epa_full_only = W->narrow.epa_full_only ? 1 : 2;
     c.solver_smem_kb = W->solver_smem / 1024;
     c.large_scene_solver = W->large_mode;
+    c.solver_threads_min = W->threads_min;
     return c;
 }
 
@@ -656,6 +698,11 @@ PSX_API psx_status psx_world_create(const psx_scene_desc* scenes, int32_t n_scen
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&W->aux_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&W->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&W->ev_join, cudaEventDisableTiming);
+    for (int t = 0; t < 2 && e == cudaSuccess; ++t) {
+        e = cudaStreamCreateWithFlags(&W->tier_stream[t], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&W->ev_tjoin[t], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&W->ev_tfork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&W->ev_fork2, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&W->ev_join2, cudaEventDisableTiming);
     if (e != cudaSuccess) { delete W; return fail(PSX_ERR_CUDA, cudaGetErrorString(e)); }
@@ -814,6 +861,15 @@ PSX_API psx_status psx_world_tune(psx_world* W, int32_t frames, psx_launch_confi
         for (int m : {1, 2}) {
             psx_launch_config c{};
             c.large_scene_solver = m;
+            k.cands.push_back(c);
+        }
+        knobs.push_back(k);
+    }
+    if (!W->block_scenes_h.empty()) {   // the smallest solver block size
+        Knob k{3, {}};
+        for (int t : {64, 128, 256}) {
+            psx_launch_config c{};
+            c.solver_threads_min = t;
             k.cands.push_back(c);
         }
         knobs.push_back(k);
