@@ -167,7 +167,8 @@ typedef struct psx_launch_config {
     int32_t epa_lanes;               /* EPA: lanes per overlapping pair, 8, 16 or 32 (default 16); below 32 a block
                                       * is one warp holding 32 / epa_lanes pairs */
     int32_t solver_threads_min;      /* smallest solver block: 64 (scenes up to 96 dynamic bodies on 64 threads, up to
-                                      * 384 on 128), 128 or 256 (default 64) */
+                                      * 384 on 128), 128 or 256 (default: 64 for worlds of more block scenes than
+                                      * two per SM, else 256) */
     int32_t epa_full_only;           /* 1: EPA with the full polytope only (lowest latency for the slowest pair);
                                       * 2: a small polytope first, the full one for the pairs that outgrow it
                                       * (highest throughput; default) */

@@ -482,7 +482,13 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
     PSX_TRY(W->upload(W->block_scenes, W->block_scenes_h));
     PSX_TRY(W->upload(W->large_scenes, W->large_scenes_h));
     for (int t = 0; t < 3; ++t) PSX_TRY(W->alloc(W->tier_scenes[t], W->block_scenes_h.size()));
-    PSX_TRY(partition_tiers(W, 64));
+    {   // smaller solver blocks pay when more scenes wait than the SMs hold at once; a
+        // world of few scenes keeps 256 threads a scene for latency
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        PSX_TRY(partition_tiers(W, (int)W->block_scenes_h.size() > 2 * sms ? 64 : 256));
+    }
     PSX_TRY(W->alloc(W->cluster_scenes, W->big_scenes_h.size()));
     PSX_TRY(W->alloc(W->grid_scenes, W->big_scenes_h.size()));
     PSX_TRY(partition_big(W, 0));
