@@ -790,6 +790,32 @@ __device__ inline bool collideAnalytic(V3 pos0, Q4 or0, const GeomD& g0, V3 pos1
     }
 }
 
+// collideAnalytic for pairs with BOXES boxes: each list's kernel holds only its own routines
+template <int BOXES>
+__device__ inline bool collideAnalyticT(V3 pos0, Q4 or0, const GeomD& g0, V3 pos1, Q4 or1, const GeomD& g1, ManifoldL& r, int* err) {
+    r.numPoints = 0;
+    r.triangleIndex = -1;
+    if constexpr (BOXES == 2) {
+        return boxBox(pos0, or0, gv(g0), pos1, or1, gv(g1), r, err);
+    } else if constexpr (BOXES == 1) {
+        if (g1.type == G_BOX) {
+            if (g0.type == G_SPHERE) return sphereBox(pos0, g0.p[0], pos1, or1, gv(g1), r);
+            return capsuleBox(pos0, or0, g0.p[0], g0.p[1], pos1, or1, gv(g1), r);
+        }
+        if (g1.type == G_SPHERE) { bool h = sphereBox(pos1, g1.p[0], pos0, or0, gv(g0), r); flipM(r); return h; }
+        bool h = capsuleBox(pos1, or1, g1.p[0], g1.p[1], pos0, or0, gv(g0), r);
+        flipM(r);
+        return h;
+    } else {
+        if (g0.type == G_SPHERE) {
+            if (g1.type == G_SPHERE) return sphereSphere(pos0, g0.p[0], pos1, g1.p[0], r);
+            return sphereCapsule(pos0, g0.p[0], pos1, or1, g1.p[0], g1.p[1], r);
+        }
+        if (g1.type == G_SPHERE) { bool h = sphereCapsule(pos1, g1.p[0], pos0, or0, g0.p[0], g0.p[1], r); flipM(r); return h; }
+        return capsuleCapsule(pos0, or0, g0.p[0], g0.p[1], pos1, or1, g1.p[0], g1.p[1], r);
+    }
+}
+
 // convex-mesh pairs of physecs::collision (Collision.cpp:414-426, 488-499, 787-807, 873-887),
 // in three parts: the two supports, GJK + EPA, and the contact generation that
 // follows EPA.  g1 is always the convex mesh here.

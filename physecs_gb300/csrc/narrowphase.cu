@@ -85,14 +85,14 @@ __global__ void k_classify(World w, FrameBuf f) {
     }
 }
 
-// analytic pairs: sphere / capsule / box, box-box pairs first (the longest), then pairs
-// with one box, then the rest
+// analytic pairs: sphere / capsule / box, one kernel per list (BOXES boxes in the pair:
+// list 5 for two, 4 for one, 0 for none), so that each kernel holds only its routines
+template <int BOXES>
 __global__ void __launch_bounds__(256) k_narrow_analytic(World w, FrameBuf f) {
-    const int n2 = f.cat_count[5], n1 = f.cat_count[4], n0 = f.cat_count[0];
-    const int n = n2 + n1 + n0;
+    constexpr int lst = BOXES == 2 ? 5 : (BOXES == 1 ? 4 : 0);
+    const int n = f.cat_count[lst];
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        int p = t < n2 ? f.cat_list[5 * (size_t)f.pair_cap + t]
-                       : (t < n2 + n1 ? f.cat_list[4 * (size_t)f.pair_cap + t - n2] : f.cat_list[t - n2 - n1]);
+        int p = f.cat_list[lst * (size_t)f.pair_cap + t];
         int2 pr = f.pairs[p];
         V3 pos0, pos1;
         Q4 or0, or1;
@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(256) k_narrow_analytic(World w, FrameBuf f) {
         collider_pose(w, pr.x, pos0, or0, g0);
         collider_pose(w, pr.y, pos1, or1, g1);
         ManifoldL m;
-        bool hit = collideAnalytic(pos0, or0, g0, pos1, or1, g1, m, w.err);
+        bool hit = collideAnalyticT<BOXES>(pos0, or0, g0, pos1, or1, g1, m, w.err);
         int cnt = (hit && m.numPoints) ? 1 : 0;
         if (cnt) store_manifold(f.man_pair[p], m, p);
         f.pair_nman[p] = cnt;
@@ -326,11 +326,14 @@ int launch_narrowphase(const World& w, FrameBuf& f, const StreamPair& sp, const 
     }
     k_convex_contacts<<<1216 * 128 / ns.contacts_threads, ns.contacts_threads, 0, sp.aux>>>(w, f);
     cudaEventRecord(sp.join, sp.aux);
-    k_narrow_analytic<<<152 * ns.analytic_blocks_per_sm, ns.analytic_threads, 0, s>>>(w, f);
+    // box-box pairs first: the longest
+    k_narrow_analytic<2><<<152 * ns.analytic_blocks_per_sm, ns.analytic_threads, 0, s>>>(w, f);
+    k_narrow_analytic<1><<<152 * ns.analytic_blocks_per_sm, ns.analytic_threads, 0, s>>>(w, f);
+    k_narrow_analytic<0><<<152 * ns.analytic_blocks_per_sm, ns.analytic_threads, 0, s>>>(w, f);
     k_narrow_tri<<<1216, 64, 0, s>>>(w, f);
     cudaStreamWaitEvent(s, sp.join, 0);
     scan_exclusive_dev(f.pair_nman, f.pair_moff, f.n_pairs, f.pair_cap, f.n_man, f.scan_scratch, s);
-    return 2 + 6 + 3;
+    return 2 + 8 + 3;
 }
 
 }  // namespace psx
