@@ -230,6 +230,51 @@ PSX_API psx_status psx_world_simulate_host(psx_world* w, float dt, float* pos, f
 PSX_API psx_status psx_world_tune(psx_world* w, int32_t frames, psx_launch_config* best);
 /* The launch shapes in effect (after defaults, tuning or opts.launch). */
 PSX_API psx_status psx_world_launch_config(psx_world* w, psx_launch_config* out);
+
+/* ---- scene queries against the world's current state */
+typedef struct psx_ray {
+    int32_t scene;
+    float origin[3];
+    float dir[3];
+    float max_distance;
+} psx_ray;
+typedef struct psx_ray_hit {
+    int32_t body;       /* scene-local body index of the closest hit, -1: none */
+    int32_t collider;   /* collider index within that body */
+    uint32_t entity;
+    float distance;
+    float pos[3];       /* origin + dir * distance */
+} psx_ray_hit;
+/* Scene::raycastClosest(origin, dir, maxDistance, filter, &hitPos) for n rays
+ * (src/Physecs.cpp:571-626, src/Raycast.cpp).  accept: one byte per world body
+ * (scene-major), nonzero where the filter accepts the body's entity; NULL accepts every
+ * entity.  (The reference's overload without a filter never reports a hit, since it
+ * tests an empty std::function; a shim for that overload returns entt::null without
+ * calling this.)  Among hits at exactly the same distance the collider with the lowest
+ * world index wins, where the reference's choice follows its own tree. */
+PSX_API psx_status psx_world_raycast(psx_world* w, int32_t n, const psx_ray* rays, const uint8_t* accept,
+                                     psx_ray_hit* hits);
+
+typedef struct psx_overlap_query {
+    int32_t scene;
+    float pos[3];
+    float quat[4];      /* x, y, z, w */
+    int32_t type;       /* PSX_SPHERE, PSX_CAPSULE, PSX_BOX, PSX_CONVEX_MESH (PSX_TRIANGLE_MESH overlaps nothing) */
+    float params[3];    /* as col_params: sphere {r}; capsule {halfHeight, r}; box {halfExtents}; convex {scale} */
+    int32_t mesh;       /* convex mesh index within the scene's desc */
+    int32_t filter;     /* collider data bits that must meet, 0: any */
+} psx_overlap_query;
+typedef struct psx_overlap_hit {
+    int32_t body;       /* scene-local body index */
+    int32_t collider;   /* collider index within that body */
+    uint32_t entity;
+} psx_overlap_hit;
+/* Scene::overlap(pos, ori, geometry, filter) for n shapes (src/Physecs.cpp:628-651,
+ * src/Overlap.cpp).  Query i's hits are hits[i * cap, i * cap + min(counts[i], cap));
+ * counts[i] is the number found (a count above cap means the list was cut).  The set
+ * is the reference's; the order is this world's tree order. */
+PSX_API psx_status psx_world_overlap(psx_world* w, int32_t n, const psx_overlap_query* queries, int32_t cap,
+                                     psx_overlap_hit* hits, int32_t* counts);
 /* counts[12] = {bodies, colliders, dynamic bodies, joints, scenes, pairs, manifolds, error bits,
  *              contact points, joint rows, simulated bodies, kernels queued since creation}
  * (per-frame values describe the last frame) */

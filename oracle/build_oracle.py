@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "liborc.so")
-SRCS = ["collide_util.cpp", "gjk_epa.cpp", "collide.cpp", "collide_tri.cpp", "world.cpp", "port_capi.cpp"]
+SRCS = ["collide_util.cpp", "gjk_epa.cpp", "collide.cpp", "collide_tri.cpp", "world.cpp", "query.cpp", "port_capi.cpp"]
 FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-Wno-unused-function",
          "-I" + os.path.join(REPO, "include")]
 

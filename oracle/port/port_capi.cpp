@@ -167,4 +167,45 @@ void orc_collider_bounds(void* h, int collider, float* out6) {
     std::memcpy(out6 + 3, &b.max, 12);
 }
 
+// n rays of 8 floats {unused, origin xyz, dir xyz, max distance}; per ray the body,
+// collider index within it (-1, -1 for no hit), distance and hit position
+void orc_scene_raycast(void* h, int n, const float* rays, const uint8_t* accept, int32_t* out_ids, float* out_f) {
+    World* w = static_cast<World*>(h);
+    for (int i = 0; i < n; ++i) {
+        const float* r = rays + 8 * i;
+        V3 o = v3(r[1], r[2], r[3]), d = v3(r[4], r[5], r[6]);
+        float dist = 0.f;
+        int c = w->raycastClosest(o, d, r[7], accept, dist);
+        float* of = out_f + 4 * i;
+        if (c < 0) {
+            out_ids[2 * i] = -1; out_ids[2 * i + 1] = -1;
+            of[0] = of[1] = of[2] = of[3] = 0.f;
+            continue;
+        }
+        out_ids[2 * i] = w->colliders[c].body;
+        out_ids[2 * i + 1] = c - w->bodies[w->colliders[c].body].firstCol;
+        V3 p = o + d * dist;   // rayOrig + rayDir * distance (src/Physecs.cpp:624)
+        of[0] = dist; of[1] = p.x; of[2] = p.y; of[3] = p.z;
+    }
+}
+
+// one shape {pos xyz, quat xyzw}, type, params, convex mesh index, data filter; writes
+// up to cap (body, collider) pairs and returns the number found
+int orc_scene_overlap(void* h, const float* pose, int type, const float* params, int mesh, int filter, int32_t* out, int cap) {
+    World* w = static_cast<World*>(h);
+    Geometry g;
+    g.type = type;
+    g.p[0] = params[0]; g.p[1] = params[1]; g.p[2] = params[2];
+    if (type == CONVEX_MESH) g.convex = w->convex[mesh].get();
+    if (type == TRIANGLE_MESH) return 0;   // a triangle mesh overlaps nothing (Overlap.cpp:194-235)
+    std::vector<int> hits;
+    w->overlap(v3(pose[0], pose[1], pose[2]), Q4{pose[3], pose[4], pose[5], pose[6]}, g, filter, hits);
+    for (int k = 0; k < (int)hits.size() && k < cap; ++k) {
+        int c = hits[k];
+        out[2 * k] = w->colliders[c].body;
+        out[2 * k + 1] = c - w->bodies[w->colliders[c].body].firstCol;
+    }
+    return (int)hits.size();
+}
+
 }  // extern "C"

@@ -124,6 +124,11 @@ struct World {
     void updateBounds(int body, bool margin);
     V3 colPos(int c) const;
     Q4 colQ(int c) const;
+
+    // scene queries (query.cpp): the closest accepted ray hit (collider index or -1,
+    // accept: per body, NULL for all) and the colliders a shape overlaps, ascending
+    int raycastClosest(V3 o, V3 d, float maxd, const uint8_t* accept, float& dist) const;
+    void overlap(V3 pos, Q4 ori, const Geometry& g, int filter, std::vector<int>& out) const;
 };
 
 }  // namespace orc

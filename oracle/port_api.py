@@ -45,6 +45,8 @@ def lib():
         _lib.orc_scene_set_contact_order.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
         _lib.orc_scene_order_error.argtypes = [C.c_void_p]
         _lib.orc_scene_contact_keys.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+        _lib.orc_scene_raycast.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.orc_scene_overlap.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int]
     return _lib
 
 
@@ -116,6 +118,25 @@ class OracleScene:
             if n <= cap:
                 return ids[:n], f[:n]
             cap = n
+
+    def raycast(self, rays, accept=None):
+        """Scene::raycastClosest per ray; rays: (n, 8) {unused, origin, dir, max distance};
+        accept: per body (nonzero: accepted) or None.  Returns {body, collider, distance, pos}."""
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        n = len(rays)
+        ids = np.zeros((max(n, 1), 2), np.int32)
+        f = np.zeros((max(n, 1), 4), np.float32)
+        acc = None if accept is None else np.ascontiguousarray(accept, np.uint8)
+        lib().orc_scene_raycast(self.h, n, _p(rays), _p(acc) if acc is not None else None, _p(ids), _p(f))
+        return {"body": ids[:n, 0].copy(), "collider": ids[:n, 1].copy(), "distance": f[:n, 0].copy(), "pos": f[:n, 1:4].copy()}
+
+    def overlap(self, pos, quat, type_, params, mesh=-1, filt=0, cap=4096):
+        """Scene::overlap for one shape: list of (body, collider) in collider order."""
+        pose = np.ascontiguousarray(list(pos) + list(quat), np.float32)
+        prm = np.ascontiguousarray((list(params) + [0.0, 0.0, 0.0])[:3], np.float32)
+        out = np.zeros((cap, 2), np.int32)
+        m = lib().orc_scene_overlap(self.h, _p(pose), int(type_), _p(prm), int(mesh), int(filt), _p(out), cap)
+        return [tuple(map(int, r)) for r in out[:min(m, cap)]]
 
     def collide(self, pairs):
         pairs = np.ascontiguousarray(pairs, np.int32).reshape(-1, 4)

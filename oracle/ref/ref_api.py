@@ -33,6 +33,8 @@ def lib():
         _lib.ref_scene_pairs.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
         _lib.ref_scene_bounds.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         _lib.ref_scene_contacts.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        _lib.ref_scene_raycast.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.ref_scene_overlap.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int]
         _lib.ref_scene_collide.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         _lib.ref_scene_joint_colors.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
     return _lib
@@ -106,6 +108,25 @@ class RefScene:
             if n <= cap:
                 return ids[:n], f[:n]
             cap = n
+
+    def raycast(self, rays, accept=None):
+        """Scene::raycastClosest per ray (the overload without a filter when accept is None);
+        returns {body (-1: none), pos}."""
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        n = len(rays)
+        body = np.zeros(max(n, 1), np.int32)
+        pos = np.zeros((max(n, 1), 3), np.float32)
+        acc = None if accept is None else np.ascontiguousarray(accept, np.uint8)
+        lib().ref_scene_raycast(self.h, n, _p(rays), _p(acc) if acc is not None else None, _p(body), _p(pos))
+        return {"body": body[:n].copy(), "pos": pos[:n].copy()}
+
+    def overlap(self, pos, quat, type_, params, mesh=-1, filt=0, cap=4096):
+        """Scene::overlap for one shape: list of (body, collider) in the reference's order."""
+        pose = np.ascontiguousarray(list(pos) + list(quat), np.float32)
+        prm = np.ascontiguousarray((list(params) + [0.0, 0.0, 0.0])[:3], np.float32)
+        out = np.zeros((cap, 2), np.int32)
+        m = lib().ref_scene_overlap(self.h, _p(pose), int(type_), _p(prm), int(mesh), int(filt), _p(out), cap)
+        return [tuple(map(int, r)) for r in out[:min(m, cap)]]
 
     def collide(self, pairs):
         pairs = np.ascontiguousarray(pairs, np.int32).reshape(-1, 4)

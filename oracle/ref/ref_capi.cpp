@@ -11,6 +11,8 @@
  * (src/Physecs.cpp:134-172), the contact constraints (src/Physecs.cpp:274-314)
  * and the per-collider bounds (src/Physecs.cpp:79-90).
  */
+#include <unordered_map>
+#include <functional>
 #include "Physecs.h"
 #include "Components.h"
 #include "Transform.h"
@@ -318,6 +320,53 @@ int ref_scene_joint_colors(void* h, int32_t* out, int cap) {
         }
     }
     return n;
+}
+
+// Scene::raycastClosest for n rays of 8 floats {unused, origin xyz, dir xyz, max
+// distance}.  accept: per body (nonzero where the filter accepts the body's entity), or
+// NULL for the overload without a filter.  Per ray: the body (-1: entt::null) and the
+// hit position the reference reports.
+void ref_scene_raycast(void* h, int n, const float* rays, const uint8_t* accept, int32_t* out_body, float* out_pos) {
+    auto* w = static_cast<RefWorld*>(h);
+    std::unordered_map<uint32_t, int> index;
+    for (size_t b = 0; b < w->entities.size(); ++b) index[(uint32_t)w->entities[b]] = (int)b;
+    std::function<bool(entt::entity)> filter = [&](entt::entity e) {
+        auto it = index.find((uint32_t)e);
+        return it != index.end() && accept[it->second] != 0;
+    };
+    for (int i = 0; i < n; ++i) {
+        const float* r = rays + 8 * i;
+        glm::vec3 o(r[1], r[2], r[3]), d(r[4], r[5], r[6]), hit(0.f);
+        entt::entity e = accept ? w->scene->raycastClosest(o, d, r[7], filter, &hit) : w->scene->raycastClosest(o, d, r[7], &hit);
+        out_body[i] = e == entt::null ? -1 : index[(uint32_t)e];
+        out_pos[3 * i] = hit.x; out_pos[3 * i + 1] = hit.y; out_pos[3 * i + 2] = hit.z;
+    }
+}
+
+// Scene::overlap for one shape {pos xyz, quat xyzw}, type, params, convex mesh index and
+// data filter: up to cap (body, collider) pairs in the reference's order; returns the count
+int ref_scene_overlap(void* h, const float* pose, int type, const float* params, int mesh, int filter, int32_t* out, int cap) {
+    auto* w = static_cast<RefWorld*>(h);
+    std::unordered_map<uint32_t, int> index;
+    for (size_t b = 0; b < w->entities.size(); ++b) index[(uint32_t)w->entities[b]] = (int)b;
+    physecs::Geometry g{};
+    switch (type) {
+        case PSX_SPHERE: g.type = physecs::SPHERE; g.sphere = {params[0]}; break;
+        case PSX_CAPSULE: g.type = physecs::CAPSULE; g.capsule = {params[0], params[1]}; break;
+        case PSX_BOX: g.type = physecs::BOX; g.box = {glm::vec3(params[0], params[1], params[2])}; break;
+        case PSX_CONVEX_MESH:
+            g.type = physecs::CONVEX_MESH;
+            g.convex.mesh = w->convex[mesh].get();
+            g.convex.scale = glm::vec3(params[0], params[1], params[2]);
+            break;
+        default: return 0;
+    }
+    auto hits = w->scene->overlap(v3(pose), glm::quat(pose[6], pose[3], pose[4], pose[5]), g, filter);
+    for (int k = 0; k < (int)hits.size() && k < cap; ++k) {
+        out[2 * k] = index[(uint32_t)hits[k].entity];
+        out[2 * k + 1] = hits[k].colIndex;
+    }
+    return (int)hits.size();
 }
 
 }  // extern "C"

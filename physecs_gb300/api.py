@@ -27,7 +27,7 @@ EXPORTS = ["psx_world_create", "psx_world_destroy", "psx_world_step", "psx_world
            "psx_server_create", "psx_server_destroy", "psx_server_admit", "psx_server_tick", "psx_server_read",
            "psx_server_release", "psx_server_stats", "psx_server_tick_begin", "psx_server_tick_end", "psx_server_world",
            "psx_server_tick_stages", "psx_server_device_bytes",
-           "psx_world_tune", "psx_world_launch_config"]
+           "psx_world_tune", "psx_world_launch_config", "psx_world_raycast", "psx_world_overlap"]
 
 _lib = None
 
@@ -225,6 +225,49 @@ class World:
         b = np.zeros((n, 6), np.float32)
         load().psx_world_get_bounds(self.h, _p(b), n)
         return b
+
+    def raycast(self, rays, accept=None):
+        """psx_world_raycast.  rays: (n, 8) float rows {scene, origin xyz, dir xyz, max
+        distance}; accept: one value per world body (nonzero: the filter accepts its
+        entity) or None for every entity.  Returns {body, collider, entity, distance, pos}
+        arrays; body -1 where a ray hits nothing."""
+        rays = np.asarray(rays, np.float64).reshape(-1, 8)
+        n = len(rays)
+        buf = np.zeros((n, 8), np.float32)
+        buf[:, 1:] = rays[:, 1:]
+        buf.view(np.int32)[:, 0] = rays[:, 0].astype(np.int32)
+        out = np.zeros((max(n, 1), 7), np.float32)   # psx_ray_hit: 7 words
+        acc = None if accept is None else np.ascontiguousarray(accept, np.uint8)
+        _check(load().psx_world_raycast(self.h, n, _p(buf), _p(acc) if acc is not None else None, _p(out)))
+        out = out[:n]
+        iv = out.view(np.int32)
+        return {"body": iv[:, 0].copy(), "collider": iv[:, 1].copy(), "entity": out.view(np.uint32)[:, 2].copy(),
+                "distance": out[:, 3].copy(), "pos": out[:, 4:7].copy()}
+
+    def overlap(self, queries, cap=64):
+        """psx_world_overlap.  queries: list of dicts {scene, pos, quat, type, params,
+        mesh (convex index within the scene), filter}.  Returns (counts, hits): hits[i] is
+        a list of (body, collider, entity) for query i, at most cap of them."""
+        n = len(queries)
+        buf = np.zeros((max(n, 1), 14), np.float32)
+        iv = buf.view(np.int32)
+        for i, q in enumerate(queries):
+            iv[i, 0] = q["scene"]
+            buf[i, 1:4] = q["pos"]
+            buf[i, 4:8] = q.get("quat", (0.0, 0.0, 0.0, 1.0))
+            iv[i, 8] = q["type"]
+            prm = list(q.get("params", (0.0, 0.0, 0.0))) + [0.0, 0.0, 0.0]
+            buf[i, 9:12] = prm[:3]
+            iv[i, 12] = q.get("mesh", -1)
+            iv[i, 13] = q.get("filter", 0)
+        hits = np.zeros((max(n * cap, 1), 3), np.int32)
+        counts = np.zeros(max(n, 1), np.int32)
+        _check(load().psx_world_overlap(self.h, n, _p(buf), cap, _p(hits), _p(counts)))
+        res = []
+        for i in range(n):
+            m = min(int(counts[i]), cap)
+            res.append([(int(b), int(c), int(np.uint32(e))) for b, c, e in hits[i * cap:i * cap + m]])
+        return counts[:n].copy(), res
 
 
 class Server:

@@ -208,8 +208,12 @@ __global__ void k_karras(World w, FrameBuf f) {
 
 // a disabled collider never pairs: it contributes empty bounds to its tree nodes, so a
 // subtree holding only disabled colliders is pruned at its root
+// ALL: every collider with its bounds (scene queries reach colliders that do not
+// simulate, as the reference's query tree holds every collider); otherwise a collider
+// with enableSimulation off gets empty bounds and pairs with nothing
+template <bool ALL>
 __device__ __forceinline__ void leaf_bounds(const World& w, int c, float4& mn, float4& mx) {
-    if (w.col_info[c].w & COL_ENABLE) {
+    if (ALL || (w.col_info[c].w & COL_ENABLE)) {
         mn = w.aabb_min[c];
         mx = w.aabb_max[c];
     } else {
@@ -218,6 +222,7 @@ __device__ __forceinline__ void leaf_bounds(const World& w, int c, float4& mn, f
     }
 }
 
+template <bool ALL>
 __global__ void k_refit(World w, FrameBuf f) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= w.n_colliders) return;
@@ -231,9 +236,9 @@ __global__ void k_refit(World w, FrameBuf f) {
         __threadfence();
         int L = f.bvh.left[node], R = f.bvh.right[node];
         float4 lmin, lmax, rmin, rmax;
-        if (L < 0) leaf_bounds(w, f.order[~L], lmin, lmax);
+        if (L < 0) leaf_bounds<ALL>(w, f.order[~L], lmin, lmax);
         else { lmin = __ldcg(&f.bvh.bmin[L]); lmax = __ldcg(&f.bvh.bmax[L]); }
-        if (R < 0) leaf_bounds(w, f.order[~R], rmin, rmax);
+        if (R < 0) leaf_bounds<ALL>(w, f.order[~R], rmin, rmax);
         else { rmin = __ldcg(&f.bvh.bmin[R]); rmax = __ldcg(&f.bvh.bmax[R]); }
         f.bvh.bmin[node] = make_float4(fminf(lmin.x, rmin.x), fminf(lmin.y, rmin.y), fminf(lmin.z, rmin.z), 0.f);
         f.bvh.bmax[node] = make_float4(fmaxf(lmax.x, rmax.x), fmaxf(lmax.y, rmax.y), fmaxf(lmax.z, rmax.z), 0.f);
@@ -371,7 +376,9 @@ __global__ void __launch_bounds__(256) k_scene_sort(World w, FrameBuf f, int pma
     }
 }
 
-int launch_broadphase(const World& w, FrameBuf& f, int scene_bits, int scene_sort_pmax, cudaStream_t s) {
+// Each scene's LBVH over the colliders' current bounds: scene bounds, Morton codes, the
+// per-scene sort, Karras' construction and the bottom-up refit.
+int launch_bvh_build(const World& w, FrameBuf& f, int scene_bits, int scene_sort_pmax, bool all_leaves, cudaStream_t s) {
     int n = w.n_colliders;
     if (n == 0) return 0;
     int nb = (n + 255) / 256;
@@ -392,7 +399,16 @@ int launch_broadphase(const World& w, FrameBuf& f, int scene_bits, int scene_sor
         ++k;
     }
     k_karras<<<nb, 256, 0, s>>>(w, f);
-    k_refit<<<nb, 256, 0, s>>>(w, f);
+    if (all_leaves) k_refit<true><<<nb, 256, 0, s>>>(w, f);
+    else k_refit<false><<<nb, 256, 0, s>>>(w, f);
+    return k + 2;
+}
+
+int launch_broadphase(const World& w, FrameBuf& f, int scene_bits, int scene_sort_pmax, cudaStream_t s) {
+    int n = w.n_colliders;
+    if (n == 0) return 0;
+    int nb = (n + 255) / 256;
+    int k = launch_bvh_build(w, f, scene_bits, scene_sort_pmax, false, s) - 2;
     k_traverse<false><<<nb, 256, 0, s>>>(w, f);
     scan_exclusive(f.leaf_cnt, f.leaf_off, n, f.n_pairs, f.scan_scratch, s);
     k_traverse<true><<<nb, 256, 0, s>>>(w, f);

@@ -83,6 +83,23 @@ int launch_aabb_range(const World& w, int c0, int c1, int margin_mode, cudaStrea
 // scene_sort_pmax > 0: every scene has at most that many colliders (a power of two) and
 // is sorted by its own block in shared memory; 0: one radix sort over the whole world
 int launch_broadphase(const World& w, FrameBuf& f, int scene_bits, int scene_sort_pmax, cudaStream_t s);
+// each scene's LBVH over the current bounds (all_leaves: every collider reachable, for queries)
+int launch_bvh_build(const World& w, FrameBuf& f, int scene_bits, int scene_sort_pmax, bool all_leaves, cudaStream_t s);
+
+// scene queries (query.cu); the layouts are psx_ray and psx_overlap_query of include/psx.h
+struct RayIn { int scene; float ox, oy, oz, dx, dy, dz, maxd; };
+struct RayOut { int collider; float dist; };   // world collider index or -1
+struct ShapeIn {
+    int scene;
+    float px, py, pz, qx, qy, qz, qw;
+    int type;
+    float p0, p1, p2;
+    int mesh;     // world convex mesh index
+    int filter;   // collider data bits (0: any)
+};
+int launch_raycast(const World& w, FrameBuf& f, const RayIn* rays, int n, const unsigned char* accept, RayOut* out,
+                   cudaStream_t s);
+int launch_overlap(const World& w, FrameBuf& f, const ShapeIn* qs, int n, int cap, int* counts, int* hits, cudaStream_t s);
 // a second stream with a fork / join event pair, for kernels that may overlap
 struct StreamPair {
     cudaStream_t aux;

@@ -17,6 +17,17 @@ struct GeomD {
 
 __device__ __forceinline__ V3 gv(const GeomD& g) { return {g.p[0], g.p[1], g.p[2]}; }
 
+// world pose and geometry of collider c: transform.position + transform.orientation *
+// collider.position, transform.orientation * collider.orientation (src/Physecs.cpp:195-198)
+__device__ __forceinline__ void collider_pose(const World& w, int c, V3& pos, Q4& ori, GeomD& g) {
+    int4 ci = w.col_info[c];
+    Q4 bq = ld4(w.quat[ci.x]);
+    pos = ld3(w.pos[ci.x]) + qrot(bq, ld3(w.col_pos[c]));
+    ori = qmul(bq, ld4(w.col_quat[c]));
+    float4 pr = w.col_params[c];
+    g = GeomD{ci.y, {pr.x, pr.y, pr.z}, ci.z};
+}
+
 // ---------------------------------------------------------------- bounds (BoundsUtil.cpp:23-85)
 
 __device__ inline Bounds getBounds(const World& w, V3 pos, Q4 ori, const GeomD& g) {

@@ -13,15 +13,6 @@
 
 namespace psx {
 
-__device__ __forceinline__ void collider_pose(const World& w, int c, V3& pos, Q4& ori, GeomD& g) {
-    int4 ci = w.col_info[c];
-    Q4 bq = ld4(w.quat[ci.x]);
-    pos = ld3(w.pos[ci.x]) + qrot(bq, ld3(w.col_pos[c]));
-    ori = qmul(bq, ld4(w.col_quat[c]));
-    float4 pr = w.col_params[c];
-    g = GeomD{ci.y, {pr.x, pr.y, pr.z}, ci.z};
-}
-
 __device__ __forceinline__ void store_manifold(Manifold& out, const ManifoldL& m, int pair) {
     out.n = st4(m.normal);
     for (int k = 0; k < 4; ++k) {

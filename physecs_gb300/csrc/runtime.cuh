@@ -40,6 +40,10 @@ struct psx_world {
     std::vector<uint32_t> h_entity;        // per body
     std::vector<int> h_body_dyn;           // per body: global dyn index or -1
     std::vector<int> h_col_local;          // per collider: index within its body
+    std::vector<int> h_col_body;           // per collider: world body index
+    std::vector<int> h_scene_convex;       // per scene (+1): first world convex mesh
+    void* qbuf = nullptr;                  // scene-query staging on the device
+    size_t qbuf_bytes = 0;
     std::vector<int> block_scenes_h, grid_scenes_h;
     int* block_scenes = nullptr;
     int* grid_scenes = nullptr;
@@ -101,6 +105,7 @@ struct psx_world {
         if (graph) cudaGraphExecDestroy(graph);
         for (void* p : allocs) cudaFree(p);
         if (pin) cudaFreeHost(pin);
+        if (qbuf) cudaFree(qbuf);
         if (ev_fork) cudaEventDestroy(ev_fork);
         if (ev_fork2) cudaEventDestroy(ev_fork2);
         if (ev_join2) cudaEventDestroy(ev_join2);

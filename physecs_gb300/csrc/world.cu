@@ -181,6 +181,7 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
         PSX_TRY(validate(d));
         int bbase = (int)pos.size(), cbase = (int)col_info.size(), dbase = (int)dyn_body.size();
         int mbase = (int)convex.size(), tbase = (int)trimesh.size(), jbase = (int)joints.size();
+        W->h_scene_convex.push_back(mbase);
         // convex meshes: vertex buffer padded to a multiple of four with the last vertex (src/ConvexMesh.cpp:3-11)
         for (int m = 0; m < d.n_convex; ++m) {
             ConvexMeshDev cm;
@@ -260,6 +261,7 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
                 col_mat.push_back(f4(d.col_material[3 * c], d.col_material[3 * c + 1], d.col_material[3 * c + 2],
                                      bits_as_float(d.col_data ? d.col_data[c] : 0)));
                 W->h_col_local.push_back(c - d.collider_start[b]);
+                W->h_col_body.push_back(bbase + b);
             }
         }
         // joints: the reference's greedy per-entity colour bitsets (src/Physecs.cpp:690-710);
@@ -334,6 +336,7 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
     std::sort(nc.begin(), nc.end(), [](int2 a, int2 b) { return a.x < b.x || (a.x == b.x && a.y < b.y); });
     nc.erase(std::unique(nc.begin(), nc.end(), [](int2 a, int2 b) { return a.x == b.x && a.y == b.y; }), nc.end());
     W->h_scene_body = scene_body;
+    W->h_scene_convex.push_back((int)convex.size());
     W->h_scene_col = scene_col;
     W->h_scene_dyn = scene_dyn;
     World& w = W->w;

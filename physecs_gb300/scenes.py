@@ -400,13 +400,17 @@ _HULL_UNIT = {}
 
 
 def _hull_unit_props(mesh):
-    """Unit-scale mass, COM and inverse inertia (column-major) of a pool hull; cached."""
+    """Unit-scale mass, COM and inverse inertia (column-major) of a pool hull; cached.
+    The entry holds the mesh itself, so its id cannot be reused by another mesh while
+    the entry lives."""
     key = id(mesh)
-    if key not in _HULL_UNIT:
+    hit = _HULL_UNIT.get(key)
+    if hit is None or hit[0] is not mesh:
         verts, faces = mesh
         m, com, I = mass_convex(verts, faces, (1.0, 1.0, 1.0))
-        _HULL_UNIT[key] = (m, com, np.linalg.inv(I).T.ravel())
-    return _HULL_UNIT[key]
+        hit = (mesh, (m, com, np.linalg.inv(I).T.ravel()))
+        _HULL_UNIT[key] = hit
+    return hit[1]
 
 
 def _mixed_bodies(s: SceneData, rng: SplitMix64, centers: np.ndarray, hull_base: int, hull_pool,

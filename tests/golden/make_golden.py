@@ -9,6 +9,8 @@ oracle/ref/build_ref.py) on seeded scenes from physecs_gb300.scenes:
                        and body state after selected frames, for whole scenes
   narrow_pairs.npz     manifolds of physecs::collision for every shape pair at
                        seeded touching poses (known-answer tests)
+  queries.npz          Scene::raycastClosest and Scene::overlap answers on stepped
+                       scenes for seeded rays and shapes
 
 Run in a checkout with the reference present:  python tests/golden/make_golden.py
 """
@@ -104,6 +106,79 @@ def narrow_kat():
     return out
 
 
+def query_scenes():
+    """name -> (scene, frames stepped before the queries)."""
+    sys.path.insert(0, os.path.dirname(HERE))
+    from scene_variants import flagged_scene
+    return {
+        "mixed": (scenes.batch_scene(12, n_bodies=200), 30),
+        "flagged": (flagged_scene(), 10),
+        "heightfield": (scenes.large_mixed(n_bodies=300, cells=32), 5),
+    }
+
+
+def query_inputs(s, pos, seed):
+    """Seeded rays (8 floats: unused, origin, dir, max distance) aimed at bodies, a
+    quarter of them exactly vertical and some starting inside a body; a per-body accept
+    table; and overlap shapes of every kind around bodies."""
+    rng = scenes.SplitMix64(0x5EED0000 + seed)
+    nb = len(pos)
+    n = 256
+    tgt = pos[(rng.uniform(n) * nb).astype(int) % nb] + 0.6 * rng.normal(3 * n).reshape(n, 3)
+    org = tgt + np.array([0.0, 15.0, 0.0]) + 2.0 * rng.normal(3 * n).reshape(n, 3)
+    d = tgt - org
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    vert = np.arange(n) % 4 == 0
+    org[vert] = tgt[vert] + np.array([0.0, 15.0, 0.0])
+    d[vert] = np.array([0.0, -1.0, 0.0])
+    inside = np.arange(n) % 16 == 1
+    org[inside] = pos[(np.arange(n)[inside] * 7) % nb]
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, 1:4], rays[:, 4:7] = org, d
+    rays[:, 7] = rng.uniform(n, 4.0, 40.0)
+    accept = (rng.uniform(nb) < 0.8).astype(np.uint8)
+    m = 96
+    kinds = (np.arange(m) % 4).astype(np.int32)
+    if not s.convex:
+        kinds[kinds == 3] = 2
+    qpos = pos[(rng.uniform(m) * nb).astype(int) % nb] + 0.7 * rng.normal(3 * m).reshape(m, 3)
+    qquat = rng.quaternions(m)
+    prm = np.zeros((m, 3), np.float32)
+    u = rng.uniform(3 * m).reshape(m, 3)
+    prm[kinds == 0, 0] = 0.2 + 1.3 * u[kinds == 0, 0]
+    prm[kinds == 1, 0] = 0.2 + 0.8 * u[kinds == 1, 0]
+    prm[kinds == 1, 1] = 0.1 + 0.5 * u[kinds == 1, 1]
+    prm[kinds == 2] = 0.2 + 1.0 * u[kinds == 2]
+    prm[kinds == 3] = 0.5 + u[kinds == 3]
+    mesh = np.where(kinds == 3, 0, -1).astype(np.int32)
+    filt = np.where(np.arange(m) % 3 == 2, 1, 0).astype(np.int32)
+    return rays, accept, qpos.astype(np.float32), qquat.astype(np.float32), kinds, prm, mesh, filt
+
+
+def query_fixture():
+    from oracle.ref.ref_api import RefScene
+    out = {}
+    for si, (name, (s, frames)) in enumerate(query_scenes().items()):
+        r = RefScene(s)
+        for _ in range(frames):
+            r.step()
+        rays, accept, qpos, qquat, kinds, prm, mesh, filt = query_inputs(s, r.state()["pos"], 500 + si)
+        hit = r.raycast(rays, accept)
+        nohit = r.raycast(rays, None)
+        starts, flat = [0], []
+        for k in range(len(kinds)):
+            hs = sorted(r.overlap(qpos[k], qquat[k], kinds[k], prm[k], mesh[k], filt[k]))
+            flat.extend(hs)
+            starts.append(len(flat))
+        pre = name + "__"
+        out.update({pre + "scene_sha256": np.array(scene_hash(s)), pre + "frames": np.array(frames, np.int32),
+                    pre + "rays": rays, pre + "accept": accept, pre + "ray_body": hit["body"], pre + "ray_pos": hit["pos"],
+                    pre + "ray_body_nofilter": nohit["body"], pre + "q_pos": qpos, pre + "q_quat": qquat,
+                    pre + "q_type": kinds, pre + "q_params": prm, pre + "q_mesh": mesh, pre + "q_filter": filt,
+                    pre + "q_start": np.asarray(starts, np.int32), pre + "q_hits": np.asarray(flat, np.int32).reshape(-1, 2)})
+    return out
+
+
 def main():
     from oracle.ref import build_ref, ref_api
     if not ref_api.available():
@@ -130,6 +205,8 @@ def main():
         print(name, "ok")
     np.savez_compressed(os.path.join(HERE, "narrow_pairs.npz"), **narrow_kat())
     print("narrow_pairs ok")
+    np.savez_compressed(os.path.join(HERE, "queries.npz"), **query_fixture())
+    print("queries ok")
 
 
 if __name__ == "__main__":
