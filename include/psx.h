@@ -275,6 +275,20 @@ typedef struct psx_overlap_hit {
  * is the reference's; the order is this world's tree order. */
 PSX_API psx_status psx_world_overlap(psx_world* w, int32_t n, const psx_overlap_query* queries, int32_t cap,
                                      psx_overlap_hit* hits, int32_t* counts);
+
+typedef struct psx_overlap_mtd_hit {
+    int32_t body;       /* scene-local body index */
+    int32_t collider;   /* collider index within that body */
+    uint32_t entity;
+    float normal[3];    /* the collision's normal, from the collider towards the query shape */
+    float mtd;          /* max(0, deepest dot(p0 - p1, normal) over the manifold's points) */
+} psx_overlap_mtd_hit;
+/* Scene::overlapWithMinTranslationalDistance(pos, ori, geometry) for n shapes
+ * (src/Physecs.cpp:653-688): one record per manifold with points of the collision
+ * between each collider and the shape (a triangle mesh yields one per touching
+ * triangle manifold).  Layout as psx_world_overlap; the filter field is not used. */
+PSX_API psx_status psx_world_overlap_mtd(psx_world* w, int32_t n, const psx_overlap_query* queries, int32_t cap,
+                                         psx_overlap_mtd_hit* hits, int32_t* counts);
 /* counts[12] = {bodies, colliders, dynamic bodies, joints, scenes, pairs, manifolds, error bits,
  *              contact points, joint rows, simulated bodies, kernels queued since creation}
  * (per-frame values describe the last frame) */

@@ -208,4 +208,25 @@ int orc_scene_overlap(void* h, const float* pose, int type, const float* params,
     return (int)hits.size();
 }
 
+// Scene::overlapWithMinTranslationalDistance for one shape: up to cap records of
+// (body, collider) in out_ids and (normal xyz, mtd) in out_f; returns the number found
+int orc_scene_overlap_mtd(void* h, const float* pose, int type, const float* params, int mesh, int32_t* out_ids, float* out_f,
+                          int cap) {
+    World* w = static_cast<World*>(h);
+    Geometry g;
+    g.type = type;
+    g.p[0] = params[0]; g.p[1] = params[1]; g.p[2] = params[2];
+    if (type == CONVEX_MESH) g.convex = w->convex[mesh].get();
+    if (type == TRIANGLE_MESH) return 0;
+    std::vector<World::MtdHit> hits;
+    w->overlapMtd(v3(pose[0], pose[1], pose[2]), Q4{pose[3], pose[4], pose[5], pose[6]}, g, hits);
+    for (int k = 0; k < (int)hits.size() && k < cap; ++k) {
+        int c = hits[k].col;
+        out_ids[2 * k] = w->colliders[c].body;
+        out_ids[2 * k + 1] = c - w->bodies[w->colliders[c].body].firstCol;
+        out_f[4 * k] = hits[k].n.x; out_f[4 * k + 1] = hits[k].n.y; out_f[4 * k + 2] = hits[k].n.z; out_f[4 * k + 3] = hits[k].mtd;
+    }
+    return (int)hits.size();
+}
+
 }  // extern "C"

@@ -297,4 +297,27 @@ void World::overlap(V3 pos, Q4 ori, const Geometry& g, int filter, std::vector<i
     std::sort(out.begin(), out.end());
 }
 
+// Scene::overlapWithMinTranslationalDistance (src/Physecs.cpp:653-688): the collision of
+// every collider whose bounds meet the shape's (collider first), one record per manifold
+// with points, its deepest point max(0, dot(p0 - p1, n))
+void World::overlapMtd(V3 pos, Q4 ori, const Geometry& g, std::vector<MtdHit>& out) const {
+    const Bounds qb = getBounds(pos, ori, g);
+    out.clear();
+    for (const BPEntry& e : bp) {
+        const int c = bodies[e.body].firstCol + e.col;
+        if (!boundsMeet(qb, e.b)) continue;
+        std::vector<Manifold> res;
+        if (!collision(colPos(c), colQ(c), colliders[c].g, pos, ori, g, res)) continue;
+        for (const Manifold& m : res) {
+            if (!m.numPoints) continue;
+            float mtd = 0;
+            for (int i = 0; i < m.numPoints; ++i) {
+                float dist = dot(m.points[i].p0 - m.points[i].p1, m.normal);
+                if (dist > mtd) mtd = dist;
+            }
+            out.push_back({c, m.normal, mtd});
+        }
+    }
+}
+
 }  // namespace orc

@@ -129,6 +129,9 @@ struct World {
     // accept: per body, NULL for all) and the colliders a shape overlaps, ascending
     int raycastClosest(V3 o, V3 d, float maxd, const uint8_t* accept, float& dist) const;
     void overlap(V3 pos, Q4 ori, const Geometry& g, int filter, std::vector<int>& out) const;
+    // Scene::overlapWithMinTranslationalDistance: (collider, normal, mtd) per manifold with points
+    struct MtdHit { int col; V3 n; float mtd; };
+    void overlapMtd(V3 pos, Q4 ori, const Geometry& g, std::vector<MtdHit>& out) const;
 };
 
 }  // namespace orc

@@ -47,6 +47,8 @@ def lib():
         _lib.orc_scene_contact_keys.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
         _lib.orc_scene_raycast.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.orc_scene_overlap.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int]
+        _lib.orc_scene_overlap_mtd.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                               C.c_int]
     return _lib
 
 
@@ -137,6 +139,16 @@ class OracleScene:
         out = np.zeros((cap, 2), np.int32)
         m = lib().orc_scene_overlap(self.h, _p(pose), int(type_), _p(prm), int(mesh), int(filt), _p(out), cap)
         return [tuple(map(int, r)) for r in out[:min(m, cap)]]
+
+    def overlap_mtd(self, pos, quat, type_, params, mesh=-1, cap=4096):
+        """Scene::overlapWithMinTranslationalDistance for one shape: list of
+        (body, collider, normal (3,), mtd)."""
+        pose = np.ascontiguousarray(list(pos) + list(quat), np.float32)
+        prm = np.ascontiguousarray((list(params) + [0.0, 0.0, 0.0])[:3], np.float32)
+        ids = np.zeros((cap, 2), np.int32)
+        f = np.zeros((cap, 4), np.float32)
+        m = lib().orc_scene_overlap_mtd(self.h, _p(pose), int(type_), _p(prm), int(mesh), _p(ids), _p(f), cap)
+        return [(int(ids[k, 0]), int(ids[k, 1]), f[k, :3].copy(), f[k, 3]) for k in range(min(m, cap))]
 
     def collide(self, pairs):
         pairs = np.ascontiguousarray(pairs, np.int32).reshape(-1, 4)

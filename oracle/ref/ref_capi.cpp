@@ -369,4 +369,33 @@ int ref_scene_overlap(void* h, const float* pose, int type, const float* params,
     return (int)hits.size();
 }
 
+// Scene::overlapWithMinTranslationalDistance for one shape: up to cap records of
+// (body, collider) and (normal xyz, mtd) in the reference's order; returns the count
+int ref_scene_overlap_mtd(void* h, const float* pose, int type, const float* params, int mesh, int32_t* out_ids, float* out_f,
+                          int cap) {
+    auto* w = static_cast<RefWorld*>(h);
+    std::unordered_map<uint32_t, int> index;
+    for (size_t b = 0; b < w->entities.size(); ++b) index[(uint32_t)w->entities[b]] = (int)b;
+    physecs::Geometry g{};
+    switch (type) {
+        case PSX_SPHERE: g.type = physecs::SPHERE; g.sphere = {params[0]}; break;
+        case PSX_CAPSULE: g.type = physecs::CAPSULE; g.capsule = {params[0], params[1]}; break;
+        case PSX_BOX: g.type = physecs::BOX; g.box = {glm::vec3(params[0], params[1], params[2])}; break;
+        case PSX_CONVEX_MESH:
+            g.type = physecs::CONVEX_MESH;
+            g.convex.mesh = w->convex[mesh].get();
+            g.convex.scale = glm::vec3(params[0], params[1], params[2]);
+            break;
+        default: return 0;
+    }
+    auto hits = w->scene->overlapWithMinTranslationalDistance(v3(pose), glm::quat(pose[6], pose[3], pose[4], pose[5]), g);
+    for (int k = 0; k < (int)hits.size() && k < cap; ++k) {
+        out_ids[2 * k] = index[(uint32_t)hits[k].entity];
+        out_ids[2 * k + 1] = hits[k].colIndex;
+        out_f[4 * k] = hits[k].normal.x; out_f[4 * k + 1] = hits[k].normal.y; out_f[4 * k + 2] = hits[k].normal.z;
+        out_f[4 * k + 3] = hits[k].mtd;
+    }
+    return (int)hits.size();
+}
+
 }  // extern "C"

@@ -27,7 +27,8 @@ EXPORTS = ["psx_world_create", "psx_world_destroy", "psx_world_step", "psx_world
            "psx_server_create", "psx_server_destroy", "psx_server_admit", "psx_server_tick", "psx_server_read",
            "psx_server_release", "psx_server_stats", "psx_server_tick_begin", "psx_server_tick_end", "psx_server_world",
            "psx_server_tick_stages", "psx_server_device_bytes",
-           "psx_world_tune", "psx_world_launch_config", "psx_world_raycast", "psx_world_overlap"]
+           "psx_world_tune", "psx_world_launch_config", "psx_world_raycast", "psx_world_overlap",
+           "psx_world_overlap_mtd"]
 
 _lib = None
 
@@ -267,6 +268,38 @@ class World:
         for i in range(n):
             m = min(int(counts[i]), cap)
             res.append([(int(b), int(c), int(np.uint32(e))) for b, c, e in hits[i * cap:i * cap + m]])
+        return counts[:n].copy(), res
+
+    @staticmethod
+    def _shapes(queries):
+        n = len(queries)
+        buf = np.zeros((max(n, 1), 14), np.float32)
+        iv = buf.view(np.int32)
+        for i, q in enumerate(queries):
+            iv[i, 0] = q["scene"]
+            buf[i, 1:4] = q["pos"]
+            buf[i, 4:8] = q.get("quat", (0.0, 0.0, 0.0, 1.0))
+            iv[i, 8] = q["type"]
+            prm = list(q.get("params", (0.0, 0.0, 0.0))) + [0.0, 0.0, 0.0]
+            buf[i, 9:12] = prm[:3]
+            iv[i, 12] = q.get("mesh", -1)
+            iv[i, 13] = q.get("filter", 0)
+        return buf
+
+    def overlap_mtd(self, queries, cap=64):
+        """psx_world_overlap_mtd.  queries as overlap (the filter is not used).  Returns
+        (counts, hits): hits[i] is a list of (body, collider, entity, normal (3,), mtd)."""
+        n = len(queries)
+        buf = self._shapes(queries)
+        hits = np.zeros((max(n * cap, 1), 7), np.float32)   # psx_overlap_mtd_hit: 7 words
+        counts = np.zeros(max(n, 1), np.int32)
+        _check(load().psx_world_overlap_mtd(self.h, n, _p(buf), cap, _p(hits), _p(counts)))
+        iv, uv = hits.view(np.int32), hits.view(np.uint32)
+        res = []
+        for i in range(n):
+            m = min(int(counts[i]), cap)
+            res.append([(int(iv[k, 0]), int(iv[k, 1]), int(uv[k, 2]), hits[k, 3:6].copy(), hits[k, 6])
+                        for k in range(i * cap, i * cap + m)])
         return counts[:n].copy(), res
 
 

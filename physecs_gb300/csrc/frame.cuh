@@ -100,6 +100,8 @@ struct ShapeIn {
 int launch_raycast(const World& w, FrameBuf& f, const RayIn* rays, int n, const unsigned char* accept, RayOut* out,
                    cudaStream_t s);
 int launch_overlap(const World& w, FrameBuf& f, const ShapeIn* qs, int n, int cap, int* counts, int* hits, cudaStream_t s);
+int launch_overlap_mtd(const World& w, FrameBuf& f, const ShapeIn* qs, int n, int cap, int* counts, float4* hits,
+                       int* hit_col, cudaStream_t s);
 // a second stream with a fork / join event pair, for kernels that may overlap
 struct StreamPair {
     cudaStream_t aux;

@@ -13,6 +13,7 @@
 // order; the set is the same).
 #include "frame.cuh"
 #include "narrow_convex.cuh"
+#include "narrow_tri.cuh"
 
 namespace psx {
 
@@ -391,6 +392,114 @@ __global__ void k_overlap(World w, FrameBuf f, const ShapeIn* qs, int n, int cap
     counts[i] = count;
 }
 
+// physecs::collision (Collision.cpp:895-1016) for one pair in one thread: the triangle-
+// mesh routine (its manifolds flipped when the mesh is the first shape), the convex
+// routine (GJK, EPA and face clipping, with the convex mesh second) or the analytic
+// one.  Up to kTriManifolds manifolds go to ms; returns their number.
+__device__ inline int collision_one(const World& w, V3 pos0, Q4 or0, GeomD g0, V3 pos1, Q4 or1, GeomD g1, ManifoldL* ms,
+                                    TCI* cand, Polytope& poly, int* err) {
+    if (g0.type == G_TRIMESH || g1.type == G_TRIMESH) {
+        if (g0.type == G_TRIMESH && g1.type == G_TRIMESH) return 0;
+        ManOut out{ms, 0, kTriManifolds, err};
+        const bool flip = g0.type == G_TRIMESH;
+        if (flip) collideTriMesh(w, pos1, or1, g1, pos0, or0, g0.mesh, out, cand, poly);
+        else collideTriMesh(w, pos0, or0, g0, pos1, or1, g1.mesh, out, cand, poly);
+        if (flip)
+            for (int k = 0; k < out.n; ++k) flipM(ms[k]);
+        return out.n;
+    }
+    if (g0.type == G_CONVEX || g1.type == G_CONVEX) {
+        const bool swap = g1.type != G_CONVEX;
+        if (swap) {
+            V3 tp = pos0; pos0 = pos1; pos1 = tp;
+            Q4 tq = or0; or0 = or1; or1 = tq;
+            GeomD tg = g0; g0 = g1; g1 = tg;
+        }
+        Support a, b;
+        convexOrderedSupports(w, pos0, or0, g0, pos1, or1, g1, a, b);
+        GjkSimplex s;
+        if (!gjk(a, b, pos1 - pos0, s)) return 0;
+        ManifoldL& r = ms[0];
+        r.numPoints = 0;
+        r.triangleIndex = -1;
+        V3 c0, c1;
+        r.normal = epa(a, b, s, c0, c1, poly, err);
+        r.points[0] = {c0, c1};
+        convexOrderedContacts(w, pos0, or0, g0, pos1, or1, g1, r, err);
+        if (swap) flipM(r);
+        return 1;
+    }
+    return collideAnalytic(pos0, or0, g0, pos1, or1, g1, ms[0], err) ? 1 : 0;
+}
+
+// Scene::overlapWithMinTranslationalDistance (src/Physecs.cpp:653-688): every collider
+// whose bounds meet the query shape's; for each manifold with points of the collision
+// (collider first, shape second) its normal and the deepest point, max(0, max over the
+// points of dot(p0 - p1, n)).  Up to cap records a query: {world collider, n xyz, mtd}.
+__global__ void __launch_bounds__(64) k_overlap_mtd(World w, FrameBuf f, const ShapeIn* qs, int n, int cap, int* counts,
+                                                    float4* hits, int* hit_col) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const ShapeIn qi = qs[i];
+    const V3 pos = {qi.px, qi.py, qi.pz};
+    const Q4 ori = {qi.qx, qi.qy, qi.qz, qi.qw};
+    const GeomD g = GeomD{qi.type, {qi.p0, qi.p1, qi.p2}, qi.mesh};
+    const Bounds b = getBounds(w, pos, ori, g);
+    const float4 qmin = make_float4(b.min.x, b.min.y, b.min.z, 0.f), qmax = make_float4(b.max.x, b.max.y, b.max.z, 0.f);
+    const int s = qi.scene;
+    const int cs = w.scene_col[s], nc = w.scene_col[s + 1] - cs;
+    ManifoldL ms[kTriManifolds];
+    TCI cand[kTriCandidates];
+    Polytope poly;
+    int count = 0;
+    auto leaf = [&](int q) {
+        const int c = f.order[q];
+        if (!boxes_meet(qmin, qmax, w.aabb_min[c], w.aabb_max[c])) return;
+        V3 cp;
+        Q4 co;
+        GeomD cg;
+        collider_pose(w, c, cp, co, cg);
+        const int nm = collision_one(w, cp, co, cg, pos, ori, g, ms, cand, poly, w.err);
+        for (int k = 0; k < nm; ++k) {
+            const ManifoldL& m = ms[k];
+            if (!m.numPoints) continue;
+            float mtd = 0.f;
+            for (int p = 0; p < m.numPoints; ++p) {
+                float dist = dot(m.points[p].p0 - m.points[p].p1, m.normal);
+                if (dist > mtd) mtd = dist;
+            }
+            if (count < cap) {
+                hits[(size_t)i * cap + count] = make_float4(m.normal.x, m.normal.y, m.normal.z, mtd);
+                hit_col[(size_t)i * cap + count] = c;
+            }
+            ++count;
+        }
+    };
+    if (nc == 1) {
+        leaf(cs);
+    } else if (nc > 1) {
+        int stack[64];
+        int sp = 0;
+        stack[sp++] = cs - s;
+        while (sp) {
+            const int c = stack[--sp];
+            if (c < 0) { leaf(~c); continue; }
+            if (!boxes_meet(qmin, qmax, f.bvh.bmin[c], f.bvh.bmax[c])) continue;
+            if (sp + 2 > 64) { atomicOr(w.err, ERR_STACK_CAPACITY); continue; }
+            stack[sp++] = f.bvh.right[c];
+            stack[sp++] = f.bvh.left[c];
+        }
+    }
+    counts[i] = count;
+}
+
+int launch_overlap_mtd(const World& w, FrameBuf& f, const ShapeIn* qs, int n, int cap, int* counts, float4* hits,
+                       int* hit_col, cudaStream_t s) {
+    if (n <= 0) return 0;
+    k_overlap_mtd<<<(n + 63) / 64, 64, 0, s>>>(w, f, qs, n, cap, counts, hits, hit_col);
+    return 1;
+}
+
 int launch_raycast(const World& w, FrameBuf& f, const RayIn* rays, int n, const unsigned char* accept, RayOut* out,
                    cudaStream_t s) {
     if (n <= 0) return 0;
@@ -430,6 +539,29 @@ psx_status query_buffer(psx_world* W, size_t bytes, char** out) {
 }
 
 size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+
+// the device form of n overlap queries: scene-local convex meshes become world meshes
+psx_status pack_shapes(psx_world* W, int n, const psx_overlap_query* queries, std::vector<ShapeIn>& in) {
+    in.resize(n);
+    for (int i = 0; i < n; ++i) {
+        const psx_overlap_query& q = queries[i];
+        if (q.scene < 0 || q.scene >= W->n_scenes) return fail(PSX_ERR_INVALID_ARG, "psx_world_overlap: scene index");
+        if (q.type < PSX_SPHERE || q.type > PSX_TRIANGLE_MESH) return fail(PSX_ERR_INVALID_ARG, "psx_world_overlap: shape type");
+        int mesh = -1;
+        if (q.type == PSX_CONVEX_MESH) {
+            const int m0 = W->h_scene_convex[q.scene], m1 = W->h_scene_convex[q.scene + 1];
+            if (q.mesh < 0 || m0 + q.mesh >= m1) return fail(PSX_ERR_INVALID_ARG, "psx_world_overlap: convex mesh index");
+            mesh = m0 + q.mesh;
+        }
+        // a triangle-mesh query overlaps nothing (Overlap.cpp:194-235); its count is set to 0
+        // on the host, and the device tests it as a sphere of radius 0
+        const bool tri = q.type == PSX_TRIANGLE_MESH;
+        in[i] = ShapeIn{q.scene, q.pos[0], q.pos[1], q.pos[2], q.quat[0], q.quat[1], q.quat[2], q.quat[3],
+                        tri ? PSX_SPHERE : q.type, tri ? 0.f : q.params[0], tri ? 0.f : q.params[1], tri ? 0.f : q.params[2],
+                        mesh, q.filter};
+    }
+    return PSX_OK;
+}
 
 // the trees the queries walk: every scene's LBVH over the current bounds, every collider a leaf
 void query_trees(psx_world* W) { launch_bvh_build(W->w, W->f, W->scene_bits, W->scene_sort_pmax, true, W->stream); }
@@ -486,24 +618,8 @@ PSX_API psx_status psx_world_overlap(psx_world* W, int32_t n, const psx_overlap_
         return fail(PSX_ERR_INVALID_ARG, "psx_world_overlap: bad arguments");
     PSX_CUDA(cudaSetDevice(W->device));
     if (n == 0) return PSX_OK;
-    std::vector<ShapeIn> in(n);
-    for (int i = 0; i < n; ++i) {
-        const psx_overlap_query& q = queries[i];
-        if (q.scene < 0 || q.scene >= W->n_scenes) return fail(PSX_ERR_INVALID_ARG, "psx_world_overlap: scene index");
-        if (q.type < PSX_SPHERE || q.type > PSX_TRIANGLE_MESH) return fail(PSX_ERR_INVALID_ARG, "psx_world_overlap: shape type");
-        int mesh = -1;
-        if (q.type == PSX_CONVEX_MESH) {
-            const int m0 = W->h_scene_convex[q.scene], m1 = W->h_scene_convex[q.scene + 1];
-            if (q.mesh < 0 || m0 + q.mesh >= m1) return fail(PSX_ERR_INVALID_ARG, "psx_world_overlap: convex mesh index");
-            mesh = m0 + q.mesh;
-        }
-        // a triangle-mesh query overlaps nothing (Overlap.cpp:194-235); its count is set to 0
-        // on the host, and the device tests it as a sphere of radius 0
-        const bool tri = q.type == PSX_TRIANGLE_MESH;
-        in[i] = ShapeIn{q.scene, q.pos[0], q.pos[1], q.pos[2], q.quat[0], q.quat[1], q.quat[2], q.quat[3],
-                        tri ? PSX_SPHERE : q.type, tri ? 0.f : q.params[0], tri ? 0.f : q.params[1], tri ? 0.f : q.params[2],
-                        mesh, q.filter};
-    }
+    std::vector<ShapeIn> in;
+    PSX_TRY(pack_shapes(W, n, queries, in));
     const size_t in_b = align256(sizeof(ShapeIn) * n), cnt_b = align256(sizeof(int) * n), hit_b = sizeof(int) * (size_t)n * cap;
     char* buf = nullptr;
     PSX_TRY(query_buffer(W, in_b + cnt_b + hit_b, &buf));
@@ -529,6 +645,53 @@ PSX_API psx_status psx_world_overlap(psx_world* W, int32_t n, const psx_overlap_
             h.body = b - W->h_scene_body[queries[i].scene];
             h.collider = W->h_col_local[c];
             h.entity = W->h_entity[b];
+        }
+    }
+    return PSX_OK;
+}
+
+PSX_API psx_status psx_world_overlap_mtd(psx_world* W, int32_t n, const psx_overlap_query* queries, int32_t cap,
+                                         psx_overlap_mtd_hit* hits, int32_t* counts) {
+    if (!W || n < 0 || cap < 0 || (n && (!queries || !counts || (cap && !hits))))
+        return fail(PSX_ERR_INVALID_ARG, "psx_world_overlap_mtd: bad arguments");
+    PSX_CUDA(cudaSetDevice(W->device));
+    if (n == 0) return PSX_OK;
+    std::vector<ShapeIn> in;
+    PSX_TRY(pack_shapes(W, n, queries, in));
+    const size_t in_b = align256(sizeof(ShapeIn) * n), cnt_b = align256(sizeof(int) * n);
+    const size_t f4_b = align256(sizeof(float4) * (size_t)n * cap), col_b = sizeof(int) * (size_t)n * cap;
+    char* buf = nullptr;
+    PSX_TRY(query_buffer(W, in_b + cnt_b + f4_b + col_b, &buf));
+    ShapeIn* d_in = reinterpret_cast<ShapeIn*>(buf);
+    int* d_cnt = reinterpret_cast<int*>(buf + in_b);
+    float4* d_f = reinterpret_cast<float4*>(buf + in_b + cnt_b);
+    int* d_col = reinterpret_cast<int*>(buf + in_b + cnt_b + f4_b);
+    cudaStream_t st = W->stream;
+    PSX_CUDA(cudaMemcpyAsync(d_in, in.data(), sizeof(ShapeIn) * n, cudaMemcpyHostToDevice, st));
+    query_trees(W);
+    launch_overlap_mtd(W->w, W->f, d_in, n, cap, d_cnt, d_f, d_col, st);
+    std::vector<int> cnt(n), col((size_t)n * cap);
+    std::vector<float4> fv((size_t)n * cap);
+    PSX_CUDA(cudaMemcpyAsync(cnt.data(), d_cnt, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+    if (cap) {
+        PSX_CUDA(cudaMemcpyAsync(fv.data(), d_f, sizeof(float4) * (size_t)n * cap, cudaMemcpyDeviceToHost, st));
+        PSX_CUDA(cudaMemcpyAsync(col.data(), d_col, col_b, cudaMemcpyDeviceToHost, st));
+    }
+    PSX_CUDA(cudaStreamSynchronize(st));
+    PSX_TRY(check_err(W));
+    for (int i = 0; i < n; ++i) {
+        counts[i] = queries[i].type == PSX_TRIANGLE_MESH ? 0 : cnt[i];
+        const int m = std::min(counts[i], cap);
+        for (int k = 0; k < m; ++k) {
+            const size_t j = (size_t)i * cap + k;
+            const int c = col[j];
+            const int b = W->h_col_body[c];
+            psx_overlap_mtd_hit& h = hits[j];
+            h.body = b - W->h_scene_body[queries[i].scene];
+            h.collider = W->h_col_local[c];
+            h.entity = W->h_entity[b];
+            h.normal[0] = fv[j].x; h.normal[1] = fv[j].y; h.normal[2] = fv[j].z;
+            h.mtd = fv[j].w;
         }
     }
     return PSX_OK;

@@ -155,6 +155,12 @@ def query_inputs(s, pos, seed):
     return rays, accept, qpos.astype(np.float32), qquat.astype(np.float32), kinds, prm, mesh, filt
 
 
+def mtd_sorted(hits):
+    """overlapWithMinTranslationalDistance records in a canonical order (the reference
+    lists them in its tree's order): by body, collider, then the float bits."""
+    return sorted(hits, key=lambda h: (h[0], h[1], tuple(np.asarray(list(h[2]) + [h[3]], np.float32).view(np.uint32))))
+
+
 def query_fixture():
     from oracle.ref.ref_api import RefScene
     out = {}
@@ -170,12 +176,20 @@ def query_fixture():
             hs = sorted(r.overlap(qpos[k], qquat[k], kinds[k], prm[k], mesh[k], filt[k]))
             flat.extend(hs)
             starts.append(len(flat))
+        mstarts, mids, mf = [0], [], []
+        for k in range(len(kinds)):
+            for b, c, nrm, mtd in mtd_sorted(r.overlap_mtd(qpos[k], qquat[k], kinds[k], prm[k], mesh[k])):
+                mids.append((b, c))
+                mf.append(list(nrm) + [mtd])
+            mstarts.append(len(mids))
         pre = name + "__"
         out.update({pre + "scene_sha256": np.array(scene_hash(s)), pre + "frames": np.array(frames, np.int32),
                     pre + "rays": rays, pre + "accept": accept, pre + "ray_body": hit["body"], pre + "ray_pos": hit["pos"],
                     pre + "ray_body_nofilter": nohit["body"], pre + "q_pos": qpos, pre + "q_quat": qquat,
                     pre + "q_type": kinds, pre + "q_params": prm, pre + "q_mesh": mesh, pre + "q_filter": filt,
-                    pre + "q_start": np.asarray(starts, np.int32), pre + "q_hits": np.asarray(flat, np.int32).reshape(-1, 2)})
+                    pre + "q_start": np.asarray(starts, np.int32), pre + "q_hits": np.asarray(flat, np.int32).reshape(-1, 2),
+                    pre + "mtd_start": np.asarray(mstarts, np.int32), pre + "mtd_ids": np.asarray(mids, np.int32).reshape(-1, 2),
+                    pre + "mtd_f": np.asarray(mf, np.float32).reshape(-1, 4)})
     return out
 
 

@@ -69,6 +69,19 @@ def _check_scene(g, o, d, pre, scene, body0, nbodies_world, min_hits=50):
         assert sorted((b, c) for b, c, _ in h) == sorted(want), k
         total += len(want)
     assert total >= min_hits
+    counts, hits = g.overlap_mtd(_queries(d, pre, scene), cap=256)
+    total = 0
+    for k, h in enumerate(hits):
+        want = make_golden.mtd_sorted(o.overlap_mtd(d[pre + "q_pos"][k], d[pre + "q_quat"][k], d[pre + "q_type"][k],
+                                                    d[pre + "q_params"][k], d[pre + "q_mesh"][k]))
+        got = make_golden.mtd_sorted([(b, c, n, m) for b, c, _, n, m in h])
+        assert counts[k] == len(want)
+        assert [(x[0], x[1]) for x in got] == [(x[0], x[1]) for x in want], k
+        fg = np.asarray([list(x[2]) + [x[3]] for x in got], np.float32).reshape(-1, 4)
+        fw = np.asarray([list(x[2]) + [x[3]] for x in want], np.float32).reshape(-1, 4)
+        assert np.array_equal(fg.view(np.uint32), fw.view(np.uint32)), k
+        total += len(want)
+    assert total >= min_hits
 
 
 @pytest.mark.parametrize("name", list(make_golden.query_scenes()))

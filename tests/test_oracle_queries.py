@@ -54,6 +54,14 @@ def test_oracle_queries_match_reference_fixture(oracle_lib, name):
         want = [tuple(map(int, r)) for r in flat[st[k]:st[k + 1]]]
         assert g == want, k
     assert st[-1] > 100
+    ms, mids, mf = d[pre + "mtd_start"], d[pre + "mtd_ids"], d[pre + "mtd_f"]
+    for k in range(len(d[pre + "q_type"])):
+        got = make_golden.mtd_sorted(o.overlap_mtd(d[pre + "q_pos"][k], d[pre + "q_quat"][k], d[pre + "q_type"][k],
+                                                   d[pre + "q_params"][k], d[pre + "q_mesh"][k]))
+        assert [(b, c) for b, c, _, _ in got] == [tuple(map(int, r)) for r in mids[ms[k]:ms[k + 1]]], k
+        gf = np.asarray([list(n) + [m] for _, _, n, m in got], np.float32).reshape(-1, 4)
+        assert np.array_equal(gf.view(np.uint32), mf[ms[k]:ms[k + 1]].view(np.uint32)), k
+    assert ms[-1] > 100
 
 
 def test_reference_raycast_without_filter_never_hits():
@@ -84,3 +92,9 @@ def test_oracle_queries_match_live_reference(oracle_lib):
             a = sorted(o.overlap(qpos[k], qquat[k], kinds[k], prm[k], mesh[k], filt[k]))
             b = sorted(r.overlap(qpos[k], qquat[k], kinds[k], prm[k], mesh[k], filt[k]))
             assert a == b, (name, k)
+            a = make_golden.mtd_sorted(o.overlap_mtd(qpos[k], qquat[k], kinds[k], prm[k], mesh[k]))
+            b = make_golden.mtd_sorted(r.overlap_mtd(qpos[k], qquat[k], kinds[k], prm[k], mesh[k]))
+            assert [(x[0], x[1]) for x in a] == [(x[0], x[1]) for x in b], (name, k)
+            fa = np.asarray([list(x[2]) + [x[3]] for x in a], np.float32).reshape(-1, 4)
+            fb = np.asarray([list(x[2]) + [x[3]] for x in b], np.float32).reshape(-1, 4)
+            assert np.array_equal(fa.view(np.uint32), fb.view(np.uint32)), (name, k)
