@@ -289,6 +289,36 @@ typedef struct psx_overlap_mtd_hit {
  * triangle manifold).  Layout as psx_world_overlap; the filter field is not used. */
 PSX_API psx_status psx_world_overlap_mtd(psx_world* w, int32_t n, const psx_overlap_query* queries, int32_t cap,
                                          psx_overlap_mtd_hit* hits, int32_t* counts);
+/* Trigger events: Scene::simulate's onTriggerEnter / onTriggerExit callbacks
+ * (src/Physecs.cpp:537-552; listeners registered by addOnTriggerEnterCallback /
+ * addOnTriggerExitCallback, :772-786).  With the default contact filter
+ * (src/Physecs.cpp:20-23) a broadphase pair with a trigger collider is a trigger pair:
+ * its colliders are tested with physecs::overlap, and a pair overlapping in a frame but
+ * not in the frame before enters, a pair overlapping in the frame before but not in this
+ * one exits (src/Physecs.cpp:200-207).  A pair's colliders are in the broadphase's order
+ * (the lower entity first), as the reference passes them. */
+#define PSX_TRIGGER_ENTER 0
+#define PSX_TRIGGER_EXIT 1
+typedef struct psx_trigger_event {
+    int32_t frame;      /* frame that raised it: frames stepped before it since the world's creation */
+    int32_t kind;       /* PSX_TRIGGER_ENTER or PSX_TRIGGER_EXIT */
+    int32_t scene;
+    int32_t body0;      /* scene-local body index */
+    int32_t collider0;  /* collider index within that body */
+    int32_t body1;
+    int32_t collider1;
+    uint32_t entity0;
+    uint32_t entity1;
+} psx_trigger_event;
+/* Delivers the trigger events of the frames stepped since the last call (waits for the
+ * world's stream): up to cap events into out, ordered by frame, then enter before exit
+ * (the reference's order), then scene, bodies and colliders (the reference's order within
+ * a frame is its hash set's); events past cap stay queued for the next call.  n_lost
+ * (optional) receives the events dropped since the last call because more than the
+ * device log's capacity (2 x the pair capacity, at least 4096) piled up between two
+ * calls.  A world without trigger colliders delivers none. */
+PSX_API psx_status psx_world_trigger_events(psx_world* w, psx_trigger_event* out, int32_t cap, int32_t* n_out,
+                                            int64_t* n_lost);
 /* counts[12] = {bodies, colliders, dynamic bodies, joints, scenes, pairs, manifolds, error bits,
  *              contact points, joint rows, simulated bodies, kernels queued since creation}
  * (per-frame values describe the last frame) */

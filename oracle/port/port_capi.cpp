@@ -229,4 +229,20 @@ int orc_scene_overlap_mtd(void* h, const float* pose, int type, const float* par
     return (int)hits.size();
 }
 
+// The trigger events of the frames stepped since the last call, in step order: up to
+// cap records of (frame, kind 0 enter / 1 exit, body0, collider0, body1, collider1),
+// removed from the scene; returns the number pending before the call
+int orc_scene_trigger_events(void* h, int32_t* out, int cap) {
+    World* w = static_cast<World*>(h);
+    const int n = (int)w->triggerEvents.size();
+    const int m = n < cap ? n : cap;
+    for (int k = 0; k < m; ++k) {
+        const World::TriggerEvent& e = w->triggerEvents[k];
+        int32_t* o = out + 6 * k;
+        o[0] = e.frame; o[1] = e.kind; o[2] = e.body0; o[3] = e.col0; o[4] = e.body1; o[5] = e.col1;
+    }
+    w->triggerEvents.erase(w->triggerEvents.begin(), w->triggerEvents.begin() + m);
+    return n;
+}
+
 }  // extern "C"

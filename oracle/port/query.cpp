@@ -300,6 +300,10 @@ void World::overlap(V3 pos, Q4 ori, const Geometry& g, int filter, std::vector<i
 // Scene::overlapWithMinTranslationalDistance (src/Physecs.cpp:653-688): the collision of
 // every collider whose bounds meet the shape's (collider first), one record per manifold
 // with points, its deepest point max(0, dot(p0 - p1, n))
+bool World::overlapColliders(V3 pos0, Q4 or0, int c0, V3 pos1, Q4 or1, int c1) const {
+    return overlapGeom(pos0, or0, colliders[c0].g, pos1, or1, colliders[c1].g);
+}
+
 void World::overlapMtd(V3 pos, Q4 ori, const Geometry& g, std::vector<MtdHit>& out) const {
     const Bounds qb = getBounds(pos, ori, g);
     out.clear();

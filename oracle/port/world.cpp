@@ -163,6 +163,7 @@ void World::broadphase() {
 void World::narrowphase() {
     contacts.clear();
     cacheTemp.clear();
+    triggerCacheTemp.clear();
     int np = (int)pairs.size() / 4;
     std::vector<Manifold> buf;
     for (int idx = np - 1; idx >= 0; --idx) {
@@ -176,7 +177,12 @@ void World::narrowphase() {
         Q4 or0 = qmul(B0.q, C0.q);
         V3 pos1 = B1.pos + qrot(B1.q, C1.pos);
         Q4 or1 = qmul(B1.q, C1.q);
-        if (C0.trigger || C1.trigger) continue;  // trigger pairs are outside the simulated path
+        // the default contact filter makes a pair with a trigger a TRIGGER pair: an overlap
+        // test, no contact, ahead of the jointed-pair filter (Physecs.cpp:20-23, 200-207)
+        if (C0.trigger || C1.trigger) {
+            if (overlapColliders(pos0, or0, c0, pos1, or1, c1)) triggerCacheTemp.insert({bA, cA, bB, cB});
+            continue;
+        }
         if (nonColliding.count({B0.entity, B1.entity})) continue;
         buf.clear();
         if (!collision(pos0, or0, C0.g, pos1, or1, C1.g, buf)) continue;
@@ -716,6 +722,13 @@ void World::step(float dt) {
             B.ang = vt[i].w;
         }
     }
+    // enter: in this frame's set only; exit: in the last frame's only (Physecs.cpp:537-552)
+    for (const auto& k : triggerCacheTemp)
+        if (!triggerCache.count(k)) triggerEvents.push_back({frame, 0, k[0], k[1], k[2], k[3]});
+    for (const auto& k : triggerCache)
+        if (!triggerCacheTemp.count(k)) triggerEvents.push_back({frame, 1, k[0], k[1], k[2], k[3]});
+    triggerCache.swap(triggerCacheTemp);
+    ++frame;
     cache.swap(cacheTemp);
     for (size_t i = 0; i < nd; ++i) {
         int b = dynBodies[i];

@@ -3,8 +3,10 @@
  * ORACLE (test infrastructure only; see omath.h).
  */
 #pragma once
+#include <array>
 #include <map>
 #include <memory>
+#include <set>
 #include <tuple>
 #include <vector>
 #include "geom.h"
@@ -106,6 +108,13 @@ struct World {
     std::vector<int> pairs;                    // last frame: {body0, col0, body1, col1} (desc indices / local collider)
     std::vector<Contact> contacts;
     std::map<CacheKey, CacheVal> cache, cacheTemp;
+    // trigger pairs (Physecs.cpp:200-207, 537-552): the overlapping trigger pairs of the
+    // last frame and of this one, {body0, collider0, body1, collider1}, and the enter (kind 0)
+    // and exit (kind 1) events of every frame stepped, in step order
+    std::set<std::array<int, 4>> triggerCache, triggerCacheTemp;
+    struct TriggerEvent { int frame, kind, body0, col0, body1, col1; };
+    std::vector<TriggerEvent> triggerEvents;
+    int frame = 0;
     std::vector<Velocity> vt;
     std::vector<Pseudo> pv;
     std::vector<Mass> mt;
@@ -132,6 +141,8 @@ struct World {
     // Scene::overlapWithMinTranslationalDistance: (collider, normal, mtd) per manifold with points
     struct MtdHit { int col; V3 n; float mtd; };
     void overlapMtd(V3 pos, Q4 ori, const Geometry& g, std::vector<MtdHit>& out) const;
+    // physecs::overlap of two colliders at the given world poses (the trigger test)
+    bool overlapColliders(V3 pos0, Q4 or0, int c0, V3 pos1, Q4 or1, int c1) const;
 };
 
 }  // namespace orc

@@ -49,6 +49,7 @@ def lib():
         _lib.orc_scene_overlap.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int]
         _lib.orc_scene_overlap_mtd.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
                                                C.c_int]
+        _lib.orc_scene_trigger_events.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
     return _lib
 
 
@@ -149,6 +150,16 @@ class OracleScene:
         f = np.zeros((cap, 4), np.float32)
         m = lib().orc_scene_overlap_mtd(self.h, _p(pose), int(type_), _p(prm), int(mesh), _p(ids), _p(f), cap)
         return [(int(ids[k, 0]), int(ids[k, 1]), f[k, :3].copy(), f[k, 3]) for k in range(min(m, cap))]
+
+    def trigger_events(self):
+        """Drain the trigger events of the frames stepped so far: an (n, 6) int32 array of
+        (frame, kind 0 enter / 1 exit, body0, collider0, body1, collider1), in step order."""
+        out = np.zeros((0, 6), np.int32)
+        n = lib().orc_scene_trigger_events(self.h, None, 0)
+        if n:
+            out = np.zeros((n, 6), np.int32)
+            lib().orc_scene_trigger_events(self.h, _p(out), n)
+        return out
 
     def collide(self, pairs):
         pairs = np.ascontiguousarray(pairs, np.int32).reshape(-1, 4)

@@ -42,12 +42,28 @@ template physecs::ConvexMeshVertices<4>::ConvexMeshVertices(const std::vector<gl
 
 namespace {
 
+// Records the scene's onTriggerEnter / onTriggerExit callbacks (src/Physecs.cpp:537-552)
+// as (frame, kind 0 enter / 1 exit, body0, collider0, body1, collider1), bodies as desc
+// indices.
+struct TriggerRecorder : physecs::OnTriggerEnterListener, physecs::OnTriggerExitListener {
+    std::unordered_map<uint32_t, int> body_of;
+    std::vector<int32_t> events;
+    int frame = 0;
+    void record(int kind, entt::entity e0, int c0, entt::entity e1, int c1) {
+        const int32_t r[6] = {frame, kind, body_of.at((uint32_t)e0), c0, body_of.at((uint32_t)e1), c1};
+        events.insert(events.end(), r, r + 6);
+    }
+    void onTriggerEnter(entt::entity e0, int c0, entt::entity e1, int c1) override { record(0, e0, c0, e1, c1); }
+    void onTriggerExit(entt::entity e0, int c0, entt::entity e1, int c1) override { record(1, e0, c0, e1, c1); }
+};
+
 struct RefWorld {
     entt::registry registry;
     std::unique_ptr<physecs::Scene> scene;
     std::vector<entt::entity> entities;
     std::vector<std::unique_ptr<physecs::ConvexMesh>> convex;
     std::vector<std::unique_ptr<physecs::TriangleMesh>> trimesh;
+    TriggerRecorder triggers;
 };
 
 glm::vec3 v3(const float* p) { return glm::vec3(p[0], p[1], p[2]); }
@@ -109,12 +125,15 @@ void* ref_scene_create(const psx_scene_desc* d, int num_threads) {
     w->scene->setNumSubSteps(d->num_substeps);
     w->scene->setNumIterations(d->num_iterations);
     w->scene->setGravity(d->gravity);
+    w->scene->addOnTriggerEnterCallback(&w->triggers);
+    w->scene->addOnTriggerExitCallback(&w->triggers);
     for (int b = 0; b < d->n_bodies; ++b) {
         entt::entity e = w->registry.create();
         if ((uint32_t)e != d->entity[b]) {
             std::fprintf(stderr, "ref_scene_create: entity %u != desc %u\n", (uint32_t)e, d->entity[b]);
         }
         w->entities.push_back(e);
+        w->triggers.body_of[(uint32_t)e] = b;
         w->registry.emplace<TransformComponent>(e, v3(d->pos + 3 * b), q4(d->quat + 4 * b), glm::vec3(1));
         std::vector<physecs::Collider> cols;
         for (int c = d->collider_start[b]; c < d->collider_start[b + 1]; ++c) cols.push_back(make_collider(*w, d, c));
@@ -178,7 +197,22 @@ void ref_scene_destroy(void* h) {
     delete w;
 }
 
-void ref_scene_step(void* h, float dt) { static_cast<RefWorld*>(h)->scene->simulate(dt); }
+void ref_scene_step(void* h, float dt) {
+    auto* w = static_cast<RefWorld*>(h);
+    w->scene->simulate(dt);
+    ++w->triggers.frame;
+}
+
+// The trigger callbacks recorded since the last call, in callback order: up to cap
+// records of 6 ints, removed; returns the number pending before the call
+int ref_scene_trigger_events(void* h, int32_t* out, int cap) {
+    auto& ev = static_cast<RefWorld*>(h)->triggers.events;
+    const int n = (int)ev.size() / 6;
+    const int m = n < cap ? n : cap;
+    if (m) std::memcpy(out, ev.data(), sizeof(int32_t) * 6 * m);
+    ev.erase(ev.begin(), ev.begin() + 6 * m);
+    return n;
+}
 
 void ref_scene_set_knobs(void* h, int substeps, int iterations, float gravity) {
     auto* w = static_cast<RefWorld*>(h);

@@ -28,7 +28,7 @@ EXPORTS = ["psx_world_create", "psx_world_destroy", "psx_world_step", "psx_world
            "psx_server_release", "psx_server_stats", "psx_server_tick_begin", "psx_server_tick_end", "psx_server_world",
            "psx_server_tick_stages", "psx_server_device_bytes",
            "psx_world_tune", "psx_world_launch_config", "psx_world_raycast", "psx_world_overlap",
-           "psx_world_overlap_mtd"]
+           "psx_world_overlap_mtd", "psx_world_trigger_events"]
 
 _lib = None
 
@@ -98,6 +98,7 @@ def load():
     lib.psx_server_tick_end.argtypes = [vp, vp, C.c_int32, vp]
     lib.psx_server_read.argtypes = [vp, C.c_int32, vp, vp, vp, vp]
     lib.psx_server_release.argtypes = [vp, C.c_int32]
+    lib.psx_world_trigger_events.argtypes = [vp, vp, C.c_int32, vp, vp]
     lib.psx_server_stats.argtypes = [vp, vp]
     _lib = lib
     return lib
@@ -250,17 +251,7 @@ class World:
         mesh (convex index within the scene), filter}.  Returns (counts, hits): hits[i] is
         a list of (body, collider, entity) for query i, at most cap of them."""
         n = len(queries)
-        buf = np.zeros((max(n, 1), 14), np.float32)
-        iv = buf.view(np.int32)
-        for i, q in enumerate(queries):
-            iv[i, 0] = q["scene"]
-            buf[i, 1:4] = q["pos"]
-            buf[i, 4:8] = q.get("quat", (0.0, 0.0, 0.0, 1.0))
-            iv[i, 8] = q["type"]
-            prm = list(q.get("params", (0.0, 0.0, 0.0))) + [0.0, 0.0, 0.0]
-            buf[i, 9:12] = prm[:3]
-            iv[i, 12] = q.get("mesh", -1)
-            iv[i, 13] = q.get("filter", 0)
+        buf = self._shapes(queries)
         hits = np.zeros((max(n * cap, 1), 3), np.int32)
         counts = np.zeros(max(n, 1), np.int32)
         _check(load().psx_world_overlap(self.h, n, _p(buf), cap, _p(hits), _p(counts)))
@@ -301,6 +292,67 @@ class World:
             res.append([(int(iv[k, 0]), int(iv[k, 1]), int(uv[k, 2]), hits[k, 3:6].copy(), hits[k, 6])
                         for k in range(i * cap, i * cap + m)])
         return counts[:n].copy(), res
+
+    # ---------------------------------------------------------------- trigger events
+
+    def trigger_events(self, cap=4096):
+        """psx_world_trigger_events until the queue is empty.  Returns (events, lost):
+        events is an (n, 9) int64 array of (frame, kind 0 enter / 1 exit, scene, body0,
+        collider0, body1, collider1, entity0, entity1) in delivery order; lost counts the
+        events dropped because the device log overflowed between two drains."""
+        lib = load()
+        chunks, lost = [], 0
+        out = np.zeros((cap, 9), np.int32)   # psx_trigger_event: 9 words
+        n, nl = C.c_int32(), C.c_int64()
+        while True:
+            _check(lib.psx_world_trigger_events(self.h, _p(out), cap, C.byref(n), C.byref(nl)))
+            lost += nl.value
+            ev = out[:n.value].astype(np.int64)
+            ev[:, 7:9] = out[:n.value, 7:9].view(np.uint32)
+            chunks.append(ev)
+            if n.value < cap:
+                break
+        return np.concatenate(chunks), lost
+
+    def _listeners(self, kind, scene):
+        if not hasattr(self, "_trigger_listeners"):
+            self._trigger_listeners = ({}, {})
+        return self._trigger_listeners[kind].setdefault(scene, [])
+
+    def add_on_trigger_enter_callback(self, listener, scene=0):
+        """Scene::addOnTriggerEnterCallback (src/Physecs.cpp:772-774) for one scene of the
+        world: listener.on_trigger_enter(entity0, collider_index0, entity1, collider_index1)
+        runs for each pair of that scene that starts to overlap, from dispatch_trigger_events."""
+        self._listeners(0, scene).append(listener)
+
+    def add_on_trigger_exit_callback(self, listener, scene=0):
+        """Scene::addOnTriggerExitCallback (src/Physecs.cpp:776-778): listener.on_trigger_exit(...)."""
+        self._listeners(1, scene).append(listener)
+
+    def remove_on_trigger_enter_callback(self, listener, scene=0):
+        """Scene::removeOnTriggerEnterCallback (src/Physecs.cpp:780-782); ValueError if absent."""
+        self._listeners(0, scene).remove(listener)
+
+    def remove_on_trigger_exit_callback(self, listener, scene=0):
+        """Scene::removeOnTriggerExitCallback (src/Physecs.cpp:784-786); ValueError if absent."""
+        self._listeners(1, scene).remove(listener)
+
+    def dispatch_trigger_events(self):
+        """Drains the trigger events and calls the listeners as Scene::simulate does at the
+        end of each frame (src/Physecs.cpp:537-552): frame by frame, every entering pair
+        calls every enter listener of its scene in registration order, then every exiting
+        pair every exit listener.  Returns the drained events (see trigger_events); raises
+        PsxError after the dispatch when events were lost to the device log's capacity."""
+        ev, lost = self.trigger_events()
+        for _frame, kind, scene, _b0, c0, _b1, c1, e0, e1 in ev.tolist():
+            for ls in list(self._listeners(kind, scene)):
+                if kind == 0:
+                    ls.on_trigger_enter(e0, c0, e1, c1)
+                else:
+                    ls.on_trigger_exit(e0, c0, e1, c1)
+        if lost:
+            raise PsxError("psx CAPACITY: %d trigger events were lost before this drain" % lost)
+        return ev
 
 
 class Server:

@@ -36,10 +36,10 @@ struct FrameBuf {
     int* n_pairs;         // device scalar
     // narrowphase
     int* pair_cat;        // 0 analytic, 1 convex mesh, 2 triangle mesh
-    int* cat_count;       // [7]: analytic pairs without a box, convex, triangle-mesh pairs, convex pairs
+    int* cat_count;       // [8]: analytic pairs without a box, convex, triangle-mesh pairs, convex pairs
                           // that overlap, analytic pairs with one box, box-box pairs, overlapping convex
-                          // pairs whose EPA polytope outgrew the small one
-    int* cat_list;        // [7 * pair_cap]: the pairs of each list
+                          // pairs whose EPA polytope outgrew the small one, trigger pairs
+    int* cat_list;        // [8 * pair_cap]: the pairs of each list
     Manifold* man_pair;   // one slot per pair (analytic / convex categories)
     int tri_cap;          // triangle-mesh pair slots
     Manifold* man_tri;    // kTriManifolds slots per triangle-mesh pair slot
@@ -69,6 +69,19 @@ struct FrameBuf {
     CacheEntry* cache_a;
     CacheEntry* cache_b;
     int* cache_parity;
+    // trigger pairs (src/Physecs.cpp:200-207, 537-552); trig_cap is 0 when the world has no
+    // trigger collider.  Two sets alternate between frames, trig_state[0] selecting this
+    // frame's: the keys (collider0 << 32 | collider1) of the overlapping trigger pairs, as a
+    // list and in an open-addressing table (~0 = empty) that records each key's slot
+    int trig_cap;                          // = pair_cap: every trigger pair is a pair
+    int trig_table_cap;                    // power of two >= 2 * trig_cap
+    unsigned long long* trig_table[2];
+    unsigned long long* trig_keys[2];
+    int* trig_slot[2];
+    int* trig_state;                       // [4]: parity, keys in set 0, keys in set 1, frame
+    int evt_cap;
+    int4* trig_evt;                        // [evt_cap] (frame, 0 enter / 1 exit, collider0, collider1)
+    int* n_evt;                            // events since the host last drained them (may pass evt_cap)
     // grid barrier: count, generation, flag
     unsigned int* bar;
     // per-frame totals: contact points, joint rows (for throughput accounting)
@@ -116,6 +129,8 @@ struct NarrowShape {
     int epa_full_only;                        // EPA: skip the small-polytope pass
 };
 int launch_narrowphase(const World& w, FrameBuf& f, const StreamPair& sp, const NarrowShape& ns, cudaStream_t s);
+// trigger pairs of this frame: overlap tests, enter and exit events, set swap (query.cu)
+int launch_triggers(const World& w, FrameBuf& f, cudaStream_t s);
 int launch_contacts(const World& w, FrameBuf& f, cudaStream_t s);
 // scenes of one frame's solver launch: small block scenes (one 256-thread block each),
 // large block scenes (one 512-thread block each, on the aux stream), grid scenes

@@ -23,10 +23,12 @@ __device__ __forceinline__ void store_manifold(Manifold& out, const ManifoldL& m
     out.pair = pair;
 }
 
-// pair category and trigger / joint filters (src/Physecs.cpp:200-209)
 // Pair category and the trigger / jointed-pair filters (src/Physecs.cpp:200-209), appended
 // to the category lists with one atomic per warp and category.  A list's order decides
-// only which thread handles which pair: every pair writes its own manifold slots.
+// only which thread handles which pair: every pair writes its own manifold slots.  The
+// default contact filter makes every pair with a trigger collider a trigger pair, tested
+// for overlap only and ahead of the jointed-pair filter (list 7, when the world keeps
+// trigger sets).
 __global__ void k_classify(World w, FrameBuf f) {
     const int2* noncolliding = w.nc_pairs;
     const int n_nc = w.n_nc;
@@ -57,6 +59,7 @@ __global__ void k_classify(World w, FrameBuf f) {
                 else cat = 0;
             }
             f.pair_cat[p] = cat;
+            if (trigger && f.trig_cap) cat = 7;
             f.pair_nman[p] = 0;
             // analytic pairs go to three lists by their boxes (none, one, two), so that a
             // warp's pairs take the same path (box-box SAT and clipping cost the most)
@@ -65,7 +68,7 @@ __global__ void k_classify(World w, FrameBuf f) {
                 cat = boxes == 0 ? 0 : (boxes == 1 ? 4 : 5);
             }
         }
-        for (int c : {0, 1, 2, 4, 5}) {
+        for (int c : {0, 1, 2, 4, 5, 7}) {
             unsigned m = __ballot_sync(0xffffffffu, cat == c);
             if (!m) continue;
             int first = 0;
@@ -293,7 +296,7 @@ static void launch_convex_epa(const World& w, FrameBuf& f, int blocks_per_sm, cu
 // The convex kernels (bound by the FP64 pipe) run on the aux stream beside the analytic
 // and triangle-mesh kernels (FP32, latency-bound); the categories write disjoint slots.
 int launch_narrowphase(const World& w, FrameBuf& f, const StreamPair& sp, const NarrowShape& ns, cudaStream_t s) {
-    cudaMemsetAsync(f.cat_count, 0, 7 * sizeof(int), s);
+    cudaMemsetAsync(f.cat_count, 0, 8 * sizeof(int), s);
     k_classify<<<1216, 256, 0, s>>>(w, f);
     cudaEventRecord(sp.fork, s);
     cudaStreamWaitEvent(sp.aux, sp.fork, 0);
@@ -322,9 +325,10 @@ int launch_narrowphase(const World& w, FrameBuf& f, const StreamPair& sp, const 
     k_narrow_analytic<1><<<152 * ns.analytic_blocks_per_sm, ns.analytic_threads, 0, s>>>(w, f);
     k_narrow_analytic<0><<<152 * ns.analytic_blocks_per_sm, ns.analytic_threads, 0, s>>>(w, f);
     k_narrow_tri<<<1216, 64, 0, s>>>(w, f);
+    const int kt = launch_triggers(w, f, s);
     cudaStreamWaitEvent(s, sp.join, 0);
     scan_exclusive_dev(f.pair_nman, f.pair_moff, f.n_pairs, f.pair_cap, f.n_man, f.scan_scratch, s);
-    return 2 + 8 + 3;
+    return 2 + 8 + 3 + kt;
 }
 
 }  // namespace psx

@@ -513,10 +513,102 @@ int launch_overlap(const World& w, FrameBuf& f, const ShapeIn* qs, int n, int ca
     return 1;
 }
 
+// ---------------------------------------------------------------- trigger pairs
+//
+// Scene::simulate keeps the overlapping trigger pairs of a frame in a set, calls
+// onTriggerEnter for the pairs new to it and onTriggerExit for the pairs gone from it,
+// and swaps it with the last frame's (src/Physecs.cpp:200-207, 537-552).  Here the two
+// sets are key lists with open-addressing tables for the lookups; each key keeps its
+// table slot so that the last frame's table is emptied entry by entry, not swept.
+// Events go to a log that the host drains.
+
+constexpr unsigned long long kNoKey = ~0ull;
+
+__device__ __forceinline__ unsigned trig_hash(unsigned long long k) {
+    k ^= k >> 33; k *= 0xff51afd7ed558ccdull; k ^= k >> 33; k *= 0xc4ceb9fe1a85ec53ull; k ^= k >> 33;
+    return (unsigned)k;
+}
+
+// A table holds at most half its capacity, so every probe sequence meets an empty slot.
+__device__ __forceinline__ bool trig_find(const unsigned long long* t, unsigned mask, unsigned long long key) {
+    unsigned h = trig_hash(key) & mask;
+    for (unsigned probe = 0; probe <= mask; ++probe, h = (h + 1) & mask) {
+        const unsigned long long v = t[h];
+        if (v == key) return true;
+        if (v == kNoKey) return false;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void trig_event(const FrameBuf& f, int frame, int kind, unsigned long long key) {
+    const int i = atomicAdd(f.n_evt, 1);
+    if (i < f.evt_cap) f.trig_evt[i] = make_int4(frame, kind, (int)(key >> 32), (int)(unsigned)key);
+}
+
+// physecs::overlap of every trigger pair at this frame's poses; a pair that overlaps
+// joins this frame's set and, when the last frame's set lacks it, enters.
+__global__ void __launch_bounds__(128) k_trigger_enter(World w, FrameBuf f) {
+    const int cur = f.trig_state[0], frame = f.trig_state[3];
+    const unsigned mask = (unsigned)f.trig_table_cap - 1u;
+    const int n = f.cat_count[7];
+    unsigned long long* tab = f.trig_table[cur];
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int2 pr = f.pairs[f.cat_list[7 * (size_t)f.pair_cap + t]];
+        V3 pos0, pos1;
+        Q4 or0, or1;
+        GeomD g0, g1;
+        collider_pose(w, pr.x, pos0, or0, g0);
+        collider_pose(w, pr.y, pos1, or1, g1);
+        if (!overlapGeom(w, pos0, or0, g0, pos1, or1, g1)) continue;
+        const unsigned long long key = ((unsigned long long)(unsigned)pr.x << 32) | (unsigned)pr.y;
+        const int i = atomicAdd(&f.trig_state[1 + cur], 1);
+        if (i >= f.trig_cap) { atomicOr(w.err, ERR_PAIR_CAPACITY); continue; }
+        unsigned h = trig_hash(key) & mask;
+        for (unsigned probe = 0; probe <= mask; ++probe, h = (h + 1) & mask)
+            if (atomicCAS(&tab[h], kNoKey, key) == kNoKey) break;
+        f.trig_keys[cur][i] = key;
+        f.trig_slot[cur][i] = (int)h;
+        if (!trig_find(f.trig_table[cur ^ 1], mask, key)) trig_event(f, frame, 0, key);
+    }
+}
+
+// The last frame's pairs missing from this frame's set exit; the last frame's table is
+// emptied for the frame after.
+__global__ void __launch_bounds__(128) k_trigger_exit(FrameBuf f) {
+    const int cur = f.trig_state[0], prev = cur ^ 1, frame = f.trig_state[3];
+    const unsigned mask = (unsigned)f.trig_table_cap - 1u;
+    const int n = min(f.trig_state[1 + prev], f.trig_cap);
+    const unsigned long long* tab = f.trig_table[cur];
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const unsigned long long key = f.trig_keys[prev][t];
+        if (!trig_find(tab, mask, key)) trig_event(f, frame, 1, key);
+        f.trig_table[prev][f.trig_slot[prev][t]] = kNoKey;
+    }
+}
+
+// This frame's set becomes the last frame's; the emptied one takes the next frame's pairs.
+__global__ void k_trigger_swap(FrameBuf f) {
+    const int prev = f.trig_state[0] ^ 1;
+    f.trig_state[1 + prev] = 0;
+    f.trig_state[0] = prev;
+    f.trig_state[3] += 1;
+}
+
+int launch_triggers(const World& w, FrameBuf& f, cudaStream_t s) {
+    if (!f.trig_cap) return 0;
+    const int blocks = std::min(152 * 4, (f.trig_cap + 127) / 128);
+    k_trigger_enter<<<blocks, 128, 0, s>>>(w, f);
+    k_trigger_exit<<<blocks, 128, 0, s>>>(f);
+    k_trigger_swap<<<1, 1, 0, s>>>(f);
+    return 3;
+}
+
 }  // namespace psx
 
 // ---------------------------------------------------------------- C ABI
 
+#include <algorithm>
+#include <tuple>
 #include <vector>
 #include "runtime.cuh"
 
@@ -694,6 +786,54 @@ PSX_API psx_status psx_world_overlap_mtd(psx_world* W, int32_t n, const psx_over
             h.mtd = fv[j].w;
         }
     }
+    return PSX_OK;
+}
+
+PSX_API psx_status psx_world_trigger_events(psx_world* W, psx_trigger_event* out, int32_t cap, int32_t* n_out,
+                                            int64_t* n_lost) {
+    if (!W || cap < 0 || (cap && !out) || !n_out) return fail(PSX_ERR_INVALID_ARG, "psx_world_trigger_events: bad arguments");
+    PSX_CUDA(cudaSetDevice(W->device));
+    const FrameBuf& f = W->f;
+    if (f.trig_cap) {
+        cudaStream_t st = W->stream;
+        int n = 0;
+        PSX_CUDA(cudaMemcpyAsync(&n, f.n_evt, sizeof(int), cudaMemcpyDeviceToHost, st));
+        PSX_CUDA(cudaStreamSynchronize(st));
+        if (n) {
+            const int kept = std::min(n, f.evt_cap);
+            std::vector<int4> ev(kept);
+            PSX_CUDA(cudaMemcpyAsync(ev.data(), f.trig_evt, sizeof(int4) * kept, cudaMemcpyDeviceToHost, st));
+            PSX_CUDA(cudaMemsetAsync(f.n_evt, 0, sizeof(int), st));
+            PSX_CUDA(cudaStreamSynchronize(st));
+            W->trig_lost += n - kept;
+            std::vector<psx_trigger_event> batch(kept);
+            for (int i = 0; i < kept; ++i) {
+                const int c0 = ev[i].z, c1 = ev[i].w, b0 = W->h_col_body[c0], b1 = W->h_col_body[c1];
+                const int sc = (int)(std::upper_bound(W->h_scene_body.begin(), W->h_scene_body.end(), b0) -
+                                     W->h_scene_body.begin()) - 1;
+                psx_trigger_event& e = batch[i];
+                e.frame = ev[i].x;
+                e.kind = ev[i].y;
+                e.scene = sc;
+                e.body0 = b0 - W->h_scene_body[sc];
+                e.collider0 = W->h_col_local[c0];
+                e.body1 = b1 - W->h_scene_body[sc];
+                e.collider1 = W->h_col_local[c1];
+                e.entity0 = W->h_entity[b0];
+                e.entity1 = W->h_entity[b1];
+            }
+            auto key = [](const psx_trigger_event& e) {
+                return std::make_tuple(e.frame, e.kind, e.scene, e.body0, e.collider0, e.body1, e.collider1);
+            };
+            std::sort(batch.begin(), batch.end(), [&](const psx_trigger_event& a, const psx_trigger_event& b) { return key(a) < key(b); });
+            W->trig_pending.insert(W->trig_pending.end(), batch.begin(), batch.end());
+        }
+    }
+    const int m = (int)std::min<size_t>((size_t)cap, W->trig_pending.size());
+    std::copy(W->trig_pending.begin(), W->trig_pending.begin() + m, out);
+    W->trig_pending.erase(W->trig_pending.begin(), W->trig_pending.begin() + m);
+    *n_out = m;
+    if (n_lost) { *n_lost = W->trig_lost; W->trig_lost = 0; }
     return PSX_OK;
 }
 

@@ -43,6 +43,8 @@ struct psx_world {
     std::vector<int> h_col_body;           // per collider: world body index
     std::vector<int> h_scene_convex;       // per scene (+1): first world convex mesh
     void* qbuf = nullptr;                  // scene-query staging on the device
+    std::vector<psx_trigger_event> trig_pending;   // drained from the device, not yet delivered
+    long long trig_lost = 0;               // events past the device log's capacity
     size_t qbuf_bytes = 0;
     std::vector<int> block_scenes_h, grid_scenes_h;
     int* block_scenes = nullptr;

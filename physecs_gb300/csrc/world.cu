@@ -425,8 +425,8 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
     PSX_TRY(W->alloc(f.pairs, f.pair_cap));
     PSX_TRY(W->alloc(f.n_pairs, 1));
     PSX_TRY(W->alloc(f.pair_cat, f.pair_cap));
-    PSX_TRY(W->alloc(f.cat_count, 7));
-    PSX_TRY(W->alloc(f.cat_list, 7 * (size_t)f.pair_cap));
+    PSX_TRY(W->alloc(f.cat_count, 8));
+    PSX_TRY(W->alloc(f.cat_list, 8 * (size_t)f.pair_cap));
     PSX_TRY(W->alloc(f.man_pair, f.pair_cap));
     PSX_TRY(W->alloc(f.man_tri, (size_t)f.tri_cap * kTriManifolds));
     PSX_TRY(W->alloc(f.pair_tslot, f.pair_cap));
@@ -462,6 +462,25 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
     PSX_CUDA(cudaMemset(f.n_pairs, 0, sizeof(int)));
     PSX_CUDA(cudaMemset(f.n_man, 0, sizeof(int)));
     PSX_CUDA(cudaMemset(f.scene_man, 0, sizeof(int) * (S + 1)));
+    // trigger sets and the event log, for a world with trigger colliders only
+    bool any_trigger = false;
+    for (const int4& ci : col_info) any_trigger |= (ci.w & COL_TRIGGER) && (ci.w & COL_ENABLE);
+    if (any_trigger) {
+        f.trig_cap = f.pair_cap;
+        f.trig_table_cap = 1 << ilog2ceil(2 * f.trig_cap);
+        f.evt_cap = std::max(4096, 2 * f.trig_cap);
+        for (int k = 0; k < 2; ++k) {
+            PSX_TRY(W->alloc(f.trig_table[k], f.trig_table_cap));
+            PSX_TRY(W->alloc(f.trig_keys[k], f.trig_cap));
+            PSX_TRY(W->alloc(f.trig_slot[k], f.trig_cap));
+            PSX_CUDA(cudaMemset(f.trig_table[k], 0xff, sizeof(unsigned long long) * (size_t)f.trig_table_cap));
+        }
+        PSX_TRY(W->alloc(f.trig_state, 4));
+        PSX_TRY(W->alloc(f.trig_evt, f.evt_cap));
+        PSX_TRY(W->alloc(f.n_evt, 1));
+        PSX_CUDA(cudaMemset(f.trig_state, 0, 4 * sizeof(int)));
+        PSX_CUDA(cudaMemset(f.n_evt, 0, sizeof(int)));
+    }
     // shared memory per solver block: the most a block may have when there are at most as
     // many block scenes as SMs, else a size that keeps two blocks resident per SM (the
     // register budget of the 256-thread solver allows two)

@@ -11,6 +11,8 @@ oracle/ref/build_ref.py) on seeded scenes from physecs_gb300.scenes:
                        seeded touching poses (known-answer tests)
   queries.npz          Scene::raycastClosest and Scene::overlap answers on stepped
                        scenes for seeded rays and shapes
+  triggers.npz         the onTriggerEnter / onTriggerExit callbacks of stepped scenes
+                       with trigger colliders
 
 Run in a checkout with the reference present:  python tests/golden/make_golden.py
 """
@@ -193,6 +195,37 @@ def query_fixture():
     return out
 
 
+def trigger_scenes():
+    """name -> (scene, frames stepped)."""
+    sys.path.insert(0, os.path.dirname(HERE))
+    from scene_variants import flagged_scene, trigger_scene
+    return {
+        "zones_a": (trigger_scene(41), 120),
+        "zones_b": (trigger_scene(42), 120),
+        "flagged": (flagged_scene(), 60),
+    }
+
+
+def events_sorted(ev):
+    """Trigger events (frame, kind, body0, collider0, body1, collider1) in a canonical
+    order: the reference calls them in its hash set's order within a frame."""
+    ev = np.asarray(ev, np.int32).reshape(-1, 6)
+    return ev[np.lexsort(ev.T[::-1])] if len(ev) else ev
+
+
+def trigger_fixture():
+    from oracle.ref.ref_api import RefScene
+    out = {}
+    for name, (s, frames) in trigger_scenes().items():
+        r = RefScene(s)
+        for _ in range(frames):
+            r.step()
+        pre = name + "__"
+        out.update({pre + "scene_sha256": np.array(scene_hash(s)), pre + "frames": np.array(frames, np.int32),
+                    pre + "events": events_sorted(r.trigger_events())})
+    return out
+
+
 def main():
     from oracle.ref import build_ref, ref_api
     if not ref_api.available():
@@ -221,6 +254,8 @@ def main():
     print("narrow_pairs ok")
     np.savez_compressed(os.path.join(HERE, "queries.npz"), **query_fixture())
     print("queries ok")
+    np.savez_compressed(os.path.join(HERE, "triggers.npz"), **trigger_fixture())
+    print("triggers ok")
 
 
 if __name__ == "__main__":

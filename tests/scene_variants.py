@@ -33,3 +33,31 @@ def apart_scene():
     """Two dynamic spheres far apart: pairs but no manifold."""
     return scenes.pair_scene(scenes.SPHERE, [0.5], ([0, 5, 0], scenes.IDENTITY_Q), scenes.SPHERE, [0.5],
                              ([10, 5, 0], scenes.IDENTITY_Q))
+
+
+def trigger_scene(seed=41, n=90):
+    """Trigger volumes in the path of falling bodies: four static trigger colliders (a
+    box slab, a sphere, a capsule and a convex hull) above a ground box, mixed dynamic
+    bodies dropped through them, a few dynamic bodies that are triggers themselves (they
+    fall through everything, the ground included) and a jointed capsule chain with a
+    trigger link (a trigger pair is tested ahead of the jointed-pair filter)."""
+    rng = scenes.SplitMix64(scenes.scene_seed(9, seed))
+    s = scenes.SceneData("triggers%d" % seed)
+    scenes._ground_box(s, (9.0, 0.5, 9.0))
+    pool = scenes._hull_pool(scenes.SplitMix64(scenes.scene_seed(9, 1 << 19)), count=4)
+    s.convex.extend(pool)
+    q = rng.quaternions(4)
+    s.add_bodies(pos=[[0.0, 3.0, 0.0], [4.5, 1.5, 4.5], [-4.5, 1.5, -4.5], [4.5, 1.5, -4.5]], quat=q, flags=0,
+                 inv_mass=0.0, com=np.zeros(3), inv_inertia=np.zeros(9),
+                 col_type=[scenes.BOX, scenes.SPHERE, scenes.CAPSULE, scenes.CONVEX_MESH],
+                 col_params=[[5.0, 0.4, 5.0, 0.0], [1.5, 0.0, 0.0, 0.0], [2.0, 0.6, 0.0, 0.0], [2.0, 2.0, 2.0, 0.0]],
+                 col_mesh=[-1, -1, -1, 0])
+    centers = scenes._jittered_grid(rng, 6, 3, 6, 1.5, [0.0, 6.0, 0.0])[:n]
+    first = scenes._mixed_bodies(s, rng, centers, 0, pool)
+    chain = scenes._chain(s, rng, 0, [0.0, -0.5, 0.0], [7.5, 6.0, 7.5], 6, [scenes.JOINT_SPHERICAL] * 6)
+    s = s.finalize()
+    trig = s.arrays["col_is_trigger"]
+    trig[1:5] = 1
+    trig[first + np.arange(3, n, 11)] = 1
+    trig[chain + 2] = 1
+    return s
