@@ -397,7 +397,9 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--workload", default="batched", choices=["batched", "large", "chains", "pyramid", "serving"])
+    ap.add_argument("--workload", default="batched", choices=["batched", "large", "chains", "pyramid", "serving",
+                                                                 "trimesh_bvh"])
+    ap.add_argument("--mesh-cells", type=int, default=256, help="trimesh_bvh: heightfield cells per side")
     ap.add_argument("--serve-seconds", type=float, default=20.0)
     ap.add_argument("--serve-load", type=float, default=0.7)
     ap.add_argument("--serve-max-bodies", type=int, default=8192)
@@ -417,6 +419,8 @@ def main():
         return run_reference(args, rank, world)
     if args.workload == "serving":
         return run_serving(args, rank, world, local)
+    if args.workload == "trimesh_bvh":
+        return run_trimesh_bvh(args, rank)
 
     dist = Dist(world, local)
     from physecs_gb300.api import World
@@ -536,6 +540,65 @@ def main():
         print(json.dumps(line))
     w.close()
     dist.close()
+
+
+def run_trimesh_bvh(args, rank):
+    """The triangle-mesh BVH build (TriangleMesh's constructor, src/TriangleMesh.cpp:144-164)
+    of one value-noise heightfield of --mesh-cells^2 cells.  value: a terrain edit,
+    psx_world_update_trimesh on a world that holds the mesh (new vertices uploaded, BVH
+    rebuilt on the device, collider bounds refreshed); e2e: psx_trimesh_build from host
+    arrays to host arrays.  Beside them, the reference's constructor on one host core."""
+    import numpy as np
+    from physecs_gb300 import scenes
+    from physecs_gb300.api import World, trimesh_build
+    if rank != 0:
+        return 0
+    cells = args.mesh_cells
+    s = scenes.large_mixed(n_bodies=64, cells=cells, seed=scenes.scene_seed(2, 99))
+    a = s.arrays
+    v = a["tri_verts"].copy()
+    ix = a["tri_indices"].copy()
+    v2 = v.copy()
+    v2[:, 1] = v2[:, 1] * np.float32(0.5)
+    w = World([s])
+    for i in range(args.warmup):
+        w.update_trimesh(0, 0, v2 if i % 2 == 0 else v)
+        trimesh_build(v, ix)
+    upd, std = [], []
+    for i in range(args.steps):
+        t = time.perf_counter()
+        w.update_trimesh(0, 0, v2 if i % 2 == 0 else v)
+        upd.append(time.perf_counter() - t)
+        t = time.perf_counter()
+        trimesh_build(v, ix)
+        std.append(time.perf_counter() - t)
+    w.close()
+    kind = cpu_kind()
+    if kind == "reference":
+        from oracle.ref.ref_api import trimesh_build as cpu_build
+    else:
+        from oracle.port_api import trimesh_build as cpu_build
+    cpu = []
+    for _ in range(3):
+        t = time.perf_counter()
+        cpu_build(v, ix)
+        cpu.append(time.perf_counter() - t)
+    nt, nv = len(ix) // 3, len(v)
+    ms = 1e3 * statistics.median(upd)
+    line = {
+        "metric": "triangle-mesh BVH build time", "value": ms, "unit": "ms", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "none", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (value-noise heightfield)",
+        "config": {"workload": "trimesh_bvh: heightfield %dx%d cells, %d triangles, %d vertices" % (cells, cells, nt, nv),
+                   "value": "psx_world_update_trimesh (vertex upload + device build + collider bounds)"},
+        "e2e": {"value": 1e3 * statistics.median(std), "unit": "ms", "h2d_bytes_per_step": 16 * nv + 16 * nt,
+                "d2h_bytes_per_step": 80 * nt + 32 * (2 * nt - 1), "call": "psx_trimesh_build"},
+        "cpu_baseline": {"value": 1e3 * statistics.median(cpu), "unit": "ms", "cores": 1, "kind": kind,
+                         "sample": "3 builds of the same mesh (TriangleMesh's constructor)"},
+        "gpu_launches": None,
+    }
+    print(json.dumps(line))
+    return 0
 
 
 def run_reference(args, rank, world):

@@ -231,6 +231,35 @@ PSX_API psx_status psx_world_tune(psx_world* w, int32_t frames, psx_launch_confi
 /* The launch shapes in effect (after defaults, tuning or opts.launch). */
 PSX_API psx_status psx_world_launch_config(psx_world* w, psx_launch_config* out);
 
+/* ---- triangle meshes: the BVH of physecs::TriangleMesh, built on the device */
+typedef struct psx_trimesh_triangle {  /* Triangle (include/Physecs/TriangleMesh.h:9-14) */
+    uint32_t indices[3];
+    uint32_t pad;
+    float bounds_min[4];               /* w = 0 */
+    float bounds_max[4];
+    float normal[4];
+    float centroid[4];
+} psx_trimesh_triangle;
+typedef struct psx_trimesh_node {      /* TriangleMeshBVHNode (include/Physecs/TriangleMesh.h:16-20) */
+    float bounds_min[3];
+    int32_t tri_count;                 /* > 0: a leaf over triangles [index, index + tri_count) */
+    float bounds_max[3];
+    int32_t index;                     /* inner node: its left child (the right one follows) */
+} psx_trimesh_node;
+/* physecs::TriangleMesh(vertices, indices) (src/TriangleMesh.cpp:144-164) on CUDA device
+ * `device`: triangles (n_indices / 3 of them) in the BVH's order and the BVH's nodes,
+ * identical to the reference's (binned SAH, 6 buckets; node 0 is the root).  nodes
+ * needs room for max(1, 2 * triangles - 1); *n_nodes receives the count.  Every index
+ * must be below n_vertices and every vertex finite (PSX_ERR_INVALID_ARG otherwise). */
+PSX_API psx_status psx_trimesh_build(int32_t device, const float* vertices, int32_t n_vertices, const uint32_t* indices,
+                                     int32_t n_indices, psx_trimesh_triangle* triangles, psx_trimesh_node* nodes,
+                                     int32_t* n_nodes);
+/* Replaces the vertices of triangle mesh `mesh` of scene `scene` (same vertex count, same
+ * indices: an edited terrain), rebuilds its BVH on the device as a new TriangleMesh over
+ * them would be built, and recomputes the bounds of the colliders that use it (as at
+ * creation, no margin).  Waits for the world's queued frames first. */
+PSX_API psx_status psx_world_update_trimesh(psx_world* w, int32_t scene, int32_t mesh, const float* vertices);
+
 /* ---- scene queries against the world's current state */
 typedef struct psx_ray {
     int32_t scene;

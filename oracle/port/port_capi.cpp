@@ -229,6 +229,31 @@ int orc_scene_overlap_mtd(void* h, const float* pose, int type, const float* par
     return (int)hits.size();
 }
 
+// TriangleMesh::build (src/TriangleMesh.cpp:144-164) of the restatement: triangles in the
+// tree's order as 20 words each (indices, pad, bounds min/max, normal, centroid, each
+// padded to four) and nodes as 8 words (bounds min, triCount, bounds max, index); nodes
+// needs room for max(1, 2 n - 1).  Returns the node count.
+int orc_trimesh_build(const float* verts, int nv, const uint32_t* idx, int nidx, uint32_t* tris, uint32_t* nodes) {
+    std::vector<V3> v(nv);
+    for (int i = 0; i < nv; ++i) v[i] = v3(verts[3 * i], verts[3 * i + 1], verts[3 * i + 2]);
+    TriangleMesh m;
+    m.build(v, std::vector<uint32_t>(idx, idx + nidx));
+    auto put = [](uint32_t* o, V3 a) { std::memcpy(o, &a.x, 4); std::memcpy(o + 1, &a.y, 4); std::memcpy(o + 2, &a.z, 4); o[3] = 0; };
+    for (size_t t = 0; t < m.triangles.size(); ++t) {
+        const Triangle& tr = m.triangles[t];
+        uint32_t* o = tris + 20 * t;
+        o[0] = tr.idx[0]; o[1] = tr.idx[1]; o[2] = tr.idx[2]; o[3] = 0;
+        put(o + 4, tr.bounds.min); put(o + 8, tr.bounds.max); put(o + 12, tr.normal); put(o + 16, tr.centroid);
+    }
+    for (size_t k = 0; k < m.bvh.size(); ++k) {
+        const TriNode& n = m.bvh[k];
+        uint32_t* o = nodes + 8 * k;
+        put(o, n.bounds.min); o[3] = (uint32_t)n.triCount;
+        put(o + 4, n.bounds.max); o[7] = (uint32_t)n.index;
+    }
+    return (int)m.bvh.size();
+}
+
 // The trigger events of the frames stepped since the last call, in step order: up to
 // cap records of (frame, kind 0 enter / 1 exit, body0, collider0, body1, collider1),
 // removed from the scene; returns the number pending before the call

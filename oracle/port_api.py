@@ -50,6 +50,7 @@ def lib():
         _lib.orc_scene_overlap_mtd.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
                                                C.c_int]
         _lib.orc_scene_trigger_events.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+        _lib.orc_trimesh_build.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
     return _lib
 
 
@@ -195,3 +196,15 @@ class OracleScene:
             if n <= cap:
                 return out[:n]
             cap = n
+
+
+def trimesh_build(verts, indices):
+    """TriangleMesh(vertices, indices) of the restatement: (triangles (n, 20) uint32 words,
+    nodes (m, 8) uint32 words) in psx_trimesh_triangle / psx_trimesh_node layout."""
+    v = np.ascontiguousarray(verts, np.float32).reshape(-1, 3)
+    ix = np.ascontiguousarray(indices, np.uint32).ravel()
+    nt = len(ix) // 3
+    tris = np.zeros((max(nt, 1), 20), np.uint32)
+    nodes = np.zeros((max(1, 2 * nt - 1), 8), np.uint32)
+    n = lib().orc_trimesh_build(_p(v), len(v), _p(ix), len(ix), _p(tris), _p(nodes))
+    return tris[:nt], nodes[:n]

@@ -40,6 +40,7 @@ def lib():
         _lib.ref_scene_collide.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         _lib.ref_scene_joint_colors.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
         _lib.ref_scene_trigger_events.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+        _lib.ref_trimesh_build.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
     return _lib
 
 
@@ -167,3 +168,18 @@ class RefScene:
         out = np.zeros((cap, 2), np.int32)
         n = lib().ref_scene_joint_colors(self.h, _p(out), cap)
         return out[:n]
+
+
+def trimesh_build(verts, indices):
+    """physecs::TriangleMesh(vertices, indices) of the reference: (triangles (n, 20) uint32
+    words, nodes (m, 8) uint32 words), in the layout of oracle.port_api.trimesh_build.
+    RuntimeError when the constructor throws (a mesh without triangles)."""
+    v = np.ascontiguousarray(verts, np.float32).reshape(-1, 3)
+    ix = np.ascontiguousarray(indices, np.uint32).ravel()
+    nt = len(ix) // 3
+    tris = np.zeros((max(nt, 1), 20), np.uint32)
+    nodes = np.zeros((max(1, 2 * nt - 1), 8), np.uint32)
+    n = lib().ref_trimesh_build(_p(v), len(v), _p(ix), len(ix), _p(tris), _p(nodes))
+    if n < 0:
+        raise RuntimeError("physecs::TriangleMesh threw")
+    return tris[:nt], nodes[:n]

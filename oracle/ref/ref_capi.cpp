@@ -203,6 +203,36 @@ void ref_scene_step(void* h, float dt) {
     ++w->triggers.frame;
 }
 
+// physecs::TriangleMesh(vertices, indices) of the reference, dumped in the layout of
+// orc_trimesh_build (20 words per triangle, 8 per node).  Returns the node count, or -1
+// when the constructor throws (a mesh without triangles: its bvh.reserve(2.f * 0 - 1)
+// asks for a size_t above the maximum, src/TriangleMesh.cpp:161).
+int ref_trimesh_build(const float* verts, int nv, const uint32_t* idx, int nidx, uint32_t* tris, uint32_t* nodes) {
+    std::vector<glm::vec3> v(nv);
+    for (int i = 0; i < nv; ++i) v[i] = v3(verts + 3 * i);
+    std::unique_ptr<physecs::TriangleMesh> mp;
+    try {
+        mp.reset(new physecs::TriangleMesh(v, std::vector<unsigned int>(idx, idx + nidx)));
+    } catch (const std::exception&) {
+        return -1;
+    }
+    const physecs::TriangleMesh& m = *mp;
+    auto put = [](uint32_t* o, glm::vec3 a) { std::memcpy(o, &a.x, 4); std::memcpy(o + 1, &a.y, 4); std::memcpy(o + 2, &a.z, 4); o[3] = 0; };
+    for (size_t t = 0; t < m.triangles.size(); ++t) {
+        const physecs::Triangle& tr = m.triangles[t];
+        uint32_t* o = tris + 20 * t;
+        o[0] = tr.indices[0]; o[1] = tr.indices[1]; o[2] = tr.indices[2]; o[3] = 0;
+        put(o + 4, tr.bounds.min); put(o + 8, tr.bounds.max); put(o + 12, tr.normal); put(o + 16, tr.centroid);
+    }
+    for (size_t k = 0; k < m.bvh.size(); ++k) {
+        const physecs::TriangleMeshBVHNode& n = m.bvh[k];
+        uint32_t* o = nodes + 8 * k;
+        put(o, n.bounds.min); o[3] = (uint32_t)n.triCount;
+        put(o + 4, n.bounds.max); o[7] = (uint32_t)n.index;
+    }
+    return (int)m.bvh.size();
+}
+
 // The trigger callbacks recorded since the last call, in callback order: up to cap
 // records of 6 ints, removed; returns the number pending before the call
 int ref_scene_trigger_events(void* h, int32_t* out, int cap) {

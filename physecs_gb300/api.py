@@ -28,7 +28,7 @@ EXPORTS = ["psx_world_create", "psx_world_destroy", "psx_world_step", "psx_world
            "psx_server_release", "psx_server_stats", "psx_server_tick_begin", "psx_server_tick_end", "psx_server_world",
            "psx_server_tick_stages", "psx_server_device_bytes",
            "psx_world_tune", "psx_world_launch_config", "psx_world_raycast", "psx_world_overlap",
-           "psx_world_overlap_mtd", "psx_world_trigger_events"]
+           "psx_world_overlap_mtd", "psx_world_trigger_events", "psx_trimesh_build", "psx_world_update_trimesh"]
 
 _lib = None
 
@@ -99,6 +99,8 @@ def load():
     lib.psx_server_read.argtypes = [vp, C.c_int32, vp, vp, vp, vp]
     lib.psx_server_release.argtypes = [vp, C.c_int32]
     lib.psx_world_trigger_events.argtypes = [vp, vp, C.c_int32, vp, vp]
+    lib.psx_trimesh_build.argtypes = [C.c_int32, vp, C.c_int32, vp, C.c_int32, vp, vp, vp]
+    lib.psx_world_update_trimesh.argtypes = [vp, C.c_int32, C.c_int32, vp]
     lib.psx_server_stats.argtypes = [vp, vp]
     _lib = lib
     return lib
@@ -293,6 +295,12 @@ class World:
                         for k in range(i * cap, i * cap + m)])
         return counts[:n].copy(), res
 
+    def update_trimesh(self, scene, mesh, vertices):
+        """psx_world_update_trimesh: new vertices (same count) for triangle mesh `mesh` of
+        `scene`, its BVH rebuilt on the device and its colliders' bounds recomputed."""
+        v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+        _check(load().psx_world_update_trimesh(self.h, scene, mesh, _p(v)))
+
     # ---------------------------------------------------------------- trigger events
 
     def trigger_events(self, cap=4096):
@@ -464,3 +472,17 @@ class Server:
         out = np.zeros(6, np.int64)
         _check(load().psx_server_stats(self.h, _p(out)))
         return dict(zip(["running", "finished", "free", "bodies", "body_frames", "slots"], (int(v) for v in out)))
+
+
+def trimesh_build(vertices, indices, device=0):
+    """psx_trimesh_build: physecs::TriangleMesh(vertices, indices) built on the GPU.
+    Returns (triangles (n, 20) uint32 words, nodes (m, 8) uint32 words) in the
+    psx_trimesh_triangle / psx_trimesh_node layouts."""
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+    ix = np.ascontiguousarray(indices, np.uint32).ravel()
+    nt = len(ix) // 3
+    tris = np.zeros((max(nt, 1), 20), np.uint32)
+    nodes = np.zeros((max(1, 2 * nt - 1), 8), np.uint32)
+    n = C.c_int32()
+    _check(load().psx_trimesh_build(device, _p(v), len(v), _p(ix), len(ix), _p(tris), _p(nodes), C.byref(n)))
+    return tris[:nt], nodes[:n.value]

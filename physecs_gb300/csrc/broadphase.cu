@@ -10,6 +10,7 @@
 // (entity0 < entity1, src/Physecs.cpp:156-170), each leaf's pairs ordered by
 // partner collider.
 #include "frame.cuh"
+#include "ordkey.cuh"
 #include "narrow_convex.cuh"
 
 namespace psx {
@@ -26,7 +27,7 @@ __global__ void k_aabb(World w, int c0, int c1, int margin_mode) {
     int4 bi = w.info[ci.x];
     bool simulated = (bi.y & BODY_DYN) && !(bi.y & BODY_KIN);
     if (margin_mode == 1 && !simulated) return;
-    if (ci.y == G_TRIMESH && margin_mode == 1) return;
+    if (ci.y == G_TRIMESH) return;   // k_trimesh_bounds (no margin: a mesh never gets one)
     Q4 bq = ld4(w.quat[ci.x]);
     V3 bp = ld3(w.pos[ci.x]);
     V3 pos = bp + qrot(bq, ld3(w.col_pos[c]));
@@ -34,20 +35,78 @@ __global__ void k_aabb(World w, int c0, int c1, int margin_mode) {
     float4 pr = w.col_params[c];
     GeomD g{ci.y, {pr.x, pr.y, pr.z}, ci.z};
     Bounds b;
-    if (ci.y == G_TRIMESH) {
-        TriMeshDev tm = w.trimesh[ci.z];
-        V3 mn = v3s(FLT_MAX), mx = v3s(-FLT_MAX);
-        for (int i = 0; i < tm.vert_count; ++i) {
-            V3 t = pos + qrot(ori, ld3(w.tri_verts[tm.vert_start + i]));
-            mn = vmin(mn, t); mx = vmax(mx, t);
-        }
-        b = {mn, mx};
-    } else {
-        b = getBounds(w, pos, ori, g);
-    }
+    b = getBounds(w, pos, ori, g);
     if (margin_mode == 1) { b.max += v3s(0.01f); b.min -= v3s(0.01f); }
     w.aabb_min[c] = st4(b.min);
     w.aabb_max[c] = st4(b.max);
+}
+
+// getBoundsTriangleMesh (src/BoundsUtil.cpp:77-85) for the triangle-mesh colliders in
+// [c0, c1): every vertex at the collider's world pose, in chunks of kMeshBoundsChunk
+// vertices a block.  The reference folds the vertices in order; (value, index) keys
+// reduced across the blocks give the same pick, and a last pass reads the picked
+// vertices back.  trimesh_keys holds [6][n_trimesh_cols] keys: min x, y, z, max x, y, z.
+__device__ __forceinline__ V3 mesh_vertex_world(const World& w, int c, const TriMeshDev& tm, int i, V3 pos, Q4 ori) {
+    return pos + qrot(ori, ld3(w.tri_verts[tm.vert_start + i]));
+}
+__device__ __forceinline__ void collider_world_pose(const World& w, int c, V3& pos, Q4& ori) {
+    const int4 ci = w.col_info[c];
+    const Q4 bq = ld4(w.quat[ci.x]);
+    pos = ld3(w.pos[ci.x]) + qrot(bq, ld3(w.col_pos[c]));
+    ori = qmul(bq, ld4(w.col_quat[c]));
+}
+
+__global__ void __launch_bounds__(256) k_trimesh_bounds_part(World w, int c0, int c1) {
+    __shared__ unsigned long long sk[6];
+    const int2 ch = w.trimesh_chunks[blockIdx.x];   // (trimesh collider slot, chunk)
+    const int c = w.trimesh_cols[ch.x];
+    if (c < c0 || c >= c1) return;
+    V3 pos;
+    Q4 ori;
+    collider_world_pose(w, c, pos, ori);
+    const TriMeshDev tm = w.trimesh[w.col_info[c].z];
+    if (threadIdx.x < 6) sk[threadIdx.x] = threadIdx.x < 3 ? kKeyMinInit : kKeyMaxInit;
+    __syncthreads();
+    unsigned long long k[6] = {kKeyMinInit, kKeyMinInit, kKeyMinInit, kKeyMaxInit, kKeyMaxInit, kKeyMaxInit};
+    const int i1 = min(tm.vert_count, (ch.y + 1) * kMeshBoundsChunk);
+    for (int i = ch.y * kMeshBoundsChunk + threadIdx.x; i < i1; i += blockDim.x) {
+        const V3 t = mesh_vertex_world(w, c, tm, i, pos, ori);
+        k[0] = min(k[0], key_min(t.x, i)); k[1] = min(k[1], key_min(t.y, i)); k[2] = min(k[2], key_min(t.z, i));
+        k[3] = max(k[3], key_max(t.x, i)); k[4] = max(k[4], key_max(t.y, i)); k[5] = max(k[5], key_max(t.z, i));
+    }
+    for (int o = 16; o; o >>= 1)
+        for (int j = 0; j < 6; ++j) {
+            const unsigned long long v = __shfl_xor_sync(0xffffffffu, k[j], o);
+            k[j] = j < 3 ? min(k[j], v) : max(k[j], v);
+        }
+    if ((threadIdx.x & 31) == 0)
+        for (int j = 0; j < 6; ++j) j < 3 ? atomicMin(&sk[j], k[j]) : atomicMax(&sk[j], k[j]);
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int j = threadIdx.x;
+        unsigned long long* d = &w.trimesh_keys[(size_t)j * w.n_trimesh_cols + ch.x];
+        j < 3 ? atomicMin(d, sk[j]) : atomicMax(d, sk[j]);
+    }
+}
+
+__global__ void k_trimesh_bounds_final(World w, int c0, int c1) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < w.n_trimesh_cols; t += gridDim.x * blockDim.x) {
+        const int c = w.trimesh_cols[t];
+        if (c < c0 || c >= c1) continue;
+        V3 pos;
+        Q4 ori;
+        collider_world_pose(w, c, pos, ori);
+        const TriMeshDev tm = w.trimesh[w.col_info[c].z];
+        float b[6];
+        for (int j = 0; j < 6; ++j) {
+            if (!tm.vert_count) { b[j] = j < 3 ? FLT_MAX : -FLT_MAX; continue; }
+            const unsigned long long k = w.trimesh_keys[(size_t)j * w.n_trimesh_cols + t];
+            const V3 v = mesh_vertex_world(w, c, tm, j < 3 ? key_min_index(k) : key_max_index(k), pos, ori);
+            b[j] = (j % 3) == 0 ? v.x : ((j % 3) == 1 ? v.y : v.z);
+        }
+        w.aabb_min[c] = make_float4(b[0], b[1], b[2], 0.f);
+        w.aabb_max[c] = make_float4(b[3], b[4], b[5], 0.f);
+    }
 }
 
 int launch_aabb(const World& w, int margin_mode, cudaStream_t s) {
@@ -57,7 +116,13 @@ int launch_aabb(const World& w, int margin_mode, cudaStream_t s) {
 int launch_aabb_range(const World& w, int c0, int c1, int margin_mode, cudaStream_t s) {
     if (c1 <= c0) return 0;
     k_aabb<<<(c1 - c0 + 255) / 256, 256, 0, s>>>(w, c0, c1, margin_mode);
-    return 1;
+    if (margin_mode == 1 || !w.n_trimesh_cols) return 1;
+    const size_t n3 = 3 * (size_t)w.n_trimesh_cols;
+    cudaMemsetAsync(w.trimesh_keys, 0xff, n3 * sizeof(unsigned long long), s);
+    cudaMemsetAsync(w.trimesh_keys + n3, 0, n3 * sizeof(unsigned long long), s);
+    k_trimesh_bounds_part<<<w.n_trimesh_chunks, 256, 0, s>>>(w, c0, c1);
+    k_trimesh_bounds_final<<<(w.n_trimesh_cols + 127) / 128, 128, 0, s>>>(w, c0, c1);
+    return 3;
 }
 
 // ---------------------------------------------------------------- Morton keys

@@ -42,6 +42,9 @@ struct psx_world {
     std::vector<int> h_col_local;          // per collider: index within its body
     std::vector<int> h_col_body;           // per collider: world body index
     std::vector<int> h_scene_convex;       // per scene (+1): first world convex mesh
+    std::vector<int> h_scene_trimesh;      // per scene (+1): first world triangle mesh
+    std::vector<psx::TriMeshDev> h_trimesh;
+    std::vector<int> h_col_trimesh;        // per collider: world triangle mesh, or -1
     void* qbuf = nullptr;                  // scene-query staging on the device
     std::vector<psx_trigger_event> trig_pending;   // drained from the device, not yet delivered
     long long trig_lost = 0;               // events past the device log's capacity

@@ -22,8 +22,12 @@ constexpr float kPi = 3.14159265358979323846f;
 
 // ---------------------------------------------------------------- restitution cache
 
-__device__ __forceinline__ unsigned long long cache_key(int ca, int cb, int tri) {
-    return ((unsigned long long)(uint32_t)ca << 41) | ((unsigned long long)(uint32_t)cb << 18) | (unsigned long long)(uint32_t)(tri + 1);
+// (collider, collider, triangle + 1) in one word: collider indices take cbits bits each
+// (every index is below 2^cbits - 1, so no key is all ones, the empty mark), the
+// triangle the remaining 64 - 2 cbits
+__device__ __forceinline__ unsigned long long cache_key(int ca, int cb, int tri, int cbits) {
+    return ((unsigned long long)(uint32_t)ca << (64 - cbits)) | ((unsigned long long)(uint32_t)cb << (64 - 2 * cbits)) |
+           (unsigned long long)(uint32_t)(tri + 1);
 }
 __device__ __forceinline__ uint32_t cache_hash(unsigned long long k) {
     k ^= k >> 33; k *= 0xff51afd7ed558ccdull; k ^= k >> 33; k *= 0xc4ceb9fe1a85ec53ull; k ^= k >> 33;
@@ -88,7 +92,7 @@ __global__ void k_build_contacts(World w, FrameBuf f) {
             c.frequency = freq; c.damping = damp;
             c.np = m.np; c.soft = soft ? 1 : 0;
             c.color = -1; c.scene = iA.w; c.pair = p; c.tri = m.tri;
-            unsigned long long key = cache_key(pr.x, pr.y, m.tri);
+            unsigned long long key = cache_key(pr.x, pr.y, m.tri, w.key_cbits);
             // previous frame's entry, if any
             const CacheEntry* pe = nullptr;
             const bool fresh = w.scene_fresh && w.scene_fresh[iA.w];

@@ -32,6 +32,7 @@ constexpr int kTriManifolds = 16;  // manifolds one body may produce against one
 constexpr int kTriCandidates = 64; // candidate triangles per body-mesh pair
 constexpr int kMaxRowsPerJoint = 8;
 constexpr int kMaxColors = 128;    // contact colours per scene
+constexpr int kMeshBoundsChunk = 8192;   // triangle-mesh vertices per block in the collider bounds
 
 struct ConvexMeshDev {   // one ConvexMesh
     int vert_start, vert_count_padded, vert_count;
@@ -131,6 +132,7 @@ struct CacheEntry {      // restitution cache (include/Physecs/Physecs.h:127-135
 
 struct World {
     int n_scenes, n_bodies, n_colliders, n_dyn, n_joints;
+    int key_cbits;       // bits of a collider index in a restitution-cache key (the rest: triangle + 1)
     int* scene_body;     // [S+1]
     int* scene_col;      // [S+1]
     int* scene_dyn;      // [S+1]
@@ -171,6 +173,12 @@ struct World {
     float4* tri_verts;
     TriDev* tris;
     TriNodeDev* tri_nodes;
+    int4* tri_src;         // per triangle, index order: mesh-local vertex indices, w = mesh's first vertex
+    int* trimesh_cols;     // colliders whose shape is a triangle mesh
+    int n_trimesh_cols;
+    int2* trimesh_chunks;  // (trimesh_cols slot, chunk of kMeshBoundsChunk vertices) for their bounds
+    int n_trimesh_chunks;
+    unsigned long long* trimesh_keys;   // [6][n_trimesh_cols] bounds reduction keys
     // joints
     JointDev* joints;
     Row* rows;             // kMaxRowsPerJoint per joint

@@ -7,12 +7,14 @@
 // queues one frame as a fixed sequence of kernels on the world's stream.
 #include <cuda_runtime.h>
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <map>
 #include <mutex>
 #include <string>
 #include <vector>
+#include "meshbvh.cuh"
 #include "runtime.cuh"
 
 using namespace psx;
@@ -33,102 +35,6 @@ psx_status fail(psx_status s, const std::string& msg) {
 using namespace psx::rt;
 
 namespace {
-
-// ---------------------------------------------------------------- triangle-mesh BVH (host)
-// Binned SAH with six buckets, exactly as src/TriangleMesh.cpp:7-164, so that triangle
-// indices (which the BVH build permutes) match the reference's.
-
-struct HTri { uint32_t idx[3]; Bounds b; V3 normal, centroid; };
-struct HNode { Bounds b; int triCount; int index; };
-
-Bounds bunion(const Bounds& a, const Bounds& b) {
-    return {{fminG(a.min.x, b.min.x), fminG(a.min.y, b.min.y), fminG(a.min.z, b.min.z)},
-            {fmaxG(a.max.x, b.max.x), fmaxG(a.max.y, b.max.y), fmaxG(a.max.z, b.max.z)}};
-}
-float barea(const Bounds& b) {
-    V3 d = b.max - b.min;
-    return 2 * (d.x * d.y + d.y * d.z + d.z * d.x);
-}
-Bounds empty_bounds() { return {v3s(FLT_MAX), v3s(-FLT_MAX)}; }
-
-struct MeshBVH {
-    std::vector<HTri> tris;
-    std::vector<HNode> nodes;
-    static constexpr int kB = 6;
-    void node_bounds(int id) {
-        Bounds b = empty_bounds();
-        for (int i = 0; i < nodes[id].triCount; ++i) b = bunion(b, tris[nodes[id].index + i].b);
-        nodes[id].b = b;
-    }
-    bool fill(int id, int axis, Bounds* bb, int* bc) {
-        const HNode& n = nodes[id];
-        for (int i = 0; i < kB; ++i) { bb[i] = empty_bounds(); bc[i] = 0; }
-        float s = at(n.b.min, axis), e = at(n.b.max, axis), len = e - s;
-        if (!len) return false;
-        for (int i = 0; i < n.triCount; ++i) {
-            const HTri& t = tris[n.index + i];
-            int bi = std::min(kB - 1, (int)((at(t.centroid, axis) - s) / len * kB));
-            bb[bi] = bunion(bb[bi], t.b);
-            bc[bi]++;
-        }
-        return true;
-    }
-    void subdivide(int id) {
-        float best = FLT_MAX;
-        int axis = 0, split = 0, cl = 0, cr = 0;
-        Bounds L{}, R{};
-        for (int a = 0; a < 3; ++a) {
-            Bounds bb[kB];
-            int bc[kB];
-            if (!fill(id, a, bb, bc)) continue;
-            for (int sp = 1; sp < kB; ++sp) {
-                Bounds l = empty_bounds(), r = empty_bounds();
-                int nl = 0, nr = 0;
-                for (int i = 0; i < kB; ++i) {
-                    if (i < sp) { l = bunion(l, bb[i]); nl += bc[i]; }
-                    else { r = bunion(r, bb[i]); nr += bc[i]; }
-                }
-                if (!nl || !nr) continue;
-                float cost = nl * barea(l) + nr * barea(r);
-                if (cost < best) { best = cost; axis = a; split = sp; L = l; R = r; cl = nl; cr = nr; }
-            }
-        }
-        if (!(cl && cr)) return;
-        HNode n = nodes[id];
-        float s = at(n.b.min, axis), e = at(n.b.max, axis), len = e - s;
-        int i = n.index, j = i + n.triCount - 1;
-        while (i <= j) {
-            int bi = (int)((at(tris[i].centroid, axis) - s) / len * kB);
-            if (bi < split) ++i;
-            else std::swap(tris[i], tris[j--]);
-        }
-        nodes.push_back({L, cl, n.index});
-        nodes.push_back({R, cr, i});
-        nodes[id].triCount = 0;
-        nodes[id].index = (int)nodes.size() - 2;
-        int left = nodes[id].index;
-        subdivide(left);
-        subdivide(left + 1);
-    }
-    void build(const float* verts, const uint32_t* idx, int nidx) {
-        for (int k = 0; k + 2 < nidx; k += 3) {
-            HTri t;
-            t.idx[0] = idx[k]; t.idx[1] = idx[k + 1]; t.idx[2] = idx[k + 2];
-            V3 a = {verts[3 * t.idx[0]], verts[3 * t.idx[0] + 1], verts[3 * t.idx[0] + 2]};
-            V3 b = {verts[3 * t.idx[1]], verts[3 * t.idx[1] + 1], verts[3 * t.idx[1] + 2]};
-            V3 c = {verts[3 * t.idx[2]], verts[3 * t.idx[2] + 1], verts[3 * t.idx[2] + 2]};
-            t.b = {vmin(vmin(a, b), c), vmax(vmax(a, b), c)};
-            t.normal = normalize(cross(b - a, c - a));
-            t.centroid = (a + b + c) / 3.f;
-            tris.push_back(t);
-        }
-        nodes.reserve(2 * tris.size() + 1);
-        nodes.push_back({Bounds{}, (int)tris.size(), 0});
-        node_bounds(0);
-        subdivide(0);
-    }
-};
-
 
 template <class T>
 struct DBuf {
@@ -157,6 +63,13 @@ psx_status psx::rt::validate(const psx_scene_desc& d) {
             return fail(PSX_ERR_INVALID_ARG, "joint body index");
     }
     if (d.num_substeps <= 0 || d.num_iterations < 0) return fail(PSX_ERR_INVALID_ARG, "knobs");
+    for (int m = 0; m < d.n_trimesh; ++m) {   // the device BVH build reads vertices by these indices
+        const int nv = d.tri_vert_start[m + 1] - d.tri_vert_start[m];
+        for (int k = d.tri_index_start[m]; k < d.tri_index_start[m + 1]; ++k)
+            if (d.tri_indices[k] >= (uint32_t)nv) return fail(PSX_ERR_INVALID_ARG, "triangle-mesh vertex index");
+        for (int v = 3 * d.tri_vert_start[m]; v < 3 * d.tri_vert_start[m + 1]; ++v)
+            if (!std::isfinite(d.tri_verts[v])) return fail(PSX_ERR_INVALID_ARG, "triangle-mesh vertex not finite");
+    }
     return PSX_OK;
 }
 
@@ -171,8 +84,8 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
     std::vector<int> face_idx_start{0}, face_idx;
     std::vector<TriMeshDev> trimesh;
     std::vector<float4> tri_verts;
-    std::vector<TriDev> tris;
-    std::vector<TriNodeDev> tri_nodes;
+    std::vector<int4> tri_src;    // per triangle: mesh-local vertex indices, w = the mesh's first vertex
+    int n_tri_nodes = 0;
     std::vector<JointDev> joints;
     std::vector<int2> nc;
     std::vector<int> jsched, jstep_start{0}, scene_jsteps{0};
@@ -182,6 +95,7 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
         int bbase = (int)pos.size(), cbase = (int)col_info.size(), dbase = (int)dyn_body.size();
         int mbase = (int)convex.size(), tbase = (int)trimesh.size(), jbase = (int)joints.size();
         W->h_scene_convex.push_back(mbase);
+        W->h_scene_trimesh.push_back(tbase);
         // convex meshes: vertex buffer padded to a multiple of four with the last vertex (src/ConvexMesh.cpp:3-11)
         for (int m = 0; m < d.n_convex; ++m) {
             ConvexMeshDev cm;
@@ -204,27 +118,18 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
         for (int m = 0; m < d.n_trimesh; ++m) {
             int v0 = d.tri_vert_start[m], v1 = d.tri_vert_start[m + 1];
             int i0 = d.tri_index_start[m], i1 = d.tri_index_start[m + 1];
-            MeshBVH bvh;
-            bvh.build(d.tri_verts + 3 * v0, d.tri_indices + i0, i1 - i0);
+            // the mesh's triangles in index order; its BVH is built on the device below
             TriMeshDev tm;
             tm.vert_start = (int)tri_verts.size();
             tm.vert_count = v1 - v0;
-            tm.tri_start = (int)tris.size();
-            tm.tri_count = (int)bvh.tris.size();
-            tm.node_start = (int)tri_nodes.size();
+            tm.tri_start = (int)tri_src.size();
+            tm.tri_count = (i1 - i0) / 3;
+            tm.node_start = n_tri_nodes;
+            n_tri_nodes += std::max(1, 2 * tm.tri_count - 1);
             for (int v = v0; v < v1; ++v) tri_verts.push_back(f4(d.tri_verts[3 * v], d.tri_verts[3 * v + 1], d.tri_verts[3 * v + 2]));
-            for (const HTri& t : bvh.tris) {
-                TriDev td;
-                td.idx = make_int4((int)t.idx[0], (int)t.idx[1], (int)t.idx[2], 0);
-                td.bmin = st4(t.b.min); td.bmax = st4(t.b.max);
-                td.normal = st4(t.normal); td.centroid = st4(t.centroid);
-                tris.push_back(td);
-            }
-            for (const HNode& n : bvh.nodes) {
-                TriNodeDev nd;
-                nd.bmin = f4(n.b.min.x, n.b.min.y, n.b.min.z, bits_as_float(n.triCount));
-                nd.bmax = f4(n.b.max.x, n.b.max.y, n.b.max.z, bits_as_float(n.index));
-                tri_nodes.push_back(nd);
+            for (int k = 0; k < tm.tri_count; ++k) {
+                const uint32_t* ix = d.tri_indices + i0 + 3 * k;
+                tri_src.push_back(make_int4((int)ix[0], (int)ix[1], (int)ix[2], tm.vert_start));
             }
             trimesh.push_back(tm);
         }
@@ -255,6 +160,7 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
                 if (d.col_is_trigger && d.col_is_trigger[c]) flags |= COL_TRIGGER;
                 if (sim) flags |= COL_DYNAMIC;
                 col_info.push_back(make_int4(bbase + b, t, mesh, flags));
+                W->h_col_trimesh.push_back(t == PSX_TRIANGLE_MESH ? mesh : -1);
                 col_pos.push_back(f4(d.col_pos[3 * c], d.col_pos[3 * c + 1], d.col_pos[3 * c + 2]));
                 col_quat.push_back(f4(d.col_quat[4 * c], d.col_quat[4 * c + 1], d.col_quat[4 * c + 2], d.col_quat[4 * c + 3]));
                 col_params.push_back(f4(d.col_params[4 * c], d.col_params[4 * c + 1], d.col_params[4 * c + 2], d.col_params[4 * c + 3]));
@@ -337,6 +243,7 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
     nc.erase(std::unique(nc.begin(), nc.end(), [](int2 a, int2 b) { return a.x == b.x && a.y == b.y; }), nc.end());
     W->h_scene_body = scene_body;
     W->h_scene_convex.push_back((int)convex.size());
+    W->h_scene_trimesh.push_back((int)trimesh.size());
     W->h_scene_col = scene_col;
     W->h_scene_dyn = scene_dyn;
     World& w = W->w;
@@ -346,7 +253,14 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
     w.n_dyn = (int)dyn_body.size();
     w.n_joints = (int)joints.size();
     if (w.n_colliders >= (1 << 23)) return fail(PSX_ERR_CAPACITY, "more than 2^23 colliders in one world");
-    for (const TriMeshDev& tm : trimesh) if (tm.tri_count >= (1 << 18) - 1) return fail(PSX_ERR_CAPACITY, "triangle mesh above 262142 triangles");
+    // restitution-cache keys: as few bits per collider as the world needs, the rest for triangles
+    w.key_cbits = 1;
+    while ((1ll << w.key_cbits) - 1 < (long long)w.n_colliders) ++w.key_cbits;   // indices below 2^cbits - 1
+    const long long tri_max = (1ll << (64 - 2 * w.key_cbits)) - 2;
+    for (const TriMeshDev& tm : trimesh)
+        if (tm.tri_count > tri_max)
+            return fail(PSX_ERR_CAPACITY, "triangle mesh above " + std::to_string(tri_max) + " triangles in a world of " +
+                                              std::to_string(w.n_colliders) + " colliders");
     PSX_TRY(W->upload(w.scene_body, scene_body));
     PSX_TRY(W->upload(w.scene_col, scene_col));
     PSX_TRY(W->upload(w.scene_dyn, scene_dyn));
@@ -380,8 +294,34 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
     PSX_TRY(W->upload(w.face_centroid, face_centroid));
     PSX_TRY(W->upload(w.trimesh, trimesh));
     PSX_TRY(W->upload(w.tri_verts, tri_verts));
-    PSX_TRY(W->upload(w.tris, tris));
-    PSX_TRY(W->upload(w.tri_nodes, tri_nodes));
+    // triangle-mesh BVHs: every mesh of every scene in one device build
+    PSX_TRY(W->upload(w.tri_src, tri_src));
+    PSX_TRY(W->alloc(w.tris, tri_src.size()));
+    PSX_TRY(W->alloc(w.tri_nodes, n_tri_nodes));
+    if (!trimesh.empty()) {
+        std::vector<BuildMesh> bm;
+        for (const TriMeshDev& tm : trimesh) bm.push_back({tm.tri_start, tm.tri_count, tm.vert_start, tm.node_start});
+        std::vector<int> counts;
+        int berr = 0;
+        PSX_CUDA(cudaDeviceSynchronize());   // the uploads above ran on the legacy stream
+        PSX_CUDA(build_mesh_bvhs(w.tri_verts, w.tri_src, bm, w.tris, w.tri_nodes, counts, &berr, W->stream));
+        if (berr) return fail(PSX_ERR_CAPACITY, "triangle-mesh BVH build");
+    }
+    W->h_trimesh = trimesh;
+    {
+        std::vector<int> tcols;
+        for (int c = 0; c < (int)W->h_col_trimesh.size(); ++c) if (W->h_col_trimesh[c] >= 0) tcols.push_back(c);
+        PSX_TRY(W->upload(w.trimesh_cols, tcols));
+        w.n_trimesh_cols = (int)tcols.size();
+        std::vector<int2> tch;
+        for (int t = 0; t < (int)tcols.size(); ++t) {
+            const int nv = trimesh[W->h_col_trimesh[tcols[t]]].vert_count;
+            for (int k = 0; k == 0 || k * kMeshBoundsChunk < nv; ++k) tch.push_back(make_int2(t, k));
+        }
+        PSX_TRY(W->upload(w.trimesh_chunks, tch));
+        w.n_trimesh_chunks = (int)tch.size();
+        PSX_TRY(W->alloc(w.trimesh_keys, 6 * tcols.size()));
+    }
     PSX_TRY(W->upload(w.joints, joints));
     PSX_TRY(W->alloc(w.rows, (size_t)kMaxRowsPerJoint * std::max(1, w.n_joints)));
     PSX_TRY(W->upload(w.jsched, jsched));

@@ -13,6 +13,8 @@ oracle/ref/build_ref.py) on seeded scenes from physecs_gb300.scenes:
                        scenes for seeded rays and shapes
   triggers.npz         the onTriggerEnter / onTriggerExit callbacks of stepped scenes
                        with trigger colliders
+  trimesh_bvh.npz      physecs::TriangleMesh's triangles and BVH nodes for seeded meshes,
+                       degenerate ones included
 
 Run in a checkout with the reference present:  python tests/golden/make_golden.py
 """
@@ -195,6 +197,56 @@ def query_fixture():
     return out
 
 
+def trimesh_cases():
+    """name -> (vertices (n, 3) float32, indices (3t,) uint32): meshes for the BVH build,
+    with the cases that steer its branches: axes without extent, triangles that share a
+    centroid (no split separates them), zero-area and duplicate triangles, signed zeros,
+    a skewed distribution, a single triangle and an empty mesh."""
+    rng = np.random.default_rng(0x7215)
+    out = {}
+    v, ix, _ = scenes.heightfield(scenes.SplitMix64(scenes.scene_seed(2, 77)), cells=12, lattice=4)
+    out["heightfield12"] = (v, ix.ravel())
+    n = 300
+    v = rng.uniform(-5, 5, (3 * n, 3)).astype(np.float32)
+    v[rng.random(3 * n) < 0.1, 1] = np.float32(-0.0)
+    v[rng.random(3 * n) < 0.1, 0] = np.float32(0.0)
+    ix = np.arange(3 * n, dtype=np.uint32)
+    dup = rng.integers(0, n, 40)
+    ix = np.concatenate([ix, ix.reshape(-1, 3)[dup].ravel()])
+    deg = rng.integers(0, 3 * n, 20)
+    ix = np.concatenate([ix, np.repeat(deg, 3).astype(np.uint32)])          # zero-area triangles
+    out["soup"] = (v, ix.astype(np.uint32))
+    xs = np.arange(11, dtype=np.float32)
+    X, Z = np.meshgrid(xs, xs, indexing="ij")
+    v = np.stack([X.ravel(), np.zeros(121, np.float32), Z.ravel()], axis=1).astype(np.float32)
+    q = np.arange(10)
+    I, J = np.meshgrid(q, q, indexing="ij")
+    a, b, c, d = (I * 11 + J).ravel(), ((I + 1) * 11 + J).ravel(), (I * 11 + J + 1).ravel(), ((I + 1) * 11 + J + 1).ravel()
+    out["flat"] = (v, np.stack([a, c, b, b, c, d], axis=1).ravel().astype(np.uint32))
+    v = np.array([[0, 0, 0], [1, 0, 0], [0, 0, 1]], np.float32)
+    out["single"] = (v, np.array([0, 1, 2], np.uint32))
+    out["same_centroid"] = (v, np.tile(np.array([0, 1, 2], np.uint32), 90))
+    k = np.arange(400)
+    x = (1.3 ** (k / 10.0)).astype(np.float32)      # exponentially spaced: lopsided splits
+    z0 = np.zeros_like(x)
+    v = np.stack([np.stack([x, z0, z0], 1), np.stack([x + 0.5, z0 + 1, z0], 1), np.stack([x, z0, z0 + 1], 1)], 1)
+    v = v.reshape(-1, 3).astype(np.float32)
+    out["skewed"] = (v, (rng.permutation(400).repeat(3) * 3 + np.tile(np.arange(3), 400)).astype(np.uint32))
+    out["empty"] = (v[:3], np.zeros(0, np.uint32))
+    return out
+
+
+def trimesh_fixture():
+    from oracle.ref.ref_api import trimesh_build
+    out = {}
+    for name, (v, ix) in trimesh_cases().items():
+        if not len(ix):
+            continue   # the reference's constructor throws for a mesh without triangles
+        tris, nodes = trimesh_build(v, ix)
+        out.update({name + "__verts": v, name + "__indices": ix, name + "__tris": tris, name + "__nodes": nodes})
+    return out
+
+
 def trigger_scenes():
     """name -> (scene, frames stepped)."""
     sys.path.insert(0, os.path.dirname(HERE))
@@ -256,6 +308,8 @@ def main():
     print("queries ok")
     np.savez_compressed(os.path.join(HERE, "triggers.npz"), **trigger_fixture())
     print("triggers ok")
+    np.savez_compressed(os.path.join(HERE, "trimesh_bvh.npz"), **trimesh_fixture())
+    print("trimesh_bvh ok")
 
 
 if __name__ == "__main__":
