@@ -398,7 +398,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--workload", default="batched", choices=["batched", "large", "chains", "pyramid", "serving",
-                                                                 "trimesh_bvh"])
+                                                                 "trimesh_bvh", "registry"])
     ap.add_argument("--mesh-cells", type=int, default=256, help="trimesh_bvh: heightfield cells per side")
     ap.add_argument("--serve-seconds", type=float, default=20.0)
     ap.add_argument("--serve-load", type=float, default=0.7)
@@ -421,6 +421,8 @@ def main():
         return run_serving(args, rank, world, local)
     if args.workload == "trimesh_bvh":
         return run_trimesh_bvh(args, rank)
+    if args.workload == "registry":
+        return run_registry(args, rank)
 
     dist = Dist(world, local)
     from physecs_gb300.api import World
@@ -595,6 +597,94 @@ def run_trimesh_bvh(args, rank):
                 "d2h_bytes_per_step": 80 * nt + 32 * (2 * nt - 1), "call": "psx_trimesh_build"},
         "cpu_baseline": {"value": 1e3 * statistics.median(cpu), "unit": "ms", "cores": 1, "kind": kind,
                          "sample": "3 builds of the same mesh (TriangleMesh's constructor)"},
+        "gpu_launches": None,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_registry(args, rank):
+    """Registry changes at scale, between frames of a batched world: --scenes scenes, one
+    character entity among their bodies each.  value: psx_world_apply_deltas of a batch
+    that patches the pose and writes the velocities of a tenth of the bodies (host fold,
+    one upload, one kernel); e2e: psx_world_move_characters of every scene's character.
+    Beside them, the reference doing the same through its registry and its
+    CharacterController, one scene after another on one host core, on a sample."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from scene_variants import character_moves, character_scene
+    from physecs_gb300.api import World, pack_deltas
+    if rank != 0:
+        return 0
+    n = args.scenes
+    base, chars = character_scene(n_chars=1, n_balls=200)
+    ss = [base] * n
+    w = World(ss)
+    nb = len(base.arrays["pos"])
+    rng = np.random.default_rng(3)
+    dyn = np.nonzero(base.arrays["flags"] & 1)[0]
+    k = max(1, nb // 10)
+
+    def batch():
+        rows = []
+        for sc in range(n):
+            for b in rng.choice(dyn, min(k, len(dyn)), replace=False):
+                rows.append({"scene": sc, "body": int(b), "pos": rng.uniform(-5, 5, 3) + [0, 3, 0], "quat": [0, 0, 0, 1],
+                             "vel": rng.normal(0, 1, 3), "ang_vel": [0, 0, 0]})
+        return pack_deltas(rows)
+    batches = [batch() for _ in range(args.steps + args.warmup)]
+    moves = character_moves(n, args.steps + args.warmup)
+    specs = [{"scene": sc, "body": chars[0], "height": 1.0, "radius": 0.3} for sc in range(n)]
+    dts, cts = [], []
+    for i in range(args.steps + args.warmup):
+        w.synchronize()
+        t = time.perf_counter()
+        w.apply_deltas(batches[i])
+        w.synchronize()
+        t1 = time.perf_counter()
+        w.move_characters(specs, moves[i])
+        t2 = time.perf_counter()
+        w.step(DT)
+        if i >= args.warmup:
+            dts.append(t1 - t)
+            cts.append(t2 - t1)
+    w.synchronize()
+    err = w.counts()["error"]
+    w.close()
+    if err:
+        raise RuntimeError("device error bits %d" % err)
+    # the reference on a sample of the scenes (the same per-scene work)
+    kind = cpu_kind()
+    sample = min(n, 32)
+    ref_d = ref_c = None
+    if kind == "reference":
+        from oracle.ref.ref_api import RefScene
+        sims = [RefScene(base) for _ in range(sample)]
+        per = len(batches[0]) // n
+        td = tc = 0.0
+        for i, r in enumerate(sims):
+            part = batches[0][i * per:(i + 1) * per]
+            t = time.perf_counter()
+            r.apply_deltas(part)
+            td += time.perf_counter() - t
+            t = time.perf_counter()
+            r.move_character(chars[0], 1.0, 0.3, moves[0][i])
+            tc += time.perf_counter() - t
+        ref_d, ref_c = 1e3 * td * n / sample, 1e3 * tc * n / sample
+    nd = len(batches[0])
+    line = {
+        "metric": "registry delta batch time", "value": 1e3 * statistics.median(dts), "unit": "ms", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(dts), "higher_is_better": False,
+        "scaling": "none", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded deltas and walks)",
+        "config": {"workload": "registry: %d scenes of %d bodies, %d pose+velocity deltas per batch, %d characters"
+                               % (n, nb, nd, n),
+                   "value": "psx_world_apply_deltas", "e2e": "psx_world_move_characters"},
+        "e2e": {"value": 1e3 * statistics.median(cts), "unit": "ms", "h2d_bytes_per_step": 40 * n, "d2h_bytes_per_step": n,
+                "call": "psx_world_move_characters"},
+        "cpu_baseline": {"value": ref_d, "unit": "ms", "cores": 1, "kind": kind,
+                         "characters_ms": ref_c,
+                         "sample": "%d scenes through the reference's registry and CharacterController, scaled to %d"
+                                   % (sample, n)},
         "gpu_launches": None,
     }
     print(json.dumps(line))

@@ -231,6 +231,36 @@ PSX_API psx_status psx_world_tune(psx_world* w, int32_t frames, psx_launch_confi
 /* The launch shapes in effect (after defaults, tuning or opts.launch). */
 PSX_API psx_status psx_world_launch_config(psx_world* w, psx_launch_config* out);
 
+/* ---- registry deltas: the changes a Physecs user makes to the registry between frames.
+ * A batch applies in array order, each record's fields in the order pose, velocity,
+ * kinematic:
+ *   PSX_DELTA_POSE      TransformComponent written, then registry.patch: the body's
+ *                       collider bounds are recomputed with the 0.01 m margin
+ *                       (onRigidBodyMove -> updateBounds, src/Physecs.cpp:51-54, 78-90);
+ *   PSX_DELTA_VELOCITY  RigidBodyDynamicComponent velocity and angularVelocity written;
+ *   PSX_DELTA_KINEMATIC Scene::setIsKinematic(entity, kinematic) (src/Physecs.cpp:753-770):
+ *                       the broadphase's dynamic flag, and zero velocities when it
+ *                       becomes kinematic. */
+#define PSX_DELTA_POSE 1
+#define PSX_DELTA_VELOCITY 2
+#define PSX_DELTA_KINEMATIC 4
+typedef struct psx_body_delta {
+    int32_t scene;
+    int32_t body;        /* scene-local body index */
+    int32_t mask;        /* PSX_DELTA_* bits */
+    int32_t kinematic;   /* PSX_DELTA_KINEMATIC: the new isKinematic */
+    float pos[3];
+    float quat[4];       /* x, y, z, w */
+    float vel[3];
+    float ang_vel[3];
+} psx_body_delta;
+/* Queues a batch of deltas on the world's stream, ahead of the next frame: one upload of
+ * the batch (coalesced per body on the host) and one kernel, plus a fix-up of the joints
+ * of bodies whose kinematic flag changed.  VELOCITY and KINEMATIC need a dynamic body;
+ * KINEMATIC is refused for a body with a joint in the overflow colour (a colour past
+ * the eighth, whose solve steps assume the dynamic bodies of creation time). */
+PSX_API psx_status psx_world_apply_deltas(psx_world* w, int32_t n, const psx_body_delta* deltas);
+
 /* ---- triangle meshes: the BVH of physecs::TriangleMesh, built on the device */
 typedef struct psx_trimesh_triangle {  /* Triangle (include/Physecs/TriangleMesh.h:9-14) */
     uint32_t indices[3];
@@ -318,6 +348,33 @@ typedef struct psx_overlap_mtd_hit {
  * triangle manifold).  Layout as psx_world_overlap; the filter field is not used. */
 PSX_API psx_status psx_world_overlap_mtd(psx_world* w, int32_t n, const psx_overlap_query* queries, int32_t cap,
                                          psx_overlap_mtd_hit* hits, int32_t* counts);
+/* physecs::CharacterController (include/Physecs/CharacterController.h:17-41) */
+typedef struct psx_character {
+    int32_t scene;
+    int32_t body;              /* the controller's entity (scene-local body); bodies of a batch differ */
+    float height, radius;
+    float max_step_height;     /* read only by the step-up test, which never fires (below) */
+    float slope_limit;         /* cosine of the steepest slope walked up (default cos 45 degrees) */
+    int32_t num_iterations;    /* default 2 */
+    float translation[3];
+} psx_character;
+#define PSX_CHARACTER_DOWN 1
+#define PSX_CHARACTER_SIDES 2
+#define PSX_CHARACTER_UP 4
+#define PSX_CHARACTER_TRUNCATED 0x80   /* an iteration met more than 32 contacts; the rest were skipped */
+/* CharacterController::move(translation, deltaTime) (src/CharacterController.cpp:5-45) for
+ * n controllers at once, on the device: the capsule (height / 2, radius) above the
+ * body is pushed out of what it overlaps, num_iterations times, and the body's pose is
+ * patched (its collider bounds get the 0.01 m margin).  flags_out[i] receives the
+ * CharacterCollisionFlags value.  As in the reference the step-up test never changes the
+ * translation: it calls Scene::raycastClosest without a filter, which never reports a
+ * hit (src/Physecs.cpp:580, 615).  The hits of one iteration apply in the order
+ * (collider, triangle) where the reference takes its tree's order, and the controllers
+ * of one batch see each other at their poses before the batch (the reference moves
+ * them one by one).  Waits. */
+PSX_API psx_status psx_world_move_characters(psx_world* w, int32_t n, const psx_character* chars, float dt,
+                                             uint8_t* flags_out);
+
 /* Trigger events: Scene::simulate's onTriggerEnter / onTriggerExit callbacks
  * (src/Physecs.cpp:537-552; listeners registered by addOnTriggerEnterCallback /
  * addOnTriggerExitCallback, :772-786).  With the default contact filter

@@ -229,6 +229,25 @@ int orc_scene_overlap_mtd(void* h, const float* pose, int type, const float* par
     return (int)hits.size();
 }
 
+// CharacterController::move of body b; returns its flags
+int orc_character_move(void* h, int b, float height, float radius, float max_step, float slope, int iterations,
+                       const float* translation) {
+    return static_cast<World*>(h)->moveCharacter(b, height, radius, max_step, slope, iterations,
+                                                 v3(translation[0], translation[1], translation[2]));
+}
+
+// A batch of registry deltas in array order (psx_body_delta; the scene field is unused)
+void orc_scene_apply_deltas(void* h, int n, const psx_body_delta* d) {
+    World* w = static_cast<World*>(h);
+    for (int i = 0; i < n; ++i) {
+        const psx_body_delta& e = d[i];
+        if (e.mask & PSX_DELTA_POSE) w->patchPose(e.body, v3(e.pos[0], e.pos[1], e.pos[2]), Q4{e.quat[0], e.quat[1], e.quat[2], e.quat[3]});
+        if (e.mask & PSX_DELTA_VELOCITY)
+            w->setVelocity(e.body, v3(e.vel[0], e.vel[1], e.vel[2]), v3(e.ang_vel[0], e.ang_vel[1], e.ang_vel[2]));
+        if (e.mask & PSX_DELTA_KINEMATIC) w->setIsKinematic(e.body, e.kinematic != 0);
+    }
+}
+
 // TriangleMesh::build (src/TriangleMesh.cpp:144-164) of the restatement: triangles in the
 // tree's order as 20 words each (indices, pad, bounds min/max, normal, centroid, each
 // padded to four) and nodes as 8 words (bounds min, triCount, bounds max, index); nodes

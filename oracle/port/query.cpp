@@ -304,6 +304,42 @@ bool World::overlapColliders(V3 pos0, Q4 or0, int c0, V3 pos1, Q4 or1, int c1) c
     return overlapGeom(pos0, or0, colliders[c0].g, pos1, or1, colliders[c1].g);
 }
 
+// CharacterController::move (CharacterController.cpp:5-45).  Its step-up test calls
+// Scene::raycastClosest without a filter, which never reports a hit (Physecs.cpp:580,
+// 615), so the translation always stays as given; maxStepHeight is never read.  The hits
+// of one iteration apply in the order (collider, triangle); the reference applies them in
+// its query tree's order, which only changes the rounding of the summed moves.
+int World::moveCharacter(int b, float height, float radius, float maxStepHeight, float slopeLimit, int iterations,
+                         V3 translation) {
+    (void)maxStepHeight;
+    Body& B = bodies[b];
+    const V3 up = qrot(B.q, v3(0, 1, 0));
+    B.pos += translation;
+    int flags = 0;
+    Geometry g;
+    g.type = CAPSULE;
+    g.p[0] = height * 0.5f;
+    g.p[1] = radius;
+    g.p[2] = 0.f;
+    std::vector<MtdHit> hits;
+    for (int i = 0; i < iterations; ++i) {
+        overlapMtd(B.pos + up * (height * 0.5f + radius), B.q, g, hits);
+        std::stable_sort(hits.begin(), hits.end(), [](const MtdHit& x, const MtdHit& y) {
+            return x.col < y.col || (x.col == y.col && x.tri < y.tri);
+        });
+        for (const MtdHit& h : hits) {
+            const float d = dot(h.n, up);
+            if (d > 0.001f) flags |= 1;
+            else if (d < -0.001f) flags |= 4;
+            else flags |= 2;
+            if (d > slopeLimit) B.pos += up * h.mtd / d;
+            else B.pos += h.n * h.mtd;
+        }
+    }
+    updateBounds(b, true);   // registry.patch<TransformComponent> -> onRigidBodyMove
+    return flags;
+}
+
 void World::overlapMtd(V3 pos, Q4 ori, const Geometry& g, std::vector<MtdHit>& out) const {
     const Bounds qb = getBounds(pos, ori, g);
     out.clear();
@@ -319,7 +355,7 @@ void World::overlapMtd(V3 pos, Q4 ori, const Geometry& g, std::vector<MtdHit>& o
                 float dist = dot(m.points[i].p0 - m.points[i].p1, m.normal);
                 if (dist > mtd) mtd = dist;
             }
-            out.push_back({c, m.normal, mtd});
+            out.push_back({c, m.normal, mtd, m.triangleIndex});
         }
     }
 }

@@ -133,6 +133,27 @@ void World::updateBounds(int b, bool margin) {
     }
 }
 
+// registry.patch<TransformComponent> after a pose write: Scene::onRigidBodyMove ->
+// updateBounds, with the margin (Physecs.cpp:51-54, 78-90)
+void World::patchPose(int b, V3 p, Q4 q) {
+    bodies[b].pos = p;
+    bodies[b].q = q;
+    updateBounds(b, true);
+}
+
+void World::setVelocity(int b, V3 v, V3 w) {
+    bodies[b].vel = v;
+    bodies[b].ang = w;
+}
+
+// Scene::setIsKinematic (Physecs.cpp:753-770)
+void World::setIsKinematic(int b, bool kinematic) {
+    Body& B = bodies[b];
+    B.kinematic = kinematic;
+    if (kinematic) { B.vel = {0, 0, 0}; B.ang = {0, 0, 0}; }
+    for (auto& e : bp) if (e.body == b) e.dynamic = !kinematic;
+}
+
 // Physecs.cpp:119-173
 void World::broadphase() {
     for (size_t i = 1; i < bp.size(); ++i) {

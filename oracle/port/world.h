@@ -139,8 +139,16 @@ struct World {
     int raycastClosest(V3 o, V3 d, float maxd, const uint8_t* accept, float& dist) const;
     void overlap(V3 pos, Q4 ori, const Geometry& g, int filter, std::vector<int>& out) const;
     // Scene::overlapWithMinTranslationalDistance: (collider, normal, mtd) per manifold with points
-    struct MtdHit { int col; V3 n; float mtd; };
+    struct MtdHit { int col; V3 n; float mtd; int tri; };
     void overlapMtd(V3 pos, Q4 ori, const Geometry& g, std::vector<MtdHit>& out) const;
+    // registry changes between frames: a patched pose (onRigidBodyMove -> updateBounds),
+    // written velocities, Scene::setIsKinematic (Physecs.cpp:51-54, 78-90, 753-770)
+    void patchPose(int b, V3 p, Q4 q);
+    void setVelocity(int b, V3 v, V3 w);
+    void setIsKinematic(int b, bool kinematic);
+    // CharacterController::move for body b (CharacterController.cpp:5-45); returns the
+    // CharacterCollisionFlags value
+    int moveCharacter(int b, float height, float radius, float maxStepHeight, float slopeLimit, int iterations, V3 translation);
     // physecs::overlap of two colliders at the given world poses (the trigger test)
     bool overlapColliders(V3 pos0, Q4 or0, int c0, V3 pos1, Q4 or1, int c1) const;
 };

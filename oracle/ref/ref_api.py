@@ -41,6 +41,9 @@ def lib():
         _lib.ref_scene_joint_colors.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
         _lib.ref_scene_trigger_events.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
         _lib.ref_trimesh_build.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+        _lib.ref_scene_apply_deltas.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        _lib.ref_character_move.argtypes = [C.c_void_p, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int,
+                                            C.c_void_p, C.c_float]
     return _lib
 
 
@@ -141,6 +144,19 @@ class RefScene:
         f = np.zeros((cap, 4), np.float32)
         m = lib().ref_scene_overlap_mtd(self.h, _p(pose), int(type_), _p(prm), int(mesh), _p(ids), _p(f), cap)
         return [(int(ids[k, 0]), int(ids[k, 1]), f[k, :3].copy(), f[k, 3]) for k in range(min(m, cap))]
+
+    def move_character(self, body, height, radius, translation, max_step_height=0.3, slope_limit=0.70710677,
+                       iterations=2, dt=1.0 / 60.0):
+        """physecs::CharacterController(...).move(translation, dt) for `body`; returns the
+        CharacterCollisionFlags value."""
+        t = np.ascontiguousarray(translation, np.float32)
+        return lib().ref_character_move(self.h, int(body), height, radius, max_step_height, slope_limit, int(iterations),
+                                        _p(t), dt)
+
+    def apply_deltas(self, deltas):
+        """Registry deltas in array order: a (n, 17) float32 array in psx_body_delta layout."""
+        d = np.ascontiguousarray(deltas, np.float32)
+        lib().ref_scene_apply_deltas(self.h, len(d), _p(d))
 
     def trigger_events(self):
         """Drain the recorded onTriggerEnter / onTriggerExit callbacks: an (n, 6) int32 array

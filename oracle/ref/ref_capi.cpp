@@ -27,6 +27,7 @@
 #include "UniversalJoint.h"
 #include "GearJoint.h"
 #include "ServoJoint.h"
+#include "CharacterController.h"
 #include "psx.h"
 
 #include <memory>
@@ -201,6 +202,38 @@ void ref_scene_step(void* h, float dt) {
     auto* w = static_cast<RefWorld*>(h);
     w->scene->simulate(dt);
     ++w->triggers.frame;
+}
+
+// physecs::CharacterController(scene, entity, height, radius, maxStepHeight, slopeLimit,
+// numIterations).move(translation, deltaTime); returns the flags' value
+int ref_character_move(void* h, int b, float height, float radius, float max_step, float slope, int iterations,
+                       const float* translation, float dt) {
+    auto* w = static_cast<RefWorld*>(h);
+    physecs::CharacterController cc(*w->scene, w->entities[b], height, radius, max_step, slope, iterations);
+    return cc.move(v3(translation), dt).value;
+}
+
+// Registry deltas as a Physecs user makes them, in array order: a pose written to the
+// TransformComponent and patched, velocities written to the RigidBodyDynamicComponent,
+// Scene::setIsKinematic (psx_body_delta; the scene field is unused)
+void ref_scene_apply_deltas(void* h, int n, const psx_body_delta* d) {
+    auto* w = static_cast<RefWorld*>(h);
+    for (int i = 0; i < n; ++i) {
+        const psx_body_delta& e = d[i];
+        entt::entity ent = w->entities[e.body];
+        if (e.mask & PSX_DELTA_POSE) {
+            auto& t = w->registry.get<TransformComponent>(ent);
+            t.position = v3(e.pos);
+            t.orientation = q4(e.quat);
+            w->registry.patch<TransformComponent>(ent);
+        }
+        if (e.mask & PSX_DELTA_VELOCITY) {
+            auto& dyn = w->registry.get<physecs::RigidBodyDynamicComponent>(ent);
+            dyn.velocity = v3(e.vel);
+            dyn.angularVelocity = v3(e.ang_vel);
+        }
+        if (e.mask & PSX_DELTA_KINEMATIC) w->scene->setIsKinematic(ent, e.kinematic != 0);
+    }
 }
 
 // physecs::TriangleMesh(vertices, indices) of the reference, dumped in the layout of

@@ -28,7 +28,8 @@ EXPORTS = ["psx_world_create", "psx_world_destroy", "psx_world_step", "psx_world
            "psx_server_release", "psx_server_stats", "psx_server_tick_begin", "psx_server_tick_end", "psx_server_world",
            "psx_server_tick_stages", "psx_server_device_bytes",
            "psx_world_tune", "psx_world_launch_config", "psx_world_raycast", "psx_world_overlap",
-           "psx_world_overlap_mtd", "psx_world_trigger_events", "psx_trimesh_build", "psx_world_update_trimesh"]
+           "psx_world_overlap_mtd", "psx_world_trigger_events", "psx_trimesh_build", "psx_world_update_trimesh",
+           "psx_world_apply_deltas", "psx_world_move_characters"]
 
 _lib = None
 
@@ -101,6 +102,8 @@ def load():
     lib.psx_world_trigger_events.argtypes = [vp, vp, C.c_int32, vp, vp]
     lib.psx_trimesh_build.argtypes = [C.c_int32, vp, C.c_int32, vp, C.c_int32, vp, vp, vp]
     lib.psx_world_update_trimesh.argtypes = [vp, C.c_int32, C.c_int32, vp]
+    lib.psx_world_apply_deltas.argtypes = [vp, C.c_int32, vp]
+    lib.psx_world_move_characters.argtypes = [vp, C.c_int32, vp, C.c_float, vp]
     lib.psx_server_stats.argtypes = [vp, vp]
     _lib = lib
     return lib
@@ -295,6 +298,30 @@ class World:
                         for k in range(i * cap, i * cap + m)])
         return counts[:n].copy(), res
 
+    def apply_deltas(self, deltas):
+        """psx_world_apply_deltas: registry changes in array order, ahead of the next frame;
+        deltas is pack_deltas' (n, 17) array or a list of its dicts."""
+        d = pack_deltas(deltas) if isinstance(deltas, (list, tuple)) else np.ascontiguousarray(deltas, np.float32)
+        _check(load().psx_world_apply_deltas(self.h, len(d), _p(d)))
+
+    def move_characters(self, chars, translations, dt=1.0 / 60.0):
+        """psx_world_move_characters.  chars: dicts {scene, body, height, radius,
+        max_step_height (0.3), slope_limit (cos 45 deg), iterations (2)}; translations: (n, 3).
+        Returns the flags (n,) uint8."""
+        n = len(chars)
+        buf = np.zeros((max(n, 1), 10), np.float32)
+        iv = buf.view(np.int32)
+        t = np.asarray(translations, np.float32).reshape(-1, 3)
+        for i, c in enumerate(chars):
+            iv[i, 0], iv[i, 1] = c.get("scene", 0), c["body"]
+            buf[i, 2], buf[i, 3] = c["height"], c["radius"]
+            buf[i, 4], buf[i, 5] = c.get("max_step_height", 0.3), c.get("slope_limit", 0.70710677)
+            iv[i, 6] = c.get("iterations", 2)
+            buf[i, 7:10] = t[i]
+        flags = np.zeros(max(n, 1), np.uint8)
+        _check(load().psx_world_move_characters(self.h, n, _p(buf), C.c_float(dt), _p(flags)))
+        return flags[:n]
+
     def update_trimesh(self, scene, mesh, vertices):
         """psx_world_update_trimesh: new vertices (same count) for triangle mesh `mesh` of
         `scene`, its BVH rebuilt on the device and its colliders' bounds recomputed."""
@@ -486,3 +513,28 @@ def trimesh_build(vertices, indices, device=0):
     n = C.c_int32()
     _check(load().psx_trimesh_build(device, _p(v), len(v), _p(ix), len(ix), _p(tris), _p(nodes), C.byref(n)))
     return tris[:nt], nodes[:n.value]
+
+
+DELTA_POSE, DELTA_VELOCITY, DELTA_KINEMATIC = 1, 2, 4
+
+
+def pack_deltas(deltas):
+    """psx_body_delta records, (n, 17) float32 (int fields as their bits), from dicts
+    {scene, body, pos + quat (a patched pose), vel + ang_vel (written velocities),
+    kinematic (Scene::setIsKinematic)}; absent keys leave that part out."""
+    out = np.zeros((len(deltas), 17), np.float32)
+    iv = out.view(np.int32)
+    for i, d in enumerate(deltas):
+        mask = 0
+        iv[i, 0], iv[i, 1] = d.get("scene", 0), d["body"]
+        if d.get("pos") is not None:
+            mask |= DELTA_POSE
+            out[i, 4:7], out[i, 7:11] = d["pos"], d.get("quat", (0.0, 0.0, 0.0, 1.0))
+        if d.get("vel") is not None:
+            mask |= DELTA_VELOCITY
+            out[i, 11:14], out[i, 14:17] = d["vel"], d.get("ang_vel", (0.0, 0.0, 0.0))
+        if d.get("kinematic") is not None:
+            mask |= DELTA_KINEMATIC
+            iv[i, 3] = int(bool(d["kinematic"]))
+        iv[i, 2] = mask
+    return out

@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(256) k_trimesh_bounds_part(World w, int c0, in
     }
 }
 
-__global__ void k_trimesh_bounds_final(World w, int c0, int c1) {
+__global__ void k_trimesh_bounds_final(World w, int c0, int c1, int margin) {
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < w.n_trimesh_cols; t += gridDim.x * blockDim.x) {
         const int c = w.trimesh_cols[t];
         if (c < c0 || c >= c1) continue;
@@ -104,9 +104,79 @@ __global__ void k_trimesh_bounds_final(World w, int c0, int c1) {
             const V3 v = mesh_vertex_world(w, c, tm, j < 3 ? key_min_index(k) : key_max_index(k), pos, ori);
             b[j] = (j % 3) == 0 ? v.x : ((j % 3) == 1 ? v.y : v.z);
         }
-        w.aabb_min[c] = make_float4(b[0], b[1], b[2], 0.f);
-        w.aabb_max[c] = make_float4(b[3], b[4], b[5], 0.f);
+        Bounds bb{{b[0], b[1], b[2]}, {b[3], b[4], b[5]}};
+        if (margin) { bb.max += v3s(0.01f); bb.min -= v3s(0.01f); }
+        w.aabb_min[c] = st4(bb.min);
+        w.aabb_max[c] = st4(bb.max);
     }
+}
+
+// Registry deltas, one coalesced record per body (the host folded the batch in order):
+// pose, velocity, the kinematic flag and the broadphase's dynamic flag of the body's
+// colliders; a posed body's colliders get updateBounds' bounds with the margin
+// (src/Physecs.cpp:51-54, 78-90, 753-770).  Triangle-mesh colliders are left to
+// k_trimesh_bounds_*.
+__global__ void k_apply_deltas(World w, const DeltaRec* d, int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const DeltaRec e = d[i];
+        const int b = e.body;
+        int4 inf = w.info[b];
+        if (e.mask & DELTA_POSE) {
+            w.pos[b] = make_float4(e.pos[0], e.pos[1], e.pos[2], 0.f);
+            w.quat[b] = make_float4(e.quat[0], e.quat[1], e.quat[2], e.quat[3]);
+        }
+        if ((e.mask & DELTA_VELOCITY) && inf.z >= 0) {
+            w.vel[inf.z] = make_float4(e.vel[0], e.vel[1], e.vel[2], 0.f);
+            w.ang[inf.z] = make_float4(e.ang[0], e.ang[1], e.ang[2], 0.f);
+        }
+        if (e.mask & DELTA_KINEMATIC) {
+            inf.y = e.kinematic ? (inf.y | BODY_KIN) : (inf.y & ~BODY_KIN);
+            w.info[b] = inf;
+        }
+        const bool sim = (inf.y & BODY_DYN) && !(inf.y & BODY_KIN);
+        const Q4 bq = ld4(w.quat[b]);
+        const V3 bp = ld3(w.pos[b]);
+        for (int c = w.body_col[b]; c < w.body_col[b + 1]; ++c) {
+            int4 ci = w.col_info[c];
+            if (e.mask & DELTA_KINEMATIC) {
+                ci.w = sim ? (ci.w | COL_DYNAMIC) : (ci.w & ~COL_DYNAMIC);
+                w.col_info[c] = ci;
+            }
+            if (!(e.mask & DELTA_POSE) || ci.y == G_TRIMESH) continue;
+            const V3 pos = bp + qrot(bq, ld3(w.col_pos[c]));
+            const Q4 ori = qmul(bq, ld4(w.col_quat[c]));
+            const float4 pr = w.col_params[c];
+            const GeomD g{ci.y, {pr.x, pr.y, pr.z}, ci.z};
+            Bounds bb = getBounds(w, pos, ori, g);
+            bb.max += v3s(0.01f);
+            bb.min -= v3s(0.01f);
+            w.aabb_min[c] = st4(bb.min);
+            w.aabb_max[c] = st4(bb.max);
+        }
+    }
+}
+
+// The joints of bodies whose kinematic flag changed: the simulated ends and the anchors
+// relative to their centre of mass, as the reference takes them each frame
+// (src/Physecs.cpp:335-345)
+__global__ void k_joint_fix(World w, const int* js, int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        JointDev& J = w.joints[js[i]];
+        const int4 i0 = w.info[J.body0], i1 = w.info[J.body1];
+        const bool s0 = (i0.y & BODY_DYN) && !(i0.y & BODY_KIN), s1 = (i1.y & BODY_DYN) && !(i1.y & BODY_KIN);
+        J.b0 = s0 ? i0.z : -1;
+        J.b1 = s1 ? i1.z : -1;
+        const V3 a0 = ld3(J.a0p), a1 = ld3(J.a1p);
+        J.r0 = st4(s0 ? a0 - ld3(w.com[i0.z]) : a0);
+        J.r1 = st4(s1 ? a1 - ld3(w.com[i1.z]) : a1);
+    }
+}
+
+int launch_apply_deltas(const World& w, const DeltaRec* d, int n, const int* joints, int nj, cudaStream_t s) {
+    int k = 0;
+    if (n > 0) { k_apply_deltas<<<(n + 127) / 128, 128, 0, s>>>(w, d, n); ++k; }
+    if (nj > 0) { k_joint_fix<<<(nj + 127) / 128, 128, 0, s>>>(w, joints, nj); ++k; }
+    return k;
 }
 
 int launch_aabb(const World& w, int margin_mode, cudaStream_t s) {
@@ -116,13 +186,18 @@ int launch_aabb(const World& w, int margin_mode, cudaStream_t s) {
 int launch_aabb_range(const World& w, int c0, int c1, int margin_mode, cudaStream_t s) {
     if (c1 <= c0) return 0;
     k_aabb<<<(c1 - c0 + 255) / 256, 256, 0, s>>>(w, c0, c1, margin_mode);
-    if (margin_mode == 1 || !w.n_trimesh_cols) return 1;
+    if (margin_mode == 1) return 1;
+    return 1 + launch_trimesh_bounds(w, c0, c1, false, s);
+}
+
+int launch_trimesh_bounds(const World& w, int c0, int c1, bool margin, cudaStream_t s) {
+    if (!w.n_trimesh_cols || c1 <= c0) return 0;
     const size_t n3 = 3 * (size_t)w.n_trimesh_cols;
     cudaMemsetAsync(w.trimesh_keys, 0xff, n3 * sizeof(unsigned long long), s);
     cudaMemsetAsync(w.trimesh_keys + n3, 0, n3 * sizeof(unsigned long long), s);
     k_trimesh_bounds_part<<<w.n_trimesh_chunks, 256, 0, s>>>(w, c0, c1);
-    k_trimesh_bounds_final<<<(w.n_trimesh_cols + 127) / 128, 128, 0, s>>>(w, c0, c1);
-    return 3;
+    k_trimesh_bounds_final<<<(w.n_trimesh_cols + 127) / 128, 128, 0, s>>>(w, c0, c1, margin ? 1 : 0);
+    return 2;
 }
 
 // ---------------------------------------------------------------- Morton keys

@@ -93,6 +93,12 @@ struct FrameBuf {
 // kernels it queued
 int launch_aabb(const World& w, int margin_mode, cudaStream_t s);
 int launch_aabb_range(const World& w, int c0, int c1, int margin_mode, cudaStream_t s);
+// getBoundsTriangleMesh for the triangle-mesh colliders in [c0, c1), with the 0.01 m
+// margin of updateBounds or without it
+int launch_trimesh_bounds(const World& w, int c0, int c1, bool margin, cudaStream_t s);
+// a coalesced batch of registry deltas (one record per body), then the joints of the
+// bodies whose kinematic flag changed
+int launch_apply_deltas(const World& w, const DeltaRec* d, int n, const int* joints, int nj, cudaStream_t s);
 // scene_sort_pmax > 0: every scene has at most that many colliders (a power of two) and
 // is sorted by its own block in shared memory; 0: one radix sort over the whole world
 int launch_broadphase(const World& w, FrameBuf& f, int scene_bits, int scene_sort_pmax, cudaStream_t s);
@@ -113,6 +119,14 @@ struct ShapeIn {
 int launch_raycast(const World& w, FrameBuf& f, const RayIn* rays, int n, const unsigned char* accept, RayOut* out,
                    cudaStream_t s);
 int launch_overlap(const World& w, FrameBuf& f, const ShapeIn* qs, int n, int cap, int* counts, int* hits, cudaStream_t s);
+// one CharacterController::move per record (psx_character layout; body is the world index)
+struct CharIn {
+    int scene, body;
+    float height, radius, max_step_height, slope_limit;
+    int iterations;
+    float tx, ty, tz;
+};
+int launch_move_characters(const World& w, FrameBuf& f, const CharIn* cs, int n, unsigned char* flags, cudaStream_t s);
 int launch_overlap_mtd(const World& w, FrameBuf& f, const ShapeIn* qs, int n, int cap, int* counts, float4* hits,
                        int* hit_col, cudaStream_t s);
 // a second stream with a fork / join event pair, for kernels that may overlap

@@ -436,22 +436,16 @@ __device__ inline int collision_one(const World& w, V3 pos0, Q4 or0, GeomD g0, V
 // whose bounds meet the query shape's; for each manifold with points of the collision
 // (collider first, shape second) its normal and the deepest point, max(0, max over the
 // points of dot(p0 - p1, n)).  Up to cap records a query: {world collider, n xyz, mtd}.
-__global__ void __launch_bounds__(64) k_overlap_mtd(World w, FrameBuf f, const ShapeIn* qs, int n, int cap, int* counts,
-                                                    float4* hits, int* hit_col) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const ShapeIn qi = qs[i];
-    const V3 pos = {qi.px, qi.py, qi.pz};
-    const Q4 ori = {qi.qx, qi.qy, qi.qz, qi.qw};
-    const GeomD g = GeomD{qi.type, {qi.p0, qi.p1, qi.p2}, qi.mesh};
+// The MTD query of overlapWithMinTranslationalDistance: every collider of scene s whose
+// bounds meet the shape's, collided with the collider first; fn(collider, manifold, mtd)
+// for each manifold with points, mtd = max(0, deepest dot(p0 - p1, normal)).  The walk
+// visits the scene's tree left first.
+template <class F>
+__device__ void for_each_mtd(const World& w, const FrameBuf& f, int s, V3 pos, Q4 ori, const GeomD& g, ManifoldL* ms,
+                             TCI* cand, Polytope& poly, F&& fn) {
     const Bounds b = getBounds(w, pos, ori, g);
     const float4 qmin = make_float4(b.min.x, b.min.y, b.min.z, 0.f), qmax = make_float4(b.max.x, b.max.y, b.max.z, 0.f);
-    const int s = qi.scene;
     const int cs = w.scene_col[s], nc = w.scene_col[s + 1] - cs;
-    ManifoldL ms[kTriManifolds];
-    TCI cand[kTriCandidates];
-    Polytope poly;
-    int count = 0;
     auto leaf = [&](int q) {
         const int c = f.order[q];
         if (!boxes_meet(qmin, qmax, w.aabb_min[c], w.aabb_max[c])) return;
@@ -468,11 +462,7 @@ __global__ void __launch_bounds__(64) k_overlap_mtd(World w, FrameBuf f, const S
                 float dist = dot(m.points[p].p0 - m.points[p].p1, m.normal);
                 if (dist > mtd) mtd = dist;
             }
-            if (count < cap) {
-                hits[(size_t)i * cap + count] = make_float4(m.normal.x, m.normal.y, m.normal.z, mtd);
-                hit_col[(size_t)i * cap + count] = c;
-            }
-            ++count;
+            fn(c, m, mtd);
         }
     };
     if (nc == 1) {
@@ -490,7 +480,98 @@ __global__ void __launch_bounds__(64) k_overlap_mtd(World w, FrameBuf f, const S
             stack[sp++] = f.bvh.left[c];
         }
     }
+}
+
+__global__ void __launch_bounds__(64) k_overlap_mtd(World w, FrameBuf f, const ShapeIn* qs, int n, int cap, int* counts,
+                                                    float4* hits, int* hit_col) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const ShapeIn qi = qs[i];
+    const V3 pos = {qi.px, qi.py, qi.pz};
+    const Q4 ori = {qi.qx, qi.qy, qi.qz, qi.qw};
+    const GeomD g = GeomD{qi.type, {qi.p0, qi.p1, qi.p2}, qi.mesh};
+    ManifoldL ms[kTriManifolds];
+    TCI cand[kTriCandidates];
+    Polytope poly;
+    int count = 0;
+    for_each_mtd(w, f, qi.scene, pos, ori, g, ms, cand, poly, [&](int c, const ManifoldL& m, float mtd) {
+        if (count < cap) {
+            hits[(size_t)i * cap + count] = make_float4(m.normal.x, m.normal.y, m.normal.z, mtd);
+            hit_col[(size_t)i * cap + count] = c;
+        }
+        ++count;
+    });
     counts[i] = count;
+}
+
+// CharacterController::move (src/CharacterController.cpp:5-45) for one controller a
+// thread.  The reference's step-up test calls Scene::raycastClosest without a filter,
+// which never reports a hit (src/Physecs.cpp:580, 615), so the translation stays as
+// given.  Each iteration collects the capsule's MTD hits and applies them in the order
+// (collider, triangle); the reference applies them in its tree's order, which only
+// changes the rounding of the summed moves.  Controllers of one batch see each other
+// at their poses before the batch.
+constexpr int kCharHits = 32;
+__global__ void __launch_bounds__(64) k_move_characters(World w, FrameBuf f, const CharIn* cs, int n, unsigned char* flags_out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const CharIn ch = cs[i];
+    const int b = ch.body;
+    const Q4 q = ld4(w.quat[b]);
+    V3 p = ld3(w.pos[b]);
+    const V3 up = qrot(q, V3{0.f, 1.f, 0.f});
+    p += V3{ch.tx, ch.ty, ch.tz};
+    const GeomD g{G_CAPSULE, {ch.height * 0.5f, ch.radius, 0.f}, -1};
+    ManifoldL ms[kTriManifolds];
+    TCI cand[kTriCandidates];
+    Polytope poly;
+    int hc[kCharHits], ht[kCharHits];
+    float4 hv[kCharHits];
+    int flags = 0;
+    for (int it = 0; it < ch.iterations; ++it) {
+        int nh = 0;
+        for_each_mtd(w, f, w.info[b].w, p + up * (ch.height * 0.5f + ch.radius), q, g, ms, cand, poly,
+                     [&](int c, const ManifoldL& m, float mtd) {
+                         if (nh == kCharHits) { flags |= 0x80; return; }
+                         // insertion by (collider, triangle), stable
+                         int k = nh++;
+                         while (k > 0 && (hc[k - 1] > c || (hc[k - 1] == c && ht[k - 1] > m.triangleIndex))) {
+                             hc[k] = hc[k - 1]; ht[k] = ht[k - 1]; hv[k] = hv[k - 1];
+                             --k;
+                         }
+                         hc[k] = c; ht[k] = m.triangleIndex;
+                         hv[k] = make_float4(m.normal.x, m.normal.y, m.normal.z, mtd);
+                     });
+        for (int k = 0; k < nh; ++k) {
+            const V3 nrm = ld3(hv[k]);
+            const float mtd = hv[k].w;
+            const float d = dot(nrm, up);
+            flags |= d > 0.001f ? 1 : (d < -0.001f ? 4 : 2);
+            if (d > ch.slope_limit) p += up * mtd / d;
+            else p += nrm * mtd;
+        }
+    }
+    w.pos[b] = st4(p);
+    // registry.patch<TransformComponent> -> updateBounds, with the margin
+    for (int c = w.body_col[b]; c < w.body_col[b + 1]; ++c) {
+        const int4 ci = w.col_info[c];
+        if (ci.y == G_TRIMESH) continue;
+        const V3 cp = p + qrot(q, ld3(w.col_pos[c]));
+        const Q4 co = qmul(q, ld4(w.col_quat[c]));
+        const float4 pr = w.col_params[c];
+        Bounds bb = getBounds(w, cp, co, GeomD{ci.y, {pr.x, pr.y, pr.z}, ci.z});
+        bb.max += v3s(0.01f);
+        bb.min -= v3s(0.01f);
+        w.aabb_min[c] = st4(bb.min);
+        w.aabb_max[c] = st4(bb.max);
+    }
+    flags_out[i] = (unsigned char)flags;
+}
+
+int launch_move_characters(const World& w, FrameBuf& f, const CharIn* cs, int n, unsigned char* flags, cudaStream_t s) {
+    if (n <= 0) return 0;
+    k_move_characters<<<(n + 63) / 64, 64, 0, s>>>(w, f, cs, n, flags);
+    return 1;
 }
 
 int launch_overlap_mtd(const World& w, FrameBuf& f, const ShapeIn* qs, int n, int cap, int* counts, float4* hits,
@@ -787,6 +868,52 @@ PSX_API psx_status psx_world_overlap_mtd(psx_world* W, int32_t n, const psx_over
         }
     }
     return PSX_OK;
+}
+
+PSX_API psx_status psx_world_move_characters(psx_world* W, int32_t n, const psx_character* chars, float dt,
+                                             uint8_t* flags_out) {
+    (void)dt;   // read by the reference only inside the step-up branch, which never runs
+    if (!W || n < 0 || (n && (!chars || !flags_out))) return fail(PSX_ERR_INVALID_ARG, "psx_world_move_characters: bad arguments");
+    PSX_CUDA(cudaSetDevice(W->device));
+    if (n == 0) return PSX_OK;
+    static_assert(sizeof(psx_character) == sizeof(CharIn), "psx_character layout");
+    std::vector<CharIn> in(n);
+    psx_status st = PSX_OK;
+    for (int i = 0; i < n; ++i) {
+        const psx_character& c = chars[i];
+        if (c.scene < 0 || c.scene >= W->n_scenes || c.body < 0 ||
+            c.body >= W->h_scene_body[c.scene + 1] - W->h_scene_body[c.scene] || c.num_iterations < 0 ||
+            !(c.height >= 0.f) || !(c.radius >= 0.f)) {
+            st = fail(PSX_ERR_INVALID_ARG, "psx_world_move_characters: record " + std::to_string(i));
+            break;
+        }
+        const int b = W->h_scene_body[c.scene] + c.body;
+        if (W->h_delta_slot[b] >= 0) {
+            st = fail(PSX_ERR_INVALID_ARG, "psx_world_move_characters: one body twice in a batch");
+            break;
+        }
+        W->h_delta_slot[b] = i;
+        in[i] = CharIn{c.scene, b, c.height, c.radius, c.max_step_height, c.slope_limit, c.num_iterations,
+                       c.translation[0], c.translation[1], c.translation[2]};
+    }
+    for (int i = 0; i < n; ++i)
+        if (chars[i].scene >= 0 && chars[i].scene < W->n_scenes) {
+            const int b = W->h_scene_body[chars[i].scene] + chars[i].body;
+            if (b >= 0 && b < (int)W->h_delta_slot.size()) W->h_delta_slot[b] = -1;
+        }
+    if (st != PSX_OK) return st;
+    const size_t in_b = align256(sizeof(CharIn) * n);
+    char* buf = nullptr;
+    PSX_TRY(query_buffer(W, in_b + n, &buf));
+    CharIn* d_in = reinterpret_cast<CharIn*>(buf);
+    unsigned char* d_fl = reinterpret_cast<unsigned char*>(buf + in_b);
+    cudaStream_t s = W->stream;
+    PSX_CUDA(cudaMemcpyAsync(d_in, in.data(), sizeof(CharIn) * n, cudaMemcpyHostToDevice, s));
+    query_trees(W);
+    launch_move_characters(W->w, W->f, d_in, n, d_fl, s);
+    PSX_CUDA(cudaMemcpyAsync(flags_out, d_fl, n, cudaMemcpyDeviceToHost, s));
+    PSX_CUDA(cudaStreamSynchronize(s));
+    return check_err(W);
 }
 
 PSX_API psx_status psx_world_trigger_events(psx_world* W, psx_trigger_event* out, int32_t cap, int32_t* n_out,

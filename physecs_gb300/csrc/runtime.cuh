@@ -45,6 +45,17 @@ struct psx_world {
     std::vector<int> h_scene_trimesh;      // per scene (+1): first world triangle mesh
     std::vector<psx::TriMeshDev> h_trimesh;
     std::vector<int> h_col_trimesh;        // per collider: world triangle mesh, or -1
+    // registry deltas
+    std::vector<int> h_body_col;           // [n_bodies + 1] each body's first collider
+    std::vector<int> h_body_flags;         // PSX_BODY_* as the device holds them
+    std::vector<int> h_bj_start, h_bj;     // joints of each body (CSR)
+    std::vector<char> h_body_overflow;     // 1: the body has a joint in the overflow colour
+    std::vector<int> h_delta_slot;         // per body: its record in the batch being packed, or -1
+    psx_body_delta* dpin = nullptr;        // pinned staging of a delta batch (records, then joint ids)
+    size_t dpin_bytes = 0;
+    char* ddev = nullptr;                  // device copy of the batch
+    size_t ddev_bytes = 0;
+    cudaEvent_t ev_delta = nullptr;        // the last batch's upload is done
     void* qbuf = nullptr;                  // scene-query staging on the device
     std::vector<psx_trigger_event> trig_pending;   // drained from the device, not yet delivered
     long long trig_lost = 0;               // events past the device log's capacity
@@ -111,6 +122,9 @@ struct psx_world {
         for (void* p : allocs) cudaFree(p);
         if (pin) cudaFreeHost(pin);
         if (qbuf) cudaFree(qbuf);
+        if (dpin) cudaFreeHost(dpin);
+        if (ddev) cudaFree(ddev);
+        if (ev_delta) cudaEventDestroy(ev_delta);
         if (ev_fork) cudaEventDestroy(ev_fork);
         if (ev_fork2) cudaEventDestroy(ev_fork2);
         if (ev_join2) cudaEventDestroy(ev_join2);

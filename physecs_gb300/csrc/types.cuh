@@ -124,6 +124,14 @@ struct SPt {
 };
 constexpr int kHdrF4 = 3, kPtF4 = 7;
 
+// one body's registry changes of a batch (the layout of psx_body_delta; body is the
+// world body index once the host has coalesced the batch)
+enum : int { DELTA_POSE = 1, DELTA_VELOCITY = 2, DELTA_KINEMATIC = 4 };
+struct DeltaRec {
+    int scene, body, mask, kinematic;
+    float pos[3], quat[4], vel[3], ang[3];
+};
+
 struct CacheEntry {      // restitution cache (include/Physecs/Physecs.h:127-135)
     unsigned long long key;
     int np, pad;
@@ -143,6 +151,7 @@ struct World {
     float4* pos;         // xyz
     float4* quat;
     int4* info;          // entity, flags, dyn index, scene
+    int* body_col;       // [n_bodies + 1] each body's first collider
     // dynamic bodies
     int* dyn_body;
     float4* vel;         // component velocity

@@ -86,6 +86,8 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
     std::vector<float4> tri_verts;
     std::vector<int4> tri_src;    // per triangle: mesh-local vertex indices, w = the mesh's first vertex
     int n_tri_nodes = 0;
+    std::vector<int2> body_joint;       // (body, joint) for every joint end
+    std::vector<int> overflow_bodies;   // bodies with a joint in the overflow colour
     std::vector<JointDev> joints;
     std::vector<int2> nc;
     std::vector<int> jsched, jstep_start{0}, scene_jsteps{0};
@@ -150,6 +152,8 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
                 for (int k = 0; k < 3; ++k) invI.push_back(f4(d.inv_inertia[9 * b + 3 * k], d.inv_inertia[9 * b + 3 * k + 1], d.inv_inertia[9 * b + 3 * k + 2]));
             }
             info.push_back(make_int4((int)d.entity[b], (int)fl, di, s));
+            W->h_body_col.push_back((int)col_info.size());
+            W->h_body_flags.push_back((int)fl);
             W->h_entity.push_back(d.entity[b]);
             W->h_body_dyn.push_back(di);
             for (int c = d.collider_start[b]; c < d.collider_start[b + 1]; ++c) {
@@ -181,6 +185,9 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
             bits[b0] |= (unsigned char)(1u << c);
             bits[b1] |= (unsigned char)(1u << c);
             colors[c].push_back(j);
+            body_joint.push_back(make_int2(bbase + b0, jbase + j));
+            body_joint.push_back(make_int2(bbase + b1, jbase + j));
+            if (c == 8) overflow_bodies.push_back(bbase + b0), overflow_bodies.push_back(bbase + b1);
             int lo = std::min(bbase + b0, bbase + b1), hi = std::max(bbase + b0, bbase + b1);
             nc.push_back(make_int2(lo, hi));
             JointDev J{};
@@ -242,6 +249,19 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
     std::sort(nc.begin(), nc.end(), [](int2 a, int2 b) { return a.x < b.x || (a.x == b.x && a.y < b.y); });
     nc.erase(std::unique(nc.begin(), nc.end(), [](int2 a, int2 b) { return a.x == b.x && a.y == b.y; }), nc.end());
     W->h_scene_body = scene_body;
+    W->h_body_col.push_back((int)col_info.size());
+    {
+        const int nb = (int)pos.size();
+        std::sort(body_joint.begin(), body_joint.end(), [](int2 a, int2 b) { return a.x < b.x || (a.x == b.x && a.y < b.y); });
+        W->h_bj_start.assign(nb + 1, 0);
+        for (const int2& e : body_joint) ++W->h_bj_start[e.x + 1];
+        for (int b = 0; b < nb; ++b) W->h_bj_start[b + 1] += W->h_bj_start[b];
+        W->h_bj.clear();
+        for (const int2& e : body_joint) W->h_bj.push_back(e.y);
+        W->h_body_overflow.assign(nb, 0);
+        for (int b : overflow_bodies) W->h_body_overflow[b] = 1;
+        W->h_delta_slot.assign(nb, -1);
+    }
     W->h_scene_convex.push_back((int)convex.size());
     W->h_scene_trimesh.push_back((int)trimesh.size());
     W->h_scene_col = scene_col;
@@ -262,6 +282,7 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
             return fail(PSX_ERR_CAPACITY, "triangle mesh above " + std::to_string(tri_max) + " triangles in a world of " +
                                               std::to_string(w.n_colliders) + " colliders");
     PSX_TRY(W->upload(w.scene_body, scene_body));
+    PSX_TRY(W->upload(w.body_col, W->h_body_col));
     PSX_TRY(W->upload(w.scene_col, scene_col));
     PSX_TRY(W->upload(w.scene_dyn, scene_dyn));
     PSX_TRY(W->upload(w.scene_joint, scene_joint));
@@ -939,6 +960,107 @@ PSX_API psx_status psx_world_write_bodies(psx_world* W, const float* pos, const 
     if (nd && vel) PSX_CUDA(cudaMemcpyAsync(w.vel, hv, nd * sizeof(float4), cudaMemcpyHostToDevice, W->stream));
     if (nd && ang) PSX_CUDA(cudaMemcpyAsync(w.ang, ha, nd * sizeof(float4), cudaMemcpyHostToDevice, W->stream));
     PSX_CUDA(cudaStreamSynchronize(W->stream));
+    return PSX_OK;
+}
+
+PSX_API psx_status psx_world_apply_deltas(psx_world* W, int32_t n, const psx_body_delta* d) {
+    if (!W || n < 0 || (n && !d)) return fail(PSX_ERR_INVALID_ARG, "psx_world_apply_deltas: bad arguments");
+    if (n == 0) return PSX_OK;
+    static_assert(sizeof(psx_body_delta) == sizeof(DeltaRec), "psx_body_delta layout");
+    PSX_CUDA(cudaSetDevice(W->device));
+    // fold the batch per body, in order: a kinematic toggle zeroes the velocities at its point
+    std::vector<DeltaRec> recs;
+    psx_status st = PSX_OK;
+    for (int i = 0; i < n && st == PSX_OK; ++i) {
+        const psx_body_delta& e = d[i];
+        if (e.scene < 0 || e.scene >= W->n_scenes || e.body < 0 ||
+            e.body >= W->h_scene_body[e.scene + 1] - W->h_scene_body[e.scene] || (e.mask & ~7)) {
+            st = fail(PSX_ERR_INVALID_ARG, "psx_world_apply_deltas: scene, body or mask of record " + std::to_string(i));
+            break;
+        }
+        const int b = W->h_scene_body[e.scene] + e.body;
+        if ((e.mask & (PSX_DELTA_VELOCITY | PSX_DELTA_KINEMATIC)) && W->h_body_dyn[b] < 0) {
+            st = fail(PSX_ERR_INVALID_ARG, "psx_world_apply_deltas: velocity or kinematic flag of a static body");
+            break;
+        }
+        if ((e.mask & PSX_DELTA_KINEMATIC) && W->h_body_overflow[b]) {
+            st = fail(PSX_ERR_INVALID_ARG, "psx_world_apply_deltas: kinematic flag of a body jointed in the overflow colour");
+            break;
+        }
+        int& slot = W->h_delta_slot[b];
+        if (slot < 0) {
+            slot = (int)recs.size();
+            DeltaRec r{};
+            r.body = b;
+            recs.push_back(r);
+        }
+        DeltaRec& r = recs[slot];
+        if (e.mask & PSX_DELTA_POSE) {
+            r.mask |= DELTA_POSE;
+            for (int k = 0; k < 3; ++k) r.pos[k] = e.pos[k];
+            for (int k = 0; k < 4; ++k) r.quat[k] = e.quat[k];
+        }
+        if (e.mask & PSX_DELTA_VELOCITY) {
+            r.mask |= DELTA_VELOCITY;
+            for (int k = 0; k < 3; ++k) { r.vel[k] = e.vel[k]; r.ang[k] = e.ang_vel[k]; }
+        }
+        if (e.mask & PSX_DELTA_KINEMATIC) {
+            r.mask |= DELTA_KINEMATIC;
+            r.kinematic = e.kinematic != 0;
+            if (r.kinematic) {
+                r.mask |= DELTA_VELOCITY;
+                for (int k = 0; k < 3; ++k) r.vel[k] = r.ang[k] = 0.f;
+            }
+        }
+    }
+    for (const DeltaRec& r : recs) W->h_delta_slot[r.body] = -1;
+    if (st != PSX_OK) return st;
+    // kinematic flags on the host, and the joints to fix up
+    std::vector<int> joints;
+    for (const DeltaRec& r : recs) {
+        if (!(r.mask & DELTA_KINEMATIC)) continue;
+        int& fl = W->h_body_flags[r.body];
+        const bool was_sim = (fl & PSX_BODY_DYNAMIC) && !(fl & PSX_BODY_KINEMATIC);
+        fl = r.kinematic ? (fl | PSX_BODY_KINEMATIC) : (fl & ~PSX_BODY_KINEMATIC);
+        const bool sim = (fl & PSX_BODY_DYNAMIC) && !(fl & PSX_BODY_KINEMATIC);
+        W->n_simulated += (int)sim - (int)was_sim;
+        for (int k = W->h_bj_start[r.body]; k < W->h_bj_start[r.body + 1]; ++k) joints.push_back(W->h_bj[k]);
+    }
+    std::sort(joints.begin(), joints.end());
+    joints.erase(std::unique(joints.begin(), joints.end()), joints.end());
+    // one staging buffer (records, then joint ids), reused once its last upload is done
+    const size_t rec_b = sizeof(DeltaRec) * recs.size(), bytes = rec_b + sizeof(int) * joints.size();
+    if (W->ev_delta) PSX_CUDA(cudaEventSynchronize(W->ev_delta));
+    else PSX_CUDA(cudaEventCreateWithFlags(&W->ev_delta, cudaEventDisableTiming));
+    if (W->dpin_bytes < bytes) {
+        if (W->dpin) cudaFreeHost(W->dpin);
+        W->dpin = nullptr;
+        W->dpin_bytes = 0;
+        PSX_CUDA(cudaMallocHost(&W->dpin, bytes));
+        W->dpin_bytes = bytes;
+    }
+    if (W->ddev_bytes < bytes) {
+        PSX_CUDA(cudaStreamSynchronize(W->stream));
+        if (W->ddev) cudaFree(W->ddev);
+        W->ddev = nullptr;
+        W->ddev_bytes = 0;
+        PSX_CUDA(cudaMalloc(&W->ddev, bytes));
+        W->ddev_bytes = bytes;
+    }
+    char* hp = reinterpret_cast<char*>(W->dpin);
+    std::memcpy(hp, recs.data(), rec_b);
+    if (!joints.empty()) std::memcpy(hp + rec_b, joints.data(), sizeof(int) * joints.size());
+    PSX_CUDA(cudaMemcpyAsync(W->ddev, hp, bytes, cudaMemcpyHostToDevice, W->stream));
+    PSX_CUDA(cudaEventRecord(W->ev_delta, W->stream));
+    const DeltaRec* dd = reinterpret_cast<const DeltaRec*>(W->ddev);
+    const int* dj = reinterpret_cast<const int*>(W->ddev + rec_b);
+    W->launches += launch_apply_deltas(W->w, dd, (int)recs.size(), dj, (int)joints.size(), W->stream);
+    // triangle-mesh colliders of posed bodies
+    for (const DeltaRec& r : recs) {
+        if (!(r.mask & DELTA_POSE)) continue;
+        for (int c = W->h_body_col[r.body]; c < W->h_body_col[r.body + 1]; ++c)
+            if (W->h_col_trimesh[c] >= 0) W->launches += launch_trimesh_bounds(W->w, c, c + 1, true, W->stream);
+    }
     return PSX_OK;
 }
 

@@ -15,6 +15,8 @@ oracle/ref/build_ref.py) on seeded scenes from physecs_gb300.scenes:
                        with trigger colliders
   trimesh_bvh.npz      physecs::TriangleMesh's triangles and BVH nodes for seeded meshes,
                        degenerate ones included
+  deltas.npz           body states of scenes stepped with seeded registry deltas (patched
+                       poses, written velocities, setIsKinematic) between frames
 
 Run in a checkout with the reference present:  python tests/golden/make_golden.py
 """
@@ -247,6 +249,37 @@ def trimesh_fixture():
     return out
 
 
+def delta_scenes():
+    """name -> (scene, frames stepped, frames whose state is recorded)."""
+    sys.path.insert(0, os.path.dirname(HERE))
+    from scene_variants import flagged_scene
+    return {
+        "flagged": (flagged_scene(), 40, [10, 20, 40]),
+        "chains": (scenes.joint_chains(n_chains=4, links=6), 40, [10, 20, 40]),
+    }
+
+
+def delta_fixture():
+    from oracle.ref.ref_api import RefScene
+    from physecs_gb300.api import pack_deltas
+    sys.path.insert(0, os.path.dirname(HERE))
+    from scene_variants import delta_schedule
+    out = {}
+    for name, (s, frames, rec) in delta_scenes().items():
+        sch = delta_schedule(s, frames)
+        r = RefScene(s)
+        pre = name + "__"
+        out[pre + "scene_sha256"] = np.array(scene_hash(s))
+        for f in range(frames):
+            if f in sch:
+                r.apply_deltas(pack_deltas(sch[f]))
+            r.step()
+            if f + 1 in rec:
+                for k, v in r.state().items():
+                    out[pre + "f%d_%s" % (f + 1, k)] = v
+    return out
+
+
 def trigger_scenes():
     """name -> (scene, frames stepped)."""
     sys.path.insert(0, os.path.dirname(HERE))
@@ -310,6 +343,8 @@ def main():
     print("triggers ok")
     np.savez_compressed(os.path.join(HERE, "trimesh_bvh.npz"), **trimesh_fixture())
     print("trimesh_bvh ok")
+    np.savez_compressed(os.path.join(HERE, "deltas.npz"), **delta_fixture())
+    print("deltas ok")
 
 
 if __name__ == "__main__":
