@@ -231,6 +231,26 @@ PSX_API psx_status psx_world_tune(psx_world* w, int32_t frames, psx_launch_confi
 /* The launch shapes in effect (after defaults, tuning or opts.launch). */
 PSX_API psx_status psx_world_launch_config(psx_world* w, psx_launch_config* out);
 
+/* ---- filters of the narrowphase */
+#define PSX_CONTACT_COLLISION 0
+#define PSX_CONTACT_TRIGGER 1
+/* ContactType (*)(bool isTrigger0, int data0, bool isTrigger1, int data1) of
+ * Scene::setContactFilter (include/Physecs/Physecs.h:42-43, 224): PSX_CONTACT_TRIGGER makes
+ * a pair a trigger pair (an overlap test and trigger events, no contact),
+ * PSX_CONTACT_COLLISION a colliding one.  Collider 0 is the pair's lower entity. */
+typedef int32_t (*psx_contact_filter)(int32_t is_trigger0, int32_t data0, int32_t is_trigger1, int32_t data1);
+/* Scene::setContactFilter (src/Physecs.cpp:795-797) for every scene of the world; NULL
+ * restores the default filter (a trigger collider makes a trigger pair,
+ * src/Physecs.cpp:20-23).  The filter is called on the host once per pair of
+ * (isTrigger, data) classes of the world's colliders (at most 1024 classes) and read on
+ * the device as a table.  Waits for queued frames. */
+PSX_API psx_status psx_world_set_contact_filter(psx_world* w, psx_contact_filter filter);
+/* Scene::setCanCollide(entity0, entity1, canCollide) (src/Physecs.cpp:788-793): the pair
+ * of bodies joins or leaves the set of pairs that never collide (jointed bodies start
+ * in it).  Waits for queued frames. */
+PSX_API psx_status psx_world_set_can_collide(psx_world* w, int32_t scene, int32_t body0, int32_t body1,
+                                             int32_t can_collide);
+
 /* ---- registry deltas: the changes a Physecs user makes to the registry between frames.
  * A batch applies in array order, each record's fields in the order pose, velocity,
  * kinematic:

@@ -236,6 +236,12 @@ int orc_character_move(void* h, int b, float height, float radius, float max_ste
                                                  v3(translation[0], translation[1], translation[2]));
 }
 
+void orc_scene_set_contact_filter(void* h, int32_t (*f)(int32_t, int32_t, int32_t, int32_t)) {
+    static_cast<World*>(h)->contactFilter = f;
+}
+
+void orc_scene_set_can_collide(void* h, int b0, int b1, int can) { static_cast<World*>(h)->setCanCollide(b0, b1, can != 0); }
+
 // A batch of registry deltas in array order (psx_body_delta; the scene field is unused)
 void orc_scene_apply_deltas(void* h, int n, const psx_body_delta* d) {
     World* w = static_cast<World*>(h);

@@ -146,6 +146,13 @@ void World::setVelocity(int b, V3 v, V3 w) {
     bodies[b].ang = w;
 }
 
+void World::setCanCollide(int b0, int b1, bool canCollide) {
+    uint32_t e0 = bodies[b0].entity, e1 = bodies[b1].entity;
+    std::pair<uint32_t, uint32_t> key = e0 < e1 ? std::make_pair(e0, e1) : std::make_pair(e1, e0);
+    if (canCollide) nonColliding.erase(key);
+    else nonColliding[key] = 1;
+}
+
 // Scene::setIsKinematic (Physecs.cpp:753-770)
 void World::setIsKinematic(int b, bool kinematic) {
     Body& B = bodies[b];
@@ -198,9 +205,12 @@ void World::narrowphase() {
         Q4 or0 = qmul(B0.q, C0.q);
         V3 pos1 = B1.pos + qrot(B1.q, C1.pos);
         Q4 or1 = qmul(B1.q, C1.q);
-        // the default contact filter makes a pair with a trigger a TRIGGER pair: an overlap
-        // test, no contact, ahead of the jointed-pair filter (Physecs.cpp:20-23, 200-207)
-        if (C0.trigger || C1.trigger) {
+        // the contact filter (the default one makes a pair with a trigger a TRIGGER pair): a
+        // TRIGGER pair gets an overlap test, no contact, ahead of the jointed-pair filter
+        // (Physecs.cpp:20-23, 200-207)
+        const bool triggerPair = contactFilter ? contactFilter(C0.trigger, C0.data, C1.trigger, C1.data) == 1
+                                               : (C0.trigger || C1.trigger);
+        if (triggerPair) {
             if (overlapColliders(pos0, or0, c0, pos1, or1, c1)) triggerCacheTemp.insert({bA, cA, bB, cB});
             continue;
         }

@@ -101,6 +101,8 @@ struct World {
     std::vector<std::vector<int>> colors{9};   // joints per colour (src/Physecs.cpp:690-710)
     std::vector<unsigned char> colorBits;      // per body
     std::map<std::pair<uint32_t, uint32_t>, int> nonColliding;
+    // Scene::setContactFilter's function (Physecs.cpp:795-797); null: the default filter
+    int32_t (*contactFilter)(int32_t, int32_t, int32_t, int32_t) = nullptr;
     std::vector<int> dynBodies;                // dyn index -> body
     int substeps = 8, iterations = 2;
     float g = 9.81f;
@@ -146,6 +148,8 @@ struct World {
     void patchPose(int b, V3 p, Q4 q);
     void setVelocity(int b, V3 v, V3 w);
     void setIsKinematic(int b, bool kinematic);
+    // Scene::setCanCollide (Physecs.cpp:788-793) for bodies b0 and b1
+    void setCanCollide(int b0, int b1, bool canCollide);
     // CharacterController::move for body b (CharacterController.cpp:5-45); returns the
     // CharacterCollisionFlags value
     int moveCharacter(int b, float height, float radius, float maxStepHeight, float slopeLimit, int iterations, V3 translation);

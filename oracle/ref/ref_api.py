@@ -42,6 +42,8 @@ def lib():
         _lib.ref_scene_trigger_events.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
         _lib.ref_trimesh_build.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
         _lib.ref_scene_apply_deltas.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        _lib.ref_scene_set_contact_filter.argtypes = [C.c_void_p, C.c_void_p]
+        _lib.ref_scene_set_can_collide.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
         _lib.ref_character_move.argtypes = [C.c_void_p, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int,
                                             C.c_void_p, C.c_float]
     return _lib
@@ -144,6 +146,18 @@ class RefScene:
         f = np.zeros((cap, 4), np.float32)
         m = lib().ref_scene_overlap_mtd(self.h, _p(pose), int(type_), _p(prm), int(mesh), _p(ids), _p(f), cap)
         return [(int(ids[k, 0]), int(ids[k, 1]), f[k, :3].copy(), f[k, 3]) for k in range(min(m, cap))]
+
+    # ContactType (*)(bool, int, bool, int)
+    FILTER = C.CFUNCTYPE(C.c_int, C.c_bool, C.c_int, C.c_bool, C.c_int)
+
+    def set_contact_filter(self, fn):
+        """Scene::setContactFilter with fn(is_trigger0, data0, is_trigger1, data1) -> 0 / 1, or
+        None for the default filter."""
+        self._filter = None if fn is None else self.FILTER(lambda a, b, c, d: int(fn(bool(a), b, bool(c), d)))
+        lib().ref_scene_set_contact_filter(self.h, C.cast(self._filter, C.c_void_p) if self._filter else None)
+
+    def set_can_collide(self, body0, body1, can_collide):
+        lib().ref_scene_set_can_collide(self.h, int(body0), int(body1), int(bool(can_collide)))
 
     def move_character(self, body, height, radius, translation, max_step_height=0.3, slope_limit=0.70710677,
                        iterations=2, dt=1.0 / 60.0):

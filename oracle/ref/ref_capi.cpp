@@ -213,6 +213,17 @@ int ref_character_move(void* h, int b, float height, float radius, float max_ste
     return cc.move(v3(translation), dt).value;
 }
 
+// Scene::setContactFilter with the caller's function (null: the default filter)
+void ref_scene_set_contact_filter(void* h, physecs::ContactType (*f)(bool, int, bool, int)) {
+    static_cast<RefWorld*>(h)->scene->setContactFilter(f ? f : physecs::defaultContactFilter);
+}
+
+// Scene::setCanCollide for the entities of bodies b0 and b1
+void ref_scene_set_can_collide(void* h, int b0, int b1, int can) {
+    auto* w = static_cast<RefWorld*>(h);
+    w->scene->setCanCollide(w->entities[b0], w->entities[b1], can != 0);
+}
+
 // Registry deltas as a Physecs user makes them, in array order: a pose written to the
 // TransformComponent and patched, velocities written to the RigidBodyDynamicComponent,
 // Scene::setIsKinematic (psx_body_delta; the scene field is unused)

@@ -29,7 +29,8 @@ EXPORTS = ["psx_world_create", "psx_world_destroy", "psx_world_step", "psx_world
            "psx_server_tick_stages", "psx_server_device_bytes",
            "psx_world_tune", "psx_world_launch_config", "psx_world_raycast", "psx_world_overlap",
            "psx_world_overlap_mtd", "psx_world_trigger_events", "psx_trimesh_build", "psx_world_update_trimesh",
-           "psx_world_apply_deltas", "psx_world_move_characters"]
+           "psx_world_apply_deltas", "psx_world_move_characters", "psx_world_set_contact_filter",
+           "psx_world_set_can_collide"]
 
 _lib = None
 
@@ -103,6 +104,8 @@ def load():
     lib.psx_trimesh_build.argtypes = [C.c_int32, vp, C.c_int32, vp, C.c_int32, vp, vp, vp]
     lib.psx_world_update_trimesh.argtypes = [vp, C.c_int32, C.c_int32, vp]
     lib.psx_world_apply_deltas.argtypes = [vp, C.c_int32, vp]
+    lib.psx_world_set_contact_filter.argtypes = [vp, vp]
+    lib.psx_world_set_can_collide.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
     lib.psx_world_move_characters.argtypes = [vp, C.c_int32, vp, C.c_float, vp]
     lib.psx_server_stats.argtypes = [vp, vp]
     _lib = lib
@@ -303,6 +306,18 @@ class World:
         deltas is pack_deltas' (n, 17) array or a list of its dicts."""
         d = pack_deltas(deltas) if isinstance(deltas, (list, tuple)) else np.ascontiguousarray(deltas, np.float32)
         _check(load().psx_world_apply_deltas(self.h, len(d), _p(d)))
+
+    CONTACT_FILTER = C.CFUNCTYPE(C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32)
+
+    def set_contact_filter(self, fn):
+        """psx_world_set_contact_filter (Scene::setContactFilter): fn(is_trigger0, data0,
+        is_trigger1, data1) -> 0 COLLISION / 1 TRIGGER, or None for the default filter."""
+        self._filter = None if fn is None else self.CONTACT_FILTER(lambda a, b, c, d: int(fn(bool(a), b, bool(c), d)))
+        _check(load().psx_world_set_contact_filter(self.h, C.cast(self._filter, C.c_void_p) if self._filter else None))
+
+    def set_can_collide(self, body0, body1, can_collide, scene=0):
+        """psx_world_set_can_collide (Scene::setCanCollide) for two bodies of one scene."""
+        _check(load().psx_world_set_can_collide(self.h, scene, body0, body1, int(bool(can_collide))))
 
     def move_characters(self, chars, translations, dt=1.0 / 60.0):
         """psx_world_move_characters.  chars: dicts {scene, body, height, radius,

@@ -40,7 +40,10 @@ __global__ void k_classify(World w, FrameBuf f) {
         if (p < np) {
             int2 pr = f.pairs[p];
             int4 a = w.col_info[pr.x], b = w.col_info[pr.y];
-            bool trigger = (a.w & COL_TRIGGER) || (b.w & COL_TRIGGER);
+            // the contact filter (src/Physecs.cpp:200): the default one, or the user's as a
+            // table over the colliders' (isTrigger, data) classes
+            bool trigger = w.filter_table ? w.filter_table[w.col_class[pr.x] * w.n_classes + w.col_class[pr.y]] != 0
+                                          : ((a.w & COL_TRIGGER) || (b.w & COL_TRIGGER));
             bool jointed = false;
             if (n_nc) {
                 // sorted (body_lo, body_hi) list of jointed body pairs

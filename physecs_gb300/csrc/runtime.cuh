@@ -45,6 +45,9 @@ struct psx_world {
     std::vector<int> h_scene_trimesh;      // per scene (+1): first world triangle mesh
     std::vector<psx::TriMeshDev> h_trimesh;
     std::vector<int> h_col_trimesh;        // per collider: world triangle mesh, or -1
+    std::vector<int> h_col_data;           // per collider: Collider::data
+    std::vector<char> h_col_trig;          // per collider: Collider::isTrigger
+    std::vector<int2> h_nc;                // non-colliding body pairs (lo, hi), sorted
     // registry deltas
     std::vector<int> h_body_col;           // [n_bodies + 1] each body's first collider
     std::vector<int> h_body_flags;         // PSX_BODY_* as the device holds them
@@ -156,6 +159,8 @@ psx_status partition_big(psx_world* W, int mode);
 // splits the block scenes into solver block sizes (64 / 128 / 256 threads), the
 // smallest size in use being threads_min
 psx_status partition_tiers(psx_world* W, int threads_min);
+// trigger sets and the event log (a world with trigger pairs)
+psx_status alloc_triggers(psx_world* W);
 // reads the device error word; maps its bits to a status
 psx_status check_err(psx_world* W);
 // pinned host staging of at least n4 float4

@@ -197,6 +197,9 @@ struct World {
     int* jstep_start;      // start of each step in jsched
     int* jstep_simd;       // 1 for colours 0..7 (4-lane arithmetic), 0 for overflow
     // jointed body pairs, sorted (lo, hi): such pairs never collide (src/Physecs.cpp:209, 694)
+    int* col_class;               // with a user contact filter: each collider's (isTrigger, data) class
+    unsigned char* filter_table;  // [n_classes^2] 1: TRIGGER for (class of collider 0, class of collider 1)
+    int n_classes;
     int2* nc_pairs;
     int n_nc;
     // serving: per-scene flags, null for a plain world (every scene runs, cache on)

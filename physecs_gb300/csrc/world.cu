@@ -165,6 +165,8 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
                 if (sim) flags |= COL_DYNAMIC;
                 col_info.push_back(make_int4(bbase + b, t, mesh, flags));
                 W->h_col_trimesh.push_back(t == PSX_TRIANGLE_MESH ? mesh : -1);
+                W->h_col_data.push_back(d.col_data ? d.col_data[c] : 0);
+                W->h_col_trig.push_back(d.col_is_trigger && d.col_is_trigger[c] ? 1 : 0);
                 col_pos.push_back(f4(d.col_pos[3 * c], d.col_pos[3 * c + 1], d.col_pos[3 * c + 2]));
                 col_quat.push_back(f4(d.col_quat[4 * c], d.col_quat[4 * c + 1], d.col_quat[4 * c + 2], d.col_quat[4 * c + 3]));
                 col_params.push_back(f4(d.col_params[4 * c], d.col_params[4 * c + 1], d.col_params[4 * c + 2], d.col_params[4 * c + 3]));
@@ -353,6 +355,7 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
     w.jstep_simd = nullptr;
     PSX_TRY(W->upload(w.nc_pairs, nc));
     w.n_nc = (int)nc.size();
+    W->h_nc = nc;
     PSX_TRY(W->alloc(w.err, 1));
     PSX_CUDA(cudaMemset(w.err, 0, sizeof(int)));
 
@@ -426,22 +429,7 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
     // trigger sets and the event log, for a world with trigger colliders only
     bool any_trigger = false;
     for (const int4& ci : col_info) any_trigger |= (ci.w & COL_TRIGGER) && (ci.w & COL_ENABLE);
-    if (any_trigger) {
-        f.trig_cap = f.pair_cap;
-        f.trig_table_cap = 1 << ilog2ceil(2 * f.trig_cap);
-        f.evt_cap = std::max(4096, 2 * f.trig_cap);
-        for (int k = 0; k < 2; ++k) {
-            PSX_TRY(W->alloc(f.trig_table[k], f.trig_table_cap));
-            PSX_TRY(W->alloc(f.trig_keys[k], f.trig_cap));
-            PSX_TRY(W->alloc(f.trig_slot[k], f.trig_cap));
-            PSX_CUDA(cudaMemset(f.trig_table[k], 0xff, sizeof(unsigned long long) * (size_t)f.trig_table_cap));
-        }
-        PSX_TRY(W->alloc(f.trig_state, 4));
-        PSX_TRY(W->alloc(f.trig_evt, f.evt_cap));
-        PSX_TRY(W->alloc(f.n_evt, 1));
-        PSX_CUDA(cudaMemset(f.trig_state, 0, 4 * sizeof(int)));
-        PSX_CUDA(cudaMemset(f.n_evt, 0, sizeof(int)));
-    }
+    if (any_trigger) PSX_TRY(alloc_triggers(W));
     // shared memory per solver block: the most a block may have when there are at most as
     // many block scenes as SMs, else a size that keeps two blocks resident per SM (the
     // register budget of the 256-thread solver allows two)
@@ -546,6 +534,28 @@ psx_status psx::rt::run_frame(psx_world* W) {
 }
 
 // Validate and apply launch shapes (0 keeps the current value).
+psx_status psx::rt::alloc_triggers(psx_world* W) {
+    FrameBuf& f = W->f;
+    if (f.trig_cap) return PSX_OK;
+    const int cap = f.pair_cap, tcap = 1 << ilog2ceil(2 * cap), ecap = std::max(4096, 2 * cap);
+    for (int k = 0; k < 2; ++k) {
+        PSX_TRY(W->alloc(f.trig_table[k], tcap));
+        PSX_TRY(W->alloc(f.trig_keys[k], cap));
+        PSX_TRY(W->alloc(f.trig_slot[k], cap));
+        PSX_CUDA(cudaMemset(f.trig_table[k], 0xff, sizeof(unsigned long long) * (size_t)tcap));
+    }
+    PSX_TRY(W->alloc(f.trig_state, 4));
+    PSX_TRY(W->alloc(f.trig_evt, ecap));
+    PSX_TRY(W->alloc(f.n_evt, 1));
+    const int state[4] = {0, 0, 0, (int)W->frames_run};   // events count frames from the world's creation
+    PSX_CUDA(cudaMemcpy(f.trig_state, state, sizeof(state), cudaMemcpyHostToDevice));
+    PSX_CUDA(cudaMemset(f.n_evt, 0, sizeof(int)));
+    f.trig_table_cap = tcap;
+    f.evt_cap = ecap;
+    f.trig_cap = cap;   // last: the frame launches the trigger kernels from here on
+    return PSX_OK;
+}
+
 psx_status psx::rt::apply_launch(psx_world* W, const psx_launch_config& c) {
     NarrowShape n = W->narrow;
     if (c.convex_warps) n.convex_warps = c.convex_warps;
@@ -1061,6 +1071,69 @@ PSX_API psx_status psx_world_apply_deltas(psx_world* W, int32_t n, const psx_bod
         for (int c = W->h_body_col[r.body]; c < W->h_body_col[r.body + 1]; ++c)
             if (W->h_col_trimesh[c] >= 0) W->launches += launch_trimesh_bounds(W->w, c, c + 1, true, W->stream);
     }
+    return PSX_OK;
+}
+
+PSX_API psx_status psx_world_set_contact_filter(psx_world* W, psx_contact_filter fn) {
+    if (!W) return fail(PSX_ERR_INVALID_ARG, "psx_world_set_contact_filter: null world");
+    PSX_CUDA(cudaSetDevice(W->device));
+    PSX_CUDA(cudaStreamSynchronize(W->stream));
+    World& w = W->w;
+    if (!fn) {
+        w.filter_table = nullptr;
+    } else {
+        // the filter sees only (isTrigger, data) of the two colliders: one call per pair of classes
+        std::map<std::pair<int, int>, int> cls;
+        std::vector<int> col_class(w.n_colliders);
+        std::vector<std::pair<int, int>> key_of;
+        for (int c = 0; c < w.n_colliders; ++c) {
+            const std::pair<int, int> k{W->h_col_trig[c], W->h_col_data[c]};
+            auto it = cls.find(k);
+            if (it == cls.end()) {
+                it = cls.emplace(k, (int)key_of.size()).first;
+                key_of.push_back(k);
+            }
+            col_class[c] = it->second;
+        }
+        const int K = (int)key_of.size();
+        if (K > 1024) return fail(PSX_ERR_CAPACITY, "psx_world_set_contact_filter: more than 1024 (isTrigger, data) classes");
+        std::vector<unsigned char> table((size_t)K * K);
+        bool any_trigger = false;
+        for (int i = 0; i < K; ++i)
+            for (int j = 0; j < K; ++j) {
+                const int r = fn(key_of[i].first, key_of[i].second, key_of[j].first, key_of[j].second);
+                if (r != PSX_CONTACT_COLLISION && r != PSX_CONTACT_TRIGGER)
+                    return fail(PSX_ERR_INVALID_ARG, "psx_world_set_contact_filter: the filter returned " + std::to_string(r));
+                table[(size_t)i * K + j] = r == PSX_CONTACT_TRIGGER;
+                any_trigger |= r == PSX_CONTACT_TRIGGER;
+            }
+        if (any_trigger) PSX_TRY(alloc_triggers(W));
+        PSX_TRY(W->upload(w.col_class, col_class));
+        PSX_TRY(W->upload(w.filter_table, table));
+        w.n_classes = K;
+    }
+    if (W->graph) { cudaGraphExecDestroy(W->graph); W->graph = nullptr; }   // the frame reads w by value
+    return PSX_OK;
+}
+
+PSX_API psx_status psx_world_set_can_collide(psx_world* W, int32_t scene, int32_t body0, int32_t body1, int32_t can_collide) {
+    if (!W || scene < 0 || scene >= W->n_scenes) return fail(PSX_ERR_INVALID_ARG, "psx_world_set_can_collide: scene");
+    const int nb = W->h_scene_body[scene + 1] - W->h_scene_body[scene];
+    if (body0 < 0 || body0 >= nb || body1 < 0 || body1 >= nb) return fail(PSX_ERR_INVALID_ARG, "psx_world_set_can_collide: body");
+    PSX_CUDA(cudaSetDevice(W->device));
+    const int b0 = W->h_scene_body[scene] + body0, b1 = W->h_scene_body[scene] + body1;
+    const int2 key = make_int2(std::min(b0, b1), std::max(b0, b1));
+    auto less = [](int2 a, int2 b) { return a.x < b.x || (a.x == b.x && a.y < b.y); };
+    auto it = std::lower_bound(W->h_nc.begin(), W->h_nc.end(), key, less);
+    const bool present = it != W->h_nc.end() && it->x == key.x && it->y == key.y;
+    if (can_collide && present) W->h_nc.erase(it);
+    else if (!can_collide && !present) W->h_nc.insert(it, key);
+    else return PSX_OK;
+    PSX_CUDA(cudaStreamSynchronize(W->stream));
+    World& w = W->w;
+    PSX_TRY(W->upload(w.nc_pairs, W->h_nc));
+    w.n_nc = (int)W->h_nc.size();
+    if (W->graph) { cudaGraphExecDestroy(W->graph); W->graph = nullptr; }
     return PSX_OK;
 }
 

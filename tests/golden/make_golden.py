@@ -17,6 +17,8 @@ oracle/ref/build_ref.py) on seeded scenes from physecs_gb300.scenes:
                        degenerate ones included
   deltas.npz           body states of scenes stepped with seeded registry deltas (patched
                        poses, written velocities, setIsKinematic) between frames
+  filters.npz          body states and trigger events of a scene stepped under a user
+                       contact filter, with setCanCollide toggled between frames
 
 Run in a checkout with the reference present:  python tests/golden/make_golden.py
 """
@@ -280,6 +282,38 @@ def delta_fixture():
     return out
 
 
+def filter_case():
+    """(scene, filter, can-collide schedule {frame: (body0, body1, can)}, frames, recorded
+    frames): colliders get data values 0..3; pairs with a trigger, or whose data share
+    bit 1, are trigger pairs."""
+    sys.path.insert(0, os.path.dirname(HERE))
+    from scene_variants import flagged_scene
+    s = flagged_scene(seed=8, n=90)
+    a = s.arrays
+    a["col_data"][:] = np.random.default_rng(4).integers(0, 4, len(a["col_data"]))
+
+    def filt(t0, d0, t1, d1):
+        return 1 if (t0 or t1 or (d0 & d1 & 2)) else 0
+    return s, filt, {10: (5, 6, False), 30: (5, 6, True), 35: (7, 12, False)}, 50, [20, 50]
+
+
+def filter_fixture():
+    from oracle.ref.ref_api import RefScene
+    s, filt, cc, frames, rec = filter_case()
+    r = RefScene(s)
+    r.set_contact_filter(filt)
+    out = {"scene_sha256": np.array(scene_hash(s))}
+    for f in range(frames):
+        if f in cc:
+            r.set_can_collide(*cc[f])
+        r.step()
+        if f + 1 in rec:
+            for k, v in r.state().items():
+                out["f%d_%s" % (f + 1, k)] = v
+    out["events"] = events_sorted(r.trigger_events())
+    return out
+
+
 def trigger_scenes():
     """name -> (scene, frames stepped)."""
     sys.path.insert(0, os.path.dirname(HERE))
@@ -345,6 +379,8 @@ def main():
     print("trimesh_bvh ok")
     np.savez_compressed(os.path.join(HERE, "deltas.npz"), **delta_fixture())
     print("deltas ok")
+    np.savez_compressed(os.path.join(HERE, "filters.npz"), **filter_fixture())
+    print("filters ok")
 
 
 if __name__ == "__main__":
