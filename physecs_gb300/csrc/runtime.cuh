@@ -48,6 +48,8 @@ struct psx_world {
     std::vector<int> h_col_data;           // per collider: Collider::data
     std::vector<char> h_col_trig;          // per collider: Collider::isTrigger
     std::vector<int2> h_nc;                // non-colliding body pairs (lo, hi), sorted
+    size_t nc_cap = 0;                     // device capacity of w.nc_pairs
+    size_t filter_cap = 0;                 // device capacity of w.filter_table (bytes)
     // registry deltas
     std::vector<int> h_body_col;           // [n_bodies + 1] each body's first collider
     std::vector<int> h_body_flags;         // PSX_BODY_* as the device holds them
@@ -110,6 +112,17 @@ struct psx_world {
         allocs.push_back(q);
         device_bytes += n * sizeof(T);
         p = (T*)q;
+        return PSX_OK;
+    }
+    // copies v into p, allocating a larger buffer only when v outgrows *cap
+    template <class T>
+    psx_status upload_reuse(T*& p, size_t& cap, const std::vector<T>& v) {
+        if (v.size() > cap || !p) {
+            psx_status s = alloc(p, std::max<size_t>(v.size(), 2 * cap));
+            if (s != PSX_OK) return s;
+            cap = std::max<size_t>(v.size(), 2 * cap);
+        }
+        if (!v.empty()) PSX_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
         return PSX_OK;
     }
     template <class T>

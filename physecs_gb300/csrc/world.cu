@@ -353,7 +353,7 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
     w.scene_jsched = nullptr;
     w.jsched_step = nullptr;
     w.jstep_simd = nullptr;
-    PSX_TRY(W->upload(w.nc_pairs, nc));
+    PSX_TRY(W->upload_reuse(w.nc_pairs, W->nc_cap, nc));
     w.n_nc = (int)nc.size();
     W->h_nc = nc;
     PSX_TRY(W->alloc(w.err, 1));
@@ -1108,8 +1108,9 @@ PSX_API psx_status psx_world_set_contact_filter(psx_world* W, psx_contact_filter
                 any_trigger |= r == PSX_CONTACT_TRIGGER;
             }
         if (any_trigger) PSX_TRY(alloc_triggers(W));
-        PSX_TRY(W->upload(w.col_class, col_class));
-        PSX_TRY(W->upload(w.filter_table, table));
+        if (!w.col_class) PSX_TRY(W->alloc(w.col_class, std::max(1, w.n_colliders)));
+        if (w.n_colliders) PSX_CUDA(cudaMemcpy(w.col_class, col_class.data(), sizeof(int) * w.n_colliders, cudaMemcpyHostToDevice));
+        PSX_TRY(W->upload_reuse(w.filter_table, W->filter_cap, table));
         w.n_classes = K;
     }
     if (W->graph) { cudaGraphExecDestroy(W->graph); W->graph = nullptr; }   // the frame reads w by value
@@ -1131,7 +1132,7 @@ PSX_API psx_status psx_world_set_can_collide(psx_world* W, int32_t scene, int32_
     else return PSX_OK;
     PSX_CUDA(cudaStreamSynchronize(W->stream));
     World& w = W->w;
-    PSX_TRY(W->upload(w.nc_pairs, W->h_nc));
+    PSX_TRY(W->upload_reuse(w.nc_pairs, W->nc_cap, W->h_nc));
     w.n_nc = (int)W->h_nc.size();
     if (W->graph) { cudaGraphExecDestroy(W->graph); W->graph = nullptr; }
     return PSX_OK;
