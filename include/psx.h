@@ -280,6 +280,11 @@ typedef struct psx_body_delta {
  * KINEMATIC is refused for a body with a joint in the overflow colour (a colour past
  * the eighth, whose solve steps assume the dynamic bodies of creation time). */
 PSX_API psx_status psx_world_apply_deltas(psx_world* w, int32_t n, const psx_body_delta* deltas);
+/* Page-locks (and releases) a caller's host buffer, e.g. the arrays handed to
+ * psx_world_read_bodies / psx_world_write_bodies / psx_world_simulate_host, so that their
+ * copies run at the host link's speed instead of through the driver's staging. */
+PSX_API psx_status psx_pin_host(void* p, size_t bytes);
+PSX_API psx_status psx_unpin_host(void* p);
 
 /* ---- triangle meshes: the BVH of physecs::TriangleMesh, built on the device */
 typedef struct psx_trimesh_triangle {  /* Triangle (include/Physecs/TriangleMesh.h:9-14) */

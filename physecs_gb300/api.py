@@ -30,7 +30,7 @@ EXPORTS = ["psx_world_create", "psx_world_destroy", "psx_world_step", "psx_world
            "psx_world_tune", "psx_world_launch_config", "psx_world_raycast", "psx_world_overlap",
            "psx_world_overlap_mtd", "psx_world_trigger_events", "psx_trimesh_build", "psx_world_update_trimesh",
            "psx_world_apply_deltas", "psx_world_move_characters", "psx_world_set_contact_filter",
-           "psx_world_set_can_collide"]
+           "psx_world_set_can_collide", "psx_pin_host", "psx_unpin_host"]
 
 _lib = None
 
@@ -105,6 +105,8 @@ def load():
     lib.psx_world_update_trimesh.argtypes = [vp, C.c_int32, C.c_int32, vp]
     lib.psx_world_apply_deltas.argtypes = [vp, C.c_int32, vp]
     lib.psx_world_set_contact_filter.argtypes = [vp, vp]
+    lib.psx_pin_host.argtypes = [vp, C.c_size_t]
+    lib.psx_unpin_host.argtypes = [vp]
     lib.psx_world_set_can_collide.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
     lib.psx_world_move_characters.argtypes = [vp, C.c_int32, vp, C.c_float, vp]
     lib.psx_server_stats.argtypes = [vp, vp]
@@ -553,3 +555,16 @@ def pack_deltas(deltas):
             iv[i, 3] = int(bool(d["kinematic"]))
         iv[i, 2] = mask
     return out
+
+
+def pin_host(*arrays):
+    """psx_pin_host for numpy arrays (e.g. the dict of read_bodies), so that the body
+    copies of read_bodies / write_bodies / simulate_host run at the host link's speed.
+    Release them with unpin_host before they are freed."""
+    for a in arrays:
+        _check(load().psx_pin_host(a.ctypes.data_as(C.c_void_p), a.nbytes))
+
+
+def unpin_host(*arrays):
+    for a in arrays:
+        _check(load().psx_unpin_host(a.ctypes.data_as(C.c_void_p)))

@@ -172,6 +172,42 @@ __global__ void k_joint_fix(World w, const int* js, int n) {
     }
 }
 
+// Body state between the caller's layout (pos, vel, ang_vel: 3 floats a body; every body,
+// static ones reading as zero velocity) and the world's float4 arrays (velocities per
+// dynamic body).  A null array is skipped.
+__global__ void k_unpack_bodies(World w, const float* pos, const float* vel, const float* ang) {
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < w.n_bodies; b += gridDim.x * blockDim.x) {
+        if (pos) w.pos[b] = make_float4(pos[3 * b], pos[3 * b + 1], pos[3 * b + 2], 0.f);
+        const int d = w.info[b].z;
+        if (d < 0) continue;
+        if (vel) w.vel[d] = make_float4(vel[3 * b], vel[3 * b + 1], vel[3 * b + 2], 0.f);
+        if (ang) w.ang[d] = make_float4(ang[3 * b], ang[3 * b + 1], ang[3 * b + 2], 0.f);
+    }
+}
+
+__global__ void k_pack_bodies(World w, float* pos, float* vel, float* ang) {
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < w.n_bodies; b += gridDim.x * blockDim.x) {
+        if (pos) { const float4 p = w.pos[b]; pos[3 * b] = p.x; pos[3 * b + 1] = p.y; pos[3 * b + 2] = p.z; }
+        const int d = w.info[b].z;
+        const float4 v = d >= 0 ? w.vel[d] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 a = d >= 0 ? w.ang[d] : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (vel) { vel[3 * b] = v.x; vel[3 * b + 1] = v.y; vel[3 * b + 2] = v.z; }
+        if (ang) { ang[3 * b] = a.x; ang[3 * b + 1] = a.y; ang[3 * b + 2] = a.z; }
+    }
+}
+
+int launch_unpack_bodies(const World& w, const float* pos, const float* vel, const float* ang, cudaStream_t s) {
+    if (!w.n_bodies || !(pos || vel || ang)) return 0;
+    k_unpack_bodies<<<std::min(152 * 8, (w.n_bodies + 255) / 256), 256, 0, s>>>(w, pos, vel, ang);
+    return 1;
+}
+
+int launch_pack_bodies(const World& w, float* pos, float* vel, float* ang, cudaStream_t s) {
+    if (!w.n_bodies || !(pos || vel || ang)) return 0;
+    k_pack_bodies<<<std::min(152 * 8, (w.n_bodies + 255) / 256), 256, 0, s>>>(w, pos, vel, ang);
+    return 1;
+}
+
 int launch_apply_deltas(const World& w, const DeltaRec* d, int n, const int* joints, int nj, cudaStream_t s) {
     int k = 0;
     if (n > 0) { k_apply_deltas<<<(n + 127) / 128, 128, 0, s>>>(w, d, n); ++k; }

@@ -99,6 +99,9 @@ int launch_trimesh_bounds(const World& w, int c0, int c1, bool margin, cudaStrea
 // a coalesced batch of registry deltas (one record per body), then the joints of the
 // bodies whose kinematic flag changed
 int launch_apply_deltas(const World& w, const DeltaRec* d, int n, const int* joints, int nj, cudaStream_t s);
+// body state between 3-float device staging (every body) and the world's float4 arrays
+int launch_unpack_bodies(const World& w, const float* pos, const float* vel, const float* ang, cudaStream_t s);
+int launch_pack_bodies(const World& w, float* pos, float* vel, float* ang, cudaStream_t s);
 // scene_sort_pmax > 0: every scene has at most that many colliders (a power of two) and
 // is sorted by its own block in shared memory; 0: one radix sort over the whole world
 int launch_broadphase(const World& w, FrameBuf& f, int scene_bits, int scene_sort_pmax, cudaStream_t s);

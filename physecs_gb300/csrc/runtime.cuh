@@ -94,9 +94,8 @@ struct psx_world {
     cudaGraphExec_t graph = nullptr;
     float graph_dt = -1.f;
     bool knobs_dirty = true;
-    // pinned staging for body transfers
-    float4* pin = nullptr;
-    size_t pin_n = 0;
+    float* bstage = nullptr;               // device staging of body state: pos, vel, ang_vel, 3 floats a body each
+    size_t bstage_n = 0;
     int device = 0;
     long long launches = 0;          // kernels queued since creation
     int n_simulated = 0;             // dynamic, non-kinematic bodies
@@ -136,7 +135,7 @@ struct psx_world {
         for (cudaEvent_t e : events) cudaEventDestroy(e);
         if (graph) cudaGraphExecDestroy(graph);
         for (void* p : allocs) cudaFree(p);
-        if (pin) cudaFreeHost(pin);
+        if (bstage) cudaFree(bstage);
         if (qbuf) cudaFree(qbuf);
         if (dpin) cudaFreeHost(dpin);
         if (ddev) cudaFree(ddev);
@@ -177,6 +176,5 @@ psx_status alloc_triggers(psx_world* W);
 // reads the device error word; maps its bits to a status
 psx_status check_err(psx_world* W);
 // pinned host staging of at least n4 float4
-psx_status ensure_pinned(psx_world* W, size_t n4);
 }  // namespace rt
 }  // namespace psx

@@ -667,16 +667,6 @@ psx_status psx::rt::check_err(psx_world* W) {
     return fail(PSX_ERR_CAPACITY, buf);
 }
 
-psx_status psx::rt::ensure_pinned(psx_world* W, size_t n4) {
-    if (W->pin_n >= n4) return PSX_OK;
-    if (W->pin) cudaFreeHost(W->pin);
-    W->pin = nullptr;
-    W->pin_n = 0;
-    PSX_CUDA(cudaMallocHost(&W->pin, n4 * sizeof(float4)));
-    W->pin_n = n4;
-    return PSX_OK;
-}
-
 extern "C" {
 
 PSX_API const char* psx_last_error_string(void) { return g_err.c_str(); }
@@ -912,30 +902,36 @@ PSX_API psx_status psx_world_synchronize(psx_world* W) {
     return check_err(W);
 }
 
+// device staging for the caller's 3-float arrays, grown once
+static psx_status body_stage(psx_world* W, float** out) {
+    const size_t n = 9 * (size_t)std::max(1, W->w.n_bodies);
+    if (W->bstage_n < n) {
+        PSX_CUDA(cudaStreamSynchronize(W->stream));
+        if (W->bstage) cudaFree(W->bstage);
+        W->bstage = nullptr;
+        W->bstage_n = 0;
+        PSX_CUDA(cudaMalloc(&W->bstage, n * sizeof(float)));
+        W->bstage_n = n;
+    }
+    *out = W->bstage;
+    return PSX_OK;
+}
+
+// The caller's arrays are copied as they are (page-locked ones through psx_pin_host at the
+// link's speed) and repacked on the device.
 static psx_status read_bodies(psx_world* W, float* pos, float* quat, float* vel, float* ang, bool sync_after) {
-    const World& w = W->w;
-    size_t nb = w.n_bodies, nd = w.n_dyn;
-    PSX_TRY(ensure_pinned(W, 2 * nb + 2 * nd));
-    float4* hp = W->pin;
-    float4* hq = hp + nb;
-    float4* hv = hq + nb;
-    float4* ha = hv + nd;
-    PSX_CUDA(cudaMemcpyAsync(hp, w.pos, nb * sizeof(float4), cudaMemcpyDeviceToHost, W->stream));
-    PSX_CUDA(cudaMemcpyAsync(hq, w.quat, nb * sizeof(float4), cudaMemcpyDeviceToHost, W->stream));
-    if (nd) {
-        PSX_CUDA(cudaMemcpyAsync(hv, w.vel, nd * sizeof(float4), cudaMemcpyDeviceToHost, W->stream));
-        PSX_CUDA(cudaMemcpyAsync(ha, w.ang, nd * sizeof(float4), cudaMemcpyDeviceToHost, W->stream));
-    }
-    PSX_CUDA(cudaStreamSynchronize(W->stream));
     (void)sync_after;
-    for (size_t b = 0; b < nb; ++b) {
-        if (pos) { pos[3 * b] = hp[b].x; pos[3 * b + 1] = hp[b].y; pos[3 * b + 2] = hp[b].z; }
-        if (quat) { quat[4 * b] = hq[b].x; quat[4 * b + 1] = hq[b].y; quat[4 * b + 2] = hq[b].z; quat[4 * b + 3] = hq[b].w; }
-        int d = W->h_body_dyn[b];
-        float4 v = d >= 0 ? hv[d] : make_float4(0, 0, 0, 0), a = d >= 0 ? ha[d] : make_float4(0, 0, 0, 0);
-        if (vel) { vel[3 * b] = v.x; vel[3 * b + 1] = v.y; vel[3 * b + 2] = v.z; }
-        if (ang) { ang[3 * b] = a.x; ang[3 * b + 1] = a.y; ang[3 * b + 2] = a.z; }
-    }
+    const World& w = W->w;
+    const size_t nb = w.n_bodies;
+    float* st = nullptr;
+    PSX_TRY(body_stage(W, &st));
+    float *sp = st, *sv = st + 3 * nb, *sa = st + 6 * nb;
+    launch_pack_bodies(w, pos ? sp : nullptr, vel ? sv : nullptr, ang ? sa : nullptr, W->stream);
+    if (pos) PSX_CUDA(cudaMemcpyAsync(pos, sp, 3 * nb * sizeof(float), cudaMemcpyDeviceToHost, W->stream));
+    if (quat) PSX_CUDA(cudaMemcpyAsync(quat, w.quat, nb * sizeof(float4), cudaMemcpyDeviceToHost, W->stream));
+    if (vel) PSX_CUDA(cudaMemcpyAsync(vel, sv, 3 * nb * sizeof(float), cudaMemcpyDeviceToHost, W->stream));
+    if (ang) PSX_CUDA(cudaMemcpyAsync(ang, sa, 3 * nb * sizeof(float), cudaMemcpyDeviceToHost, W->stream));
+    PSX_CUDA(cudaStreamSynchronize(W->stream));
     return PSX_OK;
 }
 
@@ -949,27 +945,34 @@ PSX_API psx_status psx_world_write_bodies(psx_world* W, const float* pos, const 
     if (W) cudaSetDevice(W->device);
     if (!W) return fail(PSX_ERR_INVALID_ARG, "null world");
     const World& w = W->w;
-    size_t nb = w.n_bodies, nd = w.n_dyn;
-    PSX_TRY(ensure_pinned(W, 2 * nb + 2 * nd));
-    PSX_CUDA(cudaStreamSynchronize(W->stream));
-    float4* hp = W->pin;
-    float4* hq = hp + nb;
-    float4* hv = hq + nb;
-    float4* ha = hv + nd;
-    for (size_t b = 0; b < nb; ++b) {
-        if (pos) hp[b] = make_float4(pos[3 * b], pos[3 * b + 1], pos[3 * b + 2], 0.f);
-        if (quat) hq[b] = make_float4(quat[4 * b], quat[4 * b + 1], quat[4 * b + 2], quat[4 * b + 3]);
-        int d = W->h_body_dyn[b];
-        if (d >= 0) {
-            if (vel) hv[d] = make_float4(vel[3 * b], vel[3 * b + 1], vel[3 * b + 2], 0.f);
-            if (ang) ha[d] = make_float4(ang[3 * b], ang[3 * b + 1], ang[3 * b + 2], 0.f);
-        }
-    }
-    if (pos) PSX_CUDA(cudaMemcpyAsync(w.pos, hp, nb * sizeof(float4), cudaMemcpyHostToDevice, W->stream));
-    if (quat) PSX_CUDA(cudaMemcpyAsync(w.quat, hq, nb * sizeof(float4), cudaMemcpyHostToDevice, W->stream));
-    if (nd && vel) PSX_CUDA(cudaMemcpyAsync(w.vel, hv, nd * sizeof(float4), cudaMemcpyHostToDevice, W->stream));
-    if (nd && ang) PSX_CUDA(cudaMemcpyAsync(w.ang, ha, nd * sizeof(float4), cudaMemcpyHostToDevice, W->stream));
-    PSX_CUDA(cudaStreamSynchronize(W->stream));
+    const size_t nb = w.n_bodies;
+    float* st = nullptr;
+    PSX_TRY(body_stage(W, &st));
+    float *sp = st, *sv = st + 3 * nb, *sa = st + 6 * nb;
+    if (pos) PSX_CUDA(cudaMemcpyAsync(sp, pos, 3 * nb * sizeof(float), cudaMemcpyHostToDevice, W->stream));
+    if (quat) PSX_CUDA(cudaMemcpyAsync(w.quat, quat, nb * sizeof(float4), cudaMemcpyHostToDevice, W->stream));
+    if (vel) PSX_CUDA(cudaMemcpyAsync(sv, vel, 3 * nb * sizeof(float), cudaMemcpyHostToDevice, W->stream));
+    if (ang) PSX_CUDA(cudaMemcpyAsync(sa, ang, 3 * nb * sizeof(float), cudaMemcpyHostToDevice, W->stream));
+    launch_unpack_bodies(w, pos ? sp : nullptr, vel ? sv : nullptr, ang ? sa : nullptr, W->stream);
+    PSX_CUDA(cudaStreamSynchronize(W->stream));   // the caller may reuse its arrays on return
+    return PSX_OK;
+}
+
+// A range whose pages another registration already covers stays as it is (two small
+// arrays can share a page); unpinning such a range is then a no-op.
+PSX_API psx_status psx_pin_host(void* p, size_t bytes) {
+    if (!p || !bytes) return fail(PSX_ERR_INVALID_ARG, "psx_pin_host: bad arguments");
+    const cudaError_t e = cudaHostRegister(p, bytes, cudaHostRegisterDefault);
+    if (e == cudaErrorHostMemoryAlreadyRegistered) { cudaGetLastError(); return PSX_OK; }
+    PSX_CUDA(e);
+    return PSX_OK;
+}
+
+PSX_API psx_status psx_unpin_host(void* p) {
+    if (!p) return fail(PSX_ERR_INVALID_ARG, "psx_unpin_host: null pointer");
+    const cudaError_t e = cudaHostUnregister(p);
+    if (e == cudaErrorHostMemoryNotRegistered) { cudaGetLastError(); return PSX_OK; }
+    PSX_CUDA(e);
     return PSX_OK;
 }
 
