@@ -282,7 +282,7 @@ typedef struct psx_body_delta {
 PSX_API psx_status psx_world_apply_deltas(psx_world* w, int32_t n, const psx_body_delta* deltas);
 /* Page-locks (and releases) a caller's host buffer, e.g. the arrays handed to
  * psx_world_read_bodies / psx_world_write_bodies / psx_world_simulate_host, so that their
- * copies run at the host link's speed instead of through the driver's staging. */
+ * copies run at the host link's speed instead of through CUDA's own staging buffers. */
 PSX_API psx_status psx_pin_host(void* p, size_t bytes);
 PSX_API psx_status psx_unpin_host(void* p);
 
