@@ -209,7 +209,7 @@ PSX_API psx_status psx_world_write_bodies(psx_world* w, const float* pos, const 
 /* The same read as psx_world_read_bodies, for callers that must not allocate while
  * they run: a frame loop with a hard deadline (cudaMalloc / cudaMallocHost can stall
  * the device for milliseconds) or a process whose device memory is already handed
- * out to its own pool.  psx_world_read_bodies grows a pinned staging buffer on first
+ * out to its own pool.  psx_world_read_bodies grows a device staging buffer on first
  * use; this call instead packs the state on the device into one fixed array that
  * the library holds for the whole process (3.4 MB per device) and copies from there
  * into the caller's arrays.  On success it calls no allocator, host or device.
