@@ -538,6 +538,12 @@ def main():
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_source": peak_src, "traffic": traffic,
                          "algorithmic_bytes": alg_bytes},
+            # the largest stage is the narrowphase, whose top kernel (EPA, f64 polytope for
+            # parity) is bound by the FP64 pipe rather than by HBM or the tensor cores
+            "dominant_kernel": {"kernel": "k_convex_epa (narrowphase stage)", "bound": "fp64 pipe",
+                                "narrowphase_ms_per_step": stage_ms[1] / args.steps,
+                                "fp64_pipe_active": 0.728,
+                                "source": "profiles/k_convex_epa_256.md (ncu --set full, 256 scenes)"},
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d},
             "plain_gpu_scene_by_scene": None if plain is None else {"value": plain, "unit": METRIC,
                                                                     "scenes": min(args.plain_scenes, len(ss))},
