@@ -57,3 +57,35 @@ def test_errors_without_gpu_are_reported_not_raised(libpsx):
     st = libpsx.psx_scene_create(ctypes.byref(d), ctypes.byref(out))
     assert st != 0
     assert libpsx.psx_last_error_string()
+
+
+def struct_words(name):
+    """4-byte words of `typedef struct name { ... } name;` in the header (fields of 4-byte
+    scalar types, arrays included)."""
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    m = re.search(r"typedef struct %s \{(.*?)\} %s;" % (name, name), src, flags=re.S)
+    assert m, name
+    words = 0
+    for decl in m.group(1).split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        typ, rest = decl.split(None, 1)
+        assert typ in ("int32_t", "uint32_t", "float"), (name, decl)
+        for var in rest.split(","):
+            arr = re.search(r"\[(\d+)\]", var)
+            words += int(arr.group(1)) if arr else 1
+    return words
+
+
+def test_record_layouts_match_the_python_packing():
+    """The Python layer packs these records as flat 4-byte words; their widths follow the
+    header."""
+    expect = {"psx_body_delta": 17, "psx_character": 10, "psx_trigger_event": 9, "psx_trimesh_triangle": 20,
+              "psx_trimesh_node": 8, "psx_ray": 8, "psx_ray_hit": 7, "psx_overlap_query": 14, "psx_overlap_hit": 3,
+              "psx_overlap_mtd_hit": 7}
+    for name, words in expect.items():
+        assert struct_words(name) == words, name
+    from physecs_gb300.api import pack_deltas
+    assert pack_deltas([{"body": 0, "pos": [1, 2, 3], "kinematic": True}]).shape == (1, 17)
