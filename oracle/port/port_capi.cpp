@@ -31,6 +31,11 @@ void orc_scene_read(void* h, float* pos, float* quat, float* vel, float* ang) {
     World* w = static_cast<World*>(h);
     for (size_t b = 0; b < w->bodies.size(); ++b) {
         const Body& B = w->bodies[b];
+        if (!B.alive) {   // a destroyed entity reads as zeros
+            std::memset(pos + 3 * b, 0, 12); std::memset(quat + 4 * b, 0, 16);
+            std::memset(vel + 3 * b, 0, 12); std::memset(ang + 3 * b, 0, 12);
+            continue;
+        }
         std::memcpy(pos + 3 * b, &B.pos, 12);
         std::memcpy(quat + 4 * b, &B.q, 16);
         V3 v = B.hasDyn ? B.vel : V3{0, 0, 0}, a = B.hasDyn ? B.ang : V3{0, 0, 0};
@@ -43,6 +48,7 @@ void orc_scene_write(void* h, const float* pos, const float* quat, const float* 
     World* w = static_cast<World*>(h);
     for (size_t b = 0; b < w->bodies.size(); ++b) {
         Body& B = w->bodies[b];
+        if (!B.alive) continue;
         std::memcpy(&B.pos, pos + 3 * b, 12);
         std::memcpy(&B.q, quat + 4 * b, 16);
         if (B.hasDyn) { std::memcpy(&B.vel, vel + 3 * b, 12); std::memcpy(&B.ang, ang + 3 * b, 12); }
@@ -241,6 +247,17 @@ void orc_scene_set_contact_filter(void* h, int32_t (*f)(int32_t, int32_t, int32_
 }
 
 void orc_scene_set_can_collide(void* h, int b0, int b1, int can) { static_cast<World*>(h)->setCanCollide(b0, b1, can != 0); }
+
+// an entity made from body 0 of d (meshes: this scene's); returns the body index and
+// writes the entity value
+int orc_scene_create_body(void* h, const psx_scene_desc* d, uint32_t* entity) {
+    World* w = static_cast<World*>(h);
+    const int b = w->createBody(d);
+    *entity = w->bodies[b].entity;
+    return b;
+}
+
+void orc_scene_destroy_body(void* h, int b) { static_cast<World*>(h)->destroyBody(b); }
 
 // A batch of registry deltas in array order (psx_body_delta; the scene field is unused)
 void orc_scene_apply_deltas(void* h, int n, const psx_body_delta* d) {

@@ -101,6 +101,9 @@ void World::init(const psx_scene_desc* d) {
         }
     }
     colorBits.assign(bodies.size(), 0);
+    // registry.create() hands out ids 0, 1, ... at version 0 to a fresh registry
+    for (const Body& B : bodies) entPacked.push_back(B.entity);
+    entAlive = entPacked.size();
     for (int j = 0; j < d->n_joints; ++j) {
         Joint J;
         J.type = d->joint_type[j];
@@ -131,6 +134,96 @@ void World::updateBounds(int b, bool margin) {
         e.b = getBounds(colPos(c), colQ(c), colliders[c].g);
         if (margin) { e.b.max += v3s(0.01f); e.b.min -= v3s(0.01f); }
     }
+}
+
+// EnTT 3.12: an entity's next version skips the reserved all-ones version
+static uint32_t nextVersion(uint32_t e) {
+    uint32_t v = (e >> 20) + 1;
+    if (v == 0xfffu) v = 0;
+    return (e & 0xfffffu) | (v << 20);
+}
+
+int World::createBody(const psx_scene_desc* d) {
+    // registry.create(): the entity right past the live ones (the last destroyed), else a new id
+    uint32_t e;
+    if (entAlive < entPacked.size()) e = entPacked[entAlive];
+    else { e = (uint32_t)entPacked.size(); entPacked.push_back(e); }
+    ++entAlive;
+    const int b = (int)bodies.size();
+    Body B;
+    B.entity = e;
+    B.hasDyn = (d->flags[0] & PSX_BODY_DYNAMIC) != 0;
+    B.kinematic = (d->flags[0] & PSX_BODY_KINEMATIC) != 0;
+    B.pos = ld3(d->pos);
+    B.q = ld4(d->quat);
+    if (B.hasDyn) {
+        B.vel = ld3(d->vel);
+        B.ang = ld3(d->ang_vel);
+        B.invMass = d->inv_mass[0];
+        B.com = ld3(d->com);
+        for (int k = 0; k < 3; ++k) B.invI.c[k] = ld3(d->inv_inertia + 3 * k);
+    }
+    B.firstCol = (int)colliders.size();
+    B.nCol = d->collider_start[1] - d->collider_start[0];
+    for (int c = d->collider_start[0]; c < d->collider_start[1]; ++c) {
+        Collider C;
+        C.body = b;
+        C.pos = ld3(d->col_pos + 3 * c);
+        C.q = ld4(d->col_quat + 4 * c);
+        C.g.type = d->col_type[c];
+        for (int k = 0; k < 3; ++k) C.g.p[k] = d->col_params[4 * c + k];
+        if (C.g.type == CONVEX_MESH) C.g.convex = convex[d->col_mesh[c]].get();
+        if (C.g.type == TRIANGLE_MESH) C.g.tri = tri[d->col_mesh[c]].get();
+        C.friction = d->col_material[3 * c];
+        C.restitution = d->col_material[3 * c + 1];
+        C.damping = d->col_material[3 * c + 2];
+        C.trigger = d->col_is_trigger ? d->col_is_trigger[c] != 0 : false;
+        C.enable = d->col_enable_sim ? d->col_enable_sim[c] != 0 : true;
+        C.data = d->col_data ? d->col_data[c] : 0;
+        colliders.push_back(C);
+    }
+    bodies.push_back(B);
+    colorBits.push_back(0);
+    // emplace<RigidBodyCollisionComponent>: onRigidBodyCreate appends the entries with
+    // creation bounds (Physecs.cpp:25-37); emplace<RigidBodyDynamicComponent> then
+    // appends to the dynamic storage and onDynamicCreate sets the entries' flag (:56-66)
+    for (int k = 0; k < B.nCol; ++k) {
+        const int c = B.firstCol + k;
+        bp.push_back({e, b, k, getBounds(colPos(c), colQ(c), colliders[c].g), colliders[c].enable, B.simulated()});
+    }
+    if (B.hasDyn) {
+        bodies[b].dyn = (int)dynBodies.size();
+        dynBodies.push_back(b);
+    }
+    return b;
+}
+
+void World::destroyBody(int b) {
+    Body& B = bodies[b];
+    // registry.destroy removes the components pool by pool, last created pool first:
+    // RigidBodyDynamicComponent (onDynamicDelete, then swap-and-pop of the storage),
+    // TransformComponent, RigidBodyCollisionComponent (onRigidBodyDelete, :39-49)
+    if (B.hasDyn) {
+        for (auto& e : bp) if (e.body == b) e.dynamic = false;
+        const int i = B.dyn, last = dynBodies.back();
+        dynBodies[i] = last;
+        bodies[last].dyn = i;
+        dynBodies.pop_back();
+        B.dyn = -1;
+        B.hasDyn = false;
+    }
+    for (int k = 0; k < B.nCol; ++k) {
+        size_t id = 0;
+        while (!(bp[id].body == b && bp[id].col == k)) ++id;
+        bp[id] = bp.back();
+        bp.pop_back();
+    }
+    // the entity: version bumped, swapped just past the live ones
+    size_t pos = 0;
+    while (entPacked[pos] != B.entity) ++pos;
+    entPacked[pos] = nextVersion(B.entity);
+    if (pos != --entAlive) std::swap(entPacked[pos], entPacked[entAlive]);
+    B.alive = false;
 }
 
 // registry.patch<TransformComponent> after a pose write: Scene::onRigidBodyMove ->

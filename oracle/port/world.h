@@ -24,6 +24,7 @@ struct Body {
     M3 invI{};
     int firstCol = 0, nCol = 0;
     int dyn = -1;               // position in dynamic storage (src/Physecs.cpp:271)
+    bool alive = true;          // false once its entity is destroyed
     bool simulated() const { return hasDyn && !kinematic; }
 };
 
@@ -104,6 +105,10 @@ struct World {
     // Scene::setContactFilter's function (Physecs.cpp:795-797); null: the default filter
     int32_t (*contactFilter)(int32_t, int32_t, int32_t, int32_t) = nullptr;
     std::vector<int> dynBodies;                // dyn index -> body
+    // the registry's entity storage (EnTT 3.12 storage<entity>): the first entAlive are in
+    // use, the rest destroyed (their versions bumped), reused most recent first
+    std::vector<uint32_t> entPacked;
+    size_t entAlive = 0;
     int substeps = 8, iterations = 2;
     float g = 9.81f;
 
@@ -150,6 +155,11 @@ struct World {
     void setIsKinematic(int b, bool kinematic);
     // Scene::setCanCollide (Physecs.cpp:788-793) for bodies b0 and b1
     void setCanCollide(int b0, int b1, bool canCollide);
+    // an entity created with Transform, RigidBodyCollisionComponent and (for a dynamic
+    // body) RigidBodyDynamicComponent, in that order, from body 0 of d (meshes are this
+    // world's); returns the new body's index.  registry.destroy of a body's entity.
+    int createBody(const psx_scene_desc* d);
+    void destroyBody(int b);
     // CharacterController::move for body b (CharacterController.cpp:5-45); returns the
     // CharacterCollisionFlags value
     int moveCharacter(int b, float height, float radius, float maxStepHeight, float slopeLimit, int iterations, V3 translation);

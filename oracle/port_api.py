@@ -52,6 +52,8 @@ def lib():
         _lib.orc_scene_trigger_events.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
         _lib.orc_trimesh_build.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
         _lib.orc_scene_apply_deltas.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        _lib.orc_scene_create_body.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.orc_scene_destroy_body.argtypes = [C.c_void_p, C.c_int]
         _lib.orc_scene_set_contact_filter.argtypes = [C.c_void_p, C.c_void_p]
         _lib.orc_scene_set_can_collide.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
         _lib.orc_character_move.argtypes = [C.c_void_p, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int,
@@ -174,6 +176,21 @@ class OracleScene:
         t = np.ascontiguousarray(translation, np.float32)
         return lib().orc_character_move(self.h, int(body), height, radius, max_step_height, slope_limit, int(iterations),
                                         _p(t))
+
+    def create_body(self, body_scene):
+        """A new entity from the single body of `body_scene` (a SceneData whose meshes
+        are not used: collider mesh indices refer to this scene's).  Returns (body index,
+        entity value)."""
+        from physecs_gb300.desc import make_desc
+        d = make_desc(body_scene)
+        ent = C.c_uint32()
+        b = lib().orc_scene_create_body(self.h, C.byref(d), C.byref(ent))
+        self.n = max(self.n, b + 1)
+        return b, ent.value
+
+    def destroy_body(self, b):
+        """registry.destroy of body b's entity; its state then reads as zeros."""
+        lib().orc_scene_destroy_body(self.h, int(b))
 
     def apply_deltas(self, deltas):
         """Registry deltas in array order: a (n, 17) float32 array in psx_body_delta layout

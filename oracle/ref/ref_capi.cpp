@@ -213,6 +213,36 @@ int ref_character_move(void* h, int b, float height, float radius, float max_ste
     return cc.move(v3(translation), dt).value;
 }
 
+// A new entity as a Physecs user makes one (Transform, RigidBodyCollisionComponent, then
+// RigidBodyDynamicComponent for a dynamic body) from body 0 of d, whose meshes index this
+// scene's; returns the body index and writes the entity value
+int ref_scene_create_body(void* h, const psx_scene_desc* d, uint32_t* entity) {
+    auto* w = static_cast<RefWorld*>(h);
+    entt::entity e = w->registry.create();
+    w->registry.emplace<TransformComponent>(e, v3(d->pos), q4(d->quat), glm::vec3(1));
+    std::vector<physecs::Collider> cols;
+    for (int c = d->collider_start[0]; c < d->collider_start[1]; ++c) cols.push_back(make_collider(*w, d, c));
+    w->registry.emplace<physecs::RigidBodyCollisionComponent>(e, cols);
+    if (d->flags[0] & PSX_BODY_DYNAMIC) {
+        glm::mat3 invI;
+        for (int k = 0; k < 9; ++k) invI[k / 3][k % 3] = d->inv_inertia[k];
+        w->registry.emplace<physecs::RigidBodyDynamicComponent>(e, (d->flags[0] & PSX_BODY_KINEMATIC) != 0, v3(d->vel),
+                                                                 v3(d->ang_vel), d->inv_mass[0], v3(d->com), invI);
+    }
+    const int b = (int)w->entities.size();
+    w->entities.push_back(e);
+    w->triggers.body_of[(uint32_t)e] = b;
+    *entity = (uint32_t)e;
+    return b;
+}
+
+// registry.destroy of body b's entity
+void ref_scene_destroy_body(void* h, int b) {
+    auto* w = static_cast<RefWorld*>(h);
+    w->registry.destroy(w->entities[b]);
+    w->entities[b] = entt::null;
+}
+
 // Scene::setContactFilter with the caller's function (null: the default filter)
 void ref_scene_set_contact_filter(void* h, physecs::ContactType (*f)(bool, int, bool, int)) {
     static_cast<RefWorld*>(h)->scene->setContactFilter(f ? f : physecs::defaultContactFilter);
@@ -299,6 +329,11 @@ void ref_scene_set_knobs(void* h, int substeps, int iterations, float gravity) {
 void ref_scene_read(void* h, float* pos, float* quat, float* vel, float* ang_vel) {
     auto* w = static_cast<RefWorld*>(h);
     for (size_t b = 0; b < w->entities.size(); ++b) {
+        if (w->entities[b] == entt::null) {   // a destroyed entity reads as zeros
+            std::memset(pos + 3 * b, 0, 12); std::memset(quat + 4 * b, 0, 16);
+            std::memset(vel + 3 * b, 0, 12); std::memset(ang_vel + 3 * b, 0, 12);
+            continue;
+        }
         auto& t = w->registry.get<TransformComponent>(w->entities[b]);
         pos[3 * b + 0] = t.position.x; pos[3 * b + 1] = t.position.y; pos[3 * b + 2] = t.position.z;
         quat[4 * b + 0] = t.orientation.x; quat[4 * b + 1] = t.orientation.y;
@@ -315,6 +350,7 @@ void ref_scene_read(void* h, float* pos, float* quat, float* vel, float* ang_vel
 void ref_scene_write(void* h, const float* pos, const float* quat, const float* vel, const float* ang_vel) {
     auto* w = static_cast<RefWorld*>(h);
     for (size_t b = 0; b < w->entities.size(); ++b) {
+        if (w->entities[b] == entt::null) continue;
         auto& t = w->registry.get<TransformComponent>(w->entities[b]);
         t.position = v3(pos + 3 * b);
         t.orientation = q4(quat + 4 * b);

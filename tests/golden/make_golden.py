@@ -19,6 +19,8 @@ oracle/ref/build_ref.py) on seeded scenes from physecs_gb300.scenes:
                        poses, written velocities, setIsKinematic) between frames
   filters.npz          body states and trigger events of a scene stepped under a user
                        contact filter, with setCanCollide toggled between frames
+  topology.npz         entity values and body states of a scene whose entities are
+                       destroyed and created between frames
 
 Run in a checkout with the reference present:  python tests/golden/make_golden.py
 """
@@ -314,6 +316,36 @@ def filter_fixture():
     return out
 
 
+def topology_case():
+    """(scene, schedule, frames, recorded frames) for entities destroyed and created
+    between frames (tests/scene_variants.py topology_schedule)."""
+    sys.path.insert(0, os.path.dirname(HERE))
+    from scene_variants import topology_schedule
+    s = scenes.batch_scene(11, n_bodies=60, chain_prob=0.0)
+    return s, topology_schedule(s, 60, seed=11), 60, [30, 60]
+
+
+def topology_fixture():
+    from oracle.ref.ref_api import RefScene
+    s, sch, frames, rec = topology_case()
+    r = RefScene(s)
+    out = {"scene_sha256": np.array(scene_hash(s))}
+    ents = []
+    for f in range(frames):
+        if f in sch:
+            kill, spawn = sch[f]
+            for b in kill:
+                r.destroy_body(b)
+            for sp in spawn:
+                ents.append(r.create_body(sp)[1])
+        r.step()
+        if f + 1 in rec:
+            for k, v in r.state().items():
+                out["f%d_%s" % (f + 1, k)] = v
+    out["entities"] = np.asarray(ents, np.uint32)
+    return out
+
+
 def trigger_scenes():
     """name -> (scene, frames stepped)."""
     sys.path.insert(0, os.path.dirname(HERE))
@@ -381,6 +413,8 @@ def main():
     print("deltas ok")
     np.savez_compressed(os.path.join(HERE, "filters.npz"), **filter_fixture())
     print("filters ok")
+    np.savez_compressed(os.path.join(HERE, "topology.npz"), **topology_fixture())
+    print("topology ok")
 
 
 if __name__ == "__main__":

@@ -165,3 +165,52 @@ def character_moves(n_chars, frames, seed=62):
         t = np.stack([0.12 * np.cos(head), np.full(n_chars, -0.05), 0.12 * np.sin(head)], 1).astype(np.float32)
         out.append(t)
     return out
+
+
+def spawn_body(rng, center, kind=None):
+    """A single dynamic body (sphere, box or capsule) as a SceneData, for creating an
+    entity after the scene's creation."""
+    s = scenes.SceneData("spawn")
+    kind = int(rng.integers(0, 3)) if kind is None else kind
+    if kind == 0:
+        r = float(rng.uniform(0.2, 0.5))
+        m, com, inertia = scenes.mass_sphere(r)
+        typ, prm = scenes.SPHERE, [r, 0, 0, 0]
+    elif kind == 1:
+        he = rng.uniform(0.15, 0.4, 3)
+        m, com, inertia = scenes.mass_box(he)
+        typ, prm = scenes.BOX, list(he) + [0]
+    else:
+        hh, r = float(rng.uniform(0.2, 0.5)), float(rng.uniform(0.15, 0.3))
+        m, com, inertia = scenes.mass_capsule(hh, r)
+        typ, prm = scenes.CAPSULE, [hh, r, 0, 0]
+    q = rng.normal(size=4)
+    s.add_bodies(pos=[center], quat=[q / np.linalg.norm(q)], flags=scenes.BODY_DYNAMIC, inv_mass=1.0 / m, com=com,
+                 inv_inertia=np.linalg.inv(inertia).T.ravel(), col_type=typ, col_params=prm,
+                 vel=[rng.normal(0, 1, 3)])
+    return s.finalize()
+
+
+def topology_schedule(s, frames, seed=7, every=4):
+    """frame -> (bodies to destroy, SceneData bodies to create): every `every` frames two
+    bodies that carry no joint (never the ground, body 0) are destroyed, also ones created
+    earlier, and two or three bodies are dropped in above the scene."""
+    a = s.arrays
+    rng = np.random.default_rng(seed)
+    jointed = set(np.asarray(a.get("joint_body0", []), int)) | set(np.asarray(a.get("joint_body1", []), int))
+    alive = [b for b in range(1, len(a["pos"])) if b not in jointed]
+    n = len(a["pos"])
+    lo, hi = a["pos"].min(0), a["pos"].max(0)
+    out = {}
+    for f in range(0, frames, every):
+        kill = [int(x) for x in rng.choice(alive, 2, replace=False)]
+        for b in kill:
+            alive.remove(b)
+        spawn = []
+        for _ in range(int(rng.integers(2, 4))):
+            c = [rng.uniform(lo[0], hi[0]), hi[1] + rng.uniform(1, 3), rng.uniform(lo[2], hi[2])]
+            spawn.append(spawn_body(rng, c))
+            alive.append(n)
+            n += 1
+        out[f] = (kill, spawn)
+    return out

@@ -1,0 +1,62 @@
+"""Entities destroyed and created between frames in the CPU oracle, against the
+reference: registry.destroy / registry.create with the reference's signal handlers
+(onRigidBodyCreate / onRigidBodyDelete, onDynamicCreate / onDynamicDelete,
+src/Physecs.cpp:25-66) and EnTT 3.12's storages (component storage swap-and-pop,
+entity ids recycled most recent first with their version bumped).  Entity values and
+states bit for bit: against tests/golden/topology.npz (made by the reference,
+tests/golden/make_golden.py) and live where the reference library is built.  The
+device path for topology changes is not built; this pins the semantics it must meet."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "golden"))
+import make_golden  # noqa: E402
+from scene_variants import topology_schedule  # noqa: E402
+
+
+def _run(sim, sch, frames, rec=()):
+    ents, states = [], {}
+    for f in range(frames):
+        if f in sch:
+            kill, spawn = sch[f]
+            for b in kill:
+                sim.destroy_body(b)
+            for sp in spawn:
+                ents.append(sim.create_body(sp)[1])
+        sim.step()
+        if f + 1 in rec:
+            states[f + 1] = sim.state()
+    return ents, states
+
+
+def test_oracle_topology_matches_reference_fixture(oracle_lib):
+    from oracle.port_api import OracleScene
+    d = np.load(os.path.join(HERE, "golden", "topology.npz"))
+    s, sch, frames, rec = make_golden.topology_case()
+    assert str(d["scene_sha256"]) == make_golden.scene_hash(s)
+    ents, states = _run(OracleScene(s), sch, frames, rec)
+    assert list(ents) == list(d["entities"])
+    assert any(e >> 20 for e in ents) and any(not e >> 20 for e in ents)   # recycled and fresh ids
+    for f in rec:
+        for k, v in states[f].items():
+            assert np.array_equal(v.view(np.uint32), d["f%d_%s" % (f, k)].view(np.uint32)), (f, k)
+
+
+def test_oracle_topology_matches_live_reference(oracle_lib):
+    from oracle.ref import ref_api
+    if not ref_api.available():
+        pytest.skip("reference library not built here")
+    from oracle.port_api import OracleScene
+    from oracle.ref.ref_api import RefScene
+    from physecs_gb300 import scenes
+    s = scenes.batch_scene(12, n_bodies=60, chain_prob=0.0)
+    sch = topology_schedule(s, 40, seed=12, every=3)
+    eo, so = _run(OracleScene(s), sch, 40, [40])
+    er, sr = _run(RefScene(s), sch, 40, [40])
+    assert eo == er
+    for k in so[40]:
+        assert np.array_equal(so[40][k].view(np.uint32), sr[40][k].view(np.uint32)), k
