@@ -259,6 +259,12 @@ int orc_scene_create_body(void* h, const psx_scene_desc* d, uint32_t* entity) {
 
 void orc_scene_destroy_body(void* h, int b) { static_cast<World*>(h)->destroyBody(b); }
 
+int orc_scene_create_joint(void* h, int type, int b0, int b1, const float* frames, const float* params) {
+    return static_cast<World*>(h)->createJoint(type, b0, b1, frames, params);
+}
+
+void orc_scene_destroy_joint(void* h, int j) { static_cast<World*>(h)->destroyJoint(j); }
+
 // A batch of registry deltas in array order (psx_body_delta; the scene field is unused)
 void orc_scene_apply_deltas(void* h, int n, const psx_body_delta* d) {
     World* w = static_cast<World*>(h);

@@ -104,27 +104,9 @@ void World::init(const psx_scene_desc* d) {
     // registry.create() hands out ids 0, 1, ... at version 0 to a fresh registry
     for (const Body& B : bodies) entPacked.push_back(B.entity);
     entAlive = entPacked.size();
-    for (int j = 0; j < d->n_joints; ++j) {
-        Joint J;
-        J.type = d->joint_type[j];
-        J.body0 = d->joint_body0[j];
-        J.body1 = d->joint_body1[j];
-        const float* f = d->joint_frames + 14 * j;
-        J.a0p = ld3(f); J.a0q = ld4(f + 3); J.a1p = ld3(f + 7); J.a1q = ld4(f + 10);
-        std::memcpy(J.params, d->joint_params + PSX_JOINT_PARAMS * j, sizeof(J.params));
-        if (J.type == PSX_JOINT_GEAR) J.persistent0 = J.persistent1 = J.virtual0 = J.virtual1 = 0;
-        // Scene::addJoint (Physecs.cpp:690-710)
-        uint32_t e0 = bodies[J.body0].entity, e1 = bodies[J.body1].entity;
-        nonColliding[e0 < e1 ? std::make_pair(e0, e1) : std::make_pair(e1, e0)] = 1;
-        unsigned char u = colorBits[J.body0] | colorBits[J.body1];
-        unsigned int inv = ~(unsigned int)u;
-        int i = __builtin_ctz(inv);
-        colorBits[J.body0] |= (unsigned char)(1u << i);
-        colorBits[J.body1] |= (unsigned char)(1u << i);
-        J.color = i;
-        colors[i].push_back((int)joints.size());
-        joints.push_back(J);
-    }
+    for (int j = 0; j < d->n_joints; ++j)
+        createJoint(d->joint_type[j], d->joint_body0[j], d->joint_body1[j], d->joint_frames + 14 * j,
+                    d->joint_params + PSX_JOINT_PARAMS * j);
 }
 
 void World::updateBounds(int b, bool margin) {
@@ -134,6 +116,43 @@ void World::updateBounds(int b, bool margin) {
         e.b = getBounds(colPos(c), colQ(c), colliders[c].g);
         if (margin) { e.b.max += v3s(0.01f); e.b.min -= v3s(0.01f); }
     }
+}
+
+// Scene::createJoint -> Scene::addJoint (Physecs.cpp:690-710): the pair stops colliding,
+// the joint takes the lowest colour free on both bodies and goes last in that colour
+int World::createJoint(int type, int b0, int b1, const float* f, const float* params) {
+    Joint J;
+    J.type = type;
+    J.body0 = b0;
+    J.body1 = b1;
+    J.a0p = ld3(f); J.a0q = ld4(f + 3); J.a1p = ld3(f + 7); J.a1q = ld4(f + 10);
+    std::memcpy(J.params, params, sizeof(J.params));
+    if (J.type == PSX_JOINT_GEAR) J.persistent0 = J.persistent1 = J.virtual0 = J.virtual1 = 0;
+    uint32_t e0 = bodies[b0].entity, e1 = bodies[b1].entity;
+    nonColliding[e0 < e1 ? std::make_pair(e0, e1) : std::make_pair(e1, e0)] = 1;
+    unsigned char u = colorBits[b0] | colorBits[b1];
+    unsigned int inv = ~(unsigned int)u;
+    int i = __builtin_ctz(inv);
+    colorBits[b0] |= (unsigned char)(1u << i);
+    colorBits[b1] |= (unsigned char)(1u << i);
+    J.color = i;
+    colors[i].push_back((int)joints.size());
+    joints.push_back(J);
+    return (int)joints.size() - 1;
+}
+
+// Scene::destroyJoint (Physecs.cpp:712-725): out of its colour (the others keep their
+// order), the pair collides again, the colour is free again on both bodies
+void World::destroyJoint(int j) {
+    Joint& J = joints[j];
+    auto& list = colors[J.color];
+    auto it = std::find(list.begin(), list.end(), j);
+    if (it == list.end()) return;
+    list.erase(it);
+    uint32_t e0 = bodies[J.body0].entity, e1 = bodies[J.body1].entity;
+    nonColliding.erase(e0 < e1 ? std::make_pair(e0, e1) : std::make_pair(e1, e0));
+    colorBits[J.body0] &= (unsigned char)~(1u << J.color);
+    colorBits[J.body1] &= (unsigned char)~(1u << J.color);
 }
 
 // EnTT 3.12: an entity's next version skips the reserved all-ones version

@@ -160,6 +160,9 @@ struct World {
     // world's); returns the new body's index.  registry.destroy of a body's entity.
     int createBody(const psx_scene_desc* d);
     void destroyBody(int b);
+    // Scene::createJoint / destroyJoint (Physecs.cpp:690-725) for a psx joint record
+    int createJoint(int type, int b0, int b1, const float* frames, const float* params);
+    void destroyJoint(int j);
     // CharacterController::move for body b (CharacterController.cpp:5-45); returns the
     // CharacterCollisionFlags value
     int moveCharacter(int b, float height, float radius, float maxStepHeight, float slopeLimit, int iterations, V3 translation);

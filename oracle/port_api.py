@@ -54,6 +54,8 @@ def lib():
         _lib.orc_scene_apply_deltas.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
         _lib.orc_scene_create_body.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.orc_scene_destroy_body.argtypes = [C.c_void_p, C.c_int]
+        _lib.orc_scene_create_joint.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+        _lib.orc_scene_destroy_joint.argtypes = [C.c_void_p, C.c_int]
         _lib.orc_scene_set_contact_filter.argtypes = [C.c_void_p, C.c_void_p]
         _lib.orc_scene_set_can_collide.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
         _lib.orc_character_move.argtypes = [C.c_void_p, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int,
@@ -187,6 +189,18 @@ class OracleScene:
         b = lib().orc_scene_create_body(self.h, C.byref(d), C.byref(ent))
         self.n = max(self.n, b + 1)
         return b, ent.value
+
+    def create_joint(self, jtype, body0, body1, frames, params=None):
+        """Scene::createJoint between frames: frames = 14 floats (anchor 0 position and
+        orientation, anchor 1 position and orientation), params = 8 floats.  Returns the
+        joint index."""
+        f = np.ascontiguousarray(frames, np.float32).ravel()
+        p = np.zeros(8, np.float32) if params is None else np.ascontiguousarray(params, np.float32).ravel()
+        return lib().orc_scene_create_joint(self.h, int(jtype), int(body0), int(body1), _p(f), _p(p))
+
+    def destroy_joint(self, j):
+        """Scene::destroyJoint of joint j."""
+        lib().orc_scene_destroy_joint(self.h, int(j))
 
     def destroy_body(self, b):
         """registry.destroy of body b's entity; its state then reads as zeros."""

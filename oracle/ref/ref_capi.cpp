@@ -65,6 +65,7 @@ struct RefWorld {
     std::vector<std::unique_ptr<physecs::ConvexMesh>> convex;
     std::vector<std::unique_ptr<physecs::TriangleMesh>> trimesh;
     TriggerRecorder triggers;
+    std::vector<physecs::Joint*> joints;   // by joint index; null once destroyed
 };
 
 glm::vec3 v3(const float* p) { return glm::vec3(p[0], p[1], p[2]); }
@@ -98,6 +99,49 @@ physecs::Collider make_collider(RefWorld& w, const psx_scene_desc* d, int c) {
 }
 
 }  // namespace
+
+// Scene::createJoint<T> for a psx joint record, configured as the user sets it up
+physecs::Joint* make_joint(RefWorld& w, int type, int b0, int b1, const float* f, const float* p) {
+    entt::entity e0 = w.entities[b0];
+    entt::entity e1 = w.entities[b1];
+    glm::vec3 p0 = v3(f), p1 = v3(f + 7);
+    glm::quat o0 = q4(f + 3), o1 = q4(f + 10);
+    switch (type) {
+        case PSX_JOINT_FIXED: return w.scene->createJoint<physecs::FixedJoint>(e0, p0, o0, e1, p1, o1);
+        case PSX_JOINT_REVOLUTE: {
+            auto* jt = w.scene->createJoint<physecs::RevoluteJoint>(e0, p0, o0, e1, p1, o1);
+            jt->setDriveEnabled(p[0] != 0.f);
+            jt->setDriveVelocity(p[1]);
+            jt->setDriveMaxTorque(p[2]);
+            return jt;
+        }
+        case PSX_JOINT_SPHERICAL: return w.scene->createJoint<physecs::SphericalJoint>(e0, p0, o0, e1, p1, o1);
+        case PSX_JOINT_PRISMATIC: {
+            auto* jt = w.scene->createJoint<physecs::PrismaticJoint>(e0, p0, o0, e1, p1, o1);
+            jt->setUpperLimit(p[0]);
+            jt->setLowerLimit(p[1]);
+            jt->setDriveEnabled(p[2] != 0.f);
+            jt->setTargetPosition(p[3]);
+            jt->setDriveStiffness(p[4]);
+            jt->setDriveDamping(p[5]);
+            return jt;
+        }
+        case PSX_JOINT_UNIVERSAL: return w.scene->createJoint<physecs::UniversalJoint>(e0, p0, o0, e1, p1, o1);
+        case PSX_JOINT_GEAR: {
+            auto* jt = w.scene->createJoint<physecs::GearJoint>(e0, p0, o0, e1, p1, o1);
+            jt->setGearRatio(p[0]);
+            return jt;
+        }
+        case PSX_JOINT_SERVO: {
+            auto* jt = w.scene->createJoint<physecs::ServoJoint>(e0, p0, o0, e1, p1, o1);
+            jt->setTargetAngle(p[0]);
+            jt->setDriveStiffness(p[1]);
+            jt->setDriveDamping(p[2]);
+            return jt;
+        }
+    }
+    return nullptr;
+}
 
 extern "C" {
 
@@ -147,48 +191,9 @@ void* ref_scene_create(const psx_scene_desc* d, int num_threads) {
                 d->inv_mass[b], v3(d->com + 3 * b), invI);
         }
     }
-    for (int j = 0; j < d->n_joints; ++j) {
-        entt::entity e0 = w->entities[d->joint_body0[j]];
-        entt::entity e1 = w->entities[d->joint_body1[j]];
-        const float* f = d->joint_frames + 14 * j;
-        const float* p = d->joint_params + PSX_JOINT_PARAMS * j;
-        glm::vec3 p0 = v3(f), p1 = v3(f + 7);
-        glm::quat o0 = q4(f + 3), o1 = q4(f + 10);
-        switch (d->joint_type[j]) {
-            case PSX_JOINT_FIXED: w->scene->createJoint<physecs::FixedJoint>(e0, p0, o0, e1, p1, o1); break;
-            case PSX_JOINT_REVOLUTE: {
-                auto* jt = w->scene->createJoint<physecs::RevoluteJoint>(e0, p0, o0, e1, p1, o1);
-                jt->setDriveEnabled(p[0] != 0.f);
-                jt->setDriveVelocity(p[1]);
-                jt->setDriveMaxTorque(p[2]);
-                break;
-            }
-            case PSX_JOINT_SPHERICAL: w->scene->createJoint<physecs::SphericalJoint>(e0, p0, o0, e1, p1, o1); break;
-            case PSX_JOINT_PRISMATIC: {
-                auto* jt = w->scene->createJoint<physecs::PrismaticJoint>(e0, p0, o0, e1, p1, o1);
-                jt->setUpperLimit(p[0]);
-                jt->setLowerLimit(p[1]);
-                jt->setDriveEnabled(p[2] != 0.f);
-                jt->setTargetPosition(p[3]);
-                jt->setDriveStiffness(p[4]);
-                jt->setDriveDamping(p[5]);
-                break;
-            }
-            case PSX_JOINT_UNIVERSAL: w->scene->createJoint<physecs::UniversalJoint>(e0, p0, o0, e1, p1, o1); break;
-            case PSX_JOINT_GEAR: {
-                auto* jt = w->scene->createJoint<physecs::GearJoint>(e0, p0, o0, e1, p1, o1);
-                jt->setGearRatio(p[0]);
-                break;
-            }
-            case PSX_JOINT_SERVO: {
-                auto* jt = w->scene->createJoint<physecs::ServoJoint>(e0, p0, o0, e1, p1, o1);
-                jt->setTargetAngle(p[0]);
-                jt->setDriveStiffness(p[1]);
-                jt->setDriveDamping(p[2]);
-                break;
-            }
-        }
-    }
+    for (int j = 0; j < d->n_joints; ++j)
+        w->joints.push_back(make_joint(*w, d->joint_type[j], d->joint_body0[j], d->joint_body1[j], d->joint_frames + 14 * j,
+                                       d->joint_params + PSX_JOINT_PARAMS * j));
     return w;
 }
 
@@ -234,6 +239,20 @@ int ref_scene_create_body(void* h, const psx_scene_desc* d, uint32_t* entity) {
     w->triggers.body_of[(uint32_t)e] = b;
     *entity = (uint32_t)e;
     return b;
+}
+
+// Scene::createJoint between frames (a psx joint record); returns the joint index
+int ref_scene_create_joint(void* h, int type, int b0, int b1, const float* frames, const float* params) {
+    auto* w = static_cast<RefWorld*>(h);
+    w->joints.push_back(make_joint(*w, type, b0, b1, frames, params));
+    return (int)w->joints.size() - 1;
+}
+
+// Scene::destroyJoint of joint j
+void ref_scene_destroy_joint(void* h, int j) {
+    auto* w = static_cast<RefWorld*>(h);
+    w->scene->destroyJoint(w->joints[j]);
+    w->joints[j] = nullptr;
 }
 
 // registry.destroy of body b's entity

@@ -325,11 +325,40 @@ def topology_case():
     return s, topology_schedule(s, 60, seed=11), 60, [30, 60]
 
 
+def joint_topology_case():
+    """(scene, plan {frame: ("destroy", joint) | ("create", (type, body0, body1))}, anchor
+    frames, frames): capsule chains whose joints are destroyed and created between frames,
+    a joint made between frames destroyed again among them."""
+    s = scenes.joint_chains(n_chains=4, links=6)
+    nj = len(s.arrays["joint_type"])
+    fr = np.zeros(14, np.float32)
+    fr[1], fr[6], fr[8], fr[13] = -0.35, 1.0, 0.35, 1.0
+    plan = {8: ("destroy", 3), 12: ("create", (scenes.JOINT_SPHERICAL, 6, 12)), 20: ("destroy", 10),
+            25: ("create", (scenes.JOINT_REVOLUTE, 18, 24)), 30: ("destroy", nj), 35: ("create", (scenes.JOINT_FIXED, 2, 9))}
+    return s, plan, fr, 50
+
+
+def run_joint_plan(sim, plan, fr, frames):
+    for f in range(frames):
+        if f in plan:
+            kind, arg = plan[f]
+            if kind == "destroy":
+                sim.destroy_joint(arg)
+            else:
+                sim.create_joint(arg[0], arg[1], arg[2], fr)
+        sim.step()
+    return sim.state()
+
+
 def topology_fixture():
     from oracle.ref.ref_api import RefScene
     s, sch, frames, rec = topology_case()
     r = RefScene(s)
     out = {"scene_sha256": np.array(scene_hash(s))}
+    js, plan, fr, jframes = joint_topology_case()
+    out["joints_scene_sha256"] = np.array(scene_hash(js))
+    for k, v in run_joint_plan(RefScene(js), plan, fr, jframes).items():
+        out["joints_f%d_%s" % (jframes, k)] = v
     ents = []
     for f in range(frames):
         if f in sch:

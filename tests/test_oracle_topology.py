@@ -60,3 +60,16 @@ def test_oracle_topology_matches_live_reference(oracle_lib):
     assert eo == er
     for k in so[40]:
         assert np.array_equal(so[40][k].view(np.uint32), sr[40][k].view(np.uint32)), k
+
+
+def test_oracle_joint_topology_matches_reference_fixture(oracle_lib):
+    """Scene::createJoint / destroyJoint between frames (src/Physecs.cpp:690-725): a
+    destroyed joint leaves its colour (the rest keep their order) and frees the colour
+    and the pair; a new one takes the lowest colour free on both bodies."""
+    from oracle.port_api import OracleScene
+    d = np.load(os.path.join(HERE, "golden", "topology.npz"))
+    s, plan, fr, frames = make_golden.joint_topology_case()
+    assert str(d["joints_scene_sha256"]) == make_golden.scene_hash(s)
+    st = make_golden.run_joint_plan(OracleScene(s), plan, fr, frames)
+    for k, v in st.items():
+        assert np.array_equal(v.view(np.uint32), d["joints_f%d_%s" % (frames, k)].view(np.uint32)), k
