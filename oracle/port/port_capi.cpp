@@ -105,7 +105,7 @@ int orc_scene_collide(void* h, int n_pairs, const int32_t* pairs, int32_t* ids, 
     std::vector<Manifold> buf;
     for (int i = 0; i < n_pairs; ++i) {
         int b0 = pairs[4 * i], b1 = pairs[4 * i + 2];
-        int c0 = w->bodies[b0].firstCol + pairs[4 * i + 1], c1 = w->bodies[b1].firstCol + pairs[4 * i + 3];
+        int c0 = w->bodies[b0].cols[pairs[4 * i + 1]], c1 = w->bodies[b1].cols[pairs[4 * i + 3]];
         buf.clear();
         if (!collision(w->colPos(c0), w->colQ(c0), w->colliders[c0].g, w->colPos(c1), w->colQ(c1), w->colliders[c1].g, buf)) continue;
         for (const Manifold& m : buf) {
@@ -189,7 +189,7 @@ void orc_scene_raycast(void* h, int n, const float* rays, const uint8_t* accept,
             continue;
         }
         out_ids[2 * i] = w->colliders[c].body;
-        out_ids[2 * i + 1] = c - w->bodies[w->colliders[c].body].firstCol;
+        out_ids[2 * i + 1] = w->colliders[c].local;
         V3 p = o + d * dist;   // rayOrig + rayDir * distance (src/Physecs.cpp:624)
         of[0] = dist; of[1] = p.x; of[2] = p.y; of[3] = p.z;
     }
@@ -209,7 +209,7 @@ int orc_scene_overlap(void* h, const float* pose, int type, const float* params,
     for (int k = 0; k < (int)hits.size() && k < cap; ++k) {
         int c = hits[k];
         out[2 * k] = w->colliders[c].body;
-        out[2 * k + 1] = c - w->bodies[w->colliders[c].body].firstCol;
+        out[2 * k + 1] = w->colliders[c].local;
     }
     return (int)hits.size();
 }
@@ -229,7 +229,7 @@ int orc_scene_overlap_mtd(void* h, const float* pose, int type, const float* par
     for (int k = 0; k < (int)hits.size() && k < cap; ++k) {
         int c = hits[k].col;
         out_ids[2 * k] = w->colliders[c].body;
-        out_ids[2 * k + 1] = c - w->bodies[w->colliders[c].body].firstCol;
+        out_ids[2 * k + 1] = w->colliders[c].local;
         out_f[4 * k] = hits[k].n.x; out_f[4 * k + 1] = hits[k].n.y; out_f[4 * k + 2] = hits[k].n.z; out_f[4 * k + 3] = hits[k].mtd;
     }
     return (int)hits.size();
@@ -258,6 +258,10 @@ int orc_scene_create_body(void* h, const psx_scene_desc* d, uint32_t* entity) {
 }
 
 void orc_scene_destroy_body(void* h, int b) { static_cast<World*>(h)->destroyBody(b); }
+
+void orc_scene_add_collider(void* h, int b, const psx_scene_desc* d) { static_cast<World*>(h)->addCollider(b, d); }
+
+void orc_scene_clear_colliders(void* h, int b) { static_cast<World*>(h)->clearColliders(b); }
 
 int orc_scene_create_joint(void* h, int type, int b0, int b1, const float* frames, const float* params) {
     return static_cast<World*>(h)->createJoint(type, b0, b1, frames, params);

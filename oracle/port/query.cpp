@@ -273,7 +273,7 @@ int World::raycastClosest(V3 o, V3 d, float maxd, const uint8_t* accept, float& 
     int best = -1;
     float bestT = FLT_MAX;
     for (const BPEntry& e : bp) {
-        const int c = bodies[e.body].firstCol + e.col;
+        const int c = bodies[e.body].cols[e.col];
         float t;
         if (!rayAABB(o, d, e.b.min, e.b.max, t) || t > maxd) continue;
         if (!rayGeometry(o, d, colPos(c), colQ(c), colliders[c].g, t) || t > maxd) continue;
@@ -288,7 +288,7 @@ void World::overlap(V3 pos, Q4 ori, const Geometry& g, int filter, std::vector<i
     const Bounds qb = getBounds(pos, ori, g);
     out.clear();
     for (const BPEntry& e : bp) {
-        const int c = bodies[e.body].firstCol + e.col;
+        const int c = bodies[e.body].cols[e.col];
         if (!boundsMeet(qb, e.b)) continue;
         if (filter && !(colliders[c].data & filter)) continue;
         if (!overlapGeom(pos, ori, g, colPos(c), colQ(c), colliders[c].g)) continue;
@@ -344,7 +344,7 @@ void World::overlapMtd(V3 pos, Q4 ori, const Geometry& g, std::vector<MtdHit>& o
     const Bounds qb = getBounds(pos, ori, g);
     out.clear();
     for (const BPEntry& e : bp) {
-        const int c = bodies[e.body].firstCol + e.col;
+        const int c = bodies[e.body].cols[e.col];
         if (!boundsMeet(qb, e.b)) continue;
         std::vector<Manifold> res;
         if (!collision(colPos(c), colQ(c), colliders[c].g, pos, ori, g, res)) continue;

@@ -69,8 +69,7 @@ void World::init(const psx_scene_desc* d) {
             B.dyn = (int)dynBodies.size();
             dynBodies.push_back(b);
         }
-        B.firstCol = d->collider_start[b];
-        B.nCol = d->collider_start[b + 1] - d->collider_start[b];
+        for (int c = d->collider_start[b]; c < d->collider_start[b + 1]; ++c) B.cols.push_back(c);
         bodies.push_back(B);
     }
     for (int c = 0; c < d->n_colliders; ++c) {
@@ -78,6 +77,7 @@ void World::init(const psx_scene_desc* d) {
         int b = 0;
         while (!(d->collider_start[b] <= c && c < d->collider_start[b + 1])) ++b;
         C.body = b;
+        C.local = c - d->collider_start[b];
         C.pos = ld3(d->col_pos + 3 * c);
         C.q = ld4(d->col_quat + 4 * c);
         C.g.type = d->col_type[c];
@@ -94,8 +94,8 @@ void World::init(const psx_scene_desc* d) {
     }
     // onRigidBodyCreate (Physecs.cpp:25-37): creation bounds carry no margin
     for (int b = 0; b < (int)bodies.size(); ++b) {
-        for (int k = 0; k < bodies[b].nCol; ++k) {
-            int c = bodies[b].firstCol + k;
+        for (int k = 0; k < (int)bodies[b].cols.size(); ++k) {
+            int c = bodies[b].cols[k];
             bp.push_back({bodies[b].entity, b, k, getBounds(colPos(c), colQ(c), colliders[c].g), colliders[c].enable,
                           bodies[b].simulated()});
         }
@@ -112,7 +112,7 @@ void World::init(const psx_scene_desc* d) {
 void World::updateBounds(int b, bool margin) {
     for (auto& e : bp) {
         if (e.body != b) continue;
-        int c = bodies[b].firstCol + e.col;
+        int c = bodies[b].cols[e.col];
         e.b = getBounds(colPos(c), colQ(c), colliders[c].g);
         if (margin) { e.b.max += v3s(0.01f); e.b.min -= v3s(0.01f); }
     }
@@ -155,6 +155,42 @@ void World::destroyJoint(int j) {
     colorBits[J.body1] &= (unsigned char)~(1u << J.color);
 }
 
+// Scene::addCollider (Physecs.cpp:740-751): the entry goes last, with creation bounds
+void World::addCollider(int b, const psx_scene_desc* d) {
+    Body& B = bodies[b];
+    Collider C;
+    C.body = b;
+    C.local = (int)B.cols.size();
+    C.pos = ld3(d->col_pos);
+    C.q = ld4(d->col_quat);
+    C.g.type = d->col_type[0];
+    for (int k = 0; k < 3; ++k) C.g.p[k] = d->col_params[k];
+    if (C.g.type == CONVEX_MESH) C.g.convex = convex[d->col_mesh[0]].get();
+    if (C.g.type == TRIANGLE_MESH) C.g.tri = tri[d->col_mesh[0]].get();
+    C.friction = d->col_material[0];
+    C.restitution = d->col_material[1];
+    C.damping = d->col_material[2];
+    C.trigger = d->col_is_trigger ? d->col_is_trigger[0] != 0 : false;
+    C.enable = d->col_enable_sim ? d->col_enable_sim[0] != 0 : true;
+    C.data = d->col_data ? d->col_data[0] : 0;
+    const int c = (int)colliders.size();
+    colliders.push_back(C);
+    B.cols.push_back(c);
+    bp.push_back({B.entity, b, C.local, getBounds(colPos(c), colQ(c), colliders[c].g), C.enable, B.simulated()});
+}
+
+// Scene::clearColliders (Physecs.cpp:727-738): each entry swapped with the last and popped
+void World::clearColliders(int b) {
+    Body& B = bodies[b];
+    for (int k = 0; k < (int)B.cols.size(); ++k) {
+        size_t id = 0;
+        while (!(bp[id].body == b && bp[id].col == k)) ++id;
+        bp[id] = bp.back();
+        bp.pop_back();
+    }
+    B.cols.clear();
+}
+
 // EnTT 3.12: an entity's next version skips the reserved all-ones version
 static uint32_t nextVersion(uint32_t e) {
     uint32_t v = (e >> 20) + 1;
@@ -182,11 +218,11 @@ int World::createBody(const psx_scene_desc* d) {
         B.com = ld3(d->com);
         for (int k = 0; k < 3; ++k) B.invI.c[k] = ld3(d->inv_inertia + 3 * k);
     }
-    B.firstCol = (int)colliders.size();
-    B.nCol = d->collider_start[1] - d->collider_start[0];
     for (int c = d->collider_start[0]; c < d->collider_start[1]; ++c) {
         Collider C;
         C.body = b;
+        C.local = c - d->collider_start[0];
+        B.cols.push_back((int)colliders.size());
         C.pos = ld3(d->col_pos + 3 * c);
         C.q = ld4(d->col_quat + 4 * c);
         C.g.type = d->col_type[c];
@@ -206,8 +242,8 @@ int World::createBody(const psx_scene_desc* d) {
     // emplace<RigidBodyCollisionComponent>: onRigidBodyCreate appends the entries with
     // creation bounds (Physecs.cpp:25-37); emplace<RigidBodyDynamicComponent> then
     // appends to the dynamic storage and onDynamicCreate sets the entries' flag (:56-66)
-    for (int k = 0; k < B.nCol; ++k) {
-        const int c = B.firstCol + k;
+    for (int k = 0; k < (int)B.cols.size(); ++k) {
+        const int c = B.cols[k];
         bp.push_back({e, b, k, getBounds(colPos(c), colQ(c), colliders[c].g), colliders[c].enable, B.simulated()});
     }
     if (B.hasDyn) {
@@ -231,7 +267,7 @@ void World::destroyBody(int b) {
         B.dyn = -1;
         B.hasDyn = false;
     }
-    for (int k = 0; k < B.nCol; ++k) {
+    for (int k = 0; k < (int)B.cols.size(); ++k) {
         size_t id = 0;
         while (!(bp[id].body == b && bp[id].col == k)) ++id;
         bp[id] = bp.back();
@@ -310,7 +346,7 @@ void World::narrowphase() {
         int bA = pairs[4 * idx], cA = pairs[4 * idx + 1], bB = pairs[4 * idx + 2], cB = pairs[4 * idx + 3];
         const Body& B0 = bodies[bA];
         const Body& B1 = bodies[bB];
-        int c0 = B0.firstCol + cA, c1 = B1.firstCol + cB;
+        int c0 = B0.cols[cA], c1 = B1.cols[cB];
         const Collider& C0 = colliders[c0];
         const Collider& C1 = colliders[c1];
         V3 pos0 = B0.pos + qrot(B0.q, C0.pos);

@@ -22,7 +22,7 @@ struct Body {
     float invMass = 0;
     V3 com{0, 0, 0};
     M3 invI{};
-    int firstCol = 0, nCol = 0;
+    std::vector<int> cols;      // its colliders' indices, in RigidBodyCollisionComponent order
     int dyn = -1;               // position in dynamic storage (src/Physecs.cpp:271)
     bool alive = true;          // false once its entity is destroyed
     bool simulated() const { return hasDyn && !kinematic; }
@@ -30,6 +30,7 @@ struct Body {
 
 struct Collider {
     int body;
+    int local;                  // index within its body's RigidBodyCollisionComponent
     V3 pos; Q4 q;
     Geometry g;
     float friction, restitution, damping;
@@ -160,6 +161,10 @@ struct World {
     // world's); returns the new body's index.  registry.destroy of a body's entity.
     int createBody(const psx_scene_desc* d);
     void destroyBody(int b);
+    // Scene::addCollider (collider 0 of d; meshes are this world's) / clearColliders
+    // (Physecs.cpp:727-751) for body b
+    void addCollider(int b, const psx_scene_desc* d);
+    void clearColliders(int b);
     // Scene::createJoint / destroyJoint (Physecs.cpp:690-725) for a psx joint record
     int createJoint(int type, int b0, int b1, const float* frames, const float* params);
     void destroyJoint(int j);

@@ -54,6 +54,8 @@ def lib():
         _lib.orc_scene_apply_deltas.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
         _lib.orc_scene_create_body.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.orc_scene_destroy_body.argtypes = [C.c_void_p, C.c_int]
+        _lib.orc_scene_add_collider.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        _lib.orc_scene_clear_colliders.argtypes = [C.c_void_p, C.c_int]
         _lib.orc_scene_create_joint.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
         _lib.orc_scene_destroy_joint.argtypes = [C.c_void_p, C.c_int]
         _lib.orc_scene_set_contact_filter.argtypes = [C.c_void_p, C.c_void_p]
@@ -201,6 +203,17 @@ class OracleScene:
     def destroy_joint(self, j):
         """Scene::destroyJoint of joint j."""
         lib().orc_scene_destroy_joint(self.h, int(j))
+
+    def add_collider(self, body, collider_scene):
+        """Scene::addCollider: the first collider of `collider_scene` (a SceneData; its
+        mesh indices refer to this scene's meshes) joins body `body`."""
+        from physecs_gb300.desc import make_desc
+        d = make_desc(collider_scene)
+        lib().orc_scene_add_collider(self.h, int(body), C.byref(d))
+
+    def clear_colliders(self, body):
+        """Scene::clearColliders of body `body`."""
+        lib().orc_scene_clear_colliders(self.h, int(body))
 
     def destroy_body(self, b):
         """registry.destroy of body b's entity; its state then reads as zeros."""

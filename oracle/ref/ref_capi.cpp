@@ -255,6 +255,17 @@ void ref_scene_destroy_joint(void* h, int j) {
     w->joints[j] = nullptr;
 }
 
+// Scene::addCollider(entity of body b, collider 0 of d) / Scene::clearColliders
+void ref_scene_add_collider(void* h, int b, const psx_scene_desc* d) {
+    auto* w = static_cast<RefWorld*>(h);
+    w->scene->addCollider(w->entities[b], make_collider(*w, d, 0));
+}
+
+void ref_scene_clear_colliders(void* h, int b) {
+    auto* w = static_cast<RefWorld*>(h);
+    w->scene->clearColliders(w->entities[b]);
+}
+
 // registry.destroy of body b's entity
 void ref_scene_destroy_body(void* h, int b) {
     auto* w = static_cast<RefWorld*>(h);

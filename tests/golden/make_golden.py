@@ -338,6 +338,38 @@ def joint_topology_case():
     return s, plan, fr, 50
 
 
+def _collider_scene(typ, prm, pos=(0.0, 0.0, 0.0)):
+    s = scenes.SceneData("collider")
+    s.add_bodies(pos=[[0.0, 0.0, 0.0]], quat=[scenes.IDENTITY_Q], flags=0, inv_mass=0.0, com=np.zeros(3),
+                 inv_inertia=np.zeros(9), col_type=typ, col_params=prm, col_pos=list(pos))
+    return s.finalize()
+
+
+def collider_topology_case():
+    """(scene, plan {frame: [("clear", body) | ("add", body, collider SceneData)]}, frames):
+    colliders cleared from and added to dynamic and static bodies between frames."""
+    s = scenes.batch_scene(14, n_bodies=50, chain_prob=0.0)
+    dyn = [int(b) for b in np.nonzero(s.arrays["flags"] & scenes.BODY_DYNAMIC)[0]]
+    plan = {5: [("clear", dyn[0])],
+            9: [("add", dyn[1], _collider_scene(scenes.SPHERE, [0.3, 0, 0, 0], (0.4, 0, 0)))],
+            14: [("add", dyn[0], _collider_scene(scenes.BOX, [0.3, 0.3, 0.3, 0]))],
+            20: [("add", 0, _collider_scene(scenes.BOX, [1.0, 0.2, 1.0, 0], (0, 1.0, 0))), ("clear", dyn[2])],
+            26: [("add", dyn[2], _collider_scene(scenes.CAPSULE, [0.3, 0.2, 0, 0])),
+                 ("add", dyn[2], _collider_scene(scenes.SPHERE, [0.2, 0, 0, 0], (0, 0.5, 0)))]}
+    return s, plan, 50
+
+
+def run_collider_plan(sim, plan, frames):
+    for f in range(frames):
+        for act in plan.get(f, []):
+            if act[0] == "clear":
+                sim.clear_colliders(act[1])
+            else:
+                sim.add_collider(act[1], act[2])
+        sim.step()
+    return sim.state()
+
+
 def run_joint_plan(sim, plan, fr, frames):
     for f in range(frames):
         if f in plan:
@@ -359,6 +391,10 @@ def topology_fixture():
     out["joints_scene_sha256"] = np.array(scene_hash(js))
     for k, v in run_joint_plan(RefScene(js), plan, fr, jframes).items():
         out["joints_f%d_%s" % (jframes, k)] = v
+    cs, cplan, cframes = collider_topology_case()
+    out["colliders_scene_sha256"] = np.array(scene_hash(cs))
+    for k, v in run_collider_plan(RefScene(cs), cplan, cframes).items():
+        out["colliders_f%d_%s" % (cframes, k)] = v
     ents = []
     for f in range(frames):
         if f in sch:

@@ -73,3 +73,15 @@ def test_oracle_joint_topology_matches_reference_fixture(oracle_lib):
     st = make_golden.run_joint_plan(OracleScene(s), plan, fr, frames)
     for k, v in st.items():
         assert np.array_equal(v.view(np.uint32), d["joints_f%d_%s" % (frames, k)].view(np.uint32)), k
+
+
+def test_oracle_collider_topology_matches_reference_fixture(oracle_lib):
+    """Scene::addCollider / clearColliders between frames (src/Physecs.cpp:727-751): the
+    new entry goes last with creation bounds; clearing swaps each entry out."""
+    from oracle.port_api import OracleScene
+    d = np.load(os.path.join(HERE, "golden", "topology.npz"))
+    s, plan, frames = make_golden.collider_topology_case()
+    assert str(d["colliders_scene_sha256"]) == make_golden.scene_hash(s)
+    st = make_golden.run_collider_plan(OracleScene(s), plan, frames)
+    for k, v in st.items():
+        assert np.array_equal(v.view(np.uint32), d["colliders_f%d_%s" % (frames, k)].view(np.uint32)), k
