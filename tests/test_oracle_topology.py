@@ -85,3 +85,36 @@ def test_oracle_collider_topology_matches_reference_fixture(oracle_lib):
     st = make_golden.run_collider_plan(OracleScene(s), plan, frames)
     for k, v in st.items():
         assert np.array_equal(v.view(np.uint32), d["colliders_f%d_%s" % (frames, k)].view(np.uint32)), k
+
+
+def test_trigger_events_across_entity_changes_match_live_reference(oracle_lib):
+    """Trigger bodies destroyed (their overlapping pairs exit) and trigger bodies created
+    (their pairs enter) between frames give the reference's events."""
+    from oracle.ref import ref_api
+    if not ref_api.available():
+        pytest.skip("reference library not built here")
+    from oracle.port_api import OracleScene
+    from oracle.ref.ref_api import RefScene
+    from scene_variants import spawn_body, trigger_scene
+    s = trigger_scene(41)
+    a = s.arrays
+    trig = [b for b in range(5, 95) if a["col_is_trigger"][a["collider_start"][b]]]
+    rng = np.random.default_rng(2)
+    sims = [OracleScene(s), RefScene(s)]
+    for f in range(80):
+        if f in (20, 40):
+            b = trig.pop(0)
+            for sim in sims:
+                sim.destroy_body(b)
+        if f in (30, 50):
+            sp = spawn_body(rng, [0.0, 7.0, 0.0])
+            sp.arrays["col_is_trigger"][:] = 1
+            for sim in sims:
+                sim.create_body(sp)
+        for sim in sims:
+            sim.step()
+    eo, er = (make_golden.events_sorted(sim.trigger_events()) for sim in sims)
+    assert len(eo) > 100 and np.array_equal(eo, er)
+    so, sr = sims[0].state(), sims[1].state()
+    for k in so:
+        assert np.array_equal(so[k].view(np.uint32), sr[k].view(np.uint32)), k
