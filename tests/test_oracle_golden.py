@@ -158,3 +158,32 @@ def test_oracle_matches_live_reference(oracle_lib, seed, n, chain):
         a, b = o.state(), r.state()
         for k in a:
             np.testing.assert_array_equal(a[k], b[k], err_msg="frame %d %s" % (f, k))
+
+
+def test_oracle_contact_order_keys_round_trip(oracle_lib):
+    """The ordering hook the GPU lockstep tests use: a frame's contact keys (entity,
+    collider within the body, triangle) fed to a second oracle at the same state all
+    match, in any order; a key that names no contact is counted, and so is the contact
+    it leaves without a key."""
+    from oracle.port_api import OracleScene
+    s = scenes.batch_scene(8, n_bodies=80, chain_prob=1.0)
+    a = OracleScene(s)
+    for _ in range(3):
+        a.step()
+    keys = a.contact_keys()
+    assert len(keys) > 20
+    for order in (keys, keys[::-1]):
+        b = OracleScene(s)
+        for _ in range(2):
+            b.step()
+        b.set_contact_order(order)
+        b.step()
+        assert b.order_error() == 0
+    bad = keys.copy()
+    bad[0, 1] += 100
+    c = OracleScene(s)
+    for _ in range(2):
+        c.step()
+    c.set_contact_order(bad)
+    c.step()
+    assert c.order_error() == 2
