@@ -149,11 +149,27 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def workload_config(name, n_scenes):
+def frame_window(args):
+    """The frames of the batched workload that are timed: every arm first runs --warmup
+    frames and --e2e-steps frames untimed (the GPU arm's end-to-end leg), then times
+    --steps frames of every scene."""
+    first = args.warmup + args.e2e_steps + 1
+    return first, first + args.steps - 1
+
+
+def workload_config(name, n_scenes, args=None):
+    """The workload's description.  The GPU arm and the reference arm print the same
+    dict for the batched workload: same scenes, same timed frames."""
     if name == "batched":
-        return {"workload": "batched: %d independent scenes per GPU, N log-uniform in [16,2048] bodies, "
-                            "box/sphere/capsule/hull 40/30/20/10 on a ground box, 10%% with an 8-link revolute chain, "
-                            "dt=1/60 s, 4 substeps, 8 iterations" % n_scenes, "scenes": n_scenes}
+        cfg = {"workload": "batched: %d independent scenes per GPU, N log-uniform in [16,2048] bodies, "
+                           "box/sphere/capsule/hull 40/30/20/10 on a ground box, 10%% with an 8-link revolute chain, "
+                           "dt=1/60 s, 4 substeps, 8 iterations" % n_scenes, "scenes": n_scenes,
+               "hulls": "8 seeded 16-point hulls shared by the scenes' hull bodies, each scaled U[0.5,1.5]",
+               "l2": "working set larger than L2 (no flush)"}
+        if args is not None:
+            a, b = frame_window(args)
+            cfg["timed_frames"] = "frames %d-%d of every scene, after %d untimed frames" % (a, b, a - 1)
+        return cfg
     if name == "large":
         return {"workload": "large single scene: 65536 mixed bodies over a 256x256-cell heightfield, dt=1/60, 4x8",
                 "scenes": 1}
@@ -163,18 +179,24 @@ def workload_config(name, n_scenes):
     return {"workload": "20-row box pyramid (210 cubes) on a ground box, dt=1/60, 4x8", "scenes": 1}
 
 
-def build_workload(name, rank, n_scenes):
+def build_workload(name, rank, n_scenes, args=None, world=1):
+    """The scenes of `rank`.  Batched: the workload is world x n_scenes seeded scenes,
+    split over the ranks by body count (physecs_gb300.shard), so each GPU holds about
+    n_scenes scenes' worth of bodies whatever the number of GPUs (weak scaling)."""
     from physecs_gb300 import scenes
     if name == "batched":
+        from physecs_gb300.shard import partition
+        ids = list(range(world * n_scenes))
+        part = partition([scenes.batch_scene_bodies(i) for i in ids], world)[rank] if world > 1 else ids
         pool = scenes._hull_pool(scenes.SplitMix64(scenes.scene_seed(4, 1 << 19)), count=8)
-        ss = [scenes.batch_scene(rank * n_scenes + i, pool=pool) for i in range(n_scenes)]
+        ss = [scenes.batch_scene(i, pool=pool) for i in part]
     elif name == "large":
         ss = [scenes.large_mixed()]
     elif name == "chains":
         ss = [scenes.joint_chains()]
     else:
         ss = [scenes.pyramid()]
-    return ss, workload_config(name, n_scenes)
+    return ss, workload_config(name, n_scenes, args)
 
 
 def simulated_bodies(ss):
@@ -183,40 +205,66 @@ def simulated_bodies(ss):
 
 # ---------------------------------------------------------------- CPU side
 
-def _cpu_worker(args):
-    """Oracle (CPU restatement) on a subset of scenes: returns (seconds, body-substeps)."""
-    kind, specs, frames, warm = args
+def _cpu_proc(kind, scene_ids, warm, frames, barrier, conn):
+    """One host core: the CPU implementation on its share of the batched scenes.  Builds
+    its scenes, runs the untimed frames, waits for every other core, then times
+    `frames` frames.  Sends (seconds, body-substeps)."""
     sys.path.insert(0, ROOT)
-    from physecs_gb300 import scenes
-    if kind == "reference":
-        from oracle.ref.ref_api import RefScene as Sim
-    else:
-        from oracle.port_api import OracleScene as Sim
-    pool = scenes._hull_pool(scenes.SplitMix64(scenes.scene_seed(4, 1 << 19)), count=8)
-    sims, work = [], 0
-    for idx in specs:
-        s = scenes.batch_scene(idx, pool=pool)
-        sims.append(Sim(s))
-        work += s.n_dynamic * s.num_substeps
-    for sim in sims:
-        sim.step(DT, warm)
+    try:
+        from physecs_gb300 import scenes
+        if kind == "reference":
+            from oracle.ref.ref_api import RefScene as Sim
+        else:
+            from oracle.port_api import OracleScene as Sim
+        pool = scenes._hull_pool(scenes.SplitMix64(scenes.scene_seed(4, 1 << 19)), count=8)
+        sims, work = [], 0
+        for idx in scene_ids:
+            s = scenes.batch_scene(idx, pool=pool)
+            sims.append(Sim(s))
+            work += s.n_dynamic * s.num_substeps
+        for sim in sims:
+            sim.step(DT, warm)
+    except BaseException:
+        barrier.abort()
+        raise
+    barrier.wait()
     t = time.perf_counter()
     for sim in sims:
         sim.step(DT, frames)
-    return time.perf_counter() - t, work * frames
+    conn.send((time.perf_counter() - t, work * frames))
+    conn.close()
 
 
-def cpu_throughput(kind, scene_ids, frames, warm, procs):
-    """body-substeps/s of the CPU implementation over `scene_ids`, using `procs` processes."""
+def cpu_throughput(kind, scene_ids, warm, frames, procs):
+    """body-substeps/s of the CPU implementation over the batched scenes `scene_ids`:
+    `warm` untimed frames, then `frames` timed frames, on `procs` spawned processes (one
+    per host core, numThreads = 0 in each) whose timed regions start together.  Scenes
+    are assigned longest first to the least loaded process (by body count).  Returns
+    (value, slowest process's timed seconds, processes used)."""
+    import heapq
     import multiprocessing as mp
-    chunks = [scene_ids[i::procs] for i in range(procs)]
-    chunks = [c for c in chunks if c]
-    if len(chunks) == 1:
-        t, work = _cpu_worker((kind, chunks[0], frames, warm))
-        return work / t, t, 1
+    from physecs_gb300 import scenes
+    procs = max(1, min(procs, len(scene_ids)))
+    sizes = sorted(((scenes.batch_scene_bodies(i), i) for i in scene_ids), reverse=True)
+    heap = [(0, k) for k in range(procs)]
+    chunks = [[] for _ in range(procs)]
+    for n, i in sizes:
+        load, k = heapq.heappop(heap)
+        chunks[k].append(i)
+        heapq.heappush(heap, (load + n, k))
+    chunks = [sorted(c) for c in chunks if c]
     ctx = mp.get_context("spawn")
-    with ctx.Pool(len(chunks)) as pool:
-        res = pool.map(_cpu_worker, [(kind, c, frames, warm) for c in chunks])
+    barrier = ctx.Barrier(len(chunks))
+    conns, ps = [], []
+    for c in chunks:
+        parent, child = ctx.Pipe(duplex=False)
+        p = ctx.Process(target=_cpu_proc, args=(kind, c, warm, frames, barrier, child))
+        p.start()
+        conns.append(parent)
+        ps.append(p)
+    res = [c.recv() for c in conns]
+    for p in ps:
+        p.join()
     wall = max(r[0] for r in res)
     work = sum(r[1] for r in res)
     return work / wall, wall, len(chunks)
@@ -352,7 +400,12 @@ def run_serving(args, rank, world, local):
     from physecs_gb300.api import Server
     small = args.serve_max_bodies <= 1000
     classes = (SERVE_CLASSES_SLO if args.serve_slo else SERVE_CLASSES_SMALL) if small else SERVE_CLASSES
-    reqs, pool_scene = serving_requests(384, rank, n_max=args.serve_max_bodies)
+    reqs, pool_scene = serving_requests(384 * world, 0, n_max=args.serve_max_bodies)
+    if world > 1:
+        # one request stream for every GPU's server, split by a deterministic router
+        from physecs_gb300.shard import Router
+        router = Router(world)
+        reqs = [r for r in reqs if router.route(r[0].n_dynamic * r[1]) == rank]
     from physecs_gb300.desc import make_desc
     descs = [make_desc(s) for s, _ in reqs]          # the clients' packed requests
     srv = Server(classes, mesh_pool=pool_scene, device=local if world > 1 else 0, hbm_budget=SERVE_HBM_BUDGET,
@@ -407,8 +460,8 @@ def main():
     ap.add_argument("--scenes", type=int, default=4096)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--plain-scenes", type=int, default=64)
-    ap.add_argument("--cpu-scenes", type=int, default=256)
-    ap.add_argument("--cpu-frames", type=int, default=20)
+    ap.add_argument("--cpu-stride", type=int, default=8, help="cpu_baseline: every n-th scene of the workload")
+    ap.add_argument("--eager", action="store_true", help="launch every frame's kernels instead of a CUDA graph")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="keep the default kernel launch shapes")
     args = ap.parse_args()
@@ -426,24 +479,24 @@ def main():
 
     dist = Dist(world, local)
     from physecs_gb300.api import World
-    ss, cfg = build_workload(args.workload, rank, args.scenes)
+    ss, cfg = build_workload(args.workload, rank, args.scenes, args, world)
     n_sim = simulated_bodies(ss)
     substeps = ss[0].num_substeps
     dev = local if world > 1 else 0
-    w = World(ss, device=dev)
+    use_graph = not args.eager      # the frame is captured once and replayed as a CUDA graph
+    launch = None
     if not args.no_tune and len(ss) > 1:
         # warm-up includes the autotuner: it picks launch shapes on a throwaway world's
         # frames, and the measured world is created afresh with them
+        w = World(ss, device=dev)
         launch = w.tune(frames=2)
         w.close()
-        w = World(ss, device=dev, launch=launch)
-        cfg = dict(cfg)
-        cfg["launch"] = launch
+    w = World(ss, device=dev, launch=launch, use_graph=use_graph)
     for _ in range(args.warmup):
         w.step(DT)
     w.synchronize()
     # end to end through the public call, host arrays in and out every step; run ahead of
-    # the device-timed frames, so on the earlier (heavier) frames of the same scenes
+    # the device-timed frames, so on the earlier frames of the same scenes
     e2e_value = None
     if args.e2e_steps > 0:
         from physecs_gb300.api import pin_host, unpin_host
@@ -457,7 +510,6 @@ def main():
         unpin_host(*st.values())
         e2e_s = dist.max(e2e_s)
         e2e_value = dist.sum(n_sim * substeps) / e2e_s
-    counts = w.counts()
     dist.barrier()
     with ClockSampler(local) as clk:
         total_ms, stage_ms, kernels = w.step_timed(DT, args.steps)
@@ -469,7 +521,7 @@ def main():
     if counts["error"]:
         raise RuntimeError("device error bits %d" % counts["error"])
 
-    # roofline of the dominant kernel: the solver (one launch per frame covers every substep)
+    # roofline of the solver (one launch per frame covers every substep)
     pts, rows = counts["points"], counts["rows"]
     alg_bytes = substeps * (156.0 * n_sim + 52.0 * pts + 76.0 * rows)
     solver_s = stage_ms[3] / 1000.0 / args.steps
@@ -488,11 +540,12 @@ def main():
     nb = w.n_bodies
     h2d = 4 * (3 + 4 + 3 + 3) * nb
 
-    # the plain path: the same scenes, one world per scene, stepped one scene at a time
+    # the plain path: the same scenes, one world per scene (each replaying its own frame
+    # graph), stepped one scene at a time
     plain = None
     if args.workload == "batched" and args.plain_scenes > 0 and rank == 0:
         sub = ss[:args.plain_scenes]
-        ws = [World([s]) for s in sub]
+        ws = [World([s], use_graph=use_graph) for s in sub]
         for x in ws:
             x.step(DT, 3)
         for x in ws:
@@ -500,8 +553,7 @@ def main():
         t0 = time.perf_counter()
         frames = 3
         for x in ws:
-            for _ in range(frames):
-                x.step(DT)
+            x.step(DT, frames)
             x.synchronize()
         pt = time.perf_counter() - t0
         plain = simulated_bodies(sub) * substeps * frames / pt
@@ -509,16 +561,19 @@ def main():
             x.close()
 
     cpu = None
-    if rank == 0 and not args.no_cpu and args.workload == "batched":
+    first, last = frame_window(args)
+    if rank == 0 and world == 1 and not args.no_cpu and args.workload == "batched":
         try:
             # the reference built from its own sources when available, else the oracle port;
-            # one spawned process per host core, each scene with numThreads = 0
+            # one spawned process per host core, each scene with numThreads = 0; a uniform
+            # sample of the scenes over the same frames as the GPU arm
             kind = cpu_kind()
-            ids = list(range(args.cpu_scenes))
-            v, wall, procs = cpu_throughput(kind, ids, args.cpu_frames, 2, max(1, os.cpu_count() or 1))
+            ids = list(range(0, args.scenes, args.cpu_stride))
+            v, wall, procs = cpu_throughput(kind, ids, first - 1, args.steps, max(1, os.cpu_count() or 1))
             cpu = {"value": v, "unit": METRIC, "cores": procs, "kind": kind,
-                   "sample": "%d of the batched scenes x %d frames, one process per core (%.1f s per process)" %
-                             (len(ids), args.cpu_frames, wall)}
+                   "sample": "every %d-th of the %d scenes (%d scenes), frames %d-%d after %d untimed, one process "
+                             "per core (%.1f s timed per process)" % (args.cpu_stride, args.scenes, len(ids), first, last,
+                                                                      first - 1, wall)}
         except Exception as e:  # the baseline is reported, never required
             cpu = {"value": None, "unit": METRIC, "cores": 0, "kind": "port", "sample": "failed: %s" % e}
 
@@ -529,9 +584,12 @@ def main():
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 in GJK/EPA)",
             "data": "synthetic (seeded SplitMix64 scenes)",
-            "config": dict(cfg, parallelism="scene shards" if world > 1 else "single GPU",
-                           l2="working set larger than L2 (no flush)", simulated_bodies=n_sim,
-                           contact_points=pts, joint_rows=rows, pairs=counts["pairs"], manifolds=counts["manifolds"]),
+            "config": cfg,
+            "parallelism": ("scene shards over %d GPUs (body-balanced)" % world) if world > 1 else "single GPU",
+            "frame": "CUDA graph replay" if use_graph else "eager launches",
+            "launch": launch,
+            "counts": {"simulated_bodies": n_sim, "contact_points": pts, "joint_rows": rows, "pairs": counts["pairs"],
+                       "manifolds": counts["manifolds"]},
             "stage_ms_per_step": {k: v / args.steps for k, v in zip(
                 ["broadphase", "narrowphase", "contact_joint_rows", "solver", "bounds"], stage_ms)},
             "roofline": {"kernel": "k_solve_block (solver, all substeps of a frame)", "bound": "hbm",
@@ -624,8 +682,7 @@ def run_registry(args, rank):
     Beside them, the reference doing the same through its registry and its
     CharacterController, one scene after another on one host core, on a sample."""
     import numpy as np
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    from scene_variants import character_moves, character_scene
+    from physecs_gb300.scenes import character_moves, character_scene
     from physecs_gb300.api import World, pack_deltas
     if rank != 0:
         return 0
@@ -705,26 +762,30 @@ def run_registry(args, rank):
 
 
 def run_reference(args, rank, world):
-    """The reference's own CPU implementation on the host cores, same metric and workload."""
+    """The reference's own CPU implementation (built from its sources; the oracle port
+    where it is absent) on the host cores: the GPU arm's workload and frame window, every
+    scene, one process per host core.  Under torchrun only rank 0 runs."""
     if rank != 0:
+        return 0
+    if args.workload != "batched":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference arm runs the batched workload only"}))
         return 0
     kind = cpu_kind()
     procs = max(1, os.cpu_count() or 1)
-    ids = list(range(min(args.scenes, 16 * procs)))
-    vals = []
-    for _ in range(max(1, args.steps // 10)):
-        v, wall, used = cpu_throughput(kind, ids, 10, 2, procs)
-        vals.append(v)
-    value = statistics.median(vals)
-    cfg = dict(workload_config("batched", args.scenes))
-    cfg["sample"] = "%d of the scenes x 10 frames per step" % len(ids)
+    first, last = frame_window(args)
+    ids = list(range(args.scenes))
+    t0 = time.perf_counter()
+    value, wall, used = cpu_throughput(kind, ids, first - 1, args.steps, procs)
+    total_s = time.perf_counter() - t0
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "impl": "reference",
-        "data": "synthetic (seeded SplitMix64 scenes)",
-        "config": cfg,
+        "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "impl": "reference", "data": "synthetic (seeded SplitMix64 scenes)",
+        "config": workload_config("batched", args.scenes, args),
+        "parallelism": "%d host cores, one process per core (numThreads=0 each), scenes assigned by body count" % used,
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": used, "kind": kind,
-                         "sample": "%d scenes x 10 frames, one process per host core (numThreads=0 each)" % len(ids)},
+                         "sample": "all %d scenes, frames %d-%d after %d untimed frames (%.0f s in all)"
+                                   % (args.scenes, first, last, first - 1, total_s)},
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))

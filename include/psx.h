@@ -194,11 +194,22 @@ PSX_API psx_status psx_world_destroy(psx_world* w);
 PSX_API psx_status psx_world_step(psx_world* w, float dt, int32_t frames);
 /* Like psx_world_step, timed on the world's stream with CUDA events: total_ms for all
  * frames, stage_ms[5] = {broadphase, narrowphase, contact + joint rows, solver,
- * end-of-frame bounds} summed over the frames, kernels = kernels queued.  Waits. */
+ * end-of-frame bounds} summed over the frames, kernels = kernels queued.  Waits.
+ * A world created with use_graph replays its frame graph here as in psx_world_step;
+ * total_ms then spans the replays.  stage_ms (when not NULL) then comes from one more
+ * frame, launched eagerly after the timed ones and not counted in total_ms or kernels:
+ * its stage times, each multiplied by `frames`. */
 PSX_API psx_status psx_world_step_timed(psx_world* w, float dt, int32_t frames, float* total_ms, float* stage_ms,
                                         int64_t* kernels);
 /* Waits for queued work and reports a device-side error (capacity, timeout). */
 PSX_API psx_status psx_world_synchronize(psx_world* w);
+/* The reference has no device waits.  Here a scene above the block limit that is solved
+ * by the whole grid (a cooperative launch) waits at a grid barrier between colour steps.
+ * Each wait polls at most `polls` times, 64 ns apart (0: the default, 2^23 polls, about
+ * half a second), then gives up: every block leaves the solver, the frame's results are
+ * not valid, and psx_world_synchronize returns PSX_ERR_TIMEOUT.  Takes effect from the
+ * next frame. */
+PSX_API psx_status psx_world_set_wait_limit(psx_world* w, int64_t polls);
 /* Scene::setNumSubSteps / setNumIterations / setGravity (src/Physecs.cpp:100-110) for one scene (-1: all). */
 PSX_API psx_status psx_world_set_knobs(psx_world* w, int32_t scene, int32_t substeps, int32_t iterations, float gravity);
 /* Copy every body's TransformComponent and velocities out of / into device memory
@@ -230,6 +241,14 @@ PSX_API psx_status psx_world_simulate_host(psx_world* w, float dt, float* pos, f
 PSX_API psx_status psx_world_tune(psx_world* w, int32_t frames, psx_launch_config* best);
 /* The launch shapes in effect (after defaults, tuning or opts.launch). */
 PSX_API psx_status psx_world_launch_config(psx_world* w, psx_launch_config* out);
+
+/* The setters of the joint classes (RevoluteJoint::setDriveEnabled / setDriveVelocity /
+ * setDriveMaxTorque, PrismaticJoint::setUpperLimit ... setDriveDamping, GearJoint::
+ * setGearRatio, ServoJoint::setTargetAngle ... setDriveDamping; include/Physecs/Joints/
+ * *.h) between frames: the whole PSX_JOINT_PARAMS block of joint `joint` (index within
+ * the scene's joints, in creation order) is replaced, ahead of the next frame.  A gear
+ * joint keeps its accumulated angles. */
+PSX_API psx_status psx_world_set_joint_params(psx_world* w, int32_t scene, int32_t joint, const float* params);
 
 /* ---- filters of the narrowphase */
 #define PSX_CONTACT_COLLISION 0

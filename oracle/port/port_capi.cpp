@@ -269,6 +269,13 @@ int orc_scene_create_joint(void* h, int type, int b0, int b1, const float* frame
 
 void orc_scene_destroy_joint(void* h, int j) { static_cast<World*>(h)->destroyJoint(j); }
 
+// The joint classes' setters between frames (RevoluteJoint::setDriveEnabled ...,
+// include/Physecs/Joints/*.h): joint j's parameter block is replaced; a gear joint keeps
+// its accumulated angles (GearJoint.h:10-17).
+void orc_scene_set_joint_params(void* h, int j, const float* p) {
+    std::memcpy(static_cast<World*>(h)->joints[j].params, p, sizeof(float) * PSX_JOINT_PARAMS);
+}
+
 // A batch of registry deltas in array order (psx_body_delta; the scene field is unused)
 void orc_scene_apply_deltas(void* h, int n, const psx_body_delta* d) {
     World* w = static_cast<World*>(h);

@@ -48,6 +48,7 @@ def lib():
         _lib.ref_scene_clear_colliders.argtypes = [C.c_void_p, C.c_int]
         _lib.ref_scene_create_joint.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
         _lib.ref_scene_destroy_joint.argtypes = [C.c_void_p, C.c_int]
+        _lib.ref_scene_set_joint_params.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
         _lib.ref_scene_set_contact_filter.argtypes = [C.c_void_p, C.c_void_p]
         _lib.ref_scene_set_can_collide.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
         _lib.ref_character_move.argtypes = [C.c_void_p, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int,
@@ -191,6 +192,13 @@ class RefScene:
         f = np.ascontiguousarray(frames, np.float32).ravel()
         p = np.zeros(8, np.float32) if params is None else np.ascontiguousarray(params, np.float32).ravel()
         return lib().ref_scene_create_joint(self.h, int(jtype), int(body0), int(body1), _p(f), _p(p))
+
+    def set_joint_params(self, j, params):
+        """The setters of joint j's class (RevoluteJoint::setDriveEnabled ...) with an
+        8-float parameter block."""
+        p = np.zeros(8, np.float32)
+        p[:len(params)] = params
+        lib().ref_scene_set_joint_params(self.h, int(j), _p(p))
 
     def destroy_joint(self, j):
         """Scene::destroyJoint of joint j."""

@@ -248,6 +248,22 @@ int ref_scene_create_joint(void* h, int type, int b0, int b1, const float* frame
     return (int)w->joints.size() - 1;
 }
 
+// The setters of joint j's class with a psx parameter block, as make_joint applies them
+void ref_scene_set_joint_params(void* h, int j, const float* p) {
+    auto* w = static_cast<RefWorld*>(h);
+    physecs::Joint* jt = w->joints[j];
+    if (auto* r = dynamic_cast<physecs::RevoluteJoint*>(jt)) {
+        r->setDriveEnabled(p[0] != 0.f); r->setDriveVelocity(p[1]); r->setDriveMaxTorque(p[2]);
+    } else if (auto* r = dynamic_cast<physecs::PrismaticJoint*>(jt)) {
+        r->setUpperLimit(p[0]); r->setLowerLimit(p[1]); r->setDriveEnabled(p[2] != 0.f);
+        r->setTargetPosition(p[3]); r->setDriveStiffness(p[4]); r->setDriveDamping(p[5]);
+    } else if (auto* r = dynamic_cast<physecs::GearJoint*>(jt)) {
+        r->setGearRatio(p[0]);
+    } else if (auto* r = dynamic_cast<physecs::ServoJoint*>(jt)) {
+        r->setTargetAngle(p[0]); r->setDriveStiffness(p[1]); r->setDriveDamping(p[2]);
+    }
+}
+
 // Scene::destroyJoint of joint j
 void ref_scene_destroy_joint(void* h, int j) {
     auto* w = static_cast<RefWorld*>(h);

@@ -30,7 +30,8 @@ EXPORTS = ["psx_world_create", "psx_world_destroy", "psx_world_step", "psx_world
            "psx_world_tune", "psx_world_launch_config", "psx_world_raycast", "psx_world_overlap",
            "psx_world_overlap_mtd", "psx_world_trigger_events", "psx_trimesh_build", "psx_world_update_trimesh",
            "psx_world_apply_deltas", "psx_world_move_characters", "psx_world_set_contact_filter",
-           "psx_world_set_can_collide", "psx_pin_host", "psx_unpin_host"]
+           "psx_world_set_can_collide", "psx_pin_host", "psx_unpin_host", "psx_world_set_wait_limit",
+           "psx_world_set_joint_params"]
 
 _lib = None
 
@@ -75,6 +76,8 @@ def load():
     lib.psx_world_destroy.argtypes = [vp]
     lib.psx_world_step.argtypes = [vp, C.c_float, C.c_int32]
     lib.psx_world_synchronize.argtypes = [vp]
+    lib.psx_world_set_wait_limit.argtypes = [vp, C.c_int64]
+    lib.psx_world_set_joint_params.argtypes = [vp, C.c_int32, C.c_int32, vp]
     lib.psx_world_set_knobs.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_float]
     lib.psx_world_read_bodies.argtypes = [vp, vp, vp, vp, vp]
     lib.psx_world_write_bodies.argtypes = [vp, vp, vp, vp, vp]
@@ -178,6 +181,17 @@ class World:
 
     def synchronize(self):
         _check(load().psx_world_synchronize(self.h))
+
+    def set_joint_params(self, joint, params, scene=0):
+        """psx_world_set_joint_params: the 8-float parameter block of a scene's joint."""
+        p = np.zeros(8, np.float32)
+        p[:len(params)] = params
+        _check(load().psx_world_set_joint_params(self.h, scene, joint, _p(p)))
+
+    def set_wait_limit(self, polls):
+        """psx_world_set_wait_limit: polls of a grid-barrier wait before it gives up
+        (0: the default, about half a second)."""
+        _check(load().psx_world_set_wait_limit(self.h, int(polls)))
 
     def tune(self, frames=2):
         """psx_world_tune: pick the kernels' launch shapes on this world's frames (they

@@ -162,6 +162,7 @@ struct SolverLaunch {
     const int* grid; int n_grid; int grid_blocks;
     cudaStream_t aux;
     cudaEvent_t fork, join;
+    long long wait_limit;                  // polls of a grid-barrier wait (0: kDefaultWaitPolls)
 };
 int launch_solver(const World& w, FrameBuf& f, const SolverLaunch& L, cudaStream_t s);
 int solver_grid_blocks();

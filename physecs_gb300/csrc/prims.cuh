@@ -19,34 +19,54 @@ void scan_exclusive_dev(const int* in, int* out, const int* n_dev, int n_max, in
 size_t radix_hist_ints(int n);
 int radix_sort_pairs(uint32_t* keys, int* vals, uint32_t* tmpk, int* tmpv, int n, int bits, int* hist, cudaStream_t s);
 
-// Grid-wide barrier for cooperative launches.  Every block calls it; the wait is
-// bounded: after ~0.5 s without progress the barrier records ERR_BARRIER_TIMEOUT in
-// *err and lets the caller continue so the kernel always terminates.
+// Bit of the device error word that a grid barrier whose wait ran out sets.
+constexpr int kBarrierTimeoutBit = 1 << 5;
+// Polls of a grid barrier's wait before it gives up (64 ns apart: about half a second).
+constexpr long long kDefaultWaitPolls = 1ll << 23;
+
+// Grid-wide barrier for cooperative launches.  Every block calls it.  The wait is
+// bounded: a block that polls more than `limit` times records kBarrierTimeoutBit in
+// *err.  A block that finds the bit set, because its own wait ran out or another
+// block's did, leaves the kernel at once instead of arriving.  So no block runs past
+// a barrier that the grid did not complete, and after a timeout every block ends
+// within one more bounded wait.  A kernel that uses it must leave nothing behind that
+// a later launch relies on besides *err; the barrier words themselves are reset
+// before each launch.
 struct GridBarrier {
     unsigned int* count;
     unsigned int* gen;
     int* err;
+    long long limit;
     __device__ __forceinline__ void sync() const {
+        __shared__ int leave;
         __syncthreads();
         if (threadIdx.x == 0) {
+            volatile int* verr = err;
             volatile unsigned int* vgen = gen;
-            unsigned int g = *vgen;
-            __threadfence();
-            unsigned int arrived = atomicAdd(count, 1u);
-            if (arrived == gridDim.x - 1) {
-                atomicExch(count, 0u);
+            int out = (*verr & kBarrierTimeoutBit) != 0;
+            if (!out) {
+                unsigned int g = *vgen;
                 __threadfence();
-                atomicAdd(gen, 1u);
-            } else {
-                long long spins = 0;
-                while (*vgen == g) {
-                    __nanosleep(64);
-                    if (++spins > (1ll << 23)) { atomicOr(err, 1 << 5); break; }
+                unsigned int arrived = atomicAdd(count, 1u);
+                if (arrived == gridDim.x - 1) {
+                    atomicExch(count, 0u);
+                    __threadfence();
+                    atomicAdd(gen, 1u);
+                } else {
+                    long long polls = 0;
+                    while (*vgen == g) {
+                        __nanosleep(64);
+                        if (*verr & kBarrierTimeoutBit) { out = 1; break; }
+                        if (++polls > limit) { atomicOr(err, kBarrierTimeoutBit); out = 1; break; }
+                    }
                 }
+                __threadfence();
             }
-            __threadfence();
+            leave = out;
         }
         __syncthreads();
+        // every thread of the block reads the same flag here, so the whole block leaves
+        if (leave) asm volatile("exit;");
     }
 };
 

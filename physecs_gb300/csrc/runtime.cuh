@@ -36,7 +36,7 @@ struct psx_world {
     int n_scenes = 0;
     int scene_bits = 0;     // bits of the scene index in the broadphase sort
     int scene_sort_pmax = 0; // > 0: per-scene sort in shared memory, scenes padded to this size
-    std::vector<int> h_scene_body, h_scene_col, h_scene_dyn;
+    std::vector<int> h_scene_body, h_scene_col, h_scene_dyn, h_scene_joint;
     std::vector<uint32_t> h_entity;        // per body
     std::vector<int> h_body_dyn;           // per body: global dyn index or -1
     std::vector<int> h_col_local;          // per collider: index within its body
@@ -80,6 +80,7 @@ struct psx_world {
     std::vector<int> cluster_scenes_h; // ... solved by a thread-block cluster each
     int* cluster_scenes = nullptr;     // (grid_scenes: the rest; both sized for every big scene)
     int large_mode = 0;                // 1: clusters where they fit, 2: the whole grid
+    long long wait_limit = 0;          // polls of a grid-barrier wait before it gives up (0: the default)
     // block scenes by solver block size (64, 128, 256 threads), each longest first
     std::vector<int> tier_h[3];
     int* tier_scenes[3] = {nullptr, nullptr, nullptr};

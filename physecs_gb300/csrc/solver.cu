@@ -1072,8 +1072,10 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_solve_block(World w, FrameBuf 
     solve_scene(w, f, scenes[blockIdx.x], sy, smem, smem_f4);
 }
 
-__global__ void __launch_bounds__(256, 2) k_solve_grid(World w, FrameBuf f, const int* scenes, int n) {
-    GridSync sy{GridBarrier{f.bar, f.bar + 1, w.err}, (int*)(f.bar + 2)};
+static_assert(kBarrierTimeoutBit == ERR_BARRIER_TIMEOUT, "grid barrier error bit");
+
+__global__ void __launch_bounds__(256, 2) k_solve_grid(World w, FrameBuf f, const int* scenes, int n, long long limit) {
+    GridSync sy{GridBarrier{f.bar, f.bar + 1, w.err, limit}, (int*)(f.bar + 2)};
     for (int i = 0; i < n; ++i) {
         solve_scene(w, f, scenes[i], sy, nullptr, 0);
         sy.sync();
@@ -1121,13 +1123,24 @@ int solver_grid_blocks() {
     return sms * per;
 }
 
+// The dynamic shared memory a kernel may use is a per-device attribute: it is set on
+// the current device whenever a launch there asks for more than was set before.
+constexpr int kMaxDevices = 64;
+
+static void set_kernel_smem(const void* fn, int* done, int bytes) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= kMaxDevices) return;
+    if (done[dev] < bytes) {
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        done[dev] = bytes;
+    }
+}
+
 template <int NT>
 static void set_smem(int bytes) {
-    static int done = -1;
-    if (done != bytes) {
-        cudaFuncSetAttribute(k_solve_block<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-        done = bytes;
-    }
+    static int done[kMaxDevices] = {};
+    set_kernel_smem((const void*)k_solve_block<NT>, done, bytes);
 }
 
 int launch_solver(const World& w, FrameBuf& f, const SolverLaunch& L, cudaStream_t s) {
@@ -1167,11 +1180,8 @@ int launch_solver(const World& w, FrameBuf& f, const SolverLaunch& L, cudaStream
     if (L.n_tier[1]) cudaStreamWaitEvent(s, L.tjoin[1], 0);
     if (L.n_large) cudaStreamWaitEvent(s, L.join, 0);
     if (L.n_cluster) {
-        static int cluster_smem = -1;
-        if (cluster_smem != L.smem_large) {
-            cudaFuncSetAttribute(k_solve_cluster<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, L.smem_large);
-            cluster_smem = L.smem_large;
-        }
+        static int cluster_smem[kMaxDevices] = {};
+        set_kernel_smem((const void*)k_solve_cluster<512>, cluster_smem, L.smem_large);
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(kClusterBlocks * L.n_cluster);
         cfg.blockDim = dim3(512);
@@ -1192,7 +1202,11 @@ int launch_solver(const World& w, FrameBuf& f, const SolverLaunch& L, cudaStream
         FrameBuf fc = f;
         const int* gs = L.grid;
         int ng = L.n_grid;
-        void* args[] = {(void*)&wc, (void*)&fc, (void*)&gs, (void*)&ng};
+        long long limit = L.wait_limit > 0 ? L.wait_limit : kDefaultWaitPolls;
+        // the barrier's words start from zero in every launch, whatever an earlier launch
+        // that gave up on a wait left in them
+        cudaMemsetAsync(f.bar, 0, 4 * sizeof(unsigned), s);
+        void* args[] = {(void*)&wc, (void*)&fc, (void*)&gs, (void*)&ng, (void*)&limit};
         cudaLaunchCooperativeKernel((void*)k_solve_grid, L.grid_blocks, 256, args, 0, s);
         ++k;
     }

@@ -288,6 +288,7 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
     PSX_TRY(W->upload(w.scene_col, scene_col));
     PSX_TRY(W->upload(w.scene_dyn, scene_dyn));
     PSX_TRY(W->upload(w.scene_joint, scene_joint));
+    W->h_scene_joint = scene_joint;
     PSX_TRY(W->upload(w.knobs, W->h_knobs));
     PSX_TRY(W->upload(w.pos, pos));
     PSX_TRY(W->upload(w.quat, quat));
@@ -501,7 +502,7 @@ int psx::rt::queue_frame(psx_world* W, cudaEvent_t* ev) {
                    W->large_scenes, (int)W->large_scenes_h.size(), W->solver_smem_large,
                    W->cluster_scenes, (int)W->cluster_scenes_h.size(),
                    W->grid_scenes, (int)W->grid_scenes_h.size(), W->grid_blocks,
-                   W->aux_stream, W->ev_fork, W->ev_join};
+                   W->aux_stream, W->ev_fork, W->ev_join, W->wait_limit};
     k += launch_solver(W->w, W->f, L, s);
     if (ev) cudaEventRecord(ev[4], s);
     k += launch_aabb(W->w, 1, s);
@@ -724,6 +725,17 @@ PSX_API psx_status psx_world_set_knobs(psx_world* W, int32_t scene, int32_t subs
     return PSX_OK;
 }
 
+PSX_API psx_status psx_world_set_wait_limit(psx_world* W, int64_t polls) {
+    if (!W || polls < 0) return fail(PSX_ERR_INVALID_ARG, "psx_world_set_wait_limit: bad arguments");
+    PSX_CUDA(cudaSetDevice(W->device));
+    if (W->wait_limit != polls) {
+        PSX_CUDA(cudaStreamSynchronize(W->stream));
+        W->wait_limit = polls;
+        if (W->graph) { cudaGraphExecDestroy(W->graph); W->graph = nullptr; }   // recaptured with the new limit
+    }
+    return PSX_OK;
+}
+
 PSX_API psx_status psx_world_step(psx_world* W, float dt, int32_t frames) {
     if (W) cudaSetDevice(W->device);
     if (!W || frames < 0) return fail(PSX_ERR_INVALID_ARG, "psx_world_step");
@@ -741,6 +753,7 @@ PSX_API psx_status psx_world_step(psx_world* W, float dt, int32_t frames) {
 
 PSX_API psx_status psx_world_step_timed(psx_world* W, float dt, int32_t frames, float* total_ms, float* stage_ms,
                                         int64_t* kernels) {
+    if (W) cudaSetDevice(W->device);
     if (!W || frames <= 0) return fail(PSX_ERR_INVALID_ARG, "psx_world_step_timed");
     if (W->knobs_dirty || W->h_knobs.empty() || W->h_knobs[0].w != dt) {
         for (auto& k : W->h_knobs) k.w = dt;
@@ -754,7 +767,34 @@ PSX_API psx_status psx_world_step_timed(psx_world* W, float dt, int32_t frames, 
         W->events.push_back(e);
     }
     long long k0 = W->launches;
+    if (W->use_graph) {
+        // frames as psx_world_step runs them (graph replays after the first two), timed as
+        // a whole; then, outside that time, one more frame launched eagerly between stage
+        // events gives the stage split
+        PSX_CUDA(cudaEventRecord(W->events[0], W->stream));
+        for (int i = 0; i < frames; ++i) PSX_TRY(run_frame(W));
+        PSX_CUDA(cudaEventRecord(W->events[1], W->stream));
+        PSX_CUDA(cudaGetLastError());
+        if (kernels) *kernels = W->launches - k0;
+        PSX_CUDA(cudaEventSynchronize(W->events[1]));
+        float tot = 0;
+        PSX_CUDA(cudaEventElapsedTime(&tot, W->events[0], W->events[1]));
+        if (total_ms) *total_ms = tot;
+        if (stage_ms) {
+            queue_frame(W, &W->events[0]);
+            ++W->frames_run;
+            PSX_CUDA(cudaGetLastError());
+            PSX_CUDA(cudaEventSynchronize(W->events[5]));
+            for (int s = 0; s < 5; ++s) {
+                float ms = 0;
+                PSX_CUDA(cudaEventElapsedTime(&ms, W->events[s], W->events[s + 1]));
+                stage_ms[s] = ms * frames;
+            }
+        }
+        return check_err(W);
+    }
     for (int i = 0; i < frames; ++i) queue_frame(W, &W->events[6 * (size_t)i]);
+    W->frames_run += frames;
     PSX_CUDA(cudaGetLastError());
     PSX_CUDA(cudaEventSynchronize(W->events[6 * (size_t)frames - 1]));
     float st[5] = {0, 0, 0, 0, 0};
@@ -777,6 +817,7 @@ PSX_API psx_status psx_world_step_timed(psx_world* W, float dt, int32_t frames, 
 // `frames` frames, after one untimed frame with the same shapes.
 static psx_status time_stage(psx_world* W, int frames, int stage, float* ms) {
     queue_frame(W);
+    W->frames_run += frames + 1;
     size_t need = 6 * (size_t)frames;
     while (W->events.size() < need) {
         cudaEvent_t e;
@@ -1077,6 +1118,19 @@ PSX_API psx_status psx_world_apply_deltas(psx_world* W, int32_t n, const psx_bod
     return PSX_OK;
 }
 
+PSX_API psx_status psx_world_set_joint_params(psx_world* W, int32_t scene, int32_t joint, const float* params) {
+    if (!W || !params || scene < 0 || scene >= W->n_scenes)
+        return fail(PSX_ERR_INVALID_ARG, "psx_world_set_joint_params: bad arguments");
+    const int j0 = W->h_scene_joint[scene], j1 = W->h_scene_joint[scene + 1];
+    if (joint < 0 || joint >= j1 - j0) return fail(PSX_ERR_INVALID_ARG, "psx_world_set_joint_params: joint index");
+    PSX_CUDA(cudaSetDevice(W->device));
+    // the joint's parameter block in its device record; every frame reads it (the rows a
+    // joint has are laid out per frame), so the change takes effect from the next frame
+    float* dst = W->w.joints[j0 + joint].params;
+    PSX_CUDA(cudaMemcpyAsync(dst, params, PSX_JOINT_PARAMS * sizeof(float), cudaMemcpyHostToDevice, W->stream));
+    return PSX_OK;
+}
+
 PSX_API psx_status psx_world_set_contact_filter(psx_world* W, psx_contact_filter fn) {
     if (!W) return fail(PSX_ERR_INVALID_ARG, "psx_world_set_contact_filter: null world");
     PSX_CUDA(cudaSetDevice(W->device));
@@ -1274,8 +1328,8 @@ PSX_API psx_status psx_scene_simulate(psx_scene* s, float dt) {
 }  // extern "C"
 
 // ---------------------------------------------------------------- allocation-free body read
-// psx_world_read_bodies stages through a pinned host buffer that it allocates with
-// cudaMallocHost on first use.  Some callers cannot allocate at all while they run:
+// psx_world_read_bodies repacks the state on the device into a staging buffer that it
+// grows with cudaMalloc on first use.  Some callers cannot allocate at all while they run:
 // a render or control loop with a per-frame deadline (cudaMalloc / cudaMallocHost can
 // stall the whole device for milliseconds), or a process whose device memory is
 // reserved up front by its own pool allocator.  psx_world_read_bodies_noalloc serves

@@ -549,11 +549,20 @@ def joint_chains(n_chains=2048, links=32, substeps=8, iterations=4, seed=None):
     return s.finalize()
 
 
+def _batch_bodies(rng):
+    return int(round(math.exp(rng.uniform(1, math.log(16), math.log(2048))[0])))
+
+
+def batch_scene_bodies(index, config=4):
+    """The mixed-shape body count of batch_scene(index, config=config) without building it."""
+    return _batch_bodies(SplitMix64(scene_seed(config, index)))
+
+
 def batch_scene(index, n_bodies=None, config=4, chain_prob=0.1, pool=None):
     """One config-4 scene: mixed shapes dropped on a ground box, sometimes with an 8-link revolute chain."""
     rng = SplitMix64(scene_seed(config, index))
     if n_bodies is None:
-        n_bodies = int(round(math.exp(rng.uniform(1, math.log(16), math.log(2048))[0])))
+        n_bodies = _batch_bodies(rng)
     s = SceneData("batch%d_%d" % (config, index))
     ny = max(1, int(round(n_bodies ** (1 / 3))))
     nxz = int(math.ceil(math.sqrt(n_bodies / ny)))
@@ -603,3 +612,63 @@ def pair_scene(shape0, params0, pose0, shape1, params1, pose1, mesh0=None, mesh1
                      com=np.zeros(3), inv_inertia=np.eye(3).ravel() if dyn else np.zeros(9), col_type=shape,
                      col_params=p, col_mesh=mid)
     return s.finalize()
+
+
+# ----------------------------------------------------------------------------
+# character controllers
+# ----------------------------------------------------------------------------
+
+def strip_colliders(s, bodies):
+    """The scene with the colliders of `bodies` removed: such a body is an entity with a
+    transform and an empty collider list (a character controller's entity)."""
+    a = s.arrays
+    cs = a["collider_start"]
+    keep = np.ones(cs[-1], bool)
+    for b in bodies:
+        keep[cs[b]:cs[b + 1]] = False
+    per_body = np.diff(cs).copy()
+    per_body[list(bodies)] = 0
+    for k in list(a):
+        if k.startswith("col_") and len(a[k]) == len(keep):
+            a[k] = np.ascontiguousarray(a[k][keep])
+    a["collider_start"] = np.concatenate([[0], np.cumsum(per_body)]).astype(np.int32)
+    return s
+
+
+def character_scene(seed=61, n_chars=24, n_balls=10):
+    """Character entities (transforms without colliders) among static walls, a ramp and
+    resting dynamic bodies on a ground box."""
+    rng = np.random.default_rng(seed)
+    s = SceneData("characters%d" % seed)
+    _ground_box(s, (12.0, 0.5, 12.0))
+    walls = [([0, 1, 6], [6, 1, 0.3]), ([6, 1, 0], [0.3, 1, 6]), ([-4, 0.5, -4], [1.5, 0.5, 1.5])]
+    for p, he in walls:
+        s.add_bodies(pos=[p], quat=[IDENTITY_Q], flags=0, inv_mass=0.0, com=np.zeros(3), inv_inertia=np.zeros(9),
+                     col_type=BOX, col_params=list(he) + [0.0])
+    ang = 0.35
+    s.add_bodies(pos=[[-3, 0.6, 3]], quat=[[np.sin(ang / 2), 0, 0, np.cos(ang / 2)]], flags=0, inv_mass=0.0,
+                 com=np.zeros(3), inv_inertia=np.zeros(9), col_type=BOX, col_params=[2, 0.2, 2, 0])
+    m, com, inertia = mass_sphere(0.4)
+    balls = rng.uniform(-5, 5, (n_balls, 3))
+    balls[:, 1] = 0.4 + 0.9 * (np.arange(n_balls) // 10)
+    s.add_bodies(pos=balls, quat=[IDENTITY_Q] * n_balls, flags=BODY_DYNAMIC, inv_mass=1.0 / m, com=com,
+                 inv_inertia=np.linalg.inv(inertia).T.ravel(), col_type=SPHERE, col_params=[0.4, 0, 0, 0])
+    pc = rng.uniform(-6, 6, (n_chars, 3))
+    pc[:, 1] = rng.uniform(0.0, 0.3, n_chars)
+    first = s.add_bodies(pos=pc, quat=[IDENTITY_Q] * n_chars, flags=0, inv_mass=0.0, com=np.zeros(3),
+                         inv_inertia=np.zeros(9), col_type=SPHERE, col_params=[0.1, 0, 0, 0])
+    s = s.finalize()
+    return strip_colliders(s, range(first, first + n_chars)), list(range(first, first + n_chars))
+
+
+def character_moves(n_chars, frames, seed=62):
+    """Seeded translations per frame and character: a walk in a heading that turns, plus a
+    downward pull."""
+    rng = np.random.default_rng(seed)
+    head = rng.uniform(0, 2 * np.pi, n_chars)
+    out = []
+    for _ in range(frames):
+        head += rng.normal(0, 0.3, n_chars)
+        t = np.stack([0.12 * np.cos(head), np.full(n_chars, -0.05), 0.12 * np.sin(head)], 1).astype(np.float32)
+        out.append(t)
+    return out

@@ -21,6 +21,8 @@ oracle/ref/build_ref.py) on seeded scenes from physecs_gb300.scenes:
                        contact filter, with setCanCollide toggled between frames
   topology.npz         entity values and body states of a scene whose entities are
                        destroyed and created between frames
+  mechanisms.npz       body states of every joint kind with drives, limits, a servo and
+                       a gear, with joint setters and registry edits between frames
 
 Run in a checkout with the reference present:  python tests/golden/make_golden.py
 """
@@ -442,6 +444,28 @@ def trigger_fixture():
     return out
 
 
+MECHANISM_FRAMES, MECHANISM_RECORDED = 120, [10, 30, 60, 120]
+
+
+def mechanism_fixture():
+    from oracle.ref.ref_api import RefScene
+    sys.path.insert(0, os.path.dirname(HERE))
+    from scene_variants import apply_mechanism_op, mechanism_ops, mechanism_scene
+    s, info = mechanism_scene()
+    ops = mechanism_ops(s, info)
+    r = RefScene(s)
+    out = {"scene_sha256": np.array(scene_hash(s))}
+    for f in range(MECHANISM_FRAMES):
+        for op in ops:
+            if op[0] == f:
+                apply_mechanism_op(r, op)
+        r.step()
+        if f + 1 in MECHANISM_RECORDED:
+            for k, v in r.state().items():
+                out["f%d_%s" % (f + 1, k)] = v
+    return out
+
+
 def main():
     from oracle.ref import build_ref, ref_api
     if not ref_api.available():
@@ -480,6 +504,8 @@ def main():
     print("filters ok")
     np.savez_compressed(os.path.join(HERE, "topology.npz"), **topology_fixture())
     print("topology ok")
+    np.savez_compressed(os.path.join(HERE, "mechanisms.npz"), **mechanism_fixture())
+    print("mechanisms ok")
 
 
 if __name__ == "__main__":

@@ -4,6 +4,7 @@ off (no pairs), a scene without dynamic bodies and a scene without any contact."
 import numpy as np
 
 from physecs_gb300 import scenes
+from physecs_gb300.scenes import character_moves, character_scene, strip_colliders  # noqa: F401
 
 
 def flagged_scene(seed=31, n=80):
@@ -111,62 +112,6 @@ def delta_schedule(s, frames, seed=5, every=3):
     return out
 
 
-def strip_colliders(s, bodies):
-    """The scene with the colliders of `bodies` removed: such a body is an entity with a
-    transform and an empty collider list (a character controller's entity)."""
-    a = s.arrays
-    cs = a["collider_start"]
-    keep = np.ones(cs[-1], bool)
-    for b in bodies:
-        keep[cs[b]:cs[b + 1]] = False
-    per_body = np.diff(cs).copy()
-    per_body[list(bodies)] = 0
-    for k in list(a):
-        if k.startswith("col_") and len(a[k]) == len(keep):
-            a[k] = np.ascontiguousarray(a[k][keep])
-    a["collider_start"] = np.concatenate([[0], np.cumsum(per_body)]).astype(np.int32)
-    return s
-
-
-def character_scene(seed=61, n_chars=24, n_balls=10):
-    """Character entities (transforms without colliders) among static walls, a ramp and
-    resting dynamic bodies on a ground box."""
-    rng = np.random.default_rng(seed)
-    s = scenes.SceneData("characters%d" % seed)
-    scenes._ground_box(s, (12.0, 0.5, 12.0))
-    walls = [([0, 1, 6], [6, 1, 0.3]), ([6, 1, 0], [0.3, 1, 6]), ([-4, 0.5, -4], [1.5, 0.5, 1.5])]
-    for p, he in walls:
-        s.add_bodies(pos=[p], quat=[scenes.IDENTITY_Q], flags=0, inv_mass=0.0, com=np.zeros(3), inv_inertia=np.zeros(9),
-                     col_type=scenes.BOX, col_params=list(he) + [0.0])
-    ang = 0.35
-    s.add_bodies(pos=[[-3, 0.6, 3]], quat=[[np.sin(ang / 2), 0, 0, np.cos(ang / 2)]], flags=0, inv_mass=0.0,
-                 com=np.zeros(3), inv_inertia=np.zeros(9), col_type=scenes.BOX, col_params=[2, 0.2, 2, 0])
-    m, com, inertia = scenes.mass_sphere(0.4)
-    balls = rng.uniform(-5, 5, (n_balls, 3))
-    balls[:, 1] = 0.4 + 0.9 * (np.arange(n_balls) // 10)
-    s.add_bodies(pos=balls, quat=[scenes.IDENTITY_Q] * n_balls, flags=scenes.BODY_DYNAMIC, inv_mass=1.0 / m, com=com,
-                 inv_inertia=np.linalg.inv(inertia).T.ravel(), col_type=scenes.SPHERE, col_params=[0.4, 0, 0, 0])
-    pc = rng.uniform(-6, 6, (n_chars, 3))
-    pc[:, 1] = rng.uniform(0.0, 0.3, n_chars)
-    first = s.add_bodies(pos=pc, quat=[scenes.IDENTITY_Q] * n_chars, flags=0, inv_mass=0.0, com=np.zeros(3),
-                         inv_inertia=np.zeros(9), col_type=scenes.SPHERE, col_params=[0.1, 0, 0, 0])
-    s = s.finalize()
-    return strip_colliders(s, range(first, first + n_chars)), list(range(first, first + n_chars))
-
-
-def character_moves(n_chars, frames, seed=62):
-    """Seeded translations per frame and character: a walk in a heading that turns, plus a
-    downward pull."""
-    rng = np.random.default_rng(seed)
-    head = rng.uniform(0, 2 * np.pi, n_chars)
-    out = []
-    for _ in range(frames):
-        head += rng.normal(0, 0.3, n_chars)
-        t = np.stack([0.12 * np.cos(head), np.full(n_chars, -0.05), 0.12 * np.sin(head)], 1).astype(np.float32)
-        out.append(t)
-    return out
-
-
 def spawn_body(rng, center, kind=None):
     """A single dynamic body (sphere, box or capsule) as a SceneData, for creating an
     entity after the scene's creation."""
@@ -214,3 +159,122 @@ def topology_schedule(s, frames, seed=7, every=4):
             n += 1
         out[f] = (kill, spawn)
     return out
+
+
+def mechanism_scene(seed=71):
+    """Every joint kind with its drive or parameters, beside free bodies that each touch
+    only the ground.  No dynamic body carries two contacts, and joints are solved in the
+    reference's own joint colours, so the frames do not depend on the order in which
+    contacts are solved: the reference itself, run on the same registry, is the checker.
+      - free bodies: 4 boxes, 4 spheres, 4 capsules and 4 hulls on a 4 m grid, dropped from
+        1-2 m with seeded orientations and velocities, on a static ground box;
+      - mechanisms under colliderless static anchors 8 m up, 3 m apart: a driven revolute
+        link (RevoluteJoint drive, src/Joints/RevoluteJoint.cpp:30-37, 55); a prismatic
+        link with limits and a drive (PrismaticJoint.cpp:81-97, 147-148); a servo link
+        (ServoJoint.cpp:52-54); two revolute wheels coupled by a gear joint, one of them
+        driven (GearJoint.cpp:10-57); spherical, universal and fixed two-link chains.
+    Returns (scene, info) with the indices of the free bodies and of the joints by role."""
+    rng = scenes.SplitMix64(scenes.scene_seed(11, seed))
+    s = scenes.SceneData("mechanisms%d" % seed)
+    scenes._ground_box(s, (20.0, 0.5, 20.0))
+    pool = scenes._hull_pool(scenes.SplitMix64(scenes.scene_seed(11, 1 << 19)), count=4)
+    s.convex.extend(pool)
+    g = (np.arange(4) - 1.5) * 4.0
+    xs, zs = np.meshgrid(g, g, indexing="ij")
+    centers = np.stack([xs.ravel(), 1.0 + rng.uniform(16), zs.ravel()], axis=1)
+    kinds = np.repeat([scenes.BOX, scenes.SPHERE, scenes.CAPSULE, scenes.CONVEX_MESH], 4)
+    free = []
+    for i, c in enumerate(centers):
+        mix = [0.0, 0.0, 0.0, 0.0]
+        mix[[scenes.BOX, scenes.SPHERE, scenes.CAPSULE, scenes.CONVEX_MESH].index(kinds[i])] = 1.0
+        first = scenes._mixed_bodies(s, rng, c[None, :], 0, pool, mix=tuple(mix))
+        free.append(first)
+    a_vel = rng.normal(3 * len(free)).reshape(-1, 3) * 0.5
+    hh, r = 0.25, 0.1
+    m, com, inertia = scenes.mass_capsule(hh, r)
+    inv_i = np.linalg.inv(inertia).T.ravel()
+    anchors = [[x, 8.0, 12.0] for x in np.arange(8) * 3.0 - 10.5]
+    first_anchor = s.add_bodies(pos=anchors, quat=[scenes.IDENTITY_Q] * len(anchors), flags=0, inv_mass=0.0,
+                                com=np.zeros(3), inv_inertia=np.zeros(9), col_type=scenes.SPHERE,
+                                col_params=[0.1, 0, 0, 0])
+
+    def link(at):
+        return s.add_bodies(pos=[at], quat=[scenes.IDENTITY_Q], flags=scenes.BODY_DYNAMIC, inv_mass=1.0 / m, com=com,
+                            inv_inertia=inv_i, col_type=scenes.CAPSULE, col_params=[hh, r, 0.0, 0.0])
+
+    joints = []   # (kind, body0, body1, frames, params)
+    roles = {}
+    half = hh + r
+
+    def hang(anchor, kind, params=None, links=1, q=scenes.IDENTITY_Q):
+        top = np.asarray(anchors[anchor - first_anchor])
+        prev, prev_off = anchor, [0.0, 0.0, 0.0]
+        ids = []
+        for k in range(links):
+            b = link(top - [0.0, half + 2 * half * k, 0.0])
+            joints.append((kind, prev, b, list(prev_off) + list(q) + [0.0, half, 0.0] + list(q),
+                           params if params is not None else [0.0] * 8))
+            ids.append(len(joints) - 1)
+            prev, prev_off = b, [0.0, -half, 0.0]
+        return ids
+
+    qz = [0.0, 0.0, np.sin(np.pi / 4), np.cos(np.pi / 4)]   # anchor x axis along world y: a vertical slide
+    roles["revolute_drive"] = hang(first_anchor + 0, scenes.JOINT_REVOLUTE, [1.0, 2.0, 50.0] + [0.0] * 5)
+    roles["prismatic"] = hang(first_anchor + 1, scenes.JOINT_PRISMATIC, [0.2, -0.2, 1.0, 0.1, 5.0, 1.0, 0.0, 0.0], q=qz)
+    roles["servo"] = hang(first_anchor + 2, scenes.JOINT_SERVO, [0.5, 30.0, 1.0] + [0.0] * 5)
+    roles["spherical"] = hang(first_anchor + 3, scenes.JOINT_SPHERICAL, links=2)
+    roles["universal"] = hang(first_anchor + 4, scenes.JOINT_UNIVERSAL, links=2)
+    roles["fixed"] = hang(first_anchor + 5, scenes.JOINT_FIXED, links=2)
+    # gear: two wheels on revolute joints under anchors 6 and 7, the first one driven.  The
+    # axes run along world z, across the line between the wheels: the gear's angles are
+    # measured from the direction between its anchors, which must not lie on the axis
+    qy = [0.0, -np.sin(np.pi / 4), 0.0, np.cos(np.pi / 4)]   # anchor x axis along world z
+    wa = roles["wheel_a"] = hang(first_anchor + 6, scenes.JOINT_REVOLUTE, [1.0, 1.5, 20.0] + [0.0] * 5, q=qy)
+    wb = roles["wheel_b"] = hang(first_anchor + 7, scenes.JOINT_REVOLUTE, q=qy)
+    ba, bb = joints[wa[0]][2], joints[wb[0]][2]
+    joints.append((scenes.JOINT_GEAR, ba, bb, [0.0] * 3 + qy + [0.0] * 3 + qy, [2.0] + [0.0] * 7))
+    roles["gear"] = [len(joints) - 1]
+    s.add_joints(np.array([j[0] for j in joints], np.int32), np.array([j[1] for j in joints], np.int32),
+                 np.array([j[2] for j in joints], np.int32), np.array([j[3] for j in joints]),
+                 np.array([j[4] for j in joints]))
+    s = s.finalize()
+    s.arrays["ang_vel"][free] = a_vel.astype(np.float32)
+    s = strip_colliders(s, range(first_anchor, first_anchor + len(anchors)))
+    return s, {"free": free, "joints": roles}
+
+
+OP_KINEMATIC, OP_PATCH, OP_JOINT, OP_VELOCITY = 1, 2, 3, 4
+
+
+def mechanism_ops(s, info):
+    """Registry edits between frames of mechanism_scene: (frame, op, index, values), applied
+    before the frame: joint setters (a revolute drive reversed, new servo and prismatic
+    targets, a new gear ratio), setIsKinematic on and off, a patched pose and directly
+    written velocities."""
+    free, j = info["free"], info["joints"]
+    p = s.arrays["pos"][free[5]]
+    return [
+        (20, OP_JOINT, j["revolute_drive"][0], [1.0, -3.0, 50.0]),
+        (25, OP_KINEMATIC, free[0], [1.0]),
+        (30, OP_PATCH, free[5], [float(p[0]), 2.5, float(p[2]), 0.0, 0.0, 0.0, 1.0]),
+        (35, OP_VELOCITY, free[3], [0.0, 3.0, 0.0, 0.0, 0.0, 1.0]),
+        (40, OP_KINEMATIC, free[0], [0.0]),
+        (45, OP_JOINT, j["servo"][0], [-0.5, 30.0, 1.0]),
+        (45, OP_JOINT, j["prismatic"][0], [0.2, -0.2, 1.0, -0.1, 5.0, 1.0]),
+        (50, OP_JOINT, j["gear"][0], [0.5]),
+        (55, OP_JOINT, j["wheel_a"][0], [0.0, 0.0, 0.0]),
+    ]
+
+
+def apply_mechanism_op(sim, op):
+    """One mechanism_ops entry through an OracleScene / RefScene / World interface."""
+    from physecs_gb300.api import pack_deltas
+    _, kind, idx, v = op
+    if kind == OP_JOINT:
+        sim.set_joint_params(idx, v)
+    elif kind == OP_KINEMATIC:
+        sim.apply_deltas(pack_deltas([{"body": idx, "kinematic": bool(v[0])}]))
+    elif kind == OP_PATCH:
+        sim.apply_deltas(pack_deltas([{"body": idx, "pos": v[:3], "quat": v[3:7]}]))
+    elif kind == OP_VELOCITY:
+        sim.apply_deltas(pack_deltas([{"body": idx, "vel": v[:3], "ang_vel": v[3:6]}]))
