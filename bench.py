@@ -464,6 +464,7 @@ def main():
     ap.add_argument("--eager", action="store_true", help="launch every frame's kernels instead of a CUDA graph")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="keep the default kernel launch shapes")
+    ap.add_argument("--launch", default=None, help="kernel launch shapes as JSON (psx_launch_config fields); no tuning")
     args = ap.parse_args()
     rank, world, local = dist_info()
     assert args.warmup >= 3, "at least three warm-up steps"
@@ -484,8 +485,8 @@ def main():
     substeps = ss[0].num_substeps
     dev = local if world > 1 else 0
     use_graph = not args.eager      # the frame is captured once and replayed as a CUDA graph
-    launch = None
-    if not args.no_tune and len(ss) > 1:
+    launch = json.loads(args.launch) if args.launch else None
+    if launch is None and not args.no_tune and len(ss) > 1:
         # warm-up includes the autotuner: it picks launch shapes on a throwaway world's
         # frames, and the measured world is created afresh with them
         w = World(ss, device=dev)

@@ -22,10 +22,12 @@
  *   - The same five signals as the reference connect to the registry
  *     (src/Physecs.cpp:92-98).  Creating or destroying a collision or dynamic component,
  *     addCollider, clearColliders, createJoint and destroyJoint change the topology; the
- *     next simulate() rebuilds the device world from the registry.  A rebuilt world
- *     starts as a new reference Scene would over the same registry: collider bounds
- *     without the 0.01 m margin, an empty restitution cache and trigger set, and the
- *     joints coloured greedily in creation order.
+ *     next simulate() rebuilds the device world from the registry with
+ *     psx_world_recreate, which carries over what the reference's Scene keeps across
+ *     such changes: each remaining collider's broadphase bounds, the restitution cache
+ *     and last frame's trigger pairs between remaining colliders, every joint's colour
+ *     (Scene::addJoint's lowest free colour, freed again by destroyJoint) and a gear
+ *     joint's accumulated angles.
  *   - Every simulate() uploads the components' current pose and velocities (the
  *     reference reads them in place each frame, so direct writes take effect), steps the
  *     world, and writes the results back into TransformComponent and
@@ -96,6 +98,7 @@ class Joint {
     friend class Scene;
     int color = -1;
     bool dirty = false;     // a setter ran since the parameters last reached the device
+    int deviceIndex = -1;   // position among the device world's joints, -1 before it has one
 
 protected:
     entt::entity entity0;
@@ -283,6 +286,9 @@ private:
     std::unordered_map<uint32_t, unsigned> jointColors_;   // per entity: colours its joints use
     std::unordered_set<Pair, PairHash> noCollide_;     // setCanCollide(false) pairs
     std::unordered_set<uint32_t> moved_;               // entities patched since the last frame
+    // per entity: its first collider in the device world and how many of its colliders
+    // there continue (clearColliders makes that 0; added colliders are new)
+    std::unordered_map<uint32_t, std::pair<int, int>> deviceCols_;
     ContactType (*filter_)(bool, int, bool, int) = nullptr;
     std::vector<OnTriggerEnterListener*> enter_;
     std::vector<OnTriggerExitListener*> exit_;
@@ -292,6 +298,7 @@ private:
 
     void addJoint(Joint* joint);
     void onTopology(entt::registry&, entt::entity) { rebuild_ = true; }
+    void onCollisionDestroy(entt::registry&, entt::entity e) { deviceCols_.erase((uint32_t)e); rebuild_ = true; }
     void onMove(entt::registry&, entt::entity e) { moved_.insert((uint32_t)e); }
     bool check(psx_status s) { if (s != PSX_OK) error_ = s; return s == PSX_OK; }
     void build();

@@ -175,7 +175,7 @@ ContactType defaultContactFilter(bool isTrigger0, int, bool isTrigger1, int) {
 // on the GPU.
 Scene::Scene(entt::registry& registry, int) : registry_(registry) {
     registry.on_construct<RigidBodyCollisionComponent>().connect<&Scene::onTopology>(this);
-    registry.on_destroy<RigidBodyCollisionComponent>().connect<&Scene::onTopology>(this);
+    registry.on_destroy<RigidBodyCollisionComponent>().connect<&Scene::onCollisionDestroy>(this);
     registry.on_update<TransformComponent>().connect<&Scene::onMove>(this);
     registry.on_construct<RigidBodyDynamicComponent>().connect<&Scene::onTopology>(this);
     registry.on_destroy<RigidBodyDynamicComponent>().connect<&Scene::onTopology>(this);
@@ -184,7 +184,7 @@ Scene::Scene(entt::registry& registry, int) : registry_(registry) {
 // As the reference's destructor (src/Physecs.cpp:815-821) the joints are not deleted.
 Scene::~Scene() {
     registry_.on_construct<RigidBodyCollisionComponent>().disconnect<&Scene::onTopology>(this);
-    registry_.on_destroy<RigidBodyCollisionComponent>().disconnect<&Scene::onTopology>(this);
+    registry_.on_destroy<RigidBodyCollisionComponent>().disconnect<&Scene::onCollisionDestroy>(this);
     registry_.on_update<TransformComponent>().disconnect<&Scene::onMove>(this);
     registry_.on_construct<RigidBodyDynamicComponent>().disconnect<&Scene::onTopology>(this);
     registry_.on_destroy<RigidBodyDynamicComponent>().disconnect<&Scene::onTopology>(this);
@@ -213,14 +213,6 @@ int Scene::convexIndex(const ConvexMesh* m) const {
 // collision component in storage order, then dynamic entities without one, then entities
 // only a joint names.
 void Scene::build() {
-    const bool had_world = world_ != nullptr;
-    std::unordered_set<uint32_t> simulated_before;
-    if (had_world)
-        for (entt::entity e : bodies_) {
-            auto* d = registry_.try_get<RigidBodyDynamicComponent>(e);
-            if (d && !d->isKinematic && registry_.all_of<RigidBodyCollisionComponent>(e)) simulated_before.insert((uint32_t)e);
-        }
-    release();
     bodies_.clear();
     bodyOf_.clear();
     convex_.clear();
@@ -242,7 +234,14 @@ void Scene::build() {
     std::vector<int32_t> ctype, cmesh, cdata;
     std::vector<uint8_t> ctrig, cenable;
     std::vector<const TriangleMesh*> tris;
+    std::vector<int32_t> col_from;   // the device world's collider each collider continues, or -1
     for (entt::entity e : bodies_) {
+        auto prev = deviceCols_.find((uint32_t)e);
+        const int first_new = (int)ctype.size();
+        if (const auto* col = registry_.try_get<RigidBodyCollisionComponent>(e))
+            for (int k = 0; k < (int)col->colliders.size(); ++k)
+                col_from.push_back(prev != deviceCols_.end() && k < prev->second.second ? prev->second.first + k : -1);
+        (void)first_new;
         const TransformComponent& t = registry_.get<TransformComponent>(e);
         const auto* d = registry_.try_get<RigidBodyDynamicComponent>(e);
         entity.push_back((uint32_t)e);
@@ -312,10 +311,12 @@ void Scene::build() {
         }
         ti_start.push_back((int32_t)tidx.size());
     }
-    // joints in creation order
-    std::vector<int32_t> jtype, jb0, jb1;
+    // joints in creation order, with the colours Scene::addJoint gave them
+    std::vector<int32_t> jtype, jb0, jb1, jfrom, jcolor;
     std::vector<float> jframes, jparams;
     for (Joint* j : joints_) {
+        jfrom.push_back(j->deviceIndex);
+        jcolor.push_back(j->getColor());
         jtype.push_back(j->psxKind());
         jb0.push_back(bodyOf_.at((uint32_t)j->getEntity0()));
         jb1.push_back(bodyOf_.at((uint32_t)j->getEntity1()));
@@ -349,25 +350,30 @@ void Scene::build() {
     d.joint_type = jtype.data(); d.joint_body0 = jb0.data(); d.joint_body1 = jb1.data();
     d.joint_frames = jframes.data(); d.joint_params = jparams.data();
     d.num_substeps = numSubSteps_; d.num_iterations = numIterations_; d.gravity = g_;
-    psx_world_opts o{};
-    o.use_graph = 1;
-    detail::ok(psx_world_create(&d, 1, &o, &world_), "simulate: world creation");
+    if (!world_) {
+        psx_world_opts o{};
+        o.use_graph = 1;
+        detail::ok(psx_world_create(&d, 1, &o, &world_), "simulate: world creation");
+    } else {
+        // the new topology, carrying the old world's bounds, restitution cache, trigger
+        // pairs and gear angles over to the colliders and joints that continue
+        psx_scene_carry carry{};
+        carry.from_scene = 0;
+        carry.collider_from = col_from.data();
+        carry.joint_from = jfrom.data();
+        carry.joint_color = jcolor.data();
+        psx_world* next = nullptr;
+        detail::ok(psx_world_recreate(world_, &d, 1, &carry, &next), "simulate: topology change");
+        release();
+        world_ = next;
+    }
     rebuild_ = false;
     knobsDirty_ = false;
-    // what the registry's Scene would carry over: the broadphase margin of bodies that
-    // were simulated before (src/Physecs.cpp:555-559), setCanCollide and setContactFilter
-    std::vector<psx_body_delta> margin;
-    for (uint32_t e : simulated_before) {
-        auto it = bodyOf_.find(e);
-        if (it == bodyOf_.end()) continue;
-        psx_body_delta r{};
-        r.body = it->second;
-        r.mask = PSX_DELTA_POSE;
-        std::memcpy(r.pos, &pos[3 * (size_t)r.body], sizeof r.pos);
-        std::memcpy(r.quat, &quat[4 * (size_t)r.body], sizeof r.quat);
-        margin.push_back(r);
-    }
-    if (!margin.empty()) detail::ok(psx_world_apply_deltas(world_, (int32_t)margin.size(), margin.data()), "simulate");
+    deviceCols_.clear();
+    for (size_t b = 0; b < bodies_.size(); ++b)
+        deviceCols_[(uint32_t)bodies_[b]] = {col_start[b], col_start[b + 1] - col_start[b]};
+    for (size_t j = 0; j < joints_.size(); ++j) joints_[j]->deviceIndex = (int)j;
+    // setCanCollide and setContactFilter are set again on the new world
     for (const Pair& p : noCollide_) {
         auto a = bodyOf_.find(p.e0), b = bodyOf_.find(p.e1);
         if (a != bodyOf_.end() && b != bodyOf_.end())
@@ -580,6 +586,8 @@ void Scene::destroyJoint(Joint* joint) {
 // Scene::clearColliders / addCollider (src/Physecs.cpp:725-751)
 void Scene::clearColliders(entt::entity entity) {
     registry_.get<RigidBodyCollisionComponent>(entity).colliders.clear();
+    auto it = deviceCols_.find((uint32_t)entity);
+    if (it != deviceCols_.end()) it->second.second = 0;
     rebuild_ = true;
 }
 

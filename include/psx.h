@@ -172,6 +172,8 @@ typedef struct psx_launch_config {
     int32_t epa_full_only;           /* 1: EPA with the full polytope only (lowest latency for the slowest pair);
                                       * 2: a small polytope first, the full one for the pairs that outgrow it
                                       * (highest throughput; default) */
+    int32_t large_threads;           /* block scenes above 1024 dynamic bodies: threads per block, 128 (four blocks
+                                      * an SM), 256 (two) or 512 (one, with the most shared memory; default) */
 } psx_launch_config;
 
 typedef struct psx_world_opts {
@@ -241,6 +243,34 @@ PSX_API psx_status psx_world_simulate_host(psx_world* w, float dt, float* pos, f
 PSX_API psx_status psx_world_tune(psx_world* w, int32_t frames, psx_launch_config* best);
 /* The launch shapes in effect (after defaults, tuning or opts.launch). */
 PSX_API psx_status psx_world_launch_config(psx_world* w, psx_launch_config* out);
+
+/* ---- topology changes between frames: bodies, colliders and joints created or destroyed
+ * (registry.create / registry.destroy with onRigidBodyCreate / onRigidBodyDelete /
+ * onDynamicCreate / onDynamicDelete, Scene::addCollider / clearColliders, createJoint /
+ * destroyJoint; src/Physecs.cpp:25-78, 690-751).  The caller describes its scenes as they
+ * now are (bodies with their current state, entity values as the registry gives them,
+ * joints in the order Scene keeps them) and says what continues from the old world;
+ * psx_world_recreate builds the new world and moves over, on the device, what the old
+ * world holds beyond the state:
+ *   - each continued collider's broadphase bounds (with the 0.01 m margin if its body was
+ *     simulated or patched); new colliders get creation bounds, as onRigidBodyCreate and
+ *     addCollider give them;
+ *   - the restitution cache between continued colliders (src/Physecs.cpp:209-316);
+ *   - the trigger pairs of the last frame between continued colliders (:200-207);
+ *   - a continued gear joint's accumulated angles (GearJoint.h:10-17);
+ *   - the frame count, launch shapes, wait limit, CUDA-graph use and device.
+ * The contact filter and setCanCollide pairs are the caller's to set again. */
+typedef struct psx_scene_carry {
+    int32_t from_scene;             /* the old world's scene this scene continues, -1: a new scene */
+    const int32_t* collider_from;   /* [n_colliders] the old scene-local collider each collider continues, -1: new */
+    const int32_t* joint_from;      /* [n_joints] the old scene-local joint each joint continues, -1: new; NULL: all new */
+    const int32_t* joint_color;     /* [n_joints] each joint's colour 0-8 as Scene::addJoint gave it (the lowest colour
+                                     * free at both bodies when it was created; 8 is the overflow); NULL: colours
+                                     * assigned greedily in the joints' order, as at creation */
+} psx_scene_carry;
+/* The old world stays valid until the caller destroys it. */
+PSX_API psx_status psx_world_recreate(psx_world* from, const psx_scene_desc* scenes, int32_t n_scenes,
+                                      const psx_scene_carry* carry, psx_world** out);
 
 /* The setters of the joint classes (RevoluteJoint::setDriveEnabled / setDriveVelocity /
  * setDriveMaxTorque, PrismaticJoint::setUpperLimit ... setDriveDamping, GearJoint::

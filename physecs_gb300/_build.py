@@ -16,7 +16,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libpsx.so")
-SOURCES = ["prims.cu", "broadphase.cu", "narrowphase.cu", "solver.cu", "world.cu", "server.cu", "query.cu", "meshbvh.cu"]
+SOURCES = ["prims.cu", "broadphase.cu", "narrowphase.cu", "solver.cu", "world.cu", "server.cu", "query.cu", "meshbvh.cu",
+           "carry.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
                 "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC,-ffp-contract=off,-fvisibility=hidden",

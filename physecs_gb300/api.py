@@ -31,7 +31,7 @@ EXPORTS = ["psx_world_create", "psx_world_destroy", "psx_world_step", "psx_world
            "psx_world_overlap_mtd", "psx_world_trigger_events", "psx_trimesh_build", "psx_world_update_trimesh",
            "psx_world_apply_deltas", "psx_world_move_characters", "psx_world_set_contact_filter",
            "psx_world_set_can_collide", "psx_pin_host", "psx_unpin_host", "psx_world_set_wait_limit",
-           "psx_world_set_joint_params"]
+           "psx_world_set_joint_params", "psx_world_recreate"]
 
 _lib = None
 
@@ -42,7 +42,7 @@ class PsxError(RuntimeError):
 
 LAUNCH_FIELDS = ["convex_warps", "convex_blocks_per_sm", "analytic_threads", "analytic_blocks_per_sm",
                  "contacts_threads", "solver_smem_kb", "large_scene_solver",
-                 "gjk_blocks_per_sm", "epa_lanes", "solver_threads_min", "epa_full_only"]
+                 "gjk_blocks_per_sm", "epa_lanes", "solver_threads_min", "epa_full_only", "large_threads"]
 
 
 class PsxLaunchConfig(C.Structure):
@@ -53,6 +53,11 @@ class PsxWorldOpts(C.Structure):
     _fields_ = [("pairs_per_collider", C.c_int32), ("manifolds_per_collider", C.c_int32),
                 ("block_scene_max_dyn", C.c_int32), ("use_graph", C.c_int32), ("device", C.c_int32),
                 ("launch", C.c_void_p)]
+
+
+class PsxSceneCarry(C.Structure):
+    _fields_ = [("from_scene", C.c_int32), ("collider_from", C.c_void_p), ("joint_from", C.c_void_p),
+                ("joint_color", C.c_void_p)]
 
 
 class PsxServerOpts(C.Structure):
@@ -78,6 +83,7 @@ def load():
     lib.psx_world_synchronize.argtypes = [vp]
     lib.psx_world_set_wait_limit.argtypes = [vp, C.c_int64]
     lib.psx_world_set_joint_params.argtypes = [vp, C.c_int32, C.c_int32, vp]
+    lib.psx_world_recreate.argtypes = [vp, C.POINTER(PsxSceneDesc), C.c_int32, C.POINTER(PsxSceneCarry), C.POINTER(vp)]
     lib.psx_world_set_knobs.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_float]
     lib.psx_world_read_bodies.argtypes = [vp, vp, vp, vp, vp]
     lib.psx_world_write_bodies.argtypes = [vp, vp, vp, vp, vp]
@@ -181,6 +187,39 @@ class World:
 
     def synchronize(self):
         _check(load().psx_world_synchronize(self.h))
+
+    def recreate(self, scenes, carry):
+        """psx_world_recreate: this world's scenes replaced by `scenes` (SceneData, their
+        current state), carrying over, per scene, what carry[i] = {"from_scene", "collider_from",
+        "joint_from", "joint_color"} maps (arrays, or None).  This World then holds the new
+        world; the old one is destroyed."""
+        lib = load()
+        if not isinstance(scenes, (list, tuple)):
+            scenes = [scenes]
+        arr = (PsxSceneDesc * len(scenes))()
+        for i, s in enumerate(scenes):
+            arr[i] = make_desc(s)
+        keep = []
+        car = (PsxSceneCarry * len(scenes))()
+        for i, c in enumerate(carry):
+            fields = []
+            for k in ("collider_from", "joint_from", "joint_color"):
+                v = c.get(k)
+                if v is None:
+                    fields.append(None)
+                else:
+                    a = np.ascontiguousarray(v, np.int32)
+                    keep.append(a)
+                    fields.append(a.ctypes.data_as(C.c_void_p))
+            car[i] = PsxSceneCarry(int(c.get("from_scene", -1)), *fields)
+        h = C.c_void_p()
+        _check(lib.psx_world_recreate(self.h, arr, len(scenes), car, C.byref(h)))
+        lib.psx_world_destroy(self.h)
+        self.h = h
+        self.scenes = list(scenes)
+        self._descs = arr
+        self.n_bodies = sum(len(s.arrays["pos"]) for s in scenes)
+        self.body_start = np.cumsum([0] + [len(s.arrays["pos"]) for s in scenes])
 
     def set_joint_params(self, joint, params, scene=0):
         """psx_world_set_joint_params: the 8-float parameter block of a scene's joint."""

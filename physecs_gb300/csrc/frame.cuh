@@ -5,6 +5,26 @@
 
 namespace psx {
 
+// Restitution-cache keys: (collider, collider, triangle + 1) in one word; collider indices
+// take cbits bits each (every index is below 2^cbits - 1, so no key is all ones, the
+// empty mark), the triangle the remaining 64 - 2 cbits.
+__device__ __forceinline__ unsigned long long cache_key(int ca, int cb, int tri, int cbits) {
+    return ((unsigned long long)(uint32_t)ca << (64 - cbits)) | ((unsigned long long)(uint32_t)cb << (64 - 2 * cbits)) |
+           (unsigned long long)(uint32_t)(tri + 1);
+}
+__device__ __forceinline__ uint32_t cache_hash(unsigned long long k) {
+    k ^= k >> 33; k *= 0xff51afd7ed558ccdull; k ^= k >> 33; k *= 0xc4ceb9fe1a85ec53ull; k ^= k >> 33;
+    return (uint32_t)k;
+}
+constexpr unsigned long long kEmpty = ~0ull;
+
+// Trigger-pair keys (collider0 << 32 | collider1) and their tables' hash and empty mark.
+constexpr unsigned long long kNoKey = ~0ull;
+__device__ __forceinline__ unsigned trig_hash(unsigned long long k) {
+    k ^= k >> 33; k *= 0xff51afd7ed558ccdull; k ^= k >> 33; k *= 0xc4ceb9fe1a85ec53ull; k ^= k >> 33;
+    return (unsigned)k;
+}
+
 struct BVHNodes {
     int* left;        // child index: >= 0 internal node (global), < 0 leaf ~(sorted position)
     int* right;
@@ -129,7 +149,8 @@ struct CharIn {
     int iterations;
     float tx, ty, tz;
 };
-int launch_move_characters(const World& w, FrameBuf& f, const CharIn* cs, int n, unsigned char* flags, cudaStream_t s);
+int launch_move_characters(const World& w, FrameBuf& f, const CharIn* cs, int n, unsigned char* flags, float4* moved,
+                           cudaStream_t s);
 int launch_overlap_mtd(const World& w, FrameBuf& f, const ShapeIn* qs, int n, int cap, int* counts, float4* hits,
                        int* hit_col, cudaStream_t s);
 // a second stream with a fork / join event pair, for kernels that may overlap
@@ -163,6 +184,7 @@ struct SolverLaunch {
     cudaStream_t aux;
     cudaEvent_t fork, join;
     long long wait_limit;                  // polls of a grid-barrier wait (0: kDefaultWaitPolls)
+    int large_nt;                          // threads per block of the large block scenes: 128, 256 or 512
 };
 int launch_solver(const World& w, FrameBuf& f, const SolverLaunch& L, cudaStream_t s);
 int solver_grid_blocks();

@@ -510,9 +510,11 @@ __global__ void __launch_bounds__(64) k_overlap_mtd(World w, FrameBuf f, const S
 // given.  Each iteration collects the capsule's MTD hits and applies them in the order
 // (collider, triangle); the reference applies them in its tree's order, which only
 // changes the rounding of the summed moves.  Controllers of one batch see each other
-// at their poses before the batch.
+// at their poses before the batch: this kernel only reads the world and leaves each new
+// pose in moved[i]; k_commit_characters writes them after every controller has moved.
 constexpr int kCharHits = 32;
-__global__ void __launch_bounds__(64) k_move_characters(World w, FrameBuf f, const CharIn* cs, int n, unsigned char* flags_out) {
+__global__ void __launch_bounds__(64) k_move_characters(World w, FrameBuf f, const CharIn* cs, int n, unsigned char* flags_out,
+                                                        float4* moved) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const CharIn ch = cs[i];
@@ -551,8 +553,19 @@ __global__ void __launch_bounds__(64) k_move_characters(World w, FrameBuf f, con
             else p += nrm * mtd;
         }
     }
+    moved[i] = st4(p);
+    flags_out[i] = (unsigned char)flags;
+}
+
+// The moved controllers' poses into the world, then registry.patch<TransformComponent> ->
+// updateBounds: their colliders' bounds with the margin.
+__global__ void k_commit_characters(World w, const CharIn* cs, int n, const float4* moved) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int b = cs[i].body;
+    const V3 p = ld3(moved[i]);
+    const Q4 q = ld4(w.quat[b]);
     w.pos[b] = st4(p);
-    // registry.patch<TransformComponent> -> updateBounds, with the margin
     for (int c = w.body_col[b]; c < w.body_col[b + 1]; ++c) {
         const int4 ci = w.col_info[c];
         if (ci.y == G_TRIMESH) continue;
@@ -565,13 +578,14 @@ __global__ void __launch_bounds__(64) k_move_characters(World w, FrameBuf f, con
         w.aabb_min[c] = st4(bb.min);
         w.aabb_max[c] = st4(bb.max);
     }
-    flags_out[i] = (unsigned char)flags;
 }
 
-int launch_move_characters(const World& w, FrameBuf& f, const CharIn* cs, int n, unsigned char* flags, cudaStream_t s) {
+int launch_move_characters(const World& w, FrameBuf& f, const CharIn* cs, int n, unsigned char* flags, float4* moved,
+                           cudaStream_t s) {
     if (n <= 0) return 0;
-    k_move_characters<<<(n + 63) / 64, 64, 0, s>>>(w, f, cs, n, flags);
-    return 1;
+    k_move_characters<<<(n + 63) / 64, 64, 0, s>>>(w, f, cs, n, flags, moved);
+    k_commit_characters<<<(n + 127) / 128, 128, 0, s>>>(w, cs, n, moved);
+    return 2;
 }
 
 int launch_overlap_mtd(const World& w, FrameBuf& f, const ShapeIn* qs, int n, int cap, int* counts, float4* hits,
@@ -603,12 +617,6 @@ int launch_overlap(const World& w, FrameBuf& f, const ShapeIn* qs, int n, int ca
 // table slot so that the last frame's table is emptied entry by entry, not swept.
 // Events go to a log that the host drains.
 
-constexpr unsigned long long kNoKey = ~0ull;
-
-__device__ __forceinline__ unsigned trig_hash(unsigned long long k) {
-    k ^= k >> 33; k *= 0xff51afd7ed558ccdull; k ^= k >> 33; k *= 0xc4ceb9fe1a85ec53ull; k ^= k >> 33;
-    return (unsigned)k;
-}
 
 // A table holds at most half its capacity, so every probe sequence meets an empty slot.
 __device__ __forceinline__ bool trig_find(const unsigned long long* t, unsigned mask, unsigned long long key) {
@@ -902,15 +910,16 @@ PSX_API psx_status psx_world_move_characters(psx_world* W, int32_t n, const psx_
             if (b >= 0 && b < (int)W->h_delta_slot.size()) W->h_delta_slot[b] = -1;
         }
     if (st != PSX_OK) return st;
-    const size_t in_b = align256(sizeof(CharIn) * n);
+    const size_t in_b = align256(sizeof(CharIn) * n), fl_b = align256(n);
     char* buf = nullptr;
-    PSX_TRY(query_buffer(W, in_b + n, &buf));
+    PSX_TRY(query_buffer(W, in_b + fl_b + sizeof(float4) * n, &buf));
     CharIn* d_in = reinterpret_cast<CharIn*>(buf);
     unsigned char* d_fl = reinterpret_cast<unsigned char*>(buf + in_b);
+    float4* d_moved = reinterpret_cast<float4*>(buf + in_b + fl_b);
     cudaStream_t s = W->stream;
     PSX_CUDA(cudaMemcpyAsync(d_in, in.data(), sizeof(CharIn) * n, cudaMemcpyHostToDevice, s));
     query_trees(W);
-    launch_move_characters(W->w, W->f, d_in, n, d_fl, s);
+    W->launches += launch_move_characters(W->w, W->f, d_in, n, d_fl, d_moved, s);
     PSX_CUDA(cudaMemcpyAsync(flags_out, d_fl, n, cudaMemcpyDeviceToHost, s));
     PSX_CUDA(cudaStreamSynchronize(s));
     return check_err(W);

@@ -81,6 +81,9 @@ struct psx_world {
     int* cluster_scenes = nullptr;     // (grid_scenes: the rest; both sized for every big scene)
     int large_mode = 0;                // 1: clusters where they fit, 2: the whole grid
     long long wait_limit = 0;          // polls of a grid-barrier wait before it gives up (0: the default)
+    int large_nt = 512;                // threads per block of the scenes above 1024 dynamic bodies
+    psx_world_opts opts_used{};        // the creation options (launch shapes: current_launch)
+    std::vector<const int32_t*> forced_colors;   // per scene, while building: joint colours given by the caller
     // block scenes by solver block size (64, 128, 256 threads), each longest first
     std::vector<int> tier_h[3];
     int* tier_scenes[3] = {nullptr, nullptr, nullptr};
@@ -157,6 +160,8 @@ struct psx_world {
 namespace psx {
 namespace rt {
 psx_status validate(const psx_scene_desc& d);
+psx_status create_world(const psx_scene_desc* scenes, int n_scenes, psx_world_opts o, long long frames_run,
+                        const std::vector<const int32_t*>& colors, psx_world** out);
 // packs scenes into W's device buffers and computes the creation bounds
 psx_status build_world(psx_world* W, const psx_scene_desc* scenes, int S, const psx_world_opts& o);
 // queues one frame on W's stream; ev (optional) receives 6 stage events; returns kernels queued

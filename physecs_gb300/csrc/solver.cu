@@ -14,6 +14,7 @@
 // __syncthreads between phases; large scenes run on the whole grid with a
 // bounded grid barrier.
 #include <cooperative_groups.h>
+#include "libm_f32.cuh"
 #include "frame.cuh"
 
 namespace psx {
@@ -22,18 +23,6 @@ constexpr float kPi = 3.14159265358979323846f;
 
 // ---------------------------------------------------------------- restitution cache
 
-// (collider, collider, triangle + 1) in one word: collider indices take cbits bits each
-// (every index is below 2^cbits - 1, so no key is all ones, the empty mark), the
-// triangle the remaining 64 - 2 cbits
-__device__ __forceinline__ unsigned long long cache_key(int ca, int cb, int tri, int cbits) {
-    return ((unsigned long long)(uint32_t)ca << (64 - cbits)) | ((unsigned long long)(uint32_t)cb << (64 - 2 * cbits)) |
-           (unsigned long long)(uint32_t)(tri + 1);
-}
-__device__ __forceinline__ uint32_t cache_hash(unsigned long long k) {
-    k ^= k >> 33; k *= 0xff51afd7ed558ccdull; k ^= k >> 33; k *= 0xc4ceb9fe1a85ec53ull; k ^= k >> 33;
-    return (uint32_t)k;
-}
-constexpr unsigned long long kEmpty = ~0ull;
 
 __global__ void k_cache_clear(FrameBuf f) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -260,7 +249,7 @@ __device__ void make_joint_rows(const World& w, int j) {
             p2p();
             ang(cross(u1.c[1], u0.c[0]), dot(u0.c[0], u1.c[1]));
             ang(cross(u1.c[2], u0.c[0]), dot(u0.c[0], u1.c[2]));
-            float a = acosf(clampG(dot(u0.c[2], u1.c[2]), -1.f, 1.f));
+            float a = libm::acosf(clampG(dot(u0.c[2], u1.c[2]), -1.f, 1.f));   // glm::orientedAngle
             if (dot(u0.c[0], cross(u0.c[2], u1.c[2])) < 0.f) a = -a;
             R[k].angular0 = st4(u0.c[0], a - J.params[0]);
             R[k].angular1 = st4(u0.c[0], R[k].angular1.w);
@@ -299,14 +288,14 @@ __device__ void make_joint_rows(const World& w, int j) {
                 V3 dir = normalize(p0 - p1p);
                 V3 n = cross(u0.c[0], dir);
                 M3 t = mm(transpose(m3cols(u0.c[0], -n, dir)), u0);
-                a0 = atan2f(at(t.c[1], 2), at(t.c[2], 2));
+                a0 = libm::atan2f(at(t.c[1], 2), at(t.c[2], 2));
             }
             {
                 V3 p0p = p0 + dot(p1 - p0, u1.c[0]) * u1.c[0];
                 V3 dir = normalize(p0p - p1);
                 V3 n = cross(u1.c[0], dir);
                 M3 t = mm(transpose(u1), m3cols(u1.c[0], -n, dir));
-                a1 = atan2f(at(t.c[1], 2), at(t.c[2], 2));
+                a1 = libm::atan2f(at(t.c[1], 2), at(t.c[2], 2));
             }
             if (!J.gearInit) { J.persistent0 = a0; J.persistent1 = a1; J.gearInit = 1; }
             J.virtual0 += angleDiffD(a0, J.persistent0);
@@ -1148,10 +1137,24 @@ int launch_solver(const World& w, FrameBuf& f, const SolverLaunch& L, cudaStream
     int k = 2;
     // large scenes on a second stream, concurrently with the small ones
     if (L.n_large) {
-        set_smem<512>(L.smem_large);
         cudaEventRecord(L.fork, s);
         cudaStreamWaitEvent(L.aux, L.fork, 0);
-        k_solve_block<512><<<L.n_large, 512, L.smem_large, L.aux>>>(w, f, L.large, L.smem_large / 16);
+        if (L.large_nt == 128 || L.large_nt == 256) {
+            // several blocks an SM, each with its share of the SM's shared memory (beside
+            // each block's 1 KB reserve and its static shared memory)
+            const int per = L.large_nt == 128 ? 4 : 2;
+            const int smem = (L.smem_large + 5120 - per * 6144) / per / 16 * 16;
+            if (L.large_nt == 128) {
+                set_smem<128>(smem);
+                k_solve_block<128><<<L.n_large, 128, smem, L.aux>>>(w, f, L.large, smem / 16);
+            } else {
+                set_smem<256>(smem);
+                k_solve_block<256><<<L.n_large, 256, smem, L.aux>>>(w, f, L.large, smem / 16);
+            }
+        } else {
+            set_smem<512>(L.smem_large);
+            k_solve_block<512><<<L.n_large, 512, L.smem_large, L.aux>>>(w, f, L.large, L.smem_large / 16);
+        }
         cudaEventRecord(L.join, L.aux);
         ++k;
     }

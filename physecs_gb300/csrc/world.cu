@@ -180,10 +180,17 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
         // colours 0-7 are entity-disjoint, colour 8 collects the overflow
         std::vector<unsigned char> bits(d.n_bodies, 0);
         std::vector<std::vector<int>> colors(9);
+        const int32_t* forced = s < (int)W->forced_colors.size() ? W->forced_colors[s] : nullptr;
         for (int j = 0; j < d.n_joints; ++j) {
             int b0 = d.joint_body0[j], b1 = d.joint_body1[j];
             unsigned u = bits[b0] | bits[b1];
             int c = __builtin_ctz(~u);
+            if (forced) {   // the colour the caller's scene gave the joint when it was created
+                c = forced[j];
+                if (c < 0 || c > 8 || (c < 8 && (u >> c) & 1u))
+                    return fail(PSX_ERR_INVALID_ARG, "joint colour " + std::to_string(c) + " of joint " + std::to_string(j) +
+                                                         " is out of range or taken at one of its bodies");
+            }
             bits[b0] |= (unsigned char)(1u << c);
             bits[b1] |= (unsigned char)(1u << c);
             colors[c].push_back(j);
@@ -502,7 +509,7 @@ int psx::rt::queue_frame(psx_world* W, cudaEvent_t* ev) {
                    W->large_scenes, (int)W->large_scenes_h.size(), W->solver_smem_large,
                    W->cluster_scenes, (int)W->cluster_scenes_h.size(),
                    W->grid_scenes, (int)W->grid_scenes_h.size(), W->grid_blocks,
-                   W->aux_stream, W->ev_fork, W->ev_join, W->wait_limit};
+                   W->aux_stream, W->ev_fork, W->ev_join, W->wait_limit, W->large_nt};
     k += launch_solver(W->w, W->f, L, s);
     if (ev) cudaEventRecord(ev[4], s);
     k += launch_aabb(W->w, 1, s);
@@ -586,6 +593,9 @@ psx_status psx::rt::apply_launch(psx_world* W, const psx_launch_config& c) {
     if (c.solver_threads_min && c.solver_threads_min != 64 && c.solver_threads_min != 128 && c.solver_threads_min != 256)
         return fail(PSX_ERR_INVALID_ARG, "solver_threads_min must be 64, 128 or 256");
     if (c.solver_threads_min && c.solver_threads_min != W->threads_min) PSX_TRY(partition_tiers(W, c.solver_threads_min));
+    if (c.large_threads && c.large_threads != 128 && c.large_threads != 256 && c.large_threads != 512)
+        return fail(PSX_ERR_INVALID_ARG, "large_threads must be 128, 256 or 512");
+    if (c.large_threads) W->large_nt = c.large_threads;
     W->narrow = n;
     W->solver_smem = smem;
     if (W->graph) { cudaGraphExecDestroy(W->graph); W->graph = nullptr; }   // recaptured with the new shapes
@@ -655,6 +665,7 @@ psx_launch_config psx::rt::current_launch(const psx_world* W) {
     c.solver_smem_kb = W->solver_smem / 1024;
     c.large_scene_solver = W->large_mode;
     c.solver_threads_min = W->threads_min;
+    c.large_threads = W->large_nt;
     return c;
 }
 
@@ -676,6 +687,16 @@ PSX_API psx_status psx_world_create(const psx_scene_desc* scenes, int32_t n_scen
     if (!scenes || n_scenes <= 0 || !out) return fail(PSX_ERR_INVALID_ARG, "psx_world_create: bad arguments");
     psx_world_opts o{};
     if (opts) o = *opts;
+    return create_world(scenes, n_scenes, o, 0, {}, out);
+}
+
+}  // extern "C"
+
+// A new world: streams and events, then the scenes.  frames_run: the frames an earlier
+// world of these scenes ran (trigger events count frames from there); colors: per scene,
+// the joints' colours as the caller's scene assigned them, or empty.
+psx_status psx::rt::create_world(const psx_scene_desc* scenes, int n_scenes, psx_world_opts o, long long frames_run,
+                                 const std::vector<const int32_t*>& colors, psx_world** out) {
     if (o.block_scene_max_dyn <= 0) o.block_scene_max_dyn = 8192;
     int dev_count = 0;
     if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0) return fail(PSX_ERR_CUDA, "no CUDA device");
@@ -684,6 +705,10 @@ PSX_API psx_status psx_world_create(const psx_scene_desc* scenes, int32_t n_scen
     psx_world* W = new psx_world();
     W->device = o.device;
     W->use_graph = o.use_graph != 0;
+    W->opts_used = o;
+    W->opts_used.launch = nullptr;
+    W->frames_run = frames_run;
+    W->forced_colors = colors;
     cudaError_t e = cudaStreamCreateWithFlags(&W->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&W->aux_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&W->ev_fork, cudaEventDisableTiming);
@@ -697,6 +722,7 @@ PSX_API psx_status psx_world_create(const psx_scene_desc* scenes, int32_t n_scen
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&W->ev_join2, cudaEventDisableTiming);
     if (e != cudaSuccess) { delete W; return fail(PSX_ERR_CUDA, cudaGetErrorString(e)); }
     psx_status s = build_world(W, scenes, n_scenes, o);
+    W->forced_colors.clear();
     if (s != PSX_OK) { delete W; return s; }
     if (o.launch) {
         s = apply_launch(W, *o.launch);
@@ -705,6 +731,8 @@ PSX_API psx_status psx_world_create(const psx_scene_desc* scenes, int32_t n_scen
     *out = W;
     return PSX_OK;
 }
+
+extern "C" {
 
 PSX_API psx_status psx_world_destroy(psx_world* w) {
     if (w) cudaSetDevice(w->device);
@@ -904,6 +932,15 @@ PSX_API psx_status psx_world_tune(psx_world* W, int32_t frames, psx_launch_confi
         }
         knobs.push_back(k);
     }
+    if (!W->large_scenes_h.empty()) {   // block scenes above 1024 bodies: one big block or several smaller ones an SM
+        Knob k{3, {}};
+        for (int t : {512, 256, 128}) {
+            psx_launch_config c{};
+            c.large_threads = t;
+            k.cands.push_back(c);
+        }
+        knobs.push_back(k);
+    }
     if (W->block_scenes_h.size() > 152) {   // many small scenes: shared memory per solver block
         Knob k{3, {}};
         for (int kb : {48, 64, 100}) {
@@ -1069,15 +1106,11 @@ PSX_API psx_status psx_world_apply_deltas(psx_world* W, int32_t n, const psx_bod
     }
     for (const DeltaRec& r : recs) W->h_delta_slot[r.body] = -1;
     if (st != PSX_OK) return st;
-    // kinematic flags on the host, and the joints to fix up
+    // the joints to fix up; the host's kinematic flags change only once the upload and
+    // the kernel are queued, so a failed call leaves host and device as they were
     std::vector<int> joints;
     for (const DeltaRec& r : recs) {
         if (!(r.mask & DELTA_KINEMATIC)) continue;
-        int& fl = W->h_body_flags[r.body];
-        const bool was_sim = (fl & PSX_BODY_DYNAMIC) && !(fl & PSX_BODY_KINEMATIC);
-        fl = r.kinematic ? (fl | PSX_BODY_KINEMATIC) : (fl & ~PSX_BODY_KINEMATIC);
-        const bool sim = (fl & PSX_BODY_DYNAMIC) && !(fl & PSX_BODY_KINEMATIC);
-        W->n_simulated += (int)sim - (int)was_sim;
         for (int k = W->h_bj_start[r.body]; k < W->h_bj_start[r.body + 1]; ++k) joints.push_back(W->h_bj[k]);
     }
     std::sort(joints.begin(), joints.end());
@@ -1109,6 +1142,15 @@ PSX_API psx_status psx_world_apply_deltas(psx_world* W, int32_t n, const psx_bod
     const DeltaRec* dd = reinterpret_cast<const DeltaRec*>(W->ddev);
     const int* dj = reinterpret_cast<const int*>(W->ddev + rec_b);
     W->launches += launch_apply_deltas(W->w, dd, (int)recs.size(), dj, (int)joints.size(), W->stream);
+    PSX_CUDA(cudaGetLastError());
+    for (const DeltaRec& r : recs) {
+        if (!(r.mask & DELTA_KINEMATIC)) continue;
+        int& fl = W->h_body_flags[r.body];
+        const bool was_sim = (fl & PSX_BODY_DYNAMIC) && !(fl & PSX_BODY_KINEMATIC);
+        fl = r.kinematic ? (fl | PSX_BODY_KINEMATIC) : (fl & ~PSX_BODY_KINEMATIC);
+        const bool sim = (fl & PSX_BODY_DYNAMIC) && !(fl & PSX_BODY_KINEMATIC);
+        W->n_simulated += (int)sim - (int)was_sim;
+    }
     // triangle-mesh colliders of posed bodies
     for (const DeltaRec& r : recs) {
         if (!(r.mask & DELTA_POSE)) continue;

@@ -278,3 +278,20 @@ def apply_mechanism_op(sim, op):
         sim.apply_deltas(pack_deltas([{"body": idx, "pos": v[:3], "quat": v[3:7]}]))
     elif kind == OP_VELOCITY:
         sim.apply_deltas(pack_deltas([{"body": idx, "vel": v[:3], "ang_vel": v[3:6]}]))
+
+
+def mechanism_topology_ops(s, info):
+    """Topology edits of mechanism_scene for an application driving the registry
+    (tests/shim/drive_scene.cpp op codes 5-9), each keeping every dynamic body to at
+    most one contact: a free body destroyed, another's colliders cleared, a sphere
+    collider added high above a third, a fixed and a universal joint destroyed,
+    and a sphere entity created in a free spot."""
+    free, j = info["free"], info["joints"]
+    return [
+        (15, 5, free[7], []),
+        (18, 6, free[10], []),
+        (22, 7, free[11], [0.2, 0.0, 1.8, 0.0]),
+        (26, 8, j["fixed"][1], []),
+        (28, 9, -1, [0.3, 8.0, 2.0, -8.0, 1.0 / 113.1, 1.0 / 4.07]),
+        (33, 8, j["universal"][1], []),
+    ]

@@ -13,9 +13,11 @@
  * Scene file (little endian), written by tests/shim/scene_file.py:
  *   int32 counts[13]: bodies, colliders, convex meshes, convex faces, face indices,
  *                     convex vertices, joints, substeps, iterations, frames, ops,
- *                     triangle meshes, triangle vertices ... (see scene_file.py)
+ *                     entities the ops create, and one unused (see scene_file.py)
  *   float gravity, then the arrays in psx_scene_desc order, then the ops.
- * Out file: per frame, per body: pos[3] quat[4] (x, y, z, w) vel[3] ang_vel[3] as float32.
+ * Out file: per frame, per body (the scene's, then the ones the ops create): pos[3]
+ * quat[4] (x, y, z, w) vel[3] ang_vel[3] as float32; zeros for an entity destroyed or not
+ * yet created.
  */
 #include <cstdint>
 #include <cstdio>
@@ -64,7 +66,14 @@ struct Reader {
 glm::vec3 v3(const float* p) { return glm::vec3(p[0], p[1], p[2]); }
 glm::quat q4(const float* p) { return glm::quat(p[3], p[0], p[1], p[2]); }
 
-enum Op { OP_KINEMATIC = 1, OP_PATCH = 2, OP_JOINT = 3, OP_VELOCITY = 4 };
+enum Op {
+    OP_KINEMATIC = 1, OP_PATCH = 2, OP_JOINT = 3, OP_VELOCITY = 4,
+    OP_DESTROY = 5,        // registry.destroy(entity)
+    OP_CLEAR = 6,          // Scene::clearColliders(entity)
+    OP_ADD_SPHERE = 7,     // Scene::addCollider(entity, sphere of radius v[0] at offset v[1..3])
+    OP_DESTROY_JOINT = 8,  // Scene::destroyJoint(joint)
+    OP_SPAWN_SPHERE = 9    // a new dynamic sphere entity: radius v[0], position v[1..3], invMass v[4], invI diag v[5]
+};
 
 void set_joint(physecs::Joint* j, int type, const float* p) {
     switch (type) {
@@ -95,7 +104,7 @@ int run(const char* in, const char* out) {
     Reader r{f};
     auto cnt = r.read<int32_t>(13);
     const int nb = cnt[0], nc = cnt[1], nm = cnt[2], nf = cnt[3], nfi = cnt[4], ncv = cnt[5], nj = cnt[6];
-    const int substeps = cnt[7], iterations = cnt[8], frames = cnt[9], nops = cnt[10];
+    const int substeps = cnt[7], iterations = cnt[8], frames = cnt[9], nops = cnt[10], nspawn = cnt[11];
     const float gravity = r.read<float>(1)[0];
     auto flags = r.read<uint32_t>(nb);
     auto pos = r.read<float>(3 * nb), quat = r.read<float>(4 * nb), vel = r.read<float>(3 * nb), ang = r.read<float>(3 * nb);
@@ -195,7 +204,7 @@ int run(const char* in, const char* out) {
 
     FILE* o = std::fopen(out, "wb");
     if (!o) throw std::runtime_error("cannot open the output file");
-    std::vector<float> row(13);
+    std::vector<char> dead(nb + nspawn, 0);
     int next = 0;
     for (int fr = 0; fr < frames; ++fr) {
         // registry edits scheduled before this frame
@@ -215,15 +224,50 @@ int run(const char* in, const char* out) {
                 auto& d = registry.get<physecs::RigidBodyDynamicComponent>(ents[idx]);
                 d.velocity = v3(v);
                 d.angularVelocity = v3(v + 3);
+            } else if (op == OP_DESTROY) {
+                registry.destroy(ents[idx]);
+                dead[idx] = 1;
+            } else if (op == OP_CLEAR) {
+                scene.clearColliders(ents[idx]);
+            } else if (op == OP_ADD_SPHERE) {
+                physecs::Collider col{};
+                col.position = v3(v + 1);
+                col.orientation = glm::quat(1, 0, 0, 0);
+                col.geometry.type = physecs::SPHERE;
+                col.geometry.sphere = {v[0]};
+                col.material = {0.5f, 0.f, 0.f};
+                col.enableSimulation = true;
+                scene.addCollider(ents[idx], col);
+            } else if (op == OP_DESTROY_JOINT) {
+                scene.destroyJoint(joints[idx]);
+                joints[idx] = nullptr;
+            } else if (op == OP_SPAWN_SPHERE) {
+                entt::entity e = registry.create();
+                ents.push_back(e);
+                registry.emplace<TransformComponent>(e, v3(v + 1), glm::quat(1, 0, 0, 0), glm::vec3(1));
+                physecs::Collider col{};
+                col.orientation = glm::quat(1, 0, 0, 0);
+                col.geometry.type = physecs::SPHERE;
+                col.geometry.sphere = {v[0]};
+                col.material = {0.5f, 0.f, 0.f};
+                col.enableSimulation = true;
+                registry.emplace<physecs::RigidBodyCollisionComponent>(e, std::vector<physecs::Collider>{col});
+                glm::mat3 invI(0.f);
+                invI[0][0] = invI[1][1] = invI[2][2] = v[5];
+                registry.emplace<physecs::RigidBodyDynamicComponent>(e, false, glm::vec3(0), glm::vec3(0), v[4], glm::vec3(0), invI);
             }
         }
         scene.simulate(1.f / 60.f);
-        for (int b = 0; b < nb; ++b) {
-            const auto& t = registry.get<TransformComponent>(ents[b]);
-            const auto* d = registry.try_get<physecs::RigidBodyDynamicComponent>(ents[b]);
-            const glm::vec3 vv = d ? d->velocity : glm::vec3(0), aa = d ? d->angularVelocity : glm::vec3(0);
-            const float vals[13] = {t.position.x, t.position.y, t.position.z, t.orientation.x, t.orientation.y,
-                                    t.orientation.z, t.orientation.w, vv.x, vv.y, vv.z, aa.x, aa.y, aa.z};
+        for (int b = 0; b < nb + nspawn; ++b) {
+            float vals[13] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+            if (b < (int)ents.size() && !dead[b]) {
+                const auto& t = registry.get<TransformComponent>(ents[b]);
+                const auto* d = registry.try_get<physecs::RigidBodyDynamicComponent>(ents[b]);
+                const glm::vec3 vv = d ? d->velocity : glm::vec3(0), aa = d ? d->angularVelocity : glm::vec3(0);
+                const float row[13] = {t.position.x, t.position.y, t.position.z, t.orientation.x, t.orientation.y,
+                                       t.orientation.z, t.orientation.w, vv.x, vv.y, vv.z, aa.x, aa.y, aa.z};
+                std::memcpy(vals, row, sizeof vals);
+            }
             std::fwrite(vals, sizeof(float), 13, o);
         }
     }

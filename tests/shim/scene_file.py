@@ -19,6 +19,7 @@ OUT = os.path.join(HERE, "_build")
 SRC = os.path.join(HERE, "drive_scene.cpp")
 
 OP_KINEMATIC, OP_PATCH, OP_JOINT, OP_VELOCITY = 1, 2, 3, 4
+OP_DESTROY, OP_CLEAR, OP_ADD_SPHERE, OP_DESTROY_JOINT, OP_SPAWN_SPHERE = 5, 6, 7, 8, 9
 
 
 def tree():
@@ -35,7 +36,7 @@ def write_scene(path, s, frames, ops=()):
     ops = sorted(ops, key=lambda o: o[0])
     counts = np.array([nb, nc, len(a["convex_vert_start"]) - 1, len(a["face_normal"]), len(a["face_indices"]),
                        len(a["convex_verts"]), len(a["joint_type"]), s.num_substeps, s.num_iterations, frames, len(ops),
-                       0, 0], np.int32)
+                       sum(1 for o in ops if o[1] == OP_SPAWN_SPHERE), 0], np.int32)
     parts = [counts, np.array([s.gravity], np.float32),
              a["flags"].astype(np.uint32), a["pos"], a["quat"], a["vel"], a["ang_vel"], a["inv_mass"], a["com"],
              a["inv_inertia"], a["collider_start"].astype(np.int32),

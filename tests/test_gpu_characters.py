@@ -58,3 +58,37 @@ def test_character_refusals(gpu_lib):
     with pytest.raises(PsxError):
         w.move_characters([{"scene": 1, "body": 0, "height": 1, "radius": 0.3}], np.zeros((1, 3)))
     assert len(w.move_characters([], np.zeros((0, 3)))) == 0
+
+
+def test_controllers_that_meet_move_against_the_poses_before_the_batch(gpu_lib, oracle_lib):
+    """Two controllers whose entities carry colliders, each within the other's reach: a
+    batch moves both against the world as it was before the batch (neither sees the
+    other's new pose), the same on every run, so each equals the oracle moving that
+    controller alone from the poses before the batch."""
+    from oracle.port_api import OracleScene
+    from physecs_gb300 import scenes
+    from physecs_gb300.api import World
+    s = scenes.SceneData("meeting_controllers")
+    scenes._ground_box(s, (5.0, 0.5, 5.0))
+    s.add_bodies(pos=[[0.0, 0.05, 0.0], [0.45, 0.05, 0.0]], quat=[scenes.IDENTITY_Q] * 2, flags=0, inv_mass=0.0,
+                 com=np.zeros(3), inv_inertia=np.zeros(9), col_type=scenes.CAPSULE, col_params=[0.5, 0.3, 0.0, 0.0],
+                 col_pos=[[0.0, 0.8, 0.0]] * 2)
+    s = s.finalize()
+    chars = [1, 2]
+    moves = np.array([[0.2, -0.05, 0.0], [-0.2, -0.05, 0.0]], np.float32)
+    specs = [{"body": b, "height": 1.0, "radius": 0.3} for b in chars]
+    runs = []
+    for _ in range(3):
+        g = World([s])
+        flags = g.move_characters(specs, moves)
+        runs.append((list(flags), g.read_bodies()["pos"][chars].copy()))
+        assert g.counts()["error"] == 0
+        g.close()
+    for r in runs[1:]:
+        assert r[0] == runs[0][0] and np.array_equal(r[1], runs[0][1])
+    for k, b in enumerate(chars):
+        o = OracleScene(s)
+        fo = o.move_character(b, 1.0, 0.3, moves[k])
+        assert fo == runs[0][0][k], k
+        assert np.array_equal(o.state()["pos"][b].view(np.uint32), runs[0][1][k].view(np.uint32)), k
+    assert runs[0][0][0] & 2 and runs[0][0][1] & 2   # each met the other at its side

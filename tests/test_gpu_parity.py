@@ -294,8 +294,8 @@ def test_launch_shapes_do_not_change_results(gpu_lib):
     a = _gpu(ss)
     others = [_gpu(ss, launch=dict(convex_warps=3, convex_blocks_per_sm=5, analytic_threads=128, analytic_blocks_per_sm=4,
                                    contacts_threads=256, solver_smem_kb=100, gjk_blocks_per_sm=4, epa_lanes=32)),
-              _gpu(ss, launch=dict(epa_lanes=16, convex_warps=1, convex_blocks_per_sm=4)),
-              _gpu(ss, launch=dict(epa_lanes=8, convex_warps=1, convex_blocks_per_sm=2)),
+              _gpu(ss, launch=dict(epa_lanes=16, convex_warps=1, convex_blocks_per_sm=4, large_threads=128)),
+              _gpu(ss, launch=dict(epa_lanes=8, convex_warps=1, convex_blocks_per_sm=2, large_threads=256)),
               _gpu(ss, launch=dict(epa_full_only=1, solver_threads_min=256))]
     assert [o.launch_config()["epa_lanes"] for o in others[:3]] == [32, 16, 8]
     assert others[3].launch_config()["epa_full_only"] == 1 and others[3].launch_config()["solver_threads_min"] == 256

@@ -7,11 +7,12 @@ Scene::simulate.  Built against the reference's headers and library it runs the
 reference's CPU code; built against include/physecs_gb300/Physecs.h it runs on this GPU
 through libpsx.so.  mechanism_scene keeps every dynamic body to one contact, so the
 reference's serial contact order and the GPU's colour order give the same frames: every
-frame's registry state agrees within 1e-5 relative."""
+frame's registry state agrees within 1e-5 relative, also across topology changes
+(entities destroyed and created, colliders cleared and added, joints destroyed)."""
 import numpy as np
 import pytest
 
-from tests.scene_variants import mechanism_ops, mechanism_scene
+from tests.scene_variants import mechanism_ops, mechanism_scene, mechanism_topology_ops
 
 pytestmark = pytest.mark.gpu
 
@@ -26,16 +27,20 @@ def _rel(a, b):
     return float((np.abs(a - b) / np.maximum(1.0, np.abs(b))).max()) if a.size else 0.0
 
 
-@pytest.mark.parametrize("seed", [71, 73])
-def test_application_on_the_drop_in_equals_the_reference(gpu_lib, tmp_path, seed):
+@pytest.mark.parametrize("seed,topology", [(71, False), (73, False), (71, True)])
+def test_application_on_the_drop_in_equals_the_reference(gpu_lib, tmp_path, seed, topology):
+    """With topology=True the application also destroys an entity, clears one entity's
+    colliders, adds a collider to another, destroys two joints and creates an entity
+    between frames (the drop-in rebuilds its device world with psx_world_recreate)."""
     from oracle.ref import ref_api
     if not ref_api.available():
         pytest.skip("reference library not built here")
     from tests.shim import scene_file as sf
     s, info = mechanism_scene(seed=seed)
     path = str(tmp_path / "scene")
-    sf.write_scene(path, s, FRAMES, mechanism_ops(s, info))
-    n = len(s.arrays["pos"])
+    ops = mechanism_ops(s, info) + (mechanism_topology_ops(s, info) if topology else [])
+    sf.write_scene(path, s, FRAMES, ops)
+    n = len(s.arrays["pos"]) + sum(1 for o in ops if o[1] == sf.OP_SPAWN_SPHERE)
     rc, err, ref = sf.run(sf.build_reference(), path, str(tmp_path / "ref.out"), n, FRAMES)
     assert rc == 0, err
     rc, err, gpu = sf.run(sf.build_shim(), path, str(tmp_path / "gpu.out"), n, FRAMES)
