@@ -488,8 +488,10 @@ def main():
     launch = json.loads(args.launch) if args.launch else None
     if launch is None and not args.no_tune and len(ss) > 1:
         # warm-up includes the autotuner: it picks launch shapes on a throwaway world's
-        # frames, and the measured world is created afresh with them
+        # frames, stepped first to where the timed frames begin (early frames carry other
+        # contact loads), and the measured world is created afresh with them
         w = World(ss, device=dev)
+        w.step(DT, frame_window(args)[0] - 1)
         launch = w.tune(frames=2)
         w.close()
     w = World(ss, device=dev, launch=launch, use_graph=use_graph)

@@ -256,7 +256,10 @@ PSX_API psx_status psx_world_launch_config(psx_world* w, psx_launch_config* out)
  *     simulated or patched); new colliders get creation bounds, as onRigidBodyCreate and
  *     addCollider give them;
  *   - the restitution cache between continued colliders (src/Physecs.cpp:209-316);
- *   - the trigger pairs of the last frame between continued colliders (:200-207);
+ *   - the trigger pairs of the last frame between continued colliders (:200-207); a pair
+ *     that loses a collider exits at the end of the next frame, as the reference's next
+ *     frame finds it gone (:545-551), reported with body -1 for a removed body and the
+ *     entity value it had;
  *   - a continued gear joint's accumulated angles (GearJoint.h:10-17);
  *   - the frame count, launch shapes, wait limit, CUDA-graph use and device.
  * The contact filter and setCanCollide pairs are the caller's to set again. */
@@ -463,7 +466,7 @@ typedef struct psx_trigger_event {
     int32_t frame;      /* frame that raised it: frames stepped before it since the world's creation */
     int32_t kind;       /* PSX_TRIGGER_ENTER or PSX_TRIGGER_EXIT */
     int32_t scene;
-    int32_t body0;      /* scene-local body index */
+    int32_t body0;      /* scene-local body index (-1: a body removed by psx_world_recreate) */
     int32_t collider0;  /* collider index within that body */
     int32_t body1;
     int32_t collider1;

@@ -35,7 +35,8 @@ ORACLE = os.path.dirname(HERE)
 REPO = os.path.dirname(ORACLE)
 OUT = os.path.join(ORACLE, "_ref")
 TREE = os.path.join(OUT, "tree")
-REFERENCE = os.environ.get("PSX_REFERENCE", "/root/reference")
+# the reference checkout: PSX_REFERENCE, else a `reference` directory beside this repository
+REFERENCE = os.environ.get("PSX_REFERENCE") or os.path.join(os.path.dirname(REPO), "reference")
 
 LANE_RE = re.compile(r"([A-Za-z_][A-Za-z0-9_]*(?:(?:\.|->)[A-Za-z_][A-Za-z0-9_]*)*)\.(m128_f32|m128_i32|m128i_i32)\[")
 

@@ -24,6 +24,13 @@ FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true
                 "-Xptxas", "-warn-spills", "-I" + os.path.join(os.path.dirname(HERE), "include")]
 
 
+# glibc's float acosf, which the servo rows reproduce (csrc/libm_f32.cuh), is compiled
+# with fused multiply-adds on aarch64 hosts and without on x86-64 ones
+import platform as _platform
+if _platform.machine() in ("aarch64", "arm64"):
+    FLAGS = FLAGS + ["-DPSX_LIBM_FUSED"]
+
+
 def nvcc():
     for c in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
         if c and os.path.exists(c):

@@ -147,8 +147,47 @@ PSX_API psx_status psx_world_recreate(psx_world* F, const psx_scene_desc* scenes
             if (omap[cmap[k]] >= 0) return fail(PSX_ERR_INVALID_ARG, "psx_world_recreate: two colliders continue one");
             omap[cmap[k]] = (int)k;
         }
+    // the last frame's trigger pairs that lose a collider: the reference's next frame
+    // finds them missing from its new set and calls onTriggerExit for them
+    // (src/Physecs.cpp:545-551); they are reported with body -1 for a removed body
+    std::vector<psx_trigger_event> vanished;
+    if (F->f.trig_cap) {
+        int state[4] = {0, 0, 0, 0};
+        PSX_CUDA(cudaMemcpy(state, F->f.trig_state, sizeof state, cudaMemcpyDeviceToHost));
+        const int prev = state[0] ^ 1, n = std::min(state[1 + prev], F->f.trig_cap);
+        std::vector<unsigned long long> keys(std::max(n, 0));
+        if (n > 0) PSX_CUDA(cudaMemcpy(keys.data(), F->f.trig_keys[prev], sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost));
+        std::vector<int> new_scene(F->n_scenes, -1);
+        for (int s = 0; s < n_scenes; ++s)
+            if (carry[s].from_scene >= 0) new_scene[carry[s].from_scene] = s;
+        std::vector<int> new_col_body;   // new world collider -> new scene-local body
+        for (int s = 0; s < n_scenes; ++s)
+            for (int b = 0; b < scenes[s].n_bodies; ++b)
+                for (int c = scenes[s].collider_start[b]; c < scenes[s].collider_start[b + 1]; ++c) new_col_body.push_back(b);
+        for (unsigned long long k : keys) {
+            const int c0 = (int)(k >> 32), c1 = (int)(unsigned)k;
+            if (omap[c0] >= 0 && omap[c1] >= 0) continue;
+            const int ob0 = F->h_col_body[c0], ob1 = F->h_col_body[c1];
+            const int os = (int)(std::upper_bound(F->h_scene_body.begin(), F->h_scene_body.end(), ob0) - F->h_scene_body.begin()) - 1;
+            if (os < 0 || new_scene[os] < 0) continue;
+            psx_trigger_event e{};
+            e.frame = (int)F->frames_run;
+            e.kind = PSX_TRIGGER_EXIT;
+            e.scene = new_scene[os];
+            e.body0 = omap[c0] >= 0 ? new_col_body[omap[c0]] : -1;
+            e.collider0 = F->h_col_local[c0];
+            e.body1 = omap[c1] >= 0 ? new_col_body[omap[c1]] : -1;
+            e.collider1 = F->h_col_local[c1];
+            e.entity0 = F->h_entity[ob0];
+            e.entity1 = F->h_entity[ob1];
+            vanished.push_back(e);
+        }
+    }
     psx_world* W = nullptr;
     PSX_TRY(create_world(scenes, n_scenes, F->opts_used, F->frames_run, colors, &W));
+    W->trig_vanished = F->trig_vanished;
+    W->trig_vanished.insert(W->trig_vanished.end(), vanished.begin(), vanished.end());
+    W->trig_pending = F->trig_pending;   // delivered events the caller has not drained yet stay queued
     psx_status st = apply_launch(W, current_launch(F));
     W->wait_limit = F->wait_limit;
     DevArray<int> d_cmap, d_jmap, d_omap;

@@ -23,6 +23,22 @@
 #define PSX_HD __host__ __device__ __forceinline__
 #endif
 
+// glibc built for aarch64 lets the compiler fuse a product with the sum or difference
+// that consumes it into one fused multiply-add (GCC's default on that target), and x86-64
+// builds cannot; the results differ in the last bit for a few arguments in ten thousand.
+// PSX_LIBM_FUSED (set when this library is built on an aarch64 host) selects the fused
+// form at each place where that compiler fuses, so that the device matches the C library
+// of the host it is built for.
+#if defined(PSX_LIBM_FUSED)
+#ifdef __CUDA_ARCH__
+#define PSX_MAD(a, b, c) __fmaf_rn((a), (b), (c))
+#else
+#define PSX_MAD(a, b, c) std::fma((float)(a), (float)(b), (float)(c))
+#endif
+#else
+#define PSX_MAD(a, b, c) ((a) * (b) + (c))
+#endif
+
 namespace psx {
 namespace libm {
 
@@ -146,28 +162,28 @@ PSX_HD float acosf(float x) {
     if (ix < 0x3f000000u) {                                                   // |x| < 1/2
         if (ix <= 0x23000000u) return pi_2_head + pi_2_tail;
         const float z = x * x;
-        const float p = z * (p0 + z * (p1 + z * (p2 + z * (p3 + z * (p4 + z * p5)))));
-        const float q = 1.0f + z * (q1 + z * (q2 + z * (q3 + z * q4)));
+        const float p = z * PSX_MAD(z, PSX_MAD(z, PSX_MAD(z, PSX_MAD(z, PSX_MAD(z, p5, p4), p3), p2), p1), p0);
+        const float q = PSX_MAD(z, PSX_MAD(z, PSX_MAD(z, PSX_MAD(z, q4, q3), q2), q1), 1.0f);
         const float r = p / q;
-        return pi_2_head - (x - (pi_2_tail - x * r));
+        return pi_2_head - (x - PSX_MAD(-x, r, pi_2_tail));
     }
     if (hx >> 31) {                                                           // x <= -1/2
         const float z = (1.0f + x) * 0.5f;
-        const float p = z * (p0 + z * (p1 + z * (p2 + z * (p3 + z * (p4 + z * p5)))));
-        const float q = 1.0f + z * (q1 + z * (q2 + z * (q3 + z * q4)));
+        const float p = z * PSX_MAD(z, PSX_MAD(z, PSX_MAD(z, PSX_MAD(z, PSX_MAD(z, p5, p4), p3), p2), p1), p0);
+        const float q = PSX_MAD(z, PSX_MAD(z, PSX_MAD(z, PSX_MAD(z, q4, q3), q2), q1), 1.0f);
         const float s = std::sqrt(z);
         const float r = p / q;
-        const float w = r * s - pi_2_tail;
-        return pi - 2.0f * (s + w);
+        const float w = PSX_MAD(r, s, -pi_2_tail);
+        return PSX_MAD(-2.0f, s + w, pi);
     }
     const float z = (1.0f - x) * 0.5f;                                        // x >= 1/2
     const float s = std::sqrt(z);
     const float head = from_bits(bits(s) & 0xfffff000u);
-    const float corr = (z - head * head) / (s + head);
-    const float p = z * (p0 + z * (p1 + z * (p2 + z * (p3 + z * (p4 + z * p5)))));
-    const float q = 1.0f + z * (q1 + z * (q2 + z * (q3 + z * q4)));
+    const float corr = PSX_MAD(-head, head, z) / (s + head);
+    const float p = z * PSX_MAD(z, PSX_MAD(z, PSX_MAD(z, PSX_MAD(z, PSX_MAD(z, p5, p4), p3), p2), p1), p0);
+    const float q = PSX_MAD(z, PSX_MAD(z, PSX_MAD(z, PSX_MAD(z, q4, q3), q2), q1), 1.0f);
     const float r = p / q;
-    const float w = r * s + corr;
+    const float w = PSX_MAD(r, s, corr);
     return 2.0f * (head + w);
 }
 
@@ -175,3 +191,4 @@ PSX_HD float acosf(float x) {
 }  // namespace psx
 
 #undef PSX_HD
+#undef PSX_MAD

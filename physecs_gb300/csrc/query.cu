@@ -440,9 +440,12 @@ __device__ inline int collision_one(const World& w, V3 pos0, Q4 or0, GeomD g0, V
 // bounds meet the shape's, collided with the collider first; fn(collider, manifold, mtd)
 // for each manifold with points, mtd = max(0, deepest dot(p0 - p1, normal)).  The walk
 // visits the scene's tree left first.
+// self_body (>= 0): a body whose colliders are posed at self_pos instead of its stored
+// position, while their bounds stay the stored ones (a character controller's entity,
+// moved in the registry but not yet patched).
 template <class F>
 __device__ void for_each_mtd(const World& w, const FrameBuf& f, int s, V3 pos, Q4 ori, const GeomD& g, ManifoldL* ms,
-                             TCI* cand, Polytope& poly, F&& fn) {
+                             TCI* cand, Polytope& poly, F&& fn, int self_body = -1, V3 self_pos = V3{0.f, 0.f, 0.f}) {
     const Bounds b = getBounds(w, pos, ori, g);
     const float4 qmin = make_float4(b.min.x, b.min.y, b.min.z, 0.f), qmax = make_float4(b.max.x, b.max.y, b.max.z, 0.f);
     const int cs = w.scene_col[s], nc = w.scene_col[s + 1] - cs;
@@ -453,6 +456,7 @@ __device__ void for_each_mtd(const World& w, const FrameBuf& f, int s, V3 pos, Q
         Q4 co;
         GeomD cg;
         collider_pose(w, c, cp, co, cg);
+        if (w.col_info[c].x == self_body) cp = self_pos + qrot(ld4(w.quat[self_body]), ld3(w.col_pos[c]));
         const int nm = collision_one(w, cp, co, cg, pos, ori, g, ms, cand, poly, w.err);
         for (int k = 0; k < nm; ++k) {
             const ManifoldL& m = ms[k];
@@ -512,6 +516,8 @@ __global__ void __launch_bounds__(64) k_overlap_mtd(World w, FrameBuf f, const S
 // changes the rounding of the summed moves.  Controllers of one batch see each other
 // at their poses before the batch: this kernel only reads the world and leaves each new
 // pose in moved[i]; k_commit_characters writes them after every controller has moved.
+// A controller's own colliders move with it, as the registry's transform does in the
+// reference, while their bounds stay those before the move.
 constexpr int kCharHits = 32;
 __global__ void __launch_bounds__(64) k_move_characters(World w, FrameBuf f, const CharIn* cs, int n, unsigned char* flags_out,
                                                         float4* moved) {
@@ -543,7 +549,7 @@ __global__ void __launch_bounds__(64) k_move_characters(World w, FrameBuf f, con
                          }
                          hc[k] = c; ht[k] = m.triangleIndex;
                          hv[k] = make_float4(m.normal.x, m.normal.y, m.normal.z, mtd);
-                     });
+                     }, b, p);
         for (int k = 0; k < nh; ++k) {
             const V3 nrm = ld3(hv[k]);
             const float mtd = hv[k].w;
@@ -930,15 +936,31 @@ PSX_API psx_status psx_world_trigger_events(psx_world* W, psx_trigger_event* out
     if (!W || cap < 0 || (cap && !out) || !n_out) return fail(PSX_ERR_INVALID_ARG, "psx_world_trigger_events: bad arguments");
     PSX_CUDA(cudaSetDevice(W->device));
     const FrameBuf& f = W->f;
+    std::vector<psx_trigger_event> due;   // exits of pairs a topology change removed, once their frame ran
+    for (size_t i = 0; i < W->trig_vanished.size();) {
+        if (W->trig_vanished[i].frame < W->frames_run) {
+            due.push_back(W->trig_vanished[i]);
+            W->trig_vanished.erase(W->trig_vanished.begin() + (long)i);
+        } else {
+            ++i;
+        }
+    }
+    auto key = [](const psx_trigger_event& e) {
+        return std::make_tuple(e.frame, e.kind, e.scene, e.body0, e.collider0, e.body1, e.collider1);
+    };
+    if (!f.trig_cap && !due.empty()) {
+        std::sort(due.begin(), due.end(), [&](const psx_trigger_event& a, const psx_trigger_event& b) { return key(a) < key(b); });
+        W->trig_pending.insert(W->trig_pending.end(), due.begin(), due.end());
+    }
     if (f.trig_cap) {
         cudaStream_t st = W->stream;
         int n = 0;
         PSX_CUDA(cudaMemcpyAsync(&n, f.n_evt, sizeof(int), cudaMemcpyDeviceToHost, st));
         PSX_CUDA(cudaStreamSynchronize(st));
-        if (n) {
+        if (n || !due.empty()) {
             const int kept = std::min(n, f.evt_cap);
             std::vector<int4> ev(kept);
-            PSX_CUDA(cudaMemcpyAsync(ev.data(), f.trig_evt, sizeof(int4) * kept, cudaMemcpyDeviceToHost, st));
+            if (kept) PSX_CUDA(cudaMemcpyAsync(ev.data(), f.trig_evt, sizeof(int4) * kept, cudaMemcpyDeviceToHost, st));
             PSX_CUDA(cudaMemsetAsync(f.n_evt, 0, sizeof(int), st));
             PSX_CUDA(cudaStreamSynchronize(st));
             W->trig_lost += n - kept;
@@ -958,9 +980,7 @@ PSX_API psx_status psx_world_trigger_events(psx_world* W, psx_trigger_event* out
                 e.entity0 = W->h_entity[b0];
                 e.entity1 = W->h_entity[b1];
             }
-            auto key = [](const psx_trigger_event& e) {
-                return std::make_tuple(e.frame, e.kind, e.scene, e.body0, e.collider0, e.body1, e.collider1);
-            };
+            batch.insert(batch.end(), due.begin(), due.end());
             std::sort(batch.begin(), batch.end(), [&](const psx_trigger_event& a, const psx_trigger_event& b) { return key(a) < key(b); });
             W->trig_pending.insert(W->trig_pending.end(), batch.begin(), batch.end());
         }

@@ -64,6 +64,9 @@ struct psx_world {
     void* qbuf = nullptr;                  // scene-query staging on the device
     std::vector<psx_trigger_event> trig_pending;   // drained from the device, not yet delivered
     long long trig_lost = 0;               // events past the device log's capacity
+    // exits of last-frame trigger pairs whose collider a topology change removed: due at
+    // the end of the given frame (psx_world_recreate), delivered with that frame's events
+    std::vector<psx_trigger_event> trig_vanished;
     size_t qbuf_bytes = 0;
     std::vector<int> block_scenes_h, grid_scenes_h;
     int* block_scenes = nullptr;

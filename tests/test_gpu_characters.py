@@ -70,9 +70,10 @@ def test_controllers_that_meet_move_against_the_poses_before_the_batch(gpu_lib, 
     from physecs_gb300.api import World
     s = scenes.SceneData("meeting_controllers")
     scenes._ground_box(s, (5.0, 0.5, 5.0))
-    s.add_bodies(pos=[[0.0, 0.05, 0.0], [0.45, 0.05, 0.0]], quat=[scenes.IDENTITY_Q] * 2, flags=0, inv_mass=0.0,
-                 com=np.zeros(3), inv_inertia=np.zeros(9), col_type=scenes.CAPSULE, col_params=[0.5, 0.3, 0.0, 0.0],
-                 col_pos=[[0.0, 0.8, 0.0]] * 2)
+    # each entity's sphere sits beside the other controller's capsule, clear of its own
+    s.add_bodies(pos=[[0.0, 0.05, 0.0], [0.9, 0.05, 0.0]], quat=[scenes.IDENTITY_Q] * 2, flags=0, inv_mass=0.0,
+                 com=np.zeros(3), inv_inertia=np.zeros(9), col_type=scenes.SPHERE, col_params=[0.2, 0.0, 0.0, 0.0],
+                 col_pos=[[0.6, 0.8, 0.0], [-0.6, 0.8, 0.0]])
     s = s.finalize()
     chars = [1, 2]
     moves = np.array([[0.2, -0.05, 0.0], [-0.2, -0.05, 0.0]], np.float32)

@@ -145,8 +145,14 @@ def test_trigger_pairs_carry_across_a_recreate(gpu_lib, oracle_lib):
         o.step()
         ev, lost = g.trigger_events()
         assert lost == 0
-        got.append(ev[:, [0, 1, 3, 4, 5, 6]])
-    want = make_golden.events_sorted(o.trigger_events())
-    ge = np.concatenate([e for e in got if len(e)]) if any(len(e) for e in got) else np.zeros((0, 6), np.int32)
-    assert len(want) > 50
+        got.append(ev)
+    # compare (frame, kind, entity0, collider0, entity1, collider1): a destroyed body's pairs
+    # exit under its entity, which the device reports with body -1
+    ents = np.array([B["entity"] for B in m.bodies], np.int64)
+    ow = o.trigger_events()
+    want = make_golden.events_sorted(np.stack([ow[:, 0], ow[:, 1], ents[ow[:, 2]], ow[:, 3], ents[ow[:, 4]], ow[:, 5]], 1))
+    ge = np.concatenate([e for e in got if len(e)]) if any(len(e) for e in got) else np.zeros((0, 9), np.int64)
+    assert any(e[3] < 0 or e[5] < 0 for e in ge)   # pairs of destroyed bodies exited
+    ge = np.stack([ge[:, 0], ge[:, 1], ge[:, 7], ge[:, 4], ge[:, 8], ge[:, 6]], 1)
+    assert len(want) > 50 and (ow[:, 2] >= 0).all()
     assert np.array_equal(make_golden.events_sorted(ge), want)
