@@ -917,7 +917,8 @@ __device__ void solve_scene(const World& w, FrameBuf& f, int s, const S& sy, flo
     float4 kn = w.knobs[s];
     int substeps = (int)kn.x, iterations = (int)kn.y;
     float g = kn.z, dt = kn.w;
-    int* colstart = f.color_start + s * (kMaxColors + 1);
+    int* colstart_g = f.color_start + s * (kMaxColors + 1);
+    __shared__ int colstart[kMaxColors + 1];   // this block's copy, read by every colour step
     // ---- graph colouring of the contacts.  Each colour is a maximal set of contacts with
     // no dynamic body in common, grown in rounds: every uncoloured contact whose bodies
     // the colour does not hold yet claims them with a hashed priority, and the contacts
@@ -935,15 +936,17 @@ __device__ void solve_scene(const World& w, FrameBuf& f, int s, const S& sy, flo
     const bool serial_last = ncol < 0;
     if (serial_last) ncol = -ncol;
     // counting sort of the scene's contacts by colour
-    for (int k = tid; k <= kMaxColors; k += nth) colstart[k] = 0;
+    for (int k = tid; k <= kMaxColors; k += nth) colstart_g[k] = 0;
     sy.sync();
-    for (int k = tid; k < nc; k += nth) { int cl = col[k]; if (cl >= 0) atomicAdd(&colstart[cl + 1], 1); }
+    for (int k = tid; k < nc; k += nth) { int cl = col[k]; if (cl >= 0) atomicAdd(&colstart_g[cl + 1], 1); }
     sy.sync();
     if (tid == 0) {
-        for (int k = 0; k < kMaxColors; ++k) colstart[k + 1] += colstart[k];
+        for (int k = 0; k < kMaxColors; ++k) colstart_g[k + 1] += colstart_g[k];
         f.scene_ncolor[s] = ncol;
     }
     sy.sync();
+    for (int k = threadIdx.x; k <= kMaxColors; k += blockDim.x) colstart[k] = colstart_g[k];
+    __syncthreads();
     for (int k = tid; k < nc; k += nth) {
         int cl = col[k];
         if (col_smem) f.color_of[ms + k] = cl;   // kept for inspection
