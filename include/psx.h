@@ -165,7 +165,9 @@ typedef struct psx_launch_config {
                                       * after another (default: clusters when two or more scenes fit them) */
     int32_t gjk_blocks_per_sm;       /* GJK (one thread per convex pair): 128-thread blocks per SM, 1-16 (default 16) */
     int32_t epa_lanes;               /* EPA: lanes per overlapping pair, 8, 16 or 32 (default 16); below 32 a block
-                                      * is one warp holding 32 / epa_lanes pairs */
+                                      * is one warp holding 32 / epa_lanes pairs.  1: one lane per pair with the
+                                      * warp's new faces built by all of its lanes, and 16 lanes per pair for the
+                                      * pairs that need more than 12 steps */
     int32_t solver_threads_min;      /* smallest solver block: 64 (scenes up to 96 dynamic bodies on 64 threads, up to
                                       * 384 on 128), 128 or 256 (default: 64 for worlds of more block scenes than
                                       * two per SM, else 256) */

@@ -242,27 +242,44 @@ __global__ void k_scene_bounds(World w, FrameBuf f) {
     int s = blockIdx.x;
     int cs = w.scene_col[s], ce = w.scene_col[s + 1];
     float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    float size_sum = 0.f;   // longest side of the colliders' bounds, summed
+    int count = 0;
     for (int c = cs + threadIdx.x; c < ce; c += blockDim.x) {
         if (!(w.col_info[c].w & COL_ENABLE)) continue;   // disabled colliders never pair
         float4 a = w.aabb_min[c], b = w.aabb_max[c];
         float m[3] = {(a.x + b.x) * 0.5f, (a.y + b.y) * 0.5f, (a.z + b.z) * 0.5f};
         for (int k = 0; k < 3; ++k) { lo[k] = fminf(lo[k], m[k]); hi[k] = fmaxf(hi[k], m[k]); }
+        const float size = fmaxf(fmaxf(b.x - a.x, b.y - a.y), b.z - a.z);
+        if (size < FLT_MAX) { size_sum += size; ++count; }
     }
-    __shared__ float sh[6][32];
+    __shared__ float sh[7][32];
+    __shared__ int shn[32];
     for (int k = 0; k < 3; ++k) {
         for (int o = 16; o > 0; o >>= 1) {
             lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
             hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
         }
     }
+    for (int o = 16; o > 0; o >>= 1) {
+        size_sum += __shfl_xor_sync(0xffffffffu, size_sum, o);
+        count += __shfl_xor_sync(0xffffffffu, count, o);
+    }
     int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) for (int k = 0; k < 3; ++k) { sh[k][wid] = lo[k]; sh[3 + k][wid] = hi[k]; }
+    if (lane == 0) {
+        for (int k = 0; k < 3; ++k) { sh[k][wid] = lo[k]; sh[3 + k][wid] = hi[k]; }
+        sh[6][wid] = size_sum;
+        shn[wid] = count;
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
-        for (int q = 1; q < (int)(blockDim.x >> 5); ++q)
+        for (int q = 1; q < (int)(blockDim.x >> 5); ++q) {
             for (int k = 0; k < 3; ++k) { sh[k][0] = fminf(sh[k][0], sh[k][q]); sh[3 + k][0] = fmaxf(sh[3 + k][0], sh[3 + k][q]); }
+            sh[6][0] += sh[6][q];
+            shn[0] += shn[q];
+        }
+        // .w of the upper corner: the colliders' mean longest side
         f.scene_lo[s] = make_float4(sh[0][0], sh[1][0], sh[2][0], 0.f);
-        f.scene_hi[s] = make_float4(sh[3][0], sh[4][0], sh[5][0], 0.f);
+        f.scene_hi[s] = make_float4(sh[3][0], sh[4][0], sh[5][0], shn[0] ? sh[6][0] / (float)shn[0] : 0.f);
     }
 }
 
@@ -275,7 +292,8 @@ __device__ __forceinline__ uint32_t expand_bits(uint32_t v, int bits) {
 
 // 30-bit Morton code of the collider's bounds centre within its scene's bounds.  Bit 30
 // marks a collider as large (its bounds' longest side at least a quarter of the longest
-// side of the scene's centre bounds: ground boxes, terrain), bit 31 a disabled one, so that within a scene the
+// side of the scene's centre bounds, or sixteen times the scene's mean: ground boxes,
+// terrain, a ceiling over bodies that have scattered), bit 31 a disabled one, so that within a scene the
 // ordinary colliders sort first, then the large ones, then those that never pair.  Every
 // leaf looks for partners after itself, so a large collider is found from the small
 // ones' leaves instead of walking the whole tree itself.  The code depends only on the
@@ -303,7 +321,7 @@ __global__ void k_morton(World w, FrameBuf f) {
         }
         float spread = fmaxf(fmaxf(h[0] - l[0], h[1] - l[1]), h[2] - l[2]);
         float size = fmaxf(fmaxf(b.x - a.x, b.y - a.y), b.z - a.z);
-        if (spread > 0.f && size >= 0.25f * spread) code |= 1u << 30;
+        if ((spread > 0.f && size >= 0.25f * spread) || (hi.w > 0.f && size >= 16.f * hi.w)) code |= 1u << 30;
     }
     f.mkey[c] = code;
     f.keys[c] = code;
@@ -443,9 +461,9 @@ __device__ __forceinline__ bool pair_ok(const World& w, int ca, int cb) {
 }
 
 // A warp takes 32 consecutive sorted leaves (Morton neighbours, so their bounds are
-// close) and walks their scene's tree together: a node is entered when it may hold a
-// partner of any lane, every lane reads the same node (one broadcast load), and the
-// walk stays warp-uniform.  Each lane tests only its own leaf p against the leaves q > p
+// usually close) and walks their scene's tree together: a node is entered when it may
+// hold a partner of any lane, every lane reads the same node (one broadcast load), and
+// the walk stays warp-uniform; when the leaves lie far apart, each lane walks alone.  Each lane tests only its own leaf p against the leaves q > p
 // the walk reaches.  The walk is left-first depth-first, so each lane's partners come
 // out in increasing sorted position: an order that depends only on the scene (its
 // Morton codes), never on the tree's shape, the warp's other lanes or the batch.  A
@@ -476,8 +494,60 @@ __global__ void __launch_bounds__(256) k_traverse(World w, FrameBuf f) {
         const int groot = __shfl_sync(~0u, root, leader);
         const bool mine = want && s == gs;
         pending &= ~__ballot_sync(~0u, mine);
-        int stack[64];   // the same in every lane
+        // The joint walk pays for the union of the lanes' bounds.  Leaves that are Morton
+        // neighbours but far apart (scattered bodies, where the curve jumps) make that union
+        // much larger than any lane's own bounds; each lane then walks alone.  Either walk
+        // reaches each lane's partners in increasing sorted position, so the output is the
+        // same.
+        float ulo[3] = {qmin.x, qmin.y, qmin.z}, uhi[3] = {qmax.x, qmax.y, qmax.z};
+        float own = fmaxf(fmaxf(qmax.x - qmin.x, qmax.y - qmin.y), qmax.z - qmin.z);
+        if (!mine) {
+            ulo[0] = ulo[1] = ulo[2] = FLT_MAX;
+            uhi[0] = uhi[1] = uhi[2] = -FLT_MAX;
+            own = 0.f;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                ulo[k] = fminf(ulo[k], __shfl_xor_sync(~0u, ulo[k], o));
+                uhi[k] = fmaxf(uhi[k], __shfl_xor_sync(~0u, uhi[k], o));
+            }
+            own = fmaxf(own, __shfl_xor_sync(~0u, own, o));
+        }
+        const float spread = fmaxf(fmaxf(uhi[0] - ulo[0], uhi[1] - ulo[1]), uhi[2] - ulo[2]);
+        int stack[64];
         int sp = 0;
+        if (!(spread <= 8.f * own)) {   // scattered leaves (or a NaN bound): one walk per lane
+            if (mine) stack[sp++] = groot;
+            while (sp) {
+                const int c = stack[--sp];
+                if (c < 0) {
+                    const int q = ~c;
+                    if (q <= p) continue;
+                    const int cb = f.order[q];
+                    if (!overlap_incl(qmin, qmax, w.aabb_min[cb], w.aabb_max[cb])) continue;
+                    if (!pair_ok(w, ca, cb)) continue;
+                    if (EMIT) {
+                        int slot = out + count;
+                        if (slot < f.pair_cap) {
+                            uint32_t ea = (uint32_t)w.info[w.col_info[ca].x].x, eb = (uint32_t)w.info[w.col_info[cb].x].x;
+                            f.pairs[slot] = ea < eb ? make_int2(ca, cb) : make_int2(cb, ca);
+                        }
+                    }
+                    ++count;
+                } else if (f.bvh.last[c] > p && overlap_incl(qmin, qmax, f.bvh.bmin[c], f.bvh.bmax[c])) {
+                    if (sp + 2 <= 64) {
+                        stack[sp++] = f.bvh.right[c];
+                        stack[sp++] = f.bvh.left[c];
+                    } else {
+                        atomicOr(w.err, ERR_STACK_CAPACITY);
+                    }
+                }
+            }
+            continue;
+        }
+        // the joint walk: the stack is the same in every lane
         stack[sp++] = groot;
         while (sp) {
             const int c = stack[--sp];

@@ -56,10 +56,12 @@ struct FrameBuf {
     int* n_pairs;         // device scalar
     // narrowphase
     int* pair_cat;        // 0 analytic, 1 convex mesh, 2 triangle mesh
-    int* cat_count;       // [8]: analytic pairs without a box, convex, triangle-mesh pairs, convex pairs
+    int* cat_count;       // [10]: analytic pairs without a box, convex, triangle-mesh pairs, convex pairs
                           // that overlap, analytic pairs with one box, box-box pairs, overlapping convex
-                          // pairs whose EPA polytope outgrew the small one, trigger pairs
-    int* cat_list;        // [8 * pair_cap]: the pairs of each list
+                          // pairs whose EPA polytope outgrew the small one, trigger pairs, overlapping
+                          // convex pairs that outgrew the lane-per-pair EPA; [9] the pairs that EPA
+                          // has taken so far
+    int* cat_list;        // [9 * pair_cap]: the pairs of lists 0-8
     Manifold* man_pair;   // one slot per pair (analytic / convex categories)
     int tri_cap;          // triangle-mesh pair slots
     Manifold* man_tri;    // kTriManifolds slots per triangle-mesh pair slot

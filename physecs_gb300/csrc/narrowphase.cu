@@ -10,6 +10,7 @@
 #include "frame.cuh"
 #include "narrow_tri.cuh"
 #include "narrow_warp.cuh"
+#include "narrow_epa_flat.cuh"
 
 namespace psx {
 
@@ -197,21 +198,133 @@ __device__ __forceinline__ bool epa_pair(const World& w, FrameBuf& f, int t, PT&
     return true;
 }
 
-// EPA for the overlapping pairs: a group of G lanes per pair (32 / G pairs per warp),
-// WARPS warps per block, a SmallPoly (about 4.7 KB of dynamic shared memory) per group.
-// Pairs that outgrow it go to the overflow list for k_convex_epa_full.
+// EPA for the overlapping pairs of list `src`: a group of G lanes per pair (32 / G pairs
+// per warp), WARPS warps per block, a SmallPoly (about 4.7 KB of dynamic shared memory)
+// per group.  Pairs that outgrow it go to the overflow list for k_convex_epa_full.
 template <int G, int WARPS>
-__global__ void __launch_bounds__(32 * WARPS) k_convex_epa(World w, FrameBuf f) {
+__global__ void __launch_bounds__(32 * WARPS) k_convex_epa(World w, FrameBuf f, int src) {
     extern __shared__ __align__(16) unsigned char epa_smem[];
     constexpr int GPW = 32 / G;   // groups per warp
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const Group<G> g(lane);
     SmallPoly& P = reinterpret_cast<SmallPoly*>(epa_smem)[wid * GPW + lane / G];
-    const int n = f.cat_count[3];
+    const int n = f.cat_count[src];
     for (int h = (blockIdx.x * WARPS + wid) * GPW + lane / G; h < n; h += gridDim.x * WARPS * GPW) {
-        const int t = f.cat_list[3 * (size_t)f.pair_cap + h];
+        const int t = f.cat_list[src * (size_t)f.pair_cap + h];
         if (!epa_pair<G, SmallPoly, true>(w, f, t, P, g) && g.gl == 0)
             f.cat_list[6 * (size_t)f.pair_cap + atomicAdd(&f.cat_count[6], 1)] = t;
+    }
+}
+
+// EPA for the overlapping pairs (list 3) with one lane per pair and the faces built by the
+// whole warp (narrow_epa_flat.cuh).  Each warp takes pairs from a shared counter as its
+// lanes free up; a pair whose polytope would outgrow the lane's room goes to list 8 for
+// the grouped kernel.  One block of WARPS warps per SM: the polytopes take about 54 KB of
+// shared memory a warp.
+template <int WARPS>
+__global__ void __launch_bounds__(32 * WARPS, 1) k_convex_epa_flat(World w, FrameBuf f) {
+    extern __shared__ __align__(16) unsigned char epa_smem[];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    FlatPoly& P = reinterpret_cast<FlatPoly*>(epa_smem)[wid];
+    const int n = f.cat_count[3];
+    const unsigned below = (1u << lane) - 1u;
+    int t = -1;              // the lane's pair (index into list 1), -1 when it has none
+    bool drained = false;    // no pair left for this lane
+    int p = 0, nv = 0, nf = 0, nnew = 0;
+    Support s0, s1;
+    for (;;) {
+        // lanes without a pair take the next ones
+        const bool need = t < 0 && !drained;
+        const unsigned needm = __ballot_sync(~0u, need);
+        if (needm) {
+            const int leader = __ffs(needm) - 1;
+            int base = 0;
+            if (lane == leader) base = atomicAdd(&f.cat_count[9], __popc(needm));
+            base = __shfl_sync(~0u, base, leader);
+            if (need) {
+                const int h = base + __popc(needm & below);
+                if (h < n) {
+                    t = f.cat_list[3 * (size_t)f.pair_cap + h];
+                    p = f.cat_list[f.pair_cap + t];
+                    V3 pos0, pos1;
+                    Q4 or0, or1;
+                    GeomD g0, g1;
+                    convex_pair_ordered(w, f.pairs[p], pos0, or0, g0, pos1, or1, g1);
+                    convexOrderedSupports(w, pos0, or0, g0, pos1, or1, g1, s0, s1);
+                    const Manifold& m = f.man_pair[p];
+                    GjkSimplex sx;
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const V3 sa = ld3(m.p0[i]), sb = ld3(m.p1[i]);
+                        sx.v[i] = {d3(sa - sb), sa, sb};
+                        fp_set_vertex(P, i, lane, sx.v[i]);
+                    }
+                    // EPA.h initial tetrahedron, wound so that every normal points outwards
+                    const D3 n0 = cross(sx.v[0].pos - sx.v[1].pos, sx.v[2].pos - sx.v[1].pos);
+                    const bool flip = dot(sx.v[3].pos - sx.v[0].pos, n0) < 0;
+                    const unsigned char tri[4][3] = {{0, (unsigned char)(flip ? 1 : 2), (unsigned char)(flip ? 2 : 1)},
+                                                     {3, (unsigned char)(flip ? 1 : 2), 0},
+                                                     {3, (unsigned char)(flip ? 2 : 1), (unsigned char)(flip ? 1 : 2)},
+                                                     {3, 0, (unsigned char)(flip ? 2 : 1)}};
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) { P.t0[k][lane] = tri[k][0]; P.t1[k][lane] = tri[k][1]; P.t2[k][lane] = tri[k][2]; }
+                    P.nbase[lane] = 0;
+                    nv = 4;
+                    nf = 0;
+                    nnew = 4;
+                } else {
+                    drained = true;
+                }
+            }
+        }
+        if (!__ballot_sync(~0u, t >= 0)) break;
+        // the step's new faces of every lane, built by all lanes
+        int incl = t >= 0 ? nnew : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(~0u, incl, o);
+            if (lane >= o) incl += y;
+        }
+        P.offs[lane + 1] = incl;
+        if (lane == 0) P.offs[0] = 0;
+        const int total = __shfl_sync(~0u, incl, 31);
+        __syncwarp();
+        for (int k = lane; k < total; k += 32) {
+            int lo = 0, hi = 32;   // the slot s with offs[s] <= k < offs[s + 1]
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (P.offs[mid] <= k) lo = mid; else hi = mid;
+            }
+            const int m = k - P.offs[lo];
+            fp_make_face(P, lo, P.nbase[lo] + m, P.t0[m][lo], P.t1[m][lo], P.t2[m][lo]);
+        }
+        __syncwarp();
+        if (t >= 0) {
+            nf = P.nbase[lane] + nnew;
+            nnew = 0;
+            // the closest face, by the reference's scan: the running minimum is a float
+            float minDist = (float)DBL_MAX;
+            int fi = 0;
+            for (int k = 0; k < nf; ++k) {
+                const double d = P.fd[k][lane];
+                if (d < minDist) { minDist = (float)d; fi = k; }
+            }
+            const D3 normal = fp_n(P, fi, lane);
+            const GjkVertex v = mink(s0, s1, f3(normal));
+            if (dot(v.pos, normal) - minDist < (double)0.00001f) {
+                V3 cp0, cp1;
+                fp_closest_points(P, lane, fi, cp0, cp1);
+                Manifold& m = f.man_pair[p];
+                m.n = st4(f3(normal));
+                m.p0[0] = st4(cp0);
+                m.p1[0] = st4(cp1);
+                t = -1;
+            } else if (!fp_insert(P, lane, nv, nf, nnew, v)) {
+                f.cat_list[8 * (size_t)f.pair_cap + atomicAdd(&f.cat_count[8], 1)] = t;
+                t = -1;
+            }
+        }
+        __syncwarp();
     }
 }
 
@@ -284,40 +397,59 @@ __global__ void __launch_bounds__(64) k_narrow_tri(World w, FrameBuf f) {
     }
 }
 
+// A kernel's shared memory attributes are per device: each function keeps, per device
+// index, whether they were set there.
+constexpr int kMaxDevices = 64;
+static void set_smem_attrs(const void* fn, bool* done, int bytes) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= kMaxDevices || done[dev]) return;
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    done[dev] = true;
+}
+
 template <int G, int WARPS>
-static void launch_convex_epa(const World& w, FrameBuf& f, int blocks_per_sm, cudaStream_t s) {
+static void launch_convex_epa(const World& w, FrameBuf& f, int blocks_per_sm, int src, cudaStream_t s) {
     const int smem = (int)sizeof(SmallPoly) * WARPS * (32 / G);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_convex_epa<G, WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        cudaFuncSetAttribute(k_convex_epa<G, WARPS>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-        attr_set = true;
-    }
-    k_convex_epa<G, WARPS><<<152 * blocks_per_sm, 32 * WARPS, smem, s>>>(w, f);
+    static bool done[kMaxDevices] = {};
+    set_smem_attrs((const void*)k_convex_epa<G, WARPS>, done, smem);
+    k_convex_epa<G, WARPS><<<152 * blocks_per_sm, 32 * WARPS, smem, s>>>(w, f, src);
+}
+
+constexpr int kFlatWarps = 4;
+static void launch_convex_epa_flat(const World& w, FrameBuf& f, cudaStream_t s) {
+    const int smem = (int)sizeof(FlatPoly) * kFlatWarps;
+    static bool done[kMaxDevices] = {};
+    set_smem_attrs((const void*)k_convex_epa_flat<kFlatWarps>, done, smem);
+    k_convex_epa_flat<kFlatWarps><<<152, 32 * kFlatWarps, smem, s>>>(w, f);
 }
 
 // The convex kernels (bound by the FP64 pipe) run on the aux stream beside the analytic
 // and triangle-mesh kernels (FP32, latency-bound); the categories write disjoint slots.
 int launch_narrowphase(const World& w, FrameBuf& f, const StreamPair& sp, const NarrowShape& ns, cudaStream_t s) {
-    cudaMemsetAsync(f.cat_count, 0, 8 * sizeof(int), s);
+    cudaMemsetAsync(f.cat_count, 0, 10 * sizeof(int), s);
     k_classify<<<1216, 256, 0, s>>>(w, f);
     cudaEventRecord(sp.fork, s);
     cudaStreamWaitEvent(sp.aux, sp.fork, 0);
     k_convex_gjk<<<152 * ns.gjk_blocks_per_sm, 128, 0, sp.aux>>>(w, f);
     if (!ns.epa_full_only) {
-        if (ns.epa_lanes == 8) launch_convex_epa<8, 1>(w, f, ns.convex_blocks_per_sm, sp.aux);
-        else if (ns.epa_lanes == 16) launch_convex_epa<16, 1>(w, f, ns.convex_blocks_per_sm, sp.aux);
-        else if (ns.convex_warps == 1) launch_convex_epa<32, 1>(w, f, ns.convex_blocks_per_sm, sp.aux);
-        else if (ns.convex_warps == 2) launch_convex_epa<32, 2>(w, f, ns.convex_blocks_per_sm, sp.aux);
-        else launch_convex_epa<32, 3>(w, f, ns.convex_blocks_per_sm, sp.aux);
+        // epa_lanes 1: a lane per pair first, the grouped kernel (16 lanes) for the pairs
+        // that outgrow it
+        int src = 3;
+        if (ns.epa_lanes == 1) {
+            launch_convex_epa_flat(w, f, sp.aux);
+            src = 8;
+        }
+        if (ns.epa_lanes == 8) launch_convex_epa<8, 1>(w, f, ns.convex_blocks_per_sm, src, sp.aux);
+        else if (ns.epa_lanes == 16 || ns.epa_lanes == 1) launch_convex_epa<16, 1>(w, f, ns.convex_blocks_per_sm, src, sp.aux);
+        else if (ns.convex_warps == 1) launch_convex_epa<32, 1>(w, f, ns.convex_blocks_per_sm, src, sp.aux);
+        else if (ns.convex_warps == 2) launch_convex_epa<32, 2>(w, f, ns.convex_blocks_per_sm, src, sp.aux);
+        else launch_convex_epa<32, 3>(w, f, ns.convex_blocks_per_sm, src, sp.aux);
     }
     {
-        static bool attr_set = false;
-        if (!attr_set) {
-            cudaFuncSetAttribute(k_convex_epa_full, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(WarpPoly));
-            cudaFuncSetAttribute(k_convex_epa_full, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-            attr_set = true;
-        }
+        static bool done[kMaxDevices] = {};
+        set_smem_attrs((const void*)k_convex_epa_full, done, (int)sizeof(WarpPoly));
         // the full pass alone: as many blocks as shared memory lets reside
         k_convex_epa_full<<<ns.epa_full_only ? 152 * 16 : 152 * 4, 32, sizeof(WarpPoly), sp.aux>>>(w, f, ns.epa_full_only ? 3 : 6);
     }

@@ -397,7 +397,7 @@ struct VelRef {
 };
 
 // Constraint1D(W)::solve for one row (Constraint1D.cpp:54-127 / Constraint1DW.cpp:117-233)
-__device__ void row_solve(const World& w, Row& r, float h, bool warm, bool simd, const VelRef& vr) {
+__device__ void row_solve(const World& w, Row& r, float h, bool warm, bool simd, const VelRef vr) {
     int fl = r.flags;
     bool angf = fl & 2, soft = fl & 1, lim = fl & 4;
     float inv = r.angular1t.w;
@@ -492,7 +492,7 @@ __device__ void joint_presolve(const World& w, int j) {
             if (J.rowflags[k] == c_flag_order[fi]) row_presolve(w, R[k], J.simd != 0);
 }
 
-__device__ void joint_solve(const World& w, int j, float h, bool warm, const VelRef& vr) {
+__device__ void joint_solve(const World& w, int j, float h, bool warm, const VelRef vr) {
     JointDev& J = w.joints[j];
     Row* R = w.rows + j * kMaxRowsPerJoint;
     for (int fi = 0; fi < 6; ++fi)
@@ -590,7 +590,17 @@ __device__ void contact_presolve(const World& w, SHdr& H, SPt* P, float h) {
 // ContactConstraints::solve (src/ContactConstraints.cpp:33-124).  No other thread touches
 // the contact's bodies within its colour, so their velocities stay in registers from the
 // first point to the last; every value equals a reload after each point.
-__device__ void contact_solve(const SHdr& H, SPt* P, bool useBias, const VelRef& vr) {
+// The step is one dependent chain of up to eight rows, so it is written for latency:
+//   * the header and the velocity view come by value (a store through a record pointer
+//     then cannot alias them, and nothing is reloaded after it);
+//   * the records are read ahead of the chain (the normal rows' all at once, then the
+//     friction rows') and the accumulated impulses are written after the last row;
+//   * all four rows of each kind are evaluated and a row is kept only when it is live
+//     (the reference skips a row whose inverse effective mass is zero; a contact has
+//     fewer than four points), so the chain has no branches.  A live row's operations
+//     and their order are the reference's.  Branching on the point count instead costs
+//     registers that the solver kernels do not have.
+__device__ __noinline__ void contact_solve(const SHdr H, SPt* __restrict__ P, bool useBias, const VelRef vr) {
     const V3 n = ld3(H.n);
     const float friction = H.n.w;
     const float im0 = H.m.x, im1 = H.m.y;
@@ -599,50 +609,65 @@ __device__ void contact_solve(const SHdr& H, SPt* P, bool useBias, const VelRef&
     V3 v0 = {0, 0, 0}, w0 = {0, 0, 0}, v1 = {0, 0, 0}, w1 = {0, 0, 0};
     if (b0 >= 0) { v0 = vr.lv(b0); w0 = vr.lw(b0); }
     if (b1 >= 0) { v1 = vr.lv(b1); w1 = vr.lw(b1); }
+    // every normal record of the contact is read before the chain; rows past the
+    // contact's points read its first point and stay dead
+    float4 A[4], B[4], C[4], D[4];
+    int live[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const bool has = i < np;
+        const SPt* q = P + (has ? i : 0);
+        A[i] = q->a; B[i] = q->b; C[i] = q->c; D[i] = q->d;
+        live[i] = has ? __float_as_int(q->g.w) : 0;
+    }
     bool touched = false;
-    for (int i = 0; i < np; ++i) {
-        SPt& p = P[i];
-        if (!(__float_as_int(p.g.w) & 1)) continue;
-        V3 r0xn = ld3(p.a), r1xn = ld3(p.b);
+    float lamN[4], lamT[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const bool on = (live[i] & 1) != 0;
+        const V3 r0xn = ld3(A[i]), r1xn = ld3(B[i]);
         float rv = dot(-n, v0) + dot(-r0xn, w0) + dot(n, v1) + dot(r1xn, w1);
         float lambda;
-        if (soft) lambda = (rv + p.c.w) / p.d.w;
-        else lambda = (rv - p.b.w + (useBias ? p.c.w : 0.f)) * p.d.w;
-        float prev = p.a.w;
+        if (soft) lambda = (rv + C[i].w) / D[i].w;
+        else lambda = (rv - B[i].w + (useBias ? C[i].w : 0.f)) * D[i].w;
+        const float prev = A[i].w;
         float tot = prev + lambda;
         tot = fminG(tot, 0.f);
-        p.a.w = tot;
+        lamN[i] = on ? tot : prev;
         lambda = tot - prev;
-        if (b0 >= 0) {
-            v0 = v0 + lambda * im0 * n;
-            w0 = w0 + lambda * ld3(p.c);
-        }
-        if (b1 >= 0) {
-            v1 = v1 - lambda * im1 * n;
-            w1 = w1 - lambda * ld3(p.d);
-        }
-        touched = true;
+        const V3 nv0 = v0 + lambda * im0 * n, nw0 = w0 + lambda * ld3(C[i]);
+        const V3 nv1 = v1 - lambda * im1 * n, nw1 = w1 - lambda * ld3(D[i]);
+        if (on && b0 >= 0) { v0 = nv0; w0 = nw0; }
+        if (on && b1 >= 0) { v1 = nv1; w1 = nw1; }
+        touched |= on;
     }
-    for (int i = 0; i < np; ++i) {
-        SPt& p = P[i];
-        if (!(__float_as_int(p.g.w) & 2)) continue;
-        V3 t = ld3(p.e);
-        float lambda = p.f.w;
-        float limit = friction * p.a.w;
-        float prev = p.e.w;
+    float4 E[4], F[4], G[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int q = i < np ? i : 0;
+        E[i] = P[q].e; F[i] = P[q].f; G[i] = P[q].g;
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const bool on = (live[i] & 2) != 0;
+        const V3 t = ld3(E[i]);
+        float lambda = F[i].w;
+        const float limit = friction * lamN[i];
+        const float prev = E[i].w;
         float tot = prev + lambda;
         tot = clampG(tot, limit, -limit);
-        p.e.w = tot;
+        lamT[i] = tot;
         lambda = tot - prev;
-        if (b0 >= 0) {
-            v0 = v0 + lambda * im0 * t;
-            w0 = w0 + lambda * ld3(p.f);
-        }
-        if (b1 >= 0) {
-            v1 = v1 - lambda * im1 * t;
-            w1 = w1 - lambda * ld3(p.g);
-        }
-        touched = true;
+        const V3 nv0 = v0 + lambda * im0 * t, nw0 = w0 + lambda * ld3(F[i]);
+        const V3 nv1 = v1 - lambda * im1 * t, nw1 = w1 - lambda * ld3(G[i]);
+        if (on && b0 >= 0) { v0 = nv0; w0 = nw0; }
+        if (on && b1 >= 0) { v1 = nv1; w1 = nw1; }
+        touched |= on;
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        if (live[i] & 1) P[i].a.w = lamN[i];
+        if (live[i] & 2) P[i].e.w = lamT[i];
     }
     if (touched) {
         if (b0 >= 0) { vr.sv(b0, v0); vr.sw(b0, w0); }

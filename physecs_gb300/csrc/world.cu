@@ -397,8 +397,8 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
     PSX_TRY(W->alloc(f.pairs, f.pair_cap));
     PSX_TRY(W->alloc(f.n_pairs, 1));
     PSX_TRY(W->alloc(f.pair_cat, f.pair_cap));
-    PSX_TRY(W->alloc(f.cat_count, 8));
-    PSX_TRY(W->alloc(f.cat_list, 8 * (size_t)f.pair_cap));
+    PSX_TRY(W->alloc(f.cat_count, 10));
+    PSX_TRY(W->alloc(f.cat_list, 9 * (size_t)f.pair_cap));
     PSX_TRY(W->alloc(f.man_pair, f.pair_cap));
     PSX_TRY(W->alloc(f.man_tri, (size_t)f.tri_cap * kTriManifolds));
     PSX_TRY(W->alloc(f.pair_tslot, f.pair_cap));
@@ -578,7 +578,7 @@ psx_status psx::rt::apply_launch(psx_world* W, const psx_launch_config& c) {
     if (n.convex_warps < 1 || n.convex_warps > 3 || n.convex_blocks_per_sm < 1 || n.convex_blocks_per_sm > 32 ||
         !threads_ok(n.analytic_threads) || n.analytic_blocks_per_sm < 1 || n.analytic_blocks_per_sm > 64 ||
         !threads_ok(n.contacts_threads) || n.gjk_blocks_per_sm < 1 || n.gjk_blocks_per_sm > 16 ||
-        (n.epa_lanes != 8 && n.epa_lanes != 16 && n.epa_lanes != 32))
+        (n.epa_lanes != 1 && n.epa_lanes != 8 && n.epa_lanes != 16 && n.epa_lanes != 32))
         return fail(PSX_ERR_INVALID_ARG, "launch config out of range");
     int smem = W->solver_smem;
     if (c.solver_smem_kb) {
@@ -882,9 +882,11 @@ PSX_API psx_status psx_world_tune(psx_world* W, int32_t frames, psx_launch_confi
         knobs.push_back(k);
     }
     {   // EPA: lanes per pair, warps per block, blocks per SM (a SmallPoly per pair in shared
-        // memory; the registers allow about 28 warps per SM)
+        // memory; the registers allow about 28 warps per SM); 1: a lane per pair, with the
+        // grouped kernel's blocks for the pairs that outgrow it
         Knob k{1, {}};
-        const int cands[][3] = {{32, 1, 15}, {32, 1, 24}, {32, 1, 32}, {32, 2, 12}, {32, 3, 8}, {16, 1, 20}, {8, 1, 12}};
+        const int cands[][3] = {{32, 1, 15}, {32, 1, 24}, {32, 1, 32}, {32, 2, 12}, {32, 3, 8}, {16, 1, 20}, {8, 1, 12},
+                                {1, 1, 8}};
         for (const auto& c3 : cands) {
             psx_launch_config c{};
             c.epa_lanes = c3[0];

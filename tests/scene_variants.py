@@ -295,3 +295,21 @@ def mechanism_topology_ops(s, info):
         (28, 9, -1, [0.3, 8.0, 2.0, -8.0, 1.0 / 113.1, 1.0 / 4.07]),
         (33, 8, j["universal"][1], []),
     ]
+
+
+def scattered_scene(seed=53, n_dense=480, n_clumps=160):
+    """Bodies that are neighbours on the broadphase's Morton curve yet far apart: a dense
+    block of mixed bodies on a ground box, and clumps of three overlapping bodies scattered
+    over a 400 m cube.  Warps of the pair walk then take both coherent and scattered
+    leaves (the second kind is walked one lane at a time)."""
+    rng = scenes.SplitMix64(scenes.scene_seed(11, seed))
+    s = scenes.SceneData("scattered%d" % seed)
+    scenes._ground_box(s, (12.0, 0.5, 12.0))
+    pool = scenes._hull_pool(scenes.SplitMix64(scenes.scene_seed(11, 1 << 19)), count=4)
+    s.convex.extend(pool)
+    dense = scenes._jittered_grid(rng, 10, 5, 10, 1.5, [0.0, 1.5, 0.0])[:n_dense]
+    far = rng.uniform(3 * n_clumps, -200.0, 200.0).reshape(n_clumps, 3)
+    jitter = rng.uniform(9 * n_clumps, -0.4, 0.4).reshape(n_clumps, 3, 3)
+    clumps = (far[:, None, :] + jitter).reshape(-1, 3)
+    scenes._mixed_bodies(s, rng, np.concatenate([dense, clumps]), 0, pool)
+    return s.finalize()

@@ -12,6 +12,7 @@ import pytest
 
 from physecs_gb300 import scenes
 from tests.parity import compare_contacts, gpu_keys, pair_set, rel_state_diff
+from tests.scene_variants import scattered_scene
 
 pytestmark = pytest.mark.gpu
 
@@ -29,6 +30,7 @@ def _scenes():
         "chain": scenes.batch_scene(11, n_bodies=40, chain_prob=1.0),
         "heightfield": scenes.large_mixed(n_bodies=300, cells=32),
         "joints": scenes.joint_chains(n_chains=12, links=6),
+        "scattered": scattered_scene(),
     }
 
 
@@ -47,7 +49,7 @@ def _gpu(s, **kw):
     return World(s if isinstance(s, list) else [s], **kw)
 
 
-@pytest.mark.parametrize("name", ["pyramid", "mixed", "chain", "heightfield", "joints"])
+@pytest.mark.parametrize("name", ["pyramid", "mixed", "chain", "heightfield", "joints", "scattered"])
 def test_creation_bounds_bit_exact(all_scenes, name, gpu_lib, oracle_lib):
     s = all_scenes[name]
     g = _gpu(s)
@@ -60,7 +62,7 @@ def test_creation_bounds_bit_exact(all_scenes, name, gpu_lib, oracle_lib):
     assert np.array_equal(gb[order].view(np.uint32), ob.view(np.uint32))
 
 
-@pytest.mark.parametrize("name", ["pyramid", "mixed", "chain", "heightfield", "joints"])
+@pytest.mark.parametrize("name", ["pyramid", "mixed", "chain", "heightfield", "joints", "scattered"])
 def test_first_frame_pairs_and_manifolds(all_scenes, name, gpu_lib, oracle_lib):
     s = all_scenes[name]
     g = _gpu(s)
@@ -296,8 +298,10 @@ def test_launch_shapes_do_not_change_results(gpu_lib):
                                    contacts_threads=256, solver_smem_kb=100, gjk_blocks_per_sm=4, epa_lanes=32)),
               _gpu(ss, launch=dict(epa_lanes=16, convex_warps=1, convex_blocks_per_sm=4, large_threads=128)),
               _gpu(ss, launch=dict(epa_lanes=8, convex_warps=1, convex_blocks_per_sm=2, large_threads=256)),
-              _gpu(ss, launch=dict(epa_full_only=1, solver_threads_min=256))]
+              _gpu(ss, launch=dict(epa_full_only=1, solver_threads_min=256)),
+              _gpu(ss, launch=dict(epa_lanes=1, convex_blocks_per_sm=8))]
     assert [o.launch_config()["epa_lanes"] for o in others[:3]] == [32, 16, 8]
+    assert others[4].launch_config()["epa_lanes"] == 1
     assert others[3].launch_config()["epa_full_only"] == 1 and others[3].launch_config()["solver_threads_min"] == 256
     for f in range(8):
         a.step()
@@ -386,3 +390,41 @@ def test_body_io_through_pinned_and_pageable_arrays(gpu_lib):
     b.simulate_host(s.dt, sb)
     for k in st:
         assert np.array_equal(st[k].view(np.uint32), sb[k].view(np.uint32)), k
+
+
+def _hull_heavy(seed=5, n=400):
+    """Mostly convex hulls in a pile that starts interpenetrating (about 1800 manifolds on the
+    first frame, 180 by the twelfth): many overlapping convex pairs, shallow and deep."""
+    rng = scenes.SplitMix64(scenes.scene_seed(12, seed))
+    s = scenes.SceneData("hulls%d" % seed)
+    scenes._ground_box(s, (8.0, 0.5, 8.0))
+    pool = scenes._hull_pool(scenes.SplitMix64(scenes.scene_seed(12, 1 << 19)), count=8)
+    s.convex.extend(pool)
+    centers = scenes._jittered_grid(rng, 8, 7, 8, 1.1, [0.0, 1.2, 0.0])[:n]
+    scenes._mixed_bodies(s, rng, centers, 0, pool, mix=(0.1, 0.1, 0.2, 0.6))
+    return s.finalize()
+
+
+@pytest.mark.parametrize("lanes", [1, 8, 32])
+def test_epa_schedules_agree_with_the_oracle(lanes, gpu_lib, oracle_lib):
+    """EPA with a lane per pair (new faces built by the whole warp; pairs needing more than
+    12 steps handed to the grouped kernel), and with 8 or 32 lanes per pair: manifolds
+    from identical poses within the contract (in practice bit for bit) on a hull pile,
+    and the frames in lockstep with the oracle fed the GPU's contact order."""
+    s = _hull_heavy()
+    g = _gpu(s, launch=dict(epa_lanes=lanes, convex_blocks_per_sm=8), pairs_per_collider=32, manifolds_per_collider=16)
+    o = _oracle(s)
+    for f in range(1, 13):
+        g.step()
+        g.synchronize()
+        ids, gf, meta = g.contacts()
+        keys = gpu_keys(ids, meta)
+        o.set_contact_order(keys)
+        o.step()
+        assert o.order_error() == 0, "frame %d" % f
+        _, of = o.contacts()
+        worst = compare_contacts(keys, gf, o.contact_keys(), of)
+        assert worst <= TOL, "frame %d: manifolds differ by %g" % (f, worst)
+        d = rel_state_diff(g.read_bodies(), o.state())
+        assert d <= TOL, "frame %d: relative state difference %g" % (f, d)
+    assert g.counts()["error"] == 0
