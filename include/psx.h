@@ -155,7 +155,7 @@ typedef struct psx_world psx_world;
  * changes a result; 0 in a field keeps the default.  psx_world_tune picks them. */
 typedef struct psx_launch_config {
     int32_t convex_warps;            /* EPA: warps (pairs) per block, 1-3 (default 1) */
-    int32_t convex_blocks_per_sm;    /* EPA: blocks per SM in the grid (default 20) */
+    int32_t convex_blocks_per_sm;    /* EPA: blocks per SM in the grouped kernel's grid (default 8) */
     int32_t analytic_threads;        /* sphere/capsule/box pairs: threads per block, <= 256 (default 64) */
     int32_t analytic_blocks_per_sm;  /* (default 16) */
     int32_t contacts_threads;        /* convex contact generation: threads per block, <= 256 (default 64) */
@@ -164,7 +164,7 @@ typedef struct psx_launch_config {
                                       * velocities fit the cluster's shared memory), 2 the whole grid, one scene
                                       * after another (default: clusters when two or more scenes fit them) */
     int32_t gjk_blocks_per_sm;       /* GJK (one thread per convex pair): 128-thread blocks per SM, 1-16 (default 16) */
-    int32_t epa_lanes;               /* EPA: lanes per overlapping pair, 8, 16 or 32 (default 16); below 32 a block
+    int32_t epa_lanes;               /* EPA: lanes per overlapping pair, 1, 8, 16 or 32 (default 1); below 32 a block
                                       * is one warp holding 32 / epa_lanes pairs.  1: one lane per pair with the
                                       * warp's new faces built by all of its lanes, and 16 lanes per pair for the
                                       * pairs that need more than 12 steps */
@@ -488,6 +488,11 @@ PSX_API psx_status psx_world_trigger_events(psx_world* w, psx_trigger_event* out
  *              contact points, joint rows, simulated bodies, kernels queued since creation}
  * (per-frame values describe the last frame) */
 PSX_API psx_status psx_world_counts(psx_world* w, int32_t* counts);
+/* counts[4] = {convex-mesh pairs, of them overlapping after GJK (EPA runs on these), of
+ *             those the ones that outgrew the lane-per-pair EPA (12 steps), and of those
+ *             the ones that outgrew the grouped EPA (36 steps)} of the last frame; EPA
+ *             schedules that skip a tier report 0 for it */
+PSX_API psx_status psx_world_narrow_counts(psx_world* w, int32_t* counts);
 /* Inspection of the last frame (synchronises):
  *   pairs: {scene, entity0, collider0, entity1, collider1} per broadphase pair
  *   contacts: ids {scene, b0, b1, np | soft << 8, entity0, collider0, entity1, collider1} per

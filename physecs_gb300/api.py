@@ -30,7 +30,7 @@ EXPORTS = ["psx_world_create", "psx_world_destroy", "psx_world_step", "psx_world
            "psx_world_tune", "psx_world_launch_config", "psx_world_raycast", "psx_world_overlap",
            "psx_world_overlap_mtd", "psx_world_trigger_events", "psx_trimesh_build", "psx_world_update_trimesh",
            "psx_world_apply_deltas", "psx_world_move_characters", "psx_world_set_contact_filter",
-           "psx_world_set_can_collide", "psx_pin_host", "psx_unpin_host", "psx_world_set_wait_limit",
+           "psx_world_set_can_collide", "psx_world_narrow_counts", "psx_pin_host", "psx_unpin_host", "psx_world_set_wait_limit",
            "psx_world_set_joint_params", "psx_world_recreate"]
 
 _lib = None
@@ -90,6 +90,7 @@ def load():
     lib.psx_world_read_bodies_noalloc.argtypes = [vp, vp, vp, vp, vp]
     lib.psx_world_simulate_host.argtypes = [vp, C.c_float, vp, vp, vp, vp]
     lib.psx_world_counts.argtypes = [vp, vp]
+    lib.psx_world_narrow_counts.argtypes = [vp, vp]
     lib.psx_world_step_timed.argtypes = [vp, C.c_float, C.c_int32, vp, vp, vp]
     lib.psx_world_get_pairs.argtypes = [vp, vp, C.c_int32]
     lib.psx_world_get_pairs.restype = C.c_int32
@@ -270,6 +271,12 @@ class World:
         keys = ["bodies", "colliders", "dynamic", "joints", "scenes", "pairs", "manifolds", "error", "points", "rows",
                 "simulated", "kernels"]
         return dict(zip(keys, (int(v) for v in c)))
+
+    def narrow_counts(self):
+        """psx_world_narrow_counts: the last frame's convex pairs and the EPA tiers they reached."""
+        c = np.zeros(4, np.int32)
+        _check(load().psx_world_narrow_counts(self.h, _p(c)))
+        return dict(zip(["convex", "epa", "past_lane", "past_group"], (int(v) for v in c)))
 
     def pairs(self):
         n = self.counts()["pairs"]

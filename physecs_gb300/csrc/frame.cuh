@@ -165,7 +165,8 @@ struct NarrowShape {
     int analytic_threads, analytic_blocks_per_sm;
     int contacts_threads;
     int gjk_blocks_per_sm;                    // GJK: 128-thread blocks per SM
-    int epa_lanes;                            // EPA: lanes per pair (8, 16 or 32; below 32, one warp per block)
+    int epa_lanes;                            // EPA: lanes per pair (8, 16 or 32; below 32, one warp per block);
+                                              // 1: a lane per pair, 16 for the pairs that outgrow it
     int epa_full_only;                        // EPA: skip the small-polytope pass
 };
 int launch_narrowphase(const World& w, FrameBuf& f, const StreamPair& sp, const NarrowShape& ns, cudaStream_t s);

@@ -215,6 +215,56 @@ __device__ inline bool gjk(const Support& s0, const Support& s1, V3 startDir, Gj
     return gjkT(mk, startDir, s);
 }
 
+// ---- f32 shortcuts for f64 decisions
+//
+// The FP64 pipe is the narrowphase's bottleneck, and conversions between double and float
+// run on it too.  These helpers move float data through integer operations and settle a
+// sign test in f32 when the f32 value is clear of its error bound, falling back to the
+// reference's f64 expression otherwise, so every decision is the reference's.
+
+// float from a double by truncating the mantissa (exact when the double holds a float);
+// ok is cleared when the value lies outside the normal float range (zero is exact)
+__device__ __forceinline__ float f32_trunc(double x, bool& ok) {
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const unsigned sign = hi & 0x80000000u;
+    if (((hi & 0x7fffffffu) | lo) == 0u) return __uint_as_float(sign);
+    const int e = (int)((hi >> 20) & 0x7ffu) - 896;
+    ok &= e >= 1 && e <= 254;
+    return __uint_as_float(sign | ((unsigned)(e & 0xff) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29));
+}
+// the double holding float x (exact), from its bits
+__device__ __forceinline__ double f64_of(float x) {
+    const unsigned b = __float_as_uint(x);
+    const unsigned e = (b >> 23) & 0xffu;
+    if (e == 0u || e == 0xffu) return (double)x;   // zero, subnormal, infinity, NaN
+    const unsigned hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
+    return __hiloint2double((int)hi, (int)(b << 29));
+}
+// dot(n, v - p) > 0 in f32 for v and p that are floats: 1 or 0 when the f32 value is
+// further from zero than a bound on its distance from the f64 value (n truncated: 2^-23;
+// v - p, the products and the two sums rounded: 2^-24 each; the f64 evaluation's own
+// error is far below), -1 when undecided
+__device__ __forceinline__ int sees_face_f32(D3 n, V3 vf, V3 pf) {
+    bool ok = true;
+    const float nx = f32_trunc(n.x, ok), ny = f32_trunc(n.y, ok), nz = f32_trunc(n.z, ok);
+    if (!ok) return -1;
+    const float dx = vf.x - pf.x, dy = vf.y - pf.y, dz = vf.z - pf.z;
+    const float px = nx * dx, py = ny * dy, pz = nz * dz;
+    const float sv = (px + py) + pz;
+    const float bound = ((fabsf(px) + fabsf(py)) + fabsf(pz)) * 6.0e-7f;   // 10 * 2^-24 of the magnitudes
+    if (sv > bound) return 1;
+    if (sv < -bound) return 0;
+    return -1;
+}
+// EPA.h:71: does the face (normal n, vertex p) see the new vertex v; v and p hold floats
+__device__ __forceinline__ bool sees_face(D3 n, D3 v, V3 vf, D3 p) {
+    bool ok = true;
+    const V3 pf = {f32_trunc(p.x, ok), f32_trunc(p.y, ok), f32_trunc(p.z, ok)};
+    const int r = ok ? sees_face_f32(n, vf, pf) : -1;
+    if (r >= 0) return r != 0;
+    return dot(n, v - p) > 0;
+}
+
 // EPA.h:10-186 with fixed capacities (104 vertices = 4 + 100 iterations)
 constexpr int kEpaVerts = 104;
 constexpr int kEpaFaces = 216;

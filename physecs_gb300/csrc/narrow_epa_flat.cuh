@@ -44,11 +44,14 @@ struct FlatPoly {
 };
 
 __device__ __forceinline__ D3 fp_pos(const FlatPoly& P, int i, int s) {
-    return {(double)P.px[i][s], (double)P.py[i][s], (double)P.pz[i][s]};
+    return {f64_of(P.px[i][s]), f64_of(P.py[i][s]), f64_of(P.pz[i][s])};
 }
+__device__ __forceinline__ V3 fp_posf(const FlatPoly& P, int i, int s) { return {P.px[i][s], P.py[i][s], P.pz[i][s]}; }
 __device__ __forceinline__ D3 fp_n(const FlatPoly& P, int k, int s) { return {P.nx[k][s], P.ny[k][s], P.nz[k][s]}; }
+// the Minkowski point is stored as the f32 difference of the supports that made it
 __device__ __forceinline__ void fp_set_vertex(FlatPoly& P, int i, int s, const GjkVertex& v) {
-    P.px[i][s] = (float)v.pos.x; P.py[i][s] = (float)v.pos.y; P.pz[i][s] = (float)v.pos.z;
+    const V3 d = v.sp0 - v.sp1;
+    P.px[i][s] = d.x; P.py[i][s] = d.y; P.pz[i][s] = d.z;
     P.ax[i][s] = v.sp0.x; P.ay[i][s] = v.sp0.y; P.az[i][s] = v.sp0.z;
     P.bx[i][s] = v.sp1.x; P.by[i][s] = v.sp1.y; P.bz[i][s] = v.sp1.z;
 }
@@ -71,9 +74,15 @@ __device__ __forceinline__ void fp_make_face(FlatPoly& P, int s, int k, int a, i
 __device__ __forceinline__ bool fp_insert(FlatPoly& P, int s, int& nv, int& nf, int& nnew, const GjkVertex& v) {
     // visibility of every current face, as a bitset (faces are only ever swapped in from
     // the end, and a face swapped in has been looked at already)
+    const V3 vf = v.sp0 - v.sp1;   // v.pos exactly
     unsigned vis = 0;
-    for (int k = 0; k < nf; ++k)
-        if (dot(fp_n(P, k, s), v.pos - fp_pos(P, P.i0[k][s], s)) > 0) vis |= 1u << k;
+    for (int k = 0; k < nf; ++k) {
+        const int i = P.i0[k][s];
+        const D3 n = fp_n(P, k, s);
+        int r = sees_face_f32(n, vf, fp_posf(P, i, s));
+        if (r < 0) r = dot(n, v.pos - fp_pos(P, i, s)) > 0;
+        if (r) vis |= 1u << k;
+    }
     int ne = 0, n = nf;
     bool full = false;
     for (int k = nf - 1; k >= 0; --k) {
@@ -134,12 +143,12 @@ __device__ __forceinline__ void fp_closest_points(const FlatPoly& P, int s, int 
         if (d00) { vv = d20 / d00; u = 1.0f - vv; }
         else { vv = 0; u = 1.0; }
     }
-    const D3 a0 = {(double)P.ax[f0][s], (double)P.ay[f0][s], (double)P.az[f0][s]};
-    const D3 a1 = {(double)P.ax[f1][s], (double)P.ay[f1][s], (double)P.az[f1][s]};
-    const D3 a2 = {(double)P.ax[f2][s], (double)P.ay[f2][s], (double)P.az[f2][s]};
-    const D3 b0 = {(double)P.bx[f0][s], (double)P.by[f0][s], (double)P.bz[f0][s]};
-    const D3 b1 = {(double)P.bx[f1][s], (double)P.by[f1][s], (double)P.bz[f1][s]};
-    const D3 b2 = {(double)P.bx[f2][s], (double)P.by[f2][s], (double)P.bz[f2][s]};
+    const D3 a0 = {f64_of(P.ax[f0][s]), f64_of(P.ay[f0][s]), f64_of(P.az[f0][s])};
+    const D3 a1 = {f64_of(P.ax[f1][s]), f64_of(P.ay[f1][s]), f64_of(P.az[f1][s])};
+    const D3 a2 = {f64_of(P.ax[f2][s]), f64_of(P.ay[f2][s]), f64_of(P.az[f2][s])};
+    const D3 b0 = {f64_of(P.bx[f0][s]), f64_of(P.by[f0][s]), f64_of(P.bz[f0][s])};
+    const D3 b1 = {f64_of(P.bx[f1][s]), f64_of(P.by[f1][s]), f64_of(P.bz[f1][s])};
+    const D3 b2 = {f64_of(P.bx[f2][s]), f64_of(P.by[f2][s]), f64_of(P.bz[f2][s])};
     cp0 = f3(u * a0 + vv * a1 + ww * a2);
     cp1 = f3(u * b0 + vv * b1 + ww * b2);
 }

@@ -206,11 +206,14 @@ __device__ inline bool group_epa(const Support& s0, const Support& s1, const Gjk
 
         // ---- insert v (EPA.h:62-99)
         // visibility of every current face, as a bitset over the face index
+        const V3 vf = v.sp0 - v.sp1;   // v.pos exactly: it is this f32 difference, widened
+        unsigned mine = 0;
         for (int j = 0; j < nslots; ++j) {
             int k = gl + G * j;
-            bool vis = false;
-            if (k < nf) vis = dot(wp_n(P, k), v.pos - wp_pos(P, P.i0[k])) > 0;
-            unsigned m = g.ballot(vis);
+            if (k < nf && sees_face(wp_n(P, k), v.pos, vf, wp_pos(P, P.i0[k]))) mine |= 1u << j;
+        }
+        for (int j = 0; j < nslots; ++j) {
+            unsigned m = g.ballot((mine >> j) & 1u);
             if (gl == 0) {
                 const int bit = G * j;
                 if ((bit & 31) == 0) P.vis[bit >> 5] = m;
@@ -218,46 +221,63 @@ __device__ inline bool group_epa(const Support& s0, const Support& s1, const Gjk
             }
         }
         g.sync();
-        if (gl == 0) {
+        {
+            // The horizon in the reference's order: faces from last to first; each edge of a
+            // visible face cancels the latest matching reversed edge of the list (the list's
+            // last edge moves into its place) or is appended.  The group searches the list
+            // together and its first lane edits it, so every lane follows the same counts.
             int ne = 0, n = nf;
             bool full = false;
             for (int k = nf - 1; k >= 0; --k) {
                 if (!((P.vis[k >> 5] >> (k & 31)) & 1u)) continue;
-                int a[3] = {P.i0[k], P.i1[k], P.i2[k]}, b[3] = {P.i1[k], P.i2[k], P.i0[k]};
-                bool found[3] = {false, false, false};
+                const int a[3] = {P.i0[k], P.i1[k], P.i2[k]}, b[3] = {P.i1[k], P.i2[k], P.i0[k]};
+                bool found[3];
                 for (int j = 0; j < 3; ++j) {
-                    for (int m = ne - 1; m >= 0; --m) {
-                        if (P.e0[m] == b[j] && P.e1[m] == a[j]) {
-                            found[j] = true;
-                            P.e0[m] = P.e0[ne - 1]; P.e1[m] = P.e1[ne - 1]; --ne;
-                            break;
-                        }
+                    int hit = -1;
+                    for (int m = gl; m < ne; m += G)
+                        if (P.e0[m] == b[j] && P.e1[m] == a[j]) hit = m;
+                    hit = __reduce_max_sync(g.gm, hit);
+                    found[j] = hit >= 0;
+                    if (found[j]) {
+                        if (gl == 0) { P.e0[hit] = P.e0[ne - 1]; P.e1[hit] = P.e1[ne - 1]; }
+                        --ne;
+                        g.sync();
                     }
                 }
                 for (int j = 0; j < 3; ++j) {
                     if (found[j]) continue;
-                    if (ne < PT::kE) { P.e0[ne] = (unsigned char)a[j]; P.e1[ne] = (unsigned char)b[j]; ++ne; }
-                    else if (kSpill) full = true;
-                    else raise_err(err, ERR_EPA_CAPACITY);
+                    if (ne < PT::kE) {
+                        if (gl == 0) { P.e0[ne] = (unsigned char)a[j]; P.e1[ne] = (unsigned char)b[j]; }
+                        ++ne;
+                    } else if (kSpill) {
+                        full = true;
+                    } else if (gl == 0) {
+                        raise_err(err, ERR_EPA_CAPACITY);
+                    }
                 }
                 // remove face k: the last face moves into its slot
-                int l = n - 1;
-                P.nx[k] = P.nx[l]; P.ny[k] = P.ny[l]; P.nz[k] = P.nz[l]; P.fd[k] = P.fd[l];
-                P.i0[k] = P.i0[l]; P.i1[k] = P.i1[l]; P.i2[k] = P.i2[l];
+                const int l = n - 1;
+                if (gl == 0) {
+                    P.nx[k] = P.nx[l]; P.ny[k] = P.ny[l]; P.nz[k] = P.nz[l]; P.fd[k] = P.fd[l];
+                    P.i0[k] = P.i0[l]; P.i1[k] = P.i1[l]; P.i2[k] = P.i2[l];
+                }
                 --n;
+                g.sync();
             }
-            if (kSpill && (P.nv >= PT::kV || n + ne > PT::kF)) {
-                full = true;
-            } else if (P.nv >= PT::kV) {
-                raise_err(err, ERR_EPA_CAPACITY);
-                ne = 0;
-            } else {
-                wp_set_vertex(P, P.nv, v);
-                P.nv = P.nv + 1;
+            if (gl == 0) {
+                if (kSpill && (P.nv >= PT::kV || n + ne > PT::kF)) {
+                    full = true;
+                } else if (P.nv >= PT::kV) {
+                    raise_err(err, ERR_EPA_CAPACITY);
+                    ne = 0;
+                } else {
+                    wp_set_vertex(P, P.nv, v);
+                    P.nv = P.nv + 1;
+                }
+                P.ne = ne;
+                P.nf = n;
+                P.full = full;
             }
-            P.ne = ne;
-            P.nf = n;
-            P.full = full;
         }
         g.sync();
         if (kSpill && P.full) return false;

@@ -303,15 +303,17 @@ __global__ void __launch_bounds__(32 * WARPS, 1) k_convex_epa_flat(World w, Fram
             nf = P.nbase[lane] + nnew;
             nnew = 0;
             // the closest face, by the reference's scan: the running minimum is a float
+            // (compared as the double it widens to, kept beside it)
             float minDist = (float)DBL_MAX;
+            double minWide = (double)minDist;
             int fi = 0;
             for (int k = 0; k < nf; ++k) {
                 const double d = P.fd[k][lane];
-                if (d < minDist) { minDist = (float)d; fi = k; }
+                if (d < minWide) { minDist = (float)d; minWide = f64_of(minDist); fi = k; }
             }
             const D3 normal = fp_n(P, fi, lane);
             const GjkVertex v = mink(s0, s1, f3(normal));
-            if (dot(v.pos, normal) - minDist < (double)0.00001f) {
+            if (dot(v.pos, normal) - minWide < (double)0.00001f) {
                 V3 cp0, cp1;
                 fp_closest_points(P, lane, fi, cp0, cp1);
                 Manifold& m = f.man_pair[p];
@@ -433,11 +435,13 @@ int launch_narrowphase(const World& w, FrameBuf& f, const StreamPair& sp, const 
     cudaEventRecord(sp.fork, s);
     cudaStreamWaitEvent(sp.aux, sp.fork, 0);
     k_convex_gjk<<<152 * ns.gjk_blocks_per_sm, 128, 0, sp.aux>>>(w, f);
+    const bool flat = !ns.epa_full_only && ns.epa_lanes == 1;
     if (!ns.epa_full_only) {
         // epa_lanes 1: a lane per pair first, the grouped kernel (16 lanes) for the pairs
-        // that outgrow it
+        // that outgrow it.  (Generating the finished pairs' contacts on another stream
+        // beside the longer passes was measured slower: it takes SMs from them.)
         int src = 3;
-        if (ns.epa_lanes == 1) {
+        if (flat) {
             launch_convex_epa_flat(w, f, sp.aux);
             src = 8;
         }
@@ -463,7 +467,7 @@ int launch_narrowphase(const World& w, FrameBuf& f, const StreamPair& sp, const 
     const int kt = launch_triggers(w, f, s);
     cudaStreamWaitEvent(s, sp.join, 0);
     scan_exclusive_dev(f.pair_nman, f.pair_moff, f.n_pairs, f.pair_cap, f.n_man, f.scan_scratch, s);
-    return 2 + 8 + 3 + kt;
+    return 2 + 8 + 3 + kt + (flat ? 1 : 0) - (ns.epa_full_only ? 1 : 0);
 }
 
 }  // namespace psx

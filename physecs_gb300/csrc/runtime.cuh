@@ -73,7 +73,7 @@ struct psx_world {
     int* grid_scenes = nullptr;
     int grid_blocks = 0;
     int solver_smem = 0;             // dynamic shared memory per solver block (bytes)
-    psx::NarrowShape narrow{1, 20, 64, 16, 64, 16, 16, 0};   // launch shapes of the narrowphase kernels
+    psx::NarrowShape narrow{1, 8, 64, 16, 64, 16, 1, 0};   // launch shapes of the narrowphase kernels
     long long frames_run = 0;        // frames queued since creation
     int frame_kernels = 0;           // kernels in one frame
     int solver_smem_large = 0;       // the same for the 512-thread blocks of large scenes

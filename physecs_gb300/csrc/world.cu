@@ -1265,6 +1265,20 @@ PSX_API psx_status psx_world_counts(psx_world* W, int32_t* counts) {
     return PSX_OK;
 }
 
+PSX_API psx_status psx_world_narrow_counts(psx_world* W, int32_t* counts) {
+    if (W) cudaSetDevice(W->device);
+    if (!W || !counts) return fail(PSX_ERR_INVALID_ARG, "narrow counts");
+    PSX_CUDA(cudaStreamSynchronize(W->stream));
+    int c[10] = {};
+    PSX_CUDA(cudaMemcpy(c, W->f.cat_count, sizeof c, cudaMemcpyDeviceToHost));
+    const bool flat = W->narrow.epa_lanes == 1 && !W->narrow.epa_full_only;
+    counts[0] = c[1];
+    counts[1] = c[3];
+    counts[2] = flat ? c[8] : 0;
+    counts[3] = W->narrow.epa_full_only ? 0 : c[6];
+    return PSX_OK;
+}
+
 PSX_API int32_t psx_world_get_pairs(psx_world* W, int32_t* out, int32_t cap) {
     if (W) cudaSetDevice(W->device);
     if (!W) return -1;

@@ -405,10 +405,10 @@ def _hull_heavy(seed=5, n=400):
     return s.finalize()
 
 
-@pytest.mark.parametrize("lanes", [1, 8, 32])
+@pytest.mark.parametrize("lanes", [1, 8, 16, 32])
 def test_epa_schedules_agree_with_the_oracle(lanes, gpu_lib, oracle_lib):
     """EPA with a lane per pair (new faces built by the whole warp; pairs needing more than
-    12 steps handed to the grouped kernel), and with 8 or 32 lanes per pair: manifolds
+    12 steps handed to the grouped kernel), and with 8, 16 or 32 lanes per pair: manifolds
     from identical poses within the contract (in practice bit for bit) on a hull pile,
     and the frames in lockstep with the oracle fed the GPU's contact order."""
     s = _hull_heavy()
