@@ -5,6 +5,7 @@
 // manifolds) and src/GJK.h / src/EPA.h including their mixed precision (float
 // supports, double simplex and polytope).
 #pragma once
+#include <climits>
 #include "narrow_util.cuh"
 
 namespace psx {
@@ -239,6 +240,20 @@ __device__ __forceinline__ double f64_of(float x) {
     if (e == 0u || e == 0xffu) return (double)x;   // zero, subnormal, infinity, NaN
     const unsigned hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
     return __hiloint2double((int)hi, (int)(b << 29));
+}
+// A double as an integer with the same order (for doubles that compare equal, the same
+// integer: both zeros map to 0); a NaN maps above everything, so it is never below
+// another distance, as in the f64 comparison.
+__device__ __forceinline__ long long order_key(double x) {
+    const long long b = __double_as_longlong(x);
+    const long long mag = b & 0x7fffffffffffffffLL;
+    if (mag == 0) return 0;
+    if (mag > 0x7ff0000000000000LL) return LLONG_MAX;
+    return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
+}
+// the double of a key of a number (zero comes back as +0)
+__device__ __forceinline__ double key_value(long long k) {
+    return __longlong_as_double(k >= 0 ? k : (k ^ 0x7fffffffffffffffLL));
 }
 // dot(n, v - p) > 0 in f32 for v and p that are floats: 1 or 0 when the f32 value is
 // further from zero than a bound on its distance from the f64 value (n truncated: 2^-23;

@@ -25,7 +25,7 @@
 // Every support point of the polytope is a float (held as float in shared
 // memory, exactly); the Minkowski vertices, face normals and face distances are
 // held as doubles so that the face loops convert and recompute nothing.  The whole
-// polytope of one pair takes about 12.5 KB of shared memory.
+// polytope of one pair takes about 15 KB of shared memory.
 #pragma once
 #include <math_constants.h>
 #include "narrow_convex.cuh"
@@ -38,6 +38,8 @@ struct PolyT {
     static constexpr int kV = VC, kF = FC, kE = EC;
     double nx[FC], ny[FC], nz[FC];
     double fd[FC];                                  // face distance dot(v[i0], n), fixed at creation
+    long long fk[FC];                               // fd as an ordered integer (order_key)
+    float ff[FC];                                   // fd rounded to float
     double px[VC], py[VC], pz[VC];                  // Minkowski vertex
     float ax[VC], ay[VC], az[VC];                   // support point on shape 0
     float bx[VC], by[VC], bz[VC];                   // support point on shape 1
@@ -69,7 +71,10 @@ __device__ __forceinline__ void wp_set_face(PT& P, int slot, int i0, int i1, int
     double len = length(n);
     if (len) n = n / len;
     P.nx[slot] = n.x; P.ny[slot] = n.y; P.nz[slot] = n.z;
-    P.fd[slot] = dot(wp_pos(P, i0), n);
+    const double fd = dot(wp_pos(P, i0), n);
+    P.fd[slot] = fd;
+    P.fk[slot] = order_key(fd);
+    P.ff[slot] = (float)fd;
     P.i0[slot] = (unsigned char)i0; P.i1[slot] = (unsigned char)i1; P.i2[slot] = (unsigned char)i2;
 }
 
@@ -124,9 +129,12 @@ __device__ __noinline__ GjkVertex group_mink(const Support& s0, const Support& s
 }
 
 template <int G>
-__device__ __forceinline__ double group_min_d(double v, const Group<G>& g) {
+__device__ __forceinline__ long long group_min_key(long long v, const Group<G>& g) {
 #pragma unroll
-    for (int o = G / 2; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(g.gm, v, o, G));
+    for (int o = G / 2; o > 0; o >>= 1) {
+        const long long u = __shfl_xor_sync(g.gm, v, o, G);
+        v = u < v ? u : v;
+    }
     return v;
 }
 
@@ -166,13 +174,14 @@ __device__ inline bool group_epa(const Support& s0, const Support& s1, const Gjk
     for (int it = 0; it < 100; ++it) {
         const int nf = P.nf;
         const int nslots = (nf + G - 1) / G;   // face slots in use (group-uniform)
-        // smallest distance of this lane's faces
-        double dmin = CUDART_INF;
+        // smallest distance of this lane's faces (compared as ordered integers: the
+        // FP64 pipe is the scarce one)
+        long long kmin = LLONG_MAX;
         for (int j = 0; j < nslots; ++j) {
             int k = gl + G * j;
             if (k < nf) {
-                double d = P.fd[k];
-                if (d < dmin) dmin = d;
+                const long long kk = P.fk[k];
+                if (kk < kmin) kmin = kk;
             }
         }
         // Sequential rule: a face is taken when its distance is below the running
@@ -180,26 +189,25 @@ __device__ inline bool group_epa(const Support& s0, const Support& s1, const Gjk
         // at M = float(smallest distance); the first face whose distance rounds to
         // M takes it, and after that every face with distance < M takes over.
         minDist = (float)DBL_MAX;
-        double dstar = group_min_d<G>(dmin, g);
-        if (dstar < CUDART_INF) {
-            float M = (float)dstar;
+        kmin = group_min_key<G>(kmin, g);
+        const long long kinf = order_key(CUDART_INF);
+        if (kmin < kinf) {
+            const float M = (float)key_value(kmin);
+            const long long kM = order_key(f64_of(M));
             int first = 0x7fffffff, last = -1;
             for (int j = 0; j < nslots; ++j) {
                 int k = gl + G * j;
-                if (k < nf && k < first) {
-                    double d = P.fd[k];
-                    if ((float)d == M && d < CUDART_INF) first = k;
-                }
+                if (k < nf && k < first && P.ff[k] == M && P.fk[k] < kinf) first = k;
             }
             first = __reduce_min_sync(g.gm, first);
             for (int j = 0; j < nslots; ++j) {
                 int k = gl + G * j;
-                if (k < nf && k > first && P.fd[k] < (double)M) last = k;
+                if (k < nf && k > first && P.fk[k] < kM) last = k;
             }
             last = __reduce_max_sync(g.gm, last);
             fi = last >= 0 ? last : first;
             normal = wp_n(P, fi);
-            minDist = (float)P.fd[fi];
+            minDist = P.ff[fi];
         }
         GjkVertex v = group_mink<G>(s0, s1, f3(normal), g);
         if (dot(v.pos, normal) - minDist < (double)0.00001f) break;
@@ -259,6 +267,7 @@ __device__ inline bool group_epa(const Support& s0, const Support& s1, const Gjk
                 const int l = n - 1;
                 if (gl == 0) {
                     P.nx[k] = P.nx[l]; P.ny[k] = P.ny[l]; P.nz[k] = P.nz[l]; P.fd[k] = P.fd[l];
+                    P.fk[k] = P.fk[l]; P.ff[k] = P.ff[l];
                     P.i0[k] = P.i0[l]; P.i1[k] = P.i1[l]; P.i2[k] = P.i2[l];
                 }
                 --n;

@@ -199,7 +199,7 @@ __device__ __forceinline__ bool epa_pair(const World& w, FrameBuf& f, int t, PT&
 }
 
 // EPA for the overlapping pairs of list `src`: a group of G lanes per pair (32 / G pairs
-// per warp), WARPS warps per block, a SmallPoly (about 4.7 KB of dynamic shared memory)
+// per warp), WARPS warps per block, a SmallPoly (about 5.5 KB of dynamic shared memory)
 // per group.  Pairs that outgrow it go to the overflow list for k_convex_epa_full.
 template <int G, int WARPS>
 __global__ void __launch_bounds__(32 * WARPS) k_convex_epa(World w, FrameBuf f, int src) {
@@ -330,7 +330,7 @@ __global__ void __launch_bounds__(32 * WARPS, 1) k_convex_epa_flat(World w, Fram
     }
 }
 
-// EPA with the reference's full capacity, one warp and one WarpPoly (about 12.8 KB) per
+// EPA with the reference's full capacity, one warp and one WarpPoly (about 15 KB) per
 // block, over list `lst`: the pairs whose polytope outgrew SmallPoly (6), or every
 // overlapping pair (3) when the small pass is off.
 __global__ void __launch_bounds__(32) k_convex_epa_full(World w, FrameBuf f, int lst) {
