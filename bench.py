@@ -408,8 +408,9 @@ def run_serving(args, rank, world, local):
         reqs = [r for r in reqs if router.route(r[0].n_dynamic * r[1]) == rank]
     from physecs_gb300.desc import make_desc
     descs = [make_desc(s) for s, _ in reqs]          # the clients' packed requests
+    launch = json.loads(args.launch) if args.launch else SERVE_LAUNCH
     srv = Server(classes, mesh_pool=pool_scene, device=local if world > 1 else 0, hbm_budget=SERVE_HBM_BUDGET,
-                 launch=SERVE_LAUNCH)
+                 launch=launch)
     # saturated throughput: a permanent backlog keeps every fitting slot busy
     backlog = 2 * sum(c[1] for c in classes)   # enough waiting requests to keep every class busy
     _serve(srv, reqs, None, 3.0, backlog, descs)
@@ -429,7 +430,7 @@ def run_serving(args, rank, world, local):
         "config": {"workload": "serving: Poisson request stream at %.0f%% of saturated throughput, N log-uniform in "
                                "[8,%d] bodies, K uniform in [1,120] frames, dt=1/60, 4x8" % (100 * args.serve_load,
                                                                                              args.serve_max_bodies),
-                   "slot_classes": classes, "seconds": args.serve_seconds,
+                   "slot_classes": classes, "seconds": args.serve_seconds, "launch": launch,
                    "hbm_budget_gb": SERVE_HBM_BUDGET / 1e9, "device_gb": srv.device_bytes() / 1e9},
         "p50_ms": float(np.percentile(fl, 50)), "p99_ms": float(np.percentile(fl, 99)),
         "request_p50_ms": float(np.percentile(rl, 50)) if len(rl) else None,

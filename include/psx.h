@@ -171,9 +171,10 @@ typedef struct psx_launch_config {
     int32_t solver_threads_min;      /* smallest solver block: 64 (scenes up to 96 dynamic bodies on 64 threads, up to
                                       * 384 on 128), 128 or 256 (default: 64 for worlds of more block scenes than
                                       * two per SM, else 256) */
-    int32_t epa_full_only;           /* 1: EPA with the full polytope only (lowest latency for the slowest pair);
-                                      * 2: a small polytope first, the full one for the pairs that outgrow it
-                                      * (highest throughput; default) */
+    int32_t epa_full_only;           /* 1: no grouped small-polytope pass: the pairs go to the full polytope
+                                      * directly, or with epa_lanes 1 after the lane-per-pair pass (lowest latency
+                                      * for the slowest pair); 2: the grouped pass between them (highest
+                                      * throughput; default) */
     int32_t large_threads;           /* block scenes above 1024 dynamic bodies: threads per block, 128 (four blocks
                                       * an SM), 256 (two) or 512 (one, with the most shared memory; default) */
 } psx_launch_config;

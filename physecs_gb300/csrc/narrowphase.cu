@@ -435,16 +435,14 @@ int launch_narrowphase(const World& w, FrameBuf& f, const StreamPair& sp, const 
     cudaEventRecord(sp.fork, s);
     cudaStreamWaitEvent(sp.aux, sp.fork, 0);
     k_convex_gjk<<<152 * ns.gjk_blocks_per_sm, 128, 0, sp.aux>>>(w, f);
-    const bool flat = !ns.epa_full_only && ns.epa_lanes == 1;
+    // epa_lanes 1: a lane per pair first; the pairs that outgrow it go to the grouped
+    // kernel (16 lanes), or with epa_full_only straight to the full polytope.
+    // (Generating the finished pairs' contacts on another stream beside the longer passes
+    // was measured slower: it takes SMs from them.)
+    const bool flat = ns.epa_lanes == 1;
+    if (flat) launch_convex_epa_flat(w, f, sp.aux);
     if (!ns.epa_full_only) {
-        // epa_lanes 1: a lane per pair first, the grouped kernel (16 lanes) for the pairs
-        // that outgrow it.  (Generating the finished pairs' contacts on another stream
-        // beside the longer passes was measured slower: it takes SMs from them.)
-        int src = 3;
-        if (flat) {
-            launch_convex_epa_flat(w, f, sp.aux);
-            src = 8;
-        }
+        const int src = flat ? 8 : 3;
         if (ns.epa_lanes == 8) launch_convex_epa<8, 1>(w, f, ns.convex_blocks_per_sm, src, sp.aux);
         else if (ns.epa_lanes == 16 || ns.epa_lanes == 1) launch_convex_epa<16, 1>(w, f, ns.convex_blocks_per_sm, src, sp.aux);
         else if (ns.convex_warps == 1) launch_convex_epa<32, 1>(w, f, ns.convex_blocks_per_sm, src, sp.aux);
@@ -455,7 +453,8 @@ int launch_narrowphase(const World& w, FrameBuf& f, const StreamPair& sp, const 
         static bool done[kMaxDevices] = {};
         set_smem_attrs((const void*)k_convex_epa_full, done, (int)sizeof(WarpPoly));
         // the full pass alone: as many blocks as shared memory lets reside
-        k_convex_epa_full<<<ns.epa_full_only ? 152 * 16 : 152 * 4, 32, sizeof(WarpPoly), sp.aux>>>(w, f, ns.epa_full_only ? 3 : 6);
+        const int lst = ns.epa_full_only ? (flat ? 8 : 3) : 6;
+        k_convex_epa_full<<<ns.epa_full_only && !flat ? 152 * 16 : 152 * 4, 32, sizeof(WarpPoly), sp.aux>>>(w, f, lst);
     }
     k_convex_contacts<<<1216 * 128 / ns.contacts_threads, ns.contacts_threads, 0, sp.aux>>>(w, f);
     cudaEventRecord(sp.join, sp.aux);

@@ -1271,7 +1271,7 @@ PSX_API psx_status psx_world_narrow_counts(psx_world* W, int32_t* counts) {
     PSX_CUDA(cudaStreamSynchronize(W->stream));
     int c[10] = {};
     PSX_CUDA(cudaMemcpy(c, W->f.cat_count, sizeof c, cudaMemcpyDeviceToHost));
-    const bool flat = W->narrow.epa_lanes == 1 && !W->narrow.epa_full_only;
+    const bool flat = W->narrow.epa_lanes == 1;
     counts[0] = c[1];
     counts[1] = c[3];
     counts[2] = flat ? c[8] : 0;

@@ -405,14 +405,16 @@ def _hull_heavy(seed=5, n=400):
     return s.finalize()
 
 
-@pytest.mark.parametrize("lanes", [1, 8, 16, 32])
-def test_epa_schedules_agree_with_the_oracle(lanes, gpu_lib, oracle_lib):
+@pytest.mark.parametrize("lanes,full_only", [(1, 2), (1, 1), (8, 2), (16, 2), (16, 1), (32, 2)])
+def test_epa_schedules_agree_with_the_oracle(lanes, full_only, gpu_lib, oracle_lib):
     """EPA with a lane per pair (new faces built by the whole warp; pairs needing more than
-    12 steps handed to the grouped kernel), and with 8, 16 or 32 lanes per pair: manifolds
+    12 steps handed to the grouped kernel, or with full_only 1 to the full polytope), and
+    with 8, 16 or 32 lanes per pair (full_only 1: the full polytope alone): manifolds
     from identical poses within the contract (in practice bit for bit) on a hull pile,
     and the frames in lockstep with the oracle fed the GPU's contact order."""
     s = _hull_heavy()
-    g = _gpu(s, launch=dict(epa_lanes=lanes, convex_blocks_per_sm=8), pairs_per_collider=32, manifolds_per_collider=16)
+    g = _gpu(s, launch=dict(epa_lanes=lanes, epa_full_only=full_only, convex_blocks_per_sm=8), pairs_per_collider=32,
+             manifolds_per_collider=16)
     o = _oracle(s)
     for f in range(1, 13):
         g.step()
@@ -430,4 +432,5 @@ def test_epa_schedules_agree_with_the_oracle(lanes, gpu_lib, oracle_lib):
         nc = g.narrow_counts()
         assert nc["convex"] >= nc["epa"] >= max(nc["past_lane"], nc["past_group"]) and nc["past_group"] >= 0
         assert nc["epa"] > 0 and (nc["past_lane"] >= nc["past_group"] if lanes == 1 else nc["past_lane"] == 0)
+        assert full_only == 2 or nc["past_group"] == 0
     assert g.counts()["error"] == 0
