@@ -211,6 +211,7 @@ PSX_API psx_status psx_server_create(const psx_server_opts* o, psx_server** out)
     // outgrows it is solved twice)
     psx_launch_config latency{};
     latency.epa_full_only = 1;
+    latency.epa_lanes = 16;   // not the lane-per-pair pass: its one block per SM suits full frames
     wo.launch = o->launch ? o->launch : &latency;
     psx_world* W = nullptr;
     psx_status st = psx_world_create(descs.data(), n_slots, &wo, &W);
