@@ -63,6 +63,8 @@ struct FrameBuf {
                           // has taken so far
     int* cat_list;        // [9 * pair_cap]: the pairs of lists 0-8
     Manifold* man_pair;   // one slot per pair (analytic / convex categories)
+    unsigned char* epa_save;   // polytopes handed from one EPA pass to the next (epa_save_bytes())
+    int lane_saves, group_saves;   // how many of them the lane-per-pair and grouped passes may hand over
     int tri_cap;          // triangle-mesh pair slots
     Manifold* man_tri;    // kTriManifolds slots per triangle-mesh pair slot
     int* pair_tslot;      // triangle-mesh slot of a pair
@@ -170,6 +172,8 @@ struct NarrowShape {
     int epa_full_only;                        // EPA: skip the small-polytope pass
 };
 int launch_narrowphase(const World& w, FrameBuf& f, const StreamPair& sp, const NarrowShape& ns, cudaStream_t s);
+void epa_save_caps(int pair_cap, int& lane, int& group);
+size_t epa_save_bytes(int lane, int group);
 // trigger pairs of this frame: overlap tests, enter and exit events, set swap (query.cu)
 int launch_triggers(const World& w, FrameBuf& f, cudaStream_t s);
 int launch_contacts(const World& w, FrameBuf& f, cudaStream_t s);

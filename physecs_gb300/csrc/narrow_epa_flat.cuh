@@ -15,11 +15,12 @@
 // four initial faces join the same pool.
 //
 // The polytope of a pair lives in shared memory with room for 16 vertices (12 steps;
-// about 97% of the pairs need fewer).  A pair that would outgrow it is handed over
-// untouched to the grouped EPA of narrow_warp.cuh (its GJK simplex is still in the
-// pair's manifold slot).
+// about 96.5% of the pairs need fewer).  A pair that would outgrow it is handed to the
+// grouped EPA of narrow_warp.cuh with its polytope, which goes on from the same step;
+// in the rare case that the room runs out part way through a step, the grouped pass
+// starts again from the GJK simplex, still in the pair's manifold slot.
 #pragma once
-#include "narrow_convex.cuh"
+#include "narrow_warp.cuh"
 
 namespace psx {
 
@@ -67,11 +68,16 @@ __device__ __forceinline__ void fp_make_face(FlatPoly& P, int s, int k, int a, i
     P.i0[k][s] = (unsigned char)a; P.i1[k][s] = (unsigned char)b; P.i2[k][s] = (unsigned char)c;
 }
 
+// the polytope handed to the grouped pass when a lane's pair outgrows its room
+using LaneSave = PolySave<kTV, kTF>;
+
 // One EPA step's polytope update for slot s (EPA.h:62-99): the faces that see v are
 // removed (each replaced by the current last face), their boundary edges collected in the
-// reference's order, v appended, and one new face per edge queued.  false: the polytope
-// would outgrow its room (nothing usable is left; the pair is handed over).
-__device__ __forceinline__ bool fp_insert(FlatPoly& P, int s, int& nv, int& nf, int& nnew, const GjkVertex& v) {
+// reference's order, v appended, and one new face per edge queued.  1: done; 0: no room
+// for v, the polytope untouched (it can be handed over as it stands); -1: the polytope
+// outgrew its room part way (the next pass starts again from the simplex).
+__device__ __forceinline__ int fp_insert(FlatPoly& P, int s, int& nv, int& nf, int& nnew, const GjkVertex& v) {
+    if (nv >= kTV) return 0;
     // visibility of every current face, as a bitset (faces are only ever swapped in from
     // the end, and a face swapped in has been looked at already)
     const V3 vf = v.sp0 - v.sp1;   // v.pos exactly
@@ -111,7 +117,7 @@ __device__ __forceinline__ bool fp_insert(FlatPoly& P, int s, int& nv, int& nf, 
         P.i0[k][s] = P.i0[l][s]; P.i1[k][s] = P.i1[l][s]; P.i2[k][s] = P.i2[l][s];
         --n;
     }
-    if (full || nv >= kTV || n + ne > kTF) return false;
+    if (full || n + ne > kTF) return -1;
     fp_set_vertex(P, nv, s, v);
     const int vi = nv++;
     for (int m = 0; m < ne; ++m) {
@@ -120,7 +126,24 @@ __device__ __forceinline__ bool fp_insert(FlatPoly& P, int s, int& nv, int& nf, 
     P.nbase[s] = n;
     nf = n;
     nnew = ne;
-    return true;
+    return 1;
+}
+
+// Slot s's polytope (nv vertices, nf faces) into a save record.
+__device__ __forceinline__ void fp_save(const FlatPoly& P, int s, int nv, int nf, LaneSave& out) {
+    for (int i = 0; i < nv; ++i) {
+        float* q = out.v[i];
+        q[0] = P.px[i][s]; q[1] = P.py[i][s]; q[2] = P.pz[i][s];
+        q[3] = P.ax[i][s]; q[4] = P.ay[i][s]; q[5] = P.az[i][s];
+        q[6] = P.bx[i][s]; q[7] = P.by[i][s]; q[8] = P.bz[i][s];
+    }
+    for (int k = 0; k < nf; ++k) {
+        double* q = out.n[k];
+        q[0] = P.nx[k][s]; q[1] = P.ny[k][s]; q[2] = P.nz[k][s]; q[3] = P.fd[k][s];
+        out.idx[k][0] = P.i0[k][s]; out.idx[k][1] = P.i1[k][s]; out.idx[k][2] = P.i2[k][s];
+    }
+    out.nv = nv;
+    out.nf = nf;
 }
 
 // Closest points on the closest face (EPA.h:101-143); the projection adds the face

@@ -54,6 +54,19 @@ using WarpPoly = PolyT<kEpaVerts, kEpaFaces, kEpaEdges>;
 // and a pair that outgrows it is solved again with WarpPoly
 using SmallPoly = PolyT<40, 76, 40>;
 
+// A polytope handed from one EPA pass to the next, taken at the start of a step (before
+// the step's closest face is chosen), so that the next pass goes on from that step
+// instead of starting again from the simplex.  nv == 0: nothing handed over.  Vertices
+// are floats (they hold floats exactly).
+template <int VC, int FC>
+struct PolySave {
+    static constexpr int kV = VC, kF = FC;
+    int nv, nf;
+    float v[VC][9];                                 // Minkowski point, support on shape 0, on shape 1
+    double n[FC][4];                                // normal and distance
+    unsigned char idx[FC][3];
+};
+
 template <class PT>
 __device__ __forceinline__ D3 wp_pos(const PT& P, int i) { return {P.px[i], P.py[i], P.pz[i]}; }
 template <class PT>
@@ -143,35 +156,58 @@ __device__ __forceinline__ long long group_min_key(long long v, const Group<G>& 
 // the call returns false (nothing is produced; the caller solves the pair again with a
 // larger polytope); without, the capacity error is raised and the walk goes on
 // truncated, as it can only with the reference's own 100-iteration room exhausted.
-template <int G, class PT, bool kSpill>
-__device__ inline bool group_epa(const Support& s0, const Support& s1, const GjkSimplex& s, V3& nrm, V3& cp0, V3& cp1,
-                                 PT& P, const Group<G>& g, int* err) {
+template <int G, class PT, bool kSpill, class RS>
+__device__ inline int group_epa(const Support& s0, const Support& s1, const GjkSimplex& s, V3& nrm, V3& cp0, V3& cp1,
+                                PT& P, const Group<G>& g, int* err, const RS* resume) {
     const int gl = g.gl;
-    if (gl == 0) {
-        for (int i = 0; i < 4; ++i) wp_set_vertex(P, i, s.v[i]);
-        P.nv = 4;
-    }
-    g.sync();
-    D3 n0 = cross(s.v[0].pos - s.v[1].pos, s.v[2].pos - s.v[1].pos);
-    bool flip = dot(s.v[3].pos - s.v[0].pos, n0) < 0;
-    if (gl < 4) {
-        // EPA.h initial tetrahedron, wound so that every normal points outwards
-        int t0, t1, t2;
-        switch (gl) {
-            case 0: t0 = 0; t1 = flip ? 1 : 2; t2 = flip ? 2 : 1; break;
-            case 1: t0 = 3; t1 = flip ? 1 : 2; t2 = 0; break;
-            case 2: t0 = 3; t1 = flip ? 2 : 1; t2 = flip ? 1 : 2; break;
-            default: t0 = 3; t1 = 0; t2 = flip ? 2 : 1; break;
+    int it0 = 0;
+    if (resume) {
+        // the polytope of an earlier pass, as it stood at the start of step nv - 4
+        static_assert(RS::kV <= PT::kV && RS::kF <= PT::kF, "a handed-over polytope fits");
+        const int nv = resume->nv, nf = resume->nf;
+        for (int i = gl; i < nv; i += G) {
+            const float* q = resume->v[i];
+            P.px[i] = f64_of(q[0]); P.py[i] = f64_of(q[1]); P.pz[i] = f64_of(q[2]);
+            P.ax[i] = q[3]; P.ay[i] = q[4]; P.az[i] = q[5];
+            P.bx[i] = q[6]; P.by[i] = q[7]; P.bz[i] = q[8];
         }
-        wp_set_face(P, gl, t0, t1, t2);
+        for (int k = gl; k < nf; k += G) {
+            const double* q = resume->n[k];
+            P.nx[k] = q[0]; P.ny[k] = q[1]; P.nz[k] = q[2];
+            P.fd[k] = q[3]; P.fk[k] = order_key(q[3]); P.ff[k] = (float)q[3];
+            P.i0[k] = resume->idx[k][0]; P.i1[k] = resume->idx[k][1]; P.i2[k] = resume->idx[k][2];
+        }
+        if (gl == 0) { P.nv = nv; P.nf = nf; }
+        it0 = nv - 4;
+        g.sync();
     }
-    if (gl == 0) P.nf = 4;
-    g.sync();
+    if (!resume) {   // EPA.h initial tetrahedron from the simplex
+        if (gl == 0) {
+            for (int i = 0; i < 4; ++i) wp_set_vertex(P, i, s.v[i]);
+            P.nv = 4;
+        }
+        g.sync();
+        D3 n0 = cross(s.v[0].pos - s.v[1].pos, s.v[2].pos - s.v[1].pos);
+        bool flip = dot(s.v[3].pos - s.v[0].pos, n0) < 0;
+        if (gl < 4) {
+            // EPA.h initial tetrahedron, wound so that every normal points outwards
+            int t0, t1, t2;
+            switch (gl) {
+                case 0: t0 = 0; t1 = flip ? 1 : 2; t2 = flip ? 2 : 1; break;
+                case 1: t0 = 3; t1 = flip ? 1 : 2; t2 = 0; break;
+                case 2: t0 = 3; t1 = flip ? 2 : 1; t2 = flip ? 1 : 2; break;
+                default: t0 = 3; t1 = 0; t2 = flip ? 2 : 1; break;
+            }
+            wp_set_face(P, gl, t0, t1, t2);
+        }
+        if (gl == 0) P.nf = 4;
+        g.sync();
+    }
 
     float minDist = 0;
     D3 normal = {0, 0, 0};
     int fi = 0;
-    for (int it = 0; it < 100; ++it) {
+    for (int it = it0; it < 100; ++it) {
         const int nf = P.nf;
         const int nslots = (nf + G - 1) / G;   // face slots in use (group-uniform)
         // smallest distance of this lane's faces (compared as ordered integers: the
@@ -213,6 +249,9 @@ __device__ inline bool group_epa(const Support& s0, const Support& s1, const Gjk
         if (dot(v.pos, normal) - minDist < (double)0.00001f) break;
 
         // ---- insert v (EPA.h:62-99)
+        // no room for v: hand the polytope over as it stands (the next pass redoes this
+        // step's search and support, with the same results)
+        if (kSpill && P.nv >= PT::kV) return 0;
         // visibility of every current face, as a bitset over the face index
         const V3 vf = v.sp0 - v.sp1;   // v.pos exactly: it is this f32 difference, widened
         unsigned mine = 0;
@@ -289,7 +328,7 @@ __device__ inline bool group_epa(const Support& s0, const Support& s1, const Gjk
             }
         }
         g.sync();
-        if (kSpill && P.full) return false;
+        if (kSpill && P.full) return -1;
         const int ne = P.ne, nbase = P.nf, vi = P.nv - 1;
         for (int m = gl; m < ne; m += G) {
             int slot = nbase + m;
@@ -329,7 +368,29 @@ __device__ inline bool group_epa(const Support& s0, const Support& s1, const Gjk
     cp1 = f3(u * b0 + vv * b1 + ww * b2);
     g.sync();
     nrm = f3(normal);
-    return true;
+    return 1;
+}
+
+// The group's polytope into a save record (all lanes of the group take part).
+template <int G, class PT, class RS>
+__device__ inline void group_save(const PT& P, RS& out, const Group<G>& g) {
+    const int nv = P.nv, nf = P.nf;
+    if (nv > RS::kV || nf > RS::kF) {   // cannot happen for the sizes in use; start over then
+        if (g.gl == 0) out.nv = 0;
+        return;
+    }
+    for (int i = g.gl; i < nv; i += G) {
+        float* q = out.v[i];
+        q[0] = (float)P.px[i]; q[1] = (float)P.py[i]; q[2] = (float)P.pz[i];
+        q[3] = P.ax[i]; q[4] = P.ay[i]; q[5] = P.az[i];
+        q[6] = P.bx[i]; q[7] = P.by[i]; q[8] = P.bz[i];
+    }
+    for (int k = g.gl; k < nf; k += G) {
+        double* q = out.n[k];
+        q[0] = P.nx[k]; q[1] = P.ny[k]; q[2] = P.nz[k]; q[3] = P.fd[k];
+        out.idx[k][0] = P.i0[k]; out.idx[k][1] = P.i1[k]; out.idx[k][2] = P.i2[k];
+    }
+    if (g.gl == 0) { out.nv = nv; out.nf = nf; }
 }
 
 }  // namespace psx

@@ -7,6 +7,7 @@
 // scan / compact pass produces the manifold list in pair order, so the output is
 // deterministic.  Pair geometry follows src/Physecs.cpp:188-213: collider world
 // pose = body pose composed with the collider's local pose.
+#include <algorithm>
 #include "frame.cuh"
 #include "narrow_tri.cuh"
 #include "narrow_warp.cuh"
@@ -169,11 +170,28 @@ __global__ void __launch_bounds__(128, 4) k_convex_gjk(World w, FrameBuf f) {
     }
 }
 
-// EPA for one overlapping pair, from the simplex GJK kept in its manifold slot; the
-// pair's normal and closest points replace the simplex there.  false: the polytope
-// outgrew P (kSpill), nothing was written.
-template <int G, class PT, bool kSpill>
-__device__ __forceinline__ bool epa_pair(const World& w, FrameBuf& f, int t, PT& P, const Group<G>& g) {
+// Polytopes handed between the EPA passes: the lane-per-pair pass's (LaneSave, the first
+// f.lane_saves of them a frame) and the grouped pass's (GroupSave, the first
+// f.group_saves), each by its position in the list of pairs handed over.  Pairs past
+// those counts start again from the simplex.  About 3.5 % of the overlapping pairs go on
+// from the lane pass and a few in 10^4 from the grouped one.
+using GroupSave = PolySave<SmallPoly::kV, SmallPoly::kF>;
+__device__ __forceinline__ LaneSave* lane_saves(const FrameBuf& f) { return reinterpret_cast<LaneSave*>(f.epa_save); }
+__device__ __forceinline__ GroupSave* group_saves(const FrameBuf& f) {
+    return reinterpret_cast<GroupSave*>(f.epa_save + sizeof(LaneSave) * (size_t)f.lane_saves);
+}
+void epa_save_caps(int pair_cap, int& lane, int& group) {
+    lane = std::min(32768, std::max(256, pair_cap / 16));
+    group = std::min(1024, std::max(64, pair_cap / 1024));
+}
+size_t epa_save_bytes(int lane, int group) { return sizeof(LaneSave) * (size_t)lane + sizeof(GroupSave) * (size_t)group; }
+
+// EPA for one overlapping pair, from the simplex GJK kept in its manifold slot or from a
+// handed-over polytope (resume); the pair's normal and closest points replace the
+// simplex there.  1: done; 0 / -1: the polytope outgrew P (kSpill) before / part way
+// through a step, nothing was written.
+template <int G, class PT, bool kSpill, class RS>
+__device__ __forceinline__ int epa_pair(const World& w, FrameBuf& f, int t, PT& P, const Group<G>& g, const RS* resume) {
     const int p = f.cat_list[f.pair_cap + t];
     V3 pos0, pos1;
     Q4 or0, or1;
@@ -189,13 +207,14 @@ __device__ __forceinline__ bool epa_pair(const World& w, FrameBuf& f, int t, PT&
         s.v[i] = {d3(sa - sb), sa, sb};
     }
     V3 nrm, c0, c1;
-    if (!group_epa<G, PT, kSpill>(a, b, s, nrm, c0, c1, P, g, w.err)) return false;   // ends with a group barrier
+    const int r = group_epa<G, PT, kSpill>(a, b, s, nrm, c0, c1, P, g, w.err, resume);   // ends with a group barrier
+    if (r <= 0) return r;
     if (g.gl == 0) {
         m.n = st4(nrm);
         m.p0[0] = st4(c0);
         m.p1[0] = st4(c1);
     }
-    return true;
+    return 1;
 }
 
 // EPA for the overlapping pairs of list `src`: a group of G lanes per pair (32 / G pairs
@@ -211,8 +230,22 @@ __global__ void __launch_bounds__(32 * WARPS) k_convex_epa(World w, FrameBuf f, 
     const int n = f.cat_count[src];
     for (int h = (blockIdx.x * WARPS + wid) * GPW + lane / G; h < n; h += gridDim.x * WARPS * GPW) {
         const int t = f.cat_list[src * (size_t)f.pair_cap + h];
-        if (!epa_pair<G, SmallPoly, true>(w, f, t, P, g) && g.gl == 0)
-            f.cat_list[6 * (size_t)f.pair_cap + atomicAdd(&f.cat_count[6], 1)] = t;
+        const LaneSave* rs = nullptr;
+        if (src == 8 && h < f.lane_saves && lane_saves(f)[h].nv > 0) rs = &lane_saves(f)[h];
+        const int r = epa_pair<G, SmallPoly, true>(w, f, t, P, g, rs);
+        if (r <= 0) {   // on to the full polytope, with this one when it is whole
+            int h6 = 0;
+            if (g.gl == 0) {
+                h6 = atomicAdd(&f.cat_count[6], 1);
+                f.cat_list[6 * (size_t)f.pair_cap + h6] = t;
+            }
+            h6 = __shfl_sync(g.gm, h6, g.gb);
+            if (h6 < f.group_saves) {
+                if (r == 0) group_save<G>(P, group_saves(f)[h6], g);
+                else if (g.gl == 0) group_saves(f)[h6].nv = 0;
+            }
+            g.sync();
+        }
     }
 }
 
@@ -321,9 +354,18 @@ __global__ void __launch_bounds__(32 * WARPS, 1) k_convex_epa_flat(World w, Fram
                 m.p0[0] = st4(cp0);
                 m.p1[0] = st4(cp1);
                 t = -1;
-            } else if (!fp_insert(P, lane, nv, nf, nnew, v)) {
-                f.cat_list[8 * (size_t)f.pair_cap + atomicAdd(&f.cat_count[8], 1)] = t;
-                t = -1;
+            } else {
+                const int r = fp_insert(P, lane, nv, nf, nnew, v);
+                if (r <= 0) {   // on to a longer pass, with this polytope when it is whole
+                    const int h8 = atomicAdd(&f.cat_count[8], 1);
+                    f.cat_list[8 * (size_t)f.pair_cap + h8] = t;
+                    if (h8 < f.lane_saves) {
+                        LaneSave& out = lane_saves(f)[h8];
+                        if (r == 0) fp_save(P, lane, nv, nf, out);
+                        else out.nv = 0;
+                    }
+                    t = -1;
+                }
             }
         }
         __syncwarp();
@@ -338,8 +380,15 @@ __global__ void __launch_bounds__(32) k_convex_epa_full(World w, FrameBuf f, int
     const Group<32> g(threadIdx.x);
     WarpPoly& P = *reinterpret_cast<WarpPoly*>(epa_smem);
     const int n = f.cat_count[lst];
-    for (int h = blockIdx.x; h < n; h += gridDim.x)
-        epa_pair<32, WarpPoly, false>(w, f, f.cat_list[lst * (size_t)f.pair_cap + h], P, g);
+    for (int h = blockIdx.x; h < n; h += gridDim.x) {
+        const int t = f.cat_list[lst * (size_t)f.pair_cap + h];
+        if (lst == 6 && h < f.group_saves && group_saves(f)[h].nv > 0)
+            epa_pair<32, WarpPoly, false>(w, f, t, P, g, &group_saves(f)[h]);
+        else if (lst == 8 && h < f.lane_saves && lane_saves(f)[h].nv > 0)
+            epa_pair<32, WarpPoly, false>(w, f, t, P, g, &lane_saves(f)[h]);
+        else
+            epa_pair<32, WarpPoly, false>(w, f, t, P, g, (const GroupSave*)nullptr);
+    }
 }
 
 // convex-mesh pairs, part 2: contact generation after EPA (face selection and

@@ -400,6 +400,8 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
     PSX_TRY(W->alloc(f.cat_count, 10));
     PSX_TRY(W->alloc(f.cat_list, 9 * (size_t)f.pair_cap));
     PSX_TRY(W->alloc(f.man_pair, f.pair_cap));
+    epa_save_caps(f.pair_cap, f.lane_saves, f.group_saves);
+    PSX_TRY(W->alloc(f.epa_save, epa_save_bytes(f.lane_saves, f.group_saves)));
     PSX_TRY(W->alloc(f.man_tri, (size_t)f.tri_cap * kTriManifolds));
     PSX_TRY(W->alloc(f.pair_tslot, f.pair_cap));
     PSX_TRY(W->alloc(f.pair_nman, f.pair_cap));
