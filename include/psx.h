@@ -168,9 +168,9 @@ typedef struct psx_launch_config {
                                       * is one warp holding 32 / epa_lanes pairs.  1: one lane per pair with the
                                       * warp's new faces built by all of its lanes, and 16 lanes per pair for the
                                       * pairs that need more than 12 steps */
-    int32_t solver_threads_min;      /* smallest solver block: 64 (scenes up to 96 dynamic bodies on 64 threads, up to
-                                      * 384 on 128), 128 or 256 (default: 64 for worlds of more block scenes than
-                                      * two per SM, else 256) */
+    int32_t solver_threads_min;      /* smallest solver block: 32 or 64 (scenes up to 96 dynamic bodies on 32 or 64
+                                      * threads, up to 384 on 128), 128 or 256 (default: 64 for worlds of more block
+                                      * scenes than two per SM, else 256) */
     int32_t epa_full_only;           /* 1: no grouped small-polytope pass: the pairs go to the full polytope
                                       * directly, or with epa_lanes 1 after the lane-per-pair pass (lowest latency
                                       * for the slowest pair); 2: the grouped pass between them (highest

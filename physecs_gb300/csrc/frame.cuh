@@ -182,7 +182,8 @@ int launch_contacts(const World& w, FrameBuf& f, cudaStream_t s);
 // (the whole grid, one after another)
 constexpr int kClusterBlocks = 8;   // blocks of the cluster that solves one large scene
 struct SolverLaunch {
-    const int* tier[3]; int n_tier[3]; int smem_tier[3];   // block scenes by block size 64 / 128 / 256
+    const int* tier[3]; int n_tier[3]; int smem_tier[3];   // block scenes by block size 32 or 64 / 128 / 256
+    int tier0_nt;                                          // threads per block of the smallest tier: 32 or 64
     cudaStream_t tstream[2];                               // streams of the 64- and 128-thread tiers
     cudaEvent_t tfork, tjoin[2];
     const int* large; int n_large; int smem_large;

@@ -504,9 +504,10 @@ int psx::rt::queue_frame(psx_world* W, cudaEvent_t* ev) {
     k += launch_joint_layout(W->w, W->f, s);
     if (ev) cudaEventRecord(ev[3], s);
     auto tier_smem = [&](int nt) { return std::max(12 * 1024, W->solver_smem * nt / 256) / 16 * 16; };
+    const int nt0 = W->threads_min <= 32 ? 32 : 64;
     SolverLaunch L{{W->tier_scenes[0], W->tier_scenes[1], W->tier_scenes[2]},
                    {(int)W->tier_h[0].size(), (int)W->tier_h[1].size(), (int)W->tier_h[2].size()},
-                   {tier_smem(64), tier_smem(128), W->solver_smem},
+                   {tier_smem(nt0), tier_smem(128), W->solver_smem}, nt0,
                    {W->tier_stream[0], W->tier_stream[1]}, W->ev_tfork, {W->ev_tjoin[0], W->ev_tjoin[1]},
                    W->large_scenes, (int)W->large_scenes_h.size(), W->solver_smem_large,
                    W->cluster_scenes, (int)W->cluster_scenes_h.size(),
@@ -533,7 +534,8 @@ psx_status psx::rt::run_frame(psx_world* W) {
             int k = queue_frame(W);
             W->launches -= k;   // counted when the graph runs
             PSX_CUDA(cudaStreamEndCapture(W->stream, &g));
-            PSX_CUDA(cudaGraphInstantiate(&W->graph, g, 0));
+            // the nodes keep their launches' priorities (the largest scenes' solver goes first)
+            PSX_CUDA(cudaGraphInstantiate(&W->graph, g, cudaGraphInstantiateFlagUseNodePriority));
             cudaGraphDestroy(g);
         }
         PSX_CUDA(cudaGraphLaunch(W->graph, W->stream));
@@ -592,8 +594,9 @@ psx_status psx::rt::apply_launch(psx_world* W, const psx_launch_config& c) {
     }
     if (c.large_scene_solver < 0 || c.large_scene_solver > 2) return fail(PSX_ERR_INVALID_ARG, "large_scene_solver out of range");
     if (c.large_scene_solver && c.large_scene_solver != W->large_mode) PSX_TRY(partition_big(W, c.large_scene_solver));
-    if (c.solver_threads_min && c.solver_threads_min != 64 && c.solver_threads_min != 128 && c.solver_threads_min != 256)
-        return fail(PSX_ERR_INVALID_ARG, "solver_threads_min must be 64, 128 or 256");
+    if (c.solver_threads_min && c.solver_threads_min != 32 && c.solver_threads_min != 64 && c.solver_threads_min != 128 &&
+        c.solver_threads_min != 256)
+        return fail(PSX_ERR_INVALID_ARG, "solver_threads_min must be 32, 64, 128 or 256");
     if (c.solver_threads_min && c.solver_threads_min != W->threads_min) PSX_TRY(partition_tiers(W, c.solver_threads_min));
     if (c.large_threads && c.large_threads != 128 && c.large_threads != 256 && c.large_threads != 512)
         return fail(PSX_ERR_INVALID_ARG, "large_threads must be 128, 256 or 512");
@@ -712,7 +715,13 @@ psx_status psx::rt::create_world(const psx_scene_desc* scenes, int n_scenes, psx
     W->frames_run = frames_run;
     W->forced_colors = colors;
     cudaError_t e = cudaStreamCreateWithFlags(&W->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&W->aux_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) {
+        // the aux stream carries the longest chains of the frame (the convex pairs' GJK and
+        // EPA passes, the largest scenes' solver): its blocks go first
+        int least = 0, greatest = 0;
+        cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        e = cudaStreamCreateWithPriority(&W->aux_stream, cudaStreamNonBlocking, greatest);
+    }
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&W->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&W->ev_join, cudaEventDisableTiming);
     for (int t = 0; t < 2 && e == cudaSuccess; ++t) {
@@ -929,7 +938,7 @@ PSX_API psx_status psx_world_tune(psx_world* W, int32_t frames, psx_launch_confi
     }
     if (!W->block_scenes_h.empty()) {   // the smallest solver block size
         Knob k{3, {}};
-        for (int t : {64, 128, 256}) {
+        for (int t : {32, 64, 128, 256}) {
             psx_launch_config c{};
             c.solver_threads_min = t;
             k.cands.push_back(c);

@@ -299,9 +299,11 @@ def test_launch_shapes_do_not_change_results(gpu_lib):
               _gpu(ss, launch=dict(epa_lanes=16, convex_warps=1, convex_blocks_per_sm=4, large_threads=128)),
               _gpu(ss, launch=dict(epa_lanes=8, convex_warps=1, convex_blocks_per_sm=2, large_threads=256)),
               _gpu(ss, launch=dict(epa_full_only=1, solver_threads_min=256)),
-              _gpu(ss, launch=dict(epa_lanes=1, convex_blocks_per_sm=8))]
+              _gpu(ss, launch=dict(epa_lanes=1, convex_blocks_per_sm=8)),
+              _gpu(ss, launch=dict(solver_threads_min=32))]
     assert [o.launch_config()["epa_lanes"] for o in others[:3]] == [32, 16, 8]
     assert others[4].launch_config()["epa_lanes"] == 1
+    assert others[5].launch_config()["solver_threads_min"] == 32
     assert others[3].launch_config()["epa_full_only"] == 1 and others[3].launch_config()["solver_threads_min"] == 256
     for f in range(8):
         a.step()
