@@ -15,6 +15,7 @@
 // bounded grid barrier.
 #include <cooperative_groups.h>
 #include "libm_f32.cuh"
+#include <algorithm>
 #include "frame.cuh"
 
 namespace psx {
@@ -1160,15 +1161,18 @@ static void set_smem(int bytes) {
     set_kernel_smem((const void*)k_solve_block<NT>, done, bytes);
 }
 
-// A launch whose blocks the scheduler places ahead of other streams' (the priority is a
-// launch attribute, so a CUDA graph captured from it keeps it).
+// A solver launch at a scheduling priority: `rank` 0 is the device's highest, each step
+// one lower, down to the lowest (the priority is a launch attribute, so a CUDA graph
+// captured from it keeps it).  The larger the scenes of a launch, the longer their
+// chains and the earlier their blocks should start.
 template <int NT>
-static void launch_block_first(int grid, int smem, cudaStream_t st, const World& w, FrameBuf& f, const int* scenes) {
+static void launch_block_ranked(int grid, int smem, cudaStream_t st, int rank, const World& w, FrameBuf& f,
+                                const int* scenes) {
     int least = 0, greatest = 0;
     cudaDeviceGetStreamPriorityRange(&least, &greatest);
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributePriority;
-    attr[0].val.priority = greatest;
+    attr[0].val.priority = greatest < least ? std::min(least, greatest + rank) : greatest;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(NT);
@@ -1195,14 +1199,14 @@ int launch_solver(const World& w, FrameBuf& f, const SolverLaunch& L, cudaStream
             const int smem = (L.smem_large + 5120 - per * 6144) / per / 16 * 16;
             if (L.large_nt == 128) {
                 set_smem<128>(smem);
-                launch_block_first<128>(L.n_large, smem, L.aux, w, f, L.large);
+                launch_block_ranked<128>(L.n_large, smem, L.aux, 0, w, f, L.large);
             } else {
                 set_smem<256>(smem);
-                launch_block_first<256>(L.n_large, smem, L.aux, w, f, L.large);
+                launch_block_ranked<256>(L.n_large, smem, L.aux, 0, w, f, L.large);
             }
         } else {
             set_smem<512>(L.smem_large);
-            launch_block_first<512>(L.n_large, L.smem_large, L.aux, w, f, L.large);
+            launch_block_ranked<512>(L.n_large, L.smem_large, L.aux, 0, w, f, L.large);
         }
         cudaEventRecord(L.join, L.aux);
         ++k;
@@ -1213,10 +1217,10 @@ int launch_solver(const World& w, FrameBuf& f, const SolverLaunch& L, cudaStream
         cudaStreamWaitEvent(L.tstream[0], L.tfork, 0);
         if (L.tier0_nt == 32) {   // one warp a scene: up to 16 scenes an SM
             set_smem<32>(L.smem_tier[0]);
-            k_solve_block<32><<<L.n_tier[0], 32, L.smem_tier[0], L.tstream[0]>>>(w, f, L.tier[0], L.smem_tier[0] / 16);
+            launch_block_ranked<32>(L.n_tier[0], L.smem_tier[0], L.tstream[0], 3, w, f, L.tier[0]);
         } else {
             set_smem<64>(L.smem_tier[0]);
-            k_solve_block<64><<<L.n_tier[0], 64, L.smem_tier[0], L.tstream[0]>>>(w, f, L.tier[0], L.smem_tier[0] / 16);
+            launch_block_ranked<64>(L.n_tier[0], L.smem_tier[0], L.tstream[0], 3, w, f, L.tier[0]);
         }
         cudaEventRecord(L.tjoin[0], L.tstream[0]);
         ++k;
@@ -1224,13 +1228,13 @@ int launch_solver(const World& w, FrameBuf& f, const SolverLaunch& L, cudaStream
     if (L.n_tier[1]) {
         set_smem<128>(L.smem_tier[1]);
         cudaStreamWaitEvent(L.tstream[1], L.tfork, 0);
-        k_solve_block<128><<<L.n_tier[1], 128, L.smem_tier[1], L.tstream[1]>>>(w, f, L.tier[1], L.smem_tier[1] / 16);
+        launch_block_ranked<128>(L.n_tier[1], L.smem_tier[1], L.tstream[1], 2, w, f, L.tier[1]);
         cudaEventRecord(L.tjoin[1], L.tstream[1]);
         ++k;
     }
     if (L.n_tier[2]) {
         set_smem<256>(L.smem_tier[2]);
-        k_solve_block<256><<<L.n_tier[2], 256, L.smem_tier[2], s>>>(w, f, L.tier[2], L.smem_tier[2] / 16);
+        launch_block_ranked<256>(L.n_tier[2], L.smem_tier[2], s, 1, w, f, L.tier[2]);
         ++k;
     }
     if (L.n_tier[0]) cudaStreamWaitEvent(s, L.tjoin[0], 0);
