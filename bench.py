@@ -608,7 +608,7 @@ def main():
             # largest kernel family is the solver, which the roofline above describes
             "dominant_kernel": {"kernel": "k_convex_epa_flat (narrowphase stage's top kernel)", "bound": "fp64 pipe",
                                 "narrowphase_ms_per_step": stage_ms[1] / args.steps,
-                                "fp64_pipe_active": 0.395,
+                                "fp64_pipe_active": 0.398,
                                 "source": "profiles/k_convex_epa_flat_512.md (ncu --set full, 512 scenes)"},
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d},
             "plain_gpu_scene_by_scene": None if plain is None else {"value": plain, "unit": METRIC,
