@@ -7,15 +7,18 @@
 //     reduction picks the same vertex as the reference's 4-lane SIMD scan
 //     (largest dot; among equal dots the lowest vertex index modulo 4, then the
 //     lowest index);
-//   * EPA closest face: each lane measures every G-th face; the reductions
-//     below reproduce the sequential scan in which the running minimum is kept
-//     as a float (EPA.h:52-60), including which face wins among faces whose
-//     distances round to the same float;
-//   * EPA visibility of the faces from the new vertex: one ballot per G faces;
+//   * EPA closest face: each lane measures every G-th face (distances compared as
+//     ordered integers); the reductions below reproduce the sequential scan in
+//     which the running minimum is kept as a float (EPA.h:52-60), including which
+//     face wins among faces whose distances round to the same float;
+//   * EPA visibility of the faces from the new vertex: one ballot per G faces, each
+//     test settled in f32 when clear of its error bound;
 //   * new faces on the horizon: one lane per horizon edge.
-// The horizon edge list itself is built by the group's first lane in the
-// reference's order (faces from last to first, edges removed by swapping in the
-// last edge), which fixes the order of the faces and so every later tie-break.
+// The horizon edge list is built in the reference's order (faces from last to first,
+// edges removed by swapping in the last edge), which fixes the order of the faces and
+// so every later tie-break: the group searches the list together and its first lane
+// edits it.  A pass can also go on from a polytope that an earlier pass handed over
+// (PolySave) instead of starting from the GJK simplex.
 //
 // Why groups: the FP64 pipe charges a warp instruction the same whatever the
 // number of lanes it carries, and one pair keeps only a handful of lanes busy (11
@@ -24,8 +27,8 @@
 //
 // Every support point of the polytope is a float (held as float in shared
 // memory, exactly); the Minkowski vertices, face normals and face distances are
-// held as doubles so that the face loops convert and recompute nothing.  The whole
-// polytope of one pair takes about 15 KB of shared memory.
+// held as doubles so that the face loops convert and recompute nothing.  The full
+// polytope of one pair takes about 15 KB of shared memory, the small one about 5.5 KB.
 #pragma once
 #include <math_constants.h>
 #include "narrow_convex.cuh"
