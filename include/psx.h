@@ -538,6 +538,8 @@ typedef struct psx_server_opts {
                                        * fails with PSX_ERR_OUT_OF_MEMORY when they need more */
     const psx_launch_config* launch;  /* kernel launch shapes of the slots' world, or NULL: the world defaults
                                        * with epa_full_only = 1 (frame latency before throughput) */
+    int32_t triggers;                 /* 1: the requests' trigger colliders raise events (psx_server_trigger_events);
+                                       * 0: they only keep out of contact */
 } psx_server_opts;
 
 PSX_API psx_status psx_server_create(const psx_server_opts* opts, psx_server** out);
@@ -570,6 +572,17 @@ PSX_API psx_world* psx_server_world(psx_server* s);
  * admissions (uploads and creation bounds), broadphase, narrowphase, contact and joint
  * rows, solver, end-of-frame bounds}. */
 PSX_API psx_status psx_server_tick_stages(psx_server* s, float* out);
+/* With opts.triggers set: the trigger events of the ticks ended so far, as
+ * psx_world_trigger_events gives a world's (Scene::simulate's onTriggerEnter /
+ * onTriggerExit, src/Physecs.cpp:537-552), for each request as if it ran alone: scene =
+ * the request's slot, frame = frames of the request stepped before it, bodies and
+ * colliders indexed within the request, entities the request's.  Events are decoded
+ * when their tick ends, so a slot may be released and reused before they are read.
+ * Up to cap events into out in tick order (within a tick: frame, enter before exit,
+ * slot, bodies, colliders); the rest stay queued.  n_lost (optional): events dropped
+ * because the device log overflowed within a tick. */
+PSX_API psx_status psx_server_trigger_events(psx_server* s, psx_trigger_event* out, int32_t cap, int32_t* n_out,
+                                             int64_t* n_lost);
 /* Device memory the server holds (its slots' world and flags), in bytes. */
 PSX_API psx_status psx_server_device_bytes(psx_server* s, int64_t* out);
 

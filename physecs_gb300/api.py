@@ -26,7 +26,7 @@ EXPORTS = ["psx_world_create", "psx_world_destroy", "psx_world_step", "psx_world
            "psx_scene_create", "psx_scene_destroy", "psx_scene_simulate", "psx_world_read_bodies_noalloc",
            "psx_server_create", "psx_server_destroy", "psx_server_admit", "psx_server_tick", "psx_server_read",
            "psx_server_release", "psx_server_stats", "psx_server_tick_begin", "psx_server_tick_end", "psx_server_world",
-           "psx_server_tick_stages", "psx_server_device_bytes",
+           "psx_server_tick_stages", "psx_server_device_bytes", "psx_server_trigger_events",
            "psx_world_tune", "psx_world_launch_config", "psx_world_raycast", "psx_world_overlap",
            "psx_world_overlap_mtd", "psx_world_trigger_events", "psx_trimesh_build", "psx_world_update_trimesh",
            "psx_world_apply_deltas", "psx_world_move_characters", "psx_world_set_contact_filter",
@@ -64,7 +64,7 @@ class PsxServerOpts(C.Structure):
     _fields_ = [("n_classes", C.c_int32), ("class_bodies", C.c_void_p), ("class_slots", C.c_void_p),
                 ("mesh_pool", C.c_void_p), ("pairs_per_collider", C.c_int32), ("manifolds_per_collider", C.c_int32),
                 ("device", C.c_int32), ("eager", C.c_int32), ("profile", C.c_int32),
-                ("hbm_budget", C.c_int64), ("launch", C.c_void_p)]
+                ("hbm_budget", C.c_int64), ("launch", C.c_void_p), ("triggers", C.c_int32)]
 
 
 def load():
@@ -111,6 +111,7 @@ def load():
     lib.psx_server_read.argtypes = [vp, C.c_int32, vp, vp, vp, vp]
     lib.psx_server_release.argtypes = [vp, C.c_int32]
     lib.psx_world_trigger_events.argtypes = [vp, vp, C.c_int32, vp, vp]
+    lib.psx_server_trigger_events.argtypes = [vp, vp, C.c_int32, vp, vp]
     lib.psx_trimesh_build.argtypes = [C.c_int32, vp, C.c_int32, vp, C.c_int32, vp, vp, vp]
     lib.psx_world_update_trimesh.argtypes = [vp, C.c_int32, C.c_int32, vp]
     lib.psx_world_apply_deltas.argtypes = [vp, C.c_int32, vp]
@@ -412,19 +413,7 @@ class World:
         events is an (n, 9) int64 array of (frame, kind 0 enter / 1 exit, scene, body0,
         collider0, body1, collider1, entity0, entity1) in delivery order; lost counts the
         events dropped because the device log overflowed between two drains."""
-        lib = load()
-        chunks, lost = [], 0
-        out = np.zeros((cap, 9), np.int32)   # psx_trigger_event: 9 words
-        n, nl = C.c_int32(), C.c_int64()
-        while True:
-            _check(lib.psx_world_trigger_events(self.h, _p(out), cap, C.byref(n), C.byref(nl)))
-            lost += nl.value
-            ev = out[:n.value].astype(np.int64)
-            ev[:, 7:9] = out[:n.value, 7:9].view(np.uint32)
-            chunks.append(ev)
-            if n.value < cap:
-                break
-        return np.concatenate(chunks), lost
+        return _drain_events(load().psx_world_trigger_events, self.h, cap)
 
     def _listeners(self, kind, scene):
         if not hasattr(self, "_trigger_listeners"):
@@ -467,16 +456,34 @@ class World:
         return ev
 
 
+def _drain_events(fn, h, cap):
+    """Calls fn (psx_world_trigger_events or psx_server_trigger_events) until its queue is
+    empty; returns the events as an (n, 9) int64 array and the count lost."""
+    chunks, lost = [], 0
+    out = np.zeros((cap, 9), np.int32)   # psx_trigger_event: 9 words
+    n, nl = C.c_int32(), C.c_int64()
+    while True:
+        _check(fn(h, _p(out), cap, C.byref(n), C.byref(nl)))
+        lost += nl.value
+        ev = out[:n.value].astype(np.int64)
+        ev[:, 7:9] = out[:n.value, 7:9].view(np.uint32)
+        chunks.append(ev)
+        if n.value < cap:
+            break
+    return np.concatenate(chunks), lost
+
+
 class Server:
     """Continuous batching of scene requests (psx_server_*): admit, tick, read, release.
 
     classes: [(bodies per slot, slots)] in ascending size; mesh_pool: a scene whose
-    convex meshes the requests may use."""
+    convex meshes the requests may use; triggers: the requests' trigger colliders raise
+    events (trigger_events)."""
 
     h = None
 
     def __init__(self, classes, mesh_pool=None, device=0, pairs_per_collider=0, manifolds_per_collider=0, eager=False,
-                 profile=False, hbm_budget=0, launch=None):
+                 profile=False, hbm_budget=0, launch=None, triggers=False):
         lib = load()
         self._cb = np.ascontiguousarray([c[0] for c in classes], np.int32)
         self._cs = np.ascontiguousarray([c[1] for c in classes], np.int32)
@@ -485,7 +492,7 @@ class Server:
         opts = PsxServerOpts(len(classes), self._cb.ctypes.data, self._cs.ctypes.data,
                              C.cast(C.pointer(self._pool), C.c_void_p) if self._pool is not None else None,
                              pairs_per_collider, manifolds_per_collider, device, 1 if eager else 0,
-                             1 if profile else 0, int(hbm_budget), None)
+                             1 if profile else 0, int(hbm_budget), None, 1 if triggers else 0)
         if launch:
             self._launch = PsxLaunchConfig(*[int(launch.get(n, 0)) for n in LAUNCH_FIELDS])
             opts.launch = C.cast(C.pointer(self._launch), C.c_void_p)
@@ -571,6 +578,12 @@ class Server:
         out = np.zeros(6, np.float32)
         _check(load().psx_server_tick_stages(self.h, _p(out)))
         return out
+
+    def trigger_events(self, cap=4096):
+        """psx_server_trigger_events until the queue is empty: (events, lost) as
+        World.trigger_events gives them, with scene = the request's slot and frames, bodies,
+        colliders and entities the request's own."""
+        return _drain_events(load().psx_server_trigger_events, self.h, cap)
 
     def stats(self):
         out = np.zeros(6, np.int64)

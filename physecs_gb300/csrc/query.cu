@@ -640,6 +640,13 @@ __device__ __forceinline__ void trig_event(const FrameBuf& f, int frame, int kin
     if (i < f.evt_cap) f.trig_evt[i] = make_int4(frame, kind, (int)(key >> 32), (int)(unsigned)key);
 }
 
+// Scene of a collider, and whether a scene placed into a server slot this frame: its
+// pairs enter whatever the last frame's set holds (that set is the slot's last occupant's)
+__device__ __forceinline__ int collider_scene(const World& w, int c) { return w.info[w.col_info[c].x].w; }
+__device__ __forceinline__ bool scene_is_fresh(const World& w, int c) {
+    return w.scene_fresh && w.scene_fresh[collider_scene(w, c)];
+}
+
 // physecs::overlap of every trigger pair at this frame's poses; a pair that overlaps
 // joins this frame's set and, when the last frame's set lacks it, enters.
 __global__ void __launch_bounds__(128) k_trigger_enter(World w, FrameBuf f) {
@@ -663,20 +670,26 @@ __global__ void __launch_bounds__(128) k_trigger_enter(World w, FrameBuf f) {
             if (atomicCAS(&tab[h], kNoKey, key) == kNoKey) break;
         f.trig_keys[cur][i] = key;
         f.trig_slot[cur][i] = (int)h;
-        if (!trig_find(f.trig_table[cur ^ 1], mask, key)) trig_event(f, frame, 0, key);
+        if (scene_is_fresh(w, pr.x) || !trig_find(f.trig_table[cur ^ 1], mask, key)) trig_event(f, frame, 0, key);
     }
 }
 
 // The last frame's pairs missing from this frame's set exit; the last frame's table is
-// emptied for the frame after.
-__global__ void __launch_bounds__(128) k_trigger_exit(FrameBuf f) {
+// emptied for the frame after.  In a server's world a pair whose slot is not running (its
+// request has run all its frames) or has a new occupant leaves without an event.
+__global__ void __launch_bounds__(128) k_trigger_exit(World w, FrameBuf f) {
     const int cur = f.trig_state[0], prev = cur ^ 1, frame = f.trig_state[3];
     const unsigned mask = (unsigned)f.trig_table_cap - 1u;
     const int n = min(f.trig_state[1 + prev], f.trig_cap);
     const unsigned long long* tab = f.trig_table[cur];
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         const unsigned long long key = f.trig_keys[prev][t];
-        if (!trig_find(tab, mask, key)) trig_event(f, frame, 1, key);
+        bool live = true;
+        if (w.scene_active) {
+            const int sc = collider_scene(w, (int)(key >> 32));
+            live = w.scene_active[sc] && !(w.scene_fresh && w.scene_fresh[sc]);
+        }
+        if (live && !trig_find(tab, mask, key)) trig_event(f, frame, 1, key);
         f.trig_table[prev][f.trig_slot[prev][t]] = kNoKey;
     }
 }
@@ -693,7 +706,7 @@ int launch_triggers(const World& w, FrameBuf& f, cudaStream_t s) {
     if (!f.trig_cap) return 0;
     const int blocks = std::min(152 * 4, (f.trig_cap + 127) / 128);
     k_trigger_enter<<<blocks, 128, 0, s>>>(w, f);
-    k_trigger_exit<<<blocks, 128, 0, s>>>(f);
+    k_trigger_exit<<<blocks, 128, 0, s>>>(w, f);
     k_trigger_swap<<<1, 1, 0, s>>>(f);
     return 3;
 }

@@ -10,12 +10,16 @@
 // A request's results do not depend on which slot it lands in or on the other
 // requests in flight: the broadphase order, manifold order and contact colouring
 // of a scene depend on that scene alone, and the unused bodies of a slot are
-// static, kinematic or disabled.  Requests carry no joints and no triangle meshes
+// static, kinematic or disabled.  Trigger events (opts.triggers) are decoded per request
+// at the end of each tick: the slot's flags keep a fresh request from seeing the last
+// occupant's trigger pairs and drop the exits of a finished one.  Requests carry no
+// joints and no triangle meshes
 // (the serving workload's scenes have neither); their convex meshes must be meshes
 // of the server's pool, matched by content.
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
+#include <tuple>
 #include <vector>
 #include "runtime.cuh"
 
@@ -23,6 +27,14 @@ using namespace psx;
 using namespace psx::rt;
 
 namespace {
+
+// What decodes a request's trigger events: each slot collider's request body and index
+// within that body, each request body's entity, and the world frame of its first tick.
+struct ReqMap {
+    std::vector<int> col_body, col_local;
+    std::vector<uint32_t> entity;
+    long long frame0 = 0;
+};
 
 struct Slot {
     long long first_tick = 0;                     // the first tick that simulates the request
@@ -32,6 +44,7 @@ struct Slot {
     int frames_left = 0;
     int n_bodies = 0;
     std::vector<int> dyn_of;                      // request body -> world dynamic index or -1
+    ReqMap map;                                   // the request's trigger-event decoding
 };
 
 uint64_t fnv(uint64_t h, const void* p, size_t n) {
@@ -134,6 +147,14 @@ struct psx_server {
     cudaEvent_t prof[7] = {};        // tick start, then the frame's six stage events
     int* pin_active = nullptr;       // pinned mirror of h_active for the flag copy
     int* pin_err = nullptr;          // device error word of the last tick
+    // trigger events (opts.triggers): decoded at the end of each tick
+    bool triggers = false;
+    int* pin_nevt = nullptr;                     // the device log's count after the last tick
+    std::vector<int> slot_col0;                  // first world collider of each slot, ascending
+    std::vector<ReqMap> retired;                 // per slot: the request that a re-admission
+                                                 // replaced while a tick it ran was in flight
+    std::vector<psx_trigger_event> trig_pending;
+    int64_t trig_lost = 0;
     // reads of finished requests run on their own stream, beside the next tick
     cudaStream_t read_stream = nullptr;
     float4* read_pin = nullptr;
@@ -149,6 +170,7 @@ struct psx_server {
         for (cudaEvent_t e : prof) if (e) cudaEventDestroy(e);
         if (pin_active) cudaFreeHost(pin_active);
         if (pin_err) cudaFreeHost(pin_err);
+        if (pin_nevt) cudaFreeHost(pin_nevt);
         if (read_pin) cudaFreeHost(read_pin);
         if (d_active) cudaFree(d_active);
         if (d_fresh) cudaFree(d_fresh);
@@ -217,6 +239,9 @@ PSX_API psx_status psx_server_create(const psx_server_opts* o, psx_server** out)
     psx_status st = psx_world_create(descs.data(), n_slots, &wo, &W);
     if (st != PSX_OK) { delete S; return st; }
     S->W = W;
+    // trigger sets and the event log; a trigger pair's events are kept or dropped by its
+    // slot's running and fresh flags (k_trigger_enter / k_trigger_exit)
+    if (o->triggers && (st = alloc_triggers(W)) != PSX_OK) { delete S; return st; }
     if (cudaMalloc(&S->d_active, sizeof(int) * n_slots) != cudaSuccess ||
         cudaMalloc(&S->d_fresh, sizeof(int) * n_slots) != cudaSuccess) {
         delete S;
@@ -245,6 +270,16 @@ PSX_API psx_status psx_server_create(const psx_server_opts* o, psx_server** out)
         return fail(PSX_ERR_OUT_OF_MEMORY, "server host staging");
     }
     *S->pin_err = 0;
+    if (o->triggers) {
+        if (cudaMallocHost(&S->pin_nevt, sizeof(int)) != cudaSuccess) {
+            delete S;
+            return fail(PSX_ERR_OUT_OF_MEMORY, "server host staging");
+        }
+        *S->pin_nevt = 0;
+        S->triggers = true;
+        for (const Slot& sl : S->slots) S->slot_col0.push_back(sl.col0);
+        S->retired.resize(n_slots);
+    }
     S->profile = o->profile != 0;
     for (int i = 0; S->profile && i < 7; ++i)
         if (cudaEventCreate(&S->prof[i]) != cudaSuccess) { delete S; return fail(PSX_ERR_CUDA, "server profile events"); }
@@ -295,6 +330,21 @@ PSX_API psx_status psx_server_admit(psx_server* S, const psx_scene_desc* d, int3
     S->cpos.assign(nb, f4(0, 0, 0)); S->cquat.assign(nb, f4(0, 0, 0, 1)); S->cpar.assign(nb, f4(0.1f, 0, 0));
     S->cmat.assign(nb, f4(0, 0, 0)); S->cinfo.assign(nb, make_int4(inert, PSX_SPHERE, -1, 0));
     sl.dyn_of.assign(d->n_bodies, -1);
+    if (S->triggers) {
+        // a tick in flight may have run the slot's previous request: its events are
+        // decoded at that tick's end with the map it ran under
+        if (S->in_flight) std::swap(S->retired[si], sl.map);
+        ReqMap& m = sl.map;
+        m.col_body.resize(d->n_colliders);
+        m.col_local.resize(d->n_colliders);
+        m.entity.assign(d->entity, d->entity + d->n_bodies);
+        for (int b = 0; b < d->n_bodies; ++b)
+            for (int c = d->collider_start[b]; c < d->collider_start[b + 1]; ++c) {
+                m.col_body[c] = b;
+                m.col_local[c] = c - d->collider_start[b];
+            }
+        m.frame0 = S->W->frames_run;   // the frame of the next tick: every tick begun has counted its frame
+    }
     int nd = 0, nsim = 0;
     for (int b = 0; b < d->n_bodies; ++b) {
         uint32_t fl = d->flags[b];
@@ -418,11 +468,66 @@ PSX_API psx_status psx_server_tick_begin(psx_server* S) {
     }
     PSX_CUDA(cudaMemsetAsync(S->d_fresh, 0, sizeof(int) * S->h_active.size(), st));
     PSX_CUDA(cudaMemcpyAsync(S->pin_err, W->w.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    if (S->triggers) PSX_CUDA(cudaMemcpyAsync(S->pin_nevt, W->f.n_evt, sizeof(int), cudaMemcpyDeviceToHost, st));
     PSX_CUDA(cudaEventRecord(S->tick_done, st));
     PSX_CUDA(cudaGetLastError());
     S->in_flight = true;
     return PSX_OK;
 }
+
+}  // extern "C"
+
+namespace {
+
+// The tick just ended: its raw events (world frame, kind, world colliders) become request
+// events.  A slot's colliders are a fixed range of the world's, so the range gives the
+// slot; the request that ran there in this tick gives bodies, colliders and entities.
+psx_status drain_triggers(psx_server* S) {
+    const int n = *S->pin_nevt;
+    if (!n) return PSX_OK;
+    psx_world* W = S->W;
+    const FrameBuf& f = W->f;
+    cudaStream_t st = W->stream;
+    const int kept = std::min(n, f.evt_cap);
+    std::vector<int4> ev(kept);
+    PSX_CUDA(cudaMemcpyAsync(ev.data(), f.trig_evt, sizeof(int4) * kept, cudaMemcpyDeviceToHost, st));
+    PSX_CUDA(cudaMemsetAsync(f.n_evt, 0, sizeof(int), st));
+    PSX_CUDA(cudaStreamSynchronize(st));
+    S->trig_lost += n - kept;
+    const long long tick = S->ticks_begun;
+    std::vector<psx_trigger_event> batch;
+    batch.reserve(kept);
+    for (const int4& r : ev) {
+        const int si = (int)(std::upper_bound(S->slot_col0.begin(), S->slot_col0.end(), r.z) - S->slot_col0.begin()) - 1;
+        if (si < 0) continue;
+        const Slot& sl = S->slots[si];
+        const ReqMap& m = sl.first_tick <= tick ? sl.map : S->retired[si];
+        const int c0 = r.z - sl.col0, c1 = r.w - sl.col0;
+        if (c0 < 0 || c1 < 0 || c0 >= (int)m.col_body.size() || c1 >= (int)m.col_body.size()) continue;
+        psx_trigger_event e{};
+        e.frame = (int)(r.x - m.frame0);
+        e.kind = r.y;
+        e.scene = si;
+        e.body0 = m.col_body[c0];
+        e.collider0 = m.col_local[c0];
+        e.body1 = m.col_body[c1];
+        e.collider1 = m.col_local[c1];
+        e.entity0 = m.entity[e.body0];
+        e.entity1 = m.entity[e.body1];
+        batch.push_back(e);
+    }
+    // one tick: enter before exit, then slot, bodies and colliders, as a world orders a frame's
+    auto key = [](const psx_trigger_event& e) {
+        return std::make_tuple(e.kind, e.scene, e.body0, e.collider0, e.body1, e.collider1);
+    };
+    std::sort(batch.begin(), batch.end(), [&](const psx_trigger_event& a, const psx_trigger_event& b) { return key(a) < key(b); });
+    S->trig_pending.insert(S->trig_pending.end(), batch.begin(), batch.end());
+    return PSX_OK;
+}
+
+}  // namespace
+
+extern "C" {
 
 PSX_API psx_status psx_server_tick_end(psx_server* S, int32_t* done, int32_t cap, int32_t* n_done) {
     if (!S) return fail(PSX_ERR_INVALID_ARG, "null server");
@@ -435,6 +540,7 @@ PSX_API psx_status psx_server_tick_end(psx_server* S, int32_t* done, int32_t cap
         std::snprintf(buf, sizeof buf, "device error bits 0x%x", e);
         return fail((e & ERR_BARRIER_TIMEOUT) ? PSX_ERR_TIMEOUT : PSX_ERR_CAPACITY, buf);
     }
+    if (S->triggers) PSX_TRY(drain_triggers(S));
     int nd = 0;
     for (size_t i = 0; i < S->slots.size(); ++i) {
         Slot& sl = S->slots[i];
@@ -501,6 +607,18 @@ PSX_API psx_status psx_server_release(psx_server* S, int32_t slot) {
     if (sl.state == 1) { S->h_active[sl.scene] = 0; S->active_dirty = true; }
     sl.state = 0;
     S->free_slots[sl.cls].push_back(slot);
+    return PSX_OK;
+}
+
+PSX_API psx_status psx_server_trigger_events(psx_server* S, psx_trigger_event* out, int32_t cap, int32_t* n_out,
+                                             int64_t* n_lost) {
+    if (!S || cap < 0 || (cap && !out) || !n_out) return fail(PSX_ERR_INVALID_ARG, "psx_server_trigger_events: bad arguments");
+    if (!S->triggers) return fail(PSX_ERR_INVALID_ARG, "psx_server_trigger_events: the server was created without triggers");
+    const int m = (int)std::min<size_t>((size_t)cap, S->trig_pending.size());
+    std::copy(S->trig_pending.begin(), S->trig_pending.begin() + m, out);
+    S->trig_pending.erase(S->trig_pending.begin(), S->trig_pending.begin() + m);
+    *n_out = m;
+    if (n_lost) { *n_lost = S->trig_lost; S->trig_lost = 0; }
     return PSX_OK;
 }
 

@@ -190,3 +190,105 @@ def test_hbm_budget_caps_the_slots(gpu_lib):
     srv.tick(); srv.tick()
     _same(srv.read(slot), _alone(reqs[0], 2))
     srv.close()
+
+
+def _trigger_requests(pool, ids, n_bodies):
+    """Serving requests with about one collider in eight a trigger (never the ground):
+    dynamic triggers fall through the other bodies, so pairs enter and exit."""
+    reqs = _requests(pool, ids, n_bodies)
+    for i, s in zip(ids, reqs):
+        a = s.arrays
+        ncol = len(a["col_type"])
+        cols = np.random.default_rng(i).permutation(np.arange(1, ncol))
+        a["col_is_trigger"][cols[: max(1, ncol // 8)]] = 1
+    return reqs
+
+
+def _alone_events(scene, frames):
+    from physecs_gb300.api import World
+    w = World([scene])
+    w.step(frames=frames)
+    ev, lost = w.trigger_events()
+    assert lost == 0
+    w.close()
+    return ev
+
+
+def _request_events(ev, slot):
+    got = ev[ev[:, 2] == slot].copy()
+    got[:, 2] = 0
+    return got
+
+
+def test_trigger_events_per_request_equal_alone(gpu_lib):
+    """Each request's trigger events, served beside others and in slots that earlier
+    requests left the tick before, equal those of its scene stepped alone: same frames
+    (counted from the request's first), bodies, colliders, entities and order."""
+    from physecs_gb300.api import Server
+    pool, pool_scene = _pool()
+    reqs = _trigger_requests(pool, [61, 62, 63, 64, 65, 66], [40, 200, 50, 180, 30, 60])
+    frames = [25, 18, 30, 12, 22, 16]
+    srv = Server([(64, 2), (256, 1)], mesh_pool=pool_scene, triggers=True)
+    pending, live = list(range(len(reqs))), {}
+    got = {i: [] for i in range(len(reqs))}
+
+    def admit_waiting():
+        for i in list(pending):
+            slot = srv.admit(reqs[i], frames[i])
+            if slot is not None:
+                live[slot] = i
+                pending.remove(i)
+
+    admit_waiting()
+    for _ in range(200):
+        done = srv.tick()
+        ev, lost = srv.trigger_events(cap=64)
+        assert lost == 0
+        for slot, i in live.items():
+            got[i].append(_request_events(ev, slot))
+        for slot in done:                    # released and refilled before the next tick
+            live.pop(slot)
+            srv.release(slot)
+        admit_waiting()
+        if not live and not pending:
+            break
+    assert not live and not pending
+    total = exits = 0
+    for i, r in enumerate(reqs):
+        want = _alone_events(r, frames[i])
+        have = np.concatenate(got[i])
+        assert np.array_equal(have, want), i
+        total += len(want)
+        exits += int((want[:, 1] == 1).sum())
+    assert total > 0 and exits > 0
+    srv.close()
+
+
+def test_trigger_events_of_a_request_released_mid_tick(gpu_lib):
+    """A running request released while its tick is in flight, and a new request admitted
+    into the same slot at once: the old request's events of that tick are decoded with its
+    own bodies, the new one's start clean."""
+    from physecs_gb300.api import Server
+    pool, pool_scene = _pool()
+    a, b = _trigger_requests(pool, [71, 72], [50, 60])
+    srv = Server([(64, 1)], mesh_pool=pool_scene, triggers=True)
+    sa = srv.admit(a, 40)
+    ran = 14
+    events = []
+    for _ in range(ran - 1):
+        assert not srv.tick()
+        events.append(srv.trigger_events()[0])
+    srv.tick_begin()                         # frame ran - 1 of a in flight
+    srv.release(sa)
+    sb = srv.admit(b, 9)
+    assert sb == sa
+    assert srv.tick_end() == []
+    events.append(srv.trigger_events()[0])
+    assert np.array_equal(_request_events(np.concatenate(events), sa), _alone_events(a, ran))
+    events = []
+    done = []
+    while not done:
+        done = srv.tick()
+        events.append(srv.trigger_events()[0])
+    assert np.array_equal(_request_events(np.concatenate(events), sb), _alone_events(b, 9))
+    srv.close()
