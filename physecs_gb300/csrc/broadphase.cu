@@ -468,8 +468,36 @@ __device__ __forceinline__ bool pair_ok(const World& w, int ca, int cb) {
 // out in increasing sorted position: an order that depends only on the scene (its
 // Morton codes), never on the tree's shape, the warp's other lanes or the batch.  A
 // warp whose leaves belong to two scenes walks them one after the other.
-template <bool EMIT>
+//
+// The pairs of a leaf go to pairs[leaf_off[p] + k] for its k-th partner, and leaf_off is
+// the scan of the counts, so the walk runs before the scan (counting) and after it
+// (placing).  Modes: kCount counts; kEmit places every pair; kCollect counts and keeps a
+// leaf's first trav_k pairs in a per-leaf scratch, which k_pairs_place copies into place
+// after the scan, so that one walk does both; kTail walks again only the leaves with more
+// than trav_k pairs, to place the rest.
+enum TraverseMode { kCount = 0, kEmit = 1, kCollect = 2, kTail = 3 };
+
+__device__ __forceinline__ int2* trav_scratch(const FrameBuf& f) { return reinterpret_cast<int2*>(f.cat_list); }
+
+// the count-th partner cb of leaf p (collider ca): the pair in entity order, placed or kept
+template <int MODE>
+__device__ __forceinline__ void place_pair(const World& w, const FrameBuf& f, int ca, int cb, int p, int out, int count) {
+    if (MODE == kCount || (MODE == kTail && count < f.trav_k) || (MODE == kCollect && count >= f.trav_k)) return;
+    const uint32_t ea = (uint32_t)w.info[w.col_info[ca].x].x, eb = (uint32_t)w.info[w.col_info[cb].x].x;
+    const int2 pr = ea < eb ? make_int2(ca, cb) : make_int2(cb, ca);
+    if (MODE == kCollect) {
+        trav_scratch(f)[(size_t)p * f.trav_k + count] = pr;
+    } else {
+        const int slot = out + count;
+        if (slot < f.pair_cap) f.pairs[slot] = pr;
+    }
+}
+
+template <int MODE>
 __global__ void __launch_bounds__(256) k_traverse(World w, FrameBuf f) {
+    constexpr bool EMIT = MODE == kEmit || MODE == kTail;
+    if (MODE == kTail && *f.trav_tail == 0) return;
+    if (MODE == kCollect && blockIdx.x == 0 && threadIdx.x == 0) *f.trav_tail = 0;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
     int ca = 0, s = -1, root = 0;
@@ -481,6 +509,7 @@ __global__ void __launch_bounds__(256) k_traverse(World w, FrameBuf f) {
         int cs = w.scene_col[s], n = w.scene_col[s + 1] - cs;
         bool active = !w.scene_active || w.scene_active[s];
         want = n >= 2 && active && (w.col_info[ca].w & COL_ENABLE);
+        if (MODE == kTail) want = want && f.leaf_cnt[p] > f.trav_k;
         root = cs - s;   // root of this scene's tree
         qmin = w.aabb_min[ca];
         qmax = w.aabb_max[ca];
@@ -528,13 +557,7 @@ __global__ void __launch_bounds__(256) k_traverse(World w, FrameBuf f) {
                     const int cb = f.order[q];
                     if (!overlap_incl(qmin, qmax, w.aabb_min[cb], w.aabb_max[cb])) continue;
                     if (!pair_ok(w, ca, cb)) continue;
-                    if (EMIT) {
-                        int slot = out + count;
-                        if (slot < f.pair_cap) {
-                            uint32_t ea = (uint32_t)w.info[w.col_info[ca].x].x, eb = (uint32_t)w.info[w.col_info[cb].x].x;
-                            f.pairs[slot] = ea < eb ? make_int2(ca, cb) : make_int2(cb, ca);
-                        }
-                    }
+                    place_pair<MODE>(w, f, ca, cb, p, out, count);
                     ++count;
                 } else if (f.bvh.last[c] > p && overlap_incl(qmin, qmax, f.bvh.bmin[c], f.bvh.bmax[c])) {
                     if (sp + 2 <= 64) {
@@ -557,13 +580,7 @@ __global__ void __launch_bounds__(256) k_traverse(World w, FrameBuf f) {
                 const int cb = f.order[q];
                 if (!overlap_incl(qmin, qmax, w.aabb_min[cb], w.aabb_max[cb])) continue;
                 if (!pair_ok(w, ca, cb)) continue;
-                if (EMIT) {
-                    int slot = out + count;
-                    if (slot < f.pair_cap) {
-                        uint32_t ea = (uint32_t)w.info[w.col_info[ca].x].x, eb = (uint32_t)w.info[w.col_info[cb].x].x;
-                        f.pairs[slot] = ea < eb ? make_int2(ca, cb) : make_int2(cb, ca);
-                    }
-                }
+                place_pair<MODE>(w, f, ca, cb, p, out, count);
                 ++count;
             } else {
                 const bool go = mine && f.bvh.last[c] > p && overlap_incl(qmin, qmax, f.bvh.bmin[c], f.bvh.bmax[c]);
@@ -578,6 +595,31 @@ __global__ void __launch_bounds__(256) k_traverse(World w, FrameBuf f) {
         }
     }
     if (!EMIT && p < w.n_colliders) f.leaf_cnt[p] = count;
+}
+
+// After the scan: each leaf's kept pairs (its first trav_k) copied to their places, a
+// warp per 32 leaves so that the copies of one leaf are consecutive lanes' stores.
+__global__ void __launch_bounds__(256) k_pairs_place(World w, FrameBuf f) {
+    const int K = f.trav_k;
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    const int2* scratch = trav_scratch(f);
+    bool tail = false;
+    for (int base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; base < w.n_colliders; base += warps * 32) {
+        const int p = base + lane;
+        const int cnt = p < w.n_colliders ? f.leaf_cnt[p] : 0;
+        const int off = p < w.n_colliders ? f.leaf_off[p] : 0;
+        tail |= cnt > K;
+        unsigned busy = __ballot_sync(~0u, cnt > 0);
+        while (busy) {
+            const int l = __ffs(busy) - 1;
+            busy &= busy - 1;
+            const int lc = min(__shfl_sync(~0u, cnt, l), K), lo = __shfl_sync(~0u, off, l);
+            for (int r = lane; r < lc; r += 32)
+                if (lo + r < f.pair_cap) f.pairs[lo + r] = scratch[(size_t)(base + l) * K + r];
+        }
+    }
+    if (tail) *f.trav_tail = 1;
 }
 
 __global__ void k_pairs_check(FrameBuf f, int* err) {
@@ -655,9 +697,17 @@ int launch_broadphase(const World& w, FrameBuf& f, int scene_bits, int scene_sor
     if (n == 0) return 0;
     int nb = (n + 255) / 256;
     int k = launch_bvh_build(w, f, scene_bits, scene_sort_pmax, false, s) - 2;
-    k_traverse<false><<<nb, 256, 0, s>>>(w, f);
-    scan_exclusive(f.leaf_cnt, f.leaf_off, n, f.n_pairs, f.scan_scratch, s);
-    k_traverse<true><<<nb, 256, 0, s>>>(w, f);
+    if (f.trav_k > 0) {   // one walk, the kept pairs placed after the scan, a second walk only for long lists
+        k_traverse<kCollect><<<nb, 256, 0, s>>>(w, f);
+        scan_exclusive(f.leaf_cnt, f.leaf_off, n, f.n_pairs, f.scan_scratch, s);
+        k_pairs_place<<<std::min(nb, 152 * 8), 256, 0, s>>>(w, f);
+        k_traverse<kTail><<<nb, 256, 0, s>>>(w, f);
+        ++k;
+    } else {
+        k_traverse<kCount><<<nb, 256, 0, s>>>(w, f);
+        scan_exclusive(f.leaf_cnt, f.leaf_off, n, f.n_pairs, f.scan_scratch, s);
+        k_traverse<kEmit><<<nb, 256, 0, s>>>(w, f);
+    }
     k_pairs_check<<<1, 1, 0, s>>>(f, w.err);
     return k + 4 + 3 + 1;
 }

@@ -51,6 +51,8 @@ struct FrameBuf {
     int* leaf_cnt;        // [n_colliders] pairs found per sorted leaf
     int* leaf_off;
     int* scan_scratch;
+    int trav_k;           // pairs per leaf the walk keeps in cat_list (free until k_classify), 0: none
+    int* trav_tail;       // device flag: some leaf found more than trav_k pairs
     int pair_cap;
     int2* pairs;          // collider indices, entity(a) < entity(b)
     int* n_pairs;         // device scalar

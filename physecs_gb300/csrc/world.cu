@@ -399,6 +399,10 @@ psx_status psx::rt::build_world(psx_world* W, const psx_scene_desc* scenes, int 
     PSX_TRY(W->alloc(f.pair_cat, f.pair_cap));
     PSX_TRY(W->alloc(f.cat_count, 10));
     PSX_TRY(W->alloc(f.cat_list, 9 * (size_t)f.pair_cap));
+    // the broadphase keeps each leaf's first pairs in the lists' memory until they are
+    // placed (k_pairs_place)
+    f.trav_k = n > 0 ? (int)std::min<size_t>(1 << 20, 9 * (size_t)f.pair_cap / (2 * (size_t)n)) : 0;
+    PSX_TRY(W->alloc(f.trav_tail, 1));
     PSX_TRY(W->alloc(f.man_pair, f.pair_cap));
     epa_save_caps(f.pair_cap, f.lane_saves, f.group_saves);
     PSX_TRY(W->alloc(f.epa_save, epa_save_bytes(f.lane_saves, f.group_saves)));

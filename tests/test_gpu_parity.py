@@ -436,3 +436,39 @@ def test_epa_schedules_agree_with_the_oracle(lanes, full_only, gpu_lib, oracle_l
         assert nc["epa"] > 0 and (nc["past_lane"] >= nc["past_group"] if lanes == 1 else nc["past_lane"] == 0)
         assert full_only == 2 or nc["past_group"] == 0
     assert g.counts()["error"] == 0
+
+
+def _clustered_scene(seed=3):
+    """576 spheres spread over a grid and one cluster of 60 overlapping spheres: the
+    cluster's first leaves have far more partners than the average collider."""
+    rng = np.random.default_rng(seed)
+    s = scenes.SceneData("clustered")
+    scenes._ground_box(s, (40.0, 0.5, 40.0))
+    grid = np.array([[x, 2.0, z] for x in np.arange(-36.0, 36.0, 3.0) for z in np.arange(-36.0, 36.0, 3.0)])
+    cluster = rng.uniform(-0.6, 0.6, size=(60, 3)) + [0.0, 4.0, 0.0]
+    pos = np.concatenate([grid, cluster]).astype(np.float32)
+    s.add_bodies(pos=pos, quat=[scenes.IDENTITY_Q] * len(pos), flags=scenes.BODY_DYNAMIC, inv_mass=1.0,
+                 com=np.zeros(3), inv_inertia=np.eye(3).ravel(), col_type=scenes.SPHERE,
+                 col_params=[0.4, 0.0, 0.0, 0.0], col_mesh=-1)
+    return s.finalize()
+
+
+def test_pairs_beyond_the_kept_ones_keep_their_order(gpu_lib, oracle_lib):
+    """The walk keeps a leaf's first pairs (4.5 x pairs_per_collider of them) and walks
+    again only for leaves with more.  With 4 pairs per collider the cluster's leaves take
+    that second walk; the pair list, order included, is that of a world whose leaves all
+    fit (64 pairs per collider), and the set is the oracle's."""
+    s = _clustered_scene()
+    tight, roomy = _gpu(s, pairs_per_collider=4), _gpu(s, pairs_per_collider=64)
+    for f in range(3):
+        for g in (tight, roomy):
+            g.step(); g.synchronize()
+        a, b = tight.pairs(), roomy.pairs()
+        assert f > 0 or len(a) > 1000   # the cluster separates over the next frames
+        assert np.array_equal(a, b), f
+    o = _oracle(s)
+    g = _gpu(s, pairs_per_collider=4)
+    g.step(); g.synchronize()
+    o.step()
+    assert pair_set(g.pairs()[:, 1:]) == pair_set(o.pairs())
+    assert tight.counts()["error"] == 0 and g.counts()["error"] == 0
