@@ -91,8 +91,9 @@ __device__ __forceinline__ int fp_insert(FlatPoly& P, int s, int& nv, int& nf, i
     }
     int ne = 0, n = nf;
     bool full = false;
-    for (int k = nf - 1; k >= 0; --k) {
-        if (!((vis >> k) & 1u)) continue;
+    for (unsigned bits = vis; bits; ) {   // visible faces, highest index first
+        const int k = 31 - __clz(bits);
+        bits &= ~(1u << k);
         const int a[3] = {P.i0[k][s], P.i1[k][s], P.i2[k][s]};
         const int b[3] = {a[1], a[2], a[0]};
         bool found[3] = {false, false, false};

@@ -276,10 +276,17 @@ __device__ inline int group_epa(const Support& s0, const Support& s1, const GjkS
             // visible face cancels the latest matching reversed edge of the list (the list's
             // last edge moves into its place) or is appended.  The group searches the list
             // together and its first lane edits it, so every lane follows the same counts.
+            // Only the visible faces are visited, highest index first, by walking the set
+            // bits of the bitset: a removal moves the current last face into the removed
+            // slot, and that face has a higher index, so it has been looked at already and
+            // the bits below stay valid.
             int ne = 0, n = nf;
             bool full = false;
-            for (int k = nf - 1; k >= 0; --k) {
-                if (!((P.vis[k >> 5] >> (k & 31)) & 1u)) continue;
+            for (int word = (nf - 1) >> 5; word >= 0; --word)
+            for (unsigned bits = P.vis[word]; bits; ) {
+                const int bit = 31 - __clz(bits);
+                bits &= ~(1u << bit);
+                const int k = (word << 5) + bit;
                 const int a[3] = {P.i0[k], P.i1[k], P.i2[k]}, b[3] = {P.i1[k], P.i2[k], P.i0[k]};
                 bool found[3];
                 for (int j = 0; j < 3; ++j) {
