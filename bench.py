@@ -395,6 +395,40 @@ def _serve(srv, reqs, arrivals, t_end, max_backlog=None, descs=None):
     return fl, req_lat, work, wall
 
 
+def run_serve_ticks(args):
+    """Profiling form of the serving workload: a fixed number of ticks of a profiled
+    (eagerly launched) server that keeps --serve-running requests in flight, admitted in
+    seed order as slots free up.  No wall clock decides anything, so the same command
+    launches the same kernels with or without a profiler.  Prints the ticks' stage times."""
+    import numpy as np
+    from physecs_gb300.api import Server
+    from physecs_gb300.desc import make_desc
+    small = args.serve_max_bodies <= 1000
+    classes = SERVE_CLASSES_SMALL if small else SERVE_CLASSES
+    reqs, pool_scene = serving_requests(2 * args.serve_ticks + 64, 0, n_max=args.serve_max_bodies)
+    srv = Server(classes, mesh_pool=pool_scene, hbm_budget=SERVE_HBM_BUDGET, profile=True,
+                 launch=json.loads(args.launch) if args.launch else SERVE_LAUNCH)
+    nxt, live, stages = 0, set(), []
+    for _ in range(args.serve_ticks):
+        while len(live) < args.serve_running and nxt < len(reqs):
+            slot = srv.admit(reqs[nxt][0], reqs[nxt][1], desc=make_desc(reqs[nxt][0]))
+            if slot is None:
+                break
+            live.add(slot)
+            nxt += 1
+        for slot in srv.tick():
+            live.discard(slot)
+            srv.release(slot)
+        stages.append(srv.tick_stages().copy())
+    st = np.array(stages)
+    names = ["uploads", "broadphase", "narrowphase", "rows", "solver", "bounds"]
+    pct = lambda a, q: float(np.percentile(a, q))
+    print(json.dumps({"workload": "serving ticks (profiled, eager)", "ticks": args.serve_ticks,
+                      "running": args.serve_running, "requests": nxt,
+                      "tick_ms": {"p50": pct(st.sum(1), 50), "p99": pct(st.sum(1), 99)},
+                      "stage_ms": {n: {"p50": pct(st[:, i], 50), "p99": pct(st[:, i], 99)} for i, n in enumerate(names)}}))
+
+
 def run_serving(args, rank, world, local):
     import numpy as np
     from physecs_gb300.api import Server
@@ -458,6 +492,9 @@ def main():
     ap.add_argument("--serve-load", type=float, default=0.7)
     ap.add_argument("--serve-max-bodies", type=int, default=8192)
     ap.add_argument("--serve-slo", action="store_true", help="slot budget sized for the 2 ms frame target")
+    ap.add_argument("--serve-ticks", type=int, default=0,
+                    help="serving: run this many profiled ticks with --serve-running requests in flight instead")
+    ap.add_argument("--serve-running", type=int, default=90)
     ap.add_argument("--scenes", type=int, default=4096)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--plain-scenes", type=int, default=64)
@@ -472,6 +509,8 @@ def main():
 
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.workload == "serving" and args.serve_ticks > 0:
+        return run_serve_ticks(args)
     if args.workload == "serving":
         return run_serving(args, rank, world, local)
     if args.workload == "trimesh_bvh":

@@ -180,7 +180,9 @@ typedef struct psx_launch_config {
 } psx_launch_config;
 
 typedef struct psx_world_opts {
-    int32_t pairs_per_collider;      /* broadphase pair capacity per collider (0: default 8) */
+    int32_t pairs_per_collider;      /* broadphase pair capacity per collider (0: default 8); a collider
+                                      * with more than 4.5 times as many partners after it in its tree's
+                                      * order costs a second walk of its tree in that frame */
     int32_t manifolds_per_collider;  /* contact manifold capacity per collider (0: default 4) */
     int32_t block_scene_max_dyn;     /* scenes up to this many dynamic bodies run one per CTA (0: default 8192) */
     int32_t use_graph;               /* capture the frame in a CUDA graph after the first step */
@@ -527,7 +529,8 @@ typedef struct psx_server_opts {
     const int32_t* class_bodies;      /* [n_classes] body capacity of a slot, ascending */
     const int32_t* class_slots;       /* [n_classes] slots of that class */
     const psx_scene_desc* mesh_pool;  /* convex meshes requests may use, or NULL */
-    int32_t pairs_per_collider;       /* as psx_world_opts (0: default) */
+    int32_t pairs_per_collider;       /* as psx_world_opts (0: 16, so that the broadphase keeps every
+                                       * collider's pairs from its one tree walk; see psx_world_opts) */
     int32_t manifolds_per_collider;
     int32_t device;
     int32_t eager;                    /* 1: launch every tick's kernels one by one instead of replaying a CUDA graph */

@@ -223,7 +223,9 @@ PSX_API psx_status psx_server_create(const psx_server_opts* o, psx_server** out)
         for (int m = 0; m < p.n_convex; ++m) S->pool_hash.push_back(mesh_hash(p, m));
     }
     psx_world_opts wo{};
-    wo.pairs_per_collider = o->pairs_per_collider;
+    // piled requests reach about 40 partners a collider: room for 72 keeps their pairs
+    // from the broadphase's one walk (4.5 x the pairs per collider)
+    wo.pairs_per_collider = o->pairs_per_collider ? o->pairs_per_collider : 16;
     wo.manifolds_per_collider = o->manifolds_per_collider;
     wo.block_scene_max_dyn = 1 << 30;
     wo.use_graph = (o->eager || o->profile) ? 0 : 1;   // a tick is the same fixed kernel sequence every time
