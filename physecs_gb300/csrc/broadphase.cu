@@ -559,12 +559,17 @@ __global__ void __launch_bounds__(256) k_traverse(World w, FrameBuf f) {
                     if (!pair_ok(w, ca, cb)) continue;
                     place_pair<MODE>(w, f, ca, cb, p, out, count);
                     ++count;
-                } else if (f.bvh.last[c] > p && overlap_incl(qmin, qmax, f.bvh.bmin[c], f.bvh.bmax[c])) {
-                    if (sp + 2 <= 64) {
-                        stack[sp++] = f.bvh.right[c];
-                        stack[sp++] = f.bvh.left[c];
-                    } else {
-                        atomicOr(w.err, ERR_STACK_CAPACITY);
+                } else {
+                    // the node's fields in one round of loads (c is a node of the lane's tree)
+                    const int last = f.bvh.last[c], L = f.bvh.left[c], R = f.bvh.right[c];
+                    const float4 bmn = f.bvh.bmin[c], bmx = f.bvh.bmax[c];
+                    if (last > p && overlap_incl(qmin, qmax, bmn, bmx)) {
+                        if (sp + 2 <= 64) {
+                            stack[sp++] = R;
+                            stack[sp++] = L;
+                        } else {
+                            atomicOr(w.err, ERR_STACK_CAPACITY);
+                        }
                     }
                 }
             }
@@ -583,11 +588,14 @@ __global__ void __launch_bounds__(256) k_traverse(World w, FrameBuf f) {
                 place_pair<MODE>(w, f, ca, cb, p, out, count);
                 ++count;
             } else {
-                const bool go = mine && f.bvh.last[c] > p && overlap_incl(qmin, qmax, f.bvh.bmin[c], f.bvh.bmax[c]);
+                // the node's fields in one round of loads, children before the vote
+                const int last = f.bvh.last[c], L = f.bvh.left[c], R = f.bvh.right[c];
+                const float4 bmn = f.bvh.bmin[c], bmx = f.bvh.bmax[c];
+                const bool go = mine && last > p && overlap_incl(qmin, qmax, bmn, bmx);
                 if (!__any_sync(~0u, go)) continue;
                 if (sp + 2 <= 64) {
-                    stack[sp++] = f.bvh.right[c];
-                    stack[sp++] = f.bvh.left[c];
+                    stack[sp++] = R;
+                    stack[sp++] = L;
                 } else if (lane == 0) {
                     atomicOr(w.err, ERR_STACK_CAPACITY);
                 }
