@@ -89,3 +89,33 @@ def test_record_layouts_match_the_python_packing():
         assert struct_words(name) == words, name
     from physecs_gb300.api import pack_deltas
     assert pack_deltas([{"body": 0, "pos": [1, 2, 3], "kinematic": True}]).shape == (1, 17)
+
+
+def test_ctypes_structures_match_the_header(tmp_path):
+    """The option and descriptor structures the Python layer passes by pointer have the C
+    compiler's size and field offsets (a field added on one side only shifts every later
+    one)."""
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    import subprocess
+    from physecs_gb300.api import PsxLaunchConfig, PsxSceneCarry, PsxServerOpts, PsxWorldOpts
+    from physecs_gb300.desc import PsxSceneDesc
+    structs = {"psx_launch_config": PsxLaunchConfig, "psx_world_opts": PsxWorldOpts,
+               "psx_scene_carry": PsxSceneCarry, "psx_server_opts": PsxServerOpts, "psx_scene_desc": PsxSceneDesc}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "psx.h"', "int main(void) {"]
+    for cname, cls in structs.items():
+        lines.append('printf("%s size %%zu\\n", sizeof(%s));' % (cname, cname))
+        for field, _ in cls._fields_:
+            lines.append('printf("%s %s %%zu\\n", offsetof(%s, %s));' % (cname, field, cname, field))
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([gcc, "-std=c11", "-I", os.path.dirname(HEADER), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, cls in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(cls), cname
+        for field, _ in cls._fields_:
+            assert got[(cname, field)] == getattr(cls, field).offset, (cname, field)
