@@ -334,8 +334,9 @@ PSX_API psx_status psx_server_admit(psx_server* S, const psx_scene_desc* d, int3
     sl.dyn_of.assign(d->n_bodies, -1);
     if (S->triggers) {
         // a tick in flight may have run the slot's previous request: its events are
-        // decoded at that tick's end with the map it ran under
-        if (S->in_flight) std::swap(S->retired[si], sl.map);
+        // decoded at that tick's end with the map it ran under (a request admitted and
+        // released again within the same tick never ran, and its map is simply replaced)
+        if (S->in_flight && sl.first_tick <= S->ticks_begun) std::swap(S->retired[si], sl.map);
         ReqMap& m = sl.map;
         m.col_body.resize(d->n_colliders);
         m.col_local.resize(d->n_colliders);
